@@ -1,0 +1,164 @@
+/*
+ * jsb: GB300-native soft-body solver step for Jolt Physics, C ABI.
+ *
+ * This is the drop-in boundary for SoftBodyMotionProperties' update
+ * (Jolt/Physics/SoftBody/SoftBodyMotionProperties.cpp:937-1256). A Jolt integration keeps building
+ * SoftBodySharedSettings / SoftBodyCreationSettings with Jolt, passes the settings bytes written by
+ * SoftBodySharedSettings::SaveBinaryState (SoftBodySharedSettings.cpp:1203-1236) and, optionally, the
+ * per-body state written by SoftBodyMotionProperties::SaveState (SoftBodyMotionProperties.cpp:1446-1473),
+ * steps bodies on the GPU and reads state back in the RestoreState layout (:1475-1502) together with
+ * the body position delta that PhysicsSystem::JobSoftBodyFinalize applies (PhysicsSystem.cpp:2864).
+ *
+ * Conventions: every call returns a jsb_status (0 = JSB_OK); no C++ exception crosses the boundary;
+ * jsb_last_error_string() describes the last failure of the calling thread. A context belongs to one
+ * host thread. Calls that take a stream enqueue work on it; calls without one synchronise.
+ * All pointers are host pointers unless the name says "device".
+ */
+#ifndef JSB_H
+#define JSB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int jsb_status;
+enum {
+    JSB_OK = 0,
+    JSB_ERR_INVALID_ARGUMENT = 1, /* null pointer, unknown id, bad size */
+    JSB_ERR_BLOB = 2,             /* malformed settings/state bytes (truncated, out-of-range index) */
+    JSB_ERR_UNSUPPORTED = 3,      /* constraint type or body size the GPU path does not handle */
+    JSB_ERR_CUDA = 4,             /* a CUDA runtime call failed */
+    JSB_ERR_OUT_OF_MEMORY = 5,    /* device allocation failed */
+    JSB_ERR_TIMEOUT = 6,          /* a bounded device wait gave up */
+    JSB_ERR_NONFINITE = 7,        /* a NaN/Inf vertex position or velocity was produced */
+    JSB_ERR_CAPACITY = 8          /* a fixed-size limit was exceeded */
+};
+
+typedef struct jsb_context jsb_context;
+typedef struct CUstream_st *jsb_stream; /* cudaStream_t; NULL = the default stream */
+
+/* SoftBodyCreationSettings scalars (Jolt/Physics/SoftBody/SoftBodyCreationSettings.h:61-72). */
+typedef struct jsb_creation_settings {
+    uint32_t num_iterations;      /* mNumIterations */
+    float linear_damping;         /* mLinearDamping */
+    float max_linear_velocity;    /* mMaxLinearVelocity */
+    float restitution;            /* mRestitution */
+    float friction;               /* mFriction */
+    float pressure;               /* mPressure */
+    float gravity_factor;         /* mGravityFactor */
+    float vertex_radius;          /* mVertexRadius */
+    uint8_t update_position;      /* mUpdatePosition */
+    uint8_t make_rotation_identity; /* mMakeRotationIdentity (must be 1: bodies keep identity rotation) */
+    uint8_t allow_sleeping;       /* mAllowSleeping (sleeping is not evaluated on the GPU) */
+    uint8_t faces_double_sided;   /* mFacesDoubleSided (queries only) */
+} jsb_creation_settings;
+
+enum { JSB_COLLIDER_BOX = 0, JSB_COLLIDER_SPHERE = 1 };
+
+/* A static rigid body with one convex leaf shape (BoxShape / SphereShape), world space, identity
+ * rotation. friction/restitution are the body's; they are combined with the soft body's like
+ * ContactConstraintManager's defaults (sqrt(f1 f2), max(r1, r2)). */
+typedef struct jsb_collider {
+    int32_t type;
+    float position[3];
+    float half_extent[3]; /* box */
+    float radius;         /* sphere */
+    float friction;
+    float restitution;
+} jsb_collider;
+
+/* ---- context ------------------------------------------------------------------------------ */
+jsb_status jsb_context_create(int device, jsb_context **out);
+jsb_status jsb_context_destroy(jsb_context *ctx);
+const char *jsb_last_error_string(void);
+const char *jsb_version(void);
+
+/* PhysicsSystem::SetGravity (PhysicsSystem.h). */
+jsb_status jsb_set_gravity(jsb_context *ctx, const float gravity[3]);
+
+/* ---- settings and bodies ------------------------------------------------------------------ */
+/* Upload SoftBodySharedSettings::SaveBinaryState bytes (SoftBodySharedSettings.cpp:1203-1236).
+ * Settings are immutable and may be shared by many bodies. Rejects skinned constraints and rods
+ * (JSB_ERR_UNSUPPORTED) and bodies with more than 65536 vertices. */
+jsb_status jsb_settings_upload(jsb_context *ctx, const void *blob, size_t len, uint32_t *settings_id);
+
+/* BodyInterface::CreateSoftBody + SoftBodyMotionProperties::Initialize (SoftBodyMotionProperties.cpp:59-105):
+ * vertices start at the settings' positions/velocities. `position` is the body position in world space. */
+jsb_status jsb_body_add(jsb_context *ctx, uint32_t settings_id, const jsb_creation_settings *creation,
+                        const float position[3], uint32_t *body_id);
+
+/* Overwrite a body's state with SoftBodyMotionProperties::SaveState bytes (single precision build,
+ * no rods/skinning: 101-byte MotionProperties header, N x (position, velocity), 4 bounds vectors). */
+jsb_status jsb_body_restore_state(jsb_context *ctx, uint32_t body_id, const void *state, size_t len,
+                                  const float position[3]);
+
+/* MotionProperties::AddForce: accumulated until the next step consumes it (ResetForce). */
+jsb_status jsb_body_add_force(jsb_context *ctx, uint32_t body_id, const float force[3]);
+
+jsb_status jsb_collider_add(jsb_context *ctx, const jsb_collider *collider, uint32_t *collider_id);
+
+jsb_status jsb_body_num_vertices(jsb_context *ctx, uint32_t body_id, uint32_t *num_vertices);
+
+/* ---- stepping ----------------------------------------------------------------------------- */
+/* PhysicsSystem::Update's soft-body part for every body in the context: InitializeUpdateContext,
+ * DetermineCollidingShapes, DetermineCollisionPlanes, num_iterations x (pressure, integrate,
+ * update groups, collision + velocity), UpdateSoftBodyState, body position += delta.
+ * Batched form: all bodies advance in persistent launches fed from a work queue. */
+jsb_status jsb_step(jsb_context *ctx, float dt, int collision_steps, jsb_stream stream);
+
+/* Same step, one body per launch (the plain form; what CustomUpdate would map to). */
+jsb_status jsb_step_plain(jsb_context *ctx, float dt, int collision_steps, jsb_stream stream);
+
+/* Capture `num_steps` batched steps into a CUDA graph and replay it `repeats` times. */
+jsb_status jsb_step_graph(jsb_context *ctx, float dt, int collision_steps, int num_steps, int repeats,
+                          jsb_stream stream);
+
+/* Wait for the context's work and report device-side errors (JSB_ERR_NONFINITE, JSB_ERR_TIMEOUT). */
+jsb_status jsb_synchronize(jsb_context *ctx);
+
+/* ---- readback ----------------------------------------------------------------------------- */
+/* Body position (world) and local vertex positions/velocities (3 floats each, any may be NULL). */
+jsb_status jsb_body_read(jsb_context *ctx, uint32_t body_id, float position[3], float *local_positions,
+                         float *velocities);
+
+/* SoftBodyMotionProperties::SaveState bytes for RestoreState; *len receives the size (call with
+ * state == NULL to query). */
+jsb_status jsb_body_save_state(jsb_context *ctx, uint32_t body_id, void *state, size_t capacity, size_t *len);
+
+/* Bulk transfer of all bodies' local positions and velocities in body order (used for the
+ * host-buffer round trip): 3 floats per vertex each. */
+jsb_status jsb_state_upload_all(jsb_context *ctx, const float *local_positions, const float *velocities,
+                                jsb_stream stream);
+jsb_status jsb_state_download_all(jsb_context *ctx, float *local_positions, float *velocities, jsb_stream stream);
+jsb_status jsb_total_vertices(jsb_context *ctx, uint64_t *total);
+
+/* ---- scheduling and autotuning ------------------------------------------------------------ */
+/* Number of dependency levels of a body's constraint schedule per substep and total constraints. */
+jsb_status jsb_body_schedule_info(jsb_context *ctx, uint32_t body_id, uint32_t *num_levels, uint32_t *num_constraints);
+
+/* Threads per CTA used for bodies whose vertex count is <= max_vertices (bucket table written by
+ * the autotuner; threads in {32, 64, 128, 256}). */
+jsb_status jsb_set_bucket_threads(jsb_context *ctx, uint32_t max_vertices, uint32_t threads);
+jsb_status jsb_autotune(jsb_context *ctx, float dt, int trials);
+
+/* Kernel launches issued by the most recent jsb_step / jsb_step_plain / jsb_step_graph call. */
+jsb_status jsb_last_launch_count(jsb_context *ctx, uint32_t *launches);
+
+/* Time (ms, CUDA events on the launching stream) of the dominant solver kernel launches issued by the
+ * last jsb_step_graph call, averaged per step. */
+jsb_status jsb_last_kernel_ms(jsb_context *ctx, float *ms_per_step);
+
+/* ---- scenes (seeded synthetic workloads, built with this library's SoftBodySharedSettings mirror) */
+/* Serialises a scene (colliders, bodies with SaveBinaryState bytes, creation settings, forces).
+ * name: "pinned_cloth" | "uneven_batch" | "large_cloth" | "diff_cloth" | "diff_batch"; params is a
+ * space separated "key=value" list. Call with out == NULL to query *len. */
+jsb_status jsb_scene_build(const char *name, const char *params, void *out, size_t capacity, size_t *len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JSB_H */

@@ -1,0 +1,689 @@
+// CPU oracle for the soft-body solver step. TEST INFRASTRUCTURE ONLY.
+//
+// This is a plain, single-threaded restatement of Jolt Physics' soft-body update, written to be
+// checked against the reference (oracle/_ref) and then used as the checker of the CUDA path. Only
+// tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference arm load it. The product
+// library (libjsb) never links or calls it.
+//
+// Every arithmetic step follows the reference's operation order so that the float instantiation is
+// bit-identical to the reference built with JPH_CROSS_PLATFORM_DETERMINISTIC (-ffp-contract=off):
+//   Vec3 dot  = (x*x' + y*y') + (z*z' + 0)          Jolt/Math/Vec3.inl:896-934 (ReduceSum, deterministic)
+//   Vec3 cross = separately rounded products         Jolt/Math/Vec3.inl:855-895
+//   unary minus = 0 - x                              Jolt/Math/Vec3.inl:669-700
+//   Sign(x) = x < 0 ? -1 : 1                         Jolt/Math/Math.h:116-119
+//   ACosApproximate                                  Jolt/Math/Trigonometry.h:48-65
+// The double instantiation evaluates the same sequence in FP64 ("FP64 re-evaluation").
+//
+// Step structure (Jolt/Physics/SoftBody/SoftBodyMotionProperties.cpp):
+//   InitializeUpdateContext            :937-960
+//   DetermineCollidingShapes (broad)   :120-255  (static Box/Sphere colliders, world AABB overlap)
+//   DetermineCollisionPlanes           :257-265 + BoxShape.cpp:234-283 + SphereShape.cpp:279-300
+//   per iteration: ApplyPressure :291-323, IntegratePositions :325-365,
+//                  ProcessGroup for each parallel group, then the non-parallel group :1030-1115
+//                  (volume :458-507, dihedral bend :367-456, edge :573-601, LRA :679-698),
+//                  ApplyCollisionConstraintsAndUpdateVelocities :700-825 (static-body branch)
+//   UpdateSoftBodyState                :827-921
+//   body position += delta             Jolt/Physics/PhysicsSystem.cpp:2864
+//
+// Build: g++ -O2 -std=c++17 -ffp-contract=off -fPIC -shared oracle/jsb_oracle.cpp -o oracle/liboracle.so
+
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace oracle {
+
+template <class R>
+struct V3 {
+    R x, y, z;
+};
+template <class R>
+inline V3<R> add(V3<R> a, V3<R> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class R>
+inline V3<R> sub(V3<R> a, V3<R> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class R>
+inline V3<R> mul(R s, V3<R> a) { return {s * a.x, s * a.y, s * a.z}; }
+template <class R>
+inline V3<R> mul(V3<R> a, R s) { return {a.x * s, a.y * s, a.z * s}; }
+template <class R>
+inline V3<R> divs(V3<R> a, R s) { return {a.x / s, a.y / s, a.z / s}; }
+template <class R>
+inline V3<R> neg(V3<R> a) { return {R(0) - a.x, R(0) - a.y, R(0) - a.z}; }
+template <class R>
+inline R dot(V3<R> a, V3<R> b) {
+    R px = a.x * b.x, py = a.y * b.y, pz = a.z * b.z;
+    return (px + py) + (pz + R(0));
+}
+template <class R>
+inline V3<R> cross(V3<R> a, V3<R> b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <class R>
+inline R len_sq(V3<R> a) { return dot(a, a); }
+template <class R>
+inline R len(V3<R> a) { return std::sqrt(len_sq(a)); }
+template <class R>
+inline R sgn(R v) { return v < R(0) ? R(-1) : R(1); }
+template <class R>
+inline V3<R> vmin(V3<R> a, V3<R> b) { return {a.x < b.x ? a.x : b.x, a.y < b.y ? a.y : b.y, a.z < b.z ? a.z : b.z}; }
+template <class R>
+inline V3<R> vmax(V3<R> a, V3<R> b) { return {a.x > b.x ? a.x : b.x, a.y > b.y ? a.y : b.y, a.z > b.z ? a.z : b.z}; }
+template <class R>
+inline R comp(V3<R> a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+template <class R>
+inline R acos_approx(R x) {  // Jolt/Math/Trigonometry.h:48-65
+    const R pi = R(3.14159265358979323846f);
+    R ax = std::abs(x);
+    if (ax > R(1)) ax = R(1);
+    R val = std::sqrt(R(1) - ax) * (pi / R(2) - R(0.175394f) * ax);
+    return x < R(0) ? pi - val : val;
+}
+
+// --------------------------------------------------------------------------------------------
+// Settings blob (SoftBodySharedSettings::SaveBinaryState, SoftBodySharedSettings.cpp:1203-1236)
+// --------------------------------------------------------------------------------------------
+struct Edge { uint32_t v[2]; float rest, compliance; };
+struct Bend { uint32_t v[4]; float compliance, initial_angle; };
+struct Volume { uint32_t v[4]; float six_rest_volume, compliance; };
+struct LRA { uint32_t v[2]; float max_distance; };
+struct Face { uint32_t v[3]; uint32_t material; };
+struct Group { uint32_t edge, lra, rod_ss, rod_bt, bend, volume, skinned; };
+struct SVertex { float pos[3], vel[3], inv_mass; };
+
+struct Settings {
+    std::vector<SVertex> vertices;
+    std::vector<Face> faces;
+    std::vector<Edge> edges;
+    std::vector<Bend> bends;
+    std::vector<Volume> volumes;
+    std::vector<LRA> lras;
+    std::vector<Group> groups;
+    uint32_t n_skinned = 0, n_rod_ss = 0, n_rod_bt = 0;
+};
+
+class Reader {
+public:
+    Reader(const uint8_t *p, size_t n) : p_(p), n_(n) {}
+    bool read(void *dst, size_t bytes) {
+        if (off_ + bytes > n_) return false;
+        memcpy(dst, p_ + off_, bytes);
+        off_ += bytes;
+        return true;
+    }
+    bool skip(size_t bytes) {
+        if (off_ + bytes > n_) return false;
+        off_ += bytes;
+        return true;
+    }
+    template <class T>
+    bool array(std::vector<T> &out, size_t elem_bytes) {
+        uint32_t count;
+        if (!read(&count, 4)) return false;
+        if (uint64_t(count) * elem_bytes > n_ - off_) return false;
+        out.resize(count);
+        for (uint32_t i = 0; i < count; ++i)
+            if (!read(&out[i], elem_bytes)) return false;
+        return true;
+    }
+    bool skip_array(size_t elem_bytes, uint32_t *count_out) {
+        uint32_t count;
+        if (!read(&count, 4)) return false;
+        if (count_out) *count_out = count;
+        return skip(uint64_t(count) * elem_bytes);
+    }
+    size_t offset() const { return off_; }
+
+private:
+    const uint8_t *p_;
+    size_t n_, off_ = 0;
+};
+
+inline bool parse_settings(const uint8_t *blob, size_t len, Settings &s, std::string &err) {
+    Reader r(blob, len);
+    bool ok = r.array(s.vertices, 28) && r.array(s.faces, 16) && r.array(s.edges, 16) && r.array(s.bends, 24) &&
+              r.array(s.volumes, 24) && r.skip_array(52, &s.n_skinned) && r.skip_array(4, nullptr) && r.array(s.lras, 12) &&
+              r.array(s.groups, 28) && r.skip_array(36, &s.n_rod_ss) && r.skip_array(28, &s.n_rod_bt) && r.skip_array(68, nullptr);
+    if (!ok) {
+        err = "truncated settings blob";
+        return false;
+    }
+    if (r.offset() != len) {
+        err = "trailing bytes in settings blob";
+        return false;
+    }
+    return true;
+}
+
+// --------------------------------------------------------------------------------------------
+// World
+// --------------------------------------------------------------------------------------------
+struct Collider {
+    int type;  // 0 box, 1 sphere
+    float pos[3];
+    float half[3];
+    float radius;
+    float friction, restitution;
+};
+
+struct Creation {
+    uint32_t num_iterations;
+    float linear_damping, max_linear_velocity, restitution, friction, pressure, gravity_factor, vertex_radius;
+    uint32_t update_position;
+};
+
+template <class R>
+struct Vertex {
+    V3<R> prev, pos, vel;
+    R inv_mass;
+    V3<R> plane_n;
+    R plane_c;
+    int shape_idx;
+    bool contact;
+    R largest_pen;
+};
+
+template <class R>
+struct Body {
+    std::shared_ptr<Settings> settings;
+    Creation cs;
+    std::vector<Vertex<R>> v;
+    V3<R> position;  // body (center of mass) position in world space
+    V3<R> bmin, bmax, pmin, pmax;  // local bounds and predicted bounds
+    V3<R> force;
+    V3<R> lin_vel, ang_vel;
+};
+
+template <class R>
+struct CollidingShape {
+    int collider;
+    V3<R> t;  // translation relative to the soft body (identity rotation)
+    R friction, restitution;
+};
+
+template <class R>
+class World {
+public:
+    V3<R> gravity{R(0), R(-9.81f), R(0)};
+    std::vector<Collider> colliders;
+    std::vector<Body<R>> bodies;
+
+    int add_body(std::shared_ptr<Settings> s, const float pos[3], const Creation &cs) {
+        Body<R> b;
+        b.settings = s;
+        b.cs = cs;
+        b.position = {R(pos[0]), R(pos[1]), R(pos[2])};
+        b.force = {R(0), R(0), R(0)};
+        b.lin_vel = b.ang_vel = {R(0), R(0), R(0)};
+        const R big = R(FLT_MAX);
+        b.bmin = {big, big, big};
+        b.bmax = {-big, -big, -big};
+        b.v.resize(s->vertices.size());
+        for (size_t i = 0; i < s->vertices.size(); ++i) {  // SoftBodyMotionProperties::Initialize :59-105
+            const SVertex &sv = s->vertices[i];
+            Vertex<R> &o = b.v[i];
+            o.pos = o.prev = {R(sv.pos[0]), R(sv.pos[1]), R(sv.pos[2])};
+            o.vel = {R(sv.vel[0]), R(sv.vel[1]), R(sv.vel[2])};
+            o.inv_mass = R(sv.inv_mass);
+            reset_collision(o);
+            b.bmin = vmin(b.bmin, o.pos);
+            b.bmax = vmax(b.bmax, o.pos);
+        }
+        b.pmin = b.bmin;
+        b.pmax = b.bmax;
+        bodies.push_back(std::move(b));
+        return int(bodies.size()) - 1;
+    }
+
+    static void reset_collision(Vertex<R> &o) {
+        o.largest_pen = R(-FLT_MAX);
+        o.shape_idx = -1;
+        o.contact = false;
+    }
+
+    void step(R dt, int collision_steps) {
+        R step_dt = dt / R(collision_steps);
+        for (int c = 0; c < collision_steps; ++c)
+            for (auto &b : bodies) step_body(b, step_dt);
+    }
+
+    void step_body(Body<R> &b, R dt) {
+        const Settings &s = *b.settings;
+        // InitializeUpdateContext (:937-960), identity body rotation
+        V3<R> g = mul(R(b.cs.gravity_factor), gravity);
+        const uint32_t n_it = b.cs.num_iterations;
+        R dt_sub = dt / R(float(n_it));
+        R disp_scale = R(0.5f) * R(float(n_it));
+        disp_scale = disp_scale * R(float(n_it + 1));
+        disp_scale = disp_scale * (dt_sub * dt_sub);
+        V3<R> disp_g = mul(disp_scale, g);
+
+        // DetermineCollidingShapes (:120-255)
+        std::vector<CollidingShape<R>> shapes;
+        {
+            V3<R> lmin = vmin(b.bmin, b.pmin), lmax = vmax(b.bmax, b.pmax);
+            V3<R> r3 = {R(b.cs.vertex_radius), R(b.cs.vertex_radius), R(b.cs.vertex_radius)};
+            lmin = sub(lmin, r3);
+            lmax = add(lmax, r3);
+            V3<R> wmin = add(b.position, lmin), wmax = add(b.position, lmax);
+            for (size_t ci = 0; ci < colliders.size(); ++ci) {
+                const Collider &c = colliders[ci];
+                V3<R> cp = {R(c.pos[0]), R(c.pos[1]), R(c.pos[2])};
+                V3<R> ext = c.type == 0 ? V3<R>{R(c.half[0]), R(c.half[1]), R(c.half[2])}
+                                        : V3<R>{R(c.radius), R(c.radius), R(c.radius)};
+                V3<R> cmin = add(cp, neg(ext)), cmax = add(cp, ext);
+                bool overlap = !(wmin.x > cmax.x || wmin.y > cmax.y || wmin.z > cmax.z || wmax.x < cmin.x || wmax.y < cmin.y ||
+                                 wmax.z < cmin.z);
+                if (!overlap) continue;
+                CollidingShape<R> cs;
+                cs.collider = int(ci);
+                cs.t = sub(cp, b.position);
+                cs.friction = std::sqrt(R(b.cs.friction) * R(c.friction));
+                cs.restitution = R(b.cs.restitution) > R(c.restitution) ? R(b.cs.restitution) : R(c.restitution);
+                shapes.push_back(cs);
+            }
+        }
+
+        // DetermineCollisionPlanes (:257-265)
+        for (size_t si = 0; si < shapes.size(); ++si) {
+            const Collider &c = colliders[shapes[si].collider];
+            const V3<R> t = shapes[si].t;
+            for (auto &v : b.v) {
+                if (!(v.inv_mass > R(0))) continue;
+                if (c.type == 0)
+                    collide_box(v, c, t, int(si));
+                else
+                    collide_sphere(v, c, t, int(si));
+            }
+        }
+
+        for (uint32_t it = 0; it < n_it; ++it) {
+            apply_pressure(b, dt_sub);
+            integrate(b, g, dt_sub);
+            const size_t ng = s.groups.size();
+            for (size_t gi = 0; gi < ng; ++gi) process_group(b, gi, dt_sub);
+            collide_and_update_velocities(b, shapes, g, dt_sub);
+        }
+        update_state(b, dt, disp_g);
+    }
+
+    void collide_box(Vertex<R> &v, const Collider &c, V3<R> t, int idx) {  // BoxShape.cpp:234-283
+        V3<R> local = add(v.pos, neg(t));  // inverse transform: R^T p + (-(R^T t)), R = identity
+        V3<R> h = {R(c.half[0]), R(c.half[1]), R(c.half[2])};
+        V3<R> nh = neg(h);
+        V3<R> clamped = vmax(vmin(local, h), nh);
+        if (clamped.x == local.x && clamped.y == local.y && clamped.z == local.z) {
+            V3<R> al = {std::abs(local.x), std::abs(local.y), std::abs(local.z)};
+            V3<R> delta = sub(h, al);
+            int index = delta.x < delta.y ? (delta.z < delta.x ? 2 : 0) : (delta.z < delta.y ? 2 : 1);
+            R pen = comp(delta, index);
+            if (v.largest_pen >= pen) return;
+            v.largest_pen = pen;
+            V3<R> sign = {std::signbit(local.x) ? R(-1) : R(1), std::signbit(local.y) ? R(-1) : R(1), std::signbit(local.z) ? R(-1) : R(1)};
+            V3<R> axis = {index == 0 ? R(1) : R(0), index == 1 ? R(1) : R(0), index == 2 ? R(1) : R(0)};
+            V3<R> normal = {sign.x * axis.x, sign.y * axis.y, sign.z * axis.z};
+            V3<R> point = {normal.x * h.x, normal.y * h.y, normal.z * h.z};
+            set_plane_transformed(v, normal, point, t, idx);
+        } else {
+            V3<R> normal = sub(local, clamped);
+            R nl = len(normal);
+            R pen = -nl;
+            if (v.largest_pen >= pen) return;
+            v.largest_pen = pen;
+            normal = divs(normal, nl);
+            set_plane_transformed(v, normal, clamped, t, idx);
+        }
+    }
+
+    // Plane::sFromPointAndNormal(point, normal).GetTransformed(translation t, identity rotation)
+    void set_plane_transformed(Vertex<R> &v, V3<R> normal, V3<R> point, V3<R> t, int idx) {
+        R c = -dot(normal, point);
+        // Multiply3x3 with identity columns: ((c0*x + c1*y) + c2*z)
+        V3<R> n2;
+        n2.x = (R(1) * normal.x + R(0) * normal.y) + R(0) * normal.z;
+        n2.y = (R(0) * normal.x + R(1) * normal.y) + R(0) * normal.z;
+        n2.z = (R(0) * normal.x + R(0) * normal.y) + R(1) * normal.z;
+        v.plane_n = n2;
+        v.plane_c = c - dot(t, n2);
+        v.shape_idx = idx;
+    }
+
+    void collide_sphere(Vertex<R> &v, const Collider &c, V3<R> t, int idx) {  // SphereShape.cpp:279-300
+        V3<R> center = t;
+        R radius = R(c.radius);
+        V3<R> delta = sub(v.pos, center);
+        R distance = len(delta);
+        R pen = radius - distance;
+        if (v.largest_pen >= pen) return;
+        v.largest_pen = pen;
+        V3<R> normal = distance > R(0) ? divs(delta, distance) : V3<R>{R(0), R(1), R(0)};
+        V3<R> point = add(center, mul(radius, normal));
+        v.plane_n = normal;
+        v.plane_c = -dot(normal, point);
+        v.shape_idx = idx;
+    }
+
+    void apply_pressure(Body<R> &b, R dt) {  // :291-323
+        R pc = R(b.cs.pressure);
+        if (!(pc > R(0))) return;
+        const Settings &s = *b.settings;
+        R six_volume = R(0);
+        for (const Face &f : s.faces) {
+            V3<R> x1 = b.v[f.v[0]].pos, x2 = b.v[f.v[1]].pos, x3 = b.v[f.v[2]].pos;
+            six_volume = six_volume + dot(cross(x1, x2), x3);
+        }
+        if (!(six_volume > R(0))) return;
+        R coefficient = pc * dt / six_volume;
+        for (const Face &f : s.faces) {
+            V3<R> x1 = b.v[f.v[0]].pos, x2 = b.v[f.v[1]].pos, x3 = b.v[f.v[2]].pos;
+            V3<R> impulse = mul(coefficient, cross(sub(x2, x1), sub(x3, x1)));
+            for (int k = 0; k < 3; ++k) {
+                Vertex<R> &vv = b.v[f.v[k]];
+                vv.vel = add(vv.vel, mul(vv.inv_mass, impulse));
+            }
+        }
+    }
+
+    void integrate(Body<R> &b, V3<R> g, R dt) {  // :325-365
+        R damp = R(1) - R(b.cs.linear_damping) * dt;
+        if (damp < R(0)) damp = R(0);
+        V3<R> sub_g = mul(g, dt);
+        R nv = R(float(b.v.size() > 0 ? b.v.size() : 1));
+        V3<R> sub_imp = divs(mul(b.force, dt), nv);
+        for (auto &v : b.v) {
+            if (v.inv_mass > R(0)) {
+                v.vel = add(v.vel, add(sub_g, mul(sub_imp, v.inv_mass)));
+                v.vel = mul(v.vel, damp);
+            }
+            V3<R> p = v.pos;
+            v.prev = p;
+            v.pos = add(p, mul(v.vel, dt));
+        }
+    }
+
+    void process_group(Body<R> &b, size_t gi, R dt) {  // :1030-1055
+        const Settings &s = *b.settings;
+        Group start{0, 0, 0, 0, 0, 0, 0};
+        const Group &prev = gi > 0 ? s.groups[gi - 1] : start;
+        const Group &cur = s.groups[gi];
+        R inv_dt_sq = R(1) / (dt * dt);
+        for (uint32_t i = prev.volume; i < cur.volume; ++i) apply_volume(b, s.volumes[i], inv_dt_sq);
+        for (uint32_t i = prev.bend; i < cur.bend; ++i) apply_bend(b, s.bends[i], inv_dt_sq);
+        for (uint32_t i = prev.edge; i < cur.edge; ++i) apply_edge(b, s.edges[i], inv_dt_sq);
+        for (uint32_t i = prev.lra; i < cur.lra; ++i) apply_lra(b, s.lras[i]);
+    }
+
+    void apply_bend(Body<R> &b, const Bend &c, R inv_dt_sq) {  // :367-456
+        Vertex<R> &v0 = b.v[c.v[0]], &v1 = b.v[c.v[1]], &v2 = b.v[c.v[2]], &v3 = b.v[c.v[3]];
+        V3<R> x0 = v0.pos, x1 = v1.pos, x2 = v2.pos, x3 = v3.pos;
+        V3<R> e = sub(x1, x0);
+        R e_len = len(e);
+        if (e_len < R(1.0e-6f)) return;
+        V3<R> x1x2 = sub(x2, x1), x1x3 = sub(x3, x1);
+        V3<R> n1 = cross(sub(x2, x0), x1x2);
+        V3<R> n2 = cross(x1x3, sub(x3, x0));
+        R n1_len_sq = len_sq(n1), n2_len_sq = len_sq(n2);
+        R n1n2 = n1_len_sq * n2_len_sq;
+        if (n1n2 < R(1.0e-24f)) return;
+        R sign = sgn(dot(cross(n2, n1), e));
+        R d = dot(n1, n2) / std::sqrt(n1n2);
+        const R pi = R(3.14159265358979323846f);
+        R cval = sign * acos_approx(d) - R(c.initial_angle);
+        if (cval > pi)
+            cval -= R(2.0f) * pi;
+        else if (cval < -pi)
+            cval += R(2.0f) * pi;
+        n1 = divs(n1, n1_len_sq);
+        n2 = divs(n2, n2_len_sq);
+        V3<R> d0c = divs(add(mul(dot(x1x2, e), n1), mul(dot(x1x3, e), n2)), e_len);
+        V3<R> d2c = mul(e_len, n1);
+        V3<R> d3c = mul(e_len, n2);
+        V3<R> d1c = sub(sub(neg(d0c), d2c), d3c);
+        R w0 = v0.inv_mass, w1 = v1.inv_mass, w2 = v2.inv_mass, w3 = v3.inv_mass;
+        R denom = w0 * len_sq(d0c) + w1 * len_sq(d1c) + w2 * len_sq(d2c) + w3 * len_sq(d3c) + R(c.compliance) * inv_dt_sq;
+        if (denom < R(1.0e-12f)) return;
+        R ml = cval / denom;
+        v0.pos = sub(x0, mul(ml * w0, d0c));
+        v1.pos = sub(x1, mul(ml * w1, d1c));
+        v2.pos = sub(x2, mul(ml * w2, d2c));
+        v3.pos = sub(x3, mul(ml * w3, d3c));
+    }
+
+    void apply_volume(Body<R> &b, const Volume &c, R inv_dt_sq) {  // :458-507
+        Vertex<R> &v1 = b.v[c.v[0]], &v2 = b.v[c.v[1]], &v3 = b.v[c.v[2]], &v4 = b.v[c.v[3]];
+        V3<R> x1 = v1.pos, x2 = v2.pos, x3 = v3.pos, x4 = v4.pos;
+        V3<R> x1x2 = sub(x2, x1), x1x3 = sub(x3, x1), x1x4 = sub(x4, x1);
+        R cval = std::abs(dot(cross(x1x2, x1x3), x1x4)) - R(c.six_rest_volume);
+        V3<R> d1c = cross(sub(x4, x2), sub(x3, x2));
+        V3<R> d2c = cross(x1x3, x1x4);
+        V3<R> d3c = cross(x1x4, x1x2);
+        V3<R> d4c = cross(x1x2, x1x3);
+        R w1 = v1.inv_mass, w2 = v2.inv_mass, w3 = v3.inv_mass, w4 = v4.inv_mass;
+        R denom = w1 * len_sq(d1c) + w2 * len_sq(d2c) + w3 * len_sq(d3c) + w4 * len_sq(d4c) + R(c.compliance) * inv_dt_sq;
+        if (denom < R(1.0e-12f)) return;
+        R ml = cval / denom;
+        v1.pos = sub(x1, mul(ml * w1, d1c));
+        v2.pos = sub(x2, mul(ml * w2, d2c));
+        v3.pos = sub(x3, mul(ml * w3, d3c));
+        v4.pos = sub(x4, mul(ml * w4, d4c));
+    }
+
+    void apply_edge(Body<R> &b, const Edge &c, R inv_dt_sq) {  // :573-601
+        Vertex<R> &v0 = b.v[c.v[0]], &v1 = b.v[c.v[1]];
+        V3<R> x0 = v0.pos, x1 = v1.pos;
+        V3<R> delta = sub(x1, x0);
+        R length = len(delta);
+        R denom = length * (v0.inv_mass + v1.inv_mass + R(c.compliance) * inv_dt_sq);
+        if (denom < R(1.0e-12f)) return;
+        V3<R> corr = divs(mul(delta, length - R(c.rest)), denom);
+        v0.pos = add(x0, mul(v0.inv_mass, corr));
+        v1.pos = sub(x1, mul(v1.inv_mass, corr));
+    }
+
+    void apply_lra(Body<R> &b, const LRA &c) {  // :679-698
+        const Vertex<R> &v0 = b.v[c.v[0]];
+        Vertex<R> &v1 = b.v[c.v[1]];
+        V3<R> x0 = v0.pos;
+        V3<R> delta = sub(v1.pos, x0);
+        R dls = len_sq(delta);
+        R md = R(c.max_distance);
+        if (dls > md * md) v1.pos = add(x0, divs(mul(delta, md), std::sqrt(dls)));
+    }
+
+    void collide_and_update_velocities(Body<R> &b, const std::vector<CollidingShape<R>> &shapes, V3<R> g, R dt) {  // :700-825
+        R restitution_threshold = R(-2.0f) * len(g) * dt;
+        R radius = R(b.cs.vertex_radius);
+        for (auto &v : b.v) {
+            if (!(v.inv_mass > R(0))) continue;
+            V3<R> prev_v = v.vel;
+            v.vel = divs(sub(v.pos, v.prev), dt);
+            if (v.shape_idx < 0) continue;
+            R projected = -(dot(v.pos, v.plane_n) + v.plane_c) + radius;
+            if (!(projected > R(0))) continue;
+            v.contact = true;
+            const CollidingShape<R> &cs = shapes[v.shape_idx];
+            V3<R> n = v.plane_n;
+            v.pos = add(v.pos, mul(n, projected));
+            // static body, soft body inverse mass scale 1 (:798-816)
+            V3<R> v_normal = mul(n, dot(n, v.vel));
+            V3<R> v_tan = sub(v.vel, v_normal);
+            R vtl = len(v_tan);
+            if (vtl > R(0)) {
+                R f = cs.friction * projected / (vtl * dt);
+                if (f > R(1)) f = R(1);
+                v.vel = sub(v.vel, mul(v_tan, f));
+            }
+            v.vel = sub(v.vel, v_normal);
+            R pvn = dot(prev_v, n);
+            if (pvn < restitution_threshold) v.vel = sub(v.vel, mul(cs.restitution * pvn, n));
+        }
+    }
+
+    void update_state(Body<R> &b, R dt, V3<R> disp_g) {  // :827-921
+        R max_sq = R(b.cs.max_linear_velocity) * R(b.cs.max_linear_velocity);
+        V3<R> lin = {R(0), R(0), R(0)}, ang = {R(0), R(0), R(0)};
+        const R big = R(FLT_MAX);
+        b.bmin = b.pmin = {big, big, big};
+        b.bmax = b.pmax = {-big, -big, -big};
+        for (auto &v : b.v) {
+            R vsq = len_sq(v.vel);
+            if (vsq > max_sq) v.vel = mul(v.vel, std::sqrt(max_sq / vsq));
+            lin = add(lin, v.vel);
+            ang = add(ang, cross(v.pos, v.vel));
+            b.bmin = vmin(b.bmin, v.pos);
+            b.bmax = vmax(b.bmax, v.pos);
+            V3<R> pred = add(add(v.pos, mul(v.vel, dt)), disp_g);
+            b.pmin = vmin(b.pmin, pred);
+            b.pmax = vmax(b.pmax, pred);
+            reset_collision(v);
+        }
+        R nvd = R(float(b.v.size() > 0 ? b.v.size() : 1));
+        b.lin_vel = divs(lin, nvd);
+        b.ang_vel = divs(ang, nvd);
+        if (b.cs.update_position) {
+            V3<R> delta = mul(R(0.5f), add(b.bmin, b.bmax));
+            for (auto &v : b.v) v.pos = sub(v.pos, delta);
+            b.bmin = sub(b.bmin, delta);
+            b.bmax = sub(b.bmax, delta);
+            b.pmin = sub(b.pmin, delta);
+            b.pmax = sub(b.pmax, delta);
+            V3<R> wd;  // Multiply3x3 with identity
+            wd.x = (R(1) * delta.x + R(0) * delta.y) + R(0) * delta.z;
+            wd.y = (R(0) * delta.x + R(1) * delta.y) + R(0) * delta.z;
+            wd.z = (R(0) * delta.x + R(0) * delta.y) + R(1) * delta.z;
+            b.position = add(b.position, wd);
+        }
+        b.force = {R(0), R(0), R(0)};  // ResetForce (:920)
+    }
+};
+
+struct Handle {
+    int use_double;
+    World<float> wf;
+    World<double> wd;
+    std::string err;
+};
+
+}  // namespace oracle
+
+using namespace oracle;
+
+extern "C" {
+
+void *oracle_world_create(const float gravity[3], int use_double) {
+    Handle *h = new Handle();
+    h->use_double = use_double;
+    h->wf.gravity = {gravity[0], gravity[1], gravity[2]};
+    h->wd.gravity = {double(gravity[0]), double(gravity[1]), double(gravity[2])};
+    return h;
+}
+
+void oracle_world_destroy(void *w) { delete static_cast<Handle *>(w); }
+
+int oracle_add_collider(void *w, int type, const float pos[3], const float half_extent[3], float radius, float friction,
+                        float restitution) {
+    Handle *h = static_cast<Handle *>(w);
+    Collider c;
+    c.type = type;
+    for (int k = 0; k < 3; ++k) {
+        c.pos[k] = pos[k];
+        c.half[k] = half_extent ? half_extent[k] : 0.0f;
+    }
+    c.radius = radius;
+    c.friction = friction;
+    c.restitution = restitution;
+    h->wf.colliders.push_back(c);
+    h->wd.colliders.push_back(c);
+    return int(h->wf.colliders.size()) - 1;
+}
+
+// creation: num_iterations, linear_damping, max_linear_velocity, restitution, friction, pressure,
+// gravity_factor, vertex_radius, update_position (as float 0/1)
+int oracle_add_body(void *w, const uint8_t *blob, size_t len, const float pos[3], const float creation[9]) {
+    Handle *h = static_cast<Handle *>(w);
+    auto s = std::make_shared<Settings>();
+    if (!parse_settings(blob, len, *s, h->err)) return -1;
+    if (s->n_skinned || s->n_rod_ss || s->n_rod_bt) {
+        h->err = "skinned constraints and rods are not supported";
+        return -1;
+    }
+    Creation cs;
+    cs.num_iterations = uint32_t(creation[0]);
+    cs.linear_damping = creation[1];
+    cs.max_linear_velocity = creation[2];
+    cs.restitution = creation[3];
+    cs.friction = creation[4];
+    cs.pressure = creation[5];
+    cs.gravity_factor = creation[6];
+    cs.vertex_radius = creation[7];
+    cs.update_position = creation[8] != 0.0f;
+    h->wd.add_body(s, pos, cs);
+    return h->wf.add_body(s, pos, cs);
+}
+
+int oracle_set_force(void *w, int body, const float f[3]) {
+    Handle *h = static_cast<Handle *>(w);
+    h->wf.bodies[body].force = {f[0], f[1], f[2]};
+    h->wd.bodies[body].force = {double(f[0]), double(f[1]), double(f[2])};
+    return 0;
+}
+
+int oracle_step(void *w, float dt, int collision_steps) {
+    Handle *h = static_cast<Handle *>(w);
+    if (h->use_double)
+        h->wd.step(double(dt), collision_steps);
+    else
+        h->wf.step(dt, collision_steps);
+    return 0;
+}
+
+int oracle_num_vertices(void *w, int body) { return int(static_cast<Handle *>(w)->wf.bodies[body].v.size()); }
+
+// Writes body position (3), local positions (3N), velocities (3N) as float (double results rounded).
+int oracle_get_body(void *w, int body, float *position, float *local_pos, float *vel) {
+    Handle *h = static_cast<Handle *>(w);
+    auto emit = [&](auto &b) {
+        position[0] = float(b.position.x);
+        position[1] = float(b.position.y);
+        position[2] = float(b.position.z);
+        for (size_t i = 0; i < b.v.size(); ++i) {
+            local_pos[3 * i + 0] = float(b.v[i].pos.x);
+            local_pos[3 * i + 1] = float(b.v[i].pos.y);
+            local_pos[3 * i + 2] = float(b.v[i].pos.z);
+            if (vel) {
+                vel[3 * i + 0] = float(b.v[i].vel.x);
+                vel[3 * i + 1] = float(b.v[i].vel.y);
+                vel[3 * i + 2] = float(b.v[i].vel.z);
+            }
+        }
+    };
+    if (h->use_double)
+        emit(h->wd.bodies[body]);
+    else
+        emit(h->wf.bodies[body]);
+    return 0;
+}
+
+// World-space positions in double (body position + local), for error reports against FP64.
+int oracle_get_world_positions_f64(void *w, int body, double *out) {
+    Handle *h = static_cast<Handle *>(w);
+    auto emit = [&](auto &b) {
+        for (size_t i = 0; i < b.v.size(); ++i) {
+            out[3 * i + 0] = double(b.position.x) + double(b.v[i].pos.x);
+            out[3 * i + 1] = double(b.position.y) + double(b.v[i].pos.y);
+            out[3 * i + 2] = double(b.position.z) + double(b.v[i].pos.z);
+        }
+    };
+    if (h->use_double)
+        emit(h->wd.bodies[body]);
+    else
+        emit(h->wf.bodies[body]);
+    return 0;
+}
+
+const char *oracle_last_error(void *w) { return static_cast<Handle *>(w)->err.c_str(); }
+
+}  // extern "C"

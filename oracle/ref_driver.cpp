@@ -1,0 +1,300 @@
+// Reference driver: runs the reference's own soft-body solver (Jolt Physics, built from its sources
+// by oracle/Makefile.ref) on the seeded scenes of joltphysics_gb300/csrc/host/scene_spec.h and
+// dumps what the tests need. TEST INFRASTRUCTURE ONLY: nothing in the product links or runs this.
+//
+// Bodies are created through the public API only:
+//   SoftBodySharedSettings::CreateConstraints / CalculateEdgeLengths / CalculateVolumeConstraintVolumes
+//   / Optimize (Jolt/Physics/SoftBody/SoftBodySharedSettings.cpp:189-369, 613-1182),
+//   BodyInterface::CreateAndAddSoftBody, PhysicsSystem::Update (Jolt/Physics/PhysicsSystem.cpp:176),
+//   SoftBodySharedSettings::SaveBinaryState (SoftBodySharedSettings.cpp:1203-1236),
+//   SoftBodyMotionProperties::SaveState (SoftBodyMotionProperties.cpp:1446-1473).
+//
+// Usage: ref_driver <scene> <out.bin> [key=value ...]
+//   scene: pinned_cloth | uneven_batch | large_cloth | diff_cloth | diff_batch
+//   keys : steps, dump (comma list of step numbers, 0 = initial), threads, seed, n, n_cloth, n_cube,
+//          cloth_min, cloth_max, cube_min, cube_max, time_only (1 = no dumps, print timing JSON)
+//
+// Output file (little endian):
+//   'JSBD' u32 version=2 u32 num_dumps u32 scene_len, scene_len bytes of the serialised scene
+//          (joltphysics_gb300/csrc/host/scene_io.h, settings bytes written by Jolt)
+//   per dump:  i32 step; per body: f32[3] body position, f32[3*N] local positions, f32[3*N] velocities,
+//              u32 state_len, state bytes (SaveState)
+
+#include <Jolt/Jolt.h>
+#include <Jolt/RegisterTypes.h>
+#include <Jolt/Core/Factory.h>
+#include <Jolt/Core/TempAllocator.h>
+#include <Jolt/Core/JobSystemThreadPool.h>
+#include <Jolt/Core/StreamWrapper.h>
+#include <Jolt/Physics/PhysicsSettings.h>
+#include <Jolt/Physics/PhysicsSystem.h>
+#include <Jolt/Physics/StateRecorderImpl.h>
+#include <Jolt/Physics/Collision/Shape/BoxShape.h>
+#include <Jolt/Physics/Collision/Shape/SphereShape.h>
+#include <Jolt/Physics/Body/BodyCreationSettings.h>
+#include <Jolt/Physics/SoftBody/SoftBodySharedSettings.h>
+#include <Jolt/Physics/SoftBody/SoftBodyCreationSettings.h>
+#include <Jolt/Physics/SoftBody/SoftBodyMotionProperties.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <sstream>
+#include <string>
+#include <thread>
+
+#include "../joltphysics_gb300/csrc/host/scene_io.h"
+
+using namespace JPH;
+
+namespace {
+
+namespace Layers {
+static constexpr ObjectLayer NON_MOVING = 0;
+static constexpr ObjectLayer MOVING = 1;
+static constexpr ObjectLayer NUM_LAYERS = 2;
+}  // namespace Layers
+
+class LayerPairFilter final : public ObjectLayerPairFilter {
+public:
+    bool ShouldCollide(ObjectLayer a, ObjectLayer b) const override {
+        return a == Layers::MOVING || b == Layers::MOVING;
+    }
+};
+
+class BPLayers final : public BroadPhaseLayerInterface {
+public:
+    uint GetNumBroadPhaseLayers() const override { return 2; }
+    BroadPhaseLayer GetBroadPhaseLayer(ObjectLayer l) const override { return BroadPhaseLayer(BroadPhaseLayer::Type(l)); }
+};
+
+class ObjVsBP final : public ObjectVsBroadPhaseLayerFilter {
+public:
+    bool ShouldCollide(ObjectLayer l, BroadPhaseLayer bp) const override {
+        return l == Layers::MOVING || BroadPhaseLayer::Type(bp) == BroadPhaseLayer::Type(Layers::MOVING);
+    }
+};
+
+SoftBodySharedSettings::VertexAttributes to_jolt(const jsb::scene::VertexAttributes &a) {
+    SoftBodySharedSettings::VertexAttributes r;
+    r.mCompliance = a.compliance;
+    r.mShearCompliance = a.shear_compliance;
+    r.mBendCompliance = a.bend_compliance;
+    r.mLRAType = SoftBodySharedSettings::ELRAType(int(a.lra_type));
+    r.mLRAMaxDistanceMultiplier = a.lra_max_distance_multiplier;
+    return r;
+}
+
+Ref<SoftBodySharedSettings> build_settings(const jsb::scene::MeshSpec &m) {
+    Ref<SoftBodySharedSettings> s = new SoftBodySharedSettings;
+    for (size_t i = 0; i < m.positions.size(); ++i) {
+        SoftBodySharedSettings::Vertex v;
+        v.mPosition = Float3(m.positions[i][0], m.positions[i][1], m.positions[i][2]);
+        v.mVelocity = Float3(m.velocities[i][0], m.velocities[i][1], m.velocities[i][2]);
+        v.mInvMass = m.inv_mass[i];
+        s->mVertices.push_back(v);
+    }
+    for (auto &f : m.faces) s->AddFace(SoftBodySharedSettings::Face(f[0], f[1], f[2]));
+    if (m.create_constraints) {
+        SoftBodySharedSettings::VertexAttributes a = to_jolt(m.attributes);
+        s->CreateConstraints(&a, 1, SoftBodySharedSettings::EBendType(int(m.bend_type)));
+    } else {
+        for (size_t i = 0; i < m.edges.size(); ++i)
+            s->mEdgeConstraints.push_back(SoftBodySharedSettings::Edge(m.edges[i][0], m.edges[i][1], m.edge_compliance[i]));
+        s->CalculateEdgeLengths();
+        for (size_t i = 0; i < m.volumes.size(); ++i)
+            s->mVolumeConstraints.push_back(SoftBodySharedSettings::Volume(m.volumes[i][0], m.volumes[i][1], m.volumes[i][2],
+                                                                          m.volumes[i][3], m.volume_compliance[i]));
+        s->CalculateVolumeConstraintVolumes();
+    }
+    s->Optimize();
+    if (!m.post_optimize_edge_compliance.empty())
+        for (size_t i = 0; i < s->mEdgeConstraints.size(); ++i)
+            s->mEdgeConstraints[i].mCompliance = m.post_optimize_edge_compliance[i];
+    return s;
+}
+
+std::string save_settings(const SoftBodySharedSettings &s) {
+    std::stringstream ss;
+    StreamOutWrapper w(ss);
+    s.SaveBinaryState(w);
+    return ss.str();
+}
+
+void put_u32(FILE *f, uint32_t v) { fwrite(&v, 4, 1, f); }
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    if (argc < 3) {
+        fprintf(stderr, "usage: ref_driver <scene> <out.bin> [key=value ...]\n");
+        return 2;
+    }
+    std::string scene_name = argv[1];
+    std::string out_path = argv[2];
+    std::map<std::string, std::string> kv;
+    for (int i = 3; i < argc; ++i) {
+        const char *eq = strchr(argv[i], '=');
+        if (!eq) continue;
+        kv[std::string(argv[i], eq - argv[i])] = eq + 1;
+    }
+    auto geti = [&](const char *k, long d) { return kv.count(k) ? std::stol(kv[k]) : d; };
+
+    std::string params;
+    for (auto &p : kv) params += p.first + "=" + p.second + " ";
+    jsb::scene::SceneSpec spec;
+    if (!jsb::scene::make_named_scene(scene_name, params, spec)) {
+        fprintf(stderr, "unknown scene %s\n", scene_name.c_str());
+        return 2;
+    }
+    int steps = int(geti("steps", spec.num_steps));
+    int threads = int(geti("threads", 1));
+    bool time_only = geti("time_only", 0) != 0;
+    std::vector<int> dump_steps;
+    if (kv.count("dump")) {
+        std::stringstream ds(kv["dump"]);
+        std::string tok;
+        while (std::getline(ds, tok, ',')) dump_steps.push_back(std::stoi(tok));
+    } else
+        dump_steps = {0, 1, steps};
+
+    RegisterDefaultAllocator();
+    Factory::sInstance = new Factory();
+    RegisterTypes();
+    {
+        TempAllocatorImpl temp_allocator(512 * 1024 * 1024);
+        JobSystemThreadPool job_system(cMaxPhysicsJobs, cMaxPhysicsBarriers, threads - 1);
+        BPLayers bp_layers;
+        ObjVsBP obj_vs_bp;
+        LayerPairFilter pair_filter;
+        PhysicsSystem system;
+        system.Init(uint(spec.bodies.size() + spec.colliders.size() + 16), 0, 65536, 65536, bp_layers, obj_vs_bp, pair_filter);
+        system.SetGravity(Vec3(spec.gravity[0], spec.gravity[1], spec.gravity[2]));
+        BodyInterface &bi = system.GetBodyInterface();
+
+        for (auto &c : spec.colliders) {
+            RefConst<Shape> shape;
+            if (c.type == jsb::scene::ColliderType::Box)
+                shape = new BoxShape(Vec3(c.half_extent[0], c.half_extent[1], c.half_extent[2]));
+            else
+                shape = new SphereShape(c.radius);
+            BodyCreationSettings bcs(shape, RVec3(c.position[0], c.position[1], c.position[2]), Quat::sIdentity(), EMotionType::Static,
+                                     Layers::NON_MOVING);
+            bcs.mFriction = c.friction;
+            bcs.mRestitution = c.restitution;
+            bi.CreateAndAddBody(bcs, EActivation::DontActivate);
+        }
+
+        std::vector<Ref<SoftBodySharedSettings>> settings;
+        std::vector<BodyID> ids;
+        for (auto &b : spec.bodies) {
+            settings.push_back(build_settings(b.mesh));
+            SoftBodyCreationSettings sbcs(settings.back(), RVec3(b.position[0], b.position[1], b.position[2]), Quat::sIdentity(),
+                                          Layers::MOVING);
+            sbcs.mNumIterations = b.creation.num_iterations;
+            sbcs.mLinearDamping = b.creation.linear_damping;
+            sbcs.mMaxLinearVelocity = b.creation.max_linear_velocity;
+            sbcs.mRestitution = b.creation.restitution;
+            sbcs.mFriction = b.creation.friction;
+            sbcs.mPressure = b.creation.pressure;
+            sbcs.mGravityFactor = b.creation.gravity_factor;
+            sbcs.mVertexRadius = b.creation.vertex_radius;
+            sbcs.mUpdatePosition = b.creation.update_position;
+            sbcs.mMakeRotationIdentity = b.creation.make_rotation_identity;
+            sbcs.mAllowSleeping = b.creation.allow_sleeping;
+            sbcs.mFacesDoubleSided = b.creation.faces_double_sided;
+            ids.push_back(bi.CreateAndAddSoftBody(sbcs, EActivation::Activate));
+        }
+        system.OptimizeBroadPhase();
+
+        FILE *f = nullptr;
+        if (!time_only) {
+            f = fopen(out_path.c_str(), "wb");
+            if (!f) {
+                fprintf(stderr, "cannot open %s\n", out_path.c_str());
+                return 1;
+            }
+            size_t body_index = 0;
+            std::string scene_bytes = jsb::scene::serialize_scene(spec, [&](const jsb::scene::MeshSpec &) {
+                return save_settings(*settings[body_index++]);
+            });
+            fwrite("JSBD", 4, 1, f);
+            put_u32(f, 2);
+            put_u32(f, uint32_t(dump_steps.size()));
+            put_u32(f, uint32_t(scene_bytes.size()));
+            fwrite(scene_bytes.data(), 1, scene_bytes.size(), f);
+        }
+        auto dump = [&](int step) {
+            int32_t st = step;
+            fwrite(&st, 4, 1, f);
+            BodyLockInterfaceNoLock const &lock_if = system.GetBodyLockInterfaceNoLock();
+            for (BodyID id : ids) {
+                BodyLockRead lock(lock_if, id);
+                const Body &body = lock.GetBody();
+                RVec3 p = body.GetPosition();
+                float pf[3] = {float(p.GetX()), float(p.GetY()), float(p.GetZ())};
+                fwrite(pf, 4, 3, f);
+                const SoftBodyMotionProperties *mp = static_cast<const SoftBodyMotionProperties *>(body.GetMotionProperties());
+                const auto &verts = mp->GetVertices();
+                std::vector<float> buf(verts.size() * 3);
+                for (size_t i = 0; i < verts.size(); ++i) {
+                    buf[3 * i + 0] = verts[i].mPosition.GetX();
+                    buf[3 * i + 1] = verts[i].mPosition.GetY();
+                    buf[3 * i + 2] = verts[i].mPosition.GetZ();
+                }
+                fwrite(buf.data(), 4, buf.size(), f);
+                for (size_t i = 0; i < verts.size(); ++i) {
+                    buf[3 * i + 0] = verts[i].mVelocity.GetX();
+                    buf[3 * i + 1] = verts[i].mVelocity.GetY();
+                    buf[3 * i + 2] = verts[i].mVelocity.GetZ();
+                }
+                fwrite(buf.data(), 4, buf.size(), f);
+                StateRecorderImpl rec;
+                mp->SaveState(rec);
+                std::string data = rec.GetData();
+                put_u32(f, uint32_t(data.size()));
+                fwrite(data.data(), 1, data.size(), f);
+            }
+        };
+
+        size_t next_dump = 0;
+        if (!time_only && next_dump < dump_steps.size() && dump_steps[next_dump] == 0) {
+            dump(0);
+            ++next_dump;
+        }
+        uint64_t total_vertices = 0, vi_per_step = 0;
+        for (size_t b = 0; b < spec.bodies.size(); ++b) {
+            total_vertices += spec.bodies[b].mesh.positions.size();
+            vi_per_step += uint64_t(spec.bodies[b].mesh.positions.size()) * spec.bodies[b].creation.num_iterations * spec.collision_steps;
+        }
+        double seconds = 0.0;
+        for (int step = 1; step <= steps; ++step) {
+            for (size_t b = 0; b < spec.bodies.size(); ++b) {
+                const float *fv = spec.bodies[b].force;
+                if (fv[0] != 0.0f || fv[1] != 0.0f || fv[2] != 0.0f) bi.AddForce(ids[b], Vec3(fv[0], fv[1], fv[2]));
+            }
+            auto t0 = std::chrono::steady_clock::now();
+            EPhysicsUpdateError err = system.Update(spec.dt, spec.collision_steps, &temp_allocator, &job_system);
+            auto t1 = std::chrono::steady_clock::now();
+            seconds += std::chrono::duration<double>(t1 - t0).count();
+            if (err != EPhysicsUpdateError::None) {
+                fprintf(stderr, "update error %d at step %d\n", int(err), step);
+                return 1;
+            }
+            if (!time_only && next_dump < dump_steps.size() && dump_steps[next_dump] == step) {
+                dump(step);
+                ++next_dump;
+            }
+        }
+        if (f) fclose(f);
+        printf("{\"scene\": \"%s\", \"bodies\": %zu, \"vertices\": %llu, \"steps\": %d, \"threads\": %d, \"seconds\": %.6f, "
+               "\"vertex_iterations_per_s\": %.6e}\n",
+               scene_name.c_str(), spec.bodies.size(), (unsigned long long)total_vertices, steps, threads, seconds,
+               double(vi_per_step) * steps / (seconds > 0 ? seconds : 1e-30));
+    }
+    UnregisterTypes();
+    delete Factory::sInstance;
+    Factory::sInstance = nullptr;
+    return 0;
+}

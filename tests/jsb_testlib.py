@@ -1,0 +1,224 @@
+"""Test helpers: scene/dump parsing and the CPU oracle binding.
+
+The oracle (oracle/liboracle.so) is test infrastructure: these helpers are the only code that loads it,
+and they are imported only by tests, ``__graft_entry__.smoke`` and ``bench.py``'s CPU baseline.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import struct
+import subprocess
+from dataclasses import dataclass, field
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(REPO, "oracle")
+ORACLE_LIB = os.path.join(ORACLE_DIR, "liboracle.so")
+REF_DRIVER = {v: os.path.join(ORACLE_DIR, "_ref", v, "ref_driver") for v in ("det", "fast")}
+
+CREATION_FMT = "<I7f4B"  # jsb_creation_settings, 36 bytes
+COLLIDER_FMT = "<i3f3f3f"  # type, position, half_extent, radius, friction, restitution (40 bytes)
+
+
+@dataclass
+class Collider:
+    type: int
+    position: tuple
+    half_extent: tuple
+    radius: float
+    friction: float
+    restitution: float
+
+    def pack(self) -> bytes:
+        return struct.pack(COLLIDER_FMT, self.type, *self.position, *self.half_extent, self.radius, self.friction,
+                           self.restitution)
+
+
+@dataclass
+class Body:
+    position: tuple
+    creation: tuple  # (num_iterations, damping, max_v, restitution, friction, pressure, gravity_factor, radius, 4 flags)
+    force: tuple
+    blob: bytes
+    num_vertices: int = 0
+
+    @property
+    def num_iterations(self) -> int:
+        return int(self.creation[0])
+
+    def creation_bytes(self) -> bytes:
+        return struct.pack(CREATION_FMT, *self.creation)
+
+
+@dataclass
+class Scene:
+    gravity: tuple
+    dt: float
+    collision_steps: int
+    num_steps: int
+    colliders: list = field(default_factory=list)
+    bodies: list = field(default_factory=list)
+    raw: bytes = b""
+
+
+def blob_num_vertices(blob: bytes) -> int:
+    return struct.unpack_from("<I", blob, 0)[0]
+
+
+def parse_scene(buf: bytes, off: int = 0) -> tuple[Scene, int]:
+    assert buf[off:off + 4] == b"JSBS", "not a scene"
+    start = off
+    _, nb, nc = struct.unpack_from("<III", buf, off + 4)
+    off += 16
+    g = struct.unpack_from("<3f", buf, off)
+    dt, cs, ns = struct.unpack_from("<fii", buf, off + 12)
+    off += 24
+    sc = Scene(gravity=g, dt=dt, collision_steps=cs, num_steps=ns)
+    for _ in range(nc):
+        v = struct.unpack_from(COLLIDER_FMT, buf, off)
+        off += 40
+        sc.colliders.append(Collider(v[0], v[1:4], v[4:7], v[7], v[8], v[9]))
+    for _ in range(nb):
+        pos = struct.unpack_from("<3f", buf, off)
+        off += 12
+        cr = struct.unpack_from(CREATION_FMT, buf, off)
+        off += 36
+        force = struct.unpack_from("<3f", buf, off)
+        off += 12
+        (bl,) = struct.unpack_from("<I", buf, off)
+        off += 4
+        blob = bytes(buf[off:off + bl])
+        off += bl
+        sc.bodies.append(Body(pos, cr, force, blob, blob_num_vertices(blob)))
+    sc.raw = bytes(buf[start:off])
+    return sc, off
+
+
+@dataclass
+class Dump:
+    step: int
+    positions: list  # per body: body position (3,)
+    local: list  # per body: (N, 3)
+    velocities: list  # per body: (N, 3)
+    states: list  # per body: SaveState bytes
+
+    def world(self, b: int) -> np.ndarray:
+        return self.local[b].astype(np.float64) + np.asarray(self.positions[b], np.float64)
+
+
+def parse_dump(path: str) -> tuple[Scene, list]:
+    buf = open(path, "rb").read()
+    assert buf[:4] == b"JSBD"
+    ver, nd, sl = struct.unpack_from("<III", buf, 4)
+    assert ver == 2
+    scene, off = parse_scene(buf, 16)
+    dumps = []
+    for _ in range(nd):
+        (step,) = struct.unpack_from("<i", buf, off)
+        off += 4
+        d = Dump(step, [], [], [], [])
+        for b in scene.bodies:
+            n = b.num_vertices
+            d.positions.append(np.frombuffer(buf, np.float32, 3, off).copy())
+            off += 12
+            d.local.append(np.frombuffer(buf, np.float32, 3 * n, off).reshape(n, 3).copy())
+            off += 12 * n
+            d.velocities.append(np.frombuffer(buf, np.float32, 3 * n, off).reshape(n, 3).copy())
+            off += 12 * n
+            (stl,) = struct.unpack_from("<I", buf, off)
+            off += 4
+            d.states.append(bytes(buf[off:off + stl]))
+            off += stl
+        dumps.append(d)
+    return scene, dumps
+
+
+def run_reference(variant: str, scene: str, out: str, **kv) -> dict:
+    """Runs the reference driver (only where oracle/_ref was built)."""
+    args = [REF_DRIVER[variant], scene, out] + [f"{k}={v}" for k, v in kv.items()]
+    res = subprocess.run(args, check=True, capture_output=True, text=True)
+    import json
+    return json.loads(res.stdout.strip().splitlines()[-1])
+
+
+def build_oracle() -> str:
+    src = os.path.join(ORACLE_DIR, "jsb_oracle.cpp")
+    if (not os.path.exists(ORACLE_LIB)) or os.path.getmtime(ORACLE_LIB) < os.path.getmtime(src):
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", src, "-o", ORACLE_LIB],
+                       check=True)
+    return ORACLE_LIB
+
+
+class Oracle:
+    """ctypes wrapper of the CPU oracle (float = bitwise restatement of the reference; double = FP64)."""
+
+    _lib = None
+
+    @classmethod
+    def lib(cls):
+        if cls._lib is None:
+            build_oracle()
+            L = ctypes.CDLL(ORACLE_LIB)
+            L.oracle_world_create.restype = ctypes.c_void_p
+            L.oracle_world_create.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.c_int]
+            L.oracle_world_destroy.argtypes = [ctypes.c_void_p]
+            L.oracle_add_collider.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
+                                              ctypes.POINTER(ctypes.c_float), ctypes.c_float, ctypes.c_float,
+                                              ctypes.c_float]
+            L.oracle_add_body.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t,
+                                          ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
+            L.oracle_set_force.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+            L.oracle_step.argtypes = [ctypes.c_void_p, ctypes.c_float, ctypes.c_int]
+            L.oracle_num_vertices.argtypes = [ctypes.c_void_p, ctypes.c_int]
+            L.oracle_get_body.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p]
+            L.oracle_get_world_positions_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+            L.oracle_last_error.restype = ctypes.c_char_p
+            L.oracle_last_error.argtypes = [ctypes.c_void_p]
+            cls._lib = L
+        return cls._lib
+
+    def __init__(self, scene: Scene, use_double: bool = False):
+        L = self.lib()
+        self.scene = scene
+        g = (ctypes.c_float * 3)(*scene.gravity)
+        self.h = L.oracle_world_create(g, int(use_double))
+        for c in scene.colliders:
+            L.oracle_add_collider(self.h, c.type, (ctypes.c_float * 3)(*c.position),
+                                  (ctypes.c_float * 3)(*c.half_extent), c.radius, c.friction, c.restitution)
+        self.nv = []
+        for b in scene.bodies:
+            cr = b.creation
+            creation = (ctypes.c_float * 9)(cr[0], cr[1], cr[2], cr[3], cr[4], cr[5], cr[6], cr[7], cr[8])
+            idx = L.oracle_add_body(self.h, b.blob, len(b.blob), (ctypes.c_float * 3)(*b.position), creation)
+            if idx < 0:
+                raise RuntimeError(L.oracle_last_error(self.h).decode())
+            self.nv.append(L.oracle_num_vertices(self.h, idx))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib().oracle_world_destroy(self.h)
+            self.h = None
+
+    def step(self, n: int = 1):
+        L = self.lib()
+        for _ in range(n):
+            for i, b in enumerate(self.scene.bodies):
+                if any(f != 0.0 for f in b.force):
+                    L.oracle_set_force(self.h, i, (ctypes.c_float * 3)(*b.force))
+            L.oracle_step(self.h, self.scene.dt, self.scene.collision_steps)
+
+    def body(self, i: int):
+        n = self.nv[i]
+        pos = np.zeros(3, np.float32)
+        loc = np.zeros((n, 3), np.float32)
+        vel = np.zeros((n, 3), np.float32)
+        self.lib().oracle_get_body(self.h, i, pos.ctypes.data, loc.ctypes.data, vel.ctypes.data)
+        return pos, loc, vel
+
+    def world_f64(self, i: int) -> np.ndarray:
+        out = np.zeros((self.nv[i], 3), np.float64)
+        self.lib().oracle_get_world_positions_f64(self.h, i, out.ctypes.data)
+        return out
