@@ -1,0 +1,358 @@
+"""Benchmark: soft-body vertex-iterations/s of the GPU solver step on the uneven-body batch.
+
+Workload (the batch the metric is quoted on): 384 cloths with grid side U{8..64} (one border row pinned,
+dihedral bends, edge compliance log-U[1e-7, 1e-3]) and 128 tetrahedralised cubes with U{4..12} cells
+(5 tets per cell, volume compliance log-U[1e-8, 1e-5], pressure 0 or 1e3), falling onto a static box
+floor; 5 iterations, dt = 1/60. Seeded synthetic inputs built with this library's
+SoftBodySharedSettings mirror (byte-identical to the reference's CreateConstraints/Optimize output).
+
+One bench step = one PhysicsSystem::Update(1/60, 1 collision step) of all 512 bodies: every body
+advances 5 substeps (vertex-iterations = sum of vertices x 5 per step).
+
+  value : vertex-iterations/s with the state resident in HBM, batched persistent launches replayed as a
+          CUDA graph of one step; L2 is flushed (a 512 MB write) before every timed step and each step is
+          timed alone with CUDA events on the launching stream.
+  e2e   : the same through the C ABI with host buffers: per step, positions + velocities of every vertex
+          are copied from pinned host memory (jsb_state_upload_all), the step runs, and the state is
+          copied back (jsb_state_download_all), all inside the timed region.
+
+`--impl reference` times the CPU oracle (a restatement of the reference's soft-body update that is
+bit-identical to it; the reference itself cannot be built on the GPU hosts) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "soft-body vertex-iterations/s on 1 GB300: batched+adjoint vs plain, % of roofline"
+UNIT = "vertex-iterations/s"
+WORKLOAD = "uneven_batch"
+
+
+def rank_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def scene_params(rank: int) -> dict:
+    # weak scaling: every rank simulates its own seeded batch of the same shape
+    return {"seed": 2 + rank}
+
+
+def algorithmic_bytes_per_step(scene) -> float:
+    """Per-substep bytes of every body (state as float4, every access counted, no cache credit):
+    B_sub = 180 N_v + 80 N_edge + 152 (N_bend + N_vol) + 60 N_lra + 216 N_face [pressure > 0]."""
+    import struct
+
+    total = 0.0
+    for b in scene.bodies:
+        blob = b.blob
+        off = 0
+        counts = {}
+        for name, size in [("v", 28), ("f", 16), ("e", 16), ("b", 24), ("vol", 24), ("sk", 52), ("skn", 4), ("lra", 12)]:
+            (n,) = struct.unpack_from("<I", blob, off)
+            counts[name] = n
+            off += 4 + n * size
+        pressure = b.creation[5] > 0.0
+        sub = (180 * counts["v"] + 80 * counts["e"] + 152 * (counts["b"] + counts["vol"]) + 60 * counts["lra"]
+               + (216 * counts["f"] if pressure else 0))
+        total += sub * b.num_iterations
+    return total
+
+
+def measured_peaks() -> dict:
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def profile_traffic() -> float | None:
+    """DRAM bytes per step of the solver kernel from the committed ncu summary, if present."""
+    path = os.path.join(REPO, "profiles", "step_kernel_uneven_batch.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_step:"):
+            return float(line.split(":", 1)[1].split()[0])
+    return None
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[3:7]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def run_reference_arm(args, rank, world):
+    """CPU oracle on the host cores (the reference arm)."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import joltphysics_gb300 as jsb
+    from jsb_testlib import Oracle, parse_scene
+
+    scene_bytes = jsb.build_scene(WORKLOAD, **scene_params(0))
+    scene, _ = parse_scene(scene_bytes)
+    threads = os.cpu_count() or 1
+    o = Oracle(scene, threads=threads)
+    vi_step = sum(b.num_vertices * b.num_iterations for b in scene.bodies)
+    for _ in range(args.warmup):
+        o.step(1)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.step(1)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = vi_step * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "bodies": len(scene.bodies), "vertices": sum(b.num_vertices for b in scene.bodies),
+                   "iterations": 5, "dt": scene.dt},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full steps of all {len(scene.bodies)} bodies"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def cpu_baseline(scene, budget_s: float = 12.0) -> dict:
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    from jsb_testlib import Oracle
+
+    threads = os.cpu_count() or 1
+    o = Oracle(scene, threads=threads)
+    vi_step = sum(b.num_vertices * b.num_iterations for b in scene.bodies)
+    t0 = time.perf_counter()
+    o.step(1)
+    first = time.perf_counter() - t0
+    n = max(1, min(200, int(budget_s / max(first, 1e-6))))
+    t0 = time.perf_counter()
+    o.step(n)
+    dt = time.perf_counter() - t0
+    return {"value": vi_step * n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} full steps of all {len(scene.bodies)} bodies (after 1 warm-up step)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="jsb", choices=["jsb", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-steps", type=int, default=2)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank, world, local = rank_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist = dist_mod
+        backend = "nccl"
+        dist.init_process_group(backend)
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import joltphysics_gb300 as jsb
+    from jsb_testlib import parse_scene
+
+    scene_bytes = jsb.build_scene(WORKLOAD, **scene_params(rank))
+    scene, _ = parse_scene(scene_bytes)
+    ctx = jsb.Context(local)
+    ctx.load_scene(scene_bytes)
+    n_vertices = ctx.total_vertices()
+    vi_step = sum(b.num_vertices * b.num_iterations for b in scene.bodies)
+    bytes_step = algorithmic_bytes_per_step(scene)
+
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    # autotune the launch shape per body-size bucket, then warm up (graph of one step)
+    ctx.autotune(trials=2)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            ctx.step_graph(1, 1, stream=sptr)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+
+    # ---- device-resident timed region ------------------------------------------------------------
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    launches = 0
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t_wall = time.perf_counter()
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(i & 0xFF)  # L2 flush (untimed: outside the event pair)
+                starts[i].record(stream)
+                ctx.step_graph(1, 1, stream=sptr)
+                ends[i].record(stream)
+            launches += ctx.last_launch_count()
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    ctx.synchronize()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = vi_step * world * args.steps / (total_ms / 1000.0)
+
+    # ---- end to end through the C ABI with host buffers ------------------------------------------
+    pos_h = torch.empty((n_vertices, 3), dtype=torch.float32, pin_memory=True)
+    vel_h = torch.empty((n_vertices, 3), dtype=torch.float32, pin_memory=True)
+    with torch.cuda.stream(stream):
+        ctx.download_all(pos_h.numpy(), vel_h.numpy(), stream=sptr)
+    torch.cuda.synchronize()
+    e2e_steps = max(3, args.steps // 2)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for _ in range(e2e_steps):
+            ctx.upload_all(pos_h.numpy(), vel_h.numpy(), stream=sptr)
+            ctx.step(stream=sptr)
+            ctx.download_all(pos_h.numpy(), vel_h.numpy(), stream=sptr)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = vi_step * world * e2e_steps / (e2e_ms / 1000.0)
+    io_bytes = n_vertices * 3 * 4 * 2
+
+    # ---- plain one-body-per-launch form (for the batched / plain ratio) --------------------------
+    plain_value = None
+    if args.plain_steps > 0:
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            ctx.step_plain(stream=sptr)
+            p0.record(stream)
+            for _ in range(args.plain_steps):
+                ctx.step_plain(stream=sptr)
+            p1.record(stream)
+        torch.cuda.synchronize()
+        ctx.synchronize()
+        plain_value = vi_step * args.plain_steps / (p0.elapsed_time(p1) / 1000.0)
+
+    peaks = measured_peaks()
+    mean_step_s = total_ms / 1000.0 / args.steps
+    achieved = bytes_step / mean_step_s / 1e9
+    traffic = profile_traffic()
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "bodies": len(scene.bodies), "vertices": n_vertices, "iterations": 5,
+                   "dt": scene.dt, "vertex_iterations_per_step": vi_step, "l2": "flushed before every timed step",
+                   "form": "batched persistent launches per size bucket, CUDA graph of one step"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
+                "steps": e2e_steps},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                     "peak_source": peaks["source"], "algorithmic_bytes_per_step": bytes_step},
+        "plain": {"value": plain_value, "unit": UNIT, "steps": args.plain_steps,
+                  "batched_over_plain": (value / plain_value) if plain_value else None},
+        "clocks": clocks.summary(),
+        "wall_s": t_wall,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(scene)
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

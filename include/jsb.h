@@ -98,6 +98,10 @@ jsb_status jsb_body_restore_state(jsb_context *ctx, uint32_t body_id, const void
 /* MotionProperties::AddForce: accumulated until the next step consumes it (ResetForce). */
 jsb_status jsb_body_add_force(jsb_context *ctx, uint32_t body_id, const float force[3]);
 
+/* A force added before every step (the effect of calling AddForce with the same value before each
+ * PhysicsSystem::Update); kept until changed. Unlike jsb_body_add_force it can be captured in graphs. */
+jsb_status jsb_body_set_step_force(jsb_context *ctx, uint32_t body_id, const float force[3]);
+
 jsb_status jsb_collider_add(jsb_context *ctx, const jsb_collider *collider, uint32_t *collider_id);
 
 jsb_status jsb_body_num_vertices(jsb_context *ctx, uint32_t body_id, uint32_t *num_vertices);
@@ -138,6 +142,14 @@ jsb_status jsb_total_vertices(jsb_context *ctx, uint64_t *total);
 /* ---- scheduling and autotuning ------------------------------------------------------------ */
 /* Number of dependency levels of a body's constraint schedule per substep and total constraints. */
 jsb_status jsb_body_schedule_info(jsb_context *ctx, uint32_t body_id, uint32_t *num_levels, uint32_t *num_constraints);
+
+/* Host only (no device needed): the dependency-level schedule built for these settings bytes.
+ * levels receives 4 x (num_levels + 2) uint32 {first record, end of bends, end of volumes, end of
+ * edges}, records 4 x num_records uint32 (16-byte records), source num_records uint32
+ * (type << 28 | index in the settings' constraint array; type 0 bend, 1 volume, 2 edge, 3 LRA).
+ * Pass NULL arrays to query the sizes. */
+jsb_status jsb_settings_schedule(const void *blob, size_t len, uint32_t *num_levels, uint32_t *num_records,
+                                 uint32_t *levels, uint32_t *records, uint32_t *source);
 
 /* Threads per CTA used for bodies whose vertex count is <= max_vertices (bucket table written by
  * the autotuner; threads in {32, 64, 128, 256}). */

@@ -1,0 +1,277 @@
+"""jsb: GB300-native soft-body solver step for Jolt Physics.
+
+The product is ``libjsb.so`` (CUDA kernels for sm_103a + C++ host runtime) behind the C ABI declared
+in ``include/jsb.h``. This module is a thin ctypes binding over that ABI, used by the tests and the
+benchmark; it mirrors the reference's objects (shared settings bytes, creation settings, colliders,
+bodies) and raises ``JsbError`` with the library's message on any non-zero status. There is no CPU
+fallback: importing without a built ``libjsb.so`` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import struct
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libjsb.so")
+
+JSB_OK = 0
+STATUS_NAMES = {
+    1: "JSB_ERR_INVALID_ARGUMENT", 2: "JSB_ERR_BLOB", 3: "JSB_ERR_UNSUPPORTED", 4: "JSB_ERR_CUDA",
+    5: "JSB_ERR_OUT_OF_MEMORY", 6: "JSB_ERR_TIMEOUT", 7: "JSB_ERR_NONFINITE", 8: "JSB_ERR_CAPACITY",
+}
+
+# Every entry point of include/jsb.h with its ctypes signature.
+_c = ctypes
+_P = _c.c_void_p
+SIGNATURES = {
+    "jsb_context_create": [_c.c_int, _c.POINTER(_P)],
+    "jsb_context_destroy": [_P],
+    "jsb_last_error_string": [],
+    "jsb_version": [],
+    "jsb_set_gravity": [_P, _c.POINTER(_c.c_float)],
+    "jsb_settings_upload": [_P, _c.c_char_p, _c.c_size_t, _c.POINTER(_c.c_uint32)],
+    "jsb_body_add": [_P, _c.c_uint32, _c.c_char_p, _c.POINTER(_c.c_float), _c.POINTER(_c.c_uint32)],
+    "jsb_body_restore_state": [_P, _c.c_uint32, _c.c_char_p, _c.c_size_t, _c.POINTER(_c.c_float)],
+    "jsb_body_add_force": [_P, _c.c_uint32, _c.POINTER(_c.c_float)],
+    "jsb_body_set_step_force": [_P, _c.c_uint32, _c.POINTER(_c.c_float)],
+    "jsb_collider_add": [_P, _c.c_char_p, _c.POINTER(_c.c_uint32)],
+    "jsb_body_num_vertices": [_P, _c.c_uint32, _c.POINTER(_c.c_uint32)],
+    "jsb_step": [_P, _c.c_float, _c.c_int, _P],
+    "jsb_step_plain": [_P, _c.c_float, _c.c_int, _P],
+    "jsb_step_graph": [_P, _c.c_float, _c.c_int, _c.c_int, _c.c_int, _P],
+    "jsb_synchronize": [_P],
+    "jsb_body_read": [_P, _c.c_uint32, _P, _P, _P],
+    "jsb_body_save_state": [_P, _c.c_uint32, _P, _c.c_size_t, _c.POINTER(_c.c_size_t)],
+    "jsb_state_upload_all": [_P, _P, _P, _P],
+    "jsb_state_download_all": [_P, _P, _P, _P],
+    "jsb_total_vertices": [_P, _c.POINTER(_c.c_uint64)],
+    "jsb_body_schedule_info": [_P, _c.c_uint32, _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32)],
+    "jsb_settings_schedule": [_c.c_char_p, _c.c_size_t, _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32), _P, _P, _P],
+    "jsb_set_bucket_threads": [_P, _c.c_uint32, _c.c_uint32],
+    "jsb_autotune": [_P, _c.c_float, _c.c_int],
+    "jsb_last_launch_count": [_P, _c.POINTER(_c.c_uint32)],
+    "jsb_last_kernel_ms": [_P, _c.POINTER(_c.c_float)],
+    "jsb_scene_build": [_c.c_char_p, _c.c_char_p, _P, _c.c_size_t, _c.POINTER(_c.c_size_t)],
+}
+
+
+class JsbError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Loads libjsb.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with `python -m joltphysics_gb300.build`")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_char_p if name in ("jsb_last_error_string", "jsb_version") else ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def check(status: int):
+    if status != JSB_OK:
+        raise JsbError(status, lib().jsb_last_error_string().decode(errors="replace"))
+
+
+def _f3(v) -> ctypes.Array:
+    return (ctypes.c_float * 3)(*[float(x) for x in v])
+
+
+CREATION_FMT = "<I7f4B"
+COLLIDER_FMT = "<i3f3f3f"
+
+
+def build_scene(name: str, **params) -> bytes:
+    """Serialised seeded scene (see csrc/host/scene_io.h) built with this library's settings mirror."""
+    p = " ".join(f"{k}={v}" for k, v in params.items()).encode()
+    n = ctypes.c_size_t(0)
+    check(lib().jsb_scene_build(name.encode(), p, None, 0, ctypes.byref(n)))
+    buf = ctypes.create_string_buffer(n.value)
+    check(lib().jsb_scene_build(name.encode(), p, buf, n.value, ctypes.byref(n)))
+    return buf.raw[: n.value]
+
+
+def settings_schedule(blob: bytes):
+    """Dependency-level schedule for settings bytes (host only): (levels (L+2, 4), records (R, 4), source (R,))."""
+    nl, nr = ctypes.c_uint32(), ctypes.c_uint32()
+    check(lib().jsb_settings_schedule(blob, len(blob), ctypes.byref(nl), ctypes.byref(nr), None, None, None))
+    levels = np.zeros((nl.value + 2, 4), np.uint32)
+    records = np.zeros((nr.value, 4), np.uint32)
+    source = np.zeros(nr.value, np.uint32)
+    check(lib().jsb_settings_schedule(blob, len(blob), ctypes.byref(nl), ctypes.byref(nr), levels.ctypes.data,
+                                      records.ctypes.data, source.ctypes.data))
+    return levels, records, source
+
+
+class Context:
+    """One GPU solver context (jsb_context)."""
+
+    def __init__(self, device: int = 0):
+        self.h = ctypes.c_void_p()
+        check(lib().jsb_context_create(device, ctypes.byref(self.h)))
+        self.num_vertices: list[int] = []
+
+    def close(self):
+        if self.h:
+            check(lib().jsb_context_destroy(self.h))
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- setup -----------------------------------------------------------------------------------
+    def set_gravity(self, g):
+        check(lib().jsb_set_gravity(self.h, _f3(g)))
+
+    def upload_settings(self, blob: bytes) -> int:
+        sid = ctypes.c_uint32()
+        check(lib().jsb_settings_upload(self.h, blob, len(blob), ctypes.byref(sid)))
+        return sid.value
+
+    def add_body(self, settings_id: int, creation: tuple, position) -> int:
+        bid = ctypes.c_uint32()
+        check(lib().jsb_body_add(self.h, settings_id, struct.pack(CREATION_FMT, *creation), _f3(position),
+                                 ctypes.byref(bid)))
+        n = ctypes.c_uint32()
+        check(lib().jsb_body_num_vertices(self.h, bid.value, ctypes.byref(n)))
+        self.num_vertices.append(n.value)
+        return bid.value
+
+    def add_collider(self, type_: int, position, half_extent=(0, 0, 0), radius=0.0, friction=0.2,
+                     restitution=0.0) -> int:
+        cid = ctypes.c_uint32()
+        raw = struct.pack(COLLIDER_FMT, type_, *position, *half_extent, radius, friction, restitution)
+        check(lib().jsb_collider_add(self.h, raw, ctypes.byref(cid)))
+        return cid.value
+
+    def load_scene(self, scene_bytes: bytes) -> list[dict]:
+        """Adds the colliders and bodies of a serialised scene; returns per-body info."""
+        b = scene_bytes
+        assert b[:4] == b"JSBS"
+        _, nb, nc = struct.unpack_from("<III", b, 4)
+        g = struct.unpack_from("<3f", b, 16)
+        dt, cs, ns = struct.unpack_from("<fii", b, 28)
+        self.set_gravity(g)
+        self.dt, self.collision_steps, self.scene_steps = dt, cs, ns
+        off = 40
+        for _ in range(nc):
+            v = struct.unpack_from(COLLIDER_FMT, b, off)
+            off += 40
+            self.add_collider(v[0], v[1:4], v[4:7], v[7], v[8], v[9])
+        bodies = []
+        for _ in range(nb):
+            pos = struct.unpack_from("<3f", b, off)
+            cr = struct.unpack_from(CREATION_FMT, b, off + 12)
+            force = struct.unpack_from("<3f", b, off + 48)
+            (bl,) = struct.unpack_from("<I", b, off + 60)
+            blob = b[off + 64: off + 64 + bl]
+            off += 64 + bl
+            sid = self.upload_settings(blob)
+            bid = self.add_body(sid, cr, pos)
+            bodies.append({"id": bid, "force": force, "iterations": cr[0], "vertices": self.num_vertices[bid]})
+        self.bodies = bodies
+        return bodies
+
+    # -- stepping --------------------------------------------------------------------------------
+    def add_force(self, body: int, f):
+        check(lib().jsb_body_add_force(self.h, body, _f3(f)))
+
+    def set_step_force(self, body: int, f):
+        check(lib().jsb_body_set_step_force(self.h, body, _f3(f)))
+
+    def apply_scene_forces(self):
+        """One-shot AddForce of every body's scene force (consumed by the next step)."""
+        for b in self.bodies:
+            if any(x != 0.0 for x in b["force"]):
+                self.add_force(b["id"], b["force"])
+
+    def set_scene_step_forces(self):
+        """Scene forces applied before every step (graph-capturable)."""
+        for b in self.bodies:
+            if any(x != 0.0 for x in b["force"]):
+                self.set_step_force(b["id"], b["force"])
+
+    def step(self, dt: float | None = None, collision_steps: int | None = None, stream: int = 0):
+        check(lib().jsb_step(self.h, dt or self.dt, collision_steps or self.collision_steps, ctypes.c_void_p(stream)))
+
+    def step_plain(self, dt: float | None = None, collision_steps: int | None = None, stream: int = 0):
+        check(lib().jsb_step_plain(self.h, dt or self.dt, collision_steps or self.collision_steps,
+                                   ctypes.c_void_p(stream)))
+
+    def step_graph(self, num_steps: int, repeats: int = 1, dt: float | None = None, collision_steps: int | None = None,
+                   stream: int = 0):
+        check(lib().jsb_step_graph(self.h, dt or self.dt, collision_steps or self.collision_steps, num_steps, repeats,
+                                   ctypes.c_void_p(stream)))
+
+    def synchronize(self):
+        check(lib().jsb_synchronize(self.h))
+
+    def autotune(self, dt: float | None = None, trials: int = 2):
+        check(lib().jsb_autotune(self.h, dt or self.dt, trials))
+
+    def set_bucket_threads(self, max_vertices: int, threads: int):
+        check(lib().jsb_set_bucket_threads(self.h, max_vertices, threads))
+
+    # -- readback --------------------------------------------------------------------------------
+    def read_body(self, body: int):
+        n = self.num_vertices[body]
+        pos = np.zeros(3, np.float32)
+        loc = np.zeros((n, 3), np.float32)
+        vel = np.zeros((n, 3), np.float32)
+        check(lib().jsb_body_read(self.h, body, pos.ctypes.data, loc.ctypes.data, vel.ctypes.data))
+        return pos, loc, vel
+
+    def save_state(self, body: int) -> bytes:
+        n = ctypes.c_size_t()
+        check(lib().jsb_body_save_state(self.h, body, None, 0, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value)
+        check(lib().jsb_body_save_state(self.h, body, buf, n.value, ctypes.byref(n)))
+        return buf.raw
+
+    def restore_state(self, body: int, state: bytes, position):
+        check(lib().jsb_body_restore_state(self.h, body, state, len(state), _f3(position)))
+
+    def total_vertices(self) -> int:
+        t = ctypes.c_uint64()
+        check(lib().jsb_total_vertices(self.h, ctypes.byref(t)))
+        return t.value
+
+    def schedule_info(self, body: int):
+        lv, nc = ctypes.c_uint32(), ctypes.c_uint32()
+        check(lib().jsb_body_schedule_info(self.h, body, ctypes.byref(lv), ctypes.byref(nc)))
+        return lv.value, nc.value
+
+    def last_launch_count(self) -> int:
+        n = ctypes.c_uint32()
+        check(lib().jsb_last_launch_count(self.h, ctypes.byref(n)))
+        return n.value
+
+    def last_kernel_ms(self) -> float:
+        v = ctypes.c_float()
+        check(lib().jsb_last_kernel_ms(self.h, ctypes.byref(v)))
+        return v.value
+
+    def upload_all(self, positions: np.ndarray, velocities: np.ndarray, stream: int = 0):
+        check(lib().jsb_state_upload_all(self.h, ctypes.c_void_p(positions.ctypes.data),
+                                         ctypes.c_void_p(velocities.ctypes.data), ctypes.c_void_p(stream)))
+
+    def download_all(self, positions: np.ndarray, velocities: np.ndarray, stream: int = 0):
+        check(lib().jsb_state_download_all(self.h, ctypes.c_void_p(positions.ctypes.data),
+                                           ctypes.c_void_p(velocities.ctypes.data), ctypes.c_void_p(stream)))

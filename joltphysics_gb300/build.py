@@ -1,0 +1,108 @@
+"""Builds libjsb.so (CUDA kernels for sm_103a + C++ host runtime + C ABI) in-tree.
+
+    python -m joltphysics_gb300.build            # or joltphysics_gb300.build.build()
+
+nvcc compiles the kernels with ``--fmad=false`` (the solver reproduces the reference's unfused float
+operation order) and IEEE division/square root; the host C++ is compiled with ``-ffp-contract=off``
+for the same reason. Translation units are compiled in parallel.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "libjsb.so")
+
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+CU_SOURCES = ["kernels/solver.cu", "kernels/state_io.cu"]
+CXX_SOURCES = ["host/runtime.cpp", "host/schedule.cpp", "host/shared_settings.cpp"]
+
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-std=c++17",
+                     "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(REPO, "include")]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I" + os.path.join(CUDA_HOME, "include"),
+             "-I" + os.path.join(REPO, "include")]
+
+
+def _obj(src: str) -> str:
+    return os.path.join(BUILD, src.replace("/", "_") + ".o")
+
+
+def _stale(target: str, deps: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _headers() -> list[str]:
+    out = []
+    for root, _, files in os.walk(CSRC):
+        out += [os.path.join(root, f) for f in files if f.endswith((".h", ".cuh"))]
+    out.append(os.path.join(REPO, "include", "jsb.h"))
+    return out
+
+
+def build(verbose: bool = False, extra_nvcc: list[str] | None = None) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    headers = _headers()
+    jobs = []
+    for src in CU_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = _obj(src)
+        if _stale(o, [s] + headers):
+            jobs.append(([NVCC] + NVCC_FLAGS + (extra_nvcc or []) + ["-c", s, "-o", o], o))
+    for src in CXX_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = _obj(src)
+        if _stale(o, [s] + headers):
+            jobs.append((["g++"] + CXX_FLAGS + ["-c", s, "-o", o], o))
+    procs = [(subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True), cmd) for cmd, _ in jobs]
+    failed = []
+    for p, cmd in procs:
+        out, _ = p.communicate()
+        if verbose or p.returncode != 0:
+            sys.stderr.write(" ".join(cmd) + "\n" + (out or ""))
+        if p.returncode != 0:
+            failed.append(cmd[-1])
+    if failed:
+        raise RuntimeError("compilation failed: " + ", ".join(failed))
+    objs = [_obj(s) for s in CU_SOURCES + CXX_SOURCES]
+    if jobs or _stale(LIB, objs):
+        cmd = ["g++", "-shared", "-o", LIB] + objs + ["-L" + os.path.join(CUDA_HOME, "lib64"), "-lcudart",
+                                                     "-Wl,-rpath," + os.path.join(CUDA_HOME, "lib64")]
+        subprocess.run(cmd, check=True)
+    return LIB
+
+
+def build_oracle() -> str:
+    """Compiles the CPU oracle (test infrastructure) with the same float contraction rules."""
+    src = os.path.join(REPO, "oracle", "jsb_oracle.cpp")
+    out = os.path.join(REPO, "oracle", "liboracle.so")
+    if _stale(out, [src]):
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", src, "-o", out],
+                       check=True)
+    return out
+
+
+def build_reference(ref: str = "/root/reference", jobs: int | None = None) -> bool:
+    """Builds oracle/_ref from the reference sources when they are present (never on the GPU hosts)."""
+    if not os.path.isdir(os.path.join(ref, "Jolt")) or shutil.which("make") is None:
+        return False
+    j = str(jobs or os.cpu_count() or 4)
+    subprocess.run(["make", "-f", os.path.join("oracle", "Makefile.ref"), f"REF={ref}", f"-j{j}"], cwd=REPO, check=True,
+                   stdout=subprocess.DEVNULL)
+    return True
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))
+    print(build_oracle())

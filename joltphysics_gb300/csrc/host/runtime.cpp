@@ -1,0 +1,971 @@
+// C ABI of the GPU soft-body solver (include/jsb.h): contexts, settings upload, bodies, stepping,
+// readback, CUDA graphs and the per-bucket launch-shape autotuner.
+//
+// Host-side flow for one step of all bodies (jsb_step):
+//   1. upload pending AddForce accumulators (one copy) when any body has one;
+//   2. zero the per-bucket work-queue counters;
+//   3. fork: one persistent launch of the solver kernel per body-size bucket, each on its own stream
+//      (buckets differ in threads per CTA and dynamic shared memory), joined back on the caller's stream;
+//   4. clear the device force array if it was non-zero.
+// The same sequence is recorded into a CUDA graph by jsb_step_graph.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../../include/jsb.h"
+#include "../kernels/device_types.h"
+#include "scene_io.h"
+#include "schedule.h"
+#include "shared_settings.h"
+
+namespace jsb {
+
+cudaError_t launch_step(const StepParams &p, int threads, uint32_t smem_vertices, uint32_t smem_faces, int grid,
+                        cudaStream_t stream);
+int step_occupancy(int threads, size_t smem);
+cudaError_t init_step_kernels(int max_dynamic_smem);
+cudaError_t launch_unpack_state(const float *pos3, const float *vel3, float4 *x, float4 *v, uint64_t n, int num_sms,
+                                cudaStream_t stream);
+cudaError_t launch_pack_state(const float4 *x, const float4 *v, float *pos3, float *vel3, uint64_t n, int num_sms,
+                              cudaStream_t stream);
+
+namespace {
+
+thread_local std::string g_last_error;
+
+jsb_status fail(jsb_status code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define JSB_CUDA(call)                                                                                      \
+    do {                                                                                                    \
+        cudaError_t e_ = (call);                                                                            \
+        if (e_ != cudaSuccess)                                                                              \
+            return fail(e_ == cudaErrorMemoryAllocation ? JSB_ERR_OUT_OF_MEMORY : JSB_ERR_CUDA,              \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                                \
+    } while (0)
+
+template <class T>
+struct DevBuf {
+    T *ptr = nullptr;
+    size_t count = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept : ptr(o.ptr), count(o.count) {
+        o.ptr = nullptr;
+        o.count = 0;
+    }
+    DevBuf &operator=(DevBuf &&o) noexcept {
+        if (this != &o) {
+            reset();
+            ptr = o.ptr;
+            count = o.count;
+            o.ptr = nullptr;
+            o.count = 0;
+        }
+        return *this;
+    }
+    ~DevBuf() { reset(); }
+    void reset() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        count = 0;
+    }
+    cudaError_t alloc(size_t n) {
+        reset();
+        if (n == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&ptr, n * sizeof(T));
+        if (e == cudaSuccess) count = n;
+        return e;
+    }
+    cudaError_t upload(const T *src, size_t n) {
+        cudaError_t e = alloc(n);
+        if (e != cudaSuccess || n == 0) return e;
+        return cudaMemcpy(ptr, src, n * sizeof(T), cudaMemcpyHostToDevice);
+    }
+};
+
+struct SettingsRec {
+    ParsedSettings parsed;
+    Schedule schedule;
+    std::vector<uint32_t> vf_off, vf;
+    DevBuf<uint4> levels, records, faces;
+    DevBuf<uint32_t> vf_off_dev, vf_dev;
+};
+
+struct BodyRec {
+    uint32_t settings_id;
+    jsb_creation_settings creation;
+    BodyState state;  // host copy, authoritative until the first upload
+    uint32_t vtx_offset = 0;
+};
+
+struct Bucket {
+    uint32_t max_vertices;
+    int threads;
+};
+
+struct LaunchGroup {  // bodies sharing one launch shape
+    int threads = 0;
+    uint32_t smem_vertices = 0, smem_faces = 0;
+    int grid = 0;
+    std::vector<uint32_t> bodies;
+    DevBuf<uint32_t> work;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+};
+
+}  // namespace
+}  // namespace jsb
+
+struct jsb_context {
+    int device = 0;
+    int num_sms = 0;
+    size_t max_smem_optin = 0;
+    float gravity[3] = {0.0f, -9.81f, 0.0f};
+    std::vector<std::unique_ptr<jsb::SettingsRec>> settings;
+    std::vector<jsb::BodyRec> bodies;
+    std::vector<jsb::ColliderDev> colliders;
+    std::vector<jsb::Bucket> buckets;
+    // device state
+    bool dirty = true;  // structure changed: device arrays must be rebuilt
+    uint64_t total_vertices = 0;
+    jsb::DevBuf<float4> x, v, prev, plane;
+    jsb::DevBuf<int32_t> shape;
+    jsb::DevBuf<jsb::BodyDesc> descs;
+    jsb::DevBuf<jsb::BodyState> states;
+    jsb::DevBuf<jsb::ColliderDev> colliders_dev;
+    jsb::DevBuf<uint32_t> queues;
+    jsb::DevBuf<uint32_t> error;
+    jsb::DevBuf<float> forces;  // per body: 3 floats consumed by the next step
+    jsb::DevBuf<float> step_forces;  // per body: 3 floats applied before every step
+    std::vector<float> step_force_host;
+    jsb::DevBuf<float> staging3;  // host round trip: positions then velocities, 3 floats per vertex
+    std::vector<float> pending_force;
+    float *pending_force_pinned = nullptr;
+    bool forces_pending = false;
+    std::vector<jsb::LaunchGroup> groups;
+    std::vector<uint32_t> single_work_host;
+    jsb::DevBuf<uint32_t> single_work;  // identity list for the plain form
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_steps = -1, graph_collision_steps = -1;
+    float graph_dt = -1.0f;
+    uint32_t last_launches = 0;
+    float last_kernel_ms = 0.0f;
+
+    ~jsb_context();
+};
+
+namespace jsb {
+namespace {
+
+void free_groups(jsb_context *ctx) {
+    for (auto &g : ctx->groups) {
+        if (g.stream) cudaStreamDestroy(g.stream);
+        if (g.done) cudaEventDestroy(g.done);
+    }
+    ctx->groups.clear();
+}
+
+void drop_graph(jsb_context *ctx) {
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    ctx->graph_exec = nullptr;
+    ctx->graph_steps = -1;
+}
+
+int threads_for(const jsb_context *ctx, uint32_t nv) {
+    for (const Bucket &b : ctx->buckets)
+        if (nv <= b.max_vertices) return b.threads;
+    return ctx->buckets.empty() ? 128 : ctx->buckets.back().threads;
+}
+
+BodyDesc make_desc(const jsb_context *ctx, const BodyRec &b) {
+    const SettingsRec &s = *ctx->settings[b.settings_id];
+    BodyDesc d;
+    d.levels = s.levels.ptr;
+    d.records = s.records.ptr;
+    d.faces = s.faces.ptr;
+    d.vf_off = s.vf_off_dev.ptr;
+    d.vf = s.vf_dev.ptr;
+    d.num_levels = s.schedule.num_levels;
+    d.num_records = s.schedule.num_records;
+    d.num_faces = uint32_t(s.parsed.faces.size());
+    d.num_vertices = uint32_t(s.parsed.vertices.size());
+    d.vtx_offset = b.vtx_offset;
+    d.num_iterations = b.creation.num_iterations;
+    d.linear_damping = b.creation.linear_damping;
+    d.max_linear_velocity = b.creation.max_linear_velocity;
+    d.restitution = b.creation.restitution;
+    d.friction = b.creation.friction;
+    d.pressure = b.creation.pressure;
+    d.gravity_factor = b.creation.gravity_factor;
+    d.vertex_radius = b.creation.vertex_radius;
+    d.flags = b.creation.update_position ? kFlagUpdatePosition : 0u;
+    return d;
+}
+
+// Dynamic shared memory a body needs on the single-CTA path.
+size_t smem_bytes(const SettingsRec &s, bool pressure) {
+    return s.parsed.vertices.size() * sizeof(float4) + (pressure ? s.parsed.faces.size() * sizeof(float) : 0);
+}
+
+double body_cost(const SettingsRec &s, const BodyRec &b, int threads) {
+    double levels = 0;
+    const auto &lv = s.schedule.levels;
+    for (uint32_t l = 0; l < s.schedule.num_levels; ++l) {
+        uint32_t w = lv[(l + 1) * 4] - lv[l * 4];
+        levels += double((w + threads - 1) / threads);
+    }
+    double per_vertex = double(s.parsed.vertices.size()) / threads;
+    return double(b.creation.num_iterations) * (levels + 4.0 * per_vertex);
+}
+
+// Rebuilds the device-side body tables and launch groups after structural changes.
+jsb_status rebuild(jsb_context *ctx) {
+    if (!ctx->dirty) return JSB_OK;
+    drop_graph(ctx);
+    free_groups(ctx);
+    // vertex layout
+    uint64_t total = 0;
+    for (BodyRec &b : ctx->bodies) {
+        b.vtx_offset = uint32_t(total);
+        total += ctx->settings[b.settings_id]->parsed.vertices.size();
+    }
+    if (total > 0xffffffffull) return fail(JSB_ERR_CAPACITY, "more than 2^32 vertices in one context");
+    // Keep existing device vertex state when only the tail grew (bodies are append-only).
+    std::vector<float4> hx(total), hv(total);
+    const uint64_t old_total = ctx->x.count;
+    if (old_total) {
+        JSB_CUDA(cudaMemcpy(hx.data(), ctx->x.ptr, old_total * sizeof(float4), cudaMemcpyDeviceToHost));
+        JSB_CUDA(cudaMemcpy(hv.data(), ctx->v.ptr, old_total * sizeof(float4), cudaMemcpyDeviceToHost));
+    }
+    std::vector<BodyState> hstate(ctx->bodies.size());
+    const size_t old_bodies = ctx->states.count;
+    if (old_bodies)
+        JSB_CUDA(cudaMemcpy(hstate.data(), ctx->states.ptr, old_bodies * sizeof(BodyState), cudaMemcpyDeviceToHost));
+    for (size_t bi = 0; bi < ctx->bodies.size(); ++bi) {
+        BodyRec &b = ctx->bodies[bi];
+        const ParsedSettings &ps = ctx->settings[b.settings_id]->parsed;
+        if (bi >= old_bodies) {
+            hstate[bi] = b.state;
+            for (size_t i = 0; i < ps.vertices.size(); ++i) {
+                const auto &sv = ps.vertices[i];
+                hx[b.vtx_offset + i] = make_float4(sv.pos[0], sv.pos[1], sv.pos[2], sv.inv_mass);
+                hv[b.vtx_offset + i] = make_float4(sv.vel[0], sv.vel[1], sv.vel[2], 0.0f);
+            }
+        }
+    }
+    JSB_CUDA(ctx->x.upload(hx.data(), total));
+    JSB_CUDA(ctx->v.upload(hv.data(), total));
+    JSB_CUDA(ctx->prev.alloc(total));
+    JSB_CUDA(ctx->plane.alloc(total));
+    JSB_CUDA(ctx->shape.alloc(total));
+    ctx->total_vertices = total;
+    std::vector<BodyDesc> descs;
+    for (const BodyRec &b : ctx->bodies) descs.push_back(make_desc(ctx, b));
+    JSB_CUDA(ctx->descs.upload(descs.data(), descs.size()));
+    JSB_CUDA(ctx->states.upload(hstate.data(), hstate.size()));
+    JSB_CUDA(ctx->colliders_dev.upload(ctx->colliders.data(), ctx->colliders.size()));
+    ctx->pending_force.resize(ctx->bodies.size() * 3, 0.0f);
+    if (ctx->pending_force_pinned) cudaFreeHost(ctx->pending_force_pinned);
+    ctx->pending_force_pinned = nullptr;
+    if (!ctx->bodies.empty()) JSB_CUDA(cudaMallocHost(&ctx->pending_force_pinned, ctx->bodies.size() * 3 * sizeof(float)));
+    JSB_CUDA(ctx->forces.alloc(ctx->bodies.size() * 3));
+    if (ctx->forces.count) JSB_CUDA(cudaMemset(ctx->forces.ptr, 0, ctx->forces.count * sizeof(float)));
+    ctx->step_force_host.resize(ctx->bodies.size() * 3, 0.0f);
+    JSB_CUDA(ctx->step_forces.upload(ctx->step_force_host.data(), ctx->step_force_host.size()));
+    ctx->single_work_host.resize(ctx->bodies.size());
+    for (size_t i = 0; i < ctx->bodies.size(); ++i) ctx->single_work_host[i] = uint32_t(i);
+    JSB_CUDA(ctx->single_work.upload(ctx->single_work_host.data(), ctx->single_work_host.size()));
+    if (!ctx->error.ptr) {
+        JSB_CUDA(ctx->error.alloc(1));
+        JSB_CUDA(cudaMemset(ctx->error.ptr, 0, sizeof(uint32_t)));
+    }
+
+    // launch groups: one per threads-per-CTA value
+    std::vector<int> shapes;
+    for (const BodyRec &b : ctx->bodies) {
+        int t = threads_for(ctx, uint32_t(ctx->settings[b.settings_id]->parsed.vertices.size()));
+        if (std::find(shapes.begin(), shapes.end(), t) == shapes.end()) shapes.push_back(t);
+    }
+    std::sort(shapes.begin(), shapes.end());
+    ctx->groups.resize(shapes.size());
+    for (size_t gi = 0; gi < shapes.size(); ++gi) {
+        LaunchGroup &g = ctx->groups[gi];
+        g.threads = shapes[gi];
+        std::vector<std::pair<double, uint32_t>> items;
+        for (size_t bi = 0; bi < ctx->bodies.size(); ++bi) {
+            const BodyRec &b = ctx->bodies[bi];
+            const SettingsRec &s = *ctx->settings[b.settings_id];
+            if (threads_for(ctx, uint32_t(s.parsed.vertices.size())) != g.threads) continue;
+            bool pressure = b.creation.pressure > 0.0f;
+            size_t need = smem_bytes(s, pressure);
+            if (need + 4096 > ctx->max_smem_optin)
+                return fail(JSB_ERR_UNSUPPORTED, "body " + std::to_string(bi) + " needs " + std::to_string(need) +
+                                                     " bytes of shared memory; the single-CTA solver path holds at most " +
+                                                     std::to_string(ctx->max_smem_optin - 4096));
+            g.smem_vertices = std::max(g.smem_vertices, uint32_t(s.parsed.vertices.size()));
+            if (pressure) g.smem_faces = std::max(g.smem_faces, uint32_t(s.parsed.faces.size()));
+            items.push_back({body_cost(s, b, g.threads), uint32_t(bi)});
+        }
+        // Longest-processing-time-first order for the work queue.
+        std::stable_sort(items.begin(), items.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
+        for (auto &it : items) g.bodies.push_back(it.second);
+        JSB_CUDA(g.work.upload(g.bodies.data(), g.bodies.size()));
+        size_t smem = size_t(g.smem_vertices) * sizeof(float4) + size_t(g.smem_faces) * sizeof(float);
+        int occ = step_occupancy(g.threads, smem);
+        if (occ <= 0) return fail(JSB_ERR_UNSUPPORTED, "solver kernel does not fit on an SM with this shared memory size");
+        g.grid = int(std::min<size_t>(g.bodies.size(), size_t(occ) * ctx->num_sms));
+        JSB_CUDA(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+        JSB_CUDA(cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming));
+    }
+    JSB_CUDA(ctx->queues.alloc(std::max<size_t>(ctx->groups.size(), 1)));
+    ctx->dirty = false;
+    return JSB_OK;
+}
+
+StepParams base_params(jsb_context *ctx, float dt) {
+    StepParams p;
+    p.bodies = ctx->descs.ptr;
+    p.states = ctx->states.ptr;
+    p.x = ctx->x.ptr;
+    p.v = ctx->v.ptr;
+    p.prev = ctx->prev.ptr;
+    p.plane = ctx->plane.ptr;
+    p.shape = ctx->shape.ptr;
+    p.colliders = ctx->colliders_dev.ptr;
+    p.num_colliders = uint32_t(ctx->colliders.size());
+    p.gravity[0] = ctx->gravity[0];
+    p.gravity[1] = ctx->gravity[1];
+    p.gravity[2] = ctx->gravity[2];
+    p.dt = dt;
+    p.error = ctx->error.ptr;
+    p.forces = ctx->forces.ptr;
+    p.step_forces = ctx->step_forces.ptr;
+    return p;
+}
+
+// Enqueues one batched step (all launch groups) on `stream`.
+jsb_status enqueue_batched(jsb_context *ctx, float dt, cudaStream_t stream, uint32_t &launches) {
+    if (ctx->groups.empty()) return JSB_OK;
+    JSB_CUDA(cudaMemsetAsync(ctx->queues.ptr, 0, ctx->queues.count * sizeof(uint32_t), stream));
+    JSB_CUDA(cudaEventRecord(ctx->fork, stream));
+    for (size_t gi = 0; gi < ctx->groups.size(); ++gi) {
+        LaunchGroup &g = ctx->groups[gi];
+        JSB_CUDA(cudaStreamWaitEvent(g.stream, ctx->fork, 0));
+        StepParams p = base_params(ctx, dt);
+        p.work = g.work.ptr;
+        p.num_work = uint32_t(g.bodies.size());
+        p.queue = ctx->queues.ptr + gi;
+        JSB_CUDA(launch_step(p, g.threads, g.smem_vertices, g.smem_faces, g.grid, g.stream));
+        ++launches;
+        JSB_CUDA(cudaEventRecord(g.done, g.stream));
+        JSB_CUDA(cudaStreamWaitEvent(stream, g.done, 0));
+    }
+    return JSB_OK;
+}
+
+jsb_status upload_forces(jsb_context *ctx, cudaStream_t stream, bool &uploaded) {
+    uploaded = false;
+    if (!ctx->forces_pending) return JSB_OK;
+    memcpy(ctx->pending_force_pinned, ctx->pending_force.data(), ctx->pending_force.size() * sizeof(float));
+    JSB_CUDA(cudaMemcpyAsync(ctx->forces.ptr, ctx->pending_force_pinned, ctx->pending_force.size() * sizeof(float),
+                             cudaMemcpyHostToDevice, stream));
+    std::fill(ctx->pending_force.begin(), ctx->pending_force.end(), 0.0f);
+    ctx->forces_pending = false;
+    uploaded = true;
+    return JSB_OK;
+}
+
+jsb_status step_impl(jsb_context *ctx, float dt, int collision_steps, cudaStream_t stream, bool plain, uint32_t &launches) {
+    if (!(dt > 0.0f) || collision_steps < 1) return fail(JSB_ERR_INVALID_ARGUMENT, "dt must be > 0 and collision_steps >= 1");
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    const float step_dt = dt / float(collision_steps);
+    for (int c = 0; c < collision_steps; ++c) {
+        bool uploaded = false;
+        if ((st = upload_forces(ctx, stream, uploaded)) != JSB_OK) return st;
+        if (plain) {
+            // One launch per body, one CTA each, on the caller's stream.
+            for (size_t gi = 0; gi < ctx->groups.size(); ++gi) {
+                LaunchGroup &g = ctx->groups[gi];
+                for (uint32_t b : g.bodies) {
+                    JSB_CUDA(cudaMemsetAsync(ctx->queues.ptr, 0, sizeof(uint32_t), stream));
+                    StepParams p = base_params(ctx, step_dt);
+                    p.work = ctx->single_work.ptr + b;
+                    p.num_work = 1;
+                    p.queue = ctx->queues.ptr;
+                    const SettingsRec &s = *ctx->settings[ctx->bodies[b].settings_id];
+                    bool pressure = ctx->bodies[b].creation.pressure > 0.0f;
+                    JSB_CUDA(launch_step(p, g.threads, uint32_t(s.parsed.vertices.size()),
+                                         pressure ? uint32_t(s.parsed.faces.size()) : 0u, 1, stream));
+                    ++launches;
+                }
+            }
+        } else if ((st = enqueue_batched(ctx, step_dt, stream, launches)) != JSB_OK)
+            return st;
+        if (uploaded) JSB_CUDA(cudaMemsetAsync(ctx->forces.ptr, 0, ctx->forces.count * sizeof(float), stream));
+    }
+    return JSB_OK;
+}
+
+jsb_context *check_ctx(jsb_context *ctx) {
+    if (!ctx) g_last_error = "null context";
+    return ctx;
+}
+
+}  // namespace
+}  // namespace jsb
+
+jsb_context::~jsb_context() {
+    jsb::drop_graph(this);
+    jsb::free_groups(this);
+    if (fork) cudaEventDestroy(fork);
+    if (t0) cudaEventDestroy(t0);
+    if (t1) cudaEventDestroy(t1);
+    if (pending_force_pinned) cudaFreeHost(pending_force_pinned);
+}
+
+using namespace jsb;
+
+extern "C" {
+
+const char *jsb_last_error_string(void) { return g_last_error.c_str(); }
+const char *jsb_version(void) { return "jsb 0.1 (sm_103a)"; }
+
+jsb_status jsb_context_create(int device, jsb_context **out) {
+    if (!out) return fail(JSB_ERR_INVALID_ARGUMENT, "null output pointer");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) return fail(JSB_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    if (device < 0 || device >= count) return fail(JSB_ERR_INVALID_ARGUMENT, "device index out of range");
+    JSB_CUDA(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    JSB_CUDA(cudaGetDeviceProperties(&prop, device));
+    auto ctx = std::make_unique<jsb_context>();
+    ctx->device = device;
+    ctx->num_sms = prop.multiProcessorCount;
+    ctx->max_smem_optin = prop.sharedMemPerBlockOptin;
+    ctx->buckets = {{512, 32}, {2048, 64}, {65536, 128}};
+    // static shared memory of the solver kernel is under 4 KB
+    JSB_CUDA(init_step_kernels(int(ctx->max_smem_optin) - 4096));
+    JSB_CUDA(cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming));
+    JSB_CUDA(cudaEventCreate(&ctx->t0));
+    JSB_CUDA(cudaEventCreate(&ctx->t1));
+    *out = ctx.release();
+    return JSB_OK;
+}
+
+jsb_status jsb_context_destroy(jsb_context *ctx) {
+    if (!ctx) return fail(JSB_ERR_INVALID_ARGUMENT, "null context");
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    delete ctx;
+    return JSB_OK;
+}
+
+jsb_status jsb_set_gravity(jsb_context *ctx, const float gravity[3]) {
+    if (!check_ctx(ctx) || !gravity) return fail(JSB_ERR_INVALID_ARGUMENT, "null argument");
+    memcpy(ctx->gravity, gravity, sizeof(ctx->gravity));
+    drop_graph(ctx);
+    return JSB_OK;
+}
+
+jsb_status jsb_settings_upload(jsb_context *ctx, const void *blob, size_t len, uint32_t *settings_id) {
+    if (!check_ctx(ctx) || !settings_id) return fail(JSB_ERR_INVALID_ARGUMENT, "null argument");
+    auto rec = std::make_unique<SettingsRec>();
+    bool unsupported = false;
+    std::string err = parse_settings(blob, len, rec->parsed, unsupported);
+    if (!err.empty()) return fail(unsupported ? JSB_ERR_UNSUPPORTED : JSB_ERR_BLOB, err);
+    rec->schedule = build_schedule(rec->parsed);
+    const ParsedSettings &ps = rec->parsed;
+    const size_t nv = ps.vertices.size();
+    rec->vf_off.assign(nv + 1, 0);
+    for (const auto &f : ps.faces)
+        for (int k = 0; k < 3; ++k) rec->vf_off[f.v[k] + 1]++;
+    for (size_t i = 0; i < nv; ++i) rec->vf_off[i + 1] += rec->vf_off[i];
+    rec->vf.resize(rec->vf_off[nv]);
+    std::vector<uint32_t> fill(rec->vf_off.begin(), rec->vf_off.end() - 1);
+    for (size_t fi = 0; fi < ps.faces.size(); ++fi)
+        for (int k = 0; k < 3; ++k) rec->vf[fill[ps.faces[fi].v[k]]++] = uint32_t(fi);
+    std::vector<uint4> faces(ps.faces.size());
+    for (size_t fi = 0; fi < ps.faces.size(); ++fi) faces[fi] = make_uint4(ps.faces[fi].v[0], ps.faces[fi].v[1], ps.faces[fi].v[2], 0);
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    JSB_CUDA(rec->levels.upload(reinterpret_cast<const uint4 *>(rec->schedule.levels.data()), rec->schedule.levels.size() / 4));
+    JSB_CUDA(rec->records.upload(reinterpret_cast<const uint4 *>(rec->schedule.records.data()), rec->schedule.records.size() / 4));
+    JSB_CUDA(rec->faces.upload(faces.data(), faces.size()));
+    JSB_CUDA(rec->vf_off_dev.upload(rec->vf_off.data(), rec->vf_off.size()));
+    JSB_CUDA(rec->vf_dev.upload(rec->vf.data(), rec->vf.size()));
+    ctx->settings.push_back(std::move(rec));
+    *settings_id = uint32_t(ctx->settings.size() - 1);
+    return JSB_OK;
+}
+
+jsb_status jsb_body_add(jsb_context *ctx, uint32_t settings_id, const jsb_creation_settings *creation, const float position[3],
+                        uint32_t *body_id) {
+    if (!check_ctx(ctx) || !creation || !position || !body_id) return fail(JSB_ERR_INVALID_ARGUMENT, "null argument");
+    if (settings_id >= ctx->settings.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "unknown settings id");
+    if (creation->num_iterations < 1) return fail(JSB_ERR_INVALID_ARGUMENT, "num_iterations must be >= 1");
+    if (!creation->make_rotation_identity)
+        return fail(JSB_ERR_UNSUPPORTED, "bodies must keep an identity rotation (mMakeRotationIdentity = true)");
+    BodyRec b;
+    b.settings_id = settings_id;
+    b.creation = *creation;
+    memset(&b.state, 0, sizeof(b.state));
+    for (int k = 0; k < 3; ++k) b.state.position[k] = position[k];
+    // SoftBodyMotionProperties::Initialize: local bounds of the initial vertices, predicted = local.
+    const ParsedSettings &ps = ctx->settings[settings_id]->parsed;
+    for (int k = 0; k < 3; ++k) {
+        b.state.bmin[k] = FLT_MAX;
+        b.state.bmax[k] = -FLT_MAX;
+    }
+    for (const auto &v : ps.vertices)
+        for (int k = 0; k < 3; ++k) {
+            b.state.bmin[k] = b.state.bmin[k] < v.pos[k] ? b.state.bmin[k] : v.pos[k];
+            b.state.bmax[k] = b.state.bmax[k] > v.pos[k] ? b.state.bmax[k] : v.pos[k];
+        }
+    for (int k = 0; k < 3; ++k) {
+        b.state.pmin[k] = b.state.bmin[k];
+        b.state.pmax[k] = b.state.bmax[k];
+    }
+    ctx->bodies.push_back(b);
+    ctx->dirty = true;
+    *body_id = uint32_t(ctx->bodies.size() - 1);
+    return JSB_OK;
+}
+
+jsb_status jsb_collider_add(jsb_context *ctx, const jsb_collider *c, uint32_t *collider_id) {
+    if (!check_ctx(ctx) || !c || !collider_id) return fail(JSB_ERR_INVALID_ARGUMENT, "null argument");
+    if (c->type != JSB_COLLIDER_BOX && c->type != JSB_COLLIDER_SPHERE) return fail(JSB_ERR_INVALID_ARGUMENT, "unknown collider type");
+    ColliderDev d;
+    d.type = c->type;
+    for (int k = 0; k < 3; ++k) {
+        d.position[k] = c->position[k];
+        d.half_extent[k] = c->half_extent[k];
+    }
+    d.radius = c->radius;
+    d.friction = c->friction;
+    d.restitution = c->restitution;
+    ctx->colliders.push_back(d);
+    ctx->dirty = true;
+    *collider_id = uint32_t(ctx->colliders.size() - 1);
+    return JSB_OK;
+}
+
+jsb_status jsb_body_num_vertices(jsb_context *ctx, uint32_t body_id, uint32_t *n) {
+    if (!check_ctx(ctx) || !n || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    *n = uint32_t(ctx->settings[ctx->bodies[body_id].settings_id]->parsed.vertices.size());
+    return JSB_OK;
+}
+
+jsb_status jsb_body_add_force(jsb_context *ctx, uint32_t body_id, const float force[3]) {
+    if (!check_ctx(ctx) || !force || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    for (int k = 0; k < 3; ++k) ctx->pending_force[body_id * 3 + k] += force[k];
+    ctx->forces_pending = true;
+    return JSB_OK;
+}
+
+jsb_status jsb_body_set_step_force(jsb_context *ctx, uint32_t body_id, const float force[3]) {
+    if (!check_ctx(ctx) || !force || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    for (int k = 0; k < 3; ++k) ctx->step_force_host[body_id * 3 + k] = force[k];
+    JSB_CUDA(cudaMemcpy(ctx->step_forces.ptr + body_id * 3, force, 3 * sizeof(float), cudaMemcpyHostToDevice));
+    return JSB_OK;
+}
+
+jsb_status jsb_step(jsb_context *ctx, float dt, int collision_steps, jsb_stream stream) {
+    if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    uint32_t launches = 0;
+    jsb_status st = step_impl(ctx, dt, collision_steps, reinterpret_cast<cudaStream_t>(stream), false, launches);
+    ctx->last_launches = launches;
+    return st;
+}
+
+jsb_status jsb_step_plain(jsb_context *ctx, float dt, int collision_steps, jsb_stream stream) {
+    if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    uint32_t launches = 0;
+    jsb_status st = step_impl(ctx, dt, collision_steps, reinterpret_cast<cudaStream_t>(stream), true, launches);
+    ctx->last_launches = launches;
+    return st;
+}
+
+jsb_status jsb_step_graph(jsb_context *ctx, float dt, int collision_steps, int num_steps, int repeats, jsb_stream stream_) {
+    if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
+    if (num_steps < 1 || repeats < 0) return fail(JSB_ERR_INVALID_ARGUMENT, "num_steps must be >= 1, repeats >= 0");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    if (ctx->forces_pending)
+        return fail(JSB_ERR_INVALID_ARGUMENT, "pending AddForce: forces are consumed per step; use jsb_step for forced steps");
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
+    uint32_t launches = 0;
+    if (!ctx->graph_exec || ctx->graph_steps != num_steps || ctx->graph_dt != dt || ctx->graph_collision_steps != collision_steps) {
+        drop_graph(ctx);
+        cudaStream_t cap;
+        JSB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            cudaStreamDestroy(cap);
+            return fail(JSB_ERR_CUDA, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(e));
+        }
+        const float step_dt = dt / float(collision_steps);
+        for (int s = 0; s < num_steps && st == JSB_OK; ++s)
+            for (int c = 0; c < collision_steps && st == JSB_OK; ++c) st = enqueue_batched(ctx, step_dt, cap, launches);
+        e = cudaStreamEndCapture(cap, &graph);
+        cudaStreamDestroy(cap);
+        if (st != JSB_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return st;
+        }
+        if (e != cudaSuccess) return fail(JSB_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(JSB_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        ctx->graph_steps = num_steps;
+        ctx->graph_dt = dt;
+        ctx->graph_collision_steps = collision_steps;
+    } else {
+        launches = uint32_t(ctx->groups.size()) * uint32_t(num_steps) * uint32_t(collision_steps);
+    }
+    JSB_CUDA(cudaEventRecord(ctx->t0, stream));
+    for (int r = 0; r < repeats; ++r) JSB_CUDA(cudaGraphLaunch(ctx->graph_exec, stream));
+    JSB_CUDA(cudaEventRecord(ctx->t1, stream));
+    ctx->last_launches = launches * uint32_t(repeats);
+    ctx->last_kernel_ms = -1.0f;
+    if (repeats > 0) {
+        JSB_CUDA(cudaEventSynchronize(ctx->t1));
+        float ms = 0.0f;
+        JSB_CUDA(cudaEventElapsedTime(&ms, ctx->t0, ctx->t1));
+        ctx->last_kernel_ms = ms / float(repeats * num_steps);
+    }
+    return JSB_OK;
+}
+
+jsb_status jsb_synchronize(jsb_context *ctx) {
+    if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    JSB_CUDA(cudaDeviceSynchronize());
+    if (ctx->error.ptr) {
+        uint32_t err = 0;
+        JSB_CUDA(cudaMemcpy(&err, ctx->error.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        if (err) {
+            JSB_CUDA(cudaMemset(ctx->error.ptr, 0, sizeof(uint32_t)));
+            if (err & kErrTimeout) return fail(JSB_ERR_TIMEOUT, "a bounded device wait gave up");
+            if (err & kErrNonFinite) return fail(JSB_ERR_NONFINITE, "non-finite vertex position or velocity");
+            if (err & kErrShapeOverflow)
+                return fail(JSB_ERR_CAPACITY, "more than " + std::to_string(kMaxCollidingShapes) + " colliding shapes for one body");
+        }
+    }
+    return JSB_OK;
+}
+
+jsb_status jsb_body_read(jsb_context *ctx, uint32_t body_id, float position[3], float *local_positions, float *velocities) {
+    if (!check_ctx(ctx) || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    JSB_CUDA(cudaDeviceSynchronize());
+    const BodyRec &b = ctx->bodies[body_id];
+    const size_t nv = ctx->settings[b.settings_id]->parsed.vertices.size();
+    if (position) {
+        BodyState s;
+        JSB_CUDA(cudaMemcpy(&s, ctx->states.ptr + body_id, sizeof(BodyState), cudaMemcpyDeviceToHost));
+        memcpy(position, s.position, 3 * sizeof(float));
+    }
+    std::vector<float4> tmp(nv);
+    if (local_positions) {
+        JSB_CUDA(cudaMemcpy(tmp.data(), ctx->x.ptr + b.vtx_offset, nv * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < nv; ++i) {
+            local_positions[3 * i + 0] = tmp[i].x;
+            local_positions[3 * i + 1] = tmp[i].y;
+            local_positions[3 * i + 2] = tmp[i].z;
+        }
+    }
+    if (velocities) {
+        JSB_CUDA(cudaMemcpy(tmp.data(), ctx->v.ptr + b.vtx_offset, nv * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < nv; ++i) {
+            velocities[3 * i + 0] = tmp[i].x;
+            velocities[3 * i + 1] = tmp[i].y;
+            velocities[3 * i + 2] = tmp[i].z;
+        }
+    }
+    return JSB_OK;
+}
+
+// SoftBodyMotionProperties::SaveState layout (single precision, no rods/skin):
+//   MotionProperties::SaveState (Jolt/Physics/Body/MotionProperties.cpp:63-76): linear velocity (12),
+//   angular velocity (12), force (12), torque (12), 3 sleep test spheres (48), sleep timer (4),
+//   allow sleeping (1) = 101 bytes; then per vertex position (12) + velocity (12); then local bounds
+//   and predicted bounds (4 x 12).
+static constexpr size_t kMotionHeader = 101;
+
+jsb_status jsb_body_save_state(jsb_context *ctx, uint32_t body_id, void *state, size_t capacity, size_t *len) {
+    if (!check_ctx(ctx) || !len || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    const BodyRec &b = ctx->bodies[body_id];
+    const size_t nv = ctx->settings[b.settings_id]->parsed.vertices.size();
+    const size_t need = kMotionHeader + nv * 24 + 48;
+    *len = need;
+    if (!state) return JSB_OK;
+    if (capacity < need) return fail(JSB_ERR_INVALID_ARGUMENT, "state buffer too small");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    JSB_CUDA(cudaDeviceSynchronize());
+    BodyState s;
+    JSB_CUDA(cudaMemcpy(&s, ctx->states.ptr + body_id, sizeof(BodyState), cudaMemcpyDeviceToHost));
+    std::vector<float4> hx(nv), hv(nv);
+    JSB_CUDA(cudaMemcpy(hx.data(), ctx->x.ptr + b.vtx_offset, nv * sizeof(float4), cudaMemcpyDeviceToHost));
+    JSB_CUDA(cudaMemcpy(hv.data(), ctx->v.ptr + b.vtx_offset, nv * sizeof(float4), cudaMemcpyDeviceToHost));
+    uint8_t *o = static_cast<uint8_t *>(state);
+    memset(o, 0, kMotionHeader);
+    memcpy(o + 0, s.lin_vel, 12);
+    memcpy(o + 12, s.ang_vel, 12);
+    o[100] = b.creation.allow_sleeping;
+    uint8_t *p = o + kMotionHeader;
+    for (size_t i = 0; i < nv; ++i) {
+        float pv[6] = {hx[i].x, hx[i].y, hx[i].z, hv[i].x, hv[i].y, hv[i].z};
+        memcpy(p, pv, 24);
+        p += 24;
+    }
+    memcpy(p, s.bmin, 12);
+    memcpy(p + 12, s.bmax, 12);
+    memcpy(p + 24, s.pmin, 12);
+    memcpy(p + 36, s.pmax, 12);
+    return JSB_OK;
+}
+
+jsb_status jsb_body_restore_state(jsb_context *ctx, uint32_t body_id, const void *state, size_t len, const float position[3]) {
+    if (!check_ctx(ctx) || !state || !position || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    const BodyRec &b = ctx->bodies[body_id];
+    const ParsedSettings &ps = ctx->settings[b.settings_id]->parsed;
+    const size_t nv = ps.vertices.size();
+    if (len != kMotionHeader + nv * 24 + 48) return fail(JSB_ERR_BLOB, "state size does not match the body's vertex count");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    JSB_CUDA(cudaDeviceSynchronize());
+    const uint8_t *in = static_cast<const uint8_t *>(state);
+    BodyState s;
+    JSB_CUDA(cudaMemcpy(&s, ctx->states.ptr + body_id, sizeof(BodyState), cudaMemcpyDeviceToHost));
+    memcpy(s.lin_vel, in + 0, 12);
+    memcpy(s.ang_vel, in + 12, 12);
+    memcpy(s.position, position, 12);
+    std::vector<float4> hx(nv), hv(nv);
+    const uint8_t *p = in + kMotionHeader;
+    for (size_t i = 0; i < nv; ++i) {
+        float pv[6];
+        memcpy(pv, p, 24);
+        p += 24;
+        hx[i] = make_float4(pv[0], pv[1], pv[2], ps.vertices[i].inv_mass);
+        hv[i] = make_float4(pv[3], pv[4], pv[5], 0.0f);
+    }
+    memcpy(s.bmin, p, 12);
+    memcpy(s.bmax, p + 12, 12);
+    memcpy(s.pmin, p + 24, 12);
+    memcpy(s.pmax, p + 36, 12);
+    JSB_CUDA(cudaMemcpy(ctx->x.ptr + b.vtx_offset, hx.data(), nv * sizeof(float4), cudaMemcpyHostToDevice));
+    JSB_CUDA(cudaMemcpy(ctx->v.ptr + b.vtx_offset, hv.data(), nv * sizeof(float4), cudaMemcpyHostToDevice));
+    JSB_CUDA(cudaMemcpy(ctx->states.ptr + body_id, &s, sizeof(BodyState), cudaMemcpyHostToDevice));
+    return JSB_OK;
+}
+
+jsb_status jsb_total_vertices(jsb_context *ctx, uint64_t *total) {
+    if (!check_ctx(ctx) || !total) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    uint64_t t = 0;
+    for (const BodyRec &b : ctx->bodies) t += ctx->settings[b.settings_id]->parsed.vertices.size();
+    *total = t;
+    return JSB_OK;
+}
+
+jsb_status jsb_state_upload_all(jsb_context *ctx, const float *local_positions, const float *velocities, jsb_stream stream_) {
+    if (!check_ctx(ctx) || !local_positions || !velocities) return fail(JSB_ERR_INVALID_ARGUMENT, "null argument");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
+    const uint64_t n = ctx->total_vertices;
+    if (ctx->staging3.count < 6 * n) JSB_CUDA(ctx->staging3.alloc(6 * n));
+    JSB_CUDA(cudaMemcpyAsync(ctx->staging3.ptr, local_positions, 3 * n * sizeof(float), cudaMemcpyHostToDevice, stream));
+    JSB_CUDA(cudaMemcpyAsync(ctx->staging3.ptr + 3 * n, velocities, 3 * n * sizeof(float), cudaMemcpyHostToDevice, stream));
+    JSB_CUDA(launch_unpack_state(ctx->staging3.ptr, ctx->staging3.ptr + 3 * n, ctx->x.ptr, ctx->v.ptr, n, ctx->num_sms, stream));
+    return JSB_OK;
+}
+
+jsb_status jsb_state_download_all(jsb_context *ctx, float *local_positions, float *velocities, jsb_stream stream_) {
+    if (!check_ctx(ctx) || !local_positions || !velocities) return fail(JSB_ERR_INVALID_ARGUMENT, "null argument");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
+    const uint64_t n = ctx->total_vertices;
+    if (ctx->staging3.count < 6 * n) JSB_CUDA(ctx->staging3.alloc(6 * n));
+    JSB_CUDA(launch_pack_state(ctx->x.ptr, ctx->v.ptr, ctx->staging3.ptr, ctx->staging3.ptr + 3 * n, n, ctx->num_sms, stream));
+    JSB_CUDA(cudaMemcpyAsync(local_positions, ctx->staging3.ptr, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, stream));
+    JSB_CUDA(cudaMemcpyAsync(velocities, ctx->staging3.ptr + 3 * n, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, stream));
+    return JSB_OK;
+}
+
+jsb_status jsb_body_schedule_info(jsb_context *ctx, uint32_t body_id, uint32_t *num_levels, uint32_t *num_constraints) {
+    if (!check_ctx(ctx) || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    const Schedule &s = ctx->settings[ctx->bodies[body_id].settings_id]->schedule;
+    if (num_levels) *num_levels = s.num_levels;
+    if (num_constraints) *num_constraints = s.num_records;
+    return JSB_OK;
+}
+
+jsb_status jsb_settings_schedule(const void *blob, size_t len, uint32_t *num_levels, uint32_t *num_records, uint32_t *levels,
+                                 uint32_t *records, uint32_t *source) {
+    if (!num_levels || !num_records) return fail(JSB_ERR_INVALID_ARGUMENT, "null argument");
+    ParsedSettings ps;
+    bool unsupported = false;
+    std::string err = parse_settings(blob, len, ps, unsupported);
+    if (!err.empty()) return fail(unsupported ? JSB_ERR_UNSUPPORTED : JSB_ERR_BLOB, err);
+    Schedule s = build_schedule(ps);
+    *num_levels = s.num_levels;
+    *num_records = s.num_records;
+    if (levels) memcpy(levels, s.levels.data(), s.levels.size() * sizeof(uint32_t));
+    if (records) memcpy(records, s.records.data(), s.records.size() * sizeof(uint32_t));
+    if (source) memcpy(source, s.source.data(), s.source.size() * sizeof(uint32_t));
+    return JSB_OK;
+}
+
+jsb_status jsb_set_bucket_threads(jsb_context *ctx, uint32_t max_vertices, uint32_t threads) {
+    if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
+    if (threads != 32 && threads != 64 && threads != 128 && threads != 256)
+        return fail(JSB_ERR_INVALID_ARGUMENT, "threads must be 32, 64, 128 or 256");
+    bool found = false;
+    for (Bucket &b : ctx->buckets)
+        if (b.max_vertices == max_vertices) {
+            b.threads = int(threads);
+            found = true;
+        }
+    if (!found) ctx->buckets.push_back({max_vertices, int(threads)});
+    std::sort(ctx->buckets.begin(), ctx->buckets.end(), [](const Bucket &a, const Bucket &b) { return a.max_vertices < b.max_vertices; });
+    ctx->dirty = true;
+    return JSB_OK;
+}
+
+jsb_status jsb_last_launch_count(jsb_context *ctx, uint32_t *launches) {
+    if (!check_ctx(ctx) || !launches) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    *launches = ctx->last_launches;
+    return JSB_OK;
+}
+
+jsb_status jsb_last_kernel_ms(jsb_context *ctx, float *ms) {
+    if (!check_ctx(ctx) || !ms) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    *ms = ctx->last_kernel_ms;
+    return JSB_OK;
+}
+
+// Autotuner: for every bucket, time one batched step of only that bucket's bodies with each
+// threads-per-CTA choice and keep the fastest. Device state is saved before and restored after.
+jsb_status jsb_autotune(jsb_context *ctx, float dt, int trials) {
+    if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
+    if (trials < 1) trials = 1;
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    const uint64_t n = ctx->total_vertices;
+    DevBuf<float4> sx, sv;
+    DevBuf<BodyState> ss;
+    JSB_CUDA(sx.alloc(n));
+    JSB_CUDA(sv.alloc(n));
+    JSB_CUDA(ss.alloc(ctx->bodies.size()));
+    JSB_CUDA(cudaMemcpy(sx.ptr, ctx->x.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice));
+    JSB_CUDA(cudaMemcpy(sv.ptr, ctx->v.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice));
+    JSB_CUDA(cudaMemcpy(ss.ptr, ctx->states.ptr, ctx->bodies.size() * sizeof(BodyState), cudaMemcpyDeviceToDevice));
+    std::vector<Bucket> tuned = ctx->buckets;
+    const int choices[4] = {32, 64, 128, 256};
+    for (size_t bi = 0; bi < tuned.size(); ++bi) {
+        uint32_t lo = bi == 0 ? 0 : tuned[bi - 1].max_vertices;
+        uint32_t hi = tuned[bi].max_vertices;
+        std::vector<uint32_t> members;
+        uint32_t max_nv = 0, max_faces = 0;
+        for (size_t b = 0; b < ctx->bodies.size(); ++b) {
+            const SettingsRec &s = *ctx->settings[ctx->bodies[b].settings_id];
+            uint32_t nv = uint32_t(s.parsed.vertices.size());
+            if (nv > lo && nv <= hi) {
+                members.push_back(uint32_t(b));
+                max_nv = std::max(max_nv, nv);
+                if (ctx->bodies[b].creation.pressure > 0.0f) max_faces = std::max(max_faces, uint32_t(s.parsed.faces.size()));
+            }
+        }
+        if (members.empty()) continue;
+        DevBuf<uint32_t> work;
+        JSB_CUDA(work.upload(members.data(), members.size()));
+        float best_ms = 1e30f;
+        int best = tuned[bi].threads;
+        for (int t : choices) {
+            size_t smem = size_t(max_nv) * sizeof(float4) + size_t(max_faces) * sizeof(float);
+            int occ = step_occupancy(t, smem);
+            if (occ <= 0) continue;
+            int grid = int(std::min<size_t>(members.size(), size_t(occ) * ctx->num_sms));
+            StepParams p = base_params(ctx, dt);
+            p.work = work.ptr;
+            p.num_work = uint32_t(members.size());
+            p.queue = ctx->queues.ptr;
+            float total = 0.0f;
+            for (int k = 0; k < trials + 1; ++k) {
+                JSB_CUDA(cudaMemset(ctx->queues.ptr, 0, sizeof(uint32_t)));
+                JSB_CUDA(cudaEventRecord(ctx->t0, 0));
+                JSB_CUDA(launch_step(p, t, max_nv, max_faces, grid, 0));
+                JSB_CUDA(cudaEventRecord(ctx->t1, 0));
+                JSB_CUDA(cudaEventSynchronize(ctx->t1));
+                float ms = 0;
+                JSB_CUDA(cudaEventElapsedTime(&ms, ctx->t0, ctx->t1));
+                if (k > 0) total += ms;  // first launch is warm-up
+            }
+            if (total < best_ms) {
+                best_ms = total;
+                best = t;
+            }
+        }
+        tuned[bi].threads = best;
+    }
+    JSB_CUDA(cudaMemcpy(ctx->x.ptr, sx.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice));
+    JSB_CUDA(cudaMemcpy(ctx->v.ptr, sv.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice));
+    JSB_CUDA(cudaMemcpy(ctx->states.ptr, ss.ptr, ctx->bodies.size() * sizeof(BodyState), cudaMemcpyDeviceToDevice));
+    JSB_CUDA(cudaMemset(ctx->error.ptr, 0, sizeof(uint32_t)));
+    ctx->buckets = tuned;
+    ctx->dirty = true;
+    return rebuild(ctx);
+}
+
+jsb_status jsb_scene_build(const char *name, const char *params, void *out, size_t capacity, size_t *len) {
+    if (!name || !len) return fail(JSB_ERR_INVALID_ARGUMENT, "null argument");
+    scene::SceneSpec spec;
+    try {
+        if (!scene::make_named_scene(name, params ? params : "", spec)) return fail(JSB_ERR_INVALID_ARGUMENT, std::string("unknown scene ") + name);
+        std::string bytes = scene::serialize_scene(spec, [](const scene::MeshSpec &m) { return host::build_settings(m).SaveBinaryState(); });
+        *len = bytes.size();
+        if (!out) return JSB_OK;
+        if (capacity < bytes.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "output buffer too small");
+        memcpy(out, bytes.data(), bytes.size());
+    } catch (const std::exception &e) {
+        return fail(JSB_ERR_INVALID_ARGUMENT, std::string("scene build failed: ") + e.what());
+    }
+    return JSB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,206 @@
+// Settings parsing and dependency-level scheduling (see schedule.h).
+
+#include "schedule.h"
+
+#include <algorithm>
+#include <cstring>
+
+namespace jsb {
+
+namespace {
+
+class ByteReader {
+public:
+    ByteReader(const uint8_t *p, size_t n) : p_(p), n_(n) {}
+    bool u32(uint32_t &v) { return bytes(&v, 4); }
+    bool bytes(void *dst, size_t k) {
+        if (k > n_ - off_) return false;
+        memcpy(dst, p_ + off_, k);
+        off_ += k;
+        return true;
+    }
+    template <class T>
+    bool array(std::vector<T> &out, size_t elem) {
+        uint32_t count;
+        if (!u32(count)) return false;
+        if (uint64_t(count) * elem > n_ - off_) return false;
+        out.resize(count);
+        if (count) memcpy(out.data(), p_ + off_, size_t(count) * elem);
+        off_ += size_t(count) * elem;
+        return true;
+    }
+    bool skip_array(size_t elem, uint32_t &count) {
+        if (!u32(count)) return false;
+        if (uint64_t(count) * elem > n_ - off_) return false;
+        off_ += size_t(count) * elem;
+        return true;
+    }
+    size_t remaining() const { return n_ - off_; }
+
+private:
+    const uint8_t *p_;
+    size_t n_, off_ = 0;
+};
+
+}  // namespace
+
+std::string parse_settings(const void *blob, size_t len, ParsedSettings &s, bool &unsupported) {
+    static_assert(sizeof(ParsedSettings::Vertex) == 28 && sizeof(ParsedSettings::Face) == 16 &&
+                      sizeof(ParsedSettings::Edge) == 16 && sizeof(ParsedSettings::Bend) == 24 &&
+                      sizeof(ParsedSettings::Volume) == 24 && sizeof(ParsedSettings::LRA) == 12 &&
+                      sizeof(ParsedSettings::Group) == 28,
+                  "SaveBinaryState element sizes");
+    unsupported = false;
+    if (!blob) return "null settings blob";
+    ByteReader r(static_cast<const uint8_t *>(blob), len);
+    uint32_t skinned_normals = 0;
+    if (!(r.array(s.vertices, 28) && r.array(s.faces, 16) && r.array(s.edges, 16) && r.array(s.bends, 24) &&
+          r.array(s.volumes, 24) && r.skip_array(52, s.num_skinned) && r.skip_array(4, skinned_normals) && r.array(s.lras, 12) &&
+          r.array(s.groups, 28) && r.skip_array(36, s.num_rod_stretch_shear) && r.skip_array(28, s.num_rod_bend_twist) &&
+          r.skip_array(68, s.num_inv_bind)))
+        return "truncated settings blob";
+    if (r.remaining() != 0) return "trailing bytes after settings blob";
+    const uint32_t nv = uint32_t(s.vertices.size());
+    if (s.groups.empty()) return "settings have no update groups (SoftBodySharedSettings::Optimize was not called)";
+    auto bad = [nv](const uint32_t *v, int k) {
+        for (int i = 0; i < k; ++i)
+            if (v[i] >= nv) return true;
+        return false;
+    };
+    for (auto &f : s.faces)
+        if (bad(f.v, 3)) return "face vertex index out of range";
+    for (auto &e : s.edges)
+        if (bad(e.v, 2)) return "edge vertex index out of range";
+    for (auto &b : s.bends)
+        if (bad(b.v, 4)) return "dihedral bend vertex index out of range";
+    for (auto &v : s.volumes)
+        if (bad(v.v, 4)) return "volume vertex index out of range";
+    for (auto &l : s.lras)
+        if (bad(l.v, 2)) return "LRA vertex index out of range";
+    ParsedSettings::Group prev{0, 0, 0, 0, 0, 0, 0};
+    for (auto &g : s.groups) {
+        if (g.edge < prev.edge || g.lra < prev.lra || g.bend < prev.bend || g.volume < prev.volume || g.rod_ss < prev.rod_ss ||
+            g.rod_bt < prev.rod_bt || g.skinned < prev.skinned)
+            return "update group end indices decrease";
+        prev = g;
+    }
+    if (prev.edge != s.edges.size() || prev.lra != s.lras.size() || prev.bend != s.bends.size() ||
+        prev.volume != s.volumes.size() || prev.rod_ss != s.num_rod_stretch_shear || prev.rod_bt != s.num_rod_bend_twist ||
+        prev.skinned != s.num_skinned)
+        return "update groups do not cover all constraints";
+    if (s.num_skinned || s.num_rod_stretch_shear || s.num_rod_bend_twist) {
+        unsupported = true;
+        return "skinned constraints and Cosserat rods are not supported by the GPU solver";
+    }
+    if (nv > 65536) {
+        unsupported = true;
+        return "bodies with more than 65536 vertices are not supported";
+    }
+    return std::string();
+}
+
+Schedule build_schedule(const ParsedSettings &s) {
+    const uint32_t nv = uint32_t(s.vertices.size());
+    std::vector<int32_t> last_write(nv, -1), last_read(nv, -1);
+    struct Item {
+        uint32_t level, type, index;
+    };
+    std::vector<Item> items;
+    items.reserve(s.edges.size() + s.bends.size() + s.volumes.size() + s.lras.size());
+    uint32_t max_level = 0;
+    auto place_rw = [&](const uint32_t *v, int k, uint32_t type, uint32_t index) {
+        int32_t lvl = 0;
+        for (int i = 0; i < k; ++i) lvl = std::max(lvl, std::max(last_write[v[i]], last_read[v[i]]) + 1);
+        for (int i = 0; i < k; ++i) last_write[v[i]] = lvl;
+        items.push_back({uint32_t(lvl), type, index});
+        max_level = std::max(max_level, uint32_t(lvl));
+    };
+    ParsedSettings::Group start{0, 0, 0, 0, 0, 0, 0};
+    for (size_t g = 0; g < s.groups.size(); ++g) {
+        const ParsedSettings::Group &p = g > 0 ? s.groups[g - 1] : start;
+        const ParsedSettings::Group &c = s.groups[g];
+        for (uint32_t i = p.volume; i < c.volume; ++i) place_rw(s.volumes[i].v, 4, kVolume, i);
+        for (uint32_t i = p.bend; i < c.bend; ++i) place_rw(s.bends[i].v, 4, kBend, i);
+        for (uint32_t i = p.edge; i < c.edge; ++i) place_rw(s.edges[i].v, 2, kEdge, i);
+        for (uint32_t i = p.lra; i < c.lra; ++i) {
+            uint32_t a = s.lras[i].v[0], b = s.lras[i].v[1];
+            int32_t lvl = std::max(last_write[a] + 1, std::max(last_write[b], last_read[b]) + 1);
+            if (a == b) lvl = std::max(lvl, last_read[a] + 1);
+            last_read[a] = std::max(last_read[a], lvl);
+            last_write[b] = lvl;
+            items.push_back({uint32_t(lvl), kLRA, i});
+            max_level = std::max(max_level, uint32_t(lvl));
+        }
+    }
+    Schedule out;
+    const uint32_t n = uint32_t(items.size());
+    out.num_records = n;
+    out.num_levels = n ? max_level + 1 : 0;
+    // counting sort by (level, type), stable in sequence order
+    const uint32_t nb = out.num_levels * 4;
+    std::vector<uint32_t> count(nb + 1, 0);
+    for (const Item &it : items) count[it.level * 4 + it.type + 1]++;
+    for (uint32_t k = 0; k < nb; ++k) count[k + 1] += count[k];
+    std::vector<uint32_t> bucket_start(count.begin(), count.end());
+    std::vector<uint32_t> order(n);
+    for (uint32_t k = 0; k < n; ++k) order[count[items[k].level * 4 + items[k].type]++] = k;
+    out.levels.resize(size_t(out.num_levels + 2) * 4);
+    for (uint32_t l = 0; l < out.num_levels; ++l) {
+        out.levels[l * 4 + 0] = bucket_start[l * 4 + 0];
+        out.levels[l * 4 + 1] = bucket_start[l * 4 + 1];
+        out.levels[l * 4 + 2] = bucket_start[l * 4 + 2];
+        out.levels[l * 4 + 3] = bucket_start[l * 4 + 3];
+        out.max_level_width = std::max(out.max_level_width, bucket_start[l * 4 + 4] - bucket_start[l * 4]);
+    }
+    for (uint32_t l = out.num_levels; l < out.num_levels + 2; ++l)
+        for (int k = 0; k < 4; ++k) out.levels[l * 4 + k] = n;
+    out.records.resize(size_t(n) * 4);
+    out.source.resize(n);
+    auto fbits = [](float f) {
+        uint32_t u;
+        memcpy(&u, &f, 4);
+        return u;
+    };
+    for (uint32_t k = 0; k < n; ++k) {
+        const Item &it = items[order[k]];
+        uint32_t *r = &out.records[size_t(k) * 4];
+        switch (it.type) {
+            case kBend: {
+                const auto &b = s.bends[it.index];
+                r[0] = b.v[0] | (b.v[1] << 16);
+                r[1] = b.v[2] | (b.v[3] << 16);
+                r[2] = fbits(b.compliance);
+                r[3] = fbits(b.initial_angle);
+                break;
+            }
+            case kVolume: {
+                const auto &v = s.volumes[it.index];
+                r[0] = v.v[0] | (v.v[1] << 16);
+                r[1] = v.v[2] | (v.v[3] << 16);
+                r[2] = fbits(v.six_rest_volume);
+                r[3] = fbits(v.compliance);
+                break;
+            }
+            case kEdge: {
+                const auto &e = s.edges[it.index];
+                r[0] = e.v[0] | (e.v[1] << 16);
+                r[1] = 0;
+                r[2] = fbits(e.rest);
+                r[3] = fbits(e.compliance);
+                break;
+            }
+            default: {
+                const auto &l = s.lras[it.index];
+                r[0] = l.v[0] | (l.v[1] << 16);
+                r[1] = 0;
+                r[2] = fbits(l.max_distance);
+                r[3] = 0;
+                break;
+            }
+        }
+        out.source[k] = (it.type << 28) | it.index;
+    }
+    return out;
+}
+
+}  // namespace jsb

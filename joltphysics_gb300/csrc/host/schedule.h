@@ -1,0 +1,75 @@
+// Settings parsing and the dependency-level schedule.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace jsb {
+
+// Parsed SoftBodySharedSettings::SaveBinaryState bytes (SoftBodySharedSettings.cpp:1203-1236).
+struct ParsedSettings {
+    struct Vertex {
+        float pos[3], vel[3], inv_mass;
+    };
+    struct Face {
+        uint32_t v[3], material;
+    };
+    struct Edge {
+        uint32_t v[2];
+        float rest, compliance;
+    };
+    struct Bend {
+        uint32_t v[4];
+        float compliance, initial_angle;
+    };
+    struct Volume {
+        uint32_t v[4];
+        float six_rest_volume, compliance;
+    };
+    struct LRA {
+        uint32_t v[2];
+        float max_distance;
+    };
+    struct Group {
+        uint32_t edge, lra, rod_ss, rod_bt, bend, volume, skinned;
+    };
+    std::vector<Vertex> vertices;
+    std::vector<Face> faces;
+    std::vector<Edge> edges;
+    std::vector<Bend> bends;
+    std::vector<Volume> volumes;
+    std::vector<LRA> lras;
+    std::vector<Group> groups;
+    uint32_t num_skinned = 0, num_rod_stretch_shear = 0, num_rod_bend_twist = 0, num_inv_bind = 0;
+};
+
+// Returns an empty string on success, else a description of the problem. `unsupported` is set when
+// the bytes are well formed but use constraint types the GPU path does not implement.
+std::string parse_settings(const void *blob, size_t len, ParsedSettings &out, bool &unsupported);
+
+// Constraint type order inside one dependency level (matches the level descriptor fields).
+enum RecordType : uint32_t { kBend = 0, kVolume = 1, kEdge = 2, kLRA = 3 };
+
+struct Schedule {
+    // levels[l] = {first record, end of bends, end of volumes, end of edges}; levels has
+    // num_levels + 2 entries, the last two being sentinels {n, n, n, n}.
+    std::vector<uint32_t> levels;  // 4 per entry
+    std::vector<uint32_t> records;  // 4 per record
+    std::vector<uint32_t> source;  // per record: type << 28 | index in the settings' array
+    uint32_t num_levels = 0;
+    uint32_t num_records = 0;
+    uint32_t max_level_width = 0;
+};
+
+// Builds the dependency-level schedule of one substep's constraint projection.
+//
+// Sequence: the update groups in order (parallel groups first, the non-parallel group last), and in
+// each group volumes, dihedral bends, edges, LRA (ProcessGroup, SoftBodyMotionProperties.cpp:1030-1055).
+// Level of a constraint = 1 + the latest level that wrote one of its vertices, and for vertices it
+// writes also 1 + the latest level that read them (LRA constraints only read their anchor vertex).
+// Constraints of one level therefore touch disjoint written vertices, so any execution order inside a
+// level reproduces the sequential result bit for bit.
+Schedule build_schedule(const ParsedSettings &s);
+
+}  // namespace jsb

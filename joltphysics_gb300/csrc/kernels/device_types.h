@@ -1,0 +1,104 @@
+// Data layout shared by the host runtime and the CUDA kernels.
+//
+// HBM layout of one context:
+//   vertex state, SoA over all bodies (body b owns [vtx_offset, vtx_offset + num_vertices)):
+//     x      float4  position (local to the body) in xyz, inverse mass in w
+//     v      float4  velocity in xyz
+//   per-step scratch, same indexing:
+//     prev   float4  position before the current substep's integration
+//     plane  float4  collision plane (normal xyz, constant w), relative to the body
+//     shape  int32   index into the body's colliding-shape list, -1 = none
+//   per settings object (shared by all bodies created from it):
+//     levels  uint4[num_levels + 2]  {first record, end of bends, end of volumes, end of edges};
+//                                    the LRA records of level l end where level l + 1 starts
+//     records uint4[num_records]     16-byte constraint records in dependency-level order
+//     faces   uint4[num_faces]       {v0, v1, v2, 0} (pressure only)
+//     vf_off  uint32[num_vertices+1] incident faces of each vertex, ascending (pressure only)
+//     vf      uint32[...]
+// Constraint records (vertex indices are 16-bit, local to the body):
+//   bend   {v0 | v1 << 16, v2 | v3 << 16, compliance, initial angle}
+//   volume {v0 | v1 << 16, v2 | v3 << 16, six rest volume, compliance}
+//   edge   {v0 | v1 << 16, 0, rest length, compliance}
+//   LRA    {v0 | v1 << 16, 0, max distance, 0}
+#pragma once
+
+#include <stdint.h>
+#include <vector_types.h>
+
+#if defined(__CUDACC__)
+#define JSB_HD __host__ __device__
+#else
+#define JSB_HD
+#endif
+
+namespace jsb {
+
+constexpr uint32_t kMaxVerticesPerBody = 65536;
+constexpr uint32_t kMaxCollidingShapes = 16;  // colliding shapes kept per body per step
+
+enum : uint32_t { kFlagUpdatePosition = 1u };
+
+// Device error word bits.
+enum : uint32_t { kErrNonFinite = 1u, kErrShapeOverflow = 2u, kErrTimeout = 4u };
+
+struct BodyDesc {
+    // shared settings
+    const uint4 *levels;
+    const uint4 *records;
+    const uint4 *faces;
+    const uint32_t *vf_off;
+    const uint32_t *vf;
+    uint32_t num_levels;
+    uint32_t num_records;
+    uint32_t num_faces;
+    uint32_t num_vertices;
+    // body
+    uint32_t vtx_offset;
+    uint32_t num_iterations;
+    float linear_damping;
+    float max_linear_velocity;
+    float restitution;
+    float friction;
+    float pressure;
+    float gravity_factor;
+    float vertex_radius;
+    uint32_t flags;
+};
+
+struct BodyState {
+    float position[3];  // body position in world space
+    float bmin[3], bmax[3];  // local bounds
+    float pmin[3], pmax[3];  // local predicted bounds
+    float lin_vel[3], ang_vel[3];
+};
+
+struct ColliderDev {
+    int32_t type;  // 0 box, 1 sphere
+    float position[3];
+    float half_extent[3];
+    float radius;
+    float friction;
+    float restitution;
+};
+
+struct StepParams {
+    const BodyDesc *bodies;
+    BodyState *states;
+    const uint32_t *work;  // body indices, most expensive first
+    uint32_t num_work;
+    uint32_t *queue;  // work queue counter (zeroed before each launch)
+    float4 *x;
+    float4 *v;
+    float4 *prev;
+    float4 *plane;
+    int32_t *shape;
+    const ColliderDev *colliders;
+    uint32_t num_colliders;
+    float gravity[3];
+    float dt;
+    uint32_t *error;
+    const float *forces;  // 3 floats per body: AddForce accumulators consumed by this step
+    const float *step_forces;  // 3 floats per body: force added before every step (persistent)
+};
+
+}  // namespace jsb

@@ -1,0 +1,684 @@
+// Soft-body solver step on sm_103a: one CTA advances one body through one full step
+// (Jolt/Physics/SoftBody/SoftBodyMotionProperties.cpp: InitializeUpdateContext :937-960,
+// DetermineCollidingShapes :120-255, DetermineCollisionPlanes :257-265, N x {ApplyPressure :291-323,
+// IntegratePositions :325-365, ParallelApplyConstraints :1057-1115, ApplyCollisionConstraintsAndUpdate-
+// Velocities :700-825}, UpdateSoftBodyState :827-921) and PhysicsSystem.cpp:2864 (body position).
+//
+// The body's positions (+ inverse mass) live in shared memory for the whole step. Constraint
+// projection walks a dependency-level schedule built on the host from the update groups and their
+// in-group order: constraints in one level touch disjoint vertices (LRA anchors are read-only), so
+// projecting a level's constraints concurrently and barrier-separating levels gives the bitwise result
+// of the reference's sequential Gauss-Seidel walk. No atomics are involved in the projection.
+//
+// Bitwise parity with the reference (built with JPH_CROSS_PLATFORM_DETERMINISTIC) needs the
+// reference's float operation order: this file is compiled with --fmad=false and IEEE division and
+// square root, and the helpers below evaluate Vec3 dot products as (x*x' + y*y') + (z*z' + 0)
+// (Jolt/Math/Vec3.inl:896-934), cross products with separately rounded products (:855-895) and
+// negation as 0 - x (:669-700).
+//
+// Persistent launch: the grid holds as many CTAs as fit; each CTA pulls body indices from a work
+// queue (an atomic counter over a list sorted by estimated cost, largest first) until it is empty.
+
+#include <cuda_runtime.h>
+#include <float.h>
+#include <stdint.h>
+
+#include "device_types.h"
+
+namespace jsb {
+namespace {
+
+struct f3 {
+    float x, y, z;
+};
+__device__ __forceinline__ f3 mk(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ f3 xyz(float4 a) { return {a.x, a.y, a.z}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator*(float s, f3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ f3 operator/(f3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ f3 neg(f3 a) { return {0.0f - a.x, 0.0f - a.y, 0.0f - a.z}; }
+__device__ __forceinline__ float dot(f3 a, f3 b) {
+    float px = a.x * b.x, py = a.y * b.y, pz = a.z * b.z;
+    return (px + py) + (pz + 0.0f);
+}
+__device__ __forceinline__ f3 cross(f3 a, f3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ float len_sq(f3 a) { return dot(a, a); }
+__device__ __forceinline__ float len(f3 a) { return sqrtf(len_sq(a)); }
+__device__ __forceinline__ f3 vmin(f3 a, f3 b) { return {a.x < b.x ? a.x : b.x, a.y < b.y ? a.y : b.y, a.z < b.z ? a.z : b.z}; }
+__device__ __forceinline__ f3 vmax(f3 a, f3 b) { return {a.x > b.x ? a.x : b.x, a.y > b.y ? a.y : b.y, a.z > b.z ? a.z : b.z}; }
+__device__ __forceinline__ f3 ld3(const float *p) { return {p[0], p[1], p[2]}; }
+__device__ __forceinline__ void st3(float *p, f3 a) {
+    p[0] = a.x;
+    p[1] = a.y;
+    p[2] = a.z;
+}
+__device__ __forceinline__ float4 with_w(f3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+
+constexpr float kPi = 3.14159265358979323846f;
+
+// Jolt/Math/Trigonometry.h:48-65
+__device__ __forceinline__ float acos_approximate(float x) {
+    float ax = fabsf(x);
+    ax = ax > 1.0f ? 1.0f : ax;
+    float val = sqrtf(1.0f - ax) * (kPi / 2 - 0.175394f * ax);
+    return x < 0.0f ? kPi - val : val;
+}
+
+template <int T>
+__device__ __forceinline__ void cta_sync() {
+    if (T <= 32)
+        __syncwarp();
+    else
+        __syncthreads();
+}
+
+struct SCol {  // one colliding shape, relative to the soft body
+    int32_t type;
+    float t[3];
+    float h[3];
+    float r;
+    float friction;
+    float restitution;
+};
+
+struct Shared {
+    SCol cols[kMaxCollidingShapes];
+    int ncols;
+    uint32_t item;
+    float six_volume;
+    float red[32][4];  // per-warp partials for reductions
+    int redi[32][4];
+};
+
+// ---------------------------------------------------------------------------------------------
+// Constraint projections (exact reference arithmetic)
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ void project_bend(float4 *sx, uint4 r, float inv_dt_sq) {  // :367-456
+    uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16, i2 = r.y & 0xffff, i3 = r.y >> 16;
+    float compliance = __uint_as_float(r.z), initial_angle = __uint_as_float(r.w);
+    float4 p0 = sx[i0], p1 = sx[i1], p2 = sx[i2], p3 = sx[i3];
+    f3 x0 = xyz(p0), x1 = xyz(p1), x2 = xyz(p2), x3 = xyz(p3);
+    f3 e = x1 - x0;
+    float e_len = len(e);
+    if (e_len < 1.0e-6f) return;
+    f3 x1x2 = x2 - x1, x1x3 = x3 - x1;
+    f3 n1 = cross(x2 - x0, x1x2);
+    f3 n2 = cross(x1x3, x3 - x0);
+    float n1_len_sq = len_sq(n1), n2_len_sq = len_sq(n2);
+    float n1n2 = n1_len_sq * n2_len_sq;
+    if (n1n2 < 1.0e-24f) return;
+    float sign = dot(cross(n2, n1), e) < 0.0f ? -1.0f : 1.0f;
+    float d = dot(n1, n2) / sqrtf(n1n2);
+    float c = sign * acos_approximate(d) - initial_angle;
+    if (c > kPi)
+        c -= 2.0f * kPi;
+    else if (c < -kPi)
+        c += 2.0f * kPi;
+    n1 = n1 / n1_len_sq;
+    n2 = n2 / n2_len_sq;
+    f3 d0c = (dot(x1x2, e) * n1 + dot(x1x3, e) * n2) / e_len;
+    f3 d2c = e_len * n1;
+    f3 d3c = e_len * n2;
+    f3 d1c = (neg(d0c) - d2c) - d3c;
+    float w0 = p0.w, w1 = p1.w, w2 = p2.w, w3 = p3.w;
+    float denom = w0 * len_sq(d0c) + w1 * len_sq(d1c) + w2 * len_sq(d2c) + w3 * len_sq(d3c) + compliance * inv_dt_sq;
+    if (denom < 1.0e-12f) return;
+    float ml = c / denom;
+    sx[i0] = with_w(x0 - (ml * w0) * d0c, w0);
+    sx[i1] = with_w(x1 - (ml * w1) * d1c, w1);
+    sx[i2] = with_w(x2 - (ml * w2) * d2c, w2);
+    sx[i3] = with_w(x3 - (ml * w3) * d3c, w3);
+}
+
+__device__ __forceinline__ void project_volume(float4 *sx, uint4 r, float inv_dt_sq) {  // :458-507
+    uint32_t i1 = r.x & 0xffff, i2 = r.x >> 16, i3 = r.y & 0xffff, i4 = r.y >> 16;
+    float six_rest = __uint_as_float(r.z), compliance = __uint_as_float(r.w);
+    float4 p1 = sx[i1], p2 = sx[i2], p3 = sx[i3], p4 = sx[i4];
+    f3 x1 = xyz(p1), x2 = xyz(p2), x3 = xyz(p3), x4 = xyz(p4);
+    f3 x1x2 = x2 - x1, x1x3 = x3 - x1, x1x4 = x4 - x1;
+    float c = fabsf(dot(cross(x1x2, x1x3), x1x4)) - six_rest;
+    f3 d1c = cross(x4 - x2, x3 - x2);
+    f3 d2c = cross(x1x3, x1x4);
+    f3 d3c = cross(x1x4, x1x2);
+    f3 d4c = cross(x1x2, x1x3);
+    float w1 = p1.w, w2 = p2.w, w3 = p3.w, w4 = p4.w;
+    float denom = w1 * len_sq(d1c) + w2 * len_sq(d2c) + w3 * len_sq(d3c) + w4 * len_sq(d4c) + compliance * inv_dt_sq;
+    if (denom < 1.0e-12f) return;
+    float ml = c / denom;
+    sx[i1] = with_w(x1 - (ml * w1) * d1c, w1);
+    sx[i2] = with_w(x2 - (ml * w2) * d2c, w2);
+    sx[i3] = with_w(x3 - (ml * w3) * d3c, w3);
+    sx[i4] = with_w(x4 - (ml * w4) * d4c, w4);
+}
+
+__device__ __forceinline__ void project_edge(float4 *sx, uint4 r, float inv_dt_sq) {  // :573-601
+    uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16;
+    float rest = __uint_as_float(r.z), compliance = __uint_as_float(r.w);
+    float4 p0 = sx[i0], p1 = sx[i1];
+    f3 x0 = xyz(p0), x1 = xyz(p1);
+    f3 delta = x1 - x0;
+    float length = len(delta);
+    float denom = length * (p0.w + p1.w + compliance * inv_dt_sq);
+    if (denom < 1.0e-12f) return;
+    f3 corr = (delta * (length - rest)) / denom;
+    sx[i0] = with_w(x0 + p0.w * corr, p0.w);
+    sx[i1] = with_w(x1 - p1.w * corr, p1.w);
+}
+
+__device__ __forceinline__ void project_lra(float4 *sx, uint4 r) {  // :679-698
+    uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16;
+    float md = __uint_as_float(r.z);
+    f3 x0 = xyz(sx[i0]);
+    float4 p1 = sx[i1];
+    f3 delta = xyz(p1) - x0;
+    float dls = len_sq(delta);
+    if (dls > md * md) sx[i1] = with_w(x0 + (delta * md) / sqrtf(dls), p1.w);
+}
+
+__device__ __forceinline__ void project(float4 *sx, uint4 r, uint32_t c, uint4 lv, float inv_dt_sq) {
+    if (c < lv.y)
+        project_bend(sx, r, inv_dt_sq);
+    else if (c < lv.z)
+        project_volume(sx, r, inv_dt_sq);
+    else if (c < lv.w)
+        project_edge(sx, r, inv_dt_sq);
+    else
+        project_lra(sx, r);
+}
+
+// Walks the dependency levels of one substep. Software pipelined: the next level's descriptor and
+// this thread's first record of it are loaded before the current level is projected.
+template <int T>
+__device__ __forceinline__ void apply_levels(float4 *sx, const BodyDesc &d, float inv_dt_sq) {
+    const uint4 *__restrict__ levels = d.levels;
+    const uint4 *__restrict__ rec = d.records;
+    const uint32_t tid = threadIdx.x;
+    const uint32_t L = d.num_levels;
+    if (L == 0) return;
+    uint4 l0 = __ldg(levels + 0);
+    uint4 l1 = __ldg(levels + 1);
+    uint4 r = make_uint4(0, 0, 0, 0);
+    if (l0.x + tid < l1.x) r = __ldg(rec + l0.x + tid);
+    for (uint32_t l = 0; l < L; ++l) {
+        uint4 l2 = __ldg(levels + l + 2);  // levels has num_levels + 2 entries
+        uint4 nr = make_uint4(0, 0, 0, 0);
+        if (l1.x + tid < l2.x) nr = __ldg(rec + l1.x + tid);
+        uint32_t c = l0.x + tid;
+        if (c < l1.x) {
+            project(sx, r, c, l0, inv_dt_sq);
+            for (c += T; c < l1.x; c += T) project(sx, __ldg(rec + c), c, l0, inv_dt_sq);
+        }
+        cta_sync<T>();
+        l0 = l1;
+        l1 = l2;
+        r = nr;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Collision shapes
+// ---------------------------------------------------------------------------------------------
+// Plane::sFromPointAndNormal(point, normal).GetTransformed(translation t), identity rotation.
+__device__ __forceinline__ float4 plane_transformed(f3 normal, f3 point, f3 t) {
+    float c = -dot(normal, point);
+    f3 n2;
+    n2.x = (1.0f * normal.x + 0.0f * normal.y) + 0.0f * normal.z;
+    n2.y = (0.0f * normal.x + 1.0f * normal.y) + 0.0f * normal.z;
+    n2.z = (0.0f * normal.x + 0.0f * normal.y) + 1.0f * normal.z;
+    return make_float4(n2.x, n2.y, n2.z, c - dot(t, n2));
+}
+
+// BoxShape::CollideSoftBodyVertices (BoxShape.cpp:234-283) for one vertex.
+__device__ __forceinline__ void collide_box(f3 p, const SCol &s, int idx, float &largest, float4 &plane, int &shape) {
+    f3 t = ld3(s.t), h = ld3(s.h);
+    f3 local = p + neg(t);
+    f3 clamped = vmax(vmin(local, h), neg(h));
+    if (clamped.x == local.x && clamped.y == local.y && clamped.z == local.z) {
+        f3 delta = h - mk(fabsf(local.x), fabsf(local.y), fabsf(local.z));
+        int index = delta.x < delta.y ? (delta.z < delta.x ? 2 : 0) : (delta.z < delta.y ? 2 : 1);
+        float pen = index == 0 ? delta.x : (index == 1 ? delta.y : delta.z);
+        if (largest >= pen) return;
+        largest = pen;
+        f3 sgn = mk(signbit(local.x) ? -1.0f : 1.0f, signbit(local.y) ? -1.0f : 1.0f, signbit(local.z) ? -1.0f : 1.0f);
+        f3 axis = mk(index == 0 ? 1.0f : 0.0f, index == 1 ? 1.0f : 0.0f, index == 2 ? 1.0f : 0.0f);
+        f3 normal = mk(sgn.x * axis.x, sgn.y * axis.y, sgn.z * axis.z);
+        f3 point = mk(normal.x * h.x, normal.y * h.y, normal.z * h.z);
+        plane = plane_transformed(normal, point, t);
+        shape = idx;
+    } else {
+        f3 normal = local - clamped;
+        float nl = len(normal);
+        float pen = -nl;
+        if (largest >= pen) return;
+        largest = pen;
+        normal = normal / nl;
+        plane = plane_transformed(normal, clamped, t);
+        shape = idx;
+    }
+}
+
+// SphereShape::CollideSoftBodyVertices (SphereShape.cpp:279-300) for one vertex.
+__device__ __forceinline__ void collide_sphere(f3 p, const SCol &s, int idx, float &largest, float4 &plane, int &shape) {
+    f3 center = ld3(s.t);
+    f3 delta = p - center;
+    float distance = len(delta);
+    float pen = s.r - distance;
+    if (largest >= pen) return;
+    largest = pen;
+    f3 normal = distance > 0.0f ? delta / distance : mk(0.0f, 1.0f, 0.0f);
+    f3 point = center + s.r * normal;
+    plane = make_float4(normal.x, normal.y, normal.z, -dot(normal, point));
+    shape = idx;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Reductions for UpdateSoftBodyState
+// ---------------------------------------------------------------------------------------------
+// Sequential AABox::Encapsulate keeps, among equal extreme values, the last vertex in index order
+// (mMin = mMin < p ? mMin : p). Reducing (value, index) pairs with "strictly better, else larger
+// index" reproduces that choice (it matters only for the sign of zero).
+__device__ __forceinline__ void pick_min(float &v, int &i, float ov, int oi) {
+    if (ov < v || (!(v < ov) && oi > i)) {
+        v = ov;
+        i = oi;
+    }
+}
+__device__ __forceinline__ void pick_max(float &v, int &i, float ov, int oi) {
+    if (ov > v || (!(v > ov) && oi > i)) {
+        v = ov;
+        i = oi;
+    }
+}
+
+template <int T>
+__device__ __forceinline__ void reduce_minmax4(Shared &sh, float v[4], int idx[4], const bool is_max[4]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        for (int off = 16; off > 0; off >>= 1) {
+            float ov = __shfl_down_sync(0xffffffffu, v[k], off);
+            int oi = __shfl_down_sync(0xffffffffu, idx[k], off);
+            if (is_max[k])
+                pick_max(v[k], idx[k], ov, oi);
+            else
+                pick_min(v[k], idx[k], ov, oi);
+        }
+    }
+    if (T > 32) {
+        if (lane == 0)
+            for (int k = 0; k < 4; ++k) {
+                sh.red[warp][k] = v[k];
+                sh.redi[warp][k] = idx[k];
+            }
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int w = 1; w < T / 32; ++w)
+                for (int k = 0; k < 4; ++k) {
+                    if (is_max[k])
+                        pick_max(v[k], idx[k], sh.red[w][k], sh.redi[w][k]);
+                    else
+                        pick_min(v[k], idx[k], sh.red[w][k], sh.redi[w][k]);
+                }
+        __syncthreads();
+    }
+}
+
+template <int T>
+__device__ __forceinline__ float reduce_sum(Shared &sh, float v, int slot) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (T > 32) {
+        if (lane == 0) sh.red[warp][slot] = v;
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int w = 1; w < T / 32; ++w) v += sh.red[w][slot];
+        __syncthreads();
+    }
+    return v;  // valid in thread 0
+}
+
+// ---------------------------------------------------------------------------------------------
+// One body, one step
+// ---------------------------------------------------------------------------------------------
+template <int T>
+__device__ void step_body(const StepParams &p, uint32_t b, float4 *sx, Shared &sh, float *s_face) {
+    const uint32_t tid = threadIdx.x;
+    const BodyDesc d = p.bodies[b];
+    BodyState *st = p.states + b;
+    const uint32_t nv = d.num_vertices;
+    float4 *gx = p.x + d.vtx_offset;
+    float4 *gv = p.v + d.vtx_offset;
+    float4 *gprev = p.prev + d.vtx_offset;
+    float4 *gplane = p.plane + d.vtx_offset;
+    int32_t *gshape = p.shape + d.vtx_offset;
+
+    // InitializeUpdateContext (identity body rotation)
+    const f3 g = d.gravity_factor * ld3(p.gravity);
+    const uint32_t n_it = d.num_iterations;
+    const float dt = p.dt;
+    const float dt_sub = dt / float(n_it);
+    float disp_scale = 0.5f * float(n_it);
+    disp_scale = disp_scale * float(n_it + 1);
+    disp_scale = disp_scale * (dt_sub * dt_sub);
+    const f3 disp_g = disp_scale * g;
+    const f3 body_pos = ld3(st->position);
+    const f3 force = ld3(p.forces + 3 * size_t(b)) + ld3(p.step_forces + 3 * size_t(b));
+
+    // DetermineCollidingShapes: world AABB of (bounds U predicted bounds) grown by the vertex radius
+    if (tid == 0) {
+        f3 lmin = vmin(ld3(st->bmin), ld3(st->pmin)), lmax = vmax(ld3(st->bmax), ld3(st->pmax));
+        f3 r3 = mk(d.vertex_radius, d.vertex_radius, d.vertex_radius);
+        lmin = lmin - r3;
+        lmax = lmax + r3;
+        f3 wmin = body_pos + lmin, wmax = body_pos + lmax;
+        int n = 0;
+        for (uint32_t ci = 0; ci < p.num_colliders; ++ci) {
+            const ColliderDev c = p.colliders[ci];
+            f3 cp = ld3(c.position);
+            f3 ext = c.type == 0 ? ld3(c.half_extent) : mk(c.radius, c.radius, c.radius);
+            f3 cmin = cp + neg(ext), cmax = cp + ext;
+            bool overlap = !(wmin.x > cmax.x || wmin.y > cmax.y || wmin.z > cmax.z || wmax.x < cmin.x || wmax.y < cmin.y ||
+                             wmax.z < cmin.z);
+            if (!overlap) continue;
+            if (n == int(kMaxCollidingShapes)) {
+                atomicOr(p.error, kErrShapeOverflow);
+                break;
+            }
+            SCol &s = sh.cols[n++];
+            s.type = c.type;
+            st3(s.t, cp - body_pos);
+            st3(s.h, ld3(c.half_extent));
+            s.r = c.radius;
+            s.friction = sqrtf(d.friction * c.friction);
+            s.restitution = d.restitution > c.restitution ? d.restitution : c.restitution;
+        }
+        sh.ncols = n;
+    }
+    // Stage positions in shared memory.
+    for (uint32_t i = tid; i < nv; i += T) sx[i] = gx[i];
+    __syncthreads();
+
+    // DetermineCollisionPlanes
+    const int ncols = sh.ncols;
+    for (uint32_t i = tid; i < nv; i += T) {
+        float4 pi = sx[i];
+        int shape = -1;
+        float4 plane = make_float4(0, 0, 0, 0);
+        if (pi.w > 0.0f && ncols > 0) {
+            float largest = -FLT_MAX;
+            for (int s = 0; s < ncols; ++s) {
+                if (sh.cols[s].type == 0)
+                    collide_box(xyz(pi), sh.cols[s], s, largest, plane, shape);
+                else
+                    collide_sphere(xyz(pi), sh.cols[s], s, largest, plane, shape);
+            }
+        }
+        gshape[i] = shape;
+        if (shape >= 0) gplane[i] = plane;
+    }
+
+    const float inv_dt_sq = 1.0f / (dt_sub * dt_sub);
+    float damp = 1.0f - d.linear_damping * dt_sub;
+    damp = damp < 0.0f ? 0.0f : damp;
+    const f3 sub_g = g * dt_sub;
+    const float nvf = float(nv > 0 ? nv : 1);
+    const f3 sub_imp = (force * dt_sub) / nvf;
+    const float restitution_threshold = -2.0f * len(g) * dt_sub;
+    const bool has_pressure = d.pressure > 0.0f && d.num_faces > 0;
+
+    for (uint32_t it = 0; it < n_it; ++it) {
+        // ApplyPressure
+        if (has_pressure) {
+            for (uint32_t f = tid; f < d.num_faces; f += T) {
+                uint4 fc = __ldg(d.faces + f);
+                s_face[f] = dot(cross(xyz(sx[fc.x]), xyz(sx[fc.y])), xyz(sx[fc.z]));
+            }
+            __syncthreads();
+            if (tid == 0) {
+                float six = 0.0f;
+                for (uint32_t f = 0; f < d.num_faces; ++f) six = six + s_face[f];
+                sh.six_volume = six;
+            }
+            __syncthreads();
+            const float six = sh.six_volume;
+            if (six > 0.0f) {
+                const float coefficient = d.pressure * dt_sub / six;
+                for (uint32_t i = tid; i < nv; i += T) {
+                    const float w = sx[i].w;
+                    float4 vel = gv[i];
+                    f3 v = xyz(vel);
+                    for (uint32_t k = __ldg(d.vf_off + i), ke = __ldg(d.vf_off + i + 1); k < ke; ++k) {
+                        uint4 fc = __ldg(d.faces + __ldg(d.vf + k));
+                        f3 x1 = xyz(sx[fc.x]), x2 = xyz(sx[fc.y]), x3 = xyz(sx[fc.z]);
+                        f3 impulse = coefficient * cross(x2 - x1, x3 - x1);
+                        v = v + w * impulse;
+                    }
+                    gv[i] = with_w(v, vel.w);
+                }
+            }
+            __syncthreads();
+        }
+        // IntegratePositions
+        for (uint32_t i = tid; i < nv; i += T) {
+            float4 pi = sx[i];
+            float4 vel = gv[i];
+            f3 v = xyz(vel);
+            if (pi.w > 0.0f) {
+                v = v + (sub_g + sub_imp * pi.w);
+                v = v * damp;
+            }
+            gprev[i] = pi;
+            f3 x = xyz(pi) + v * dt_sub;
+            sx[i] = with_w(x, pi.w);
+            gv[i] = with_w(v, vel.w);
+        }
+        __syncthreads();
+        // Update groups in dependency-level order
+        apply_levels<T>(sx, d, inv_dt_sq);
+        __syncthreads();
+        // ApplyCollisionConstraintsAndUpdateVelocities (static colliders)
+        for (uint32_t i = tid; i < nv; i += T) {
+            float4 pi = sx[i];
+            if (!(pi.w > 0.0f)) continue;
+            f3 x = xyz(pi);
+            float4 vel = gv[i];
+            f3 prev_v = xyz(vel);
+            f3 v = (x - xyz(gprev[i])) / dt_sub;
+            int shape = ncols > 0 ? gshape[i] : -1;
+            if (shape >= 0) {
+                float4 pl = gplane[i];
+                f3 n = xyz(pl);
+                float projected = -(dot(x, n) + pl.w) + d.vertex_radius;
+                if (projected > 0.0f) {
+                    const SCol &cs = sh.cols[shape];
+                    x = x + n * projected;
+                    sx[i] = with_w(x, pi.w);
+                    f3 v_normal = n * dot(n, v);
+                    f3 v_tan = v - v_normal;
+                    float vtl = len(v_tan);
+                    if (vtl > 0.0f) {
+                        float fr = cs.friction * projected / (vtl * dt_sub);
+                        fr = fr > 1.0f ? 1.0f : fr;
+                        v = v - v_tan * fr;
+                    }
+                    v = v - v_normal;
+                    float pvn = dot(prev_v, n);
+                    if (pvn < restitution_threshold) v = v - (cs.restitution * pvn) * n;
+                }
+            }
+            gv[i] = with_w(v, vel.w);
+        }
+        __syncthreads();
+    }
+
+    // UpdateSoftBodyState
+    const float max_sq = d.max_linear_velocity * d.max_linear_velocity;
+    float mm[4] = {FLT_MAX, FLT_MAX, FLT_MAX, 0};
+    int mi[4] = {-1, -1, -1, -1};
+    float xx[4] = {-FLT_MAX, -FLT_MAX, -FLT_MAX, 0};
+    int xi[4] = {-1, -1, -1, -1};
+    float pm[4] = {FLT_MAX, FLT_MAX, FLT_MAX, 0};
+    int pmi[4] = {-1, -1, -1, -1};
+    float px[4] = {-FLT_MAX, -FLT_MAX, -FLT_MAX, 0};
+    int pxi[4] = {-1, -1, -1, -1};
+    f3 lin = mk(0, 0, 0), ang = mk(0, 0, 0);
+    bool finite = true;
+    for (uint32_t i = tid; i < nv; i += T) {
+        float4 pi = sx[i];
+        float4 vel = gv[i];
+        f3 v = xyz(vel), x = xyz(pi);
+        float vsq = len_sq(v);
+        if (vsq > max_sq) v = v * sqrtf(max_sq / vsq);
+        gv[i] = with_w(v, vel.w);
+        lin = lin + v;
+        ang = ang + cross(x, v);
+        f3 pred = (x + v * dt) + disp_g;
+        pick_min(mm[0], mi[0], x.x, int(i));
+        pick_min(mm[1], mi[1], x.y, int(i));
+        pick_min(mm[2], mi[2], x.z, int(i));
+        pick_max(xx[0], xi[0], x.x, int(i));
+        pick_max(xx[1], xi[1], x.y, int(i));
+        pick_max(xx[2], xi[2], x.z, int(i));
+        pick_min(pm[0], pmi[0], pred.x, int(i));
+        pick_min(pm[1], pmi[1], pred.y, int(i));
+        pick_min(pm[2], pmi[2], pred.z, int(i));
+        pick_max(px[0], pxi[0], pred.x, int(i));
+        pick_max(px[1], pxi[1], pred.y, int(i));
+        pick_max(px[2], pxi[2], pred.z, int(i));
+        finite = finite && isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
+    }
+    if (!finite) atomicOr(p.error, kErrNonFinite);
+    {
+        const bool mins[4] = {false, false, false, false};
+        const bool maxs[4] = {true, true, true, true};
+        reduce_minmax4<T>(sh, mm, mi, mins);
+        reduce_minmax4<T>(sh, xx, xi, maxs);
+        reduce_minmax4<T>(sh, pm, pmi, mins);
+        reduce_minmax4<T>(sh, px, pxi, maxs);
+    }
+    float sums[6];
+    sums[0] = reduce_sum<T>(sh, lin.x, 0);
+    sums[1] = reduce_sum<T>(sh, lin.y, 1);
+    sums[2] = reduce_sum<T>(sh, lin.z, 2);
+    sums[3] = reduce_sum<T>(sh, ang.x, 3);
+    sums[4] = reduce_sum<T>(sh, ang.y, 0);
+    sums[5] = reduce_sum<T>(sh, ang.z, 1);
+    __shared__ float s_delta[3];
+    if (tid == 0) {
+        f3 bmin = mk(mm[0], mm[1], mm[2]), bmax = mk(xx[0], xx[1], xx[2]);
+        f3 pmin = mk(pm[0], pm[1], pm[2]), pmax = mk(px[0], px[1], px[2]);
+        st3(st->lin_vel, mk(sums[0], sums[1], sums[2]) / nvf);
+        st3(st->ang_vel, mk(sums[3], sums[4], sums[5]) / nvf);
+        f3 delta = mk(0, 0, 0);
+        f3 pos = body_pos;
+        if (d.flags & kFlagUpdatePosition) {
+            delta = 0.5f * (bmin + bmax);
+            f3 nd = neg(delta);
+            bmin = bmin + nd;
+            bmax = bmax + nd;
+            pmin = pmin + nd;
+            pmax = pmax + nd;
+            f3 wd;
+            wd.x = (1.0f * delta.x + 0.0f * delta.y) + 0.0f * delta.z;
+            wd.y = (0.0f * delta.x + 1.0f * delta.y) + 0.0f * delta.z;
+            wd.z = (0.0f * delta.x + 0.0f * delta.y) + 1.0f * delta.z;
+            pos = pos + wd;
+        }
+        st3(st->bmin, bmin);
+        st3(st->bmax, bmax);
+        st3(st->pmin, pmin);
+        st3(st->pmax, pmax);
+        st3(st->position, pos);
+        st3(s_delta, delta);
+    }
+    __syncthreads();
+    const f3 delta = ld3(s_delta);
+    const bool shift = (d.flags & kFlagUpdatePosition) != 0;
+    for (uint32_t i = tid; i < nv; i += T) {
+        float4 pi = sx[i];
+        gx[i] = shift ? with_w(xyz(pi) - delta, pi.w) : pi;
+    }
+    __syncthreads();
+}
+
+template <int T>
+__global__ void __launch_bounds__(T) step_kernel(StepParams p, uint32_t face_offset_floats) {
+    extern __shared__ float4 smem[];
+    __shared__ Shared sh;
+    float4 *sx = smem;
+    float *s_face = reinterpret_cast<float *>(smem) + face_offset_floats;
+    for (;;) {
+        if (threadIdx.x == 0) sh.item = atomicAdd(p.queue, 1u);
+        __syncthreads();
+        const uint32_t item = sh.item;
+        __syncthreads();
+        if (item >= p.num_work) return;
+        step_body<T>(p, p.work[item], sx, sh, s_face);
+    }
+}
+
+}  // namespace
+
+// Launches one persistent step over `p.num_work` bodies with `threads` threads per CTA.
+// smem_vertices / smem_faces size the dynamic shared memory (largest body of the launch).
+cudaError_t launch_step(const StepParams &p, int threads, uint32_t smem_vertices, uint32_t smem_faces, int grid,
+                        cudaStream_t stream) {
+    size_t face_off = size_t(smem_vertices) * 4;  // in floats
+    size_t smem = size_t(smem_vertices) * sizeof(float4) + size_t(smem_faces) * sizeof(float);
+    switch (threads) {
+        case 32:
+            step_kernel<32><<<grid, 32, smem, stream>>>(p, uint32_t(face_off));
+            break;
+        case 64:
+            step_kernel<64><<<grid, 64, smem, stream>>>(p, uint32_t(face_off));
+            break;
+        case 128:
+            step_kernel<128><<<grid, 128, smem, stream>>>(p, uint32_t(face_off));
+            break;
+        case 256:
+            step_kernel<256><<<grid, 256, smem, stream>>>(p, uint32_t(face_off));
+            break;
+        default:
+            return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// Allows every solver kernel instance to use up to `max_dynamic_smem` bytes of dynamic shared memory
+// (done once per device, outside any stream capture).
+cudaError_t init_step_kernels(int max_dynamic_smem) {
+    cudaError_t e = cudaSuccess;
+    e = cudaFuncSetAttribute(step_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+    return e;
+}
+
+// Occupancy of step_kernel<threads> with the given dynamic shared memory (CTAs per SM).
+int step_occupancy(int threads, size_t smem) {
+    int n = 0;
+    switch (threads) {
+        case 32:
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<32>, 32, smem);
+            break;
+        case 64:
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<64>, 64, smem);
+            break;
+        case 128:
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<128>, 128, smem);
+            break;
+        case 256:
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<256>, 256, smem);
+            break;
+        default:
+            return 0;
+    }
+    return n;
+}
+
+}  // namespace jsb

@@ -27,12 +27,14 @@
 //
 // Build: g++ -O2 -std=c++17 -ffp-contract=off -fPIC -shared oracle/jsb_oracle.cpp -o oracle/liboracle.so
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace oracle {
@@ -244,10 +246,25 @@ public:
         o.contact = false;
     }
 
+    int threads = 1;
+
+    // Bodies are independent within a step, so they may be stepped on several threads (body i on
+    // thread i % threads); each body's arithmetic is unchanged.
     void step(R dt, int collision_steps) {
         R step_dt = dt / R(collision_steps);
-        for (int c = 0; c < collision_steps; ++c)
-            for (auto &b : bodies) step_body(b, step_dt);
+        for (int c = 0; c < collision_steps; ++c) {
+            if (threads <= 1 || bodies.size() < 2) {
+                for (auto &b : bodies) step_body(b, step_dt);
+                continue;
+            }
+            std::vector<std::thread> pool;
+            int n = int(std::min<size_t>(size_t(threads), bodies.size()));
+            for (int t = 0; t < n; ++t)
+                pool.emplace_back([this, t, n, step_dt] {
+                    for (size_t i = size_t(t); i < bodies.size(); i += size_t(n)) step_body(bodies[i], step_dt);
+                });
+            for (auto &th : pool) th.join();
+        }
     }
 
     void step_body(Body<R> &b, R dt) {
@@ -582,6 +599,12 @@ void *oracle_world_create(const float gravity[3], int use_double) {
 }
 
 void oracle_world_destroy(void *w) { delete static_cast<Handle *>(w); }
+
+void oracle_set_threads(void *w, int threads) {
+    Handle *h = static_cast<Handle *>(w);
+    h->wf.threads = threads;
+    h->wd.threads = threads;
+}
 
 int oracle_add_collider(void *w, int type, const float pos[3], const float half_extent[3], float radius, float friction,
                         float restitution) {

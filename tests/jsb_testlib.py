@@ -146,8 +146,8 @@ def run_reference(variant: str, scene: str, out: str, **kv) -> dict:
 def build_oracle() -> str:
     src = os.path.join(ORACLE_DIR, "jsb_oracle.cpp")
     if (not os.path.exists(ORACLE_LIB)) or os.path.getmtime(ORACLE_LIB) < os.path.getmtime(src):
-        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", src, "-o", ORACLE_LIB],
-                       check=True)
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", src, "-o",
+                        ORACLE_LIB], check=True)
     return ORACLE_LIB
 
 
@@ -164,6 +164,7 @@ class Oracle:
             L.oracle_world_create.restype = ctypes.c_void_p
             L.oracle_world_create.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.c_int]
             L.oracle_world_destroy.argtypes = [ctypes.c_void_p]
+            L.oracle_set_threads.argtypes = [ctypes.c_void_p, ctypes.c_int]
             L.oracle_add_collider.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
                                               ctypes.POINTER(ctypes.c_float), ctypes.c_float, ctypes.c_float,
                                               ctypes.c_float]
@@ -180,11 +181,12 @@ class Oracle:
             cls._lib = L
         return cls._lib
 
-    def __init__(self, scene: Scene, use_double: bool = False):
+    def __init__(self, scene: Scene, use_double: bool = False, threads: int = 1):
         L = self.lib()
         self.scene = scene
         g = (ctypes.c_float * 3)(*scene.gravity)
         self.h = L.oracle_world_create(g, int(use_double))
+        L.oracle_set_threads(self.h, int(threads))
         for c in scene.colliders:
             L.oracle_add_collider(self.h, c.type, (ctypes.c_float * 3)(*c.position),
                                   (ctypes.c_float * 3)(*c.half_extent), c.radius, c.friction, c.restitution)

@@ -1,0 +1,103 @@
+"""Dependency-level schedule invariants (host only).
+
+The GPU projects all constraints of one level concurrently. That reproduces the reference's sequential
+Gauss-Seidel order bit for bit iff (1) every constraint appears once, (2) for every vertex, a write
+happens at a later level than every earlier access of that vertex in sequence order and a read happens
+at a later level than the latest earlier write; the order inside a level is then irrelevant.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_path
+from jsb_testlib import parse_scene
+
+TYPE_BEND, TYPE_VOLUME, TYPE_EDGE, TYPE_LRA = 0, 1, 2, 3
+
+
+def parse_constraints(blob):
+    import struct
+    off = 0
+    out = {}
+    for name, size in [("vertices", 28), ("faces", 16), ("edges", 16), ("bends", 24), ("volumes", 24),
+                       ("skinned", 52), ("skinned_normals", 4), ("lras", 12), ("groups", 28)]:
+        (n,) = struct.unpack_from("<I", blob, off)
+        off += 4
+        out[name] = np.frombuffer(blob, np.uint32, n * size // 4, off).reshape(n, size // 4) if n else np.zeros((0, size // 4), np.uint32)
+        off += n * size
+    return out
+
+
+def sequence(c):
+    """(type, index, written vertices, read-only vertices) in the reference's processing order."""
+    seq = []
+    prev = np.zeros(7, np.int64)
+    for g in c["groups"].astype(np.int64):
+        # group fields: edge, lra, rod_ss, rod_bt, bend, volume, skinned
+        for i in range(prev[5], g[5]):
+            seq.append((TYPE_VOLUME, i, tuple(c["volumes"][i, :4]), ()))
+        for i in range(prev[4], g[4]):
+            seq.append((TYPE_BEND, i, tuple(c["bends"][i, :4]), ()))
+        for i in range(prev[0], g[0]):
+            seq.append((TYPE_EDGE, i, tuple(c["edges"][i, :2]), ()))
+        for i in range(prev[1], g[1]):
+            seq.append((TYPE_LRA, i, (c["lras"][i, 1],), (c["lras"][i, 0],)))
+        prev = g
+    return seq
+
+
+@pytest.mark.parametrize("name,body", [("pinned_cloth", 0), ("uneven_small", 0), ("uneven_small", 7),
+                                       ("large_cloth_32", 0), ("diff_batch_small", 5)])
+def test_levels_reproduce_sequential_order(jsb, name, body):
+    scene, _ = parse_scene(np.load(golden_path(name))["scene"].tobytes())
+    blob = scene.bodies[body].blob
+    levels, records, source = jsb.settings_schedule(blob)
+    c = parse_constraints(blob)
+    seq = sequence(c)
+    assert len(source) == len(seq)
+    # level of every (type, index)
+    level_of = {}
+    L = len(levels) - 2
+    for l in range(L):
+        start, eb, ev, ee = levels[l]
+        end = levels[l + 1][0]
+        assert start <= eb <= ev <= ee <= end
+        for k in range(start, end):
+            t = int(source[k]) >> 28
+            expect = TYPE_BEND if k < eb else TYPE_VOLUME if k < ev else TYPE_EDGE if k < ee else TYPE_LRA
+            assert t == expect
+            key = (t, int(source[k]) & 0x0FFFFFFF)
+            assert key not in level_of
+            level_of[key] = l
+    assert len(level_of) == len(seq)
+    last_write = {}
+    max_access = {}
+    for t, i, writes, reads in seq:
+        l = level_of[(t, i)]
+        for v in writes:
+            assert l > max_access.get(v, -1)
+        for v in reads:
+            assert l > last_write.get(v, -1)
+        for v in writes:
+            last_write[v] = l
+            max_access[v] = max(max_access.get(v, -1), l)
+        for v in reads:
+            max_access[v] = max(max_access.get(v, -1), l)
+    # records carry the constraint data of their source
+    for k in range(len(source)):
+        t, i = int(source[k]) >> 28, int(source[k]) & 0x0FFFFFFF
+        r = records[k]
+        if t == TYPE_EDGE:
+            e = c["edges"][i]
+            assert r[0] == (e[0] | (e[1] << 16)) and r[2] == e[2] and r[3] == e[3]
+        elif t == TYPE_BEND:
+            b = c["bends"][i]
+            assert r[0] == (b[0] | (b[1] << 16)) and r[1] == (b[2] | (b[3] << 16)) and r[2] == b[4] and r[3] == b[5]
+
+
+def test_level_counts_pinned_cloth(jsb):
+    """Schedule depth for the 30x30 pinned cloth (4 parallel groups + non-parallel group)."""
+    scene, _ = parse_scene(np.load(golden_path("pinned_cloth"))["scene"].tobytes())
+    levels, records, source = jsb.settings_schedule(scene.bodies[0].blob)
+    L = len(levels) - 2
+    assert len(source) == 3422 + 2465
+    assert 100 < L < 600
