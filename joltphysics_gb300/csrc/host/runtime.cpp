@@ -29,9 +29,10 @@
 
 namespace jsb {
 
-cudaError_t launch_step(const StepParams &p, int threads, uint32_t smem_vertices, uint32_t smem_faces, int grid,
-                        cudaStream_t stream);
-int step_occupancy(int threads, size_t smem);
+cudaError_t launch_step(const StepParams &p, int threads, bool smem_state, uint32_t smem_vertices, uint32_t smem_faces,
+                        int grid, cudaStream_t stream);
+int step_occupancy(int threads, bool smem_state, size_t smem);
+size_t step_smem_bytes(bool smem_state, uint32_t vertices, uint32_t faces);
 cudaError_t init_step_kernels(int max_dynamic_smem);
 cudaError_t launch_unpack_state(const float *pos3, const float *vel3, float4 *x, float4 *v, uint64_t n, int num_sms,
                                 cudaStream_t stream);
@@ -118,6 +119,7 @@ struct Bucket {
 
 struct LaunchGroup {  // bodies sharing one launch shape
     int threads = 0;
+    bool smem_state = true;  // velocities / previous positions staged in shared memory
     uint32_t smem_vertices = 0, smem_faces = 0;
     int grid = 0;
     std::vector<uint32_t> bodies;
@@ -195,13 +197,13 @@ int threads_for(const jsb_context *ctx, uint32_t nv) {
 BodyDesc make_desc(const jsb_context *ctx, const BodyRec &b) {
     const SettingsRec &s = *ctx->settings[b.settings_id];
     BodyDesc d;
-    d.levels = s.levels.ptr;
+    d.levels = s.levels.ptr;  // padded device layout
     d.records = s.records.ptr;
     d.faces = s.faces.ptr;
     d.vf_off = s.vf_off_dev.ptr;
     d.vf = s.vf_dev.ptr;
     d.num_levels = s.schedule.num_levels;
-    d.num_records = s.schedule.num_records;
+    d.num_records = s.schedule.num_slots;
     d.num_faces = uint32_t(s.parsed.faces.size());
     d.num_vertices = uint32_t(s.parsed.vertices.size());
     d.vtx_offset = b.vtx_offset;
@@ -217,9 +219,21 @@ BodyDesc make_desc(const jsb_context *ctx, const BodyRec &b) {
     return d;
 }
 
-// Dynamic shared memory a body needs on the single-CTA path.
-size_t smem_bytes(const SettingsRec &s, bool pressure) {
-    return s.parsed.vertices.size() * sizeof(float4) + (pressure ? s.parsed.faces.size() * sizeof(float) : 0);
+constexpr size_t kStaticSmemReserve = 4096;  // static shared memory of the solver kernel
+
+uint32_t pressure_faces(const SettingsRec &s, const BodyRec &b) {
+    return b.creation.pressure > 0.0f ? uint32_t(s.parsed.faces.size()) : 0u;
+}
+
+// Whether a body's whole vertex state (x, v, prev) fits in one CTA's shared memory; if not, only
+// the positions are staged there. Returns false in `fits` when even that does not fit.
+bool body_smem_state(const jsb_context *ctx, const SettingsRec &s, const BodyRec &b, bool &fits) {
+    uint32_t nv = uint32_t(s.parsed.vertices.size()), nf = pressure_faces(s, b);
+    const size_t cap = ctx->max_smem_optin - kStaticSmemReserve;
+    fits = true;
+    if (step_smem_bytes(true, nv, nf) <= cap) return true;
+    fits = step_smem_bytes(false, nv, nf) <= cap;
+    return false;
 }
 
 double body_cost(const SettingsRec &s, const BodyRec &b, int threads) {
@@ -295,38 +309,41 @@ jsb_status rebuild(jsb_context *ctx) {
         JSB_CUDA(cudaMemset(ctx->error.ptr, 0, sizeof(uint32_t)));
     }
 
-    // launch groups: one per threads-per-CTA value
-    std::vector<int> shapes;
-    for (const BodyRec &b : ctx->bodies) {
-        int t = threads_for(ctx, uint32_t(ctx->settings[b.settings_id]->parsed.vertices.size()));
-        if (std::find(shapes.begin(), shapes.end(), t) == shapes.end()) shapes.push_back(t);
+    // launch groups: one per (threads per CTA, state-in-shared-memory) pair
+    std::vector<std::pair<int, bool>> shapes;
+    std::vector<std::pair<int, bool>> body_shape(ctx->bodies.size());
+    for (size_t bi = 0; bi < ctx->bodies.size(); ++bi) {
+        const BodyRec &b = ctx->bodies[bi];
+        const SettingsRec &s = *ctx->settings[b.settings_id];
+        bool fits = true;
+        bool smem_state = body_smem_state(ctx, s, b, fits);
+        if (!fits)
+            return fail(JSB_ERR_UNSUPPORTED, "body " + std::to_string(bi) + " with " + std::to_string(s.parsed.vertices.size()) +
+                                                 " vertices does not fit the shared-memory solver path");
+        body_shape[bi] = {threads_for(ctx, uint32_t(s.parsed.vertices.size())), smem_state};
+        if (std::find(shapes.begin(), shapes.end(), body_shape[bi]) == shapes.end()) shapes.push_back(body_shape[bi]);
     }
     std::sort(shapes.begin(), shapes.end());
     ctx->groups.resize(shapes.size());
     for (size_t gi = 0; gi < shapes.size(); ++gi) {
         LaunchGroup &g = ctx->groups[gi];
-        g.threads = shapes[gi];
+        g.threads = shapes[gi].first;
+        g.smem_state = shapes[gi].second;
         std::vector<std::pair<double, uint32_t>> items;
         for (size_t bi = 0; bi < ctx->bodies.size(); ++bi) {
+            if (body_shape[bi] != shapes[gi]) continue;
             const BodyRec &b = ctx->bodies[bi];
             const SettingsRec &s = *ctx->settings[b.settings_id];
-            if (threads_for(ctx, uint32_t(s.parsed.vertices.size())) != g.threads) continue;
-            bool pressure = b.creation.pressure > 0.0f;
-            size_t need = smem_bytes(s, pressure);
-            if (need + 4096 > ctx->max_smem_optin)
-                return fail(JSB_ERR_UNSUPPORTED, "body " + std::to_string(bi) + " needs " + std::to_string(need) +
-                                                     " bytes of shared memory; the single-CTA solver path holds at most " +
-                                                     std::to_string(ctx->max_smem_optin - 4096));
             g.smem_vertices = std::max(g.smem_vertices, uint32_t(s.parsed.vertices.size()));
-            if (pressure) g.smem_faces = std::max(g.smem_faces, uint32_t(s.parsed.faces.size()));
+            g.smem_faces = std::max(g.smem_faces, pressure_faces(s, b));
             items.push_back({body_cost(s, b, g.threads), uint32_t(bi)});
         }
         // Longest-processing-time-first order for the work queue.
         std::stable_sort(items.begin(), items.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
         for (auto &it : items) g.bodies.push_back(it.second);
         JSB_CUDA(g.work.upload(g.bodies.data(), g.bodies.size()));
-        size_t smem = size_t(g.smem_vertices) * sizeof(float4) + size_t(g.smem_faces) * sizeof(float);
-        int occ = step_occupancy(g.threads, smem);
+        size_t smem = step_smem_bytes(g.smem_state, g.smem_vertices, g.smem_faces);
+        int occ = step_occupancy(g.threads, g.smem_state, smem);
         if (occ <= 0) return fail(JSB_ERR_UNSUPPORTED, "solver kernel does not fit on an SM with this shared memory size");
         g.grid = int(std::min<size_t>(g.bodies.size(), size_t(occ) * ctx->num_sms));
         JSB_CUDA(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
@@ -370,7 +387,7 @@ jsb_status enqueue_batched(jsb_context *ctx, float dt, cudaStream_t stream, uint
         p.work = g.work.ptr;
         p.num_work = uint32_t(g.bodies.size());
         p.queue = ctx->queues.ptr + gi;
-        JSB_CUDA(launch_step(p, g.threads, g.smem_vertices, g.smem_faces, g.grid, g.stream));
+        JSB_CUDA(launch_step(p, g.threads, g.smem_state, g.smem_vertices, g.smem_faces, g.grid, g.stream));
         ++launches;
         JSB_CUDA(cudaEventRecord(g.done, g.stream));
         JSB_CUDA(cudaStreamWaitEvent(stream, g.done, 0));
@@ -409,9 +426,8 @@ jsb_status step_impl(jsb_context *ctx, float dt, int collision_steps, cudaStream
                     p.num_work = 1;
                     p.queue = ctx->queues.ptr;
                     const SettingsRec &s = *ctx->settings[ctx->bodies[b].settings_id];
-                    bool pressure = ctx->bodies[b].creation.pressure > 0.0f;
-                    JSB_CUDA(launch_step(p, g.threads, uint32_t(s.parsed.vertices.size()),
-                                         pressure ? uint32_t(s.parsed.faces.size()) : 0u, 1, stream));
+                    JSB_CUDA(launch_step(p, g.threads, g.smem_state, uint32_t(s.parsed.vertices.size()),
+                                         pressure_faces(s, ctx->bodies[b]), 1, stream));
                     ++launches;
                 }
             }
@@ -462,7 +478,7 @@ jsb_status jsb_context_create(int device, jsb_context **out) {
     ctx->max_smem_optin = prop.sharedMemPerBlockOptin;
     ctx->buckets = {{512, 32}, {2048, 64}, {65536, 128}};
     // static shared memory of the solver kernel is under 4 KB
-    JSB_CUDA(init_step_kernels(int(ctx->max_smem_optin) - 4096));
+    JSB_CUDA(init_step_kernels(int(ctx->max_smem_optin - kStaticSmemReserve)));
     JSB_CUDA(cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming));
     JSB_CUDA(cudaEventCreate(&ctx->t0));
     JSB_CUDA(cudaEventCreate(&ctx->t1));
@@ -505,8 +521,10 @@ jsb_status jsb_settings_upload(jsb_context *ctx, const void *blob, size_t len, u
     std::vector<uint4> faces(ps.faces.size());
     for (size_t fi = 0; fi < ps.faces.size(); ++fi) faces[fi] = make_uint4(ps.faces[fi].v[0], ps.faces[fi].v[1], ps.faces[fi].v[2], 0);
     JSB_CUDA(cudaSetDevice(ctx->device));
-    JSB_CUDA(rec->levels.upload(reinterpret_cast<const uint4 *>(rec->schedule.levels.data()), rec->schedule.levels.size() / 4));
-    JSB_CUDA(rec->records.upload(reinterpret_cast<const uint4 *>(rec->schedule.records.data()), rec->schedule.records.size() / 4));
+    JSB_CUDA(rec->levels.upload(reinterpret_cast<const uint4 *>(rec->schedule.padded_levels.data()),
+                                rec->schedule.padded_levels.size() / 4));
+    JSB_CUDA(rec->records.upload(reinterpret_cast<const uint4 *>(rec->schedule.padded_records.data()),
+                                 rec->schedule.padded_records.size() / 4));
     JSB_CUDA(rec->faces.upload(faces.data(), faces.size()));
     JSB_CUDA(rec->vf_off_dev.upload(rec->vf_off.data(), rec->vf_off.size()));
     JSB_CUDA(rec->vf_dev.upload(rec->vf.data(), rec->vf.size()));
@@ -902,13 +920,16 @@ jsb_status jsb_autotune(jsb_context *ctx, float dt, int trials) {
         uint32_t hi = tuned[bi].max_vertices;
         std::vector<uint32_t> members;
         uint32_t max_nv = 0, max_faces = 0;
+        bool smem_state = true;
         for (size_t b = 0; b < ctx->bodies.size(); ++b) {
             const SettingsRec &s = *ctx->settings[ctx->bodies[b].settings_id];
             uint32_t nv = uint32_t(s.parsed.vertices.size());
             if (nv > lo && nv <= hi) {
                 members.push_back(uint32_t(b));
                 max_nv = std::max(max_nv, nv);
-                if (ctx->bodies[b].creation.pressure > 0.0f) max_faces = std::max(max_faces, uint32_t(s.parsed.faces.size()));
+                max_faces = std::max(max_faces, pressure_faces(s, ctx->bodies[b]));
+                bool fits = true;
+                smem_state = smem_state && body_smem_state(ctx, s, ctx->bodies[b], fits);
             }
         }
         if (members.empty()) continue;
@@ -917,8 +938,8 @@ jsb_status jsb_autotune(jsb_context *ctx, float dt, int trials) {
         float best_ms = 1e30f;
         int best = tuned[bi].threads;
         for (int t : choices) {
-            size_t smem = size_t(max_nv) * sizeof(float4) + size_t(max_faces) * sizeof(float);
-            int occ = step_occupancy(t, smem);
+            size_t smem = step_smem_bytes(smem_state, max_nv, max_faces);
+            int occ = step_occupancy(t, smem_state, smem);
             if (occ <= 0) continue;
             int grid = int(std::min<size_t>(members.size(), size_t(occ) * ctx->num_sms));
             StepParams p = base_params(ctx, dt);
@@ -929,7 +950,7 @@ jsb_status jsb_autotune(jsb_context *ctx, float dt, int trials) {
             for (int k = 0; k < trials + 1; ++k) {
                 JSB_CUDA(cudaMemset(ctx->queues.ptr, 0, sizeof(uint32_t)));
                 JSB_CUDA(cudaEventRecord(ctx->t0, 0));
-                JSB_CUDA(launch_step(p, t, max_nv, max_faces, grid, 0));
+                JSB_CUDA(launch_step(p, t, smem_state, max_nv, max_faces, grid, 0));
                 JSB_CUDA(cudaEventRecord(ctx->t1, 0));
                 JSB_CUDA(cudaEventSynchronize(ctx->t1));
                 float ms = 0;

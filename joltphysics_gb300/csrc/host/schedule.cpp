@@ -200,6 +200,44 @@ Schedule build_schedule(const ParsedSettings &s) {
         }
         out.source[k] = (it.type << 28) | it.index;
     }
+    // padded device layout
+    auto pad = [](uint32_t v) { return (v + 31u) & ~31u; };
+    out.padded_levels.resize(size_t(out.num_levels + 2) * 4);
+    uint32_t slot = 0;
+    for (uint32_t l = 0; l < out.num_levels; ++l) {
+        const uint32_t *lv = &out.levels[l * 4];
+        const uint32_t next = out.levels[(l + 1) * 4];
+        uint32_t nb = lv[1] - lv[0], nvol = lv[2] - lv[1], ne = lv[3] - lv[2], nl = next - lv[3];
+        uint32_t b_end = pad(nb), v_end = b_end + pad(nvol), e_end = v_end + pad(ne), total = e_end + pad(nl);
+        out.padded_levels[l * 4 + 0] = slot;
+        out.padded_levels[l * 4 + 1] = b_end;
+        out.padded_levels[l * 4 + 2] = v_end;
+        out.padded_levels[l * 4 + 3] = e_end;
+        out.max_level_slots = std::max(out.max_level_slots, total);
+        slot += total;
+    }
+    out.num_slots = slot;
+    for (uint32_t l = out.num_levels; l < out.num_levels + 2; ++l) {
+        out.padded_levels[l * 4 + 0] = slot;
+        out.padded_levels[l * 4 + 1] = out.padded_levels[l * 4 + 2] = out.padded_levels[l * 4 + 3] = 0;
+    }
+    out.padded_records.assign(size_t(slot) * 4, 0);
+    out.padded_source.assign(slot, 0xffffffffu);
+    for (uint32_t k = 0; k < slot; ++k) out.padded_records[size_t(k) * 4] = kPadRecord;
+    for (uint32_t l = 0; l < out.num_levels; ++l) {
+        const uint32_t *lv = &out.levels[l * 4];
+        const uint32_t next = out.levels[(l + 1) * 4];
+        const uint32_t base = out.padded_levels[l * 4];
+        const uint32_t group_first[4] = {lv[0], lv[1], lv[2], lv[3]};
+        const uint32_t group_last[4] = {lv[1], lv[2], lv[3], next};
+        const uint32_t group_slot[4] = {0, out.padded_levels[l * 4 + 1], out.padded_levels[l * 4 + 2], out.padded_levels[l * 4 + 3]};
+        for (int t = 0; t < 4; ++t)
+            for (uint32_t c = group_first[t]; c < group_last[t]; ++c) {
+                uint32_t dst = base + group_slot[t] + (c - group_first[t]);
+                for (int k = 0; k < 4; ++k) out.padded_records[size_t(dst) * 4 + k] = out.records[size_t(c) * 4 + k];
+                out.padded_source[dst] = out.source[c];
+            }
+    }
     return out;
 }
 

@@ -60,7 +60,20 @@ struct Schedule {
     uint32_t num_levels = 0;
     uint32_t num_records = 0;
     uint32_t max_level_width = 0;
+
+    // Device layout: the same records with every type group of a level padded to a multiple of 32
+    // slots (padding slots hold kPadRecord), so a warp projects one constraint type and slot s of a
+    // level is simply record start + s.
+    //   padded_levels[l] = {first slot, end of bend slots, end of volume slots, end of edge slots}
+    //   (ends relative to the first slot); num_levels + 2 entries with two sentinels.
+    std::vector<uint32_t> padded_levels;
+    std::vector<uint32_t> padded_records;  // 4 per slot
+    std::vector<uint32_t> padded_source;   // per slot: source of the record, 0xffffffff for padding
+    uint32_t num_slots = 0;
+    uint32_t max_level_slots = 0;
 };
+
+constexpr uint32_t kPadRecord = 0xffffffffu;  // first word of a padding slot
 
 // Builds the dependency-level schedule of one substep's constraint projection.
 //

@@ -28,6 +28,22 @@
 namespace jsb {
 namespace {
 
+// IEEE-exact division and square root with a short path for zero operands. The hardware-independent
+// results are unchanged (0 / b = +-0 with the xor of the signs for finite non-zero b, NaN for b = 0 or
+// NaN; sqrt(+-0) = +-0), but the general IEEE routines take a slow path (several times the latency)
+// for zero inputs, which flat cloth and converged constraints produce constantly. The general routine
+// is still evaluated, on a non-zero stand-in, so both branches have the same latency.
+__device__ __forceinline__ float jdiv(float a, float b) {
+    float q = __fdiv_rn(a == 0.0f ? 1.0f : a, b);
+    if (a == 0.0f)
+        q = (b == 0.0f || b != b) ? __int_as_float(0x7fffffff) : __int_as_float((__float_as_int(a) ^ __float_as_int(b)) & int(0x80000000));
+    return q;
+}
+__device__ __forceinline__ float jsqrt(float a) {
+    float r = __fsqrt_rn(a == 0.0f ? 1.0f : a);
+    return a == 0.0f ? a : r;
+}
+
 struct f3 {
     float x, y, z;
 };
@@ -37,7 +53,7 @@ __device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b
 __device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 __device__ __forceinline__ f3 operator*(float s, f3 a) { return {s * a.x, s * a.y, s * a.z}; }
 __device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
-__device__ __forceinline__ f3 operator/(f3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ f3 operator/(f3 a, float s) { return {jdiv(a.x, s), jdiv(a.y, s), jdiv(a.z, s)}; }
 __device__ __forceinline__ f3 neg(f3 a) { return {0.0f - a.x, 0.0f - a.y, 0.0f - a.z}; }
 __device__ __forceinline__ float dot(f3 a, f3 b) {
     float px = a.x * b.x, py = a.y * b.y, pz = a.z * b.z;
@@ -47,7 +63,7 @@ __device__ __forceinline__ f3 cross(f3 a, f3 b) {
     return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
 __device__ __forceinline__ float len_sq(f3 a) { return dot(a, a); }
-__device__ __forceinline__ float len(f3 a) { return sqrtf(len_sq(a)); }
+__device__ __forceinline__ float len(f3 a) { return jsqrt(len_sq(a)); }
 __device__ __forceinline__ f3 vmin(f3 a, f3 b) { return {a.x < b.x ? a.x : b.x, a.y < b.y ? a.y : b.y, a.z < b.z ? a.z : b.z}; }
 __device__ __forceinline__ f3 vmax(f3 a, f3 b) { return {a.x > b.x ? a.x : b.x, a.y > b.y ? a.y : b.y, a.z > b.z ? a.z : b.z}; }
 __device__ __forceinline__ f3 ld3(const float *p) { return {p[0], p[1], p[2]}; }
@@ -64,7 +80,7 @@ constexpr float kPi = 3.14159265358979323846f;
 __device__ __forceinline__ float acos_approximate(float x) {
     float ax = fabsf(x);
     ax = ax > 1.0f ? 1.0f : ax;
-    float val = sqrtf(1.0f - ax) * (kPi / 2 - 0.175394f * ax);
+    float val = jsqrt(1.0f - ax) * (kPi / 2 - 0.175394f * ax);
     return x < 0.0f ? kPi - val : val;
 }
 
@@ -90,6 +106,8 @@ struct Shared {
     int ncols;
     uint32_t item;
     float six_volume;
+    float delta[3];
+    uint4 ring_desc[4];
     float red[32][4];  // per-warp partials for reductions
     int redi[32][4];
 };
@@ -112,7 +130,7 @@ __device__ __forceinline__ void project_bend(float4 *sx, uint4 r, float inv_dt_s
     float n1n2 = n1_len_sq * n2_len_sq;
     if (n1n2 < 1.0e-24f) return;
     float sign = dot(cross(n2, n1), e) < 0.0f ? -1.0f : 1.0f;
-    float d = dot(n1, n2) / sqrtf(n1n2);
+    float d = jdiv(dot(n1, n2), jsqrt(n1n2));
     float c = sign * acos_approximate(d) - initial_angle;
     if (c > kPi)
         c -= 2.0f * kPi;
@@ -127,7 +145,7 @@ __device__ __forceinline__ void project_bend(float4 *sx, uint4 r, float inv_dt_s
     float w0 = p0.w, w1 = p1.w, w2 = p2.w, w3 = p3.w;
     float denom = w0 * len_sq(d0c) + w1 * len_sq(d1c) + w2 * len_sq(d2c) + w3 * len_sq(d3c) + compliance * inv_dt_sq;
     if (denom < 1.0e-12f) return;
-    float ml = c / denom;
+    float ml = jdiv(c, denom);
     sx[i0] = with_w(x0 - (ml * w0) * d0c, w0);
     sx[i1] = with_w(x1 - (ml * w1) * d1c, w1);
     sx[i2] = with_w(x2 - (ml * w2) * d2c, w2);
@@ -148,7 +166,7 @@ __device__ __forceinline__ void project_volume(float4 *sx, uint4 r, float inv_dt
     float w1 = p1.w, w2 = p2.w, w3 = p3.w, w4 = p4.w;
     float denom = w1 * len_sq(d1c) + w2 * len_sq(d2c) + w3 * len_sq(d3c) + w4 * len_sq(d4c) + compliance * inv_dt_sq;
     if (denom < 1.0e-12f) return;
-    float ml = c / denom;
+    float ml = jdiv(c, denom);
     sx[i1] = with_w(x1 - (ml * w1) * d1c, w1);
     sx[i2] = with_w(x2 - (ml * w2) * d2c, w2);
     sx[i3] = with_w(x3 - (ml * w3) * d3c, w3);
@@ -176,47 +194,104 @@ __device__ __forceinline__ void project_lra(float4 *sx, uint4 r) {  // :679-698
     float4 p1 = sx[i1];
     f3 delta = xyz(p1) - x0;
     float dls = len_sq(delta);
-    if (dls > md * md) sx[i1] = with_w(x0 + (delta * md) / sqrtf(dls), p1.w);
+    if (dls > md * md) sx[i1] = with_w(x0 + (delta * md) / jsqrt(dls), p1.w);
 }
 
-__device__ __forceinline__ void project(float4 *sx, uint4 r, uint32_t c, uint4 lv, float inv_dt_sq) {
-    if (c < lv.y)
+__device__ __forceinline__ void project(float4 *sx, uint4 r, int type, float inv_dt_sq) {
+    if (type == 0)
         project_bend(sx, r, inv_dt_sq);
-    else if (c < lv.z)
+    else if (type == 1)
         project_volume(sx, r, inv_dt_sq);
-    else if (c < lv.w)
+    else if (type == 2)
         project_edge(sx, r, inv_dt_sq);
     else
         project_lra(sx, r);
 }
 
-// Walks the dependency levels of one substep. Software pipelined: the next level's descriptor and
-// this thread's first record of it are loaded before the current level is projected.
+// Type of slot `s` of a level with descriptor {first slot, bend end, volume end, edge end}: the
+// type groups are padded to multiples of 32 slots, so the type is uniform across a warp.
+__device__ __forceinline__ int slot_type(uint4 lv, uint32_t s) {
+    return s < lv.y ? 0 : (s < lv.z ? 1 : (s < lv.w ? 2 : 3));
+}
+
+// ---- asynchronous copies (cp.async, 16 bytes per thread) -----------------------------------------
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src) {
+    const uint32_t dst = uint32_t(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Record ring: kRingDepth levels of up to kRingSlots records each are streamed into shared memory
+// ahead of the level being projected; the ring holds kRingDepth + 1 levels.
+constexpr int kRingDepth = 3;
+constexpr int kRingLevels = kRingDepth + 1;
+constexpr uint32_t kRingSlots = 256;
+constexpr size_t kRingBytes = size_t(kRingLevels) * kRingSlots * sizeof(uint4);
+
+struct LevelRing {
+    uint4 *rec;   // [kRingLevels][kRingSlots]
+    uint4 *desc;  // [kRingLevels] level descriptors
+};
+
+// Stages level `idx` (descriptor, and its records when they fit a ring slot) into ring position
+// idx % kRingLevels. idx == num_levels stages the sentinel descriptor only.
 template <int T>
-__device__ __forceinline__ void apply_levels(float4 *sx, const BodyDesc &d, float inv_dt_sq) {
+__device__ __forceinline__ void ring_stage(const LevelRing &ring, const uint4 *__restrict__ levels, const uint4 *__restrict__ rec,
+                                           uint32_t idx, uint32_t L, uint4 lv, uint32_t next_first) {
+    const uint32_t pos = idx % kRingLevels;
+    if (idx < L) {
+        const uint32_t n = next_first - lv.x;
+        if (n <= kRingSlots)
+            for (uint32_t s = threadIdx.x; s < n; s += T) cp_async16(ring.rec + pos * kRingSlots + s, rec + lv.x + s);
+    }
+    if (threadIdx.x == 0) ring.desc[pos] = lv;
+}
+
+// Walks the dependency levels of one substep. Level l + kRingDepth is staged (cp.async) while level
+// l is projected, so the critical path of a level is: descriptor and records from shared memory,
+// positions from shared memory, projection, positions to shared memory, barrier.
+template <int T>
+__device__ __forceinline__ void apply_levels(float4 *sx, const BodyDesc &d, float inv_dt_sq, const LevelRing &ring) {
     const uint4 *__restrict__ levels = d.levels;
     const uint4 *__restrict__ rec = d.records;
     const uint32_t tid = threadIdx.x;
     const uint32_t L = d.num_levels;
     if (L == 0) return;
-    uint4 l0 = __ldg(levels + 0);
-    uint4 l1 = __ldg(levels + 1);
-    uint4 r = make_uint4(0, 0, 0, 0);
-    if (l0.x + tid < l1.x) r = __ldg(rec + l0.x + tid);
-    for (uint32_t l = 0; l < L; ++l) {
-        uint4 l2 = __ldg(levels + l + 2);  // levels has num_levels + 2 entries
-        uint4 nr = make_uint4(0, 0, 0, 0);
-        if (l1.x + tid < l2.x) nr = __ldg(rec + l1.x + tid);
-        uint32_t c = l0.x + tid;
-        if (c < l1.x) {
-            project(sx, r, c, l0, inv_dt_sq);
-            for (c += T; c < l1.x; c += T) project(sx, __ldg(rec + c), c, l0, inv_dt_sq);
-        }
-        cta_sync<T>();
-        l0 = l1;
-        l1 = l2;
-        r = nr;
+    // prologue: stage levels 0 .. kRingDepth - 1 (levels has L + 2 entries)
+#pragma unroll
+    for (int k = 0; k < kRingDepth; ++k) {
+        if (uint32_t(k) <= L) ring_stage<T>(ring, levels, rec, k, L, __ldg(levels + k), __ldg(levels + k + 1).x);
+        cp_async_commit();
     }
+    cp_async_wait<kRingDepth - 1>();
+    __syncthreads();
+    for (uint32_t l = 0; l < L; ++l) {
+        const uint32_t ahead = l + kRingDepth;
+        uint4 lv_ahead = make_uint4(0, 0, 0, 0);
+        uint32_t next_ahead = 0;
+        if (ahead <= L) {
+            lv_ahead = __ldg(levels + ahead);
+            next_ahead = __ldg(levels + ahead + 1).x;
+        }
+        const uint32_t pos = l % kRingLevels;
+        const uint4 lv = ring.desc[pos];
+        const uint32_t n = ring.desc[(l + 1) % kRingLevels].x - lv.x;
+        const bool in_ring = n <= kRingSlots;
+        const uint4 *src = in_ring ? ring.rec + pos * kRingSlots : rec + lv.x;
+        for (uint32_t s = tid; s < n; s += T) {
+            const uint4 r = src[s];
+            if (r.x != 0xffffffffu) project(sx, r, slot_type(lv, s), inv_dt_sq);
+        }
+        if (ahead <= L) ring_stage<T>(ring, levels, rec, ahead, L, lv_ahead, next_ahead);
+        cp_async_commit();
+        cp_async_wait<kRingDepth - 1>();
+        cta_sync<T>();
+    }
+    cp_async_wait<0>();
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -344,17 +419,28 @@ __device__ __forceinline__ float reduce_sum(Shared &sh, float v, int slot) {
 // ---------------------------------------------------------------------------------------------
 // One body, one step
 // ---------------------------------------------------------------------------------------------
-template <int T>
-__device__ void step_body(const StepParams &p, uint32_t b, float4 *sx, Shared &sh, float *s_face) {
+// Shared memory of one CTA (dynamic part), cap = the launch's largest vertex count:
+//   kSmemState:  x[cap] | v[cap] (shape index in v.w) | prev[cap] | faces[...]
+//   otherwise:   x[cap] | faces[...]       (v, prev, shape stay in HBM)
+// faces: per-face triple product, then per-face pressure impulse (pressure bodies only).
+template <int T, bool kSmemState>
+__device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_t cap, Shared &sh) {
     const uint32_t tid = threadIdx.x;
     const BodyDesc d = p.bodies[b];
     BodyState *st = p.states + b;
     const uint32_t nv = d.num_vertices;
-    float4 *gx = p.x + d.vtx_offset;
-    float4 *gv = p.v + d.vtx_offset;
-    float4 *gprev = p.prev + d.vtx_offset;
-    float4 *gplane = p.plane + d.vtx_offset;
-    int32_t *gshape = p.shape + d.vtx_offset;
+    float4 *__restrict__ gx = p.x + d.vtx_offset;
+    float4 *__restrict__ gv = p.v + d.vtx_offset;
+    float4 *__restrict__ gprev = p.prev + d.vtx_offset;
+    float4 *__restrict__ gplane = p.plane + d.vtx_offset;
+    int32_t *__restrict__ gshape = p.shape + d.vtx_offset;
+    float4 *sx = smem;
+    float4 *sv = smem + cap;
+    float4 *sprev = smem + 2 * cap;
+    float4 *sface = smem + (kSmemState ? 3 * cap : cap);  // pressure faces; the record ring reuses it
+    LevelRing ring;
+    ring.rec = reinterpret_cast<uint4 *>(sface);
+    ring.desc = sh.ring_desc;
 
     // InitializeUpdateContext (identity body rotation)
     const f3 g = d.gravity_factor * ld3(p.gravity);
@@ -398,11 +484,14 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *sx, Shared &s
         }
         sh.ncols = n;
     }
-    // Stage positions in shared memory.
-    for (uint32_t i = tid; i < nv; i += T) sx[i] = gx[i];
+    // Stage the state in shared memory.
+    for (uint32_t i = tid; i < nv; i += T) {
+        sx[i] = gx[i];
+        if (kSmemState) sv[i] = gv[i];
+    }
     __syncthreads();
 
-    // DetermineCollisionPlanes
+    // DetermineCollisionPlanes (per vertex, once per step)
     const int ncols = sh.ncols;
     for (uint32_t i = tid; i < nv; i += T) {
         float4 pi = sx[i];
@@ -417,7 +506,10 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *sx, Shared &s
                     collide_sphere(xyz(pi), sh.cols[s], s, largest, plane, shape);
             }
         }
-        gshape[i] = shape;
+        if (kSmemState)
+            sv[i].w = __int_as_float(shape);
+        else
+            gshape[i] = shape;
         if (shape >= 0) gplane[i] = plane;
     }
 
@@ -433,31 +525,37 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *sx, Shared &s
     for (uint32_t it = 0; it < n_it; ++it) {
         // ApplyPressure
         if (has_pressure) {
+            float *s_six = reinterpret_cast<float *>(sface);
             for (uint32_t f = tid; f < d.num_faces; f += T) {
                 uint4 fc = __ldg(d.faces + f);
-                s_face[f] = dot(cross(xyz(sx[fc.x]), xyz(sx[fc.y])), xyz(sx[fc.z]));
+                s_six[f] = dot(cross(xyz(sx[fc.x]), xyz(sx[fc.y])), xyz(sx[fc.z]));
             }
             __syncthreads();
-            if (tid == 0) {
+            if (tid == 0) {  // the reference sums the faces sequentially
                 float six = 0.0f;
-                for (uint32_t f = 0; f < d.num_faces; ++f) six = six + s_face[f];
+                for (uint32_t f = 0; f < d.num_faces; ++f) six = six + s_six[f];
                 sh.six_volume = six;
             }
             __syncthreads();
             const float six = sh.six_volume;
             if (six > 0.0f) {
-                const float coefficient = d.pressure * dt_sub / six;
+                const float coefficient = jdiv(d.pressure * dt_sub, six);
+                for (uint32_t f = tid; f < d.num_faces; f += T) {
+                    uint4 fc = __ldg(d.faces + f);
+                    f3 x1 = xyz(sx[fc.x]), x2 = xyz(sx[fc.y]), x3 = xyz(sx[fc.z]);
+                    sface[f] = with_w(coefficient * cross(x2 - x1, x3 - x1), 0.0f);
+                }
+                __syncthreads();
                 for (uint32_t i = tid; i < nv; i += T) {
                     const float w = sx[i].w;
-                    float4 vel = gv[i];
+                    float4 vel = kSmemState ? sv[i] : gv[i];
                     f3 v = xyz(vel);
-                    for (uint32_t k = __ldg(d.vf_off + i), ke = __ldg(d.vf_off + i + 1); k < ke; ++k) {
-                        uint4 fc = __ldg(d.faces + __ldg(d.vf + k));
-                        f3 x1 = xyz(sx[fc.x]), x2 = xyz(sx[fc.y]), x3 = xyz(sx[fc.z]);
-                        f3 impulse = coefficient * cross(x2 - x1, x3 - x1);
-                        v = v + w * impulse;
-                    }
-                    gv[i] = with_w(v, vel.w);
+                    for (uint32_t k = __ldg(d.vf_off + i), ke = __ldg(d.vf_off + i + 1); k < ke; ++k)
+                        v = v + w * xyz(sface[__ldg(d.vf + k)]);
+                    if (kSmemState)
+                        sv[i] = with_w(v, vel.w);
+                    else
+                        gv[i] = with_w(v, vel.w);
                 }
             }
             __syncthreads();
@@ -465,30 +563,36 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *sx, Shared &s
         // IntegratePositions
         for (uint32_t i = tid; i < nv; i += T) {
             float4 pi = sx[i];
-            float4 vel = gv[i];
+            float4 vel = kSmemState ? sv[i] : gv[i];
             f3 v = xyz(vel);
             if (pi.w > 0.0f) {
                 v = v + (sub_g + sub_imp * pi.w);
                 v = v * damp;
             }
-            gprev[i] = pi;
-            f3 x = xyz(pi) + v * dt_sub;
-            sx[i] = with_w(x, pi.w);
-            gv[i] = with_w(v, vel.w);
+            if (kSmemState) {
+                sprev[i] = pi;
+                sv[i] = with_w(v, vel.w);
+            } else {
+                gprev[i] = pi;
+                gv[i] = with_w(v, vel.w);
+            }
+            sx[i] = with_w(xyz(pi) + v * dt_sub, pi.w);
         }
         __syncthreads();
         // Update groups in dependency-level order
-        apply_levels<T>(sx, d, inv_dt_sq);
+        apply_levels<T>(sx, d, inv_dt_sq, ring);
         __syncthreads();
         // ApplyCollisionConstraintsAndUpdateVelocities (static colliders)
         for (uint32_t i = tid; i < nv; i += T) {
             float4 pi = sx[i];
             if (!(pi.w > 0.0f)) continue;
             f3 x = xyz(pi);
-            float4 vel = gv[i];
+            float4 vel = kSmemState ? sv[i] : gv[i];
+            float4 prev = kSmemState ? sprev[i] : gprev[i];
             f3 prev_v = xyz(vel);
-            f3 v = (x - xyz(gprev[i])) / dt_sub;
-            int shape = ncols > 0 ? gshape[i] : -1;
+            f3 v = (x - xyz(prev)) / dt_sub;
+            int shape = -1;
+            if (ncols > 0) shape = kSmemState ? __float_as_int(vel.w) : gshape[i];
             if (shape >= 0) {
                 float4 pl = gplane[i];
                 f3 n = xyz(pl);
@@ -501,7 +605,7 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *sx, Shared &s
                     f3 v_tan = v - v_normal;
                     float vtl = len(v_tan);
                     if (vtl > 0.0f) {
-                        float fr = cs.friction * projected / (vtl * dt_sub);
+                        float fr = jdiv(cs.friction * projected, vtl * dt_sub);
                         fr = fr > 1.0f ? 1.0f : fr;
                         v = v - v_tan * fr;
                     }
@@ -510,7 +614,10 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *sx, Shared &s
                     if (pvn < restitution_threshold) v = v - (cs.restitution * pvn) * n;
                 }
             }
-            gv[i] = with_w(v, vel.w);
+            if (kSmemState)
+                sv[i] = with_w(v, vel.w);
+            else
+                gv[i] = with_w(v, vel.w);
         }
         __syncthreads();
     }
@@ -529,11 +636,11 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *sx, Shared &s
     bool finite = true;
     for (uint32_t i = tid; i < nv; i += T) {
         float4 pi = sx[i];
-        float4 vel = gv[i];
+        float4 vel = kSmemState ? sv[i] : gv[i];
         f3 v = xyz(vel), x = xyz(pi);
         float vsq = len_sq(v);
-        if (vsq > max_sq) v = v * sqrtf(max_sq / vsq);
-        gv[i] = with_w(v, vel.w);
+        if (vsq > max_sq) v = v * jsqrt(jdiv(max_sq, vsq));
+        gv[i] = with_w(v, 0.0f);
         lin = lin + v;
         ang = ang + cross(x, v);
         f3 pred = (x + v * dt) + disp_g;
@@ -567,7 +674,6 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *sx, Shared &s
     sums[3] = reduce_sum<T>(sh, ang.x, 3);
     sums[4] = reduce_sum<T>(sh, ang.y, 0);
     sums[5] = reduce_sum<T>(sh, ang.z, 1);
-    __shared__ float s_delta[3];
     if (tid == 0) {
         f3 bmin = mk(mm[0], mm[1], mm[2]), bmax = mk(xx[0], xx[1], xx[2]);
         f3 pmin = mk(pm[0], pm[1], pm[2]), pmax = mk(px[0], px[1], px[2]);
@@ -593,10 +699,10 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *sx, Shared &s
         st3(st->pmin, pmin);
         st3(st->pmax, pmax);
         st3(st->position, pos);
-        st3(s_delta, delta);
+        st3(sh.delta, delta);
     }
     __syncthreads();
-    const f3 delta = ld3(s_delta);
+    const f3 delta = ld3(sh.delta);
     const bool shift = (d.flags & kFlagUpdatePosition) != 0;
     for (uint32_t i = tid; i < nv; i += T) {
         float4 pi = sx[i];
@@ -605,79 +711,63 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *sx, Shared &s
     __syncthreads();
 }
 
-template <int T>
-__global__ void __launch_bounds__(T) step_kernel(StepParams p, uint32_t face_offset_floats) {
+template <int T, bool kSmemState>
+__global__ void __launch_bounds__(T) step_kernel(StepParams p, uint32_t cap) {
     extern __shared__ float4 smem[];
     __shared__ Shared sh;
-    float4 *sx = smem;
-    float *s_face = reinterpret_cast<float *>(smem) + face_offset_floats;
     for (;;) {
         if (threadIdx.x == 0) sh.item = atomicAdd(p.queue, 1u);
         __syncthreads();
         const uint32_t item = sh.item;
         __syncthreads();
         if (item >= p.num_work) return;
-        step_body<T>(p, p.work[item], sx, sh, s_face);
+        step_body<T, kSmemState>(p, p.work[item], smem, cap, sh);
     }
 }
 
 }  // namespace
 
+// Bytes of dynamic shared memory for a launch whose largest body has `vertices` vertices and whose
+// largest pressurised body has `faces` faces.
+size_t step_smem_bytes(bool smem_state, uint32_t vertices, uint32_t faces) {
+    size_t faces_bytes = size_t(faces) * sizeof(float4);
+    return size_t(vertices) * sizeof(float4) * (smem_state ? 3 : 1) + (faces_bytes > kRingBytes ? faces_bytes : kRingBytes);
+}
+
+#define JSB_FOR_EACH_SHAPE(X) X(32, true) X(64, true) X(128, true) X(256, true) X(32, false) X(64, false) X(128, false) X(256, false)
+
 // Launches one persistent step over `p.num_work` bodies with `threads` threads per CTA.
-// smem_vertices / smem_faces size the dynamic shared memory (largest body of the launch).
-cudaError_t launch_step(const StepParams &p, int threads, uint32_t smem_vertices, uint32_t smem_faces, int grid,
+cudaError_t launch_step(const StepParams &p, int threads, bool smem_state, uint32_t smem_vertices, uint32_t smem_faces, int grid,
                         cudaStream_t stream) {
-    size_t face_off = size_t(smem_vertices) * 4;  // in floats
-    size_t smem = size_t(smem_vertices) * sizeof(float4) + size_t(smem_faces) * sizeof(float);
-    switch (threads) {
-        case 32:
-            step_kernel<32><<<grid, 32, smem, stream>>>(p, uint32_t(face_off));
-            break;
-        case 64:
-            step_kernel<64><<<grid, 64, smem, stream>>>(p, uint32_t(face_off));
-            break;
-        case 128:
-            step_kernel<128><<<grid, 128, smem, stream>>>(p, uint32_t(face_off));
-            break;
-        case 256:
-            step_kernel<256><<<grid, 256, smem, stream>>>(p, uint32_t(face_off));
-            break;
-        default:
-            return cudaErrorInvalidValue;
+    size_t smem = step_smem_bytes(smem_state, smem_vertices, smem_faces);
+#define JSB_LAUNCH(TT, SS)                                                      \
+    if (threads == TT && smem_state == SS) {                                    \
+        step_kernel<TT, SS><<<grid, TT, smem, stream>>>(p, smem_vertices);      \
+        return cudaGetLastError();                                              \
     }
-    return cudaGetLastError();
+    JSB_FOR_EACH_SHAPE(JSB_LAUNCH)
+#undef JSB_LAUNCH
+    return cudaErrorInvalidValue;
 }
 
 // Allows every solver kernel instance to use up to `max_dynamic_smem` bytes of dynamic shared memory
 // (done once per device, outside any stream capture).
 cudaError_t init_step_kernels(int max_dynamic_smem) {
     cudaError_t e = cudaSuccess;
-    e = cudaFuncSetAttribute(step_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+#define JSB_ATTR(TT, SS) \
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel<TT, SS>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+    JSB_FOR_EACH_SHAPE(JSB_ATTR)
+#undef JSB_ATTR
     return e;
 }
 
-// Occupancy of step_kernel<threads> with the given dynamic shared memory (CTAs per SM).
-int step_occupancy(int threads, size_t smem) {
+// Occupancy of step_kernel (CTAs per SM) for a launch shape and dynamic shared memory size.
+int step_occupancy(int threads, bool smem_state, size_t smem) {
     int n = 0;
-    switch (threads) {
-        case 32:
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<32>, 32, smem);
-            break;
-        case 64:
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<64>, 64, smem);
-            break;
-        case 128:
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<128>, 128, smem);
-            break;
-        case 256:
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<256>, 256, smem);
-            break;
-        default:
-            return 0;
-    }
+#define JSB_OCC(TT, SS) \
+    if (threads == TT && smem_state == SS) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<TT, SS>, TT, smem);
+    JSB_FOR_EACH_SHAPE(JSB_OCC)
+#undef JSB_OCC
     return n;
 }
 
