@@ -169,6 +169,49 @@ jsb_status jsb_last_kernel_ms(jsb_context *ctx, float *ms_per_step);
  * space separated "key=value" list. Call with out == NULL to query *len. */
 jsb_status jsb_scene_build(const char *name, const char *params, void *out, size_t capacity, size_t *len);
 
+
+/* ---- allocation-free single-body step -------------------------------------------------------- */
+/* Body record in device memory for jsb_step_body_noalloc: the body's world position, its local bounds
+ * and predicted bounds (SoftBodyMotionProperties mLocalBounds / mLocalPredictedBounds, which the next
+ * step's collider query uses), and the linear / angular velocity the step writes. */
+typedef struct jsb_body_state {
+    float position[3];
+    float bounds_min[3], bounds_max[3];
+    float predicted_min[3], predicted_max[3];
+    float linear_velocity[3], angular_velocity[3];
+} jsb_body_state;
+
+/* Limits of jsb_step_body_noalloc: its scratch is a fixed array in the library's device memory. */
+#define JSB_NOALLOC_MAX_VERTICES 16384
+#define JSB_NOALLOC_MAX_SLOTS 65536   /* constraint slots of the padded schedule (constraints + padding) */
+#define JSB_NOALLOC_MAX_LEVELS 8192   /* dependency levels per substep */
+#define JSB_NOALLOC_MAX_FACES 16384
+#define JSB_NOALLOC_MAX_COLLIDERS 16
+
+/* One full step of ONE body without any device allocation (this entry point has no counterpart in
+ * the reference; it is an addition for callers that cannot call cudaMalloc: engines that own all
+ * device memory through their own fixed arenas or budgets, and frame loops that must not hit the
+ * implicit synchronisation and latency spikes of a device allocation).
+ *
+ * The caller passes the settings bytes (SoftBodySharedSettings::SaveBinaryState) and creation
+ * settings on the host, and the body's state in its own device memory: x_device = float4[N]
+ * (local position, inverse mass in w), v_device = float4[N] (velocity, w ignored), state_device, and
+ * error_device (device-side error bits of jsb_synchronize's codes OR-ed in: 1 non-finite, 2 too many
+ * colliders; clear it before the call). Colliders, gravity and force are host values.
+ *
+ * Scratch (the constraint schedule, per-vertex previous positions, collision planes and shape indices)
+ * lives in one static device array of about 2.3 MB that every GPU loading the library holds until
+ * exit; sizes beyond the JSB_NOALLOC_* limits are rejected with JSB_ERR_CAPACITY. The first call on a
+ * device resolves the array's device address (cudaGetSymbolAddress) and sets the kernel's shared
+ * memory limit; make that first call before any stream capture. Every call shares the array and
+ * leaves its contents behind (nothing in it needs to start at zero: each call overwrites what it
+ * reads); calls whose work overlaps on the GPU (several streams, or host threads) race on it, so
+ * serialise them. */
+jsb_status jsb_step_body_noalloc(const void *settings_blob, size_t len, const jsb_creation_settings *creation,
+                                 const jsb_collider *colliders, uint32_t num_colliders, const float gravity[3],
+                                 const float force[3], float dt, void *x_device, void *v_device,
+                                 jsb_body_state *state_device, uint32_t *error_device, jsb_stream stream);
+
 #ifdef __cplusplus
 }
 #endif

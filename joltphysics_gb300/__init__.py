@@ -55,6 +55,8 @@ SIGNATURES = {
     "jsb_last_launch_count": [_P, _c.POINTER(_c.c_uint32)],
     "jsb_last_kernel_ms": [_P, _c.POINTER(_c.c_float)],
     "jsb_scene_build": [_c.c_char_p, _c.c_char_p, _P, _c.c_size_t, _c.POINTER(_c.c_size_t)],
+    "jsb_step_body_noalloc": [_c.c_char_p, _c.c_size_t, _c.c_char_p, _c.c_char_p, _c.c_uint32, _c.POINTER(_c.c_float),
+                              _c.POINTER(_c.c_float), _c.c_float, _P, _P, _P, _P, _P],
 }
 
 

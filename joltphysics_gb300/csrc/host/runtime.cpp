@@ -129,6 +129,10 @@ struct LaunchGroup {  // bodies sharing one launch shape
 };
 
 }  // namespace
+
+// Lets other translation units of the library report failures through jsb_last_error_string.
+jsb_status report_error(jsb_status code, const std::string &msg) { return fail(code, msg); }
+
 }  // namespace jsb
 
 struct jsb_context {

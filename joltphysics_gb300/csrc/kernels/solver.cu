@@ -772,3 +772,254 @@ int step_occupancy(int threads, bool smem_state, size_t smem) {
 }
 
 }  // namespace jsb
+
+// =============================================================================================
+// Allocation-free single-body step (jsb_step_body_noalloc)
+// =============================================================================================
+// For callers that cannot call cudaMalloc (engines whose device memory all comes from their own
+// fixed arenas, frame loops that must not pay a device allocation's implicit synchronisation): the
+// step kernel's scratch -- the body's constraint schedule, previous positions, collision planes and
+// shape indices -- lives in the static array below instead of context buffers. The caller owns the
+// inputs and outputs (vertex state, body record, error word) in its own device memory.
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../../include/jsb.h"
+#include "../host/schedule.h"
+
+namespace jsb {
+
+jsb_status report_error(jsb_status code, const std::string &msg);
+
+namespace noalloc {
+
+constexpr uint32_t kMaxVertices = JSB_NOALLOC_MAX_VERTICES;
+constexpr uint32_t kMaxSlots = JSB_NOALLOC_MAX_SLOTS;
+constexpr uint32_t kMaxLevels = JSB_NOALLOC_MAX_LEVELS;
+constexpr uint32_t kMaxFaces = JSB_NOALLOC_MAX_FACES;
+constexpr uint32_t kMaxColliders = JSB_NOALLOC_MAX_COLLIDERS;
+static_assert(kMaxColliders <= kMaxCollidingShapes, "collider limit");
+
+// Layout of the scratch array, in float4 units.
+constexpr size_t kOffPrev = 0;
+constexpr size_t kOffPlane = kOffPrev + kMaxVertices;
+constexpr size_t kOffShape = kOffPlane + kMaxVertices;             // int32[kMaxVertices]
+constexpr size_t kOffLevels = kOffShape + kMaxVertices / 4;        // uint4[kMaxLevels + 2]
+constexpr size_t kOffRecords = kOffLevels + kMaxLevels + 2;        // uint4[kMaxSlots]
+constexpr size_t kOffFaces = kOffRecords + kMaxSlots;              // uint4[kMaxFaces]
+constexpr size_t kOffVfOff = kOffFaces + kMaxFaces;                // uint32[kMaxVertices + 4]
+constexpr size_t kOffVf = kOffVfOff + (kMaxVertices + 4) / 4;      // uint32[3 * kMaxFaces]
+constexpr size_t kScratchFloat4 = kOffVf + (3 * kMaxFaces) / 4;    // about 2.3 MB
+
+static __device__ __align__(256) float4 g_scratch[kScratchFloat4];
+
+struct Params {
+    BodyDesc desc;
+    BodyState *state;
+    float4 *x, *v;
+    float4 *prev, *plane;
+    int32_t *shape;
+    ColliderDev colliders[kMaxColliders];
+    uint32_t num_colliders;
+    float gravity[3];
+    float dt;
+    float force[3];
+    float zero3[3];
+    uint32_t zero_work;
+    uint32_t *error;
+};
+
+template <int T, bool kSmemState>
+__global__ void __launch_bounds__(T) step_kernel_noalloc(const __grid_constant__ Params q, uint32_t cap) {
+    extern __shared__ float4 smem[];
+    __shared__ Shared sh;
+    StepParams p;
+    p.bodies = &q.desc;
+    p.states = q.state;
+    p.work = &q.zero_work;
+    p.num_work = 1;
+    p.queue = nullptr;
+    p.x = q.x;
+    p.v = q.v;
+    p.prev = q.prev;
+    p.plane = q.plane;
+    p.shape = q.shape;
+    p.colliders = q.colliders;
+    p.num_colliders = q.num_colliders;
+    p.gravity[0] = q.gravity[0];
+    p.gravity[1] = q.gravity[1];
+    p.gravity[2] = q.gravity[2];
+    p.dt = q.dt;
+    p.error = q.error;
+    p.forces = q.force;
+    p.step_forces = q.zero3;
+    step_body<T, kSmemState>(p, 0, smem, cap, sh);
+}
+
+constexpr int kThreads = 128;
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mutex;
+float4 *g_scratch_ptr[kMaxDevices] = {};
+size_t g_smem_limit[kMaxDevices] = {};
+
+// Once per device, with that device current: the device address of the scratch array (a host-side
+// reference to g_scratch is not a device address) and the kernel's dynamic shared memory limit.
+jsb_status setup(int device, float4 **scratch, size_t *smem_limit) {
+    if (device < 0 || device >= kMaxDevices) return report_error(JSB_ERR_INVALID_ARGUMENT, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    if (!g_scratch_ptr[device]) {
+        void *ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_scratch);
+        if (e != cudaSuccess || !ptr)
+            return report_error(JSB_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+        int optin = 0;
+        e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+        if (e != cudaSuccess) return report_error(JSB_ERR_CUDA, std::string("cudaDeviceGetAttribute: ") + cudaGetErrorString(e));
+        const int limit = optin - 4096;
+        e = cudaFuncSetAttribute(step_kernel_noalloc<kThreads, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(step_kernel_noalloc<kThreads, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
+        if (e != cudaSuccess) return report_error(JSB_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+        g_smem_limit[device] = size_t(limit);
+        g_scratch_ptr[device] = static_cast<float4 *>(ptr);
+    }
+    *scratch = g_scratch_ptr[device];
+    *smem_limit = g_smem_limit[device];
+    return JSB_OK;
+}
+
+}  // namespace noalloc
+}  // namespace jsb
+
+extern "C" jsb_status jsb_step_body_noalloc(const void *settings_blob, size_t len, const jsb_creation_settings *creation,
+                                            const jsb_collider *colliders, uint32_t num_colliders, const float gravity[3],
+                                            const float force[3], float dt, void *x_device, void *v_device,
+                                            jsb_body_state *state_device, uint32_t *error_device, jsb_stream stream) {
+    using namespace jsb;
+    using namespace jsb::noalloc;
+    static_assert(sizeof(jsb_body_state) == sizeof(BodyState), "jsb_body_state layout");
+    if (!settings_blob || !creation || !gravity || !x_device || !v_device || !state_device || !error_device ||
+        (num_colliders && !colliders))
+        return report_error(JSB_ERR_INVALID_ARGUMENT, "null argument");
+    if (!(dt > 0.0f) || creation->num_iterations < 1)
+        return report_error(JSB_ERR_INVALID_ARGUMENT, "dt must be > 0 and num_iterations >= 1");
+    if (!creation->make_rotation_identity)
+        return report_error(JSB_ERR_UNSUPPORTED, "bodies must keep an identity rotation (mMakeRotationIdentity = true)");
+    if (num_colliders > kMaxColliders)
+        return report_error(JSB_ERR_CAPACITY, "jsb_step_body_noalloc takes at most " + std::to_string(kMaxColliders) + " colliders");
+
+    // Host side: parse the settings and build the padded dependency-level schedule.
+    ParsedSettings ps;
+    bool unsupported = false;
+    std::string err = parse_settings(settings_blob, len, ps, unsupported);
+    if (!err.empty()) return report_error(unsupported ? JSB_ERR_UNSUPPORTED : JSB_ERR_BLOB, err);
+    const uint32_t nv = uint32_t(ps.vertices.size());
+    const bool pressure = creation->pressure > 0.0f;
+    const uint32_t nf = pressure ? uint32_t(ps.faces.size()) : 0u;
+    if (nv > kMaxVertices)
+        return report_error(JSB_ERR_CAPACITY, "body has " + std::to_string(nv) + " vertices; jsb_step_body_noalloc handles at most " +
+                                                  std::to_string(kMaxVertices));
+    if (nf > kMaxFaces)
+        return report_error(JSB_ERR_CAPACITY, "body has " + std::to_string(nf) + " pressure faces; jsb_step_body_noalloc handles at most " +
+                                                  std::to_string(kMaxFaces));
+    Schedule sched = build_schedule(ps);
+    if (sched.num_slots > kMaxSlots || sched.num_levels > kMaxLevels)
+        return report_error(JSB_ERR_CAPACITY, "constraint schedule of " + std::to_string(sched.num_slots) + " slots / " +
+                                                  std::to_string(sched.num_levels) + " levels exceeds jsb_step_body_noalloc's " +
+                                                  std::to_string(kMaxSlots) + " / " + std::to_string(kMaxLevels));
+    std::vector<uint32_t> vf_off(nv + 1, 0), vf;
+    std::vector<uint4> faces;
+    if (pressure) {
+        for (const auto &f : ps.faces)
+            for (int k = 0; k < 3; ++k) vf_off[f.v[k] + 1]++;
+        for (uint32_t i = 0; i < nv; ++i) vf_off[i + 1] += vf_off[i];
+        vf.resize(vf_off[nv]);
+        std::vector<uint32_t> fill(vf_off.begin(), vf_off.end() - 1);
+        for (uint32_t fi = 0; fi < nf; ++fi)
+            for (int k = 0; k < 3; ++k) vf[fill[ps.faces[fi].v[k]]++] = fi;
+        faces.resize(nf);
+        for (uint32_t fi = 0; fi < nf; ++fi) faces[fi] = make_uint4(ps.faces[fi].v[0], ps.faces[fi].v[1], ps.faces[fi].v[2], 0);
+    }
+
+    // Device side: scratch address (set-up on the first call on this device), then stage the schedule.
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess) return report_error(JSB_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    float4 *scratch = nullptr;
+    size_t smem_limit = 0;
+    jsb_status st = setup(device, &scratch, &smem_limit);
+    if (st != JSB_OK) return st;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    auto copy = [&](size_t off_float4, const void *src, size_t bytes) {
+        return bytes ? cudaMemcpyAsync(scratch + off_float4, src, bytes, cudaMemcpyHostToDevice, s) : cudaSuccess;
+    };
+    e = copy(kOffLevels, sched.padded_levels.data(), sched.padded_levels.size() * sizeof(uint32_t));
+    if (e == cudaSuccess) e = copy(kOffRecords, sched.padded_records.data(), sched.padded_records.size() * sizeof(uint32_t));
+    if (e == cudaSuccess && pressure) e = copy(kOffFaces, faces.data(), faces.size() * sizeof(uint4));
+    if (e == cudaSuccess && pressure) e = copy(kOffVfOff, vf_off.data(), vf_off.size() * sizeof(uint32_t));
+    if (e == cudaSuccess && pressure) e = copy(kOffVf, vf.data(), vf.size() * sizeof(uint32_t));
+    if (e != cudaSuccess) return report_error(JSB_ERR_CUDA, std::string("cudaMemcpyAsync(schedule): ") + cudaGetErrorString(e));
+
+    Params q = {};
+    BodyDesc &d = q.desc;
+    d.levels = reinterpret_cast<const uint4 *>(scratch + kOffLevels);
+    d.records = reinterpret_cast<const uint4 *>(scratch + kOffRecords);
+    d.faces = reinterpret_cast<const uint4 *>(scratch + kOffFaces);
+    d.vf_off = reinterpret_cast<const uint32_t *>(scratch + kOffVfOff);
+    d.vf = reinterpret_cast<const uint32_t *>(scratch + kOffVf);
+    d.num_levels = sched.num_levels;
+    d.num_records = sched.num_slots;
+    d.num_faces = pressure ? nf : 0u;
+    d.num_vertices = nv;
+    d.vtx_offset = 0;
+    d.num_iterations = creation->num_iterations;
+    d.linear_damping = creation->linear_damping;
+    d.max_linear_velocity = creation->max_linear_velocity;
+    d.restitution = creation->restitution;
+    d.friction = creation->friction;
+    d.pressure = creation->pressure;
+    d.gravity_factor = creation->gravity_factor;
+    d.vertex_radius = creation->vertex_radius;
+    d.flags = creation->update_position ? kFlagUpdatePosition : 0u;
+    q.state = reinterpret_cast<BodyState *>(state_device);
+    q.x = static_cast<float4 *>(x_device);
+    q.v = static_cast<float4 *>(v_device);
+    q.prev = scratch + kOffPrev;
+    q.plane = scratch + kOffPlane;
+    q.shape = reinterpret_cast<int32_t *>(scratch + kOffShape);
+    for (uint32_t i = 0; i < num_colliders; ++i) {
+        ColliderDev &c = q.colliders[i];
+        c.type = colliders[i].type;
+        for (int k = 0; k < 3; ++k) {
+            c.position[k] = colliders[i].position[k];
+            c.half_extent[k] = colliders[i].half_extent[k];
+        }
+        c.radius = colliders[i].radius;
+        c.friction = colliders[i].friction;
+        c.restitution = colliders[i].restitution;
+    }
+    q.num_colliders = num_colliders;
+    for (int k = 0; k < 3; ++k) {
+        q.gravity[k] = gravity[k];
+        q.force[k] = force ? force[k] : 0.0f;
+        q.zero3[k] = 0.0f;
+    }
+    q.dt = dt;
+    q.zero_work = 0;
+    q.error = error_device;
+
+    // Whole vertex state in shared memory when it fits, else positions only (as in the batched path).
+    const bool smem_state = step_smem_bytes(true, nv, nf) <= smem_limit;
+    const size_t smem = step_smem_bytes(smem_state, nv, nf);
+    if (smem > smem_limit)
+        return report_error(JSB_ERR_UNSUPPORTED, "body does not fit the shared-memory solver path");
+    if (smem_state)
+        step_kernel_noalloc<kThreads, true><<<1, kThreads, smem, s>>>(q, nv);
+    else
+        step_kernel_noalloc<kThreads, false><<<1, kThreads, smem, s>>>(q, nv);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return report_error(JSB_ERR_CUDA, std::string("step_kernel_noalloc: ") + cudaGetErrorString(e));
+    return JSB_OK;
+}
