@@ -243,7 +243,8 @@ def main():
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
     # autotune the launch shape per body-size bucket, then warm up (graph of one step)
-    ctx.autotune(trials=2)
+    ctx.autotune(trials=3)
+    buckets = [b for b in ctx.bucket_table()]
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             ctx.step_graph(1, 1, stream=sptr)
@@ -335,7 +336,8 @@ def main():
         "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "bodies": len(scene.bodies), "vertices": n_vertices, "iterations": 5,
                    "dt": scene.dt, "vertex_iterations_per_step": vi_step, "l2": "flushed before every timed step",
-                   "form": "batched persistent launches per size bucket, CUDA graph of one step"},
+                   "form": "batched persistent launches per size bucket, CUDA graph of one step",
+                   "buckets_max_vertices_threads_state": buckets},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
                 "steps": e2e_steps},
         "gpu_launches": launches,

@@ -151,9 +151,16 @@ jsb_status jsb_body_schedule_info(jsb_context *ctx, uint32_t body_id, uint32_t *
 jsb_status jsb_settings_schedule(const void *blob, size_t len, uint32_t *num_levels, uint32_t *num_records,
                                  uint32_t *levels, uint32_t *records, uint32_t *source);
 
-/* Threads per CTA used for bodies whose vertex count is <= max_vertices (bucket table written by
- * the autotuner; threads in {32, 64, 128, 256}). */
+/* Launch shape of the size bucket of bodies with vertex count <= max_vertices (and above the next
+ * smaller bucket): threads per CTA in {32, 64, 128, 256}; state_mode 0 keeps positions, velocities and
+ * previous positions in shared memory when they fit, 1 keeps only positions there. The autotuner
+ * writes this table; the calls below set or read it directly. */
+jsb_status jsb_set_bucket_config(jsb_context *ctx, uint32_t max_vertices, uint32_t threads, uint32_t state_mode);
 jsb_status jsb_set_bucket_threads(jsb_context *ctx, uint32_t max_vertices, uint32_t threads);
+jsb_status jsb_get_bucket_config(jsb_context *ctx, uint32_t index, uint32_t *max_vertices, uint32_t *threads,
+                                 uint32_t *state_mode);
+/* Tunes the bucket table on the context's own bodies (coordinate descent, each shape timed as a
+ * whole batched step); the bodies' state is restored afterwards. */
 jsb_status jsb_autotune(jsb_context *ctx, float dt, int trials);
 
 /* Kernel launches issued by the most recent jsb_step / jsb_step_plain / jsb_step_graph call. */

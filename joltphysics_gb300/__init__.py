@@ -50,7 +50,9 @@ SIGNATURES = {
     "jsb_total_vertices": [_P, _c.POINTER(_c.c_uint64)],
     "jsb_body_schedule_info": [_P, _c.c_uint32, _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32)],
     "jsb_settings_schedule": [_c.c_char_p, _c.c_size_t, _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32), _P, _P, _P],
+    "jsb_set_bucket_config": [_P, _c.c_uint32, _c.c_uint32, _c.c_uint32],
     "jsb_set_bucket_threads": [_P, _c.c_uint32, _c.c_uint32],
+    "jsb_get_bucket_config": [_P, _c.c_uint32, _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32)],
     "jsb_autotune": [_P, _c.c_float, _c.c_int],
     "jsb_last_launch_count": [_P, _c.POINTER(_c.c_uint32)],
     "jsb_last_kernel_ms": [_P, _c.POINTER(_c.c_float)],
@@ -230,6 +232,18 @@ class Context:
 
     def set_bucket_threads(self, max_vertices: int, threads: int):
         check(lib().jsb_set_bucket_threads(self.h, max_vertices, threads))
+
+    def set_bucket_config(self, max_vertices: int, threads: int, state_mode: int):
+        check(lib().jsb_set_bucket_config(self.h, max_vertices, threads, state_mode))
+
+    def bucket_table(self) -> list[tuple[int, int, int]]:
+        out, i = [], 0
+        while True:
+            mv, t, m = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+            if lib().jsb_get_bucket_config(self.h, i, ctypes.byref(mv), ctypes.byref(t), ctypes.byref(m)) != JSB_OK:
+                return out
+            out.append((mv.value, t.value, m.value))
+            i += 1
 
     # -- readback --------------------------------------------------------------------------------
     def read_body(self, body: int):

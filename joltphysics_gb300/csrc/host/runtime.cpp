@@ -32,7 +32,7 @@ namespace jsb {
 cudaError_t launch_step(const StepParams &p, int threads, bool smem_state, uint32_t smem_vertices, uint32_t smem_faces,
                         int grid, cudaStream_t stream);
 int step_occupancy(int threads, bool smem_state, size_t smem);
-size_t step_smem_bytes(bool smem_state, uint32_t vertices, uint32_t faces);
+size_t step_smem_bytes(bool smem_state, uint32_t vertices, uint32_t faces, uint32_t ring_slots);
 cudaError_t init_step_kernels(int max_dynamic_smem);
 cudaError_t launch_unpack_state(const float *pos3, const float *vel3, float4 *x, float4 *v, uint64_t n, int num_sms,
                                 cudaStream_t stream);
@@ -112,15 +112,19 @@ struct BodyRec {
     uint32_t vtx_offset = 0;
 };
 
+// Bodies are bucketed by vertex count; each bucket is one persistent launch per step with its own
+// threads per CTA and vertex-state placement, chosen by the autotuner.
 struct Bucket {
     uint32_t max_vertices;
     int threads;
+    int state_mode;  // 0: x, v, prev in shared memory when they fit; 1: only positions in shared memory
 };
 
-struct LaunchGroup {  // bodies sharing one launch shape
+struct LaunchGroup {  // the bodies of one bucket
     int threads = 0;
     bool smem_state = true;  // velocities / previous positions staged in shared memory
     uint32_t smem_vertices = 0, smem_faces = 0;
+    uint32_t ring_slots = 32;  // record ring capacity per level
     int grid = 0;
     std::vector<uint32_t> bodies;
     DevBuf<uint32_t> work;
@@ -146,6 +150,7 @@ struct jsb_context {
     std::vector<jsb::Bucket> buckets;
     // device state
     bool dirty = true;  // structure changed: device arrays must be rebuilt
+    bool groups_dirty = true;  // bucket table changed: launch groups must be rebuilt
     uint64_t total_vertices = 0;
     jsb::DevBuf<float4> x, v, prev, plane;
     jsb::DevBuf<int32_t> shape;
@@ -192,10 +197,10 @@ void drop_graph(jsb_context *ctx) {
     ctx->graph_steps = -1;
 }
 
-int threads_for(const jsb_context *ctx, uint32_t nv) {
-    for (const Bucket &b : ctx->buckets)
-        if (nv <= b.max_vertices) return b.threads;
-    return ctx->buckets.empty() ? 128 : ctx->buckets.back().threads;
+size_t bucket_for(const jsb_context *ctx, uint32_t nv) {
+    for (size_t i = 0; i < ctx->buckets.size(); ++i)
+        if (nv <= ctx->buckets[i].max_vertices) return i;
+    return ctx->buckets.size() - 1;
 }
 
 BodyDesc make_desc(const jsb_context *ctx, const BodyRec &b) {
@@ -229,15 +234,11 @@ uint32_t pressure_faces(const SettingsRec &s, const BodyRec &b) {
     return b.creation.pressure > 0.0f ? uint32_t(s.parsed.faces.size()) : 0u;
 }
 
-// Whether a body's whole vertex state (x, v, prev) fits in one CTA's shared memory; if not, only
-// the positions are staged there. Returns false in `fits` when even that does not fit.
-bool body_smem_state(const jsb_context *ctx, const SettingsRec &s, const BodyRec &b, bool &fits) {
-    uint32_t nv = uint32_t(s.parsed.vertices.size()), nf = pressure_faces(s, b);
-    const size_t cap = ctx->max_smem_optin - kStaticSmemReserve;
-    fits = true;
-    if (step_smem_bytes(true, nv, nf) <= cap) return true;
-    fits = step_smem_bytes(false, nv, nf) <= cap;
-    return false;
+constexpr uint32_t kMaxRingSlots = 256;
+
+uint32_t ring_slots_for(const SettingsRec &s) {
+    uint32_t r = (s.schedule.max_level_slots + 31u) & ~31u;
+    return std::max<uint32_t>(32u, std::min(r, kMaxRingSlots));
 }
 
 double body_cost(const SettingsRec &s, const BodyRec &b, int threads) {
@@ -251,9 +252,11 @@ double body_cost(const SettingsRec &s, const BodyRec &b, int threads) {
     return double(b.creation.num_iterations) * (levels + 4.0 * per_vertex);
 }
 
-// Rebuilds the device-side body tables and launch groups after structural changes.
+jsb_status rebuild_groups(jsb_context *ctx);
+
+// Rebuilds the device-side body tables (and then the launch groups) after structural changes.
 jsb_status rebuild(jsb_context *ctx) {
-    if (!ctx->dirty) return JSB_OK;
+    if (!ctx->dirty) return ctx->groups_dirty ? rebuild_groups(ctx) : JSB_OK;
     drop_graph(ctx);
     free_groups(ctx);
     // vertex layout
@@ -313,48 +316,62 @@ jsb_status rebuild(jsb_context *ctx) {
         JSB_CUDA(cudaMemset(ctx->error.ptr, 0, sizeof(uint32_t)));
     }
 
-    // launch groups: one per (threads per CTA, state-in-shared-memory) pair
-    std::vector<std::pair<int, bool>> shapes;
-    std::vector<std::pair<int, bool>> body_shape(ctx->bodies.size());
+    ctx->dirty = false;
+    ctx->groups_dirty = true;
+    return rebuild_groups(ctx);
+}
+
+// One launch group per non-empty bucket: dynamic shared memory sized for its largest body, ring
+// capacity for its widest level, bodies queued longest first.
+jsb_status rebuild_groups(jsb_context *ctx) {
+    drop_graph(ctx);
+    free_groups(ctx);
+    const size_t cap = ctx->max_smem_optin - kStaticSmemReserve;
+    std::vector<std::vector<std::pair<double, uint32_t>>> members(ctx->buckets.size());
     for (size_t bi = 0; bi < ctx->bodies.size(); ++bi) {
         const BodyRec &b = ctx->bodies[bi];
         const SettingsRec &s = *ctx->settings[b.settings_id];
-        bool fits = true;
-        bool smem_state = body_smem_state(ctx, s, b, fits);
-        if (!fits)
-            return fail(JSB_ERR_UNSUPPORTED, "body " + std::to_string(bi) + " with " + std::to_string(s.parsed.vertices.size()) +
-                                                 " vertices does not fit the shared-memory solver path");
-        body_shape[bi] = {threads_for(ctx, uint32_t(s.parsed.vertices.size())), smem_state};
-        if (std::find(shapes.begin(), shapes.end(), body_shape[bi]) == shapes.end()) shapes.push_back(body_shape[bi]);
+        size_t k = bucket_for(ctx, uint32_t(s.parsed.vertices.size()));
+        members[k].push_back({body_cost(s, b, ctx->buckets[k].threads), uint32_t(bi)});
     }
-    std::sort(shapes.begin(), shapes.end());
-    ctx->groups.resize(shapes.size());
-    for (size_t gi = 0; gi < shapes.size(); ++gi) {
-        LaunchGroup &g = ctx->groups[gi];
-        g.threads = shapes[gi].first;
-        g.smem_state = shapes[gi].second;
-        std::vector<std::pair<double, uint32_t>> items;
-        for (size_t bi = 0; bi < ctx->bodies.size(); ++bi) {
-            if (body_shape[bi] != shapes[gi]) continue;
-            const BodyRec &b = ctx->bodies[bi];
+    for (size_t k = 0; k < ctx->buckets.size(); ++k) {
+        if (members[k].empty()) continue;
+        ctx->groups.emplace_back();
+        LaunchGroup &g = ctx->groups.back();
+        g.threads = ctx->buckets[k].threads;
+        for (auto &m : members[k]) {
+            const BodyRec &b = ctx->bodies[m.second];
             const SettingsRec &s = *ctx->settings[b.settings_id];
             g.smem_vertices = std::max(g.smem_vertices, uint32_t(s.parsed.vertices.size()));
             g.smem_faces = std::max(g.smem_faces, pressure_faces(s, b));
-            items.push_back({body_cost(s, b, g.threads), uint32_t(bi)});
+            g.ring_slots = std::max(g.ring_slots, ring_slots_for(s));
         }
+        g.smem_state = ctx->buckets[k].state_mode == 0 && step_smem_bytes(true, g.smem_vertices, g.smem_faces, g.ring_slots) <= cap;
+        if (step_smem_bytes(g.smem_state, g.smem_vertices, g.smem_faces, g.ring_slots) > cap)
+            return fail(JSB_ERR_UNSUPPORTED, "a body with " + std::to_string(g.smem_vertices) +
+                                                 " vertices does not fit the shared-memory solver path");
         // Longest-processing-time-first order for the work queue.
-        std::stable_sort(items.begin(), items.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
-        for (auto &it : items) g.bodies.push_back(it.second);
+        std::stable_sort(members[k].begin(), members[k].end(), [](const auto &a, const auto &b) { return a.first > b.first; });
+        for (auto &m : members[k]) g.bodies.push_back(m.second);
         JSB_CUDA(g.work.upload(g.bodies.data(), g.bodies.size()));
-        size_t smem = step_smem_bytes(g.smem_state, g.smem_vertices, g.smem_faces);
+        size_t smem = step_smem_bytes(g.smem_state, g.smem_vertices, g.smem_faces, g.ring_slots);
         int occ = step_occupancy(g.threads, g.smem_state, smem);
         if (occ <= 0) return fail(JSB_ERR_UNSUPPORTED, "solver kernel does not fit on an SM with this shared memory size");
         g.grid = int(std::min<size_t>(g.bodies.size(), size_t(occ) * ctx->num_sms));
-        JSB_CUDA(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
         JSB_CUDA(cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming));
     }
-    JSB_CUDA(ctx->queues.alloc(std::max<size_t>(ctx->groups.size(), 1)));
-    ctx->dirty = false;
+    // Larger buckets get higher stream priority (and are launched first): their bodies carry the
+    // longest dependency chains, and a CTA sized for them needs an SM nobody else occupies.
+    int least = 0, greatest = 0;
+    JSB_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    const int ng = int(ctx->groups.size());
+    for (int gi = 0; gi < ng; ++gi) {
+        int prio = least;
+        if (ng > 1 && greatest != least) prio = least + (greatest - least) * gi / (ng - 1);
+        JSB_CUDA(cudaStreamCreateWithPriority(&ctx->groups[gi].stream, cudaStreamNonBlocking, prio));
+    }
+    if (ctx->queues.count < std::max<size_t>(ctx->groups.size(), 1)) JSB_CUDA(ctx->queues.alloc(std::max<size_t>(ctx->groups.size(), 1)));
+    ctx->groups_dirty = false;
     return JSB_OK;
 }
 
@@ -376,6 +393,7 @@ StepParams base_params(jsb_context *ctx, float dt) {
     p.error = ctx->error.ptr;
     p.forces = ctx->forces.ptr;
     p.step_forces = ctx->step_forces.ptr;
+    p.ring_slots = kMaxRingSlots;
     return p;
 }
 
@@ -384,13 +402,15 @@ jsb_status enqueue_batched(jsb_context *ctx, float dt, cudaStream_t stream, uint
     if (ctx->groups.empty()) return JSB_OK;
     JSB_CUDA(cudaMemsetAsync(ctx->queues.ptr, 0, ctx->queues.count * sizeof(uint32_t), stream));
     JSB_CUDA(cudaEventRecord(ctx->fork, stream));
-    for (size_t gi = 0; gi < ctx->groups.size(); ++gi) {
+    for (size_t k = ctx->groups.size(); k-- > 0;) {  // largest bucket first
+        const size_t gi = k;
         LaunchGroup &g = ctx->groups[gi];
         JSB_CUDA(cudaStreamWaitEvent(g.stream, ctx->fork, 0));
         StepParams p = base_params(ctx, dt);
         p.work = g.work.ptr;
         p.num_work = uint32_t(g.bodies.size());
         p.queue = ctx->queues.ptr + gi;
+        p.ring_slots = g.ring_slots;
         JSB_CUDA(launch_step(p, g.threads, g.smem_state, g.smem_vertices, g.smem_faces, g.grid, g.stream));
         ++launches;
         JSB_CUDA(cudaEventRecord(g.done, g.stream));
@@ -430,6 +450,7 @@ jsb_status step_impl(jsb_context *ctx, float dt, int collision_steps, cudaStream
                     p.num_work = 1;
                     p.queue = ctx->queues.ptr;
                     const SettingsRec &s = *ctx->settings[ctx->bodies[b].settings_id];
+                    p.ring_slots = ring_slots_for(s);
                     JSB_CUDA(launch_step(p, g.threads, g.smem_state, uint32_t(s.parsed.vertices.size()),
                                          pressure_faces(s, ctx->bodies[b]), 1, stream));
                     ++launches;
@@ -480,7 +501,8 @@ jsb_status jsb_context_create(int device, jsb_context **out) {
     ctx->device = device;
     ctx->num_sms = prop.multiProcessorCount;
     ctx->max_smem_optin = prop.sharedMemPerBlockOptin;
-    ctx->buckets = {{512, 32}, {2048, 64}, {65536, 128}};
+    ctx->buckets = {{128, 32, 0},   {256, 32, 0},   {512, 32, 0},   {1024, 64, 0},  {1536, 64, 0},
+                    {2048, 64, 0},  {3072, 128, 0}, {4096, 128, 0}, {8192, 128, 0}, {65536, 128, 0}};
     // static shared memory of the solver kernel is under 4 KB
     JSB_CUDA(init_step_kernels(int(ctx->max_smem_optin - kStaticSmemReserve)));
     JSB_CUDA(cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming));
@@ -872,19 +894,38 @@ jsb_status jsb_settings_schedule(const void *blob, size_t len, uint32_t *num_lev
     return JSB_OK;
 }
 
-jsb_status jsb_set_bucket_threads(jsb_context *ctx, uint32_t max_vertices, uint32_t threads) {
+jsb_status jsb_set_bucket_config(jsb_context *ctx, uint32_t max_vertices, uint32_t threads, uint32_t state_mode) {
     if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
     if (threads != 32 && threads != 64 && threads != 128 && threads != 256)
         return fail(JSB_ERR_INVALID_ARGUMENT, "threads must be 32, 64, 128 or 256");
+    if (state_mode > 1) return fail(JSB_ERR_INVALID_ARGUMENT, "state_mode must be 0 or 1");
     bool found = false;
     for (Bucket &b : ctx->buckets)
         if (b.max_vertices == max_vertices) {
             b.threads = int(threads);
+            b.state_mode = int(state_mode);
             found = true;
         }
-    if (!found) ctx->buckets.push_back({max_vertices, int(threads)});
+    if (!found) ctx->buckets.push_back({max_vertices, int(threads), int(state_mode)});
     std::sort(ctx->buckets.begin(), ctx->buckets.end(), [](const Bucket &a, const Bucket &b) { return a.max_vertices < b.max_vertices; });
-    ctx->dirty = true;
+    ctx->groups_dirty = true;
+    return JSB_OK;
+}
+
+jsb_status jsb_set_bucket_threads(jsb_context *ctx, uint32_t max_vertices, uint32_t threads) {
+    if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
+    uint32_t mode = 0;
+    for (const Bucket &b : ctx->buckets)
+        if (b.max_vertices == max_vertices) mode = uint32_t(b.state_mode);
+    return jsb_set_bucket_config(ctx, max_vertices, threads, mode);
+}
+
+jsb_status jsb_get_bucket_config(jsb_context *ctx, uint32_t index, uint32_t *max_vertices, uint32_t *threads, uint32_t *state_mode) {
+    if (!check_ctx(ctx) || !max_vertices || !threads || !state_mode) return fail(JSB_ERR_INVALID_ARGUMENT, "null argument");
+    if (index >= ctx->buckets.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bucket index out of range");
+    *max_vertices = ctx->buckets[index].max_vertices;
+    *threads = uint32_t(ctx->buckets[index].threads);
+    *state_mode = uint32_t(ctx->buckets[index].state_mode);
     return JSB_OK;
 }
 
@@ -900,14 +941,18 @@ jsb_status jsb_last_kernel_ms(jsb_context *ctx, float *ms) {
     return JSB_OK;
 }
 
-// Autotuner: for every bucket, time one batched step of only that bucket's bodies with each
-// threads-per-CTA choice and keep the fastest. Device state is saved before and restored after.
+// Autotuner: coordinate descent over the bucket table. For every occupied bucket (largest first) each
+// launch shape -- threads per CTA in {32, 64, 128, 256} x vertex state in shared / global memory -- is
+// tried with the other buckets fixed, and the one giving the fastest whole batched step (all buckets
+// running concurrently, as in jsb_step) is kept. Device state is saved before and restored after.
 jsb_status jsb_autotune(jsb_context *ctx, float dt, int trials) {
     if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
     if (trials < 1) trials = 1;
+    if (!(dt > 0.0f)) return fail(JSB_ERR_INVALID_ARGUMENT, "dt must be > 0");
     JSB_CUDA(cudaSetDevice(ctx->device));
     jsb_status st = rebuild(ctx);
     if (st != JSB_OK) return st;
+    if (ctx->bodies.empty()) return JSB_OK;
     const uint64_t n = ctx->total_vertices;
     DevBuf<float4> sx, sv;
     DevBuf<BodyState> ss;
@@ -917,63 +962,61 @@ jsb_status jsb_autotune(jsb_context *ctx, float dt, int trials) {
     JSB_CUDA(cudaMemcpy(sx.ptr, ctx->x.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice));
     JSB_CUDA(cudaMemcpy(sv.ptr, ctx->v.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice));
     JSB_CUDA(cudaMemcpy(ss.ptr, ctx->states.ptr, ctx->bodies.size() * sizeof(BodyState), cudaMemcpyDeviceToDevice));
-    std::vector<Bucket> tuned = ctx->buckets;
+    cudaStream_t stream;
+    JSB_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    auto measure = [&](float &ms_out) -> jsb_status {
+        jsb_status s2 = rebuild_groups(ctx);
+        if (s2 != JSB_OK) return s2;
+        std::vector<float> times;
+        for (int k = 0; k < trials + 1; ++k) {
+            uint32_t launches = 0;
+            JSB_CUDA(cudaEventRecord(ctx->t0, stream));
+            if ((s2 = enqueue_batched(ctx, dt, stream, launches)) != JSB_OK) return s2;
+            JSB_CUDA(cudaEventRecord(ctx->t1, stream));
+            JSB_CUDA(cudaEventSynchronize(ctx->t1));
+            float ms = 0.0f;
+            JSB_CUDA(cudaEventElapsedTime(&ms, ctx->t0, ctx->t1));
+            if (k > 0) times.push_back(ms);  // the first launch is a warm-up
+        }
+        std::sort(times.begin(), times.end());
+        ms_out = times[times.size() / 2];
+        return JSB_OK;
+    };
+    std::vector<size_t> occupied;
+    for (size_t k = 0; k < ctx->buckets.size(); ++k)
+        for (const BodyRec &b : ctx->bodies)
+            if (bucket_for(ctx, uint32_t(ctx->settings[b.settings_id]->parsed.vertices.size())) == k) {
+                occupied.push_back(k);
+                break;
+            }
+    float best_ms = 0.0f;
+    st = measure(best_ms);
     const int choices[4] = {32, 64, 128, 256};
-    for (size_t bi = 0; bi < tuned.size(); ++bi) {
-        uint32_t lo = bi == 0 ? 0 : tuned[bi - 1].max_vertices;
-        uint32_t hi = tuned[bi].max_vertices;
-        std::vector<uint32_t> members;
-        uint32_t max_nv = 0, max_faces = 0;
-        bool smem_state = true;
-        for (size_t b = 0; b < ctx->bodies.size(); ++b) {
-            const SettingsRec &s = *ctx->settings[ctx->bodies[b].settings_id];
-            uint32_t nv = uint32_t(s.parsed.vertices.size());
-            if (nv > lo && nv <= hi) {
-                members.push_back(uint32_t(b));
-                max_nv = std::max(max_nv, nv);
-                max_faces = std::max(max_faces, pressure_faces(s, ctx->bodies[b]));
-                bool fits = true;
-                smem_state = smem_state && body_smem_state(ctx, s, ctx->bodies[b], fits);
+    for (auto it = occupied.rbegin(); st == JSB_OK && it != occupied.rend(); ++it) {
+        Bucket &bk = ctx->buckets[*it];
+        Bucket best = bk;
+        for (int mode = 0; mode < 2 && st == JSB_OK; ++mode)
+            for (int t : choices) {
+                if (t == best.threads && mode == best.state_mode) continue;
+                bk.threads = t;
+                bk.state_mode = mode;
+                float ms = 0.0f;
+                st = measure(ms);
+                if (st != JSB_OK) break;
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best = bk;
+                }
             }
-        }
-        if (members.empty()) continue;
-        DevBuf<uint32_t> work;
-        JSB_CUDA(work.upload(members.data(), members.size()));
-        float best_ms = 1e30f;
-        int best = tuned[bi].threads;
-        for (int t : choices) {
-            size_t smem = step_smem_bytes(smem_state, max_nv, max_faces);
-            int occ = step_occupancy(t, smem_state, smem);
-            if (occ <= 0) continue;
-            int grid = int(std::min<size_t>(members.size(), size_t(occ) * ctx->num_sms));
-            StepParams p = base_params(ctx, dt);
-            p.work = work.ptr;
-            p.num_work = uint32_t(members.size());
-            p.queue = ctx->queues.ptr;
-            float total = 0.0f;
-            for (int k = 0; k < trials + 1; ++k) {
-                JSB_CUDA(cudaMemset(ctx->queues.ptr, 0, sizeof(uint32_t)));
-                JSB_CUDA(cudaEventRecord(ctx->t0, 0));
-                JSB_CUDA(launch_step(p, t, smem_state, max_nv, max_faces, grid, 0));
-                JSB_CUDA(cudaEventRecord(ctx->t1, 0));
-                JSB_CUDA(cudaEventSynchronize(ctx->t1));
-                float ms = 0;
-                JSB_CUDA(cudaEventElapsedTime(&ms, ctx->t0, ctx->t1));
-                if (k > 0) total += ms;  // first launch is warm-up
-            }
-            if (total < best_ms) {
-                best_ms = total;
-                best = t;
-            }
-        }
-        tuned[bi].threads = best;
+        bk = best;
     }
+    cudaStreamDestroy(stream);
     JSB_CUDA(cudaMemcpy(ctx->x.ptr, sx.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice));
     JSB_CUDA(cudaMemcpy(ctx->v.ptr, sv.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice));
     JSB_CUDA(cudaMemcpy(ctx->states.ptr, ss.ptr, ctx->bodies.size() * sizeof(BodyState), cudaMemcpyDeviceToDevice));
     JSB_CUDA(cudaMemset(ctx->error.ptr, 0, sizeof(uint32_t)));
-    ctx->buckets = tuned;
-    ctx->dirty = true;
+    if (st != JSB_OK) return st;
+    ctx->groups_dirty = true;
     return rebuild(ctx);
 }
 

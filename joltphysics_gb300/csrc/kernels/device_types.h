@@ -99,6 +99,7 @@ struct StepParams {
     uint32_t *error;
     const float *forces;  // 3 floats per body: AddForce accumulators consumed by this step
     const float *step_forces;  // 3 floats per body: force added before every step (persistent)
+    uint32_t ring_slots;  // record ring capacity per level (multiple of 32); wider levels read HBM/L2 directly
 };
 
 }  // namespace jsb

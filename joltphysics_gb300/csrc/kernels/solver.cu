@@ -225,16 +225,15 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// Record ring: kRingDepth levels of up to kRingSlots records each are streamed into shared memory
+// Record ring: kRingDepth levels of up to `slots` records each are streamed into shared memory
 // ahead of the level being projected; the ring holds kRingDepth + 1 levels.
 constexpr int kRingDepth = 3;
 constexpr int kRingLevels = kRingDepth + 1;
-constexpr uint32_t kRingSlots = 256;
-constexpr size_t kRingBytes = size_t(kRingLevels) * kRingSlots * sizeof(uint4);
 
 struct LevelRing {
-    uint4 *rec;   // [kRingLevels][kRingSlots]
-    uint4 *desc;  // [kRingLevels] level descriptors
+    uint4 *rec;      // [kRingLevels][slots]
+    uint4 *desc;     // [kRingLevels] level descriptors
+    uint32_t slots;  // capacity per level
 };
 
 // Stages level `idx` (descriptor, and its records when they fit a ring slot) into ring position
@@ -245,8 +244,8 @@ __device__ __forceinline__ void ring_stage(const LevelRing &ring, const uint4 *_
     const uint32_t pos = idx % kRingLevels;
     if (idx < L) {
         const uint32_t n = next_first - lv.x;
-        if (n <= kRingSlots)
-            for (uint32_t s = threadIdx.x; s < n; s += T) cp_async16(ring.rec + pos * kRingSlots + s, rec + lv.x + s);
+        if (n <= ring.slots)
+            for (uint32_t s = threadIdx.x; s < n; s += T) cp_async16(ring.rec + pos * ring.slots + s, rec + lv.x + s);
     }
     if (threadIdx.x == 0) ring.desc[pos] = lv;
 }
@@ -280,8 +279,8 @@ __device__ __forceinline__ void apply_levels(float4 *sx, const BodyDesc &d, floa
         const uint32_t pos = l % kRingLevels;
         const uint4 lv = ring.desc[pos];
         const uint32_t n = ring.desc[(l + 1) % kRingLevels].x - lv.x;
-        const bool in_ring = n <= kRingSlots;
-        const uint4 *src = in_ring ? ring.rec + pos * kRingSlots : rec + lv.x;
+        const bool in_ring = n <= ring.slots;
+        const uint4 *src = in_ring ? ring.rec + pos * ring.slots : rec + lv.x;
         for (uint32_t s = tid; s < n; s += T) {
             const uint4 r = src[s];
             if (r.x != 0xffffffffu) project(sx, r, slot_type(lv, s), inv_dt_sq);
@@ -441,6 +440,7 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     LevelRing ring;
     ring.rec = reinterpret_cast<uint4 *>(sface);
     ring.desc = sh.ring_desc;
+    ring.slots = p.ring_slots;
 
     // InitializeUpdateContext (identity body rotation)
     const f3 g = d.gravity_factor * ld3(p.gravity);
@@ -729,9 +729,10 @@ __global__ void __launch_bounds__(T) step_kernel(StepParams p, uint32_t cap) {
 
 // Bytes of dynamic shared memory for a launch whose largest body has `vertices` vertices and whose
 // largest pressurised body has `faces` faces.
-size_t step_smem_bytes(bool smem_state, uint32_t vertices, uint32_t faces) {
-    size_t faces_bytes = size_t(faces) * sizeof(float4);
-    return size_t(vertices) * sizeof(float4) * (smem_state ? 3 : 1) + (faces_bytes > kRingBytes ? faces_bytes : kRingBytes);
+size_t step_smem_bytes(bool smem_state, uint32_t vertices, uint32_t faces, uint32_t ring_slots) {
+    const size_t faces_bytes = size_t(faces) * sizeof(float4);
+    const size_t ring_bytes = size_t(kRingLevels) * ring_slots * sizeof(uint4);
+    return size_t(vertices) * sizeof(float4) * (smem_state ? 3 : 1) + (faces_bytes > ring_bytes ? faces_bytes : ring_bytes);
 }
 
 #define JSB_FOR_EACH_SHAPE(X) X(32, true) X(64, true) X(128, true) X(256, true) X(32, false) X(64, false) X(128, false) X(256, false)
@@ -739,7 +740,7 @@ size_t step_smem_bytes(bool smem_state, uint32_t vertices, uint32_t faces) {
 // Launches one persistent step over `p.num_work` bodies with `threads` threads per CTA.
 cudaError_t launch_step(const StepParams &p, int threads, bool smem_state, uint32_t smem_vertices, uint32_t smem_faces, int grid,
                         cudaStream_t stream) {
-    size_t smem = step_smem_bytes(smem_state, smem_vertices, smem_faces);
+    size_t smem = step_smem_bytes(smem_state, smem_vertices, smem_faces, p.ring_slots);
 #define JSB_LAUNCH(TT, SS)                                                      \
     if (threads == TT && smem_state == SS) {                                    \
         step_kernel<TT, SS><<<grid, TT, smem, stream>>>(p, smem_vertices);      \
@@ -855,6 +856,7 @@ __global__ void __launch_bounds__(T) step_kernel_noalloc(const __grid_constant__
     p.error = q.error;
     p.forces = q.force;
     p.step_forces = q.zero3;
+    p.ring_slots = 256;
     step_body<T, kSmemState>(p, 0, smem, cap, sh);
 }
 
@@ -1011,8 +1013,9 @@ extern "C" jsb_status jsb_step_body_noalloc(const void *settings_blob, size_t le
     q.error = error_device;
 
     // Whole vertex state in shared memory when it fits, else positions only (as in the batched path).
-    const bool smem_state = step_smem_bytes(true, nv, nf) <= smem_limit;
-    const size_t smem = step_smem_bytes(smem_state, nv, nf);
+    const uint32_t ring_slots = 256;
+    const bool smem_state = step_smem_bytes(true, nv, nf, ring_slots) <= smem_limit;
+    const size_t smem = step_smem_bytes(smem_state, nv, nf, ring_slots);
     if (smem > smem_limit)
         return report_error(JSB_ERR_UNSUPPORTED, "body does not fit the shared-memory solver path");
     if (smem_state)
