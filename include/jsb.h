@@ -177,6 +177,33 @@ jsb_status jsb_last_kernel_ms(jsb_context *ctx, float *ms_per_step);
 jsb_status jsb_scene_build(const char *name, const char *params, void *out, size_t capacity, size_t *len);
 
 
+/* ---- differentiable runs (hand-written adjoint) ----------------------------------------------- */
+/* Per-constraint compliance of one body, in the settings' constraint order (mEdgeConstraints /
+ * mVolumeConstraints after SoftBodySharedSettings::Optimize); either array may be NULL. The body's
+ * settings must not be shared with another body. */
+jsb_status jsb_body_set_compliance(jsb_context *ctx, uint32_t body_id, const float *edge_compliance, uint32_t num_edges,
+                                   const float *volume_compliance, uint32_t num_volumes);
+
+/* A differentiable run of num_steps batched steps (dt, one collision step) of every body in the
+ * context, starting from the current state. jsb_adjoint_forward runs the steps (up to until_step, so
+ * that positions of intermediate steps can be read between calls) and stores a checkpoint every
+ * checkpoint_every steps; jsb_adjoint_seed adds d loss / d (world) vertex positions
+ * of one body after a given step (1 .. num_steps); jsb_adjoint_backward recomputes each checkpoint
+ * segment with a tape and reverses it (collision active set frozen) and leaves the context at the
+ * forward run's final state; jsb_adjoint_gradients returns d loss / d initial positions and
+ * velocities (3 floats per vertex), d loss / d the body's step force (3 floats, jsb_body_set_step_force)
+ * and d loss / d each edge and volume compliance (settings order); any output may be NULL.
+ * Bodies with dihedral bends are rejected (JSB_ERR_UNSUPPORTED): the reference's ACosApproximate is not
+ * differentiable at flat triangle pairs. Positions and the body position are related by the body's
+ * recentering, which leaves world positions unchanged; the adjoint is taken in world coordinates. */
+jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int checkpoint_every);
+jsb_status jsb_adjoint_forward(jsb_context *ctx, int until_step); /* -1 = all num_steps; may be called in pieces */
+jsb_status jsb_adjoint_seed(jsb_context *ctx, int step, uint32_t body_id, const float *dl_dx);
+jsb_status jsb_adjoint_backward(jsb_context *ctx);
+jsb_status jsb_adjoint_gradients(jsb_context *ctx, uint32_t body_id, float *dl_dx0, float *dl_dv0, float *dl_dforce,
+                                 float *dl_dedge_compliance, float *dl_dvolume_compliance);
+jsb_status jsb_adjoint_end(jsb_context *ctx);
+
 /* ---- allocation-free single-body step -------------------------------------------------------- */
 /* Body record in device memory for jsb_step_body_noalloc: the body's world position, its local bounds
  * and predicted bounds (SoftBodyMotionProperties mLocalBounds / mLocalPredictedBounds, which the next

@@ -57,6 +57,13 @@ SIGNATURES = {
     "jsb_last_launch_count": [_P, _c.POINTER(_c.c_uint32)],
     "jsb_last_kernel_ms": [_P, _c.POINTER(_c.c_float)],
     "jsb_scene_build": [_c.c_char_p, _c.c_char_p, _P, _c.c_size_t, _c.POINTER(_c.c_size_t)],
+    "jsb_body_set_compliance": [_P, _c.c_uint32, _P, _c.c_uint32, _P, _c.c_uint32],
+    "jsb_adjoint_begin": [_P, _c.c_float, _c.c_int, _c.c_int],
+    "jsb_adjoint_forward": [_P, _c.c_int],
+    "jsb_adjoint_seed": [_P, _c.c_int, _c.c_uint32, _P],
+    "jsb_adjoint_backward": [_P],
+    "jsb_adjoint_gradients": [_P, _c.c_uint32, _P, _P, _P, _P, _P],
+    "jsb_adjoint_end": [_P],
     "jsb_step_body_noalloc": [_c.c_char_p, _c.c_size_t, _c.c_char_p, _c.c_char_p, _c.c_uint32, _c.POINTER(_c.c_float),
                               _c.POINTER(_c.c_float), _c.c_float, _P, _P, _P, _P, _P],
 }
@@ -97,6 +104,18 @@ def _f3(v) -> ctypes.Array:
 
 CREATION_FMT = "<I7f4B"
 COLLIDER_FMT = "<i3f3f3f"
+
+
+def blob_counts(blob: bytes) -> dict:
+    """Element counts of a SaveBinaryState blob (vertices, faces, edges, bends, volumes, ..., lra)."""
+    names = [("vertices", 28), ("faces", 16), ("edges", 16), ("bends", 24), ("volumes", 24), ("skinned", 52),
+             ("skinned_normals", 4), ("lra", 12)]
+    out, off = {}, 0
+    for name, size in names:
+        (n,) = struct.unpack_from("<I", blob, off)
+        out[name] = n
+        off += 4 + n * size
+    return out
 
 
 def build_scene(name: str, **params) -> bytes:
@@ -189,7 +208,10 @@ class Context:
             off += 64 + bl
             sid = self.upload_settings(blob)
             bid = self.add_body(sid, cr, pos)
-            bodies.append({"id": bid, "force": force, "iterations": cr[0], "vertices": self.num_vertices[bid]})
+            counts = blob_counts(blob)
+            bodies.append({"id": bid, "force": force, "iterations": cr[0], "vertices": self.num_vertices[bid],
+                           "position": pos, "num_edges": counts["edges"], "num_volumes": counts["volumes"],
+                           "num_bends": counts["bends"]})
         self.bodies = bodies
         return bodies
 
@@ -283,6 +305,40 @@ class Context:
         v = ctypes.c_float()
         check(lib().jsb_last_kernel_ms(self.h, ctypes.byref(v)))
         return v.value
+
+    # -- differentiable runs ---------------------------------------------------------------------
+    def set_compliance(self, body: int, edge=None, volume=None):
+        e = None if edge is None else np.ascontiguousarray(edge, np.float32)
+        v = None if volume is None else np.ascontiguousarray(volume, np.float32)
+        check(lib().jsb_body_set_compliance(self.h, body, None if e is None else e.ctypes.data, 0 if e is None else len(e),
+                                            None if v is None else v.ctypes.data, 0 if v is None else len(v)))
+
+    def adjoint_begin(self, num_steps: int, checkpoint_every: int, dt: float | None = None):
+        check(lib().jsb_adjoint_begin(self.h, dt or self.dt, num_steps, checkpoint_every))
+
+    def adjoint_forward(self, until_step: int = -1):
+        check(lib().jsb_adjoint_forward(self.h, until_step))
+
+    def adjoint_seed(self, step: int, body: int, dl_dx: np.ndarray):
+        a = np.ascontiguousarray(dl_dx, np.float32)
+        check(lib().jsb_adjoint_seed(self.h, step, body, a.ctypes.data))
+
+    def adjoint_backward(self):
+        check(lib().jsb_adjoint_backward(self.h))
+
+    def adjoint_gradients(self, body: int, num_edges: int = 0, num_volumes: int = 0):
+        n = self.num_vertices[body]
+        dx = np.zeros((n, 3), np.float32)
+        dv = np.zeros((n, 3), np.float32)
+        df = np.zeros(3, np.float32)
+        de = np.zeros(num_edges, np.float32)
+        dvol = np.zeros(num_volumes, np.float32)
+        check(lib().jsb_adjoint_gradients(self.h, body, dx.ctypes.data, dv.ctypes.data, df.ctypes.data,
+                                          de.ctypes.data if num_edges else None, dvol.ctypes.data if num_volumes else None))
+        return {"x0": dx, "v0": dv, "force": df, "edge_compliance": de, "volume_compliance": dvol}
+
+    def adjoint_end(self):
+        check(lib().jsb_adjoint_end(self.h))
 
     def upload_all(self, positions: np.ndarray, velocities: np.ndarray, stream: int = 0):
         check(lib().jsb_state_upload_all(self.h, ctypes.c_void_p(positions.ctypes.data),

@@ -34,6 +34,14 @@ cudaError_t launch_step(const StepParams &p, int threads, bool smem_state, uint3
 int step_occupancy(int threads, bool smem_state, size_t smem);
 size_t step_smem_bytes(bool smem_state, uint32_t vertices, uint32_t faces, uint32_t ring_slots);
 cudaError_t init_step_kernels(int max_dynamic_smem);
+cudaError_t launch_step_tape(const StepParams &p, bool smem_state, uint32_t smem_vertices, uint32_t smem_faces, int grid,
+                             cudaStream_t stream);
+int step_tape_occupancy(bool smem_state, size_t smem);
+size_t adjoint_smem_bytes(uint32_t vertices, uint32_t faces);
+cudaError_t init_adjoint_kernels(int max_dynamic_smem);
+int adjoint_occupancy(size_t smem);
+cudaError_t launch_adjoint(const AdjParams &q, uint32_t cap_vertices, uint32_t cap_faces, int grid, cudaStream_t stream);
+cudaError_t launch_add(float4 *dst, const float4 *src, uint64_t n, int num_sms, cudaStream_t stream);
 cudaError_t launch_unpack_state(const float *pos3, const float *vel3, float4 *x, float4 *v, uint64_t n, int num_sms,
                                 cudaStream_t stream);
 cudaError_t launch_pack_state(const float4 *x, const float4 *v, float *pos3, float *vel3, uint64_t n, int num_sms,
@@ -132,6 +140,31 @@ struct LaunchGroup {  // the bodies of one bucket
     cudaEvent_t done = nullptr;
 };
 
+// State of one differentiable run (jsb_adjoint_*): checkpoints every `every` steps, the tape of one
+// checkpoint segment, adjoint accumulators and loss seeds.
+struct AdjointSession {
+    float dt = 0.0f;
+    int steps = 0, every = 1;
+    bool forward_done = false, backward_done = false;
+    int cur_step = 0;  // steps run by jsb_adjoint_forward so far
+    std::vector<DevBuf<float4>> ckpt_x, ckpt_v;
+    std::vector<DevBuf<BodyState>> ckpt_state;
+    DevBuf<float4> final_x, final_v;
+    DevBuf<BodyState> final_state;
+    DevBuf<float4> tape_cons, tape_state, tape_plane;
+    DevBuf<int32_t> tape_shape;
+    DevBuf<float2> tape_cols;
+    DevBuf<float> grad_slots, grad_force;
+    DevBuf<TapeDesc> tape_desc;
+    std::vector<size_t> slot_offset;  // per body, into grad_slots
+    DevBuf<float4> adj_x, adj_v, seed_dev;
+    std::vector<std::pair<int, std::vector<float4>>> seeds;  // (step, dL/dx of every vertex)
+    DevBuf<uint32_t> all_work;
+    bool tape_smem_state = true;
+    uint32_t cap_vertices = 0, cap_faces = 0, ring_slots = 32;
+    int tape_grid = 1, adj_grid = 1;
+};
+
 }  // namespace
 
 // Lets other translation units of the library report failures through jsb_last_error_string.
@@ -169,6 +202,7 @@ struct jsb_context {
     std::vector<jsb::LaunchGroup> groups;
     std::vector<uint32_t> single_work_host;
     jsb::DevBuf<uint32_t> single_work;  // identity list for the plain form
+    std::unique_ptr<jsb::AdjointSession> adjoint;
     cudaEvent_t fork = nullptr;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
@@ -394,6 +428,8 @@ StepParams base_params(jsb_context *ctx, float dt) {
     p.forces = ctx->forces.ptr;
     p.step_forces = ctx->step_forces.ptr;
     p.ring_slots = kMaxRingSlots;
+    p.tape = nullptr;
+    p.tape_step = 0;
     return p;
 }
 
@@ -505,6 +541,7 @@ jsb_status jsb_context_create(int device, jsb_context **out) {
                     {2048, 64, 0},  {3072, 128, 0}, {4096, 128, 0}, {8192, 128, 0}, {65536, 128, 0}};
     // static shared memory of the solver kernel is under 4 KB
     JSB_CUDA(init_step_kernels(int(ctx->max_smem_optin - kStaticSmemReserve)));
+    JSB_CUDA(init_adjoint_kernels(int(ctx->max_smem_optin - kStaticSmemReserve)));
     JSB_CUDA(cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming));
     JSB_CUDA(cudaEventCreate(&ctx->t0));
     JSB_CUDA(cudaEventCreate(&ctx->t1));
@@ -1018,6 +1055,299 @@ jsb_status jsb_autotune(jsb_context *ctx, float dt, int trials) {
     if (st != JSB_OK) return st;
     ctx->groups_dirty = true;
     return rebuild(ctx);
+}
+
+// ---- differentiable runs ----------------------------------------------------------------------------
+
+jsb_status jsb_body_set_compliance(jsb_context *ctx, uint32_t body_id, const float *edge_compliance, uint32_t num_edges,
+                                   const float *volume_compliance, uint32_t num_volumes) {
+    if (!check_ctx(ctx) || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    const uint32_t sid = ctx->bodies[body_id].settings_id;
+    for (size_t b = 0; b < ctx->bodies.size(); ++b)
+        if (b != body_id && ctx->bodies[b].settings_id == sid)
+            return fail(JSB_ERR_INVALID_ARGUMENT, "settings are shared with another body; upload a separate copy to change compliance");
+    SettingsRec &s = *ctx->settings[sid];
+    if ((edge_compliance && num_edges != s.parsed.edges.size()) || (volume_compliance && num_volumes != s.parsed.volumes.size()))
+        return fail(JSB_ERR_INVALID_ARGUMENT, "compliance arrays must cover every edge / volume constraint");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    JSB_CUDA(cudaDeviceSynchronize());
+    if (edge_compliance)
+        for (uint32_t i = 0; i < num_edges; ++i) s.parsed.edges[i].compliance = edge_compliance[i];
+    if (volume_compliance)
+        for (uint32_t i = 0; i < num_volumes; ++i) s.parsed.volumes[i].compliance = volume_compliance[i];
+    s.schedule = build_schedule(s.parsed);  // same layout, new compliance words
+    JSB_CUDA(cudaMemcpy(s.records.ptr, s.schedule.padded_records.data(), s.schedule.padded_records.size() * sizeof(uint32_t),
+                        cudaMemcpyHostToDevice));
+    drop_graph(ctx);
+    return JSB_OK;
+}
+
+namespace {
+
+jsb_status save_state(jsb_context *ctx, DevBuf<float4> &x, DevBuf<float4> &v, DevBuf<BodyState> &st) {
+    const uint64_t n = ctx->total_vertices;
+    if (x.count != n) JSB_CUDA(x.alloc(n));
+    if (v.count != n) JSB_CUDA(v.alloc(n));
+    if (st.count != ctx->bodies.size()) JSB_CUDA(st.alloc(ctx->bodies.size()));
+    JSB_CUDA(cudaMemcpy(x.ptr, ctx->x.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice));
+    JSB_CUDA(cudaMemcpy(v.ptr, ctx->v.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice));
+    JSB_CUDA(cudaMemcpy(st.ptr, ctx->states.ptr, ctx->bodies.size() * sizeof(BodyState), cudaMemcpyDeviceToDevice));
+    return JSB_OK;
+}
+
+jsb_status load_state(jsb_context *ctx, const DevBuf<float4> &x, const DevBuf<float4> &v, const DevBuf<BodyState> &st) {
+    const uint64_t n = ctx->total_vertices;
+    JSB_CUDA(cudaMemcpy(ctx->x.ptr, x.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice));
+    JSB_CUDA(cudaMemcpy(ctx->v.ptr, v.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice));
+    JSB_CUDA(cudaMemcpy(ctx->states.ptr, st.ptr, ctx->bodies.size() * sizeof(BodyState), cudaMemcpyDeviceToDevice));
+    return JSB_OK;
+}
+
+}  // namespace
+
+jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int checkpoint_every) {
+    if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
+    if (!(dt > 0.0f) || num_steps < 1 || checkpoint_every < 1)
+        return fail(JSB_ERR_INVALID_ARGUMENT, "dt must be > 0, num_steps >= 1 and checkpoint_every >= 1");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    if (ctx->forces_pending)
+        return fail(JSB_ERR_INVALID_ARGUMENT, "one-shot AddForce cannot be differentiated; use jsb_body_set_step_force");
+    for (size_t b = 0; b < ctx->bodies.size(); ++b)
+        if (!ctx->settings[ctx->bodies[b].settings_id]->parsed.bends.empty())
+            return fail(JSB_ERR_UNSUPPORTED, "body " + std::to_string(b) +
+                                                 " has dihedral bend constraints, which differentiable runs do not support");
+    auto a = std::make_unique<AdjointSession>();
+    a->dt = dt;
+    a->steps = num_steps;
+    a->every = std::min(checkpoint_every, num_steps);
+    const size_t nb = ctx->bodies.size();
+    const size_t K = size_t(a->every);
+    size_t cons = 0, state = 0, planes = 0, slots = 0;
+    std::vector<TapeDesc> desc(nb);
+    std::vector<size_t> cons_off(nb), state_off(nb), plane_off(nb);
+    a->slot_offset.resize(nb);
+    const size_t cap = ctx->max_smem_optin - kStaticSmemReserve;
+    for (size_t b = 0; b < nb; ++b) {
+        const BodyRec &br = ctx->bodies[b];
+        const SettingsRec &s = *ctx->settings[br.settings_id];
+        const size_t nv = s.parsed.vertices.size(), ns = s.schedule.num_slots, it = br.creation.num_iterations;
+        cons_off[b] = cons;
+        state_off[b] = state;
+        plane_off[b] = planes;
+        a->slot_offset[b] = slots;
+        cons += K * it * ns * 3;
+        state += K * it * 3 * nv;
+        planes += K * nv;
+        slots += ns;
+        a->cap_vertices = std::max(a->cap_vertices, uint32_t(nv));
+        a->cap_faces = std::max(a->cap_faces, pressure_faces(s, br));
+        a->ring_slots = std::max(a->ring_slots, ring_slots_for(s));
+    }
+    JSB_CUDA(a->tape_cons.alloc(cons));
+    JSB_CUDA(a->tape_state.alloc(state));
+    JSB_CUDA(a->tape_plane.alloc(planes));
+    JSB_CUDA(a->tape_shape.alloc(planes));
+    JSB_CUDA(a->tape_cols.alloc(nb * K * kMaxCollidingShapes));
+    JSB_CUDA(a->grad_slots.alloc(std::max<size_t>(slots, 1)));
+    JSB_CUDA(a->grad_force.alloc(nb * 3));
+    for (size_t b = 0; b < nb; ++b) {
+        desc[b].cons = a->tape_cons.ptr + cons_off[b];
+        desc[b].state = a->tape_state.ptr + state_off[b];
+        desc[b].plane = a->tape_plane.ptr + plane_off[b];
+        desc[b].shape = a->tape_shape.ptr + plane_off[b];
+        desc[b].cols = a->tape_cols.ptr + b * K * kMaxCollidingShapes;
+        desc[b].grad = a->grad_slots.ptr + a->slot_offset[b];
+        desc[b].slots = ctx->settings[ctx->bodies[b].settings_id]->schedule.num_slots;
+        desc[b].pad = 0;
+    }
+    JSB_CUDA(a->tape_desc.upload(desc.data(), nb));
+    std::vector<uint32_t> all(nb);
+    for (size_t b = 0; b < nb; ++b) all[b] = uint32_t(b);
+    JSB_CUDA(a->all_work.upload(all.data(), nb));
+    JSB_CUDA(a->adj_x.alloc(ctx->total_vertices));
+    JSB_CUDA(a->adj_v.alloc(ctx->total_vertices));
+    JSB_CUDA(a->seed_dev.alloc(ctx->total_vertices));
+    a->tape_smem_state = step_smem_bytes(true, a->cap_vertices, a->cap_faces, a->ring_slots) <= cap;
+    const size_t tsmem = step_smem_bytes(a->tape_smem_state, a->cap_vertices, a->cap_faces, a->ring_slots);
+    const size_t asmem = adjoint_smem_bytes(a->cap_vertices, a->cap_faces);
+    if (tsmem > cap || asmem > cap) return fail(JSB_ERR_UNSUPPORTED, "a body is too large for the differentiable (taped) path");
+    a->tape_grid = int(std::min<size_t>(nb, size_t(std::max(1, step_tape_occupancy(a->tape_smem_state, tsmem))) * ctx->num_sms));
+    a->adj_grid = int(std::min<size_t>(nb, size_t(std::max(1, adjoint_occupancy(asmem))) * ctx->num_sms));
+    const int n_ckpt = (num_steps + a->every - 1) / a->every;
+    a->ckpt_x.resize(n_ckpt);
+    a->ckpt_v.resize(n_ckpt);
+    a->ckpt_state.resize(n_ckpt);
+    ctx->adjoint = std::move(a);
+    return JSB_OK;
+}
+
+jsb_status jsb_adjoint_forward(jsb_context *ctx, int until_step) {
+    if (!check_ctx(ctx) || !ctx->adjoint) return fail(JSB_ERR_INVALID_ARGUMENT, "no differentiable run (jsb_adjoint_begin)");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    AdjointSession &a = *ctx->adjoint;
+    if (until_step < 0) until_step = a.steps;
+    if (until_step < a.cur_step || until_step > a.steps)
+        return fail(JSB_ERR_INVALID_ARGUMENT, "until_step must lie between the steps already run and num_steps");
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    if (a.cur_step == 0) {
+        a.seeds.clear();
+        a.backward_done = false;
+    }
+    uint32_t launches = 0;
+    for (int s = a.cur_step; s < until_step; ++s) {
+        if (s % a.every == 0) {
+            JSB_CUDA(cudaDeviceSynchronize());
+            if ((st = save_state(ctx, a.ckpt_x[s / a.every], a.ckpt_v[s / a.every], a.ckpt_state[s / a.every])) != JSB_OK) return st;
+        }
+        if ((st = enqueue_batched(ctx, a.dt, 0, launches)) != JSB_OK) return st;
+    }
+    JSB_CUDA(cudaDeviceSynchronize());
+    a.cur_step = until_step;
+    if (a.cur_step == a.steps) {
+        if ((st = save_state(ctx, a.final_x, a.final_v, a.final_state)) != JSB_OK) return st;
+        a.forward_done = true;
+    }
+    ctx->last_launches = launches;
+    return JSB_OK;
+}
+
+jsb_status jsb_adjoint_seed(jsb_context *ctx, int step, uint32_t body_id, const float *dl_dx) {
+    if (!check_ctx(ctx) || !ctx->adjoint || !dl_dx || body_id >= ctx->bodies.size())
+        return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    AdjointSession &a = *ctx->adjoint;
+    if (step < 1 || step > a.steps) return fail(JSB_ERR_INVALID_ARGUMENT, "seed step must be in 1 .. num_steps");
+    std::vector<float4> *dst = nullptr;
+    for (auto &sd : a.seeds)
+        if (sd.first == step) dst = &sd.second;
+    if (!dst) {
+        a.seeds.push_back({step, std::vector<float4>(ctx->total_vertices, make_float4(0, 0, 0, 0))});
+        dst = &a.seeds.back().second;
+    }
+    const BodyRec &b = ctx->bodies[body_id];
+    const size_t nv = ctx->settings[b.settings_id]->parsed.vertices.size();
+    for (size_t i = 0; i < nv; ++i) {
+        float4 &d = (*dst)[b.vtx_offset + i];
+        d.x += dl_dx[3 * i + 0];
+        d.y += dl_dx[3 * i + 1];
+        d.z += dl_dx[3 * i + 2];
+    }
+    return JSB_OK;
+}
+
+jsb_status jsb_adjoint_backward(jsb_context *ctx) {
+    if (!check_ctx(ctx) || !ctx->adjoint) return fail(JSB_ERR_INVALID_ARGUMENT, "no differentiable run (jsb_adjoint_begin)");
+    AdjointSession &a = *ctx->adjoint;
+    if (!a.forward_done) return fail(JSB_ERR_INVALID_ARGUMENT, "jsb_adjoint_forward must run before the backward pass");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    const uint64_t n = ctx->total_vertices;
+    const uint32_t nb = uint32_t(ctx->bodies.size());
+    JSB_CUDA(cudaMemset(a.adj_x.ptr, 0, n * sizeof(float4)));
+    JSB_CUDA(cudaMemset(a.adj_v.ptr, 0, n * sizeof(float4)));
+    JSB_CUDA(cudaMemset(a.grad_slots.ptr, 0, a.grad_slots.count * sizeof(float)));
+    JSB_CUDA(cudaMemset(a.grad_force.ptr, 0, a.grad_force.count * sizeof(float)));
+    uint32_t launches = 0;
+    const int n_ckpt = int(a.ckpt_x.size());
+    for (int seg = n_ckpt - 1; seg >= 0; --seg) {
+        const int s0 = seg * a.every, s1 = std::min(s0 + a.every, a.steps);
+        if ((st = load_state(ctx, a.ckpt_x[seg], a.ckpt_v[seg], a.ckpt_state[seg])) != JSB_OK) return st;
+        for (int s = s0; s < s1; ++s) {  // recompute the segment, recording the tape
+            JSB_CUDA(cudaMemsetAsync(ctx->queues.ptr, 0, sizeof(uint32_t), 0));
+            StepParams p = base_params(ctx, a.dt);
+            p.work = a.all_work.ptr;
+            p.num_work = nb;
+            p.queue = ctx->queues.ptr;
+            p.ring_slots = a.ring_slots;
+            p.tape = a.tape_desc.ptr;
+            p.tape_step = uint32_t(s - s0);
+            JSB_CUDA(launch_step_tape(p, a.tape_smem_state, a.cap_vertices, a.cap_faces, a.tape_grid, 0));
+            ++launches;
+        }
+        for (int s = s1 - 1; s >= s0; --s) {  // reverse the segment
+            for (auto &sd : a.seeds)
+                if (sd.first == s + 1) {
+                    JSB_CUDA(cudaMemcpy(a.seed_dev.ptr, sd.second.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+                    JSB_CUDA(launch_add(a.adj_x.ptr, a.seed_dev.ptr, n, ctx->num_sms, 0));
+                    ++launches;
+                }
+            JSB_CUDA(cudaMemsetAsync(ctx->queues.ptr, 0, sizeof(uint32_t), 0));
+            AdjParams q;
+            q.bodies = ctx->descs.ptr;
+            q.tape = a.tape_desc.ptr;
+            q.tape_step = uint32_t(s - s0);
+            q.work = a.all_work.ptr;
+            q.num_work = nb;
+            q.queue = ctx->queues.ptr;
+            q.adj_x = a.adj_x.ptr;
+            q.adj_v = a.adj_v.ptr;
+            q.grad_force = a.grad_force.ptr;
+            for (int k = 0; k < 3; ++k) q.gravity[k] = ctx->gravity[k];
+            q.dt = a.dt;
+            JSB_CUDA(launch_adjoint(q, a.cap_vertices, a.cap_faces, a.adj_grid, 0));
+            ++launches;
+        }
+    }
+    JSB_CUDA(cudaDeviceSynchronize());
+    if ((st = load_state(ctx, a.final_x, a.final_v, a.final_state)) != JSB_OK) return st;
+    a.backward_done = true;
+    ctx->last_launches = launches;
+    return JSB_OK;
+}
+
+jsb_status jsb_adjoint_gradients(jsb_context *ctx, uint32_t body_id, float *dl_dx0, float *dl_dv0, float *dl_dforce,
+                                 float *dl_dedge_compliance, float *dl_dvolume_compliance) {
+    if (!check_ctx(ctx) || !ctx->adjoint || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    AdjointSession &a = *ctx->adjoint;
+    if (!a.backward_done) return fail(JSB_ERR_INVALID_ARGUMENT, "jsb_adjoint_backward has not run");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    const BodyRec &b = ctx->bodies[body_id];
+    const SettingsRec &s = *ctx->settings[b.settings_id];
+    const size_t nv = s.parsed.vertices.size();
+    std::vector<float4> tmp(nv);
+    if (dl_dx0) {
+        JSB_CUDA(cudaMemcpy(tmp.data(), a.adj_x.ptr + b.vtx_offset, nv * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < nv; ++i) {
+            dl_dx0[3 * i + 0] = tmp[i].x;
+            dl_dx0[3 * i + 1] = tmp[i].y;
+            dl_dx0[3 * i + 2] = tmp[i].z;
+        }
+    }
+    if (dl_dv0) {
+        JSB_CUDA(cudaMemcpy(tmp.data(), a.adj_v.ptr + b.vtx_offset, nv * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < nv; ++i) {
+            dl_dv0[3 * i + 0] = tmp[i].x;
+            dl_dv0[3 * i + 1] = tmp[i].y;
+            dl_dv0[3 * i + 2] = tmp[i].z;
+        }
+    }
+    if (dl_dforce) JSB_CUDA(cudaMemcpy(dl_dforce, a.grad_force.ptr + 3 * body_id, 3 * sizeof(float), cudaMemcpyDeviceToHost));
+    if (dl_dedge_compliance || dl_dvolume_compliance) {
+        std::vector<float> g(s.schedule.num_slots);
+        if (!g.empty())
+            JSB_CUDA(cudaMemcpy(g.data(), a.grad_slots.ptr + a.slot_offset[body_id], g.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        if (dl_dedge_compliance) std::fill(dl_dedge_compliance, dl_dedge_compliance + s.parsed.edges.size(), 0.0f);
+        if (dl_dvolume_compliance) std::fill(dl_dvolume_compliance, dl_dvolume_compliance + s.parsed.volumes.size(), 0.0f);
+        for (size_t c = 0; c < g.size(); ++c) {
+            const uint32_t src = s.schedule.padded_source[c];
+            if (src == 0xffffffffu) continue;
+            const uint32_t type = src >> 28, idx = src & 0x0fffffffu;
+            if (type == kEdge && dl_dedge_compliance) dl_dedge_compliance[idx] += g[c];
+            if (type == kVolume && dl_dvolume_compliance) dl_dvolume_compliance[idx] += g[c];
+        }
+    }
+    return JSB_OK;
+}
+
+jsb_status jsb_adjoint_end(jsb_context *ctx) {
+    if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    ctx->adjoint.reset();
+    return JSB_OK;
 }
 
 jsb_status jsb_scene_build(const char *name, const char *params, void *out, size_t capacity, size_t *len) {

@@ -1,0 +1,411 @@
+// Adjoint (reverse-mode) of the soft-body solver step on sm_103a.
+//
+// One CTA reverses one body through one step, substeps in reverse:
+//   velocity clamp of UpdateSoftBodyState (last substep only)
+//   ApplyCollisionConstraintsAndUpdateVelocities (SoftBodyMotionProperties.cpp:700-825), with the
+//     collision active set frozen: the plane, shape index and the contact / friction-clamp /
+//     restitution branch decisions are those of the forward pass
+//   the constraint levels in reverse order (edge :573-601, tetra volume :458-507, LRA :679-698)
+//   IntegratePositions (:325-365), accumulating d loss / d force
+//   ApplyPressure (:291-323)
+// Recentering of the body (UpdateSoftBodyState :882-898) moves local positions and the body
+// position by opposite amounts; world positions, and so the adjoint, pass through it unchanged.
+//
+// The forward values each reverse stage needs come from the tape written by the taped forward step
+// (constraint inputs, substep states, collision planes). Constraints of one level write disjoint
+// vertices, so their reverse projections also run concurrently between barriers; an LRA anchor is only
+// read, and the adjoint contributions of several LRA constraints to one anchor are added atomically.
+// d loss / d compliance accumulates per schedule slot; a slot is reversed by the same thread in every
+// substep, so the accumulation is race free and deterministic.
+//
+// Dihedral bends are not differentiated (the runtime rejects differentiable runs of bodies with
+// bends): the reference's ACosApproximate has an unbounded derivative at flat triangle pairs.
+
+#include <cuda_runtime.h>
+#include <float.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "device_types.h"
+
+namespace jsb {
+namespace {
+
+__device__ __forceinline__ f3 vzero() { return mk(0.0f, 0.0f, 0.0f); }
+__device__ __forceinline__ int adj_slot_type(uint4 lv, uint32_t s) {
+    return s < lv.y ? 0 : (s < lv.z ? 1 : (s < lv.w ? 2 : 3));
+}
+
+// x0' = x0 + w0 c, x1' = x1 - w1 c, c = d phi, d = x1 - x0, phi = (1 - rest / |d|) / (w0 + w1 + alpha k)
+__device__ __forceinline__ void edge_adjoint(float4 *lx, const float *sw, uint4 r, const float4 *tin, float inv_dt_sq,
+                                             float *grad) {
+    const uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16;
+    const float w0 = sw[i0], w1 = sw[i1];
+    const float rest = __uint_as_float(r.z), alpha = __uint_as_float(r.w);
+    const f3 dl = xyz(tin[0]);
+    const float L = len(dl);
+    const float s = w0 + w1 + alpha * inv_dt_sq;
+    if (L * s < 1.0e-12f) return;
+    const float phi = (1.0f - rest / L) / s;
+    const f3 l0 = xyz(lx[i0]), l1 = xyz(lx[i1]);
+    const f3 lc = w0 * l0 - w1 * l1;
+    const float dc = dot(dl, lc);
+    const f3 ld = phi * lc + dl * (rest / (L * L * L * s) * dc);
+    lx[i0] = with_w(l0 - ld, 0.0f);
+    lx[i1] = with_w(l1 + ld, 0.0f);
+    *grad += dc * (-phi / s) * inv_dt_sq;
+}
+
+// x_i' = x_i - ml w_i d_i, ml = (|T| - V0) / (sum w_i |d_i|^2 + alpha k), T = (a x b) . c with
+// a = x2 - x1, b = x3 - x1, c = x4 - x1 and d1 = (c - a) x (b - a), d2 = b x c, d3 = c x a, d4 = a x b.
+__device__ __forceinline__ void volume_adjoint(float4 *lx, const float *sw, uint4 r, const float4 *tin, float inv_dt_sq,
+                                               float *grad) {
+    const uint32_t i1 = r.x & 0xffff, i2 = r.x >> 16, i3 = r.y & 0xffff, i4 = r.y >> 16;
+    const float w1 = sw[i1], w2 = sw[i2], w3 = sw[i3], w4 = sw[i4];
+    const float v0 = __uint_as_float(r.z), alpha = __uint_as_float(r.w);
+    const f3 a = xyz(tin[0]), b = xyz(tin[1]), c = xyz(tin[2]);
+    const f3 d1 = cross(c - a, b - a), d2 = cross(b, c), d3 = cross(c, a), d4 = cross(a, b);
+    const float T = dot(d4, c);
+    const float C = fabsf(T) - v0;
+    const float denom = w1 * len_sq(d1) + w2 * len_sq(d2) + w3 * len_sq(d3) + w4 * len_sq(d4) + alpha * inv_dt_sq;
+    if (denom < 1.0e-12f) return;
+    const float ml = C / denom;
+    const f3 L1 = xyz(lx[i1]), L2 = xyz(lx[i2]), L3 = xyz(lx[i3]), L4 = xyz(lx[i4]);
+    const float lml = -(w1 * dot(d1, L1) + w2 * dot(d2, L2) + w3 * dot(d3, L3) + w4 * dot(d4, L4));
+    const float lC = lml / denom;
+    const float ldenom = -ml / denom * lml;
+    const f3 G1 = (-ml * w1) * L1 + (2.0f * w1 * ldenom) * d1;
+    const f3 G2 = (-ml * w2) * L2 + (2.0f * w2 * ldenom) * d2;
+    const f3 G3 = (-ml * w3) * L3 + (2.0f * w3 * ldenom) * d3;
+    const f3 G4 = (-ml * w4) * L4 + (2.0f * w4 * ldenom) * d4;
+    *grad += ldenom * inv_dt_sq;
+    const float lT = (T >= 0.0f ? 1.0f : -1.0f) * lC;
+    f3 la = lT * cross(b, c), lb = lT * cross(c, a), lcv = lT * d4;
+    // d1 = u x v, u = c - a, v = b - a
+    const f3 lu = cross(b - a, G1), lv = cross(G1, c - a);
+    lcv = lcv + lu;
+    lb = lb + lv;
+    la = la - (lu + lv);
+    lb = lb + cross(c, G2);  // d2 = b x c
+    lcv = lcv + cross(G2, b);
+    lcv = lcv + cross(a, G3);  // d3 = c x a
+    la = la + cross(G3, c);
+    la = la + cross(b, G4);  // d4 = a x b
+    lb = lb + cross(G4, a);
+    lx[i1] = with_w(L1 - ((la + lb) + lcv), 0.0f);
+    lx[i2] = with_w(L2 + la, 0.0f);
+    lx[i3] = with_w(L3 + lb, 0.0f);
+    lx[i4] = with_w(L4 + lcv, 0.0f);
+}
+
+// x1' = x0 + d md / |d| when |d| > md (d = x1 - x0); the anchor x0 is only read.
+__device__ __forceinline__ void lra_adjoint(float4 *lx, uint4 r, const float4 *tin) {
+    const uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16;
+    const float md = __uint_as_float(r.z);
+    const f3 dl = xyz(tin[0]);
+    const float dls = len_sq(dl);
+    if (!(dls > md * md)) return;
+    const float L = sqrtf(dls);
+    const f3 l = xyz(lx[i1]);
+    const f3 ldl = (md / L) * (l - dl * (dot(dl, l) / dls));
+    const f3 add = l - ldl;
+    atomicAdd(&lx[i0].x, add.x);
+    atomicAdd(&lx[i0].y, add.y);
+    atomicAdd(&lx[i0].z, add.z);
+    lx[i1] = with_w(ldl, 0.0f);
+}
+
+
+struct AdjShared {
+    uint32_t item;
+    float red[32];
+    float v6, lcoef;
+};
+
+template <int T>
+__device__ __forceinline__ float block_sum(AdjShared &sh, float v) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    __syncthreads();
+    if (lane == 0) sh.red[warp] = v;
+    __syncthreads();
+    float t = 0.0f;
+    for (int w = 0; w < T / 32; ++w) t += sh.red[w];
+    __syncthreads();
+    return t;  // every thread
+}
+
+// Reverse of one substep's constraint levels on the position adjoints lx.
+template <int T>
+__device__ __forceinline__ void reverse_levels(float4 *lx, const float *sw, const BodyDesc &d, const float4 *cons, float *grad,
+                                               float inv_dt_sq) {
+    const uint4 *__restrict__ levels = d.levels;
+    const uint4 *__restrict__ rec = d.records;
+    for (int l = int(d.num_levels) - 1; l >= 0; --l) {
+        const uint4 lv = __ldg(levels + l);
+        const uint32_t n = __ldg(levels + l + 1).x - lv.x;
+        for (uint32_t s = threadIdx.x; s < n; s += T) {
+            const uint32_t c = lv.x + s;
+            const uint4 r = __ldg(rec + c);
+            if (r.x == 0xffffffffu) continue;
+            const float4 *tin = cons + size_t(c) * 3;
+            const int type = adj_slot_type(lv, s);
+            if (type == 2)
+                edge_adjoint(lx, sw, r, tin, inv_dt_sq, grad + c);
+            else if (type == 1)
+                volume_adjoint(lx, sw, r, tin, inv_dt_sq, grad + c);
+            else if (type == 3)
+                lra_adjoint(lx, r, tin);
+        }
+        __syncthreads();
+    }
+}
+
+// Shared memory (dynamic), cap = the launch's largest vertex count:
+//   lx[cap] position adjoints | lv[cap] velocity adjoints | lp[cap] previous-position adjoints, then
+//   substep positions for the pressure adjoint | w[cap] inverse masses | per-face pressure scratch
+template <int T>
+__device__ void adjoint_body(const AdjParams &q, uint32_t b, float4 *smem, uint32_t cap, AdjShared &sh) {
+    const uint32_t tid = threadIdx.x;
+    const BodyDesc d = q.bodies[b];
+    const TapeDesc td = q.tape[b];
+    const uint32_t nv = d.num_vertices, n_it = d.num_iterations;
+    float4 *lx = smem, *lv = smem + cap, *lp = smem + 2 * cap;
+    float *sw = reinterpret_cast<float *>(smem + 3 * cap);
+    float4 *sface = smem + 3 * cap + (cap + 3) / 4;
+    float4 *gax = q.adj_x + d.vtx_offset, *gav = q.adj_v + d.vtx_offset;
+
+    const float dt_sub = q.dt / float(n_it);
+    const f3 g = d.gravity_factor * ld3(q.gravity);
+    const float inv_dt_sq = 1.0f / (dt_sub * dt_sub);
+    float damp = 1.0f - d.linear_damping * dt_sub;
+    damp = damp < 0.0f ? 0.0f : damp;
+    const float inv_dt = 1.0f / dt_sub;
+    const float restitution_threshold = -2.0f * len(g) * dt_sub;
+    const float max_sq = d.max_linear_velocity * d.max_linear_velocity;
+    const bool has_pressure = d.pressure > 0.0f && d.num_faces > 0;
+    const float4 *planes = td.plane + size_t(q.tape_step) * nv;
+    const int32_t *shapes = td.shape + size_t(q.tape_step) * nv;
+    const float2 *cols = td.cols + size_t(q.tape_step) * kMaxCollidingShapes;
+    const float4 *ts0 = td.state + size_t(q.tape_step) * n_it * 3 * nv;
+
+    for (uint32_t i = tid; i < nv; i += T) {
+        lx[i] = gax[i];
+        lv[i] = gav[i];
+        sw[i] = ts0[i].w;
+    }
+    __syncthreads();
+
+    f3 force_acc = vzero();
+    for (int it = int(n_it) - 1; it >= 0; --it) {
+        const float4 *ts = td.state + (size_t(q.tape_step) * n_it + it) * 3 * nv;
+        // ---- collision and velocity update ----
+        for (uint32_t i = tid; i < nv; i += T) {
+            const float w = sw[i];
+            if (!(w > 0.0f)) {  // kinematic: position and velocity pass through; prev unused
+                lp[i] = make_float4(0, 0, 0, 0);
+                if (it == int(n_it) - 1) {  // velocity clamp of UpdateSoftBodyState
+                    const f3 vk = xyz(ts[nv + i]), lk = xyz(lv[i]);
+                    const float vsq = len_sq(vk);
+                    if (vsq > max_sq) lv[i] = with_w(sqrtf(max_sq / vsq) * (lk - vk * (dot(vk, lk) / vsq)), 0.0f);
+                }
+                continue;
+            }
+            const f3 xs = xyz(ts[i]), pv = xyz(ts[nv + i]), xc = xyz(ts[2 * nv + i]);
+            const f3 lxf = xyz(lx[i]);
+            f3 lv3 = xyz(lv[i]);
+            const f3 v0 = (xc - xs) * inv_dt;
+            const int shape = shapes[i];
+            bool contact = false;
+            f3 n = vzero();
+            float pd = 0.0f;
+            if (shape >= 0) {
+                const float4 pl = planes[i];
+                n = xyz(pl);
+                pd = -(dot(xc, n) + pl.w) + d.vertex_radius;
+                contact = pd > 0.0f;
+            }
+            f3 vn = vzero(), vt = vzero(), v3 = v0;
+            float vtl = 0.0f, f = 0.0f, mu = 0.0f, e = 0.0f;
+            bool unclamped = false, rest = false;
+            if (contact) {
+                mu = cols[shape].x;
+                e = cols[shape].y;
+                vn = n * dot(n, v0);
+                vt = v0 - vn;
+                vtl = len(vt);
+                f3 v1 = v0;
+                if (vtl > 0.0f) {
+                    const float fq = mu * pd / (vtl * dt_sub);
+                    unclamped = !(fq > 1.0f);
+                    f = unclamped ? fq : 1.0f;
+                    v1 = v0 - vt * f;
+                }
+                const f3 v2 = v1 - vn;
+                const float pvn = dot(pv, n);
+                rest = pvn < restitution_threshold;
+                v3 = rest ? v2 - (e * pvn) * n : v2;
+            }
+            if (it == int(n_it) - 1) {  // velocity clamp of UpdateSoftBodyState
+                const float vsq = len_sq(v3);
+                if (vsq > max_sq) {
+                    const float sc = sqrtf(max_sq / vsq);
+                    lv3 = sc * (lv3 - v3 * (dot(v3, lv3) / vsq));
+                }
+            }
+            f3 lxc, lpv = vzero(), lv0;
+            if (!contact) {
+                lv0 = lv3;
+                lxc = lxf;
+            } else {
+                if (rest) lpv = n * (-e * dot(n, lv3));
+                const f3 lv1 = lv3;
+                f3 lvn = vzero() - lv3;
+                lv0 = lv1;
+                f3 lvt = vzero();
+                float lpd = 0.0f;
+                if (vtl > 0.0f) {
+                    lvt = (-f) * lv1;
+                    if (unclamped) {
+                        const float lf = -dot(vt, lv1);
+                        lpd += mu / (vtl * dt_sub) * lf;
+                        const float lvtl = -f / vtl * lf;
+                        lvt = lvt + vt * (lvtl / vtl);
+                    }
+                }
+                lv0 = lv0 + lvt;
+                lvn = lvn - lvt;
+                lv0 = lv0 + n * dot(n, lvn);
+                lpd += dot(n, lxf);
+                lxc = lxf - n * lpd;
+            }
+            lx[i] = with_w(lxc + lv0 * inv_dt, 0.0f);
+            lv[i] = with_w(lpv, 0.0f);
+            lp[i] = with_w(vzero() - lv0 * inv_dt, 0.0f);
+        }
+        __syncthreads();
+        // ---- constraint levels, reversed ----
+        reverse_levels<T>(lx, sw, d, td.cons + (size_t(q.tape_step) * n_it + it) * size_t(td.slots) * 3, td.grad, inv_dt_sq);
+        // ---- integration: x' = x + v' dt, v' = (v + g dt + F dt w / N) damp ----
+        for (uint32_t i = tid; i < nv; i += T) {
+            const float w = sw[i];
+            const f3 lxp = xyz(lx[i]);
+            const f3 lvp = xyz(lv[i]) + lxp * dt_sub;
+            f3 lvs = lvp;
+            if (w > 0.0f) {
+                lvs = lvp * damp;
+                force_acc = force_acc + lvp * (w * damp);
+            }
+            lx[i] = with_w(lxp + xyz(lp[i]), 0.0f);
+            lv[i] = with_w(lvs, 0.0f);
+        }
+        __syncthreads();
+        // ---- pressure: v += w coef (x2 - x1) x (x3 - x1) per face, coef = p dt / V6 ----
+        if (has_pressure) {
+            for (uint32_t i = tid; i < nv; i += T) lp[i] = ts[i];
+            __syncthreads();
+            float part = 0.0f;
+            for (uint32_t f = tid; f < d.num_faces; f += T) {
+                const uint4 fc = __ldg(d.faces + f);
+                part += dot(cross(xyz(lp[fc.x]), xyz(lp[fc.y])), xyz(lp[fc.z]));
+            }
+            const float v6 = block_sum<T>(sh, part);
+            if (v6 > 0.0f) {
+                const float coef = d.pressure * dt_sub / v6;
+                float lpart = 0.0f;
+                for (uint32_t f = tid; f < d.num_faces; f += T) {
+                    const uint4 fc = __ldg(d.faces + f);
+                    const f3 x1 = xyz(lp[fc.x]), x2 = xyz(lp[fc.y]), x3 = xyz(lp[fc.z]);
+                    const f3 gf = (sw[fc.x] * xyz(lv[fc.x]) + sw[fc.y] * xyz(lv[fc.y])) + sw[fc.z] * xyz(lv[fc.z]);
+                    lpart += dot(gf, cross(x2 - x1, x3 - x1));
+                    sface[f] = with_w(gf, 0.0f);
+                }
+                const float lcoef = block_sum<T>(sh, lpart);
+                const float lv6 = -coef / v6 * lcoef;
+                for (uint32_t i = tid; i < nv; i += T) {
+                    f3 acc = xyz(lx[i]);
+                    for (uint32_t k = __ldg(d.vf_off + i), ke = __ldg(d.vf_off + i + 1); k < ke; ++k) {
+                        const uint32_t f = __ldg(d.vf + k);
+                        const uint4 fc = __ldg(d.faces + f);
+                        const f3 x1 = xyz(lp[fc.x]), x2 = xyz(lp[fc.y]), x3 = xyz(lp[fc.z]);
+                        const f3 G = coef * xyz(sface[f]);
+                        const f3 dx2 = cross(x3 - x1, G), dx3 = cross(G, x2 - x1);
+                        if (i == fc.x)
+                            acc = acc - (dx2 + dx3) + lv6 * cross(x2, x3);
+                        else if (i == fc.y)
+                            acc = acc + dx2 + lv6 * cross(x3, x1);
+                        else
+                            acc = acc + dx3 + lv6 * cross(x1, x2);
+                    }
+                    lx[i] = with_w(acc, 0.0f);
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // d loss / d force: v' gets sub_imp w with sub_imp = F dt / N
+    const float fs = dt_sub / float(nv > 0 ? nv : 1);
+    const float fx = block_sum<T>(sh, force_acc.x), fy = block_sum<T>(sh, force_acc.y), fz = block_sum<T>(sh, force_acc.z);
+    if (tid == 0) {
+        q.grad_force[3 * b + 0] += fx * fs;
+        q.grad_force[3 * b + 1] += fy * fs;
+        q.grad_force[3 * b + 2] += fz * fs;
+    }
+    for (uint32_t i = tid; i < nv; i += T) {
+        gax[i] = lx[i];
+        gav[i] = lv[i];
+    }
+    __syncthreads();
+}
+
+constexpr int kAdjThreads = 128;
+
+__global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(AdjParams q, uint32_t cap) {
+    extern __shared__ float4 smem[];
+    __shared__ AdjShared sh;
+    for (;;) {
+        if (threadIdx.x == 0) sh.item = atomicAdd(q.queue, 1u);
+        __syncthreads();
+        const uint32_t item = sh.item;
+        __syncthreads();
+        if (item >= q.num_work) return;
+        adjoint_body<kAdjThreads>(q, q.work[item], smem, cap, sh);
+    }
+}
+
+__global__ void add_kernel(float4 *__restrict__ dst, const float4 *__restrict__ src, uint64_t n) {
+    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+        float4 a = dst[i], b = src[i];
+        dst[i] = make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+    }
+}
+
+}  // namespace
+
+size_t adjoint_smem_bytes(uint32_t vertices, uint32_t faces) {
+    return size_t(vertices) * sizeof(float4) * 3 + size_t((vertices + 3) / 4) * sizeof(float4) + size_t(faces) * sizeof(float4);
+}
+
+cudaError_t init_adjoint_kernels(int max_dynamic_smem) {
+    return cudaFuncSetAttribute(adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+}
+
+int adjoint_occupancy(size_t smem) {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, adjoint_kernel, kAdjThreads, smem);
+    return n;
+}
+
+cudaError_t launch_adjoint(const AdjParams &q, uint32_t cap_vertices, uint32_t cap_faces, int grid, cudaStream_t stream) {
+    adjoint_kernel<<<grid, kAdjThreads, adjoint_smem_bytes(cap_vertices, cap_faces), stream>>>(q, cap_vertices);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_add(float4 *dst, const float4 *src, uint64_t n, int num_sms, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    uint64_t blocks = (n + 255) / 256, cap = uint64_t(num_sms) * 8;
+    add_kernel<<<unsigned(blocks < cap ? blocks : cap), 256, 0, stream>>>(dst, src, n);
+    return cudaGetLastError();
+}
+
+}  // namespace jsb

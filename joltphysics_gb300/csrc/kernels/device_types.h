@@ -81,6 +81,20 @@ struct ColliderDev {
     float restitution;
 };
 
+// Per-body tape of one checkpoint segment of a differentiable run (written by the taped forward step,
+// read by the adjoint step).
+struct TapeDesc {
+    float4 *cons;    // [segment substeps][slots][3]: constraint inputs as vertex differences
+    float4 *state;   // [segment substeps][3][num_vertices]: x at substep start, v after integration,
+                     //                                     x after the constraint levels
+    float4 *plane;   // [segment steps][num_vertices]: collision plane (normal, constant)
+    int32_t *shape;  // [segment steps][num_vertices]: colliding shape index, -1 none
+    float2 *cols;    // [segment steps][kMaxCollidingShapes]: combined friction, restitution
+    float *grad;     // [slots]: d loss / d compliance of the slot's constraint
+    uint32_t slots;
+    uint32_t pad;
+};
+
 struct StepParams {
     const BodyDesc *bodies;
     BodyState *states;
@@ -100,6 +114,23 @@ struct StepParams {
     const float *forces;  // 3 floats per body: AddForce accumulators consumed by this step
     const float *step_forces;  // 3 floats per body: force added before every step (persistent)
     uint32_t ring_slots;  // record ring capacity per level (multiple of 32); wider levels read HBM/L2 directly
+    const TapeDesc *tape;  // per-body tapes (taped forward only)
+    uint32_t tape_step;    // step index within the checkpoint segment (taped forward only)
+};
+
+// Parameters of one adjoint step over a set of bodies (the reverse of one forward step).
+struct AdjParams {
+    const BodyDesc *bodies;
+    const TapeDesc *tape;
+    uint32_t tape_step;  // step index within the checkpoint segment
+    const uint32_t *work;
+    uint32_t num_work;
+    uint32_t *queue;
+    float4 *adj_x;  // d loss / d position (local = world), context vertex indexing
+    float4 *adj_v;  // d loss / d velocity
+    float *grad_force;  // 3 per body
+    float gravity[3];
+    float dt;
 };
 
 }  // namespace jsb

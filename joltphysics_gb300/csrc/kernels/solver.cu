@@ -23,74 +23,11 @@
 #include <float.h>
 #include <stdint.h>
 
+#include "common.cuh"
 #include "device_types.h"
 
 namespace jsb {
 namespace {
-
-// IEEE-exact division and square root with a short path for zero operands. The hardware-independent
-// results are unchanged (0 / b = +-0 with the xor of the signs for finite non-zero b, NaN for b = 0 or
-// NaN; sqrt(+-0) = +-0), but the general IEEE routines take a slow path (several times the latency)
-// for zero inputs, which flat cloth and converged constraints produce constantly. The general routine
-// is still evaluated, on a non-zero stand-in, so both branches have the same latency.
-__device__ __forceinline__ float jdiv(float a, float b) {
-    float q = __fdiv_rn(a == 0.0f ? 1.0f : a, b);
-    if (a == 0.0f)
-        q = (b == 0.0f || b != b) ? __int_as_float(0x7fffffff) : __int_as_float((__float_as_int(a) ^ __float_as_int(b)) & int(0x80000000));
-    return q;
-}
-__device__ __forceinline__ float jsqrt(float a) {
-    float r = __fsqrt_rn(a == 0.0f ? 1.0f : a);
-    return a == 0.0f ? a : r;
-}
-
-struct f3 {
-    float x, y, z;
-};
-__device__ __forceinline__ f3 mk(float x, float y, float z) { return {x, y, z}; }
-__device__ __forceinline__ f3 xyz(float4 a) { return {a.x, a.y, a.z}; }
-__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-__device__ __forceinline__ f3 operator*(float s, f3 a) { return {s * a.x, s * a.y, s * a.z}; }
-__device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
-__device__ __forceinline__ f3 operator/(f3 a, float s) { return {jdiv(a.x, s), jdiv(a.y, s), jdiv(a.z, s)}; }
-__device__ __forceinline__ f3 neg(f3 a) { return {0.0f - a.x, 0.0f - a.y, 0.0f - a.z}; }
-__device__ __forceinline__ float dot(f3 a, f3 b) {
-    float px = a.x * b.x, py = a.y * b.y, pz = a.z * b.z;
-    return (px + py) + (pz + 0.0f);
-}
-__device__ __forceinline__ f3 cross(f3 a, f3 b) {
-    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
-}
-__device__ __forceinline__ float len_sq(f3 a) { return dot(a, a); }
-__device__ __forceinline__ float len(f3 a) { return jsqrt(len_sq(a)); }
-__device__ __forceinline__ f3 vmin(f3 a, f3 b) { return {a.x < b.x ? a.x : b.x, a.y < b.y ? a.y : b.y, a.z < b.z ? a.z : b.z}; }
-__device__ __forceinline__ f3 vmax(f3 a, f3 b) { return {a.x > b.x ? a.x : b.x, a.y > b.y ? a.y : b.y, a.z > b.z ? a.z : b.z}; }
-__device__ __forceinline__ f3 ld3(const float *p) { return {p[0], p[1], p[2]}; }
-__device__ __forceinline__ void st3(float *p, f3 a) {
-    p[0] = a.x;
-    p[1] = a.y;
-    p[2] = a.z;
-}
-__device__ __forceinline__ float4 with_w(f3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
-
-constexpr float kPi = 3.14159265358979323846f;
-
-// Jolt/Math/Trigonometry.h:48-65
-__device__ __forceinline__ float acos_approximate(float x) {
-    float ax = fabsf(x);
-    ax = ax > 1.0f ? 1.0f : ax;
-    float val = jsqrt(1.0f - ax) * (kPi / 2 - 0.175394f * ax);
-    return x < 0.0f ? kPi - val : val;
-}
-
-template <int T>
-__device__ __forceinline__ void cta_sync() {
-    if (T <= 32)
-        __syncwarp();
-    else
-        __syncthreads();
-}
 
 struct SCol {  // one colliding shape, relative to the soft body
     int32_t type;
@@ -253,8 +190,21 @@ __device__ __forceinline__ void ring_stage(const LevelRing &ring, const uint4 *_
 // Walks the dependency levels of one substep. Level l + kRingDepth is staged (cp.async) while level
 // l is projected, so the critical path of a level is: descriptor and records from shared memory,
 // positions from shared memory, projection, positions to shared memory, barrier.
-template <int T>
-__device__ __forceinline__ void apply_levels(float4 *sx, const BodyDesc &d, float inv_dt_sq, const LevelRing &ring) {
+// Records a constraint's inputs for the adjoint: vertex differences relative to its first vertex
+// (edge / LRA: x1 - x0; volume / bend: x2 - x1, x3 - x1, x4 - x1 in record order).
+__device__ __forceinline__ void tape_inputs(const float4 *sx, uint4 r, int type, float4 *out) {
+    const uint32_t a = r.x & 0xffff, b = r.x >> 16;
+    const f3 xa = xyz(sx[a]);
+    out[0] = with_w(xyz(sx[b]) - xa, 0.0f);
+    if (type <= 1) {
+        out[1] = with_w(xyz(sx[r.y & 0xffff]) - xa, 0.0f);
+        out[2] = with_w(xyz(sx[r.y >> 16]) - xa, 0.0f);
+    }
+}
+
+template <int T, bool kTape>
+__device__ __forceinline__ void apply_levels(float4 *sx, const BodyDesc &d, float inv_dt_sq, const LevelRing &ring,
+                                             float4 *tape_cons) {
     const uint4 *__restrict__ levels = d.levels;
     const uint4 *__restrict__ rec = d.records;
     const uint32_t tid = threadIdx.x;
@@ -283,7 +233,10 @@ __device__ __forceinline__ void apply_levels(float4 *sx, const BodyDesc &d, floa
         const uint4 *src = in_ring ? ring.rec + pos * ring.slots : rec + lv.x;
         for (uint32_t s = tid; s < n; s += T) {
             const uint4 r = src[s];
-            if (r.x != 0xffffffffu) project(sx, r, slot_type(lv, s), inv_dt_sq);
+            if (r.x != 0xffffffffu) {
+                if (kTape) tape_inputs(sx, r, slot_type(lv, s), tape_cons + size_t(lv.x + s) * 3);
+                project(sx, r, slot_type(lv, s), inv_dt_sq);
+            }
         }
         if (ahead <= L) ring_stage<T>(ring, levels, rec, ahead, L, lv_ahead, next_ahead);
         cp_async_commit();
@@ -422,7 +375,7 @@ __device__ __forceinline__ float reduce_sum(Shared &sh, float v, int slot) {
 //   kSmemState:  x[cap] | v[cap] (shape index in v.w) | prev[cap] | faces[...]
 //   otherwise:   x[cap] | faces[...]       (v, prev, shape stay in HBM)
 // faces: per-face triple product, then per-face pressure impulse (pressure bodies only).
-template <int T, bool kSmemState>
+template <int T, bool kSmemState, bool kTape = false>
 __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_t cap, Shared &sh) {
     const uint32_t tid = threadIdx.x;
     const BodyDesc d = p.bodies[b];
@@ -437,6 +390,8 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     float4 *sv = smem + cap;
     float4 *sprev = smem + 2 * cap;
     float4 *sface = smem + (kSmemState ? 3 * cap : cap);  // pressure faces; the record ring reuses it
+    TapeDesc td = {};
+    if (kTape) td = p.tape[b];
     LevelRing ring;
     ring.rec = reinterpret_cast<uint4 *>(sface);
     ring.desc = sh.ring_desc;
@@ -483,6 +438,9 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
             s.restitution = d.restitution > c.restitution ? d.restitution : c.restitution;
         }
         sh.ncols = n;
+        if (kTape)
+            for (int k = 0; k < n; ++k)
+                td.cols[size_t(p.tape_step) * kMaxCollidingShapes + k] = make_float2(sh.cols[k].friction, sh.cols[k].restitution);
     }
     // Stage the state in shared memory.
     for (uint32_t i = tid; i < nv; i += T) {
@@ -511,6 +469,10 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
         else
             gshape[i] = shape;
         if (shape >= 0) gplane[i] = plane;
+        if (kTape) {
+            td.plane[size_t(p.tape_step) * nv + i] = plane;
+            td.shape[size_t(p.tape_step) * nv + i] = shape;
+        }
     }
 
     const float inv_dt_sq = 1.0f / (dt_sub * dt_sub);
@@ -523,6 +485,11 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     const bool has_pressure = d.pressure > 0.0f && d.num_faces > 0;
 
     for (uint32_t it = 0; it < n_it; ++it) {
+        float4 *tape_state = nullptr;
+        if (kTape) {
+            tape_state = td.state + (size_t(p.tape_step) * n_it + it) * 3 * nv;
+            for (uint32_t i = tid; i < nv; i += T) tape_state[i] = sx[i];
+        }
         // ApplyPressure
         if (has_pressure) {
             float *s_six = reinterpret_cast<float *>(sface);
@@ -577,11 +544,15 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
                 gv[i] = with_w(v, vel.w);
             }
             sx[i] = with_w(xyz(pi) + v * dt_sub, pi.w);
+            if (kTape) tape_state[nv + i] = with_w(v, 0.0f);
         }
         __syncthreads();
         // Update groups in dependency-level order
-        apply_levels<T>(sx, d, inv_dt_sq, ring);
+        apply_levels<T, kTape>(sx, d, inv_dt_sq, ring,
+                               kTape ? td.cons + (size_t(p.tape_step) * n_it + it) * size_t(td.slots) * 3 : nullptr);
         __syncthreads();
+        if (kTape)
+            for (uint32_t i = tid; i < nv; i += T) tape_state[2 * nv + i] = sx[i];
         // ApplyCollisionConstraintsAndUpdateVelocities (static colliders)
         for (uint32_t i = tid; i < nv; i += T) {
             float4 pi = sx[i];
@@ -711,7 +682,7 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     __syncthreads();
 }
 
-template <int T, bool kSmemState>
+template <int T, bool kSmemState, bool kTape = false>
 __global__ void __launch_bounds__(T) step_kernel(StepParams p, uint32_t cap) {
     extern __shared__ float4 smem[];
     __shared__ Shared sh;
@@ -721,7 +692,7 @@ __global__ void __launch_bounds__(T) step_kernel(StepParams p, uint32_t cap) {
         const uint32_t item = sh.item;
         __syncthreads();
         if (item >= p.num_work) return;
-        step_body<T, kSmemState>(p, p.work[item], smem, cap, sh);
+        step_body<T, kSmemState, kTape>(p, p.work[item], smem, cap, sh);
     }
 }
 
@@ -751,6 +722,26 @@ cudaError_t launch_step(const StepParams &p, int threads, bool smem_state, uint3
     return cudaErrorInvalidValue;
 }
 
+// Taped forward step (differentiable runs): 128 threads per CTA, every body of the launch.
+cudaError_t launch_step_tape(const StepParams &p, bool smem_state, uint32_t smem_vertices, uint32_t smem_faces, int grid,
+                             cudaStream_t stream) {
+    size_t smem = step_smem_bytes(smem_state, smem_vertices, smem_faces, p.ring_slots);
+    if (smem_state)
+        step_kernel<128, true, true><<<grid, 128, smem, stream>>>(p, smem_vertices);
+    else
+        step_kernel<128, false, true><<<grid, 128, smem, stream>>>(p, smem_vertices);
+    return cudaGetLastError();
+}
+
+int step_tape_occupancy(bool smem_state, size_t smem) {
+    int n = 0;
+    if (smem_state)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<128, true, true>, 128, smem);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<128, false, true>, 128, smem);
+    return n;
+}
+
 // Allows every solver kernel instance to use up to `max_dynamic_smem` bytes of dynamic shared memory
 // (done once per device, outside any stream capture).
 cudaError_t init_step_kernels(int max_dynamic_smem) {
@@ -759,6 +750,8 @@ cudaError_t init_step_kernels(int max_dynamic_smem) {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel<TT, SS>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
     JSB_FOR_EACH_SHAPE(JSB_ATTR)
 #undef JSB_ATTR
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel<128, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel<128, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
     return e;
 }
 

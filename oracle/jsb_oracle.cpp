@@ -197,6 +197,7 @@ struct Body {
     V3<R> bmin, bmax, pmin, pmax;  // local bounds and predicted bounds
     V3<R> force;
     V3<R> lin_vel, ang_vel;
+    std::vector<R> edge_c, vol_c;  // per-constraint compliance (the settings' values unless overridden)
 };
 
 template <class R>
@@ -224,6 +225,8 @@ public:
         b.bmin = {big, big, big};
         b.bmax = {-big, -big, -big};
         b.v.resize(s->vertices.size());
+        for (const Edge &e : s->edges) b.edge_c.push_back(R(e.compliance));
+        for (const Volume &vol : s->volumes) b.vol_c.push_back(R(vol.compliance));
         for (size_t i = 0; i < s->vertices.size(); ++i) {  // SoftBodyMotionProperties::Initialize :59-105
             const SVertex &sv = s->vertices[i];
             Vertex<R> &o = b.v[i];
@@ -427,9 +430,9 @@ public:
         const Group &prev = gi > 0 ? s.groups[gi - 1] : start;
         const Group &cur = s.groups[gi];
         R inv_dt_sq = R(1) / (dt * dt);
-        for (uint32_t i = prev.volume; i < cur.volume; ++i) apply_volume(b, s.volumes[i], inv_dt_sq);
+        for (uint32_t i = prev.volume; i < cur.volume; ++i) apply_volume(b, s.volumes[i], b.vol_c[i], inv_dt_sq);
         for (uint32_t i = prev.bend; i < cur.bend; ++i) apply_bend(b, s.bends[i], inv_dt_sq);
-        for (uint32_t i = prev.edge; i < cur.edge; ++i) apply_edge(b, s.edges[i], inv_dt_sq);
+        for (uint32_t i = prev.edge; i < cur.edge; ++i) apply_edge(b, s.edges[i], b.edge_c[i], inv_dt_sq);
         for (uint32_t i = prev.lra; i < cur.lra; ++i) apply_lra(b, s.lras[i]);
     }
 
@@ -469,7 +472,7 @@ public:
         v3.pos = sub(x3, mul(ml * w3, d3c));
     }
 
-    void apply_volume(Body<R> &b, const Volume &c, R inv_dt_sq) {  // :458-507
+    void apply_volume(Body<R> &b, const Volume &c, R compliance, R inv_dt_sq) {  // :458-507
         Vertex<R> &v1 = b.v[c.v[0]], &v2 = b.v[c.v[1]], &v3 = b.v[c.v[2]], &v4 = b.v[c.v[3]];
         V3<R> x1 = v1.pos, x2 = v2.pos, x3 = v3.pos, x4 = v4.pos;
         V3<R> x1x2 = sub(x2, x1), x1x3 = sub(x3, x1), x1x4 = sub(x4, x1);
@@ -479,7 +482,7 @@ public:
         V3<R> d3c = cross(x1x4, x1x2);
         V3<R> d4c = cross(x1x2, x1x3);
         R w1 = v1.inv_mass, w2 = v2.inv_mass, w3 = v3.inv_mass, w4 = v4.inv_mass;
-        R denom = w1 * len_sq(d1c) + w2 * len_sq(d2c) + w3 * len_sq(d3c) + w4 * len_sq(d4c) + R(c.compliance) * inv_dt_sq;
+        R denom = w1 * len_sq(d1c) + w2 * len_sq(d2c) + w3 * len_sq(d3c) + w4 * len_sq(d4c) + compliance * inv_dt_sq;
         if (denom < R(1.0e-12f)) return;
         R ml = cval / denom;
         v1.pos = sub(x1, mul(ml * w1, d1c));
@@ -488,12 +491,12 @@ public:
         v4.pos = sub(x4, mul(ml * w4, d4c));
     }
 
-    void apply_edge(Body<R> &b, const Edge &c, R inv_dt_sq) {  // :573-601
+    void apply_edge(Body<R> &b, const Edge &c, R compliance, R inv_dt_sq) {  // :573-601
         Vertex<R> &v0 = b.v[c.v[0]], &v1 = b.v[c.v[1]];
         V3<R> x0 = v0.pos, x1 = v1.pos;
         V3<R> delta = sub(x1, x0);
         R length = len(delta);
-        R denom = length * (v0.inv_mass + v1.inv_mass + R(c.compliance) * inv_dt_sq);
+        R denom = length * (v0.inv_mass + v1.inv_mass + compliance * inv_dt_sq);
         if (denom < R(1.0e-12f)) return;
         V3<R> corr = divs(mul(delta, length - R(c.rest)), denom);
         v0.pos = add(x0, mul(v0.inv_mass, corr));
@@ -708,5 +711,44 @@ int oracle_get_world_positions_f64(void *w, int body, double *out) {
 }
 
 const char *oracle_last_error(void *w) { return static_cast<Handle *>(w)->err.c_str(); }
+
+// FP64 parameter setters for central finite differences (double world only): initial local positions
+// and velocities (3 doubles per vertex, may be NULL), per-constraint compliance, force.
+int oracle_set_state_f64(void *w, int body, const double *pos3, const double *vel3) {
+    Handle *h = static_cast<Handle *>(w);
+    auto &b = h->wd.bodies[body];
+    for (size_t i = 0; i < b.v.size(); ++i) {
+        if (pos3) b.v[i].pos = b.v[i].prev = {pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2]};
+        if (vel3) b.v[i].vel = {vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2]};
+    }
+    return 0;
+}
+
+int oracle_set_compliance_f64(void *w, int body, const double *edge, int num_edges, const double *vol, int num_vol) {
+    Handle *h = static_cast<Handle *>(w);
+    auto &b = h->wd.bodies[body];
+    if (edge)
+        for (int i = 0; i < num_edges && i < int(b.edge_c.size()); ++i) b.edge_c[i] = edge[i];
+    if (vol)
+        for (int i = 0; i < num_vol && i < int(b.vol_c.size()); ++i) b.vol_c[i] = vol[i];
+    return 0;
+}
+
+int oracle_set_force_f64(void *w, int body, const double f[3]) {
+    Handle *h = static_cast<Handle *>(w);
+    h->wd.bodies[body].force = {f[0], f[1], f[2]};
+    return 0;
+}
+
+int oracle_get_world_f64(void *w, int body, double *out) {
+    Handle *h = static_cast<Handle *>(w);
+    auto &b = h->wd.bodies[body];
+    for (size_t i = 0; i < b.v.size(); ++i) {
+        out[3 * i + 0] = b.position.x + b.v[i].pos.x;
+        out[3 * i + 1] = b.position.y + b.v[i].pos.y;
+        out[3 * i + 2] = b.position.z + b.v[i].pos.z;
+    }
+    return 0;
+}
 
 }  // extern "C"

@@ -176,6 +176,11 @@ class Oracle:
             L.oracle_get_body.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p]
             L.oracle_get_world_positions_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+            L.oracle_set_state_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+            L.oracle_set_compliance_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                                    ctypes.c_void_p, ctypes.c_int]
+            L.oracle_set_force_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+            L.oracle_get_world_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
             L.oracle_last_error.restype = ctypes.c_char_p
             L.oracle_last_error.argtypes = [ctypes.c_void_p]
             cls._lib = L
@@ -224,3 +229,79 @@ class Oracle:
         out = np.zeros((self.nv[i], 3), np.float64)
         self.lib().oracle_get_world_positions_f64(self.h, i, out.ctypes.data)
         return out
+
+
+def blob_arrays(blob: bytes):
+    """Initial local positions, velocities (N, 3) and inverse masses (N,) of a settings blob."""
+    n = struct.unpack_from("<I", blob, 0)[0]
+    v = np.frombuffer(blob, np.float32, 7 * n, 4).reshape(n, 7)
+    return v[:, 0:3].astype(np.float64), v[:, 3:6].astype(np.float64), v[:, 6].copy()
+
+
+def blob_compliance(blob: bytes):
+    """Edge and volume compliance arrays (settings order) of a settings blob."""
+    off, out = 0, {}
+    for name, size in [("v", 28), ("f", 16), ("e", 16), ("b", 24), ("vol", 24)]:
+        (n,) = struct.unpack_from("<I", blob, off)
+        out[name] = (off + 4, n)
+        off += 4 + n * size
+    eo, en = out["e"]
+    vo, vn = out["vol"]
+    edges = np.frombuffer(blob, np.float32, 4 * en, eo).reshape(en, 4)[:, 3].astype(np.float64) if en else np.zeros(0)
+    vols = np.frombuffer(blob, np.float32, 6 * vn, vo).reshape(vn, 6)[:, 5].astype(np.float64) if vn else np.zeros(0)
+    return edges, vols
+
+
+class FD64:
+    """Linear functionals of the FP64 oracle trajectory, for central finite differences.
+
+    loss(params) = sum over (step, body) seeds of seed . world positions after that step, with optional
+    per-body overrides of initial local positions "x0", velocities "v0", edge / volume compliance and a
+    step force "force" (added before every step, like the scene forces)."""
+
+    def __init__(self, scene: Scene, seeds: dict, steps: int):
+        self.scene, self.seeds, self.steps = scene, seeds, steps
+
+    def loss(self, overrides: dict | None = None) -> float:
+        overrides = overrides or {}
+        L = Oracle.lib()
+        o = Oracle(self.scene, use_double=True)
+        forces = {}
+        for b, body in enumerate(self.scene.bodies):
+            ov = overrides.get(b, {})
+            x0, v0, _ = blob_arrays(body.blob)
+            x0 = np.ascontiguousarray(ov.get("x0", x0), np.float64)
+            v0 = np.ascontiguousarray(ov.get("v0", v0), np.float64)
+            L.oracle_set_state_f64(o.h, b, x0.ctypes.data, v0.ctypes.data)
+            ec, vc = blob_compliance(body.blob)
+            ec = np.ascontiguousarray(ov.get("edge", ec), np.float64)
+            vc = np.ascontiguousarray(ov.get("volume", vc), np.float64)
+            L.oracle_set_compliance_f64(o.h, b, ec.ctypes.data, len(ec), vc.ctypes.data, len(vc))
+            forces[b] = np.ascontiguousarray(ov.get("force", np.asarray(body.force, np.float64)), np.float64)
+        total = 0.0
+        for step in range(1, self.steps + 1):
+            for b, f in forces.items():
+                if np.any(f != 0.0):
+                    L.oracle_set_force_f64(o.h, b, f.ctypes.data)
+            L.oracle_step(o.h, self.scene.dt, self.scene.collision_steps)
+            for b, r in self.seeds.get(step, {}).items():
+                w = np.zeros((self.scene.bodies[b].num_vertices, 3), np.float64)
+                L.oracle_get_world_f64(o.h, b, w.ctypes.data)
+                total += float((np.asarray(r, np.float64) * w).sum())
+        return total
+
+    def central(self, body: int, kind: str, index: tuple, eps: float) -> float:
+        """Central difference of the loss in one parameter component."""
+        base = self.base_params(body)[kind]
+        vals = []
+        for sgn in (1.0, -1.0):
+            p = base.copy()
+            p[index] += sgn * eps
+            vals.append(self.loss({body: {kind: p}}))
+        return (vals[0] - vals[1]) / (2.0 * eps)
+
+    def base_params(self, body: int) -> dict:
+        b = self.scene.bodies[body]
+        x0, v0, _ = blob_arrays(b.blob)
+        ec, vc = blob_compliance(b.blob)
+        return {"x0": x0, "v0": v0, "edge": ec, "volume": vc, "force": np.asarray(b.force, np.float64)}

@@ -1,0 +1,134 @@
+"""Hand-written adjoint of the GPU step against FP64 central finite differences of the CPU oracle.
+
+The loss is a random linear functional of world positions after chosen steps; its FP64 central
+differences (the oracle's double-precision evaluation of the same constraint order) are compared with the
+GPU adjoint's gradient for a random sample of initial positions, initial velocities, per-edge and
+per-volume compliance and step force. Bar: relative error <= 1e-3 (relative to the finite difference, or
+to 1e-2 of the largest finite difference of the same kind for near-zero components).
+"""
+import numpy as np
+import pytest
+
+from jsb_testlib import FD64, parse_scene
+
+pytestmark = pytest.mark.gpu
+
+EPS = {"x0": 1e-6, "v0": 1e-6, "force": 1e-6}
+
+
+def gpu_gradients(jsb, scene_bytes, seeds, steps, every, forces=None):
+    ctx = jsb.Context(0)
+    ctx.load_scene(scene_bytes)
+    ctx.set_scene_step_forces()
+    for b, f in (forces or {}).items():
+        ctx.set_step_force(b, f)
+    ctx.adjoint_begin(steps, every)
+    ctx.adjoint_forward()
+    for step, per_body in seeds.items():
+        for b, r in per_body.items():
+            ctx.adjoint_seed(step, b, r.astype(np.float32))
+    ctx.adjoint_backward()
+    out = [ctx.adjoint_gradients(b["id"], b["num_edges"], b["num_volumes"]) for b in ctx.bodies]
+    ctx.adjoint_end()
+    ctx.close()
+    return out
+
+
+def sample_and_compare(fd, grads, picks, rng):
+    errors = []
+    for body, kind, count in picks:
+        base = fd.base_params(body)[kind]
+        g = grads[body]
+        key = {"x0": "x0", "v0": "v0", "edge": "edge_compliance", "volume": "volume_compliance", "force": "force"}[kind]
+        gpu = g[key]
+        idxs = [tuple(np.unravel_index(rng.integers(base.size), base.shape)) for _ in range(count)]
+        fds, gps = [], []
+        for idx in idxs:
+            eps = EPS.get(kind, 1e-6 * abs(base[idx]) + 1e-14)
+            fds.append(fd.central(body, kind, idx, eps))
+            gps.append(float(gpu[idx]))
+        fds, gps = np.array(fds), np.array(gps)
+        floor = 1e-2 * np.abs(fds).max() + 1e-30
+        rel = np.abs(gps - fds) / np.maximum(np.abs(fds), floor)
+        errors.append((kind, body, rel.max(), fds, gps))
+    return errors
+
+
+def test_adjoint_cloth_vs_fd(jsb):
+    scene_bytes = jsb.build_scene("diff_cloth", n=10, steps=16)
+    scene, _ = parse_scene(scene_bytes)
+    rng = np.random.default_rng(7)
+    nv = scene.bodies[0].num_vertices
+    seeds = {8: {0: rng.standard_normal((nv, 3))}, 16: {0: rng.standard_normal((nv, 3))}}
+    force = {0: np.array([0.3, -0.2, 0.1], np.float32)}
+    grads = gpu_gradients(jsb, scene_bytes, seeds, 16, 5, force)
+    fd = FD64(scene, seeds, 16)
+    scene.bodies[0].force = tuple(float(v) for v in force[0])
+    errs = sample_and_compare(fd, grads, [(0, "x0", 10), (0, "v0", 10), (0, "edge", 9), (0, "force", 3)], rng)
+    for kind, body, e, fds, gps in errs:
+        print(kind, body, "max rel", e)
+    assert max(e for _, _, e, _, _ in errs) <= 1e-3, [(k, e) for k, _, e, _, _ in errs]
+
+
+def test_adjoint_batch_with_contacts_vs_fd(jsb):
+    """Cloths and pressurised tet cubes falling onto a floor and a sphere, with step forces."""
+    scene_bytes = jsb.build_scene("diff_batch", n_cloth=2, n_cube=2, steps=40)
+    scene, _ = parse_scene(scene_bytes)
+    rng = np.random.default_rng(11)
+    seeds = {40: {b: rng.standard_normal((body.num_vertices, 3)) for b, body in enumerate(scene.bodies)},
+             25: {2: rng.standard_normal((scene.bodies[2].num_vertices, 3))}}
+    grads = gpu_gradients(jsb, scene_bytes, seeds, 40, 10)
+    fd = FD64(scene, seeds, 40)
+    errs = sample_and_compare(fd, grads, [(0, "x0", 6), (0, "force", 3), (2, "v0", 6), (2, "volume", 6), (3, "force", 3)],
+                              rng)
+    for kind, body, e, fds, gps in errs:
+        print(kind, body, "max rel", e)
+    assert max(e for _, _, e, _, _ in errs) <= 1e-3, [(k, b, e) for k, b, e, _, _ in errs]
+
+
+def test_checkpoint_interval_does_not_change_gradients(jsb):
+    scene_bytes = jsb.build_scene("diff_batch", n_cloth=2, n_cube=1, steps=12)
+    scene, _ = parse_scene(scene_bytes)
+    rng = np.random.default_rng(3)
+    seeds = {12: {b: rng.standard_normal((body.num_vertices, 3)) for b, body in enumerate(scene.bodies)}}
+    a = gpu_gradients(jsb, scene_bytes, seeds, 12, 1)
+    b = gpu_gradients(jsb, scene_bytes, seeds, 12, 5)
+    for ga, gb in zip(a, b):
+        for k in ga:
+            assert np.array_equal(ga[k], gb[k]), k
+
+
+def test_torch_autograd_binding(jsb):
+    """rollout() as a torch.autograd.Function: its gradient equals the C ABI's and follows FD."""
+    import torch
+
+    from joltphysics_gb300.autograd import Simulation, rollout
+
+    scene_bytes = jsb.build_scene("diff_cloth", n=8, steps=10)
+    scene, _ = parse_scene(scene_bytes)
+    ctx = jsb.Context(0)
+    ctx.load_scene(scene_bytes)
+    sim = Simulation(ctx, checkpoint_every=4)
+    from jsb_testlib import blob_arrays, blob_compliance
+
+    x0n, v0n, _ = blob_arrays(scene.bodies[0].blob)
+    ecn, _ = blob_compliance(scene.bodies[0].blob)
+    x0 = torch.tensor(x0n, dtype=torch.float32, requires_grad=True)
+    v0 = torch.tensor(v0n, dtype=torch.float32, requires_grad=True)
+    ec = torch.tensor(ecn, dtype=torch.float32, requires_grad=True)
+    force = torch.zeros((1, 3), dtype=torch.float32, requires_grad=True)
+    rng = np.random.default_rng(5)
+    target = torch.tensor(rng.standard_normal((2, x0n.shape[0], 3)) * 0.01, dtype=torch.float32)
+    pos = rollout(sim, x0, v0, ec, force, (5, 10))
+    base = torch.tensor(np.asarray(scene.bodies[0].position, np.float32))
+    loss = ((pos - (base + torch.tensor(x0n, dtype=torch.float32)) - target) ** 2).mean()
+    loss.backward()
+    assert torch.isfinite(x0.grad).all() and torch.isfinite(ec.grad).all() and torch.isfinite(force.grad).all()
+    # d loss / d pos is linear in pos: check v0 gradient components against FP64 finite differences
+    g_pos = (2.0 / pos.numel()) * (pos - (base + torch.tensor(x0n, dtype=torch.float32)) - target).detach().numpy()
+    seeds = {5: {0: g_pos[0]}, 10: {0: g_pos[1]}}
+    fd = FD64(scene, seeds, 10)
+    for idx in [(3, 1), (20, 0), (40, 2)]:
+        f = fd.central(0, "v0", idx, 1e-6)
+        assert abs(float(v0.grad[idx]) - f) <= 1e-3 * max(abs(f), 1e-6), (idx, float(v0.grad[idx]), f)
+    ctx.close()
