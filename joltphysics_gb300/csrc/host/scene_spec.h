@@ -432,8 +432,9 @@ inline SceneSpec make_diff_cloth(uint64_t seed = 4, uint32_t n = 64, int steps =
 // Differentiable batch: `n_cloth` cloths with side U{16..48} (0.05 m spacing, edges only, one border
 // row pinned) and `n_cube` 5-tet cubes with U{4..8} cells of 0.25 m and pressure 5e2; per-body
 // force N(0, 2 N) per axis, initial velocity N(0, 0.5 m/s); static box floor and a sphere of
-// radius 0.5; 90 steps with 5 iterations.
-inline SceneSpec make_diff_batch(uint64_t seed = 5, uint32_t n_cloth = 192, uint32_t n_cube = 64, int steps = 90) {
+// radius 0.5; 90 steps with 5 iterations. drop_height: gap between the bodies and the floor level.
+inline SceneSpec make_diff_batch(uint64_t seed = 5, uint32_t n_cloth = 192, uint32_t n_cube = 64, int steps = 90,
+                                 float drop_height = 1.0f) {
     SceneSpec s;
     Rng rng(seed);
     for (uint32_t i = 0; i < n_cloth + n_cube; ++i) {
@@ -444,12 +445,12 @@ inline SceneSpec make_diff_batch(uint64_t seed = 5, uint32_t n_cloth = 192, uint
             b.mesh = make_edge_pinned_cloth(n, 0.05f, side);
             b.mesh.attributes = VertexAttributes{1.0e-5f, 1.0e-5f, 3.402823466e+38f};
             b.mesh.bend_type = BendType::None;
-            b.position[1] = 0.5f * 0.05f * float(n) + 1.0f;
+            b.position[1] = 0.5f * 0.05f * float(n) + drop_height;
         } else {
             uint32_t n = uint32_t(rng.uniform_int(4, 8));
             b.mesh = make_tet_cube(n, 0.25f, 0.0f, 1.0e-6f);
             b.creation.pressure = 5.0e2f;
-            b.position[1] = 0.5f * 0.25f * float(n) + 1.0f;
+            b.position[1] = 0.5f * 0.25f * float(n) + drop_height;
         }
         for (int k = 0; k < 3; ++k) b.force[k] = float(2.0 * rng.normal());
         float v0[3];
