@@ -153,10 +153,19 @@ jsb_status jsb_settings_schedule(const void *blob, size_t len, uint32_t *num_lev
 
 /* Launch shape of the size bucket of bodies with vertex count <= max_vertices (and above the next
  * smaller bucket): threads per CTA in {32, 64, 128, 256}; state_mode 0 keeps positions, velocities and
- * previous positions in shared memory when they fit, 1 keeps only positions there. The autotuner
- * writes this table; the calls below set or read it directly. */
+ * previous positions in shared memory when they fit, 1 keeps only positions there, 2 sends the
+ * bucket's bodies to the thread-block-cluster path. The autotuner writes this table; the calls below
+ * set or read it directly. Bodies whose positions do not fit one CTA's shared memory always take the
+ * cluster path. */
 jsb_status jsb_set_bucket_config(jsb_context *ctx, uint32_t max_vertices, uint32_t threads, uint32_t state_mode);
 jsb_status jsb_set_bucket_threads(jsb_context *ctx, uint32_t max_vertices, uint32_t threads);
+/* Thread-block-cluster path (bodies too large for one SM, up to 65,536 vertices; no counterpart in the
+ * reference, whose SoftBodyMotionProperties::ParallelUpdate spreads one body over job-system threads,
+ * SoftBodyMotionProperties.cpp:1057-1115): CTAs per cluster in {2, 4, 8, 16} (0 = the largest that fits)
+ * and threads per CTA in {128, 256, 512}. The getter reports the shape in use after the launch groups
+ * are built, and how many bodies take the path. */
+jsb_status jsb_set_cluster_config(jsb_context *ctx, uint32_t cluster_size, uint32_t threads);
+jsb_status jsb_get_cluster_config(jsb_context *ctx, uint32_t *cluster_size, uint32_t *threads, uint32_t *num_bodies);
 jsb_status jsb_get_bucket_config(jsb_context *ctx, uint32_t index, uint32_t *max_vertices, uint32_t *threads,
                                  uint32_t *state_mode);
 /* Tunes the bucket table on the context's own bodies (coordinate descent, each shape timed as a

@@ -22,6 +22,7 @@ STATUS_NAMES = {
     1: "JSB_ERR_INVALID_ARGUMENT", 2: "JSB_ERR_BLOB", 3: "JSB_ERR_UNSUPPORTED", 4: "JSB_ERR_CUDA",
     5: "JSB_ERR_OUT_OF_MEMORY", 6: "JSB_ERR_TIMEOUT", 7: "JSB_ERR_NONFINITE", 8: "JSB_ERR_CAPACITY",
 }
+globals().update({name: code for code, name in STATUS_NAMES.items()})
 
 # Every entry point of include/jsb.h with its ctypes signature.
 _c = ctypes
@@ -53,6 +54,8 @@ SIGNATURES = {
     "jsb_set_bucket_config": [_P, _c.c_uint32, _c.c_uint32, _c.c_uint32],
     "jsb_set_bucket_threads": [_P, _c.c_uint32, _c.c_uint32],
     "jsb_get_bucket_config": [_P, _c.c_uint32, _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32)],
+    "jsb_set_cluster_config": [_P, _c.c_uint32, _c.c_uint32],
+    "jsb_get_cluster_config": [_P, _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32)],
     "jsb_autotune": [_P, _c.c_float, _c.c_int],
     "jsb_last_launch_count": [_P, _c.POINTER(_c.c_uint32)],
     "jsb_last_kernel_ms": [_P, _c.POINTER(_c.c_float)],
@@ -147,6 +150,7 @@ class Context:
         self.h = ctypes.c_void_p()
         check(lib().jsb_context_create(device, ctypes.byref(self.h)))
         self.num_vertices: list[int] = []
+        self.bodies: list[dict] = []
 
     def close(self):
         if self.h:
@@ -185,7 +189,8 @@ class Context:
         return cid.value
 
     def load_scene(self, scene_bytes: bytes) -> list[dict]:
-        """Adds the colliders and bodies of a serialised scene; returns per-body info."""
+        """Adds the colliders and bodies of a serialised scene; returns per-body info of the added bodies
+        (`self.bodies` lists every body of the context)."""
         b = scene_bytes
         assert b[:4] == b"JSBS"
         _, nb, nc = struct.unpack_from("<III", b, 4)
@@ -212,7 +217,7 @@ class Context:
             bodies.append({"id": bid, "force": force, "iterations": cr[0], "vertices": self.num_vertices[bid],
                            "position": pos, "num_edges": counts["edges"], "num_volumes": counts["volumes"],
                            "num_bends": counts["bends"]})
-        self.bodies = bodies
+        self.bodies = self.bodies + bodies
         return bodies
 
     # -- stepping --------------------------------------------------------------------------------
@@ -257,6 +262,15 @@ class Context:
 
     def set_bucket_config(self, max_vertices: int, threads: int, state_mode: int):
         check(lib().jsb_set_bucket_config(self.h, max_vertices, threads, state_mode))
+
+    def set_cluster_config(self, cluster_size: int = 0, threads: int = 256):
+        """Shape of the thread-block-cluster path (cluster_size 0 = largest that fits)."""
+        check(lib().jsb_set_cluster_config(self.h, cluster_size, threads))
+
+    def cluster_config(self) -> dict:
+        c, t, n = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        check(lib().jsb_get_cluster_config(self.h, ctypes.byref(c), ctypes.byref(t), ctypes.byref(n)))
+        return {"cluster_size": c.value, "threads": t.value, "bodies": n.value}
 
     def bucket_table(self) -> list[tuple[int, int, int]]:
         out, i = [], 0

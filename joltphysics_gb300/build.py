@@ -23,7 +23,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["kernels/solver.cu", "kernels/adjoint.cu", "kernels/state_io.cu"]
+CU_SOURCES = ["kernels/solver.cu", "kernels/cluster.cu", "kernels/adjoint.cu", "kernels/state_io.cu"]
 CXX_SOURCES = ["host/runtime.cpp", "host/schedule.cpp", "host/shared_settings.cpp"]
 
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-std=c++17",

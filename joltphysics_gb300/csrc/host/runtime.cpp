@@ -37,6 +37,11 @@ cudaError_t init_step_kernels(int max_dynamic_smem);
 cudaError_t launch_step_tape(const StepParams &p, bool smem_state, uint32_t smem_vertices, uint32_t smem_faces, int grid,
                              cudaStream_t stream);
 int step_tape_occupancy(bool smem_state, size_t smem);
+size_t cluster_smem_bytes(uint32_t shift, uint32_t desc_cap, uint32_t rpt, int threads);
+cudaError_t launch_cluster_step(const StepParams &p, int cluster, int threads, uint32_t shift, uint32_t desc_cap, uint32_t rpt,
+                                cudaStream_t stream);
+cudaError_t init_cluster_kernels(int max_dynamic_smem);
+int cluster_occupancy(int cluster, int threads, size_t smem);
 size_t adjoint_smem_bytes(uint32_t vertices, uint32_t faces);
 cudaError_t init_adjoint_kernels(int max_dynamic_smem);
 int adjoint_occupancy(size_t smem);
@@ -125,10 +130,13 @@ struct BodyRec {
 struct Bucket {
     uint32_t max_vertices;
     int threads;
-    int state_mode;  // 0: x, v, prev in shared memory when they fit; 1: only positions in shared memory
+    int state_mode;  // 0: x, v, prev in shared memory when they fit; 1: only positions in shared memory;
+                     // 2: thread-block-cluster path
 };
 
-struct LaunchGroup {  // the bodies of one bucket
+struct LaunchGroup {  // the bodies of one bucket (or every body on the cluster path)
+    int cluster = 0;  // > 0: CTAs per cluster, one cluster per body (cluster.cu)
+    uint32_t shift = 0, desc_cap = 0, rpt = 1;  // cluster path: vertices per CTA (log2), cached level descriptors, ring depth
     int threads = 0;
     bool smem_state = true;  // velocities / previous positions staged in shared memory
     uint32_t smem_vertices = 0, smem_faces = 0;
@@ -181,6 +189,8 @@ struct jsb_context {
     std::vector<jsb::BodyRec> bodies;
     std::vector<jsb::ColliderDev> colliders;
     std::vector<jsb::Bucket> buckets;
+    int cluster_size = 0;       // CTAs per cluster on the cluster path, 0 = largest that fits
+    int cluster_threads = 256;  // threads per CTA on the cluster path
     // device state
     bool dirty = true;  // structure changed: device arrays must be rebuilt
     bool groups_dirty = true;  // bucket table changed: launch groups must be rebuilt
@@ -269,6 +279,7 @@ uint32_t pressure_faces(const SettingsRec &s, const BodyRec &b) {
 }
 
 constexpr uint32_t kMaxRingSlots = 256;
+constexpr uint32_t kMaxCachedLevels = 4096;  // level descriptors a cluster CTA keeps in shared memory
 
 uint32_t ring_slots_for(const SettingsRec &s) {
     uint32_t r = (s.schedule.max_level_slots + 31u) & ~31u;
@@ -355,6 +366,47 @@ jsb_status rebuild(jsb_context *ctx) {
     return rebuild_groups(ctx);
 }
 
+// The launch group of the cluster path: one cluster per body; the cluster size is the configured one,
+// or the largest (16, 8, 4, 2) that the device can co-schedule with the shared memory it needs.
+jsb_status make_cluster_group(jsb_context *ctx, const std::vector<uint32_t> &bodies, size_t cap) {
+    uint32_t max_nv = 0, max_levels = 0, max_slots = 0;
+    for (uint32_t bi : bodies) {
+        const SettingsRec &s = *ctx->settings[ctx->bodies[bi].settings_id];
+        max_nv = std::max(max_nv, uint32_t(s.parsed.vertices.size()));
+        max_levels = std::max(max_levels, s.schedule.num_levels);
+        max_slots = std::max(max_slots, s.schedule.max_level_slots);
+    }
+    const int T = ctx->cluster_threads;
+    const int sizes[4] = {16, 8, 4, 2};
+    for (int c : sizes) {
+        if (ctx->cluster_size > 0 && c != ctx->cluster_size) continue;
+        const uint32_t per_cta = std::max<uint32_t>(32u, (max_nv + uint32_t(c) - 1) / uint32_t(c));
+        uint32_t shift = 5;
+        while ((1u << shift) < per_cta) ++shift;
+        uint32_t rpt = std::max<uint32_t>(1u, std::min<uint32_t>(4u, (max_slots + uint32_t(c * T) - 1) / uint32_t(c * T)));
+        uint32_t desc_cap = std::min<uint32_t>(max_levels + 2, kMaxCachedLevels);
+        // Shrink the descriptor cache, then the ring, until the CTA fits.
+        while (cluster_smem_bytes(shift, desc_cap, rpt, T) > cap && desc_cap > 0) desc_cap = desc_cap > 256 ? desc_cap - 256 : 0;
+        while (cluster_smem_bytes(shift, desc_cap, rpt, T) > cap && rpt > 1) --rpt;
+        const size_t smem = cluster_smem_bytes(shift, desc_cap, rpt, T);
+        if (smem > cap || cluster_occupancy(c, T, smem) < 1) continue;
+        ctx->groups.emplace_back();
+        LaunchGroup &g = ctx->groups.back();
+        g.cluster = c;
+        g.threads = T;
+        g.shift = shift;
+        g.desc_cap = desc_cap;
+        g.rpt = rpt;
+        g.smem_vertices = max_nv;
+        g.bodies = bodies;
+        g.grid = c * int(bodies.size());
+        JSB_CUDA(g.work.upload(g.bodies.data(), g.bodies.size()));
+        JSB_CUDA(cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming));
+        return JSB_OK;
+    }
+    return fail(JSB_ERR_UNSUPPORTED, "a body with " + std::to_string(max_nv) + " vertices does not fit a thread-block cluster");
+}
+
 // One launch group per non-empty bucket: dynamic shared memory sized for its largest body, ring
 // capacity for its widest level, bodies queued longest first.
 jsb_status rebuild_groups(jsb_context *ctx) {
@@ -362,10 +414,20 @@ jsb_status rebuild_groups(jsb_context *ctx) {
     free_groups(ctx);
     const size_t cap = ctx->max_smem_optin - kStaticSmemReserve;
     std::vector<std::vector<std::pair<double, uint32_t>>> members(ctx->buckets.size());
+    std::vector<uint32_t> cluster_bodies;
     for (size_t bi = 0; bi < ctx->bodies.size(); ++bi) {
         const BodyRec &b = ctx->bodies[bi];
         const SettingsRec &s = *ctx->settings[b.settings_id];
-        size_t k = bucket_for(ctx, uint32_t(s.parsed.vertices.size()));
+        const uint32_t nv = uint32_t(s.parsed.vertices.size());
+        size_t k = bucket_for(ctx, nv);
+        // Bodies whose positions do not fit one CTA's shared memory take the cluster path.
+        if (ctx->buckets[k].state_mode == 2 || step_smem_bytes(false, nv, pressure_faces(s, b), ring_slots_for(s)) > cap) {
+            if (pressure_faces(s, b) > 0)
+                return fail(JSB_ERR_UNSUPPORTED, "a pressurised body with " + std::to_string(nv) +
+                                                     " vertices is too large for one CTA, and the cluster path has no pressure");
+            cluster_bodies.push_back(uint32_t(bi));
+            continue;
+        }
         members[k].push_back({body_cost(s, b, ctx->buckets[k].threads), uint32_t(bi)});
     }
     for (size_t k = 0; k < ctx->buckets.size(); ++k) {
@@ -393,6 +455,10 @@ jsb_status rebuild_groups(jsb_context *ctx) {
         if (occ <= 0) return fail(JSB_ERR_UNSUPPORTED, "solver kernel does not fit on an SM with this shared memory size");
         g.grid = int(std::min<size_t>(g.bodies.size(), size_t(occ) * ctx->num_sms));
         JSB_CUDA(cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming));
+    }
+    if (!cluster_bodies.empty()) {
+        jsb_status st = make_cluster_group(ctx, cluster_bodies, cap);
+        if (st != JSB_OK) return st;
     }
     // Larger buckets get higher stream priority (and are launched first): their bodies carry the
     // longest dependency chains, and a CTA sized for them needs an SM nobody else occupies.
@@ -447,7 +513,10 @@ jsb_status enqueue_batched(jsb_context *ctx, float dt, cudaStream_t stream, uint
         p.num_work = uint32_t(g.bodies.size());
         p.queue = ctx->queues.ptr + gi;
         p.ring_slots = g.ring_slots;
-        JSB_CUDA(launch_step(p, g.threads, g.smem_state, g.smem_vertices, g.smem_faces, g.grid, g.stream));
+        if (g.cluster > 0)
+            JSB_CUDA(launch_cluster_step(p, g.cluster, g.threads, g.shift, g.desc_cap, g.rpt, g.stream));
+        else
+            JSB_CUDA(launch_step(p, g.threads, g.smem_state, g.smem_vertices, g.smem_faces, g.grid, g.stream));
         ++launches;
         JSB_CUDA(cudaEventRecord(g.done, g.stream));
         JSB_CUDA(cudaStreamWaitEvent(stream, g.done, 0));
@@ -487,8 +556,11 @@ jsb_status step_impl(jsb_context *ctx, float dt, int collision_steps, cudaStream
                     p.queue = ctx->queues.ptr;
                     const SettingsRec &s = *ctx->settings[ctx->bodies[b].settings_id];
                     p.ring_slots = ring_slots_for(s);
-                    JSB_CUDA(launch_step(p, g.threads, g.smem_state, uint32_t(s.parsed.vertices.size()),
-                                         pressure_faces(s, ctx->bodies[b]), 1, stream));
+                    if (g.cluster > 0)
+                        JSB_CUDA(launch_cluster_step(p, g.cluster, g.threads, g.shift, g.desc_cap, g.rpt, stream));
+                    else
+                        JSB_CUDA(launch_step(p, g.threads, g.smem_state, uint32_t(s.parsed.vertices.size()),
+                                             pressure_faces(s, ctx->bodies[b]), 1, stream));
                     ++launches;
                 }
             }
@@ -542,6 +614,7 @@ jsb_status jsb_context_create(int device, jsb_context **out) {
     // static shared memory of the solver kernel is under 4 KB
     JSB_CUDA(init_step_kernels(int(ctx->max_smem_optin - kStaticSmemReserve)));
     JSB_CUDA(init_adjoint_kernels(int(ctx->max_smem_optin - kStaticSmemReserve)));
+    JSB_CUDA(init_cluster_kernels(int(ctx->max_smem_optin - kStaticSmemReserve)));
     JSB_CUDA(cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming));
     JSB_CUDA(cudaEventCreate(&ctx->t0));
     JSB_CUDA(cudaEventCreate(&ctx->t1));
@@ -935,7 +1008,7 @@ jsb_status jsb_set_bucket_config(jsb_context *ctx, uint32_t max_vertices, uint32
     if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
     if (threads != 32 && threads != 64 && threads != 128 && threads != 256)
         return fail(JSB_ERR_INVALID_ARGUMENT, "threads must be 32, 64, 128 or 256");
-    if (state_mode > 1) return fail(JSB_ERR_INVALID_ARGUMENT, "state_mode must be 0 or 1");
+    if (state_mode > 2) return fail(JSB_ERR_INVALID_ARGUMENT, "state_mode must be 0, 1 or 2");
     bool found = false;
     for (Bucket &b : ctx->buckets)
         if (b.max_vertices == max_vertices) {
@@ -946,6 +1019,34 @@ jsb_status jsb_set_bucket_config(jsb_context *ctx, uint32_t max_vertices, uint32
     if (!found) ctx->buckets.push_back({max_vertices, int(threads), int(state_mode)});
     std::sort(ctx->buckets.begin(), ctx->buckets.end(), [](const Bucket &a, const Bucket &b) { return a.max_vertices < b.max_vertices; });
     ctx->groups_dirty = true;
+    return JSB_OK;
+}
+
+jsb_status jsb_set_cluster_config(jsb_context *ctx, uint32_t cluster_size, uint32_t threads) {
+    if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
+    if (cluster_size != 0 && cluster_size != 2 && cluster_size != 4 && cluster_size != 8 && cluster_size != 16)
+        return fail(JSB_ERR_INVALID_ARGUMENT, "cluster_size must be 0 (automatic), 2, 4, 8 or 16");
+    if (threads != 128 && threads != 256 && threads != 512)
+        return fail(JSB_ERR_INVALID_ARGUMENT, "threads must be 128, 256 or 512 on the cluster path");
+    ctx->cluster_size = int(cluster_size);
+    ctx->cluster_threads = int(threads);
+    ctx->groups_dirty = true;
+    return JSB_OK;
+}
+
+jsb_status jsb_get_cluster_config(jsb_context *ctx, uint32_t *cluster_size, uint32_t *threads, uint32_t *num_bodies) {
+    if (!check_ctx(ctx) || !cluster_size || !threads || !num_bodies) return fail(JSB_ERR_INVALID_ARGUMENT, "null argument");
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    *cluster_size = uint32_t(ctx->cluster_size);
+    *threads = uint32_t(ctx->cluster_threads);
+    *num_bodies = 0;
+    for (const LaunchGroup &g : ctx->groups)
+        if (g.cluster > 0) {
+            *cluster_size = uint32_t(g.cluster);
+            *threads = uint32_t(g.threads);
+            *num_bodies = uint32_t(g.bodies.size());
+        }
     return JSB_OK;
 }
 

@@ -1,0 +1,412 @@
+// Soft-body step for bodies too large for one CTA's shared memory (up to 65,536 vertices): one
+// thread-block cluster advances one body through one full step (the same reference functions as
+// solver.cu: SoftBodyMotionProperties.cpp InitializeUpdateContext :937-960, DetermineCollidingShapes
+// :120-255, DetermineCollisionPlanes :257-265, N x {IntegratePositions :325-365,
+// ParallelApplyConstraints :1057-1115, ApplyCollisionConstraintsAndUpdateVelocities :700-825},
+// UpdateSoftBodyState :827-921).
+//
+// Vertex ownership: CTA r of the cluster owns vertices [r << shift, (r + 1) << shift) and keeps their
+// positions (+ inverse mass) in its shared memory for the whole step; velocities, previous positions,
+// planes and shape indices of its vertices stay in HBM (they are touched once per substep, by the
+// owner, coalesced). A constraint reads and writes its vertices wherever they live through distributed
+// shared memory (mapa + ld/st.shared::cluster). Every dependency level ends at a cluster barrier
+// (arrive.release / wait.acquire), so the level schedule gives the same bitwise result as the one-CTA
+// solver and as the reference's sequential Gauss-Seidel walk.
+//
+// Level slots are dealt round-robin over all threads of the cluster. Each thread streams the records
+// it will project a few levels ahead into its own slice of a shared-memory ring with cp.async, so no
+// barrier is needed for the ring: a thread only waits for its own copies. The level descriptors are
+// copied into shared memory once per step.
+//
+// Pressure (ApplyPressure) needs a sequential sum over all faces and is not supported on this path;
+// the host rejects such bodies. The taped (differentiable) step does not run here either.
+
+#include <cuda_runtime.h>
+#include <float.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "device_types.h"
+#include "projection.cuh"
+
+namespace jsb {
+namespace {
+
+// ---- cluster primitives ------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cluster_size() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return uint32_t(__cvta_generic_to_shared(p)); }
+// Address of the same shared-memory location in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t map_rank(uint32_t local, uint32_t rank) {
+    uint32_t out;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(out) : "r"(local), "r"(rank));
+    return out;
+}
+__device__ __forceinline__ float ld_cluster_f32(uint32_t addr) {
+    float v;
+    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr) : "memory");
+    return v;
+}
+__device__ __forceinline__ int ld_cluster_s32(uint32_t addr) {
+    int v;
+    asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+    return v;
+}
+
+// Position store spread over the cluster: vertex i is at offset (i & mask) of CTA (i >> shift).
+struct ClusterX {
+    uint32_t base;  // shared::cta address of the position array (same in every CTA)
+    uint32_t shift;
+};
+__device__ __forceinline__ uint32_t vertex_addr(ClusterX c, uint32_t i) {
+    return map_rank(c.base + ((i & ((1u << c.shift) - 1u)) << 4), i >> c.shift);
+}
+__device__ __forceinline__ float4 ldx(ClusterX c, uint32_t i) {
+    float4 v;
+    asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(vertex_addr(c, i)));
+    return v;
+}
+__device__ __forceinline__ void stx(ClusterX c, uint32_t i, float4 v) {
+    asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(vertex_addr(c, i)), "f"(v.x), "f"(v.y), "f"(v.z),
+                 "f"(v.w)
+                 : "memory");
+}
+
+constexpr int kCRingDepth = 3;  // levels staged ahead
+constexpr int kCRingLevels = kCRingDepth + 1;
+
+// Per-CTA partial results of UpdateSoftBodyState, read by rank 0 through distributed shared memory.
+struct Partials {
+    float val[12];  // min x, y, z | max x, y, z | predicted min x, y, z | predicted max x, y, z
+    int idx[12];
+    float sum[6];  // linear velocity, angular velocity sums
+};
+
+struct CShared {
+    SCol cols[kMaxCollidingShapes];
+    int ncols;
+    float delta[3];
+    Partials part;
+    float red[32][4];
+    int redi[32][4];
+};
+
+// Walks the dependency levels of one substep with every thread of the cluster. Thread g of the cluster
+// projects slots g, g + G, g + 2G, ... of each level (G = cluster threads); the first `rpt` of them are
+// staged kCRingDepth levels ahead into the thread's ring slice.
+template <int T>
+__device__ __forceinline__ void cluster_levels(ClusterX cx, const BodyDesc &d, const uint4 *sdesc, uint32_t desc_cap, uint4 *ring,
+                                               uint32_t rpt, uint32_t g, uint32_t G, float inv_dt_sq) {
+    const uint32_t L = d.num_levels;
+    if (L == 0) return;
+    const uint4 *__restrict__ rec = d.records;
+    const uint4 *__restrict__ levels = d.levels;
+    uint4 *mine = ring + threadIdx.x;
+    auto desc = [&](uint32_t l) { return l < desc_cap ? sdesc[l] : __ldg(levels + l); };
+    auto stage = [&](uint32_t l) {
+        const uint4 lv = desc(l);
+        const uint32_t n = desc(l + 1).x - lv.x;
+        uint4 *dst = mine + (l % kCRingLevels) * rpt * T;
+        uint32_t s = g;
+        for (uint32_t k = 0; k < rpt && s < n; ++k, s += G) cp_async16(dst + k * T, rec + lv.x + s);
+    };
+#pragma unroll
+    for (int k = 0; k < kCRingDepth; ++k) {
+        if (uint32_t(k) < L) stage(k);
+        cp_async_commit();
+    }
+    for (uint32_t l = 0; l < L; ++l) {
+        if (l + kCRingDepth < L) stage(l + kCRingDepth);
+        cp_async_commit();
+        cp_async_wait<kCRingDepth>();  // this thread's copies of level l have landed
+        const uint4 lv = desc(l);
+        const uint32_t n = desc(l + 1).x - lv.x;
+        const uint4 *src = mine + (l % kCRingLevels) * rpt * T;
+        uint32_t k = 0;
+        for (uint32_t s = g; s < n; s += G, ++k) {
+            const uint4 r = k < rpt ? src[k * T] : __ldg(rec + lv.x + s);
+            if (r.x != 0xffffffffu) project(cx, r, slot_type(lv, s), inv_dt_sq);
+        }
+        cluster_barrier();
+    }
+    cp_async_wait<0>();
+}
+
+// Dynamic shared memory of one CTA: positions [1 << shift] | level descriptors [desc_cap] |
+// record ring [kCRingLevels][rpt][T].
+template <int T>
+__global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t shift, uint32_t desc_cap, uint32_t rpt) {
+    extern __shared__ float4 smem[];
+    __shared__ CShared sh;
+    const uint32_t tid = threadIdx.x;
+    const uint32_t rank = cluster_rank(), C = cluster_size();
+    const uint32_t item = blockIdx.x / C;  // one cluster per body
+    if (item >= p.num_work) return;       // uniform over the cluster
+    const uint32_t b = p.work[item];
+    const BodyDesc d = p.bodies[b];
+    BodyState *st = p.states + b;
+    const uint32_t nv = d.num_vertices;
+    const uint32_t first = min(nv, rank << shift), last = min(nv, (rank + 1) << shift);
+    float4 *sx = smem;
+    uint4 *sdesc = reinterpret_cast<uint4 *>(smem + (size_t(1) << shift));
+    uint4 *ring = sdesc + desc_cap;
+    const ClusterX cx{smem_u32(sx), shift};
+    float4 *__restrict__ gx = p.x + d.vtx_offset;
+    float4 *__restrict__ gv = p.v + d.vtx_offset;
+    float4 *__restrict__ gprev = p.prev + d.vtx_offset;
+    float4 *__restrict__ gplane = p.plane + d.vtx_offset;
+    int32_t *__restrict__ gshape = p.shape + d.vtx_offset;
+
+    // InitializeUpdateContext (identity body rotation)
+    const f3 g = d.gravity_factor * ld3(p.gravity);
+    const uint32_t n_it = d.num_iterations;
+    const float dt = p.dt;
+    const float dt_sub = dt / float(n_it);
+    float disp_scale = 0.5f * float(n_it);
+    disp_scale = disp_scale * float(n_it + 1);
+    disp_scale = disp_scale * (dt_sub * dt_sub);
+    const f3 disp_g = disp_scale * g;
+    const f3 body_pos = ld3(st->position);
+    const f3 force = ld3(p.forces + 3 * size_t(b)) + ld3(p.step_forces + 3 * size_t(b));
+
+    // DetermineCollidingShapes (every CTA evaluates it; the result is the same), level descriptors and
+    // the positions this CTA owns.
+    if (tid == 0) sh.ncols = colliding_shapes(p, d, st, body_pos, sh.cols);
+    const uint32_t nd = min(d.num_levels + 2, desc_cap);
+    for (uint32_t l = tid; l < nd; l += T) sdesc[l] = __ldg(d.levels + l);
+    for (uint32_t i = first + tid; i < last; i += T) sx[i - first] = gx[i];
+    __syncthreads();
+
+    // DetermineCollisionPlanes (owned vertices)
+    const int ncols = sh.ncols;
+    for (uint32_t i = first + tid; i < last; i += T) {
+        const float4 pi = sx[i - first];
+        int shape = -1;
+        float4 plane = make_float4(0, 0, 0, 0);
+        if (pi.w > 0.0f && ncols > 0) shape = collision_plane(xyz(pi), sh.cols, ncols, plane);
+        gshape[i] = shape;
+        if (shape >= 0) gplane[i] = plane;
+    }
+
+    const float inv_dt_sq = 1.0f / (dt_sub * dt_sub);
+    float damp = 1.0f - d.linear_damping * dt_sub;
+    damp = damp < 0.0f ? 0.0f : damp;
+    const f3 sub_g = g * dt_sub;
+    const float nvf = float(nv > 0 ? nv : 1);
+    const f3 sub_imp = (force * dt_sub) / nvf;
+    const float restitution_threshold = -2.0f * len(g) * dt_sub;
+    const uint32_t gthread = rank * T + tid, G = C * T;
+
+    for (uint32_t it = 0; it < n_it; ++it) {
+        // IntegratePositions (owned vertices)
+        for (uint32_t i = first + tid; i < last; i += T) {
+            const float4 pi = sx[i - first];
+            const float4 vel = gv[i];
+            f3 v = xyz(vel);
+            if (pi.w > 0.0f) {
+                v = v + (sub_g + sub_imp * pi.w);
+                v = v * damp;
+            }
+            gprev[i] = pi;
+            gv[i] = with_w(v, vel.w);
+            sx[i - first] = with_w(xyz(pi) + v * dt_sub, pi.w);
+        }
+        cluster_barrier();  // every position integrated before any constraint reads it
+        cluster_levels<T>(cx, d, sdesc, desc_cap, ring, rpt, gthread, G, inv_dt_sq);
+        // ApplyCollisionConstraintsAndUpdateVelocities (owned vertices; the last level's barrier made
+        // every remote write visible). The next integration touches owned vertices only.
+        for (uint32_t i = first + tid; i < last; i += T) {
+            const float4 pi = sx[i - first];
+            if (!(pi.w > 0.0f)) continue;
+            f3 x = xyz(pi);
+            const float4 vel = gv[i];
+            const float4 prev = gprev[i];
+            const f3 prev_v = xyz(vel);
+            f3 v = (x - xyz(prev)) / dt_sub;
+            const int shape = ncols > 0 ? gshape[i] : -1;
+            if (shape >= 0 && collide_vertex(x, v, prev_v, gplane[i], sh.cols[shape], d.vertex_radius, dt_sub, restitution_threshold))
+                sx[i - first] = with_w(x, pi.w);
+            gv[i] = with_w(v, vel.w);
+        }
+    }
+
+    // UpdateSoftBodyState: per-CTA partials over owned vertices, combined by rank 0.
+    __syncthreads();
+    const float max_sq = d.max_linear_velocity * d.max_linear_velocity;
+    float mm[4] = {FLT_MAX, FLT_MAX, FLT_MAX, 0};
+    int mi[4] = {-1, -1, -1, -1};
+    float xx[4] = {-FLT_MAX, -FLT_MAX, -FLT_MAX, 0};
+    int xi[4] = {-1, -1, -1, -1};
+    float pm[4] = {FLT_MAX, FLT_MAX, FLT_MAX, 0};
+    int pmi[4] = {-1, -1, -1, -1};
+    float px[4] = {-FLT_MAX, -FLT_MAX, -FLT_MAX, 0};
+    int pxi[4] = {-1, -1, -1, -1};
+    f3 lin = mk(0, 0, 0), ang = mk(0, 0, 0);
+    bool finite = true;
+    for (uint32_t i = first + tid; i < last; i += T) {
+        const float4 pi = sx[i - first];
+        f3 v = xyz(gv[i]), x = xyz(pi);
+        const float vsq = len_sq(v);
+        if (vsq > max_sq) v = v * jsqrt(jdiv(max_sq, vsq));
+        gv[i] = with_w(v, 0.0f);
+        lin = lin + v;
+        ang = ang + cross(x, v);
+        const f3 pred = (x + v * dt) + disp_g;
+        pick_min(mm[0], mi[0], x.x, int(i));
+        pick_min(mm[1], mi[1], x.y, int(i));
+        pick_min(mm[2], mi[2], x.z, int(i));
+        pick_max(xx[0], xi[0], x.x, int(i));
+        pick_max(xx[1], xi[1], x.y, int(i));
+        pick_max(xx[2], xi[2], x.z, int(i));
+        pick_min(pm[0], pmi[0], pred.x, int(i));
+        pick_min(pm[1], pmi[1], pred.y, int(i));
+        pick_min(pm[2], pmi[2], pred.z, int(i));
+        pick_max(px[0], pxi[0], pred.x, int(i));
+        pick_max(px[1], pxi[1], pred.y, int(i));
+        pick_max(px[2], pxi[2], pred.z, int(i));
+        finite = finite && isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
+    }
+    if (!finite) atomicOr(p.error, kErrNonFinite);
+    {
+        const bool mins[4] = {false, false, false, false};
+        const bool maxs[4] = {true, true, true, true};
+        reduce_minmax4<T>(sh, mm, mi, mins);
+        reduce_minmax4<T>(sh, xx, xi, maxs);
+        reduce_minmax4<T>(sh, pm, pmi, mins);
+        reduce_minmax4<T>(sh, px, pxi, maxs);
+    }
+    float sums[6];
+    sums[0] = reduce_sum<T>(sh, lin.x, 0);
+    sums[1] = reduce_sum<T>(sh, lin.y, 1);
+    sums[2] = reduce_sum<T>(sh, lin.z, 2);
+    sums[3] = reduce_sum<T>(sh, ang.x, 3);
+    sums[4] = reduce_sum<T>(sh, ang.y, 0);
+    sums[5] = reduce_sum<T>(sh, ang.z, 1);
+    if (tid == 0) {
+        for (int k = 0; k < 3; ++k) {
+            sh.part.val[k] = mm[k], sh.part.idx[k] = mi[k];
+            sh.part.val[3 + k] = xx[k], sh.part.idx[3 + k] = xi[k];
+            sh.part.val[6 + k] = pm[k], sh.part.idx[6 + k] = pmi[k];
+            sh.part.val[9 + k] = px[k], sh.part.idx[9 + k] = pxi[k];
+        }
+        for (int k = 0; k < 6; ++k) sh.part.sum[k] = sums[k];
+    }
+    cluster_barrier();
+    if (rank == 0 && tid == 0) {
+        Partials acc = sh.part;
+        const uint32_t local = smem_u32(&sh.part);
+        for (uint32_t r = 1; r < C; ++r) {
+            const uint32_t base = map_rank(local, r);
+            for (int k = 0; k < 12; ++k) {
+                const float ov = ld_cluster_f32(base + uint32_t(offsetof(Partials, val)) + 4u * k);
+                const int oi = ld_cluster_s32(base + uint32_t(offsetof(Partials, idx)) + 4u * k);
+                if ((k / 3) & 1)
+                    pick_max(acc.val[k], acc.idx[k], ov, oi);
+                else
+                    pick_min(acc.val[k], acc.idx[k], ov, oi);
+            }
+            for (int k = 0; k < 6; ++k) acc.sum[k] = acc.sum[k] + ld_cluster_f32(base + uint32_t(offsetof(Partials, sum)) + 4u * k);
+        }
+        const f3 delta = finish_body_state(st, d, body_pos, mk(acc.val[0], acc.val[1], acc.val[2]), mk(acc.val[3], acc.val[4], acc.val[5]),
+                                           mk(acc.val[6], acc.val[7], acc.val[8]), mk(acc.val[9], acc.val[10], acc.val[11]), acc.sum,
+                                           nvf);
+        st3(sh.delta, delta);
+    }
+    cluster_barrier();
+    f3 delta;
+    {
+        const uint32_t base = map_rank(smem_u32(sh.delta), 0);
+        delta = mk(ld_cluster_f32(base), ld_cluster_f32(base + 4), ld_cluster_f32(base + 8));
+    }
+    const bool recentre = (d.flags & kFlagUpdatePosition) != 0;
+    for (uint32_t i = first + tid; i < last; i += T) {
+        const float4 pi = sx[i - first];
+        gx[i] = recentre ? with_w(xyz(pi) - delta, pi.w) : pi;
+    }
+    cluster_barrier();  // rank 0's shared memory stays alive until every CTA has read the offset
+}
+
+}  // namespace
+
+// Bytes of dynamic shared memory of one cluster CTA.
+size_t cluster_smem_bytes(uint32_t shift, uint32_t desc_cap, uint32_t rpt, int threads) {
+    return (size_t(1) << shift) * sizeof(float4) + size_t(desc_cap) * sizeof(uint4) +
+           size_t(kCRingLevels) * rpt * size_t(threads) * sizeof(uint4);
+}
+
+#define JSB_FOR_EACH_CLUSTER_SHAPE(X) X(128) X(256) X(512)
+
+static cudaLaunchConfig_t cluster_config(int cluster, int threads, size_t smem, unsigned grid, cudaStream_t stream,
+                                         cudaLaunchAttribute *attr) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid, 1, 1);
+    cfg.blockDim = dim3(unsigned(threads), 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    attr->id = cudaLaunchAttributeClusterDimension;
+    attr->val.clusterDim.x = unsigned(cluster);
+    attr->val.clusterDim.y = 1;
+    attr->val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+
+// Launches one step of `p.num_work` bodies, one cluster of `cluster` CTAs each.
+cudaError_t launch_cluster_step(const StepParams &p, int cluster, int threads, uint32_t shift, uint32_t desc_cap, uint32_t rpt,
+                                cudaStream_t stream) {
+    cudaLaunchAttribute attr;
+    const cudaLaunchConfig_t cfg = cluster_config(cluster, threads, cluster_smem_bytes(shift, desc_cap, rpt, threads),
+                                                  unsigned(cluster) * p.num_work, stream, &attr);
+#define JSB_CLAUNCH(TT) \
+    if (threads == TT) return cudaLaunchKernelEx(&cfg, cluster_step_kernel<TT>, p, shift, desc_cap, rpt);
+    JSB_FOR_EACH_CLUSTER_SHAPE(JSB_CLAUNCH)
+#undef JSB_CLAUNCH
+    return cudaErrorInvalidValue;
+}
+
+// Allows the cluster kernels up to `max_dynamic_smem` bytes of dynamic shared memory and clusters of
+// up to 16 CTAs (done once per device, outside any stream capture).
+cudaError_t init_cluster_kernels(int max_dynamic_smem) {
+    cudaError_t e = cudaSuccess;
+#define JSB_CATTR(TT)                                                                                                        \
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(cluster_step_kernel<TT>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                                   max_dynamic_smem);                                                       \
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(cluster_step_kernel<TT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    JSB_FOR_EACH_CLUSTER_SHAPE(JSB_CATTR)
+#undef JSB_CATTR
+    return e;
+}
+
+// Clusters of this shape that fit on the device at once (0: the shape cannot be launched).
+int cluster_occupancy(int cluster, int threads, size_t smem) {
+    cudaLaunchAttribute attr;
+    const cudaLaunchConfig_t cfg = cluster_config(cluster, threads, smem, unsigned(cluster), nullptr, &attr);
+    int n = 0;
+    cudaError_t e = cudaErrorInvalidValue;
+#define JSB_COCC(TT) \
+    if (threads == TT) e = cudaOccupancyMaxActiveClusters(&n, cluster_step_kernel<TT>, &cfg);
+    JSB_FOR_EACH_CLUSTER_SHAPE(JSB_COCC)
+#undef JSB_COCC
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+}  // namespace jsb

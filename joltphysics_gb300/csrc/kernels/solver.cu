@@ -25,18 +25,11 @@
 
 #include "common.cuh"
 #include "device_types.h"
+#include "projection.cuh"
 
 namespace jsb {
 namespace {
 
-struct SCol {  // one colliding shape, relative to the soft body
-    int32_t type;
-    float t[3];
-    float h[3];
-    float r;
-    float friction;
-    float restitution;
-};
 
 struct Shared {
     SCol cols[kMaxCollidingShapes];
@@ -49,118 +42,6 @@ struct Shared {
     int redi[32][4];
 };
 
-// ---------------------------------------------------------------------------------------------
-// Constraint projections (exact reference arithmetic)
-// ---------------------------------------------------------------------------------------------
-__device__ __forceinline__ void project_bend(float4 *sx, uint4 r, float inv_dt_sq) {  // :367-456
-    uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16, i2 = r.y & 0xffff, i3 = r.y >> 16;
-    float compliance = __uint_as_float(r.z), initial_angle = __uint_as_float(r.w);
-    float4 p0 = sx[i0], p1 = sx[i1], p2 = sx[i2], p3 = sx[i3];
-    f3 x0 = xyz(p0), x1 = xyz(p1), x2 = xyz(p2), x3 = xyz(p3);
-    f3 e = x1 - x0;
-    float e_len = len(e);
-    if (e_len < 1.0e-6f) return;
-    f3 x1x2 = x2 - x1, x1x3 = x3 - x1;
-    f3 n1 = cross(x2 - x0, x1x2);
-    f3 n2 = cross(x1x3, x3 - x0);
-    float n1_len_sq = len_sq(n1), n2_len_sq = len_sq(n2);
-    float n1n2 = n1_len_sq * n2_len_sq;
-    if (n1n2 < 1.0e-24f) return;
-    float sign = dot(cross(n2, n1), e) < 0.0f ? -1.0f : 1.0f;
-    float d = jdiv(dot(n1, n2), jsqrt(n1n2));
-    float c = sign * acos_approximate(d) - initial_angle;
-    if (c > kPi)
-        c -= 2.0f * kPi;
-    else if (c < -kPi)
-        c += 2.0f * kPi;
-    n1 = n1 / n1_len_sq;
-    n2 = n2 / n2_len_sq;
-    f3 d0c = (dot(x1x2, e) * n1 + dot(x1x3, e) * n2) / e_len;
-    f3 d2c = e_len * n1;
-    f3 d3c = e_len * n2;
-    f3 d1c = (neg(d0c) - d2c) - d3c;
-    float w0 = p0.w, w1 = p1.w, w2 = p2.w, w3 = p3.w;
-    float denom = w0 * len_sq(d0c) + w1 * len_sq(d1c) + w2 * len_sq(d2c) + w3 * len_sq(d3c) + compliance * inv_dt_sq;
-    if (denom < 1.0e-12f) return;
-    float ml = jdiv(c, denom);
-    sx[i0] = with_w(x0 - (ml * w0) * d0c, w0);
-    sx[i1] = with_w(x1 - (ml * w1) * d1c, w1);
-    sx[i2] = with_w(x2 - (ml * w2) * d2c, w2);
-    sx[i3] = with_w(x3 - (ml * w3) * d3c, w3);
-}
-
-__device__ __forceinline__ void project_volume(float4 *sx, uint4 r, float inv_dt_sq) {  // :458-507
-    uint32_t i1 = r.x & 0xffff, i2 = r.x >> 16, i3 = r.y & 0xffff, i4 = r.y >> 16;
-    float six_rest = __uint_as_float(r.z), compliance = __uint_as_float(r.w);
-    float4 p1 = sx[i1], p2 = sx[i2], p3 = sx[i3], p4 = sx[i4];
-    f3 x1 = xyz(p1), x2 = xyz(p2), x3 = xyz(p3), x4 = xyz(p4);
-    f3 x1x2 = x2 - x1, x1x3 = x3 - x1, x1x4 = x4 - x1;
-    float c = fabsf(dot(cross(x1x2, x1x3), x1x4)) - six_rest;
-    f3 d1c = cross(x4 - x2, x3 - x2);
-    f3 d2c = cross(x1x3, x1x4);
-    f3 d3c = cross(x1x4, x1x2);
-    f3 d4c = cross(x1x2, x1x3);
-    float w1 = p1.w, w2 = p2.w, w3 = p3.w, w4 = p4.w;
-    float denom = w1 * len_sq(d1c) + w2 * len_sq(d2c) + w3 * len_sq(d3c) + w4 * len_sq(d4c) + compliance * inv_dt_sq;
-    if (denom < 1.0e-12f) return;
-    float ml = jdiv(c, denom);
-    sx[i1] = with_w(x1 - (ml * w1) * d1c, w1);
-    sx[i2] = with_w(x2 - (ml * w2) * d2c, w2);
-    sx[i3] = with_w(x3 - (ml * w3) * d3c, w3);
-    sx[i4] = with_w(x4 - (ml * w4) * d4c, w4);
-}
-
-__device__ __forceinline__ void project_edge(float4 *sx, uint4 r, float inv_dt_sq) {  // :573-601
-    uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16;
-    float rest = __uint_as_float(r.z), compliance = __uint_as_float(r.w);
-    float4 p0 = sx[i0], p1 = sx[i1];
-    f3 x0 = xyz(p0), x1 = xyz(p1);
-    f3 delta = x1 - x0;
-    float length = len(delta);
-    float denom = length * (p0.w + p1.w + compliance * inv_dt_sq);
-    if (denom < 1.0e-12f) return;
-    f3 corr = (delta * (length - rest)) / denom;
-    sx[i0] = with_w(x0 + p0.w * corr, p0.w);
-    sx[i1] = with_w(x1 - p1.w * corr, p1.w);
-}
-
-__device__ __forceinline__ void project_lra(float4 *sx, uint4 r) {  // :679-698
-    uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16;
-    float md = __uint_as_float(r.z);
-    f3 x0 = xyz(sx[i0]);
-    float4 p1 = sx[i1];
-    f3 delta = xyz(p1) - x0;
-    float dls = len_sq(delta);
-    if (dls > md * md) sx[i1] = with_w(x0 + (delta * md) / jsqrt(dls), p1.w);
-}
-
-__device__ __forceinline__ void project(float4 *sx, uint4 r, int type, float inv_dt_sq) {
-    if (type == 0)
-        project_bend(sx, r, inv_dt_sq);
-    else if (type == 1)
-        project_volume(sx, r, inv_dt_sq);
-    else if (type == 2)
-        project_edge(sx, r, inv_dt_sq);
-    else
-        project_lra(sx, r);
-}
-
-// Type of slot `s` of a level with descriptor {first slot, bend end, volume end, edge end}: the
-// type groups are padded to multiples of 32 slots, so the type is uniform across a warp.
-__device__ __forceinline__ int slot_type(uint4 lv, uint32_t s) {
-    return s < lv.y ? 0 : (s < lv.z ? 1 : (s < lv.w ? 2 : 3));
-}
-
-// ---- asynchronous copies (cp.async, 16 bytes per thread) -----------------------------------------
-__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src) {
-    const uint32_t dst = uint32_t(__cvta_generic_to_shared(smem_dst));
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(gmem_src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
 
 // Record ring: kRingDepth levels of up to `slots` records each are streamed into shared memory
 // ahead of the level being projected; the ring holds kRingDepth + 1 levels.
@@ -246,127 +127,6 @@ __device__ __forceinline__ void apply_levels(float4 *sx, const BodyDesc &d, floa
     cp_async_wait<0>();
 }
 
-// ---------------------------------------------------------------------------------------------
-// Collision shapes
-// ---------------------------------------------------------------------------------------------
-// Plane::sFromPointAndNormal(point, normal).GetTransformed(translation t), identity rotation.
-__device__ __forceinline__ float4 plane_transformed(f3 normal, f3 point, f3 t) {
-    float c = -dot(normal, point);
-    f3 n2;
-    n2.x = (1.0f * normal.x + 0.0f * normal.y) + 0.0f * normal.z;
-    n2.y = (0.0f * normal.x + 1.0f * normal.y) + 0.0f * normal.z;
-    n2.z = (0.0f * normal.x + 0.0f * normal.y) + 1.0f * normal.z;
-    return make_float4(n2.x, n2.y, n2.z, c - dot(t, n2));
-}
-
-// BoxShape::CollideSoftBodyVertices (BoxShape.cpp:234-283) for one vertex.
-__device__ __forceinline__ void collide_box(f3 p, const SCol &s, int idx, float &largest, float4 &plane, int &shape) {
-    f3 t = ld3(s.t), h = ld3(s.h);
-    f3 local = p + neg(t);
-    f3 clamped = vmax(vmin(local, h), neg(h));
-    if (clamped.x == local.x && clamped.y == local.y && clamped.z == local.z) {
-        f3 delta = h - mk(fabsf(local.x), fabsf(local.y), fabsf(local.z));
-        int index = delta.x < delta.y ? (delta.z < delta.x ? 2 : 0) : (delta.z < delta.y ? 2 : 1);
-        float pen = index == 0 ? delta.x : (index == 1 ? delta.y : delta.z);
-        if (largest >= pen) return;
-        largest = pen;
-        f3 sgn = mk(signbit(local.x) ? -1.0f : 1.0f, signbit(local.y) ? -1.0f : 1.0f, signbit(local.z) ? -1.0f : 1.0f);
-        f3 axis = mk(index == 0 ? 1.0f : 0.0f, index == 1 ? 1.0f : 0.0f, index == 2 ? 1.0f : 0.0f);
-        f3 normal = mk(sgn.x * axis.x, sgn.y * axis.y, sgn.z * axis.z);
-        f3 point = mk(normal.x * h.x, normal.y * h.y, normal.z * h.z);
-        plane = plane_transformed(normal, point, t);
-        shape = idx;
-    } else {
-        f3 normal = local - clamped;
-        float nl = len(normal);
-        float pen = -nl;
-        if (largest >= pen) return;
-        largest = pen;
-        normal = normal / nl;
-        plane = plane_transformed(normal, clamped, t);
-        shape = idx;
-    }
-}
-
-// SphereShape::CollideSoftBodyVertices (SphereShape.cpp:279-300) for one vertex.
-__device__ __forceinline__ void collide_sphere(f3 p, const SCol &s, int idx, float &largest, float4 &plane, int &shape) {
-    f3 center = ld3(s.t);
-    f3 delta = p - center;
-    float distance = len(delta);
-    float pen = s.r - distance;
-    if (largest >= pen) return;
-    largest = pen;
-    f3 normal = distance > 0.0f ? delta / distance : mk(0.0f, 1.0f, 0.0f);
-    f3 point = center + s.r * normal;
-    plane = make_float4(normal.x, normal.y, normal.z, -dot(normal, point));
-    shape = idx;
-}
-
-// ---------------------------------------------------------------------------------------------
-// Reductions for UpdateSoftBodyState
-// ---------------------------------------------------------------------------------------------
-// Sequential AABox::Encapsulate keeps, among equal extreme values, the last vertex in index order
-// (mMin = mMin < p ? mMin : p). Reducing (value, index) pairs with "strictly better, else larger
-// index" reproduces that choice (it matters only for the sign of zero).
-__device__ __forceinline__ void pick_min(float &v, int &i, float ov, int oi) {
-    if (ov < v || (!(v < ov) && oi > i)) {
-        v = ov;
-        i = oi;
-    }
-}
-__device__ __forceinline__ void pick_max(float &v, int &i, float ov, int oi) {
-    if (ov > v || (!(v > ov) && oi > i)) {
-        v = ov;
-        i = oi;
-    }
-}
-
-template <int T>
-__device__ __forceinline__ void reduce_minmax4(Shared &sh, float v[4], int idx[4], const bool is_max[4]) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        for (int off = 16; off > 0; off >>= 1) {
-            float ov = __shfl_down_sync(0xffffffffu, v[k], off);
-            int oi = __shfl_down_sync(0xffffffffu, idx[k], off);
-            if (is_max[k])
-                pick_max(v[k], idx[k], ov, oi);
-            else
-                pick_min(v[k], idx[k], ov, oi);
-        }
-    }
-    if (T > 32) {
-        if (lane == 0)
-            for (int k = 0; k < 4; ++k) {
-                sh.red[warp][k] = v[k];
-                sh.redi[warp][k] = idx[k];
-            }
-        __syncthreads();
-        if (threadIdx.x == 0)
-            for (int w = 1; w < T / 32; ++w)
-                for (int k = 0; k < 4; ++k) {
-                    if (is_max[k])
-                        pick_max(v[k], idx[k], sh.red[w][k], sh.redi[w][k]);
-                    else
-                        pick_min(v[k], idx[k], sh.red[w][k], sh.redi[w][k]);
-                }
-        __syncthreads();
-    }
-}
-
-template <int T>
-__device__ __forceinline__ float reduce_sum(Shared &sh, float v, int slot) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    if (T > 32) {
-        if (lane == 0) sh.red[warp][slot] = v;
-        __syncthreads();
-        if (threadIdx.x == 0)
-            for (int w = 1; w < T / 32; ++w) v += sh.red[w][slot];
-        __syncthreads();
-    }
-    return v;  // valid in thread 0
-}
 
 // ---------------------------------------------------------------------------------------------
 // One body, one step
@@ -411,32 +171,7 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
 
     // DetermineCollidingShapes: world AABB of (bounds U predicted bounds) grown by the vertex radius
     if (tid == 0) {
-        f3 lmin = vmin(ld3(st->bmin), ld3(st->pmin)), lmax = vmax(ld3(st->bmax), ld3(st->pmax));
-        f3 r3 = mk(d.vertex_radius, d.vertex_radius, d.vertex_radius);
-        lmin = lmin - r3;
-        lmax = lmax + r3;
-        f3 wmin = body_pos + lmin, wmax = body_pos + lmax;
-        int n = 0;
-        for (uint32_t ci = 0; ci < p.num_colliders; ++ci) {
-            const ColliderDev c = p.colliders[ci];
-            f3 cp = ld3(c.position);
-            f3 ext = c.type == 0 ? ld3(c.half_extent) : mk(c.radius, c.radius, c.radius);
-            f3 cmin = cp + neg(ext), cmax = cp + ext;
-            bool overlap = !(wmin.x > cmax.x || wmin.y > cmax.y || wmin.z > cmax.z || wmax.x < cmin.x || wmax.y < cmin.y ||
-                             wmax.z < cmin.z);
-            if (!overlap) continue;
-            if (n == int(kMaxCollidingShapes)) {
-                atomicOr(p.error, kErrShapeOverflow);
-                break;
-            }
-            SCol &s = sh.cols[n++];
-            s.type = c.type;
-            st3(s.t, cp - body_pos);
-            st3(s.h, ld3(c.half_extent));
-            s.r = c.radius;
-            s.friction = sqrtf(d.friction * c.friction);
-            s.restitution = d.restitution > c.restitution ? d.restitution : c.restitution;
-        }
+        const int n = colliding_shapes(p, d, st, body_pos, sh.cols);
         sh.ncols = n;
         if (kTape)
             for (int k = 0; k < n; ++k)
@@ -455,15 +190,7 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
         float4 pi = sx[i];
         int shape = -1;
         float4 plane = make_float4(0, 0, 0, 0);
-        if (pi.w > 0.0f && ncols > 0) {
-            float largest = -FLT_MAX;
-            for (int s = 0; s < ncols; ++s) {
-                if (sh.cols[s].type == 0)
-                    collide_box(xyz(pi), sh.cols[s], s, largest, plane, shape);
-                else
-                    collide_sphere(xyz(pi), sh.cols[s], s, largest, plane, shape);
-            }
-        }
+        if (pi.w > 0.0f && ncols > 0) shape = collision_plane(xyz(pi), sh.cols, ncols, plane);
         if (kSmemState)
             sv[i].w = __int_as_float(shape);
         else
@@ -564,27 +291,8 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
             f3 v = (x - xyz(prev)) / dt_sub;
             int shape = -1;
             if (ncols > 0) shape = kSmemState ? __float_as_int(vel.w) : gshape[i];
-            if (shape >= 0) {
-                float4 pl = gplane[i];
-                f3 n = xyz(pl);
-                float projected = -(dot(x, n) + pl.w) + d.vertex_radius;
-                if (projected > 0.0f) {
-                    const SCol &cs = sh.cols[shape];
-                    x = x + n * projected;
-                    sx[i] = with_w(x, pi.w);
-                    f3 v_normal = n * dot(n, v);
-                    f3 v_tan = v - v_normal;
-                    float vtl = len(v_tan);
-                    if (vtl > 0.0f) {
-                        float fr = jdiv(cs.friction * projected, vtl * dt_sub);
-                        fr = fr > 1.0f ? 1.0f : fr;
-                        v = v - v_tan * fr;
-                    }
-                    v = v - v_normal;
-                    float pvn = dot(prev_v, n);
-                    if (pvn < restitution_threshold) v = v - (cs.restitution * pvn) * n;
-                }
-            }
+            if (shape >= 0 && collide_vertex(x, v, prev_v, gplane[i], sh.cols[shape], d.vertex_radius, dt_sub, restitution_threshold))
+                sx[i] = with_w(x, pi.w);
             if (kSmemState)
                 sv[i] = with_w(v, vel.w);
             else
@@ -646,30 +354,8 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     sums[4] = reduce_sum<T>(sh, ang.y, 0);
     sums[5] = reduce_sum<T>(sh, ang.z, 1);
     if (tid == 0) {
-        f3 bmin = mk(mm[0], mm[1], mm[2]), bmax = mk(xx[0], xx[1], xx[2]);
-        f3 pmin = mk(pm[0], pm[1], pm[2]), pmax = mk(px[0], px[1], px[2]);
-        st3(st->lin_vel, mk(sums[0], sums[1], sums[2]) / nvf);
-        st3(st->ang_vel, mk(sums[3], sums[4], sums[5]) / nvf);
-        f3 delta = mk(0, 0, 0);
-        f3 pos = body_pos;
-        if (d.flags & kFlagUpdatePosition) {
-            delta = 0.5f * (bmin + bmax);
-            f3 nd = neg(delta);
-            bmin = bmin + nd;
-            bmax = bmax + nd;
-            pmin = pmin + nd;
-            pmax = pmax + nd;
-            f3 wd;
-            wd.x = (1.0f * delta.x + 0.0f * delta.y) + 0.0f * delta.z;
-            wd.y = (0.0f * delta.x + 1.0f * delta.y) + 0.0f * delta.z;
-            wd.z = (0.0f * delta.x + 0.0f * delta.y) + 1.0f * delta.z;
-            pos = pos + wd;
-        }
-        st3(st->bmin, bmin);
-        st3(st->bmax, bmax);
-        st3(st->pmin, pmin);
-        st3(st->pmax, pmax);
-        st3(st->position, pos);
+        const f3 delta = finish_body_state(st, d, body_pos, mk(mm[0], mm[1], mm[2]), mk(xx[0], xx[1], xx[2]),
+                                           mk(pm[0], pm[1], pm[2]), mk(px[0], px[1], px[2]), sums, nvf);
         st3(sh.delta, delta);
     }
     __syncthreads();
