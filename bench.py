@@ -198,6 +198,103 @@ def cpu_baseline(scene, budget_s: float = 12.0) -> dict:
             "sample": f"{n} full steps of all {len(scene.bodies)} bodies (after 1 warm-up step)"}
 
 
+def bench_adjoint(jsb, stream_ptr, steps: int = 90, every: int = 15) -> dict:
+    """Forward+adjoint against forward only on the differentiable batch: 192 cloths (side U{16..48}) and 64
+    pressurised tet cubes (U{4..8} cells), per-body step forces N(0, 2 N), v0 N(0, 0.5 m/s), floor + sphere,
+    90 steps of 5 iterations. Loss = sum over bodies of |centre of mass - target|^2 after the last step;
+    gradients w.r.t. initial positions / velocities, compliance and force, checkpoints every 15 steps.
+    Both sides are timed on the host clock around synchronised work (whole job, one run each after a
+    warm-up run)."""
+    scene_bytes = jsb.build_scene("diff_batch")
+    ctx = jsb.Context(0)
+    ctx.load_scene(scene_bytes)
+    ctx.set_scene_step_forces()
+    nb = len(ctx.bodies)
+    rng = np.random.default_rng(17)
+    targets = rng.normal(0.0, 1.0, (nb, 3)) + np.array([0.0, 0.5, 0.0])
+    init = ctx.save_all()
+    counts = np.asarray(ctx.num_vertices, np.int64)
+    offsets = np.concatenate([[0], np.cumsum(counts)])
+    loc = np.zeros((int(offsets[-1]), 3), np.float32)
+    vel = np.zeros_like(loc)
+
+    def forward_only():
+        ctx.restore_all(init)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        ctx.step_graph(steps, 1, stream=stream_ptr)
+        ctx.synchronize()
+        return time.perf_counter() - t0
+
+    def forward_adjoint():
+        ctx.restore_all(init)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        ctx.adjoint_begin(steps, every)
+        ctx.adjoint_forward()
+        ctx.download_all(loc, vel)
+        ctx.synchronize()
+        pos = ctx.body_positions().astype(np.float64)
+        com = np.add.reduceat(loc.astype(np.float64), offsets[:-1], axis=0) / counts[:, None] + pos
+        seed = np.repeat(2.0 * (com - targets) / counts[:, None], counts, axis=0)
+        ctx.adjoint_seed_all(steps, seed.astype(np.float32))
+        ctx.adjoint_backward()
+        grads = ctx.adjoint_gradients_all()
+        ctx.adjoint_end()
+        ctx.synchronize()
+        return time.perf_counter() - t0, grads
+
+    forward_only()
+    t_fwd = forward_only()
+    forward_adjoint()
+    t_adj, grads = forward_adjoint()
+    finite = bool(np.isfinite(grads["force"]).all() and np.isfinite(grads["v0"]).all())
+    ctx.close()
+    return {"workload": "diff_batch", "bodies": nb, "steps": steps, "checkpoint_every": every,
+            "forward_s": t_fwd, "forward_adjoint_s": t_adj, "ratio": t_adj / t_fwd, "target_ratio": 4.0,
+            "gradients_finite": bool(finite), "timing": "host clock around synchronised work, forward as a CUDA graph"}
+
+
+def bench_large_body(jsb, torch, stream, steps: int, with_cpu: bool) -> dict:
+    """The 256 x 256 cloth (65,536 vertices, LRA tethers, sphere on a floor, 8 iterations) on the
+    thread-block-cluster path: device-timed steps (CUDA graph of one step, L2 flushed before each)."""
+    scene_bytes = jsb.build_scene("large_cloth")
+    ctx = jsb.Context(0)
+    ctx.load_scene(scene_bytes)
+    sptr = stream.cuda_stream
+    vi_step = ctx.total_vertices() * 8
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            ctx.step_graph(1, 1, stream=sptr)
+    torch.cuda.synchronize()
+    cfg = ctx.cluster_config()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for i in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xFF)
+            ev[i][0].record(stream)
+            ctx.step_graph(1, 1, stream=sptr)
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    out = {"workload": "large_cloth 256x256", "vertices": ctx.total_vertices(), "iterations": 8, "steps": steps,
+           "ms_per_step": ms, "value": vi_step / (ms / 1000.0), "unit": UNIT, "cluster": cfg}
+    ctx.close()
+    if with_cpu:
+        from jsb_testlib import Oracle, parse_scene
+
+        scene, _ = parse_scene(scene_bytes)
+        o = Oracle(scene)
+        o.step(1)
+        t0 = time.perf_counter()
+        o.step(2)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": vi_step * 2 / dt, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": "2 steps after 1 warm-up step (one body: the oracle runs it on one thread)"}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -206,6 +303,8 @@ def main():
     ap.add_argument("--impl", default="jsb", choices=["jsb", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=2)
+    ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and large-body measurements")
+    ap.add_argument("--large-steps", type=int, default=10)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -351,6 +450,9 @@ def main():
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(scene)
+    if not args.no_extras:
+        line["adjoint"] = bench_adjoint(jsb, sptr)
+        line["large_body"] = bench_large_body(jsb, torch, stream, args.large_steps, not args.no_cpu_baseline)
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

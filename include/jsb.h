@@ -137,6 +137,9 @@ jsb_status jsb_body_save_state(jsb_context *ctx, uint32_t body_id, void *state, 
 jsb_status jsb_state_upload_all(jsb_context *ctx, const float *local_positions, const float *velocities,
                                 jsb_stream stream);
 jsb_status jsb_state_download_all(jsb_context *ctx, float *local_positions, float *velocities, jsb_stream stream);
+/* World positions of every body (3 floats per body, body order; synchronous). World vertex positions
+ * are body position + local position. */
+jsb_status jsb_body_positions_all(jsb_context *ctx, float *positions);
 jsb_status jsb_total_vertices(jsb_context *ctx, uint64_t *total);
 
 /* ---- scheduling and autotuning ------------------------------------------------------------ */
@@ -209,6 +212,11 @@ jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int chec
 jsb_status jsb_adjoint_forward(jsb_context *ctx, int until_step); /* -1 = all num_steps; may be called in pieces */
 jsb_status jsb_adjoint_seed(jsb_context *ctx, int step, uint32_t body_id, const float *dl_dx);
 jsb_status jsb_adjoint_backward(jsb_context *ctx);
+/* Every body at once, in context vertex order (bodies in creation order, 3 floats per vertex):
+ * seeds d loss / d world positions after `step`, and reads d loss / d initial positions, initial
+ * velocities and per-body force (3 floats per body); NULL outputs are skipped. */
+jsb_status jsb_adjoint_seed_all(jsb_context *ctx, int step, const float *dl_dx);
+jsb_status jsb_adjoint_gradients_all(jsb_context *ctx, float *dl_dx0, float *dl_dv0, float *dl_dforce);
 jsb_status jsb_adjoint_gradients(jsb_context *ctx, uint32_t body_id, float *dl_dx0, float *dl_dv0, float *dl_dforce,
                                  float *dl_dedge_compliance, float *dl_dvolume_compliance);
 jsb_status jsb_adjoint_end(jsb_context *ctx);

@@ -64,6 +64,9 @@ SIGNATURES = {
     "jsb_adjoint_begin": [_P, _c.c_float, _c.c_int, _c.c_int],
     "jsb_adjoint_forward": [_P, _c.c_int],
     "jsb_adjoint_seed": [_P, _c.c_int, _c.c_uint32, _P],
+    "jsb_adjoint_seed_all": [_P, _c.c_int, _c.c_void_p],
+    "jsb_adjoint_gradients_all": [_P, _c.c_void_p, _c.c_void_p, _c.c_void_p],
+    "jsb_body_positions_all": [_P, _c.c_void_p],
     "jsb_adjoint_backward": [_P],
     "jsb_adjoint_gradients": [_P, _c.c_uint32, _P, _P, _P, _P, _P],
     "jsb_adjoint_end": [_P],
@@ -300,6 +303,14 @@ class Context:
     def restore_state(self, body: int, state: bytes, position):
         check(lib().jsb_body_restore_state(self.h, body, state, len(state), _f3(position)))
 
+    def save_all(self) -> list[tuple[bytes, np.ndarray]]:
+        """SaveState bytes and world position of every body."""
+        return [(self.save_state(b), self.read_body(b)[0]) for b in range(len(self.num_vertices))]
+
+    def restore_all(self, saved: list[tuple[bytes, np.ndarray]]):
+        for b, (state, position) in enumerate(saved):
+            self.restore_state(b, state, position)
+
     def total_vertices(self) -> int:
         t = ctypes.c_uint64()
         check(lib().jsb_total_vertices(self.h, ctypes.byref(t)))
@@ -336,6 +347,25 @@ class Context:
     def adjoint_seed(self, step: int, body: int, dl_dx: np.ndarray):
         a = np.ascontiguousarray(dl_dx, np.float32)
         check(lib().jsb_adjoint_seed(self.h, step, body, a.ctypes.data))
+
+    def body_positions(self) -> np.ndarray:
+        """World positions of every body (num_bodies x 3)."""
+        out = np.zeros((len(self.num_vertices), 3), np.float32)
+        check(lib().jsb_body_positions_all(self.h, out.ctypes.data))
+        return out
+
+    def adjoint_seed_all(self, step: int, dl_dx: np.ndarray):
+        """d loss / d world positions of every vertex of the context after `step` (total_vertices x 3)."""
+        a = np.ascontiguousarray(dl_dx, np.float32)
+        check(lib().jsb_adjoint_seed_all(self.h, step, a.ctypes.data))
+
+    def adjoint_gradients_all(self) -> dict:
+        n, nb = sum(self.num_vertices), len(self.num_vertices)
+        dx = np.zeros((n, 3), np.float32)
+        dv = np.zeros((n, 3), np.float32)
+        df = np.zeros((nb, 3), np.float32)
+        check(lib().jsb_adjoint_gradients_all(self.h, dx.ctypes.data, dv.ctypes.data, df.ctypes.data))
+        return {"x0": dx, "v0": dv, "force": df}
 
     def adjoint_backward(self):
         check(lib().jsb_adjoint_backward(self.h))

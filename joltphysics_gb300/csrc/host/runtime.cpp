@@ -42,7 +42,8 @@ cudaError_t launch_cluster_step(const StepParams &p, int cluster, int threads, u
                                 cudaStream_t stream);
 cudaError_t init_cluster_kernels(int max_dynamic_smem);
 int cluster_occupancy(int cluster, int threads, size_t smem);
-size_t adjoint_smem_bytes(uint32_t vertices, uint32_t faces);
+size_t adjoint_smem_bytes(uint32_t vertices, uint32_t faces, uint32_t depth, uint32_t rpt);
+int adjoint_threads();
 cudaError_t init_adjoint_kernels(int max_dynamic_smem);
 int adjoint_occupancy(size_t smem);
 cudaError_t launch_adjoint(const AdjParams &q, uint32_t cap_vertices, uint32_t cap_faces, int grid, cudaStream_t stream);
@@ -148,9 +149,31 @@ struct LaunchGroup {  // the bodies of one bucket (or every body on the cluster 
     cudaEvent_t done = nullptr;
 };
 
+// The bodies of one launch group in a differentiable run, with the taped-forward and adjoint launch
+// shapes sized for them (the groups run concurrently on their own streams, like the forward step).
+struct AdjGroup {
+    DevBuf<uint32_t> work;
+    uint32_t num_work = 0;
+    uint32_t cap_vertices = 0, cap_faces = 0, ring_slots = 32, max_level_slots = 0;
+    bool tape_smem_state = true;
+    int tape_grid = 1, adj_grid = 1;
+    uint32_t adj_depth = 0, adj_rpt = 1;  // adjoint record / tape ring: levels ahead, slots per thread
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+};
+
 // State of one differentiable run (jsb_adjoint_*): checkpoints every `every` steps, the tape of one
 // checkpoint segment, adjoint accumulators and loss seeds.
 struct AdjointSession {
+    ~AdjointSession() {
+        for (AdjGroup &g : groups) {
+            if (g.stream) cudaStreamDestroy(g.stream);
+            if (g.done) cudaEventDestroy(g.done);
+        }
+        if (fork) cudaEventDestroy(fork);
+    }
+    std::vector<AdjGroup> groups;
+    cudaEvent_t fork = nullptr;
     float dt = 0.0f;
     int steps = 0, every = 1;
     bool forward_done = false, backward_done = false;
@@ -167,10 +190,7 @@ struct AdjointSession {
     std::vector<size_t> slot_offset;  // per body, into grad_slots
     DevBuf<float4> adj_x, adj_v, seed_dev;
     std::vector<std::pair<int, std::vector<float4>>> seeds;  // (step, dL/dx of every vertex)
-    DevBuf<uint32_t> all_work;
-    bool tape_smem_state = true;
-    uint32_t cap_vertices = 0, cap_faces = 0, ring_slots = 32;
-    int tape_grid = 1, adj_grid = 1;
+    int tape_segment = -1;  // checkpoint segment whose tape is in the tape buffers
 };
 
 }  // namespace
@@ -567,6 +587,58 @@ jsb_status step_impl(jsb_context *ctx, float dt, int collision_steps, cudaStream
         } else if ((st = enqueue_batched(ctx, step_dt, stream, launches)) != JSB_OK)
             return st;
         if (uploaded) JSB_CUDA(cudaMemsetAsync(ctx->forces.ptr, 0, ctx->forces.count * sizeof(float), stream));
+    }
+    return JSB_OK;
+}
+
+// Enqueues one taped forward step of every body (tape position `tape_step` of the segment): one launch
+// per group on the group's stream, forked from and joined back into `stream`.
+jsb_status enqueue_taped(jsb_context *ctx, const AdjointSession &a, int tape_step, cudaStream_t stream, uint32_t &launches) {
+    JSB_CUDA(cudaMemsetAsync(ctx->queues.ptr, 0, a.groups.size() * sizeof(uint32_t), stream));
+    JSB_CUDA(cudaEventRecord(a.fork, stream));
+    for (size_t gi = a.groups.size(); gi-- > 0;) {  // largest bodies first
+        const AdjGroup &g = a.groups[gi];
+        JSB_CUDA(cudaStreamWaitEvent(g.stream, a.fork, 0));
+        StepParams p = base_params(ctx, a.dt);
+        p.work = g.work.ptr;
+        p.num_work = g.num_work;
+        p.queue = ctx->queues.ptr + gi;
+        p.ring_slots = g.ring_slots;
+        p.tape = a.tape_desc.ptr;
+        p.tape_step = uint32_t(tape_step);
+        JSB_CUDA(launch_step_tape(p, g.tape_smem_state, g.cap_vertices, g.cap_faces, g.tape_grid, g.stream));
+        ++launches;
+        JSB_CUDA(cudaEventRecord(g.done, g.stream));
+        JSB_CUDA(cudaStreamWaitEvent(stream, g.done, 0));
+    }
+    return JSB_OK;
+}
+
+// Enqueues the adjoint of step `tape_step` of the segment for every body, like enqueue_taped.
+jsb_status enqueue_adjoint(jsb_context *ctx, const AdjointSession &a, int tape_step, cudaStream_t stream, uint32_t &launches) {
+    JSB_CUDA(cudaMemsetAsync(ctx->queues.ptr, 0, a.groups.size() * sizeof(uint32_t), stream));
+    JSB_CUDA(cudaEventRecord(a.fork, stream));
+    for (size_t gi = a.groups.size(); gi-- > 0;) {
+        const AdjGroup &g = a.groups[gi];
+        JSB_CUDA(cudaStreamWaitEvent(g.stream, a.fork, 0));
+        AdjParams q;
+        q.bodies = ctx->descs.ptr;
+        q.tape = a.tape_desc.ptr;
+        q.tape_step = uint32_t(tape_step);
+        q.work = g.work.ptr;
+        q.num_work = g.num_work;
+        q.queue = ctx->queues.ptr + gi;
+        q.adj_x = a.adj_x.ptr;
+        q.adj_v = a.adj_v.ptr;
+        q.grad_force = a.grad_force.ptr;
+        for (int k = 0; k < 3; ++k) q.gravity[k] = ctx->gravity[k];
+        q.dt = a.dt;
+        q.ring_depth = g.adj_depth;
+        q.ring_rpt = g.adj_rpt;
+        JSB_CUDA(launch_adjoint(q, g.cap_vertices, g.cap_faces, g.adj_grid, g.stream));
+        ++launches;
+        JSB_CUDA(cudaEventRecord(g.done, g.stream));
+        JSB_CUDA(cudaStreamWaitEvent(stream, g.done, 0));
     }
     return JSB_OK;
 }
@@ -980,6 +1052,18 @@ jsb_status jsb_state_download_all(jsb_context *ctx, float *local_positions, floa
     return JSB_OK;
 }
 
+jsb_status jsb_body_positions_all(jsb_context *ctx, float *positions) {
+    if (!check_ctx(ctx) || !positions) return fail(JSB_ERR_INVALID_ARGUMENT, "null argument");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    std::vector<BodyState> hs(ctx->bodies.size());
+    if (!hs.empty()) JSB_CUDA(cudaMemcpy(hs.data(), ctx->states.ptr, hs.size() * sizeof(BodyState), cudaMemcpyDeviceToHost));
+    for (size_t b = 0; b < hs.size(); ++b)
+        for (int k = 0; k < 3; ++k) positions[3 * b + k] = hs[b].position[k];
+    return JSB_OK;
+}
+
 jsb_status jsb_body_schedule_info(jsb_context *ctx, uint32_t body_id, uint32_t *num_levels, uint32_t *num_constraints) {
     if (!check_ctx(ctx) || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
     const Schedule &s = ctx->settings[ctx->bodies[body_id].settings_id]->schedule;
@@ -1242,9 +1326,6 @@ jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int chec
         state += K * it * 3 * nv;
         planes += K * nv;
         slots += ns;
-        a->cap_vertices = std::max(a->cap_vertices, uint32_t(nv));
-        a->cap_faces = std::max(a->cap_faces, pressure_faces(s, br));
-        a->ring_slots = std::max(a->ring_slots, ring_slots_for(s));
     }
     JSB_CUDA(a->tape_cons.alloc(cons));
     JSB_CUDA(a->tape_state.alloc(state));
@@ -1264,18 +1345,51 @@ jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int chec
         desc[b].pad = 0;
     }
     JSB_CUDA(a->tape_desc.upload(desc.data(), nb));
-    std::vector<uint32_t> all(nb);
-    for (size_t b = 0; b < nb; ++b) all[b] = uint32_t(b);
-    JSB_CUDA(a->all_work.upload(all.data(), nb));
     JSB_CUDA(a->adj_x.alloc(ctx->total_vertices));
     JSB_CUDA(a->adj_v.alloc(ctx->total_vertices));
     JSB_CUDA(a->seed_dev.alloc(ctx->total_vertices));
-    a->tape_smem_state = step_smem_bytes(true, a->cap_vertices, a->cap_faces, a->ring_slots) <= cap;
-    const size_t tsmem = step_smem_bytes(a->tape_smem_state, a->cap_vertices, a->cap_faces, a->ring_slots);
-    const size_t asmem = adjoint_smem_bytes(a->cap_vertices, a->cap_faces);
-    if (tsmem > cap || asmem > cap) return fail(JSB_ERR_UNSUPPORTED, "a body is too large for the differentiable (taped) path");
-    a->tape_grid = int(std::min<size_t>(nb, size_t(std::max(1, step_tape_occupancy(a->tape_smem_state, tsmem))) * ctx->num_sms));
-    a->adj_grid = int(std::min<size_t>(nb, size_t(std::max(1, adjoint_occupancy(asmem))) * ctx->num_sms));
+    // One taped-forward / adjoint launch per launch group of the forward step.
+    const uint32_t T = uint32_t(adjoint_threads());
+    int least = 0, greatest = 0;
+    JSB_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    JSB_CUDA(cudaEventCreateWithFlags(&a->fork, cudaEventDisableTiming));
+    const int ng = int(ctx->groups.size());
+    for (int gi = 0; gi < ng; ++gi) {
+        const LaunchGroup &g = ctx->groups[gi];
+        if (g.cluster > 0)
+            return fail(JSB_ERR_UNSUPPORTED, "bodies on the thread-block-cluster path cannot take part in a differentiable run");
+        a->groups.emplace_back();
+        AdjGroup &ag = a->groups.back();
+        for (uint32_t b : g.bodies) {
+            const BodyRec &br = ctx->bodies[b];
+            const SettingsRec &s = *ctx->settings[br.settings_id];
+            ag.cap_vertices = std::max(ag.cap_vertices, uint32_t(s.parsed.vertices.size()));
+            ag.cap_faces = std::max(ag.cap_faces, pressure_faces(s, br));
+            ag.ring_slots = std::max(ag.ring_slots, ring_slots_for(s));
+            ag.max_level_slots = std::max(ag.max_level_slots, s.schedule.max_level_slots);
+        }
+        ag.tape_smem_state = step_smem_bytes(true, ag.cap_vertices, ag.cap_faces, ag.ring_slots) <= cap;
+        const size_t tsmem = step_smem_bytes(ag.tape_smem_state, ag.cap_vertices, ag.cap_faces, ag.ring_slots);
+        if (adjoint_smem_bytes(ag.cap_vertices, ag.cap_faces, 0, 1) > cap || tsmem > cap)
+            return fail(JSB_ERR_UNSUPPORTED, "a body is too large for the differentiable (taped) path");
+        // Deepest adjoint ring (up to 3 levels ahead, up to 4 slots per thread) that fits beside the state.
+        ag.adj_rpt = std::max<uint32_t>(1u, std::min<uint32_t>(4u, (ag.max_level_slots + T - 1) / T));
+        ag.adj_depth = 3;
+        while (ag.adj_depth > 0 && adjoint_smem_bytes(ag.cap_vertices, ag.cap_faces, ag.adj_depth, ag.adj_rpt) > cap) {
+            if (ag.adj_rpt > 1)
+                --ag.adj_rpt;
+            else
+                --ag.adj_depth;
+        }
+        const size_t asmem = adjoint_smem_bytes(ag.cap_vertices, ag.cap_faces, ag.adj_depth, ag.adj_rpt);
+        ag.num_work = uint32_t(g.bodies.size());
+        ag.tape_grid = int(std::min<size_t>(ag.num_work, size_t(std::max(1, step_tape_occupancy(ag.tape_smem_state, tsmem))) * ctx->num_sms));
+        ag.adj_grid = int(std::min<size_t>(ag.num_work, size_t(std::max(1, adjoint_occupancy(asmem))) * ctx->num_sms));
+        JSB_CUDA(ag.work.upload(g.bodies.data(), g.bodies.size()));
+        const int prio = (ng > 1 && greatest != least) ? least + (greatest - least) * gi / (ng - 1) : least;
+        JSB_CUDA(cudaStreamCreateWithPriority(&ag.stream, cudaStreamNonBlocking, prio));
+        JSB_CUDA(cudaEventCreateWithFlags(&ag.done, cudaEventDisableTiming));
+    }
     const int n_ckpt = (num_steps + a->every - 1) / a->every;
     a->ckpt_x.resize(n_ckpt);
     a->ckpt_v.resize(n_ckpt);
@@ -1296,20 +1410,27 @@ jsb_status jsb_adjoint_forward(jsb_context *ctx, int until_step) {
     if (a.cur_step == 0) {
         a.seeds.clear();
         a.backward_done = false;
+        a.tape_segment = -1;
     }
     uint32_t launches = 0;
+    const int last_seg_start = ((a.steps - 1) / a.every) * a.every;
     for (int s = a.cur_step; s < until_step; ++s) {
         if (s % a.every == 0) {
             JSB_CUDA(cudaDeviceSynchronize());
             if ((st = save_state(ctx, a.ckpt_x[s / a.every], a.ckpt_v[s / a.every], a.ckpt_state[s / a.every])) != JSB_OK) return st;
         }
-        if ((st = enqueue_batched(ctx, a.dt, 0, launches)) != JSB_OK) return st;
+        if (s >= last_seg_start) {
+            // The last segment runs taped, so the backward pass starts without recomputing it.
+            if ((st = enqueue_taped(ctx, a, s - last_seg_start, 0, launches)) != JSB_OK) return st;
+        } else if ((st = enqueue_batched(ctx, a.dt, 0, launches)) != JSB_OK)
+            return st;
     }
     JSB_CUDA(cudaDeviceSynchronize());
     a.cur_step = until_step;
     if (a.cur_step == a.steps) {
         if ((st = save_state(ctx, a.final_x, a.final_v, a.final_state)) != JSB_OK) return st;
         a.forward_done = true;
+        a.tape_segment = (a.steps - 1) / a.every;
     }
     ctx->last_launches = launches;
     return JSB_OK;
@@ -1338,6 +1459,49 @@ jsb_status jsb_adjoint_seed(jsb_context *ctx, int step, uint32_t body_id, const 
     return JSB_OK;
 }
 
+jsb_status jsb_adjoint_seed_all(jsb_context *ctx, int step, const float *dl_dx) {
+    if (!check_ctx(ctx) || !ctx->adjoint || !dl_dx) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    AdjointSession &a = *ctx->adjoint;
+    if (step < 1 || step > a.steps) return fail(JSB_ERR_INVALID_ARGUMENT, "seed step must be in 1 .. num_steps");
+    std::vector<float4> *dst = nullptr;
+    for (auto &sd : a.seeds)
+        if (sd.first == step) dst = &sd.second;
+    if (!dst) {
+        a.seeds.push_back({step, std::vector<float4>(ctx->total_vertices, make_float4(0, 0, 0, 0))});
+        dst = &a.seeds.back().second;
+    }
+    for (uint64_t i = 0; i < ctx->total_vertices; ++i) {
+        float4 &d = (*dst)[i];
+        d.x += dl_dx[3 * i + 0];
+        d.y += dl_dx[3 * i + 1];
+        d.z += dl_dx[3 * i + 2];
+    }
+    return JSB_OK;
+}
+
+jsb_status jsb_adjoint_gradients_all(jsb_context *ctx, float *dl_dx0, float *dl_dv0, float *dl_dforce) {
+    if (!check_ctx(ctx) || !ctx->adjoint) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    AdjointSession &a = *ctx->adjoint;
+    if (!a.backward_done) return fail(JSB_ERR_INVALID_ARGUMENT, "jsb_adjoint_backward has not run");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    const uint64_t n = ctx->total_vertices;
+    std::vector<float4> tmp(n);
+    float *outs[2] = {dl_dx0, dl_dv0};
+    const DevBuf<float4> *srcs[2] = {&a.adj_x, &a.adj_v};
+    for (int k = 0; k < 2; ++k) {
+        if (!outs[k]) continue;
+        JSB_CUDA(cudaMemcpy(tmp.data(), srcs[k]->ptr, n * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (uint64_t i = 0; i < n; ++i) {
+            outs[k][3 * i + 0] = tmp[i].x;
+            outs[k][3 * i + 1] = tmp[i].y;
+            outs[k][3 * i + 2] = tmp[i].z;
+        }
+    }
+    if (dl_dforce && !ctx->bodies.empty())
+        JSB_CUDA(cudaMemcpy(dl_dforce, a.grad_force.ptr, ctx->bodies.size() * 3 * sizeof(float), cudaMemcpyDeviceToHost));
+    return JSB_OK;
+}
+
 jsb_status jsb_adjoint_backward(jsb_context *ctx) {
     if (!check_ctx(ctx) || !ctx->adjoint) return fail(JSB_ERR_INVALID_ARGUMENT, "no differentiable run (jsb_adjoint_begin)");
     AdjointSession &a = *ctx->adjoint;
@@ -1346,7 +1510,6 @@ jsb_status jsb_adjoint_backward(jsb_context *ctx) {
     jsb_status st = rebuild(ctx);
     if (st != JSB_OK) return st;
     const uint64_t n = ctx->total_vertices;
-    const uint32_t nb = uint32_t(ctx->bodies.size());
     JSB_CUDA(cudaMemset(a.adj_x.ptr, 0, n * sizeof(float4)));
     JSB_CUDA(cudaMemset(a.adj_v.ptr, 0, n * sizeof(float4)));
     JSB_CUDA(cudaMemset(a.grad_slots.ptr, 0, a.grad_slots.count * sizeof(float)));
@@ -1355,18 +1518,11 @@ jsb_status jsb_adjoint_backward(jsb_context *ctx) {
     const int n_ckpt = int(a.ckpt_x.size());
     for (int seg = n_ckpt - 1; seg >= 0; --seg) {
         const int s0 = seg * a.every, s1 = std::min(s0 + a.every, a.steps);
-        if ((st = load_state(ctx, a.ckpt_x[seg], a.ckpt_v[seg], a.ckpt_state[seg])) != JSB_OK) return st;
-        for (int s = s0; s < s1; ++s) {  // recompute the segment, recording the tape
-            JSB_CUDA(cudaMemsetAsync(ctx->queues.ptr, 0, sizeof(uint32_t), 0));
-            StepParams p = base_params(ctx, a.dt);
-            p.work = a.all_work.ptr;
-            p.num_work = nb;
-            p.queue = ctx->queues.ptr;
-            p.ring_slots = a.ring_slots;
-            p.tape = a.tape_desc.ptr;
-            p.tape_step = uint32_t(s - s0);
-            JSB_CUDA(launch_step_tape(p, a.tape_smem_state, a.cap_vertices, a.cap_faces, a.tape_grid, 0));
-            ++launches;
+        if (a.tape_segment != seg) {  // the forward pass leaves the last segment's tape in place
+            if ((st = load_state(ctx, a.ckpt_x[seg], a.ckpt_v[seg], a.ckpt_state[seg])) != JSB_OK) return st;
+            for (int s = s0; s < s1; ++s)  // recompute the segment, recording the tape
+                if ((st = enqueue_taped(ctx, a, s - s0, 0, launches)) != JSB_OK) return st;
+            a.tape_segment = seg;
         }
         for (int s = s1 - 1; s >= s0; --s) {  // reverse the segment
             for (auto &sd : a.seeds)
@@ -1375,21 +1531,7 @@ jsb_status jsb_adjoint_backward(jsb_context *ctx) {
                     JSB_CUDA(launch_add(a.adj_x.ptr, a.seed_dev.ptr, n, ctx->num_sms, 0));
                     ++launches;
                 }
-            JSB_CUDA(cudaMemsetAsync(ctx->queues.ptr, 0, sizeof(uint32_t), 0));
-            AdjParams q;
-            q.bodies = ctx->descs.ptr;
-            q.tape = a.tape_desc.ptr;
-            q.tape_step = uint32_t(s - s0);
-            q.work = a.all_work.ptr;
-            q.num_work = nb;
-            q.queue = ctx->queues.ptr;
-            q.adj_x = a.adj_x.ptr;
-            q.adj_v = a.adj_v.ptr;
-            q.grad_force = a.grad_force.ptr;
-            for (int k = 0; k < 3; ++k) q.gravity[k] = ctx->gravity[k];
-            q.dt = a.dt;
-            JSB_CUDA(launch_adjoint(q, a.cap_vertices, a.cap_faces, a.adj_grid, 0));
-            ++launches;
+            if ((st = enqueue_adjoint(ctx, a, s - s0, 0, launches)) != JSB_OK) return st;
         }
     }
     JSB_CUDA(cudaDeviceSynchronize());

@@ -135,21 +135,92 @@ __device__ __forceinline__ float block_sum(AdjShared &sh, float v) {
     return t;  // every thread
 }
 
+// ---- asynchronous copies (cp.async, 16 bytes per thread) -----------------------------------------
+__device__ __forceinline__ void adj_cp_async16(void *smem_dst, const void *gmem_src) {
+    const uint32_t dst = uint32_t(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void adj_cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+// Waits until at most `pending` (0 .. 3) of this thread's newest copy groups are still in flight.
+__device__ __forceinline__ void adj_cp_async_wait(uint32_t pending) {
+    if (pending >= 3)
+        asm volatile("cp.async.wait_group 3;\n" ::: "memory");
+    else if (pending == 2)
+        asm volatile("cp.async.wait_group 2;\n" ::: "memory");
+    else if (pending == 1)
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    else
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
 // Reverse of one substep's constraint levels on the position adjoints lx.
+//
+// Thread t reverses slots t, t + T, ... of every level. The record and taped inputs of its first `rpt`
+// slots are streamed `depth` levels ahead (in reverse level order) into the thread's own slice of a
+// shared-memory ring with cp.async; a thread reads only what it copied itself, so the ring needs no
+// barrier. Ring layout: [(depth + 1) levels][rpt slots][record, 3 taped inputs][T threads] x 16 bytes.
 template <int T>
 __device__ __forceinline__ void reverse_levels(float4 *lx, const float *sw, const BodyDesc &d, const float4 *cons, float *grad,
-                                               float inv_dt_sq) {
+                                               float inv_dt_sq, uint4 *ring, uint32_t depth, uint32_t rpt) {
     const uint4 *__restrict__ levels = d.levels;
     const uint4 *__restrict__ rec = d.records;
-    for (int l = int(d.num_levels) - 1; l >= 0; --l) {
+    const int L = int(d.num_levels);
+    const uint32_t tid = threadIdx.x;
+    const uint32_t nring = depth + 1;
+    auto slot = [&](uint32_t l, uint32_t k) { return ring + ((l % nring) * rpt + k) * 4 * T + tid; };
+    auto stage = [&](int l) {
         const uint4 lv = __ldg(levels + l);
         const uint32_t n = __ldg(levels + l + 1).x - lv.x;
-        for (uint32_t s = threadIdx.x; s < n; s += T) {
+        uint32_t s = tid;
+        for (uint32_t k = 0; k < rpt && s < n; ++k, s += T) {
             const uint32_t c = lv.x + s;
-            const uint4 r = __ldg(rec + c);
-            if (r.x == 0xffffffffu) continue;
-            const float4 *tin = cons + size_t(c) * 3;
+            uint4 *dst = slot(uint32_t(l), k);
+            const float4 *src = cons + size_t(c) * 3;
+            adj_cp_async16(dst, rec + c);
+            adj_cp_async16(dst + T, src);
+            if (adj_slot_type(lv, s) == 1) {
+                adj_cp_async16(dst + 2 * T, src + 1);
+                adj_cp_async16(dst + 3 * T, src + 2);
+            }
+        }
+    };
+    if (depth > 0)
+        for (uint32_t k = 0; k < depth; ++k) {
+            if (L - 1 - int(k) >= 0) stage(L - 1 - int(k));
+            adj_cp_async_commit();
+        }
+    for (int l = L - 1; l >= 0; --l) {
+        if (depth > 0) {
+            if (l - int(depth) >= 0) stage(l - int(depth));
+            adj_cp_async_commit();
+            adj_cp_async_wait(depth);  // this thread's copies of level l have landed
+        }
+        const uint4 lv = __ldg(levels + l);
+        const uint32_t n = __ldg(levels + l + 1).x - lv.x;
+        uint32_t k = 0;
+        for (uint32_t s = tid; s < n; s += T, ++k) {
+            const uint32_t c = lv.x + s;
             const int type = adj_slot_type(lv, s);
+            uint4 r;
+            float4 tin[3];
+            if (depth > 0 && k < rpt) {
+                const uint4 *src = slot(uint32_t(l), k);
+                r = src[0];
+                tin[0] = *reinterpret_cast<const float4 *>(src + T);
+                if (type == 1) {
+                    tin[1] = *reinterpret_cast<const float4 *>(src + 2 * T);
+                    tin[2] = *reinterpret_cast<const float4 *>(src + 3 * T);
+                }
+            } else {
+                r = __ldg(rec + c);
+                const float4 *src = cons + size_t(c) * 3;
+                tin[0] = src[0];
+                if (type == 1) {
+                    tin[1] = src[1];
+                    tin[2] = src[2];
+                }
+            }
+            if (r.x == 0xffffffffu) continue;
             if (type == 2)
                 edge_adjoint(lx, sw, r, tin, inv_dt_sq, grad + c);
             else if (type == 1)
@@ -159,13 +230,14 @@ __device__ __forceinline__ void reverse_levels(float4 *lx, const float *sw, cons
         }
         __syncthreads();
     }
+    if (depth > 0) adj_cp_async_wait(0);
 }
 
 // Shared memory (dynamic), cap = the launch's largest vertex count:
 //   lx[cap] position adjoints | lv[cap] velocity adjoints | lp[cap] previous-position adjoints, then
 //   substep positions for the pressure adjoint | w[cap] inverse masses | per-face pressure scratch
 template <int T>
-__device__ void adjoint_body(const AdjParams &q, uint32_t b, float4 *smem, uint32_t cap, AdjShared &sh) {
+__device__ void adjoint_body(const AdjParams &q, uint32_t b, float4 *smem, uint32_t cap, uint32_t cap_faces, AdjShared &sh) {
     const uint32_t tid = threadIdx.x;
     const BodyDesc d = q.bodies[b];
     const TapeDesc td = q.tape[b];
@@ -173,6 +245,7 @@ __device__ void adjoint_body(const AdjParams &q, uint32_t b, float4 *smem, uint3
     float4 *lx = smem, *lv = smem + cap, *lp = smem + 2 * cap;
     float *sw = reinterpret_cast<float *>(smem + 3 * cap);
     float4 *sface = smem + 3 * cap + (cap + 3) / 4;
+    uint4 *ring = reinterpret_cast<uint4 *>(sface + cap_faces);
     float4 *gax = q.adj_x + d.vtx_offset, *gav = q.adj_v + d.vtx_offset;
 
     const float dt_sub = q.dt / float(n_it);
@@ -285,7 +358,8 @@ __device__ void adjoint_body(const AdjParams &q, uint32_t b, float4 *smem, uint3
         }
         __syncthreads();
         // ---- constraint levels, reversed ----
-        reverse_levels<T>(lx, sw, d, td.cons + (size_t(q.tape_step) * n_it + it) * size_t(td.slots) * 3, td.grad, inv_dt_sq);
+        reverse_levels<T>(lx, sw, d, td.cons + (size_t(q.tape_step) * n_it + it) * size_t(td.slots) * 3, td.grad, inv_dt_sq, ring,
+                          q.ring_depth, q.ring_rpt);
         // ---- integration: x' = x + v' dt, v' = (v + g dt + F dt w / N) damp ----
         for (uint32_t i = tid; i < nv; i += T) {
             const float w = sw[i];
@@ -360,7 +434,7 @@ __device__ void adjoint_body(const AdjParams &q, uint32_t b, float4 *smem, uint3
 
 constexpr int kAdjThreads = 128;
 
-__global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(AdjParams q, uint32_t cap) {
+__global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(AdjParams q, uint32_t cap, uint32_t cap_faces) {
     extern __shared__ float4 smem[];
     __shared__ AdjShared sh;
     for (;;) {
@@ -369,7 +443,7 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(AdjParams q, uint3
         const uint32_t item = sh.item;
         __syncthreads();
         if (item >= q.num_work) return;
-        adjoint_body<kAdjThreads>(q, q.work[item], smem, cap, sh);
+        adjoint_body<kAdjThreads>(q, q.work[item], smem, cap, cap_faces, sh);
     }
 }
 
@@ -382,9 +456,15 @@ __global__ void add_kernel(float4 *__restrict__ dst, const float4 *__restrict__ 
 
 }  // namespace
 
-size_t adjoint_smem_bytes(uint32_t vertices, uint32_t faces) {
-    return size_t(vertices) * sizeof(float4) * 3 + size_t((vertices + 3) / 4) * sizeof(float4) + size_t(faces) * sizeof(float4);
+// Dynamic shared memory of the adjoint CTA: 3 adjoint arrays + inverse masses + pressure scratch +
+// the level ring of `depth` levels ahead with `rpt` slots per thread.
+size_t adjoint_smem_bytes(uint32_t vertices, uint32_t faces, uint32_t depth, uint32_t rpt) {
+    const size_t ring = depth > 0 ? size_t(depth + 1) * rpt * 4 * kAdjThreads * sizeof(uint4) : 0;
+    return size_t(vertices) * sizeof(float4) * 3 + size_t((vertices + 3) / 4) * sizeof(float4) + size_t(faces) * sizeof(float4) +
+           ring;
 }
+
+int adjoint_threads() { return kAdjThreads; }
 
 cudaError_t init_adjoint_kernels(int max_dynamic_smem) {
     return cudaFuncSetAttribute(adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
@@ -397,7 +477,8 @@ int adjoint_occupancy(size_t smem) {
 }
 
 cudaError_t launch_adjoint(const AdjParams &q, uint32_t cap_vertices, uint32_t cap_faces, int grid, cudaStream_t stream) {
-    adjoint_kernel<<<grid, kAdjThreads, adjoint_smem_bytes(cap_vertices, cap_faces), stream>>>(q, cap_vertices);
+    adjoint_kernel<<<grid, kAdjThreads, adjoint_smem_bytes(cap_vertices, cap_faces, q.ring_depth, q.ring_rpt), stream>>>(
+        q, cap_vertices, cap_faces);
     return cudaGetLastError();
 }
 

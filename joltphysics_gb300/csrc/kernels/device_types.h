@@ -131,6 +131,8 @@ struct AdjParams {
     float *grad_force;  // 3 per body
     float gravity[3];
     float dt;
+    uint32_t ring_depth;  // levels of records + taped inputs streamed ahead (0: read in place)
+    uint32_t ring_rpt;    // ring slots per thread and level
 };
 
 }  // namespace jsb

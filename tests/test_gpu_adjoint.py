@@ -183,3 +183,36 @@ def test_torch_autograd_binding(jsb):
         f = fd.central(0, "v0", idx, 1e-6)
         assert abs(float(v0.grad[idx]) - f) <= 1e-3 * max(abs(f), 1e-6), (idx, float(v0.grad[idx]), f)
     ctx.close()
+
+
+def test_bulk_seed_and_gradients_equal_per_body(jsb):
+    """jsb_adjoint_seed_all / jsb_adjoint_gradients_all == the per-body calls, and the last checkpoint
+    segment taped during the forward pass gives the same gradients as a recomputed one (a second
+    backward pass recomputes every segment)."""
+    scene_bytes = jsb.build_scene("diff_batch", n_cloth=3, n_cube=2, steps=10)
+    scene, _ = parse_scene(scene_bytes)
+    rng = np.random.default_rng(8)
+    seeds = {10: {b: rng.standard_normal((body.num_vertices, 3)) for b, body in enumerate(scene.bodies)}}
+    per_body = gpu_gradients(jsb, scene_bytes, seeds, 10, 4)
+    ctx = jsb.Context(0)
+    ctx.load_scene(scene_bytes)
+    ctx.set_scene_step_forces()
+    pos = ctx.body_positions()
+    for b in range(len(scene.bodies)):
+        assert np.array_equal(pos[b], ctx.read_body(b)[0])
+    ctx.adjoint_begin(10, 4)
+    ctx.adjoint_forward()
+    ctx.adjoint_seed_all(10, np.concatenate([seeds[10][b] for b in range(len(scene.bodies))]).astype(np.float32))
+    ctx.adjoint_backward()
+    bulk = ctx.adjoint_gradients_all()
+    ctx.adjoint_backward()
+    again = ctx.adjoint_gradients_all()
+    ctx.adjoint_end()
+    off = 0
+    for b, g in enumerate(per_body):
+        n = scene.bodies[b].num_vertices
+        for key in ("x0", "v0"):
+            assert np.array_equal(bulk[key][off:off + n], g[key]), (b, key)
+            assert np.array_equal(again[key][off:off + n], g[key]), (b, key)
+        assert np.array_equal(bulk["force"][b], g["force"]) and np.array_equal(again["force"][b], g["force"])
+        off += n
