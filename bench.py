@@ -295,6 +295,31 @@ def bench_large_body(jsb, torch, stream, steps: int, with_cpu: bool) -> dict:
     return out
 
 
+def profile_driver(args) -> None:
+    """A bare step loop of one workload for ncu captures (warm-up steps, then the captured steps):
+    uneven_batch and large_cloth run batched steps on the default stream; diff_batch_adjoint runs a
+    forward+adjoint pass of `--steps` steps of the differentiable batch (checkpoint every 5)."""
+    import joltphysics_gb300 as jsb
+
+    if args.profile == "diff_batch_adjoint":
+        ctx = jsb.Context(0)
+        ctx.load_scene(jsb.build_scene("diff_batch", steps=args.steps))
+        ctx.set_scene_step_forces()
+        n = sum(ctx.num_vertices)
+        ctx.adjoint_begin(args.steps, 5)
+        ctx.adjoint_forward()
+        ctx.adjoint_seed_all(args.steps, np.full((n, 3), 1e-3, np.float32))
+        ctx.adjoint_backward()
+        ctx.adjoint_end()
+        ctx.synchronize()
+        return
+    ctx = jsb.Context(0)
+    ctx.load_scene(jsb.build_scene(args.profile))
+    for _ in range(args.warmup + args.steps):
+        ctx.step()
+    ctx.synchronize()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -305,8 +330,12 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and large-body measurements")
     ap.add_argument("--large-steps", type=int, default=10)
+    ap.add_argument("--profile", choices=["uneven_batch", "large_cloth", "diff_batch_adjoint"],
+                    help="profiling driver for ncu: run --warmup then --steps steps of one workload, print nothing")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.profile:
+        return profile_driver(args)
 
     rank, world, local = rank_env()
     dist = None

@@ -105,43 +105,66 @@ struct CShared {
     int redi[32][4];
 };
 
-// Walks the dependency levels of one substep with every thread of the cluster. Thread g of the cluster
-// projects slots g, g + G, g + 2G, ... of each level (G = cluster threads); the first `rpt` of them are
-// staged kCRingDepth levels ahead into the thread's ring slice.
+// Walks the dependency levels of one substep with every thread of the cluster. A level wider than one
+// CTA is dealt round-robin over the cluster: thread g (= rank * T + tid) projects slots g, g + G, ...
+// (G = cluster threads) and the level ends at a cluster barrier. A level of at most T slots goes to
+// CTA 0 alone (slot s to thread s); a run of such levels is separated by CTA 0's own barriers and ends
+// with one cluster barrier, which the other CTAs reach directly. The first `rpt` slots of each thread
+// are staged kCRingDepth levels ahead into the thread's ring slice.
 template <int T>
 __device__ __forceinline__ void cluster_levels(ClusterX cx, const BodyDesc &d, const uint4 *sdesc, uint32_t desc_cap, uint4 *ring,
-                                               uint32_t rpt, uint32_t g, uint32_t G, float inv_dt_sq) {
+                                               uint32_t rpt, uint32_t rank, uint32_t G, float inv_dt_sq) {
     const uint32_t L = d.num_levels;
     if (L == 0) return;
     const uint4 *__restrict__ rec = d.records;
     const uint4 *__restrict__ levels = d.levels;
-    uint4 *mine = ring + threadIdx.x;
+    const uint32_t tid = threadIdx.x, g = rank * T + tid;
+    uint4 *mine = ring + tid;
     auto desc = [&](uint32_t l) { return l < desc_cap ? sdesc[l] : __ldg(levels + l); };
+    // First slot of this thread in a level of n slots (>= n: none) and the stride to its next slot.
+    auto first_slot = [&](uint32_t n, uint32_t &stride) -> uint32_t {
+        if (n <= uint32_t(T)) {
+            stride = n;
+            return rank == 0 ? tid : n;
+        }
+        stride = G;
+        return g;
+    };
     auto stage = [&](uint32_t l) {
         const uint4 lv = desc(l);
         const uint32_t n = desc(l + 1).x - lv.x;
         uint4 *dst = mine + (l % kCRingLevels) * rpt * T;
-        uint32_t s = g;
-        for (uint32_t k = 0; k < rpt && s < n; ++k, s += G) cp_async16(dst + k * T, rec + lv.x + s);
+        uint32_t stride;
+        uint32_t s = first_slot(n, stride);
+        for (uint32_t k = 0; k < rpt && s < n; ++k, s += stride) cp_async16(dst + k * T, rec + lv.x + s);
     };
 #pragma unroll
     for (int k = 0; k < kCRingDepth; ++k) {
         if (uint32_t(k) < L) stage(k);
         cp_async_commit();
     }
+    uint32_t next_first = desc(0).x;
     for (uint32_t l = 0; l < L; ++l) {
         if (l + kCRingDepth < L) stage(l + kCRingDepth);
         cp_async_commit();
         cp_async_wait<kCRingDepth>();  // this thread's copies of level l have landed
         const uint4 lv = desc(l);
-        const uint32_t n = desc(l + 1).x - lv.x;
+        const uint32_t end = desc(l + 1).x;
+        const uint32_t n = end - lv.x;
+        next_first = end;
         const uint4 *src = mine + (l % kCRingLevels) * rpt * T;
+        uint32_t stride;
         uint32_t k = 0;
-        for (uint32_t s = g; s < n; s += G, ++k) {
+        for (uint32_t s = first_slot(n, stride); s < n; s += stride, ++k) {
             const uint4 r = k < rpt ? src[k * T] : __ldg(rec + lv.x + s);
             if (r.x != 0xffffffffu) project(cx, r, slot_type(lv, s), inv_dt_sq);
         }
-        cluster_barrier();
+        const bool narrow_pair = n <= uint32_t(T) && l + 1 < L && desc(l + 2).x - next_first <= uint32_t(T);
+        if (narrow_pair) {
+            if (rank == 0) __syncthreads();  // only CTA 0 works on both levels
+        } else {
+            cluster_barrier();
+        }
     }
     cp_async_wait<0>();
 }
@@ -209,7 +232,7 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
     const float nvf = float(nv > 0 ? nv : 1);
     const f3 sub_imp = (force * dt_sub) / nvf;
     const float restitution_threshold = -2.0f * len(g) * dt_sub;
-    const uint32_t gthread = rank * T + tid, G = C * T;
+    const uint32_t G = C * T;
 
     for (uint32_t it = 0; it < n_it; ++it) {
         // IntegratePositions (owned vertices)
@@ -226,7 +249,7 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
             sx[i - first] = with_w(xyz(pi) + v * dt_sub, pi.w);
         }
         cluster_barrier();  // every position integrated before any constraint reads it
-        cluster_levels<T>(cx, d, sdesc, desc_cap, ring, rpt, gthread, G, inv_dt_sq);
+        cluster_levels<T>(cx, d, sdesc, desc_cap, ring, rpt, rank, G, inv_dt_sq);
         // ApplyCollisionConstraintsAndUpdateVelocities (owned vertices; the last level's barrier made
         // every remote write visible). The next integration touches owned vertices only.
         for (uint32_t i = first + tid; i < last; i += T) {
