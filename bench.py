@@ -10,14 +10,17 @@ One bench step = one PhysicsSystem::Update(1/60, 1 collision step) of all 512 bo
 advances 5 substeps (vertex-iterations = sum of vertices x 5 per step).
 
   value : vertex-iterations/s with the state resident in HBM, batched persistent launches replayed as a
-          CUDA graph of one step; L2 is flushed (a 512 MB write) before every timed step and each step is
-          timed alone with CUDA events on the launching stream.
-  e2e   : the same through the C ABI with host buffers: per step, positions + velocities of every vertex
-          are copied from pinned host memory (jsb_state_upload_all), the step runs, and the state is
-          copied back (jsb_state_download_all), all inside the timed region.
+          CUDA graph of one step. The configuration's 240-step run is simulated from the initial state and
+          K steps spread evenly over it are timed, each alone with CUDA events on the launching stream,
+          with L2 flushed (a 512 MB write) before it: the step cost changes along the run (contacts; a few
+          large stiff cloths go non-finite in the reference's own arithmetic, reproduced here bit for bit).
+  e2e   : the whole run through the C ABI with host buffers: per step, positions + velocities of every
+          vertex are copied from pinned host memory (jsb_state_upload_all), the step runs, and the state
+          is copied back (jsb_state_download_all), all inside the timed region.
 
 `--impl reference` times the CPU oracle (a restatement of the reference's soft-body update that is
-bit-identical to it; the reference itself cannot be built on the GPU hosts) on all host cores.
+bit-identical to it; the reference itself cannot be built on the GPU hosts) on all host cores, on the
+same K evenly spread steps of the run.
 """
 from __future__ import annotations
 
@@ -156,25 +159,33 @@ def run_reference_arm(args, rank, world):
     scene_bytes = jsb.build_scene(WORKLOAD, **scene_params(0))
     scene, _ = parse_scene(scene_bytes)
     threads = os.cpu_count() or 1
-    o = Oracle(scene, threads=threads)
     vi_step = sum(b.num_vertices * b.num_iterations for b in scene.bodies)
+    warm = Oracle(scene, threads=threads)
     for _ in range(args.warmup):
-        o.step(1)
-    times = []
-    for _ in range(args.steps):
+        warm.step(1)
+    # the same timed steps as the GPU arm: K steps spread evenly over the configuration's run
+    run_steps = max(scene.num_steps, args.steps)
+    timed = sorted({max(1, round((j + 1) * run_steps / args.steps)) for j in range(args.steps)})
+    o = Oracle(scene, threads=threads)
+    times, done = [], 0
+    for step in timed:
+        if step - 1 > done:
+            o.step(step - 1 - done)
         t0 = time.perf_counter()
         o.step(1)
         times.append(time.perf_counter() - t0)
+        done = step
     total = sum(times)
-    value = vi_step * args.steps / total
+    value = vi_step * len(timed) / total
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": len(timed),
+        "warmup": args.warmup, "ms_per_step": 1000 * total / len(timed), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "bodies": len(scene.bodies), "vertices": sum(b.num_vertices for b in scene.bodies),
                    "iterations": 5, "dt": scene.dt},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} full steps of all {len(scene.bodies)} bodies"},
+                         "sample": f"{len(timed)} full steps of all {len(scene.bodies)} bodies, spread evenly over the "
+                                   f"{run_steps}-step run (untimed steps in between)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -190,12 +201,12 @@ def cpu_baseline(scene, budget_s: float = 12.0) -> dict:
     t0 = time.perf_counter()
     o.step(1)
     first = time.perf_counter() - t0
-    n = max(1, min(200, int(budget_s / max(first, 1e-6))))
+    n = max(1, min(scene.num_steps - 1, int(budget_s / max(first, 1e-6))))
     t0 = time.perf_counter()
     o.step(n)
     dt = time.perf_counter() - t0
     return {"value": vi_step * n / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} full steps of all {len(scene.bodies)} bodies (after 1 warm-up step)"}
+            "sample": f"steps 2..{n + 1} of the run, all {len(scene.bodies)} bodies (after 1 warm-up step)"}
 
 
 def bench_adjoint(jsb, stream_ptr, steps: int = 90, every: int = 15) -> dict:
@@ -371,6 +382,7 @@ def main():
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
     # autotune the launch shape per body-size bucket, then warm up (graph of one step)
+    initial = ctx.save_all()
     ctx.autotune(trials=3)
     buckets = [b for b in ctx.bucket_table()]
     with torch.cuda.stream(stream):
@@ -380,39 +392,59 @@ def main():
     ctx.synchronize()
 
     # ---- device-resident timed region ------------------------------------------------------------
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    # The configuration's whole run (240 steps) is simulated from the initial state; K of its steps,
+    # spread evenly over the run, are timed (each alone, L2 flushed before it). The per-step cost changes
+    # along the run (bodies land on the floor; a few large stiff cloths go non-finite in the reference's
+    # own arithmetic, which this solver reproduces), so evenly spread samples stand for the whole run.
+    run_steps = max(scene.num_steps, args.steps)
+    timed = sorted({max(1, round((j + 1) * run_steps / args.steps)) for j in range(args.steps)})
+    ctx.restore_all(initial)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in timed]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in timed]
     launches = 0
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         t_wall = time.perf_counter()
-        for i in range(args.steps):
+        k = 0
+        for step in range(1, run_steps + 1):
             with torch.cuda.stream(stream):
-                flush.fill_(i & 0xFF)  # L2 flush (untimed: outside the event pair)
-                starts[i].record(stream)
-                ctx.step_graph(1, 1, stream=sptr)
-                ends[i].record(stream)
-            launches += ctx.last_launch_count()
+                if k < len(timed) and step == timed[k]:
+                    flush.fill_(step & 0xFF)  # L2 flush (untimed: outside the event pair)
+                    starts[k].record(stream)
+                    ctx.step_graph(1, 1, stream=sptr)
+                    ends[k].record(stream)
+                    launches += ctx.last_launch_count()
+                    k += 1
+                else:
+                    ctx.step_graph(1, 1, stream=sptr)
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall
-    ctx.synchronize()
+    non_finite = False
+    try:
+        ctx.synchronize()
+    except jsb.JsbError as e:  # the reference's own blow-ups (see above); the state is still stepped
+        non_finite = e.status == jsb.JSB_ERR_NONFINITE
+        if not non_finite:
+            raise
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = sum(step_ms)
     if dist:
         t = torch.tensor([total_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
-    value = vi_step * world * args.steps / (total_ms / 1000.0)
+    n_timed = len(timed)
+    value = vi_step * world * n_timed / (total_ms / 1000.0)
 
-    # ---- end to end through the C ABI with host buffers ------------------------------------------
+    # ---- end to end through the C ABI with host buffers: the whole run again ---------------------
+    ctx.restore_all(initial)
     pos_h = torch.empty((n_vertices, 3), dtype=torch.float32, pin_memory=True)
     vel_h = torch.empty((n_vertices, 3), dtype=torch.float32, pin_memory=True)
     with torch.cuda.stream(stream):
         ctx.download_all(pos_h.numpy(), vel_h.numpy(), stream=sptr)
     torch.cuda.synchronize()
-    e2e_steps = max(3, args.steps // 2)
+    e2e_steps = run_steps
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     if dist:
@@ -426,7 +458,11 @@ def main():
             ctx.download_all(pos_h.numpy(), vel_h.numpy(), stream=sptr)
         e1.record(stream)
     torch.cuda.synchronize()
-    ctx.synchronize()
+    try:
+        ctx.synchronize()
+    except jsb.JsbError as e:
+        if e.status != jsb.JSB_ERR_NONFINITE:
+            raise
     e2e_ms = e0.elapsed_time(e1)
     if dist:
         t = torch.tensor([e2e_ms], device="cuda")
@@ -435,23 +471,39 @@ def main():
     e2e_value = vi_step * world * e2e_steps / (e2e_ms / 1000.0)
     io_bytes = n_vertices * 3 * 4 * 2
 
-    # ---- plain one-body-per-launch form (for the batched / plain ratio) --------------------------
-    plain_value = None
+    # ---- plain one-body-per-launch form against batched, on the same state (mid-run) -------------
+    plain_value = batched_same = None
     if args.plain_steps > 0:
+        ctx.restore_all(initial)
+        with torch.cuda.stream(stream):
+            ctx.step_graph(run_steps // 2, 1, stream=sptr)
+        torch.cuda.synchronize()
+        mid = ctx.save_all()
         p0 = torch.cuda.Event(enable_timing=True)
         p1 = torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
-            ctx.step_plain(stream=sptr)
             p0.record(stream)
             for _ in range(args.plain_steps):
                 ctx.step_plain(stream=sptr)
             p1.record(stream)
         torch.cuda.synchronize()
-        ctx.synchronize()
         plain_value = vi_step * args.plain_steps / (p0.elapsed_time(p1) / 1000.0)
+        ctx.restore_all(mid)
+        with torch.cuda.stream(stream):
+            p0.record(stream)
+            for _ in range(args.plain_steps):
+                ctx.step_graph(1, 1, stream=sptr)
+            p1.record(stream)
+        torch.cuda.synchronize()
+        batched_same = vi_step * args.plain_steps / (p0.elapsed_time(p1) / 1000.0)
+        try:
+            ctx.synchronize()
+        except jsb.JsbError as e:
+            if e.status != jsb.JSB_ERR_NONFINITE:
+                raise
 
     peaks = measured_peaks()
-    mean_step_s = total_ms / 1000.0 / args.steps
+    mean_step_s = total_ms / 1000.0 / n_timed
     achieved = bytes_step / mean_step_s / 1e9
     traffic = profile_traffic()
     if rank != 0:
@@ -459,21 +511,25 @@ def main():
             dist.destroy_process_group()
         return
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": n_timed, "warmup": args.warmup,
+        "ms_per_step": total_ms / n_timed, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "bodies": len(scene.bodies), "vertices": n_vertices, "iterations": 5,
                    "dt": scene.dt, "vertex_iterations_per_step": vi_step, "l2": "flushed before every timed step",
                    "form": "batched persistent launches per size bucket, CUDA graph of one step",
+                   "timed_steps": f"{n_timed} steps spread evenly over the {run_steps}-step run from the initial state",
+                   "step_ms_min_max": [min(step_ms), max(step_ms)],
+                   "reference_non_finite_bodies_in_run": non_finite,
                    "buckets_max_vertices_threads_state": buckets},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
-                "steps": e2e_steps},
+                "steps": e2e_steps, "note": "the whole run through the C ABI, host copies every step"},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                      "peak_source": peaks["source"], "algorithmic_bytes_per_step": bytes_step},
-        "plain": {"value": plain_value, "unit": UNIT, "steps": args.plain_steps,
-                  "batched_over_plain": (value / plain_value) if plain_value else None},
+        "plain": {"value": plain_value, "unit": UNIT, "steps": args.plain_steps, "state": "mid-run",
+                  "batched_same_state": batched_same,
+                  "batched_over_plain": (batched_same / plain_value) if plain_value else None},
         "clocks": clocks.summary(),
         "wall_s": t_wall,
     }

@@ -1186,9 +1186,14 @@ jsb_status jsb_autotune(jsb_context *ctx, float dt, int trials) {
     JSB_CUDA(cudaMemcpy(ss.ptr, ctx->states.ptr, ctx->bodies.size() * sizeof(BodyState), cudaMemcpyDeviceToDevice));
     cudaStream_t stream;
     JSB_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    // Every configuration is timed on the same steps: the saved state is restored before each one.
     auto measure = [&](float &ms_out) -> jsb_status {
         jsb_status s2 = rebuild_groups(ctx);
         if (s2 != JSB_OK) return s2;
+        JSB_CUDA(cudaMemcpyAsync(ctx->x.ptr, sx.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
+        JSB_CUDA(cudaMemcpyAsync(ctx->v.ptr, sv.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
+        JSB_CUDA(cudaMemcpyAsync(ctx->states.ptr, ss.ptr, ctx->bodies.size() * sizeof(BodyState), cudaMemcpyDeviceToDevice,
+                                 stream));
         std::vector<float> times;
         for (int k = 0; k < trials + 1; ++k) {
             uint32_t launches = 0;
