@@ -341,6 +341,7 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and large-body measurements")
     ap.add_argument("--large-steps", type=int, default=10)
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch-shape table")
     ap.add_argument("--profile", choices=["uneven_batch", "large_cloth", "diff_batch_adjoint"],
                     help="profiling driver for ncu: run --warmup then --steps steps of one workload, print nothing")
     args = ap.parse_args()
@@ -383,7 +384,8 @@ def main():
 
     # autotune the launch shape per body-size bucket, then warm up (graph of one step)
     initial = ctx.save_all()
-    ctx.autotune(trials=3)
+    if not args.no_autotune:
+        ctx.autotune(trials=3)
     buckets = [b for b in ctx.bucket_table()]
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -519,6 +521,7 @@ def main():
                    "form": "batched persistent launches per size bucket, CUDA graph of one step",
                    "timed_steps": f"{n_timed} steps spread evenly over the {run_steps}-step run from the initial state",
                    "step_ms_min_max": [min(step_ms), max(step_ms)],
+                   "step_ms": {str(st): round(ms, 3) for st, ms in zip(timed, step_ms)},
                    "reference_non_finite_bodies_in_run": non_finite,
                    "buckets_max_vertices_threads_state": buckets},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,

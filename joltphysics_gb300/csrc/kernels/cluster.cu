@@ -94,13 +94,16 @@ struct Partials {
     float val[12];  // min x, y, z | max x, y, z | predicted min x, y, z | predicted max x, y, z
     int idx[12];
     float sum[6];  // linear velocity, angular velocity sums
+    int last_nan[6];  // last owned vertex with a NaN component (positions x, y, z, predicted x, y, z)
 };
 
 struct CShared {
     SCol cols[kMaxCollidingShapes];
     int ncols;
+    int nan_flag[2];  // this CTA's vertices hold a NaN after the substep's integration (by substep parity)
     float delta[3];
     Partials part;
+    int last_nan[6];  // over the whole body
     float red[32][4];
     int redi[32][4];
 };
@@ -111,7 +114,7 @@ struct CShared {
 // CTA 0 alone (slot s to thread s); a run of such levels is separated by CTA 0's own barriers and ends
 // with one cluster barrier, which the other CTAs reach directly. The first `rpt` slots of each thread
 // are staged kCRingDepth levels ahead into the thread's ring slice.
-template <int T>
+template <int T, bool kGuard>
 __device__ __forceinline__ void cluster_levels(ClusterX cx, const BodyDesc &d, const uint4 *sdesc, uint32_t desc_cap, uint4 *ring,
                                                uint32_t rpt, uint32_t rank, uint32_t G, float inv_dt_sq) {
     const uint32_t L = d.num_levels;
@@ -157,7 +160,7 @@ __device__ __forceinline__ void cluster_levels(ClusterX cx, const BodyDesc &d, c
         uint32_t k = 0;
         for (uint32_t s = first_slot(n, stride); s < n; s += stride, ++k) {
             const uint4 r = k < rpt ? src[k * T] : __ldg(rec + lv.x + s);
-            if (r.x != 0xffffffffu) project(cx, r, slot_type(lv, s), inv_dt_sq);
+            if (r.x != 0xffffffffu) project<kGuard>(cx, r, slot_type(lv, s), inv_dt_sq);
         }
         const bool narrow_pair = n <= uint32_t(T) && l + 1 < L && desc(l + 2).x - next_first <= uint32_t(T);
         if (narrow_pair) {
@@ -236,6 +239,7 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
 
     for (uint32_t it = 0; it < n_it; ++it) {
         // IntegratePositions (owned vertices)
+        bool nan_seen = false;
         for (uint32_t i = first + tid; i < last; i += T) {
             const float4 pi = sx[i - first];
             const float4 vel = gv[i];
@@ -246,10 +250,20 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
             }
             gprev[i] = pi;
             gv[i] = with_w(v, vel.w);
-            sx[i - first] = with_w(xyz(pi) + v * dt_sub, pi.w);
+            const f3 xn = xyz(pi) + v * dt_sub;
+            nan_seen = nan_seen || has_nan(xn);
+            sx[i - first] = with_w(xn, pi.w);
         }
+        nan_seen = __syncthreads_or(nan_seen);
+        if (tid == 0) sh.nan_flag[it & 1] = nan_seen ? 1 : 0;
         cluster_barrier();  // every position integrated before any constraint reads it
-        cluster_levels<T>(cx, d, sdesc, desc_cap, ring, rpt, rank, G, inv_dt_sq);
+        // NaN-guarded projections when any CTA's vertices hold a NaN (flags double-buffered by substep)
+        bool guard = false;
+        for (uint32_t q = 0; q < C; ++q) guard = guard || ld_cluster_s32(map_rank(smem_u32(&sh.nan_flag[it & 1]), q)) != 0;
+        if (guard)
+            cluster_levels<T, true>(cx, d, sdesc, desc_cap, ring, rpt, rank, G, inv_dt_sq);
+        else
+            cluster_levels<T, false>(cx, d, sdesc, desc_cap, ring, rpt, rank, G, inv_dt_sq);
         // ApplyCollisionConstraintsAndUpdateVelocities (owned vertices; the last level's barrier made
         // every remote write visible). The next integration touches owned vertices only.
         for (uint32_t i = first + tid; i < last; i += T) {
@@ -270,14 +284,9 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
     // UpdateSoftBodyState: per-CTA partials over owned vertices, combined by rank 0.
     __syncthreads();
     const float max_sq = d.max_linear_velocity * d.max_linear_velocity;
-    float mm[4] = {FLT_MAX, FLT_MAX, FLT_MAX, 0};
-    int mi[4] = {-1, -1, -1, -1};
-    float xx[4] = {-FLT_MAX, -FLT_MAX, -FLT_MAX, 0};
-    int xi[4] = {-1, -1, -1, -1};
-    float pm[4] = {FLT_MAX, FLT_MAX, FLT_MAX, 0};
-    int pmi[4] = {-1, -1, -1, -1};
-    float px[4] = {-FLT_MAX, -FLT_MAX, -FLT_MAX, 0};
-    int pxi[4] = {-1, -1, -1, -1};
+    const int all[6] = {-1, -1, -1, -1, -1, -1};
+    Bounds bd;
+    bounds_init(bd);
     f3 lin = mk(0, 0, 0), ang = mk(0, 0, 0);
     bool finite = true;
     for (uint32_t i = first + tid; i < last; i += T) {
@@ -289,29 +298,12 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
         lin = lin + v;
         ang = ang + cross(x, v);
         const f3 pred = (x + v * dt) + disp_g;
-        pick_min(mm[0], mi[0], x.x, int(i));
-        pick_min(mm[1], mi[1], x.y, int(i));
-        pick_min(mm[2], mi[2], x.z, int(i));
-        pick_max(xx[0], xi[0], x.x, int(i));
-        pick_max(xx[1], xi[1], x.y, int(i));
-        pick_max(xx[2], xi[2], x.z, int(i));
-        pick_min(pm[0], pmi[0], pred.x, int(i));
-        pick_min(pm[1], pmi[1], pred.y, int(i));
-        pick_min(pm[2], pmi[2], pred.z, int(i));
-        pick_max(px[0], pxi[0], pred.x, int(i));
-        pick_max(px[1], pxi[1], pred.y, int(i));
-        pick_max(px[2], pxi[2], pred.z, int(i));
+        bounds_add(bd, x, pred, int(i), all);
         finite = finite && isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
     }
     if (!finite) atomicOr(p.error, kErrNonFinite);
-    {
-        const bool mins[4] = {false, false, false, false};
-        const bool maxs[4] = {true, true, true, true};
-        reduce_minmax4<T>(sh, mm, mi, mins);
-        reduce_minmax4<T>(sh, xx, xi, maxs);
-        reduce_minmax4<T>(sh, pm, pmi, mins);
-        reduce_minmax4<T>(sh, px, pxi, maxs);
-    }
+    bounds_reduce<T>(sh, bd);
+    reduce_last_nan<T>(bd.last_nan, sh.last_nan);
     float sums[6];
     sums[0] = reduce_sum<T>(sh, lin.x, 0);
     sums[1] = reduce_sum<T>(sh, lin.y, 1);
@@ -319,16 +311,46 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
     sums[3] = reduce_sum<T>(sh, ang.x, 3);
     sums[4] = reduce_sum<T>(sh, ang.y, 0);
     sums[5] = reduce_sum<T>(sh, ang.z, 1);
-    if (tid == 0) {
+    auto write_bounds = [&]() {
         for (int k = 0; k < 3; ++k) {
-            sh.part.val[k] = mm[k], sh.part.idx[k] = mi[k];
-            sh.part.val[3 + k] = xx[k], sh.part.idx[3 + k] = xi[k];
-            sh.part.val[6 + k] = pm[k], sh.part.idx[6 + k] = pmi[k];
-            sh.part.val[9 + k] = px[k], sh.part.idx[9 + k] = pxi[k];
+            sh.part.val[k] = bd.mm[k], sh.part.idx[k] = bd.mi[k];
+            sh.part.val[3 + k] = bd.xx[k], sh.part.idx[3 + k] = bd.xi[k];
+            sh.part.val[6 + k] = bd.pm[k], sh.part.idx[6 + k] = bd.pmi[k];
+            sh.part.val[9 + k] = bd.px[k], sh.part.idx[9 + k] = bd.pxi[k];
         }
-        for (int k = 0; k < 6; ++k) sh.part.sum[k] = sums[k];
+    };
+    if (tid == 0) {
+        write_bounds();
+        for (int k = 0; k < 6; ++k) sh.part.sum[k] = sums[k], sh.part.last_nan[k] = sh.last_nan[k];
     }
     cluster_barrier();
+    // The body's last NaN index per component (the maximum over the CTAs); a body holding NaNs repeats
+    // its bounds over the vertices after it (the reference's sequential _mm_min_ps / _mm_max_ps).
+    if (tid == 0) {
+        int m[6] = {-1, -1, -1, -1, -1, -1};
+        for (uint32_t q = 0; q < C; ++q) {
+            const uint32_t base = map_rank(smem_u32(&sh.part), q) + uint32_t(offsetof(Partials, last_nan));
+            for (int k = 0; k < 6; ++k) m[k] = max(m[k], ld_cluster_s32(base + 4u * k));
+        }
+        for (int k = 0; k < 6; ++k) sh.last_nan[k] = m[k];
+    }
+    __syncthreads();
+    int skip[6];
+    bool redo = false;
+    for (int k = 0; k < 6; ++k) {
+        skip[k] = sh.last_nan[k];
+        redo = redo || skip[k] >= 0;
+    }
+    if (redo) {  // uniform over the cluster
+        bounds_init(bd);
+        for (uint32_t i = first + tid; i < last; i += T) {
+            const f3 x = xyz(sx[i - first]), v = xyz(gv[i]);
+            bounds_add(bd, x, (x + v * dt) + disp_g, int(i), skip);
+        }
+        bounds_reduce<T>(sh, bd);
+        if (tid == 0) write_bounds();
+        cluster_barrier();
+    }
     if (rank == 0 && tid == 0) {
         Partials acc = sh.part;
         const uint32_t local = smem_u32(&sh.part);
@@ -343,6 +365,13 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
                     pick_min(acc.val[k], acc.idx[k], ov, oi);
             }
             for (int k = 0; k < 6; ++k) acc.sum[k] = acc.sum[k] + ld_cluster_f32(base + uint32_t(offsetof(Partials, sum)) + 4u * k);
+        }
+        if (redo) {
+            const float q = __int_as_float(0x7fffffff);
+            for (int k = 0; k < 3; ++k) {
+                if (skip[k] == int(nv) - 1) acc.val[k] = acc.val[3 + k] = q;
+                if (skip[3 + k] == int(nv) - 1) acc.val[6 + k] = acc.val[9 + k] = q;
+            }
         }
         const f3 delta = finish_body_state(st, d, body_pos, mk(acc.val[0], acc.val[1], acc.val[2]), mk(acc.val[3], acc.val[4], acc.val[5]),
                                            mk(acc.val[6], acc.val[7], acc.val[8]), mk(acc.val[9], acc.val[10], acc.val[11]), acc.sum,

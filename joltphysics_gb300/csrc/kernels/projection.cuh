@@ -27,15 +27,37 @@ struct SCol {  // one colliding shape, relative to the soft body
     float restitution;
 };
 
+// NaN positions (a body that has blown up in the reference's own arithmetic) would send every division
+// and square root of a projection down the IEEE routines' slow path. For a body holding NaN positions
+// the walkers run the projections with kGuard set, which test their inputs once instead: with a NaN
+// coordinate among them, the reference's bend, volume and edge projections write NaN to every
+// coordinate of every vertex they move (no early exit can be taken on a NaN; a bend's e_len exit only
+// while x0 and x1 are finite), and that is written directly, as the canonical NaN the GPU's arithmetic
+// produces, so the result is the same with or without the guard.
+__device__ __forceinline__ bool has_nan(f3 a) { return a.x != a.x || a.y != a.y || a.z != a.z; }
+__device__ __forceinline__ float4 nan_w(float w) {
+    const float q = __int_as_float(0x7fffffff);
+    return make_float4(q, q, q, w);
+}
+
 // ---------------------------------------------------------------------------------------------
 // Constraint projections (exact reference arithmetic)
 // ---------------------------------------------------------------------------------------------
-template <class X>
+template <bool kGuard = false, class X>
 __device__ __forceinline__ void project_bend(X sx, uint4 r, float inv_dt_sq) {  // :367-456
     uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16, i2 = r.y & 0xffff, i3 = r.y >> 16;
     float compliance = __uint_as_float(r.z), initial_angle = __uint_as_float(r.w);
     float4 p0 = ldx(sx, i0), p1 = ldx(sx, i1), p2 = ldx(sx, i2), p3 = ldx(sx, i3);
     f3 x0 = xyz(p0), x1 = xyz(p1), x2 = xyz(p2), x3 = xyz(p3);
+    if (kGuard && (has_nan(x0) || has_nan(x1) || has_nan(x2) || has_nan(x3))) {
+        // e_len < 1e-6 is the only exit that can still be taken: with x0 and x1 finite and close
+        if (!has_nan(x0) && !has_nan(x1) && len(x1 - x0) < 1.0e-6f) return;
+        stx(sx, i0, nan_w(p0.w));
+        stx(sx, i1, nan_w(p1.w));
+        stx(sx, i2, nan_w(p2.w));
+        stx(sx, i3, nan_w(p3.w));
+        return;
+    }
     f3 e = x1 - x0;
     float e_len = len(e);
     if (e_len < 1.0e-6f) return;
@@ -68,12 +90,19 @@ __device__ __forceinline__ void project_bend(X sx, uint4 r, float inv_dt_sq) {  
     stx(sx, i3, with_w(x3 - (ml * w3) * d3c, w3));
 }
 
-template <class X>
+template <bool kGuard = false, class X>
 __device__ __forceinline__ void project_volume(X sx, uint4 r, float inv_dt_sq) {  // :458-507
     uint32_t i1 = r.x & 0xffff, i2 = r.x >> 16, i3 = r.y & 0xffff, i4 = r.y >> 16;
     float six_rest = __uint_as_float(r.z), compliance = __uint_as_float(r.w);
     float4 p1 = ldx(sx, i1), p2 = ldx(sx, i2), p3 = ldx(sx, i3), p4 = ldx(sx, i4);
     f3 x1 = xyz(p1), x2 = xyz(p2), x3 = xyz(p3), x4 = xyz(p4);
+    if (kGuard && (has_nan(x1) || has_nan(x2) || has_nan(x3) || has_nan(x4))) {
+        stx(sx, i1, nan_w(p1.w));
+        stx(sx, i2, nan_w(p2.w));
+        stx(sx, i3, nan_w(p3.w));
+        stx(sx, i4, nan_w(p4.w));
+        return;
+    }
     f3 x1x2 = x2 - x1, x1x3 = x3 - x1, x1x4 = x4 - x1;
     float c = fabsf(dot(cross(x1x2, x1x3), x1x4)) - six_rest;
     f3 d1c = cross(x4 - x2, x3 - x2);
@@ -90,12 +119,17 @@ __device__ __forceinline__ void project_volume(X sx, uint4 r, float inv_dt_sq) {
     stx(sx, i4, with_w(x4 - (ml * w4) * d4c, w4));
 }
 
-template <class X>
+template <bool kGuard = false, class X>
 __device__ __forceinline__ void project_edge(X sx, uint4 r, float inv_dt_sq) {  // :573-601
     uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16;
     float rest = __uint_as_float(r.z), compliance = __uint_as_float(r.w);
     float4 p0 = ldx(sx, i0), p1 = ldx(sx, i1);
     f3 x0 = xyz(p0), x1 = xyz(p1);
+    if (kGuard && (has_nan(x0) || has_nan(x1))) {
+        stx(sx, i0, nan_w(p0.w));
+        stx(sx, i1, nan_w(p1.w));
+        return;
+    }
     f3 delta = x1 - x0;
     float length = len(delta);
     float denom = length * (p0.w + p1.w + compliance * inv_dt_sq);
@@ -116,16 +150,16 @@ __device__ __forceinline__ void project_lra(X sx, uint4 r) {  // :679-698
     if (dls > md * md) stx(sx, i1, with_w(x0 + (delta * md) / jsqrt(dls), p1.w));
 }
 
-template <class X>
+template <bool kGuard = false, class X>
 __device__ __forceinline__ void project(X sx, uint4 r, int type, float inv_dt_sq) {
     if (type == 0)
-        project_bend(sx, r, inv_dt_sq);
+        project_bend<kGuard>(sx, r, inv_dt_sq);
     else if (type == 1)
-        project_volume(sx, r, inv_dt_sq);
+        project_volume<kGuard>(sx, r, inv_dt_sq);
     else if (type == 2)
-        project_edge(sx, r, inv_dt_sq);
+        project_edge<kGuard>(sx, r, inv_dt_sq);
     else
-        project_lra(sx, r);
+        project_lra(sx, r);  // a NaN input fails its distance test: no division, no write
 }
 
 // Type of slot `s` of a level with descriptor {first slot, bend end, volume end, edge end}: the
@@ -368,6 +402,83 @@ __device__ __forceinline__ float reduce_sum(S &sh, float v, int slot) {
         __syncthreads();
     }
     return v;  // valid in thread 0
+}
+
+
+// ---------------------------------------------------------------------------------------------
+// Bounds of UpdateSoftBodyState (SoftBodyMotionProperties.cpp:852-875)
+// ---------------------------------------------------------------------------------------------
+// The reference encapsulates vertices in order with AABox::Encapsulate, i.e. Vec3::sMin / sMax, which are
+// _mm_min_ps / _mm_max_ps on its deterministic x86 build: per component, m = (m < p) ? m : p. Among
+// finite values that is the minimum, later vertices winning ties; a NaN component resets the running
+// value (to NaN, then to the next vertex's value). So per component the result is the extreme over the
+// vertices after the last one whose component is NaN, or NaN if that is the last vertex. The pass below
+// collects (value, index) extremes of vertices with index > skip[c] (skip = -1: all) and the last NaN
+// index per component; a body holding NaNs repeats the pass with skip = those indices.
+struct Bounds {
+    float mm[4], xx[4], pm[4], px[4];  // min / max of positions, min / max of predicted positions
+    int mi[4], xi[4], pmi[4], pxi[4];
+    int last_nan[6];  // positions x, y, z, predicted x, y, z
+};
+__device__ __forceinline__ void bounds_init(Bounds &b) {
+    for (int k = 0; k < 4; ++k) {
+        b.mm[k] = FLT_MAX, b.xx[k] = -FLT_MAX, b.pm[k] = FLT_MAX, b.px[k] = -FLT_MAX;
+        b.mi[k] = b.xi[k] = b.pmi[k] = b.pxi[k] = -1;
+    }
+    for (int k = 0; k < 6; ++k) b.last_nan[k] = -1;
+}
+__device__ __forceinline__ void bounds_add(Bounds &b, f3 x, f3 pred, int i, const int skip[6]) {
+    const float c[6] = {x.x, x.y, x.z, pred.x, pred.y, pred.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        if (i > skip[k]) {
+            pick_min(b.mm[k], b.mi[k], c[k], i);
+            pick_max(b.xx[k], b.xi[k], c[k], i);
+        }
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        if (i > skip[3 + k]) {
+            pick_min(b.pm[k], b.pmi[k], c[3 + k], i);
+            pick_max(b.px[k], b.pxi[k], c[3 + k], i);
+        }
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+        if (c[k] != c[k]) b.last_nan[k] = i;  // vertices arrive in increasing index order per thread
+}
+template <int T, class S>
+__device__ __forceinline__ void bounds_reduce(S &sh, Bounds &b) {
+    const bool mins[4] = {false, false, false, false};
+    const bool maxs[4] = {true, true, true, true};
+    reduce_minmax4<T>(sh, b.mm, b.mi, mins);
+    reduce_minmax4<T>(sh, b.xx, b.xi, maxs);
+    reduce_minmax4<T>(sh, b.pm, b.pmi, mins);
+    reduce_minmax4<T>(sh, b.px, b.pxi, maxs);
+}
+// Block-wide maximum of the six last-NaN indices, written to out[6] (shared) and visible to every thread.
+template <int T>
+__device__ __forceinline__ void reduce_last_nan(const int v[6], int *out) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int r[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        r[k] = v[k];
+        for (int off = 16; off > 0; off >>= 1) r[k] = max(r[k], __shfl_down_sync(0xffffffffu, r[k], off));
+    }
+    __syncthreads();  // earlier readers of out are done
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 6; ++k) out[k] = r[k];
+    __syncthreads();
+    if (T > 32 && lane == 0 && warp > 0)
+        for (int k = 0; k < 6; ++k) atomicMax(out + k, r[k]);
+    __syncthreads();
+}
+// Components whose last vertex is NaN end as NaN (the canonical NaN).
+__device__ __forceinline__ void bounds_nan_tail(Bounds &b, const int *last_nan, int num_vertices) {
+    const float q = __int_as_float(0x7fffffff);
+    for (int k = 0; k < 3; ++k) {
+        if (last_nan[k] == num_vertices - 1) b.mm[k] = b.xx[k] = q;
+        if (last_nan[3 + k] == num_vertices - 1) b.pm[k] = b.px[k] = q;
+    }
 }
 
 }  // namespace

@@ -38,6 +38,7 @@ struct Shared {
     float six_volume;
     float delta[3];
     uint4 ring_desc[4];
+    int last_nan[6];
     float red[32][4];  // per-warp partials for reductions
     int redi[32][4];
 };
@@ -83,7 +84,7 @@ __device__ __forceinline__ void tape_inputs(const float4 *sx, uint4 r, int type,
     }
 }
 
-template <int T, bool kTape>
+template <int T, bool kTape, bool kGuard>
 __device__ __forceinline__ void apply_levels(float4 *sx, const BodyDesc &d, float inv_dt_sq, const LevelRing &ring,
                                              float4 *tape_cons) {
     const uint4 *__restrict__ levels = d.levels;
@@ -116,7 +117,7 @@ __device__ __forceinline__ void apply_levels(float4 *sx, const BodyDesc &d, floa
             const uint4 r = src[s];
             if (r.x != 0xffffffffu) {
                 if (kTape) tape_inputs(sx, r, slot_type(lv, s), tape_cons + size_t(lv.x + s) * 3);
-                project(sx, r, slot_type(lv, s), inv_dt_sq);
+                project<kGuard>(sx, r, slot_type(lv, s), inv_dt_sq);
             }
         }
         if (ahead <= L) ring_stage<T>(ring, levels, rec, ahead, L, lv_ahead, next_ahead);
@@ -255,6 +256,7 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
             __syncthreads();
         }
         // IntegratePositions
+        bool nan_seen = false;
         for (uint32_t i = tid; i < nv; i += T) {
             float4 pi = sx[i];
             float4 vel = kSmemState ? sv[i] : gv[i];
@@ -270,13 +272,17 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
                 gprev[i] = pi;
                 gv[i] = with_w(v, vel.w);
             }
-            sx[i] = with_w(xyz(pi) + v * dt_sub, pi.w);
+            const f3 xn = xyz(pi) + v * dt_sub;
+            nan_seen = nan_seen || has_nan(xn);
+            sx[i] = with_w(xn, pi.w);
             if (kTape) tape_state[nv + i] = with_w(v, 0.0f);
         }
-        __syncthreads();
-        // Update groups in dependency-level order
-        apply_levels<T, kTape>(sx, d, inv_dt_sq, ring,
-                               kTape ? td.cons + (size_t(p.tape_step) * n_it + it) * size_t(td.slots) * 3 : nullptr);
+        // Update groups in dependency-level order (NaN-guarded projections for a body holding NaNs)
+        float4 *cons = kTape ? td.cons + (size_t(p.tape_step) * n_it + it) * size_t(td.slots) * 3 : nullptr;
+        if (__syncthreads_or(nan_seen))
+            apply_levels<T, kTape, true>(sx, d, inv_dt_sq, ring, cons);
+        else
+            apply_levels<T, kTape, false>(sx, d, inv_dt_sq, ring, cons);
         __syncthreads();
         if (kTape)
             for (uint32_t i = tid; i < nv; i += T) tape_state[2 * nv + i] = sx[i];
@@ -303,14 +309,9 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
 
     // UpdateSoftBodyState
     const float max_sq = d.max_linear_velocity * d.max_linear_velocity;
-    float mm[4] = {FLT_MAX, FLT_MAX, FLT_MAX, 0};
-    int mi[4] = {-1, -1, -1, -1};
-    float xx[4] = {-FLT_MAX, -FLT_MAX, -FLT_MAX, 0};
-    int xi[4] = {-1, -1, -1, -1};
-    float pm[4] = {FLT_MAX, FLT_MAX, FLT_MAX, 0};
-    int pmi[4] = {-1, -1, -1, -1};
-    float px[4] = {-FLT_MAX, -FLT_MAX, -FLT_MAX, 0};
-    int pxi[4] = {-1, -1, -1, -1};
+    const int all[6] = {-1, -1, -1, -1, -1, -1};
+    Bounds bd;
+    bounds_init(bd);
     f3 lin = mk(0, 0, 0), ang = mk(0, 0, 0);
     bool finite = true;
     for (uint32_t i = tid; i < nv; i += T) {
@@ -323,28 +324,25 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
         lin = lin + v;
         ang = ang + cross(x, v);
         f3 pred = (x + v * dt) + disp_g;
-        pick_min(mm[0], mi[0], x.x, int(i));
-        pick_min(mm[1], mi[1], x.y, int(i));
-        pick_min(mm[2], mi[2], x.z, int(i));
-        pick_max(xx[0], xi[0], x.x, int(i));
-        pick_max(xx[1], xi[1], x.y, int(i));
-        pick_max(xx[2], xi[2], x.z, int(i));
-        pick_min(pm[0], pmi[0], pred.x, int(i));
-        pick_min(pm[1], pmi[1], pred.y, int(i));
-        pick_min(pm[2], pmi[2], pred.z, int(i));
-        pick_max(px[0], pxi[0], pred.x, int(i));
-        pick_max(px[1], pxi[1], pred.y, int(i));
-        pick_max(px[2], pxi[2], pred.z, int(i));
+        bounds_add(bd, x, pred, int(i), all);
         finite = finite && isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
     }
     if (!finite) atomicOr(p.error, kErrNonFinite);
-    {
-        const bool mins[4] = {false, false, false, false};
-        const bool maxs[4] = {true, true, true, true};
-        reduce_minmax4<T>(sh, mm, mi, mins);
-        reduce_minmax4<T>(sh, xx, xi, maxs);
-        reduce_minmax4<T>(sh, pm, pmi, mins);
-        reduce_minmax4<T>(sh, px, pxi, maxs);
+    if (__syncthreads_or(!finite)) {
+        // NaN components: extremes over the vertices after the last NaN (the reference's sequential
+        // _mm_min_ps / _mm_max_ps semantics)
+        reduce_last_nan<T>(bd.last_nan, sh.last_nan);
+        int skip[6];
+        for (int k = 0; k < 6; ++k) skip[k] = sh.last_nan[k];
+        bounds_init(bd);
+        for (uint32_t i = tid; i < nv; i += T) {
+            const f3 x = xyz(sx[i]), v = xyz(gv[i]);
+            bounds_add(bd, x, (x + v * dt) + disp_g, int(i), skip);
+        }
+        bounds_reduce<T>(sh, bd);
+        bounds_nan_tail(bd, skip, int(nv));
+    } else {
+        bounds_reduce<T>(sh, bd);
     }
     float sums[6];
     sums[0] = reduce_sum<T>(sh, lin.x, 0);
@@ -354,8 +352,8 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     sums[4] = reduce_sum<T>(sh, ang.y, 0);
     sums[5] = reduce_sum<T>(sh, ang.z, 1);
     if (tid == 0) {
-        const f3 delta = finish_body_state(st, d, body_pos, mk(mm[0], mm[1], mm[2]), mk(xx[0], xx[1], xx[2]),
-                                           mk(pm[0], pm[1], pm[2]), mk(px[0], px[1], px[2]), sums, nvf);
+        const f3 delta = finish_body_state(st, d, body_pos, mk(bd.mm[0], bd.mm[1], bd.mm[2]), mk(bd.xx[0], bd.xx[1], bd.xx[2]),
+                                           mk(bd.pm[0], bd.pm[1], bd.pm[2]), mk(bd.px[0], bd.px[1], bd.px[2]), sums, nvf);
         st3(sh.delta, delta);
     }
     __syncthreads();

@@ -714,6 +714,18 @@ const char *oracle_last_error(void *w) { return static_cast<Handle *>(w)->err.c_
 
 // FP64 parameter setters for central finite differences (double world only): initial local positions
 // and velocities (3 doubles per vertex, may be NULL), per-constraint compliance, force.
+// Overwrites the local positions and velocities of a body of the float world (3 floats per vertex each,
+// either may be NULL).
+int oracle_set_state(void *w, int body, const float *pos3, const float *vel3) {
+    Handle *h = static_cast<Handle *>(w);
+    auto &b = h->wf.bodies[body];
+    for (size_t i = 0; i < b.v.size(); ++i) {
+        if (pos3) b.v[i].pos = b.v[i].prev = {pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2]};
+        if (vel3) b.v[i].vel = {vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2]};
+    }
+    return 0;
+}
+
 int oracle_set_state_f64(void *w, int body, const double *pos3, const double *vel3) {
     Handle *h = static_cast<Handle *>(w);
     auto &b = h->wd.bodies[body];

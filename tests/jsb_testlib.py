@@ -177,6 +177,7 @@ class Oracle:
                                           ctypes.c_void_p]
             L.oracle_get_world_positions_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
             L.oracle_set_state_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+            L.oracle_set_state.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
             L.oracle_set_compliance_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                                     ctypes.c_void_p, ctypes.c_int]
             L.oracle_set_force_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
@@ -216,6 +217,12 @@ class Oracle:
                 if any(f != 0.0 for f in b.force):
                     L.oracle_set_force(self.h, i, (ctypes.c_float * 3)(*b.force))
             L.oracle_step(self.h, self.scene.dt, self.scene.collision_steps)
+
+    def set_state(self, i: int, local_positions, velocities):
+        """Local positions and velocities (N, 3) of body i (float world)."""
+        p = np.ascontiguousarray(local_positions, np.float32)
+        v = np.ascontiguousarray(velocities, np.float32)
+        self.lib().oracle_set_state(self.h, i, p.ctypes.data, v.ctypes.data)
 
     def body(self, i: int):
         n = self.nv[i]

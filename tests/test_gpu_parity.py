@@ -188,3 +188,48 @@ def test_nonfinite_state_reported(jsb):
     with pytest.raises(jsb.JsbError) as e:
         a.synchronize()
     assert e.value.status == 7
+
+
+@pytest.mark.parametrize("path", ["one_cta", "cluster"])
+def test_nan_propagation_matches_oracle(jsb, path):
+    """A body holding NaN positions (as a body that has blown up does) keeps being stepped: the vertices
+    that become NaN are those that become NaN in the reference's arithmetic (NaN-guarded projections),
+    and the other bodies are untouched, bit for bit."""
+    scene_bytes = jsb.build_scene("uneven_batch", n_cloth=4, n_cube=0, cloth_max=24, steps=3, seed=9)
+    scene, _ = parse_scene(scene_bytes)
+    ctx = make_ctx(jsb, scene_bytes)
+    if path == "cluster":
+        for mv, t, _ in ctx.bucket_table():
+            ctx.set_bucket_config(mv, t, 2)
+    n = ctx.total_vertices()
+    pos = np.zeros((n, 3), np.float32)
+    vel = np.zeros((n, 3), np.float32)
+    ctx.download_all(pos, vel)
+    ctx.synchronize()
+    nv = [b.num_vertices for b in scene.bodies]
+    poisoned = 0  # a cloth: a few vertices in its interior
+    off = 0
+    idx = [nv[poisoned] // 2, nv[poisoned] // 2 + 1, nv[poisoned] // 3]
+    pos[[off + i for i in idx], 1] = np.nan
+    ctx.upload_all(pos, vel)
+    o = Oracle(scene)
+    offs = np.concatenate([[0], np.cumsum(nv)])
+    for b in range(len(nv)):
+        o.set_state(b, pos[offs[b]:offs[b + 1]], vel[offs[b]:offs[b + 1]])
+    for step in range(3):
+        o.step(1)
+        ctx.step()
+        with pytest.raises(jsb.JsbError):
+            ctx.synchronize()
+        snap = snapshot(ctx)
+        for b in range(len(nv)):
+            ref = o.body(b)
+            if b == poisoned:
+                gm, rm = np.isnan(snap[b][1]), np.isnan(ref[1])
+                assert np.array_equal(gm, rm), (step, int(gm.sum()), int(rm.sum()), np.isnan(snap[b][0]), np.isnan(ref[0]),
+                                                 np.argwhere(gm != rm)[:6].tolist(), int(np.isnan(snap[b][2]).sum()),
+                                                 int(np.isnan(ref[2]).sum()))
+                assert gm.any()
+            else:
+                for k in range(3):
+                    assert np.array_equal(snap[b][k], ref[k]), (b, k)
