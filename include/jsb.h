@@ -171,8 +171,9 @@ jsb_status jsb_set_cluster_config(jsb_context *ctx, uint32_t cluster_size, uint3
 jsb_status jsb_get_cluster_config(jsb_context *ctx, uint32_t *cluster_size, uint32_t *threads, uint32_t *num_bodies);
 jsb_status jsb_get_bucket_config(jsb_context *ctx, uint32_t index, uint32_t *max_vertices, uint32_t *threads,
                                  uint32_t *state_mode);
-/* Tunes the bucket table on the context's own bodies (coordinate descent, each shape timed as a
- * whole batched step); the bodies' state is restored afterwards. */
+/* Tunes the bucket table on the context's own bodies: a few uniform starting tables, then up to two
+ * rounds of coordinate descent over each occupied bucket's (threads, state placement), every candidate
+ * timed as whole batched steps from the same state; the bodies' state is restored afterwards. */
 jsb_status jsb_autotune(jsb_context *ctx, float dt, int trials);
 
 /* Kernel launches issued by the most recent jsb_step / jsb_step_plain / jsb_step_graph call. */

@@ -1218,24 +1218,59 @@ jsb_status jsb_autotune(jsb_context *ctx, float dt, int trials) {
             }
     float best_ms = 0.0f;
     st = measure(best_ms);
-    const int choices[4] = {32, 64, 128, 256};
-    for (auto it = occupied.rbegin(); st == JSB_OK && it != occupied.rend(); ++it) {
-        Bucket &bk = ctx->buckets[*it];
-        Bucket best = bk;
-        for (int mode = 0; mode < 2 && st == JSB_OK; ++mode)
-            for (int t : choices) {
-                if (t == best.threads && mode == best.state_mode) continue;
-                bk.threads = t;
-                bk.state_mode = mode;
-                float ms = 0.0f;
-                st = measure(ms);
-                if (st != JSB_OK) break;
-                if (ms < best_ms) {
-                    best_ms = ms;
-                    best = bk;
+    // Starting points: the current table and a few uniform ones (buckets interact through SM sharing,
+    // so coordinate descent from a single start can stall in a poor local optimum).
+    {
+        const std::vector<Bucket> current = ctx->buckets;
+        std::vector<Bucket> best_table = current;
+        for (int variant = 0; variant < 4 && st == JSB_OK; ++variant) {
+            std::vector<Bucket> t = current;
+            for (Bucket &b : t) {
+                if (b.state_mode == 2) continue;
+                const bool large = b.max_vertices >= 1024;
+                switch (variant) {
+                    case 0: b.state_mode = 1; break;  // positions only in shared memory: more CTAs per SM
+                    case 1: b.state_mode = 1, b.threads = large ? 128 : 32; break;
+                    case 2: b.state_mode = 1, b.threads = large ? 256 : 64; break;
+                    default: b.state_mode = 0, b.threads = large ? 128 : 32; break;
                 }
             }
-        bk = best;
+            ctx->buckets = t;
+            float ms = 0.0f;
+            st = measure(ms);
+            if (st == JSB_OK && ms < best_ms) {
+                best_ms = ms;
+                best_table = t;
+            }
+        }
+        ctx->buckets = best_table;
+    }
+    // Coordinate descent over each occupied bucket's (threads, state placement), largest bucket first,
+    // for up to two rounds.
+    const int choices[4] = {32, 64, 128, 256};
+    for (int round = 0; round < 2 && st == JSB_OK; ++round) {
+        bool improved = false;
+        for (auto it = occupied.rbegin(); st == JSB_OK && it != occupied.rend(); ++it) {
+            Bucket &bk = ctx->buckets[*it];
+            if (bk.state_mode == 2) continue;
+            Bucket best = bk;
+            for (int mode = 0; mode < 2 && st == JSB_OK; ++mode)
+                for (int t : choices) {
+                    if (t == best.threads && mode == best.state_mode) continue;
+                    bk.threads = t;
+                    bk.state_mode = mode;
+                    float ms = 0.0f;
+                    st = measure(ms);
+                    if (st != JSB_OK) break;
+                    if (ms < best_ms) {
+                        best_ms = ms;
+                        best = bk;
+                        improved = true;
+                    }
+                }
+            bk = best;
+        }
+        if (!improved) break;
     }
     cudaStreamDestroy(stream);
     JSB_CUDA(cudaMemcpy(ctx->x.ptr, sx.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice));
