@@ -90,3 +90,14 @@ def test_pressurised_body_rejected_on_cluster_path(jsb):
     with pytest.raises(jsb.JsbError) as e:
         ctx.step()
     assert e.value.status == jsb.JSB_ERR_UNSUPPORTED
+
+
+def test_cluster_config_validation(jsb):
+    ctx = jsb.Context(0)
+    for size, threads in ((3, 256), (32, 256), (8, 64), (8, 1024)):
+        with pytest.raises(jsb.JsbError) as e:
+            ctx.set_cluster_config(size, threads)
+        assert e.value.status == jsb.JSB_ERR_INVALID_ARGUMENT
+    ctx.set_cluster_config(0, 512)
+    assert ctx.cluster_config() == {"cluster_size": 0, "threads": 512, "bodies": 0}
+    ctx.close()
