@@ -320,6 +320,85 @@ def bench_large_body(jsb, torch, stream, steps: int, with_cpu: bool) -> dict:
     return out
 
 
+def bench_pinned_cloth(jsb, torch, stream, with_cpu: bool) -> dict:
+    """The plain single cloth (30 x 30 vertices, 0.75 m spacing, two far corners pinned, edge / shear
+    compliance 1e-5, dihedral bends 1e-4, 5 iterations, no colliders): its 300-step run as one CUDA
+    graph, device-timed, and the oracle on one thread for the same run."""
+    scene_bytes = jsb.build_scene("pinned_cloth")
+    ctx = jsb.Context(0)
+    ctx.load_scene(scene_bytes)
+    sptr = stream.cuda_stream
+    steps = ctx.scene_steps
+    vi = ctx.total_vertices() * 5 * steps
+    initial = ctx.save_all()
+    with torch.cuda.stream(stream):
+        ctx.step_graph(steps, 1, stream=sptr)
+    torch.cuda.synchronize()
+    ctx.restore_all(initial)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        ctx.step_graph(steps, 1, stream=sptr)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    ctx.close()
+    out = {"workload": "pinned_cloth 30x30", "steps": steps, "ms_per_step": ms / steps, "value": vi / (ms / 1000.0),
+           "unit": UNIT, "timing": "the whole run as one CUDA graph replay"}
+    if with_cpu:
+        from jsb_testlib import Oracle, parse_scene
+
+        scene, _ = parse_scene(scene_bytes)
+        o = Oracle(scene)
+        t0 = time.perf_counter()
+        o.step(steps)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": vi / dt, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"the {steps}-step run"}
+    return out
+
+
+def bench_diff_cloth(jsb, steps: int = 120, every: int = 10) -> dict:
+    """The differentiable single cloth (64 x 64, 0.05 m spacing, top row pinned, per-edge compliance
+    log-U[1e-6, 1e-4], v0 N(0, 0.1)): forward + adjoint of the 120-step run with checkpoints every 10
+    steps and the loss at steps 60 and 120, against the forward alone (host clock, synchronised)."""
+    ctx = jsb.Context(0)
+    ctx.load_scene(jsb.build_scene("diff_cloth"))
+    init = ctx.save_all()
+    n = ctx.total_vertices()
+    rng = np.random.default_rng(3)
+    seed = rng.standard_normal((n, 3)).astype(np.float32) * 1e-3
+
+    def forward():
+        ctx.restore_all(init)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        ctx.step_graph(steps, 1)
+        ctx.synchronize()
+        return time.perf_counter() - t0
+
+    def forward_adjoint():
+        ctx.restore_all(init)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        ctx.adjoint_begin(steps, every)
+        ctx.adjoint_forward()
+        ctx.adjoint_seed_all(steps // 2, seed)
+        ctx.adjoint_seed_all(steps, seed)
+        ctx.adjoint_backward()
+        ctx.adjoint_gradients(0, num_edges=ctx.bodies[0]["num_edges"])
+        ctx.adjoint_end()
+        ctx.synchronize()
+        return time.perf_counter() - t0
+
+    forward()
+    t_fwd = forward()
+    forward_adjoint()
+    t_adj = forward_adjoint()
+    ctx.close()
+    return {"workload": "diff_cloth 64x64", "steps": steps, "checkpoint_every": every, "forward_s": t_fwd,
+            "forward_adjoint_s": t_adj, "ratio": t_adj / t_fwd, "target_ratio": 4.0}
+
+
 def profile_driver(args) -> None:
     """A bare step loop of one workload for ncu captures (warm-up steps, then the captured steps):
     uneven_batch and large_cloth run batched steps on the default stream; diff_batch_adjoint runs a
@@ -555,6 +634,8 @@ def main():
     if not args.no_extras:
         line["adjoint"] = bench_adjoint(jsb, sptr)
         line["large_body"] = bench_large_body(jsb, torch, stream, args.large_steps, not args.no_cpu_baseline)
+        line["pinned_cloth"] = bench_pinned_cloth(jsb, torch, stream, not args.no_cpu_baseline)
+        line["diff_cloth_adjoint"] = bench_diff_cloth(jsb)
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
