@@ -154,6 +154,16 @@ jsb_status jsb_body_schedule_info(jsb_context *ctx, uint32_t body_id, uint32_t *
 jsb_status jsb_settings_schedule(const void *blob, size_t len, uint32_t *num_levels, uint32_t *num_records,
                                  uint32_t *levels, uint32_t *records, uint32_t *source);
 
+/* Host only: the whole-step schedule (see jsb_set_step_walk) of these settings for `num_iterations`
+ * substeps, in the padded device layout. levels receives 4 x num_levels uint32 {first slot, bend end |
+ * volume end << 16, edge end | LRA end << 16, slots of the level} (ends relative to the first slot;
+ * vertex slots from the LRA end on), records 4 x num_slots uint32 (padding slots have 0xffffffff in
+ * their first word; a vertex slot is {vertex index, 0, 0, 0}), source 2 x num_slots uint32 {type << 28 |
+ * index, substep} (type 0 bend, 1 volume, 2 edge, 3 LRA, 4 vertex; 0xffffffff for padding). Sizes are
+ * 0 when the settings have no whole-step schedule (num_iterations < 2, or a level of 65,536 slots or
+ * more). Pass NULL arrays to query the sizes. */
+jsb_status jsb_settings_step_schedule(const void *blob, size_t len, uint32_t num_iterations, uint32_t *num_levels,
+                                      uint32_t *num_slots, uint32_t *levels, uint32_t *records, uint32_t *source);
 /* Launch shape of the size bucket of bodies with vertex count <= max_vertices (and above the next
  * smaller bucket): threads per CTA in {32, 64, 128, 256}; state_mode 0 keeps positions, velocities and
  * previous positions in shared memory when they fit, 1 keeps only positions there, 2 sends the
@@ -168,6 +178,13 @@ jsb_status jsb_set_bucket_threads(jsb_context *ctx, uint32_t max_vertices, uint3
  * and threads per CTA in {128, 256, 512}. The getter reports the shape in use after the launch groups
  * are built, and how many bodies take the path. */
 jsb_status jsb_set_cluster_config(jsb_context *ctx, uint32_t cluster_size, uint32_t threads);
+/* Whole-step walk (no counterpart in the reference; on by default): a body without pressure on the
+ * one-CTA path walks one dependency-level schedule for its whole step, in which each vertex takes the
+ * velocity update of the substep it leaves and the integration of the next one right after its own last
+ * constraint (ApplyCollisionConstraintsAndUpdateVelocities and IntegratePositions are per-vertex passes,
+ * SoftBodyMotionProperties.cpp:325-365, 700-825), so substeps overlap. Results are bitwise those of the
+ * per-substep walk (enable = 0), which pressurised bodies, differentiable runs and the cluster path keep. */
+jsb_status jsb_set_step_walk(jsb_context *ctx, int enable);
 jsb_status jsb_get_cluster_config(jsb_context *ctx, uint32_t *cluster_size, uint32_t *threads, uint32_t *num_bodies);
 jsb_status jsb_get_bucket_config(jsb_context *ctx, uint32_t index, uint32_t *max_vertices, uint32_t *threads,
                                  uint32_t *state_mode);

@@ -55,6 +55,9 @@ SIGNATURES = {
     "jsb_set_bucket_threads": [_P, _c.c_uint32, _c.c_uint32],
     "jsb_get_bucket_config": [_P, _c.c_uint32, _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32)],
     "jsb_set_cluster_config": [_P, _c.c_uint32, _c.c_uint32],
+    "jsb_set_step_walk": [_P, _c.c_int],
+    "jsb_settings_step_schedule": [_c.c_char_p, _c.c_size_t, _c.c_uint32, _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32), _P,
+                                   _P, _P],
     "jsb_get_cluster_config": [_P, _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint32)],
     "jsb_autotune": [_P, _c.c_float, _c.c_int],
     "jsb_last_launch_count": [_P, _c.POINTER(_c.c_uint32)],
@@ -143,6 +146,21 @@ def settings_schedule(blob: bytes):
     source = np.zeros(nr.value, np.uint32)
     check(lib().jsb_settings_schedule(blob, len(blob), ctypes.byref(nl), ctypes.byref(nr), levels.ctypes.data,
                                       records.ctypes.data, source.ctypes.data))
+    return levels, records, source
+
+
+def settings_step_schedule(blob: bytes, num_iterations: int):
+    """Whole-step schedule for settings bytes (host only): (levels (L, 4), records (S, 4), source (S, 2)),
+    or None when the settings have none."""
+    nl, ns = ctypes.c_uint32(), ctypes.c_uint32()
+    check(lib().jsb_settings_step_schedule(blob, len(blob), num_iterations, ctypes.byref(nl), ctypes.byref(ns), None, None, None))
+    if nl.value == 0:
+        return None
+    levels = np.zeros((nl.value, 4), np.uint32)
+    records = np.zeros((ns.value, 4), np.uint32)
+    source = np.zeros((ns.value, 2), np.uint32)
+    check(lib().jsb_settings_step_schedule(blob, len(blob), num_iterations, ctypes.byref(nl), ctypes.byref(ns),
+                                           levels.ctypes.data, records.ctypes.data, source.ctypes.data))
     return levels, records, source
 
 
@@ -269,6 +287,10 @@ class Context:
     def set_cluster_config(self, cluster_size: int = 0, threads: int = 256):
         """Shape of the thread-block-cluster path (cluster_size 0 = largest that fits)."""
         check(lib().jsb_set_cluster_config(self.h, cluster_size, threads))
+
+    def set_step_walk(self, enable: bool):
+        """Whole-step walk for bodies without pressure (default on); off walks every substep separately."""
+        check(lib().jsb_set_step_walk(self.h, 1 if enable else 0))
 
     def cluster_config(self) -> dict:
         c, t, n = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()

@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -111,12 +112,19 @@ struct DevBuf {
     }
 };
 
+// Whole-step schedule of one settings object for one iteration count (bodies without pressure).
+struct StepSchedRec {
+    StepSchedule sched;
+    DevBuf<uint4> levels, records;
+};
+
 struct SettingsRec {
     ParsedSettings parsed;
     Schedule schedule;
     std::vector<uint32_t> vf_off, vf;
     DevBuf<uint4> levels, records, faces;
     DevBuf<uint32_t> vf_off_dev, vf_dev;
+    std::map<uint32_t, std::unique_ptr<StepSchedRec>> steps;  // by iteration count; null: none (a level too wide)
 };
 
 struct BodyRec {
@@ -211,6 +219,7 @@ struct jsb_context {
     std::vector<jsb::Bucket> buckets;
     int cluster_size = 0;       // CTAs per cluster on the cluster path, 0 = largest that fits
     int cluster_threads = 256;  // threads per CTA on the cluster path
+    bool step_walk = true;  // walk whole-step schedules where a body has one (jsb_set_step_walk)
     // device state
     bool dirty = true;  // structure changed: device arrays must be rebuilt
     bool groups_dirty = true;  // bucket table changed: launch groups must be rebuilt
@@ -267,6 +276,35 @@ size_t bucket_for(const jsb_context *ctx, uint32_t nv) {
     return ctx->buckets.size() - 1;
 }
 
+// The whole-step schedule body b walks, or null (pressure, a single iteration, the walk switched off,
+// or a schedule level too wide for the 16-bit level descriptor).
+const StepSchedRec *step_sched(const jsb_context *ctx, const BodyRec &b) {
+    if (!ctx->step_walk || b.creation.pressure > 0.0f) return nullptr;
+    const SettingsRec &s = *ctx->settings[b.settings_id];
+    auto it = s.steps.find(b.creation.num_iterations);
+    return it == s.steps.end() ? nullptr : it->second.get();
+}
+
+// Builds and uploads the whole-step schedules the bodies need (once per settings and iteration count).
+jsb_status ensure_step_schedules(jsb_context *ctx) {
+    if (!ctx->step_walk) return JSB_OK;
+    for (const BodyRec &b : ctx->bodies) {
+        if (b.creation.pressure > 0.0f || b.creation.num_iterations < 2) continue;
+        SettingsRec &s = *ctx->settings[b.settings_id];
+        if (s.steps.count(b.creation.num_iterations)) continue;
+        auto rec = std::make_unique<StepSchedRec>();
+        if (build_step_schedule(s.parsed, b.creation.num_iterations, rec->sched)) {
+            JSB_CUDA(rec->levels.upload(reinterpret_cast<const uint4 *>(rec->sched.levels.data()), rec->sched.levels.size() / 4));
+            JSB_CUDA(rec->records.upload(reinterpret_cast<const uint4 *>(rec->sched.records.data()), rec->sched.records.size() / 4));
+            std::vector<uint32_t>().swap(rec->sched.records);  // the device copy is the one used
+        } else {
+            rec.reset();
+        }
+        s.steps[b.creation.num_iterations] = std::move(rec);
+    }
+    return JSB_OK;
+}
+
 BodyDesc make_desc(const jsb_context *ctx, const BodyRec &b) {
     const SettingsRec &s = *ctx->settings[b.settings_id];
     BodyDesc d;
@@ -277,6 +315,10 @@ BodyDesc make_desc(const jsb_context *ctx, const BodyRec &b) {
     d.vf = s.vf_dev.ptr;
     d.num_levels = s.schedule.num_levels;
     d.num_records = s.schedule.num_slots;
+    const StepSchedRec *ss = step_sched(ctx, b);
+    d.step_levels = ss ? ss->levels.ptr : nullptr;
+    d.step_records = ss ? ss->records.ptr : nullptr;
+    d.num_step_levels = ss ? ss->sched.num_levels : 0u;
     d.num_faces = uint32_t(s.parsed.faces.size());
     d.num_vertices = uint32_t(s.parsed.vertices.size());
     d.vtx_offset = b.vtx_offset;
@@ -301,19 +343,36 @@ uint32_t pressure_faces(const SettingsRec &s, const BodyRec &b) {
 constexpr uint32_t kMaxRingSlots = 256;
 constexpr uint32_t kMaxCachedLevels = 4096;  // level descriptors a cluster CTA keeps in shared memory
 
+constexpr uint32_t kMaxStepRingSlots = 512;  // whole-step levels are wider (slots beyond the ring are read in place)
+
 uint32_t ring_slots_for(const SettingsRec &s) {
     uint32_t r = (s.schedule.max_level_slots + 31u) & ~31u;
     return std::max<uint32_t>(32u, std::min(r, kMaxRingSlots));
 }
 
-double body_cost(const SettingsRec &s, const BodyRec &b, int threads) {
+// Record ring capacity for body b: its whole-step schedule's widest level when it walks one.
+uint32_t ring_slots_for(const jsb_context *ctx, const BodyRec &b) {
+    const SettingsRec &s = *ctx->settings[b.settings_id];
+    const StepSchedRec *ss = step_sched(ctx, b);
+    if (!ss) return ring_slots_for(s);
+    uint32_t r = (ss->sched.max_level_slots + 31u) & ~31u;
+    return std::max<uint32_t>(32u, std::min(r, kMaxStepRingSlots));
+}
+
+double body_cost(const jsb_context *ctx, const BodyRec &b, int threads) {
+    const SettingsRec &s = *ctx->settings[b.settings_id];
+    double per_vertex = double(s.parsed.vertices.size()) / threads;
     double levels = 0;
+    if (const StepSchedRec *ss = step_sched(ctx, b)) {
+        const auto &lv = ss->sched.levels;
+        for (uint32_t l = 0; l < ss->sched.num_levels; ++l) levels += double((lv[l * 4 + 3] + threads - 1) / threads);
+        return levels + 6.0 * per_vertex;
+    }
     const auto &lv = s.schedule.levels;
     for (uint32_t l = 0; l < s.schedule.num_levels; ++l) {
         uint32_t w = lv[(l + 1) * 4] - lv[l * 4];
         levels += double((w + threads - 1) / threads);
     }
-    double per_vertex = double(s.parsed.vertices.size()) / threads;
     return double(b.creation.num_iterations) * (levels + 4.0 * per_vertex);
 }
 
@@ -360,6 +419,8 @@ jsb_status rebuild(jsb_context *ctx) {
     JSB_CUDA(ctx->plane.alloc(total));
     JSB_CUDA(ctx->shape.alloc(total));
     ctx->total_vertices = total;
+    jsb_status sst = ensure_step_schedules(ctx);
+    if (sst != JSB_OK) return sst;
     std::vector<BodyDesc> descs;
     for (const BodyRec &b : ctx->bodies) descs.push_back(make_desc(ctx, b));
     JSB_CUDA(ctx->descs.upload(descs.data(), descs.size()));
@@ -448,7 +509,7 @@ jsb_status rebuild_groups(jsb_context *ctx) {
             cluster_bodies.push_back(uint32_t(bi));
             continue;
         }
-        members[k].push_back({body_cost(s, b, ctx->buckets[k].threads), uint32_t(bi)});
+        members[k].push_back({body_cost(ctx, b, ctx->buckets[k].threads), uint32_t(bi)});
     }
     for (size_t k = 0; k < ctx->buckets.size(); ++k) {
         if (members[k].empty()) continue;
@@ -460,8 +521,15 @@ jsb_status rebuild_groups(jsb_context *ctx) {
             const SettingsRec &s = *ctx->settings[b.settings_id];
             g.smem_vertices = std::max(g.smem_vertices, uint32_t(s.parsed.vertices.size()));
             g.smem_faces = std::max(g.smem_faces, pressure_faces(s, b));
-            g.ring_slots = std::max(g.ring_slots, ring_slots_for(s));
+            g.ring_slots = std::max(g.ring_slots, ring_slots_for(ctx, b));
         }
+        // A ring wider than the per-substep cap only serves whole-step walks: shrink it (down to that
+        // cap) before giving up shared-memory state.
+        if (ctx->buckets[k].state_mode == 0)
+            while (g.ring_slots > kMaxRingSlots && step_smem_bytes(true, g.smem_vertices, g.smem_faces, g.ring_slots) > cap)
+                g.ring_slots -= 32;
+        while (g.ring_slots > kMaxRingSlots && step_smem_bytes(false, g.smem_vertices, g.smem_faces, g.ring_slots) > cap)
+            g.ring_slots -= 32;
         g.smem_state = ctx->buckets[k].state_mode == 0 && step_smem_bytes(true, g.smem_vertices, g.smem_faces, g.ring_slots) <= cap;
         if (step_smem_bytes(g.smem_state, g.smem_vertices, g.smem_faces, g.ring_slots) > cap)
             return fail(JSB_ERR_UNSUPPORTED, "a body with " + std::to_string(g.smem_vertices) +
@@ -575,7 +643,7 @@ jsb_status step_impl(jsb_context *ctx, float dt, int collision_steps, cudaStream
                     p.num_work = 1;
                     p.queue = ctx->queues.ptr;
                     const SettingsRec &s = *ctx->settings[ctx->bodies[b].settings_id];
-                    p.ring_slots = ring_slots_for(s);
+                    p.ring_slots = g.cluster > 0 ? ring_slots_for(s) : std::min(ring_slots_for(ctx, ctx->bodies[b]), g.ring_slots);
                     if (g.cluster > 0)
                         JSB_CUDA(launch_cluster_step(p, g.cluster, g.threads, g.shift, g.desc_cap, g.rpt, stream));
                     else
@@ -1088,6 +1156,27 @@ jsb_status jsb_settings_schedule(const void *blob, size_t len, uint32_t *num_lev
     return JSB_OK;
 }
 
+jsb_status jsb_settings_step_schedule(const void *blob, size_t len, uint32_t num_iterations, uint32_t *num_levels,
+                                      uint32_t *num_slots, uint32_t *levels, uint32_t *records, uint32_t *source) {
+    if (!num_levels || !num_slots) return fail(JSB_ERR_INVALID_ARGUMENT, "null argument");
+    ParsedSettings ps;
+    bool unsupported = false;
+    std::string err = parse_settings(blob, len, ps, unsupported);
+    if (!err.empty()) return fail(unsupported ? JSB_ERR_UNSUPPORTED : JSB_ERR_BLOB, err);
+    StepSchedule s;
+    if (!build_step_schedule(ps, num_iterations, s, source != nullptr)) {
+        *num_levels = 0;
+        *num_slots = 0;
+        return JSB_OK;
+    }
+    *num_levels = s.num_levels;
+    *num_slots = s.num_slots;
+    if (levels) memcpy(levels, s.levels.data(), s.levels.size() * sizeof(uint32_t));
+    if (records) memcpy(records, s.records.data(), s.records.size() * sizeof(uint32_t));
+    if (source) memcpy(source, s.source.data(), s.source.size() * sizeof(uint32_t));
+    return JSB_OK;
+}
+
 jsb_status jsb_set_bucket_config(jsb_context *ctx, uint32_t max_vertices, uint32_t threads, uint32_t state_mode) {
     if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
     if (threads != 32 && threads != 64 && threads != 128 && threads != 256)
@@ -1115,6 +1204,14 @@ jsb_status jsb_set_cluster_config(jsb_context *ctx, uint32_t cluster_size, uint3
     ctx->cluster_size = int(cluster_size);
     ctx->cluster_threads = int(threads);
     ctx->groups_dirty = true;
+    return JSB_OK;
+}
+
+jsb_status jsb_set_step_walk(jsb_context *ctx, int enable) {
+    if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
+    if (ctx->step_walk == (enable != 0)) return JSB_OK;
+    ctx->step_walk = enable != 0;
+    ctx->dirty = true;  // body descriptors and launch groups change
     return JSB_OK;
 }
 
@@ -1303,6 +1400,13 @@ jsb_status jsb_body_set_compliance(jsb_context *ctx, uint32_t body_id, const flo
     s.schedule = build_schedule(s.parsed);  // same layout, new compliance words
     JSB_CUDA(cudaMemcpy(s.records.ptr, s.schedule.padded_records.data(), s.schedule.padded_records.size() * sizeof(uint32_t),
                         cudaMemcpyHostToDevice));
+    for (auto &kv : s.steps) {
+        if (!kv.second) continue;
+        StepSchedRec &r = *kv.second;
+        if (!build_step_schedule(s.parsed, kv.first, r.sched)) return fail(JSB_ERR_CAPACITY, "whole-step schedule rebuild failed");
+        JSB_CUDA(cudaMemcpy(r.records.ptr, r.sched.records.data(), r.sched.records.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        std::vector<uint32_t>().swap(r.sched.records);
+    }
     drop_graph(ctx);
     return JSB_OK;
 }

@@ -241,4 +241,133 @@ Schedule build_schedule(const ParsedSettings &s) {
     return out;
 }
 
+bool build_step_schedule(const ParsedSettings &s, uint32_t num_iterations, StepSchedule &out, bool with_source) {
+    out = StepSchedule();
+    if (num_iterations < 2) return false;
+    const uint32_t nv = uint32_t(s.vertices.size());
+    std::vector<int32_t> last_write(nv, -1), last_read(nv, -1);
+    struct Item {
+        uint32_t level, type, index, substep;
+    };
+    std::vector<Item> items;
+    uint32_t cur_substep = 0;
+    const size_t per_substep = s.edges.size() + s.bends.size() + s.volumes.size() + s.lras.size() + nv;
+    items.reserve(per_substep * num_iterations);
+    uint32_t max_level = 0;
+    auto place_rw = [&](const uint32_t *v, int k, uint32_t type, uint32_t index) {
+        int32_t lvl = 0;
+        for (int i = 0; i < k; ++i) lvl = std::max(lvl, std::max(last_write[v[i]], last_read[v[i]]) + 1);
+        for (int i = 0; i < k; ++i) last_write[v[i]] = lvl;
+        items.push_back({uint32_t(lvl), type, index, cur_substep});
+        max_level = std::max(max_level, uint32_t(lvl));
+    };
+    for (uint32_t it = 0; it < num_iterations; ++it) {
+        cur_substep = it;
+        if (it > 0)
+            for (uint32_t v = 0; v < nv; ++v) place_rw(&v, 1, kVertexOp, v);
+        ParsedSettings::Group start{0, 0, 0, 0, 0, 0, 0};
+        for (size_t g = 0; g < s.groups.size(); ++g) {
+            const ParsedSettings::Group &p = g > 0 ? s.groups[g - 1] : start;
+            const ParsedSettings::Group &c = s.groups[g];
+            for (uint32_t i = p.volume; i < c.volume; ++i) place_rw(s.volumes[i].v, 4, kVolume, i);
+            for (uint32_t i = p.bend; i < c.bend; ++i) place_rw(s.bends[i].v, 4, kBend, i);
+            for (uint32_t i = p.edge; i < c.edge; ++i) place_rw(s.edges[i].v, 2, kEdge, i);
+            for (uint32_t i = p.lra; i < c.lra; ++i) {
+                uint32_t a = s.lras[i].v[0], b = s.lras[i].v[1];
+                int32_t lvl = std::max(last_write[a] + 1, std::max(last_write[b], last_read[b]) + 1);
+                if (a == b) lvl = std::max(lvl, last_read[a] + 1);
+                last_read[a] = std::max(last_read[a], lvl);
+                last_write[b] = lvl;
+                items.push_back({uint32_t(lvl), kLRA, i, it});
+                max_level = std::max(max_level, uint32_t(lvl));
+            }
+        }
+    }
+    if (items.empty()) return false;
+    const uint32_t L = max_level + 1;
+    // per (level, type) counts, padded to multiples of 32 slots
+    std::vector<uint32_t> count(size_t(L) * 5, 0);
+    for (const Item &it : items) count[size_t(it.level) * 5 + it.type]++;
+    auto pad = [](uint32_t v) { return (v + 31u) & ~31u; };
+    std::vector<uint32_t> slot_of(size_t(L) * 5);  // next free slot of each (level, type)
+    out.levels.resize(size_t(L) * 4);
+    uint32_t slot = 0;
+    for (uint32_t l = 0; l < L; ++l) {
+        const uint32_t *c = &count[size_t(l) * 5];
+        const uint32_t be = pad(c[kBend]), ve = be + pad(c[kVolume]), ee = ve + pad(c[kEdge]), le = ee + pad(c[kLRA]);
+        const uint32_t total = le + pad(c[kVertexOp]);
+        if (total >= 65536u) {
+            out = StepSchedule();
+            return false;
+        }
+        out.levels[l * 4 + 0] = slot;
+        out.levels[l * 4 + 1] = be | (ve << 16);
+        out.levels[l * 4 + 2] = ee | (le << 16);
+        out.levels[l * 4 + 3] = total;
+        slot_of[size_t(l) * 5 + kBend] = slot;
+        slot_of[size_t(l) * 5 + kVolume] = slot + be;
+        slot_of[size_t(l) * 5 + kEdge] = slot + ve;
+        slot_of[size_t(l) * 5 + kLRA] = slot + ee;
+        slot_of[size_t(l) * 5 + kVertexOp] = slot + le;
+        out.max_level_slots = std::max(out.max_level_slots, total);
+        slot += total;
+    }
+    out.num_levels = L;
+    out.num_slots = slot;
+    out.num_iterations = num_iterations;
+    out.records.assign(size_t(slot) * 4, 0);
+    for (uint32_t k = 0; k < slot; ++k) out.records[size_t(k) * 4] = kPadRecord;
+    if (with_source) out.source.assign(size_t(slot) * 2, 0xffffffffu);
+    auto fbits = [](float f) {
+        uint32_t u;
+        memcpy(&u, &f, 4);
+        return u;
+    };
+    // items are in sequence order, so filling each (level, type) in that order keeps the in-level order
+    // of build_schedule
+    for (const Item &it : items) {
+        const uint32_t k = slot_of[size_t(it.level) * 5 + it.type]++;
+        uint32_t *r = &out.records[size_t(k) * 4];
+        if (with_source) {
+            out.source[size_t(k) * 2] = (it.type << 28) | it.index;
+            out.source[size_t(k) * 2 + 1] = it.substep;
+        }
+        switch (it.type) {
+            case kBend: {
+                const auto &b = s.bends[it.index];
+                r[0] = b.v[0] | (b.v[1] << 16);
+                r[1] = b.v[2] | (b.v[3] << 16);
+                r[2] = fbits(b.compliance);
+                r[3] = fbits(b.initial_angle);
+                break;
+            }
+            case kVolume: {
+                const auto &v = s.volumes[it.index];
+                r[0] = v.v[0] | (v.v[1] << 16);
+                r[1] = v.v[2] | (v.v[3] << 16);
+                r[2] = fbits(v.six_rest_volume);
+                r[3] = fbits(v.compliance);
+                break;
+            }
+            case kEdge: {
+                const auto &e = s.edges[it.index];
+                r[0] = e.v[0] | (e.v[1] << 16);
+                r[2] = fbits(e.rest);
+                r[3] = fbits(e.compliance);
+                break;
+            }
+            case kLRA: {
+                const auto &l = s.lras[it.index];
+                r[0] = l.v[0] | (l.v[1] << 16);
+                r[2] = fbits(l.max_distance);
+                break;
+            }
+            default:
+                r[0] = it.index;
+                break;
+        }
+    }
+    return true;
+}
+
 }  // namespace jsb

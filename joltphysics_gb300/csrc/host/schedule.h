@@ -85,4 +85,34 @@ constexpr uint32_t kPadRecord = 0xffffffffu;  // first word of a padding slot
 // level reproduces the sequential result bit for bit.
 Schedule build_schedule(const ParsedSettings &s);
 
+// Dependency-level schedule of a whole step of `num_iterations` substeps (bodies without pressure).
+//
+// Between the constraint projections of substep k - 1 and k the reference runs two per-vertex passes:
+// ApplyCollisionConstraintsAndUpdateVelocities (static colliders, SoftBodyMotionProperties.cpp:700-825)
+// and IntegratePositions (:325-365). Each reads and writes only its own vertex, so a vertex can take
+// both as soon as its own last constraint of substep k - 1 has been projected, and the next substep's
+// constraints on it can follow, while other vertices are still in substep k - 1. The schedule walks the
+// reference's whole sequence (substep 0 constraints, then per vertex "velocity update + integrate",
+// then substep 1 constraints, ...) with the same level rule as build_schedule, the per-vertex pair
+// being a fifth slot type on one vertex. Substep 0's integration and the last substep's velocity update
+// stay bulk passes around the walk. Only pressure couples all vertices between substeps (the volume is
+// a sum over every face), so pressurised bodies keep the per-substep walk.
+//   levels[l] = {first slot, bend end | volume end << 16, edge end | LRA end << 16, slots of the level}
+//   (ends relative to the first slot, each type padded to a multiple of 32 slots; vertex slots run from
+//   the LRA end to the level's slot count; a vertex slot's record is {vertex index, 0, 0, 0}).
+struct StepSchedule {
+    std::vector<uint32_t> levels;   // 4 per level
+    std::vector<uint32_t> records;  // 4 per slot
+    std::vector<uint32_t> source;   // 2 per slot when asked for: {type << 28 | index, substep}; padding 0xffffffff
+    uint32_t num_levels = 0;
+    uint32_t num_slots = 0;
+    uint32_t max_level_slots = 0;
+    uint32_t num_iterations = 0;
+};
+enum : uint32_t { kVertexOp = 4 };
+
+// Returns false (and leaves `out` empty) when a level holds 65,536 slots or more, or num_iterations < 2.
+// `with_source` also fills `source` (for tests of the order).
+bool build_step_schedule(const ParsedSettings &s, uint32_t num_iterations, StepSchedule &out, bool with_source = false);
+
 }  // namespace jsb

@@ -20,6 +20,9 @@
 //   volume {v0 | v1 << 16, v2 | v3 << 16, six rest volume, compliance}
 //   edge   {v0 | v1 << 16, 0, rest length, compliance}
 //   LRA    {v0 | v1 << 16, 0, max distance, 0}
+//   per (settings, iteration count), bodies without pressure:
+//     step_levels  uint4[num_step_levels]  whole-step dependency levels (host/schedule.h)
+//     step_records uint4[...]              the step's constraint records and per-vertex slots
 #pragma once
 
 #include <stdint.h>
@@ -52,6 +55,12 @@ struct BodyDesc {
     uint32_t num_records;
     uint32_t num_faces;
     uint32_t num_vertices;
+    // whole-step schedule for this body's iteration count (null: walk the per-substep schedule);
+    // levels {first slot, bend end | volume end << 16, edge end | LRA end << 16, slots}, vertex slots
+    // {vertex index, 0, 0, 0} from the LRA end on (see build_step_schedule)
+    const uint4 *step_levels;
+    const uint4 *step_records;
+    uint32_t num_step_levels;
     // body
     uint32_t vtx_offset;
     uint32_t num_iterations;

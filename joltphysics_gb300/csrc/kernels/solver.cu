@@ -128,6 +128,108 @@ __device__ __forceinline__ void apply_levels(float4 *sx, const BodyDesc &d, floa
     cp_async_wait<0>();
 }
 
+// ---------------------------------------------------------------------------------------------
+// Whole-step walk (bodies without pressure): the constraint levels of every substep and, between them,
+// each vertex's velocity update of the substep it leaves and integration of the substep it enters,
+// placed by the host right after the vertex's own last constraint (csrc/host/schedule.h,
+// build_step_schedule). Same reads and writes as the per-substep walk, so the same bits.
+// ---------------------------------------------------------------------------------------------
+struct VertexPass {
+    float4 *sv, *sprev;  // shared memory (kSmemState)
+    float4 *gv, *gprev;  // HBM (otherwise)
+    const int32_t *gshape;
+    const float4 *gplane;
+    const SCol *cols;
+    int ncols;
+    f3 sub_g, sub_imp;
+    float damp, dt_sub, radius, restitution_threshold;
+};
+
+// ApplyCollisionConstraintsAndUpdateVelocities (:700-825, static colliders) of the substep vertex i
+// leaves, then IntegratePositions (:325-365) of the substep it enters, for one vertex: the arithmetic
+// of the two bulk passes of step_body in the same order.
+template <bool kSmemState>
+__device__ __forceinline__ void vertex_between_substeps(float4 *sx, const VertexPass &vp, uint32_t i) {
+    float4 pi = sx[i];
+    float4 vel = kSmemState ? vp.sv[i] : vp.gv[i];
+    if (pi.w > 0.0f) {
+        const float4 prev = kSmemState ? vp.sprev[i] : vp.gprev[i];
+        f3 x = xyz(pi);
+        const f3 prev_v = xyz(vel);
+        f3 v = (x - xyz(prev)) / vp.dt_sub;
+        int shape = -1;
+        if (vp.ncols > 0) shape = kSmemState ? __float_as_int(vel.w) : vp.gshape[i];
+        if (shape >= 0 && collide_vertex(x, v, prev_v, vp.gplane[i], vp.cols[shape], vp.radius, vp.dt_sub, vp.restitution_threshold))
+            pi = with_w(x, pi.w);
+        v = v + (vp.sub_g + vp.sub_imp * pi.w);
+        v = v * vp.damp;
+        vel = with_w(v, vel.w);
+    }
+    if (kSmemState) {
+        vp.sprev[i] = pi;
+        vp.sv[i] = vel;
+    } else {
+        vp.gprev[i] = pi;
+        vp.gv[i] = vel;
+    }
+    sx[i] = with_w(xyz(pi) + xyz(vel) * vp.dt_sub, pi.w);
+}
+
+// Slot type of a whole-step level: 0 bend, 1 volume, 2 edge, 3 LRA, 4 vertex.
+__device__ __forceinline__ int step_slot_type(uint4 lv, uint32_t s) {
+    return s < (lv.y & 0xffffu) ? 0 : (s < (lv.y >> 16) ? 1 : (s < (lv.z & 0xffffu) ? 2 : (s < (lv.z >> 16) ? 3 : 4)));
+}
+
+// Stages the first ring.slots records of whole-step level `idx` and its descriptor; slots beyond the
+// ring's capacity are read in place by the walker.
+template <int T>
+__device__ __forceinline__ void step_ring_stage(const LevelRing &ring, const uint4 *__restrict__ rec, uint32_t idx, uint4 lv) {
+    const uint32_t pos = idx % kRingLevels;
+    const uint32_t n = lv.w < ring.slots ? lv.w : ring.slots;
+    for (uint32_t s = threadIdx.x; s < n; s += T) cp_async16(ring.rec + pos * ring.slots + s, rec + lv.x + s);
+    if (threadIdx.x == 0) ring.desc[pos] = lv;
+}
+
+template <int T, bool kSmemState, bool kGuard>
+__device__ __forceinline__ void apply_step_levels(float4 *sx, const BodyDesc &d, float inv_dt_sq, const LevelRing &ring,
+                                                  const VertexPass &vp) {
+    const uint4 *__restrict__ levels = d.step_levels;
+    const uint4 *__restrict__ rec = d.step_records;
+    const uint32_t tid = threadIdx.x;
+    const uint32_t L = d.num_step_levels;
+    if (L == 0) return;
+#pragma unroll
+    for (int k = 0; k < kRingDepth; ++k) {
+        if (uint32_t(k) < L) step_ring_stage<T>(ring, rec, k, __ldg(levels + k));
+        cp_async_commit();
+    }
+    cp_async_wait<kRingDepth - 1>();
+    __syncthreads();
+    for (uint32_t l = 0; l < L; ++l) {
+        const uint32_t ahead = l + kRingDepth;
+        uint4 lv_ahead = make_uint4(0, 0, 0, 0);
+        if (ahead < L) lv_ahead = __ldg(levels + ahead);
+        const uint32_t pos = l % kRingLevels;
+        const uint4 lv = ring.desc[pos];
+        const uint4 *ring_rec = ring.rec + pos * ring.slots;
+        for (uint32_t s = tid; s < lv.w; s += T) {
+            const uint4 r = s < ring.slots ? ring_rec[s] : __ldg(rec + lv.x + s);
+            if (r.x != 0xffffffffu) {
+                const int type = step_slot_type(lv, s);
+                if (type == 4)
+                    vertex_between_substeps<kSmemState>(sx, vp, r.x);
+                else
+                    project<kGuard>(sx, r, type, inv_dt_sq);
+            }
+        }
+        if (ahead < L) step_ring_stage<T>(ring, rec, ahead, lv_ahead);
+        cp_async_commit();
+        cp_async_wait<kRingDepth - 1>();
+        cta_sync<T>();
+    }
+    cp_async_wait<0>();
+}
+
 
 // ---------------------------------------------------------------------------------------------
 // One body, one step
@@ -211,8 +313,29 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     const f3 sub_imp = (force * dt_sub) / nvf;
     const float restitution_threshold = -2.0f * len(g) * dt_sub;
     const bool has_pressure = d.pressure > 0.0f && d.num_faces > 0;
+    // Whole-step walk: substep 0's integration below, then every substep's constraint levels with the
+    // per-vertex passes between substeps inside the walk, then the last substep's velocity update.
+    const bool step_walk = !kTape && d.step_levels != nullptr && !has_pressure;
+    VertexPass vp{};
+    if (step_walk) {
+        vp.sv = sv;
+        vp.sprev = sprev;
+        vp.gv = gv;
+        vp.gprev = gprev;
+        vp.gshape = gshape;
+        vp.gplane = gplane;
+        vp.cols = sh.cols;
+        vp.ncols = ncols;
+        vp.sub_g = sub_g;
+        vp.sub_imp = sub_imp;
+        vp.damp = damp;
+        vp.dt_sub = dt_sub;
+        vp.radius = d.vertex_radius;
+        vp.restitution_threshold = restitution_threshold;
+    }
+    const uint32_t passes = step_walk ? 1u : n_it;
 
-    for (uint32_t it = 0; it < n_it; ++it) {
+    for (uint32_t it = 0; it < passes; ++it) {
         float4 *tape_state = nullptr;
         if (kTape) {
             tape_state = td.state + (size_t(p.tape_step) * n_it + it) * 3 * nv;
@@ -279,7 +402,15 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
         }
         // Update groups in dependency-level order (NaN-guarded projections for a body holding NaNs)
         float4 *cons = kTape ? td.cons + (size_t(p.tape_step) * n_it + it) * size_t(td.slots) * 3 : nullptr;
-        if (__syncthreads_or(nan_seen))
+        const bool nan_any = __syncthreads_or(nan_seen);
+        if (!kTape && step_walk) {
+            // (a body that turns non-finite within the step finishes it on the unguarded walk: same
+            // result, slower)
+            if (nan_any)
+                apply_step_levels<T, kSmemState, true>(sx, d, inv_dt_sq, ring, vp);
+            else
+                apply_step_levels<T, kSmemState, false>(sx, d, inv_dt_sq, ring, vp);
+        } else if (nan_any)
             apply_levels<T, kTape, true>(sx, d, inv_dt_sq, ring, cons);
         else
             apply_levels<T, kTape, false>(sx, d, inv_dt_sq, ring, cons);

@@ -233,3 +233,32 @@ def test_nan_propagation_matches_oracle(jsb, path):
             else:
                 for k in range(3):
                     assert np.array_equal(snap[b][k], ref[k]), (b, k)
+
+
+@pytest.mark.parametrize("state_mode", [0, 1])
+def test_step_walk_equals_substep_walk_and_oracle(jsb, state_mode):
+    """Whole-step walk (default) against the per-substep walk and the oracle, through contact: bodies of
+    the uneven batch's full size ranges drop onto the floor (cubes land, pinned cloths hang), 90
+    steps; state_mode 1 keeps velocities and previous positions in HBM, which the per-vertex passes
+    inside the walk then read and write there."""
+    scene_bytes = jsb.build_scene("uneven_batch", n_cloth=10, n_cube=6, steps=90, seed=11)
+    scene, _ = parse_scene(scene_bytes)
+    a = make_ctx(jsb, scene_bytes)
+    b = jsb.Context(0)
+    b.set_step_walk(False)
+    b.load_scene(scene_bytes)
+    for ctx in (a, b):
+        for mv, t, _ in ctx.bucket_table():
+            ctx.set_bucket_config(mv, t, state_mode)
+    o = Oracle(scene)
+    cur = 0
+    for step in (1, 45, 90):
+        advance(a, step - cur)
+        advance(b, step - cur, "graph")
+        o.step(step - cur)
+        cur = step
+        sa = snapshot(a)
+        assert_same(sa, snapshot(b), f"step walk vs substep walk, step {step}")
+        assert_same(sa, [o.body(i) for i in range(len(scene.bodies))], f"step walk vs oracle, step {step}")
+    # the floor was reached: some vertex of a cube sits on it
+    assert min((loc[:, 1] + pos[1]).min() for pos, loc, _ in sa[10:]) < 0.05

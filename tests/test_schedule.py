@@ -101,3 +101,78 @@ def test_level_counts_pinned_cloth(jsb):
     L = len(levels) - 2
     assert len(source) == 3422 + 2465
     assert 100 < L < 600
+
+
+TYPE_VERTEX = 4
+
+
+def step_sequence(c, num_iterations):
+    """The reference's whole-step order (type, index, substep, written, read): substep k's constraints,
+    and before substeps 1.. each vertex's velocity update + integration (per-vertex passes)."""
+    one = sequence(c)
+    nv = len(c["vertices"])
+    out = []
+    for k in range(num_iterations):
+        if k > 0:
+            out += [(TYPE_VERTEX, v, k, (v,), ()) for v in range(nv)]
+        out += [(t, i, k, w, r) for t, i, w, r in one]
+    return out
+
+
+@pytest.mark.parametrize("name,body", [("pinned_cloth", 0), ("uneven_small", 0), ("uneven_small", 7),
+                                       ("large_cloth_32", 0), ("diff_batch_small", 5)])
+def test_step_levels_reproduce_sequential_order(jsb, name, body):
+    """Whole-step schedule: every constraint of every substep and every per-vertex pass between substeps
+    appears once, typed as its level descriptor says, after every earlier access of its vertices."""
+    scene, _ = parse_scene(np.load(golden_path(name))["scene"].tobytes())
+    b = scene.bodies[body]
+    n_it = b.num_iterations
+    sched = jsb.settings_step_schedule(b.blob, n_it)
+    assert sched is not None
+    levels, records, source = sched
+    c = parse_constraints(b.blob)
+    seq = step_sequence(c, n_it)
+    level_of = {}
+    slot = 0
+    for l, (start, bv, el, n) in enumerate(levels):
+        assert start == slot
+        ends = [bv & 0xFFFF, bv >> 16, el & 0xFFFF, el >> 16, n]
+        assert all(e % 32 == 0 for e in ends) and ends == sorted(ends)
+        for s in range(n):
+            k = start + s
+            src, sub = int(source[k, 0]), int(source[k, 1])
+            if src == 0xFFFFFFFF:
+                assert records[k, 0] == 0xFFFFFFFF
+                continue
+            t = src >> 28
+            assert t == next(i for i, e in enumerate(ends) if s < e)
+            key = (t, src & 0x0FFFFFFF, sub)
+            assert key not in level_of
+            level_of[key] = l
+            if t == TYPE_VERTEX:
+                assert records[k, 0] == (src & 0x0FFFFFFF)
+        slot += n
+    assert slot == len(source)
+    assert len(level_of) == len(seq)
+    last_write, max_access = {}, {}
+    for t, i, k, writes, reads in seq:
+        l = level_of[(t, i, k)]
+        for v in writes:
+            assert l > max_access.get(v, -1)
+        for v in reads:
+            assert l > last_write.get(v, -1)
+        for v in writes:
+            last_write[v] = l
+            max_access[v] = max(max_access.get(v, -1), l)
+        for v in reads:
+            max_access[v] = max(max_access.get(v, -1), l)
+
+
+def test_step_schedule_shortens_the_chain(jsb):
+    """The 30x30 pinned cloth: the whole-step walk needs far fewer levels than 5 per-substep walks."""
+    scene, _ = parse_scene(np.load(golden_path("pinned_cloth"))["scene"].tobytes())
+    b = scene.bodies[0]
+    per_substep = len(jsb.settings_schedule(b.blob)[0]) - 2
+    levels, _, _ = jsb.settings_step_schedule(b.blob, b.num_iterations)
+    assert len(levels) < 0.6 * b.num_iterations * per_substep
+    assert jsb.settings_step_schedule(b.blob, 1) is None
