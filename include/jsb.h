@@ -158,7 +158,7 @@ jsb_status jsb_settings_schedule(const void *blob, size_t len, uint32_t *num_lev
  * substeps, in the padded device layout. levels receives 4 x num_levels uint32 {first slot, bend end |
  * volume end << 16, edge end | LRA end << 16, slots of the level} (ends relative to the first slot;
  * vertex slots from the LRA end on), records 4 x num_slots uint32 (padding slots have 0xffffffff in
- * their first word; a vertex slot is {vertex index, 0, 0, 0}), source 2 x num_slots uint32 {type << 28 |
+ * their first word; a vertex slot is {vertex index, substep it enters, 0, 0}), source 2 x num_slots uint32 {type << 28 |
  * index, substep} (type 0 bend, 1 volume, 2 edge, 3 LRA, 4 vertex; 0xffffffff for padding). Sizes are
  * 0 when the settings have no whole-step schedule (num_iterations < 2, or a level of 65,536 slots or
  * more). Pass NULL arrays to query the sizes. */

@@ -196,6 +196,7 @@ struct AdjointSession {
     DevBuf<float> grad_slots, grad_force;
     DevBuf<TapeDesc> tape_desc;
     std::vector<size_t> slot_offset;  // per body, into grad_slots
+    std::vector<uint32_t> step_slots;  // per body: slots of the whole-step schedule it walks, 0 = per-substep walk
     DevBuf<float4> adj_x, adj_v, seed_dev;
     std::vector<std::pair<int, std::vector<float4>>> seeds;  // (step, dL/dx of every vertex)
     int tape_segment = -1;  // checkpoint segment whose tape is in the tape buffers
@@ -1210,6 +1211,7 @@ jsb_status jsb_set_cluster_config(jsb_context *ctx, uint32_t cluster_size, uint3
 jsb_status jsb_set_step_walk(jsb_context *ctx, int enable) {
     if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
     if (ctx->step_walk == (enable != 0)) return JSB_OK;
+    if (ctx->adjoint) return fail(JSB_ERR_INVALID_ARGUMENT, "the walk cannot change during a differentiable run (jsb_adjoint_end first)");
     ctx->step_walk = enable != 0;
     ctx->dirty = true;  // body descriptors and launch groups change
     return JSB_OK;
@@ -1457,19 +1459,21 @@ jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int chec
     std::vector<TapeDesc> desc(nb);
     std::vector<size_t> cons_off(nb), state_off(nb), plane_off(nb);
     a->slot_offset.resize(nb);
+    a->step_slots.assign(nb, 0);
     const size_t cap = ctx->max_smem_optin - kStaticSmemReserve;
     for (size_t b = 0; b < nb; ++b) {
         const BodyRec &br = ctx->bodies[b];
         const SettingsRec &s = *ctx->settings[br.settings_id];
         const size_t nv = s.parsed.vertices.size(), ns = s.schedule.num_slots, it = br.creation.num_iterations;
+        if (const StepSchedRec *ss = step_sched(ctx, br)) a->step_slots[b] = ss->sched.num_slots;
         cons_off[b] = cons;
         state_off[b] = state;
         plane_off[b] = planes;
         a->slot_offset[b] = slots;
-        cons += K * it * ns * 3;
+        cons += a->step_slots[b] ? K * a->step_slots[b] * 3 : K * it * ns * 3;
         state += K * it * 3 * nv;
         planes += K * nv;
-        slots += ns;
+        slots += a->step_slots[b] ? a->step_slots[b] : ns;
     }
     JSB_CUDA(a->tape_cons.alloc(cons));
     JSB_CUDA(a->tape_state.alloc(state));
@@ -1486,7 +1490,7 @@ jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int chec
         desc[b].cols = a->tape_cols.ptr + b * K * kMaxCollidingShapes;
         desc[b].grad = a->grad_slots.ptr + a->slot_offset[b];
         desc[b].slots = ctx->settings[ctx->bodies[b].settings_id]->schedule.num_slots;
-        desc[b].pad = 0;
+        desc[b].step_slots = a->step_slots[b];
     }
     JSB_CUDA(a->tape_desc.upload(desc.data(), nb));
     JSB_CUDA(a->adj_x.alloc(ctx->total_vertices));
@@ -1509,10 +1513,14 @@ jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int chec
             const SettingsRec &s = *ctx->settings[br.settings_id];
             ag.cap_vertices = std::max(ag.cap_vertices, uint32_t(s.parsed.vertices.size()));
             ag.cap_faces = std::max(ag.cap_faces, pressure_faces(s, br));
-            ag.ring_slots = std::max(ag.ring_slots, ring_slots_for(s));
-            ag.max_level_slots = std::max(ag.max_level_slots, s.schedule.max_level_slots);
+            ag.ring_slots = std::max(ag.ring_slots, ring_slots_for(ctx, br));
+            const StepSchedRec *ss = step_sched(ctx, br);
+            ag.max_level_slots = std::max(ag.max_level_slots, ss ? ss->sched.max_level_slots : s.schedule.max_level_slots);
         }
+        while (ag.ring_slots > kMaxRingSlots && step_smem_bytes(true, ag.cap_vertices, ag.cap_faces, ag.ring_slots) > cap) ag.ring_slots -= 32;
         ag.tape_smem_state = step_smem_bytes(true, ag.cap_vertices, ag.cap_faces, ag.ring_slots) <= cap;
+        while (ag.ring_slots > kMaxRingSlots && step_smem_bytes(ag.tape_smem_state, ag.cap_vertices, ag.cap_faces, ag.ring_slots) > cap)
+            ag.ring_slots -= 32;
         const size_t tsmem = step_smem_bytes(ag.tape_smem_state, ag.cap_vertices, ag.cap_faces, ag.ring_slots);
         if (adjoint_smem_bytes(ag.cap_vertices, ag.cap_faces, 0, 1) > cap || tsmem > cap)
             return fail(JSB_ERR_UNSUPPORTED, "a body is too large for the differentiable (taped) path");
@@ -1713,13 +1721,21 @@ jsb_status jsb_adjoint_gradients(jsb_context *ctx, uint32_t body_id, float *dl_d
     }
     if (dl_dforce) JSB_CUDA(cudaMemcpy(dl_dforce, a.grad_force.ptr + 3 * body_id, 3 * sizeof(float), cudaMemcpyDeviceToHost));
     if (dl_dedge_compliance || dl_dvolume_compliance) {
-        std::vector<float> g(s.schedule.num_slots);
+        // per-slot sums of the reverse sweep -> Jolt's constraint order (a whole-step schedule holds each
+        // constraint once per substep)
+        const uint32_t step_slots = a.step_slots[body_id];
+        StepSchedule steps;
+        if (step_slots && (!build_step_schedule(s.parsed, b.creation.num_iterations, steps, true) || steps.num_slots != step_slots))
+            return fail(JSB_ERR_CAPACITY, "whole-step schedule rebuild failed");
+        const std::vector<uint32_t> &source = step_slots ? steps.source : s.schedule.padded_source;
+        const size_t stride = step_slots ? 2 : 1;
+        std::vector<float> g(step_slots ? step_slots : s.schedule.num_slots);
         if (!g.empty())
             JSB_CUDA(cudaMemcpy(g.data(), a.grad_slots.ptr + a.slot_offset[body_id], g.size() * sizeof(float), cudaMemcpyDeviceToHost));
         if (dl_dedge_compliance) std::fill(dl_dedge_compliance, dl_dedge_compliance + s.parsed.edges.size(), 0.0f);
         if (dl_dvolume_compliance) std::fill(dl_dvolume_compliance, dl_dvolume_compliance + s.parsed.volumes.size(), 0.0f);
         for (size_t c = 0; c < g.size(); ++c) {
-            const uint32_t src = s.schedule.padded_source[c];
+            const uint32_t src = source[c * stride];
             if (src == 0xffffffffu) continue;
             const uint32_t type = src >> 28, idx = src & 0x0fffffffu;
             if (type == kEdge && dl_dedge_compliance) dl_dedge_compliance[idx] += g[c];

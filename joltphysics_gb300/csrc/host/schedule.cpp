@@ -364,6 +364,7 @@ bool build_step_schedule(const ParsedSettings &s, uint32_t num_iterations, StepS
             }
             default:
                 r[0] = it.index;
+                r[1] = it.substep;
                 break;
         }
     }

@@ -99,7 +99,7 @@ Schedule build_schedule(const ParsedSettings &s);
 // a sum over every face), so pressurised bodies keep the per-substep walk.
 //   levels[l] = {first slot, bend end | volume end << 16, edge end | LRA end << 16, slots of the level}
 //   (ends relative to the first slot, each type padded to a multiple of 32 slots; vertex slots run from
-//   the LRA end to the level's slot count; a vertex slot's record is {vertex index, 0, 0, 0}).
+//   the LRA end to the level's slot count; a vertex slot's record is {vertex index, substep entered, 0, 0}).
 struct StepSchedule {
     std::vector<uint32_t> levels;   // 4 per level
     std::vector<uint32_t> records;  // 4 per slot

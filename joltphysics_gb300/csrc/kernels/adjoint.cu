@@ -18,6 +18,11 @@
 // d loss / d compliance accumulates per schedule slot; a slot is reversed by the same thread in every
 // substep, so the accumulation is race free and deterministic.
 //
+// A body that walked its whole-step schedule forward (no pressure) is reversed along that schedule:
+// the last velocity update, then its levels last to first, where a vertex slot reverses the integration
+// of the substep the vertex entered and the velocity update of the one it left, then substep 0's
+// integration. The taped forward step records the same substep states either way.
+//
 // Dihedral bends are not differentiated (the runtime rejects differentiable runs of bodies with
 // bends): the reference's ACosApproximate has an unbounded derivative at flat triangle pairs.
 
@@ -233,6 +238,212 @@ __device__ __forceinline__ void reverse_levels(float4 *lx, const float *sw, cons
     if (depth > 0) adj_cp_async_wait(0);
 }
 
+// Everything the per-vertex reverse passes of one body and step need.
+struct VertexAdj {
+    float4 *lx, *lv, *lp;
+    const float *sw;
+    const float4 *tape;  // this step's substep states [substep][3][nv]
+    const float4 *planes;
+    const int32_t *shapes;
+    const float2 *cols;
+    uint32_t nv, n_it;
+    float dt_sub, inv_dt, damp, restitution_threshold, max_sq, radius;
+};
+
+// Reverse of ApplyCollisionConstraintsAndUpdateVelocities (:700-825) of substep `it` for vertex i, with
+// the velocity clamp of UpdateSoftBodyState after the last substep: maps the adjoints of the position
+// and velocity after the update to those of the position after the constraints (lx), the velocity
+// before the update (lv, through restitution only) and the position at substep start (lp).
+__device__ __forceinline__ void velocity_adjoint(const VertexAdj &a, uint32_t i, uint32_t it) {
+    const float4 *ts = a.tape + size_t(it) * 3 * a.nv;
+    const uint32_t nv = a.nv;
+    const bool last = it == a.n_it - 1;
+    const float w = a.sw[i];
+    if (!(w > 0.0f)) {  // kinematic: position and velocity pass through; prev unused
+        a.lp[i] = make_float4(0, 0, 0, 0);
+        if (last) {  // velocity clamp of UpdateSoftBodyState
+            const f3 vk = xyz(ts[nv + i]), lk = xyz(a.lv[i]);
+            const float vsq = len_sq(vk);
+            if (vsq > a.max_sq) a.lv[i] = with_w(sqrtf(a.max_sq / vsq) * (lk - vk * (dot(vk, lk) / vsq)), 0.0f);
+        }
+        return;
+    }
+    const f3 xs = xyz(ts[i]), pv = xyz(ts[nv + i]), xc = xyz(ts[2 * nv + i]);
+    const f3 lxf = xyz(a.lx[i]);
+    f3 lv3 = xyz(a.lv[i]);
+    const f3 v0 = (xc - xs) * a.inv_dt;
+    const int shape = a.shapes[i];
+    bool contact = false;
+    f3 n = vzero();
+    float pd = 0.0f;
+    if (shape >= 0) {
+        const float4 pl = a.planes[i];
+        n = xyz(pl);
+        pd = -(dot(xc, n) + pl.w) + a.radius;
+        contact = pd > 0.0f;
+    }
+    f3 vn = vzero(), vt = vzero(), v3 = v0;
+    float vtl = 0.0f, f = 0.0f, mu = 0.0f, e = 0.0f;
+    bool unclamped = false, rest = false;
+    if (contact) {
+        mu = a.cols[shape].x;
+        e = a.cols[shape].y;
+        vn = n * dot(n, v0);
+        vt = v0 - vn;
+        vtl = len(vt);
+        f3 v1 = v0;
+        if (vtl > 0.0f) {
+            const float fq = mu * pd / (vtl * a.dt_sub);
+            unclamped = !(fq > 1.0f);
+            f = unclamped ? fq : 1.0f;
+            v1 = v0 - vt * f;
+        }
+        const f3 v2 = v1 - vn;
+        const float pvn = dot(pv, n);
+        rest = pvn < a.restitution_threshold;
+        v3 = rest ? v2 - (e * pvn) * n : v2;
+    }
+    if (last) {  // velocity clamp of UpdateSoftBodyState
+        const float vsq = len_sq(v3);
+        if (vsq > a.max_sq) {
+            const float sc = sqrtf(a.max_sq / vsq);
+            lv3 = sc * (lv3 - v3 * (dot(v3, lv3) / vsq));
+        }
+    }
+    f3 lxc, lpv = vzero(), lv0;
+    if (!contact) {
+        lv0 = lv3;
+        lxc = lxf;
+    } else {
+        if (rest) lpv = n * (-e * dot(n, lv3));
+        const f3 lv1 = lv3;
+        f3 lvn = vzero() - lv3;
+        lv0 = lv1;
+        f3 lvt = vzero();
+        float lpd = 0.0f;
+        if (vtl > 0.0f) {
+            lvt = (-f) * lv1;
+            if (unclamped) {
+                const float lf = -dot(vt, lv1);
+                lpd += mu / (vtl * a.dt_sub) * lf;
+                const float lvtl = -f / vtl * lf;
+                lvt = lvt + vt * (lvtl / vtl);
+            }
+        }
+        lv0 = lv0 + lvt;
+        lvn = lvn - lvt;
+        lv0 = lv0 + n * dot(n, lvn);
+        lpd += dot(n, lxf);
+        lxc = lxf - n * lpd;
+    }
+    a.lx[i] = with_w(lxc + lv0 * a.inv_dt, 0.0f);
+    a.lv[i] = with_w(lpv, 0.0f);
+    a.lp[i] = with_w(vzero() - lv0 * a.inv_dt, 0.0f);
+}
+
+// Reverse of IntegratePositions (:325-365) for vertex i: x' = x + v' dt, v' = (v + g dt + F dt w / N) damp.
+// Accumulates d loss / d (sub-step impulse) into force_acc.
+__device__ __forceinline__ void integrate_adjoint(const VertexAdj &a, uint32_t i, f3 &force_acc) {
+    const float w = a.sw[i];
+    const f3 lxp = xyz(a.lx[i]);
+    const f3 lvp = xyz(a.lv[i]) + lxp * a.dt_sub;
+    f3 lvs = lvp;
+    if (w > 0.0f) {
+        lvs = lvp * a.damp;
+        force_acc = force_acc + lvp * (w * a.damp);
+    }
+    a.lx[i] = with_w(lxp + xyz(a.lp[i]), 0.0f);
+    a.lv[i] = with_w(lvs, 0.0f);
+}
+
+// Reverse of a whole-step walk (bodies without pressure that walked their whole-step schedule): the
+// levels last to first; a constraint slot is reversed as in reverse_levels, a vertex slot {i, k} runs
+// the reverse of substep k's integration, then of substep k - 1's velocity update. The ring works as in
+// reverse_levels. d loss / d compliance accumulates per whole-step slot (the host sums a constraint's
+// slots over the substeps).
+template <int T>
+__device__ __forceinline__ void reverse_step_levels(const VertexAdj &a, const BodyDesc &d, const float4 *cons, float *grad,
+                                                    float inv_dt_sq, uint4 *ring, uint32_t depth, uint32_t rpt, f3 &force_acc) {
+    const uint4 *__restrict__ levels = d.step_levels;
+    const uint4 *__restrict__ rec = d.step_records;
+    const int L = int(d.num_step_levels);
+    const uint32_t tid = threadIdx.x;
+    const uint32_t nring = depth + 1;
+    auto slot = [&](uint32_t l, uint32_t k) { return ring + ((l % nring) * rpt + k) * 4 * T + tid; };
+    auto stage = [&](int l) {
+        const uint4 lv = __ldg(levels + l);
+        uint32_t s = tid;
+        for (uint32_t k = 0; k < rpt && s < lv.w; ++k, s += T) {
+            const uint32_t c = lv.x + s;
+            const int type = step_slot_type(lv, s);
+            uint4 *dst = slot(uint32_t(l), k);
+            adj_cp_async16(dst, rec + c);
+            if (type == 4) continue;
+            const float4 *src = cons + size_t(c) * 3;
+            adj_cp_async16(dst + T, src);
+            if (type == 1) {
+                adj_cp_async16(dst + 2 * T, src + 1);
+                adj_cp_async16(dst + 3 * T, src + 2);
+            }
+        }
+    };
+    if (depth > 0)
+        for (uint32_t k = 0; k < depth; ++k) {
+            if (L - 1 - int(k) >= 0) stage(L - 1 - int(k));
+            adj_cp_async_commit();
+        }
+    for (int l = L - 1; l >= 0; --l) {
+        if (depth > 0) {
+            if (l - int(depth) >= 0) stage(l - int(depth));
+            adj_cp_async_commit();
+            adj_cp_async_wait(depth);  // this thread's copies of level l have landed
+        }
+        const uint4 lv = __ldg(levels + l);
+        uint32_t k = 0;
+        for (uint32_t s = tid; s < lv.w; s += T, ++k) {
+            const uint32_t c = lv.x + s;
+            const int type = step_slot_type(lv, s);
+            uint4 r;
+            float4 tin[3];
+            const bool staged = depth > 0 && k < rpt;
+            if (staged) {
+                const uint4 *src = slot(uint32_t(l), k);
+                r = src[0];
+                if (type != 4) {
+                    tin[0] = *reinterpret_cast<const float4 *>(src + T);
+                    if (type == 1) {
+                        tin[1] = *reinterpret_cast<const float4 *>(src + 2 * T);
+                        tin[2] = *reinterpret_cast<const float4 *>(src + 3 * T);
+                    }
+                }
+            } else {
+                r = __ldg(rec + c);
+                if (type != 4) {
+                    const float4 *src = cons + size_t(c) * 3;
+                    tin[0] = src[0];
+                    if (type == 1) {
+                        tin[1] = src[1];
+                        tin[2] = src[2];
+                    }
+                }
+            }
+            if (r.x == 0xffffffffu) continue;
+            if (type == 4) {
+                integrate_adjoint(a, r.x, force_acc);
+                velocity_adjoint(a, r.x, r.y - 1);
+            } else if (type == 2) {
+                edge_adjoint(a.lx, a.sw, r, tin, inv_dt_sq, grad + c);
+            } else if (type == 1) {
+                volume_adjoint(a.lx, a.sw, r, tin, inv_dt_sq, grad + c);
+            } else if (type == 3) {
+                lra_adjoint(a.lx, r, tin);
+            }
+        }
+        __syncthreads();
+    }
+    if (depth > 0) adj_cp_async_wait(0);
+}
+
 // Shared memory (dynamic), cap = the launch's largest vertex count:
 //   lx[cap] position adjoints | lv[cap] velocity adjoints | lp[cap] previous-position adjoints, then
 //   substep positions for the pressure adjoint | w[cap] inverse masses | per-face pressure scratch
@@ -269,110 +480,46 @@ __device__ void adjoint_body(const AdjParams &q, uint32_t b, float4 *smem, uint3
     }
     __syncthreads();
 
+    VertexAdj va;
+    va.lx = lx;
+    va.lv = lv;
+    va.lp = lp;
+    va.sw = sw;
+    va.tape = ts0;
+    va.planes = planes;
+    va.shapes = shapes;
+    va.cols = cols;
+    va.nv = nv;
+    va.n_it = n_it;
+    va.dt_sub = dt_sub;
+    va.inv_dt = inv_dt;
+    va.damp = damp;
+    va.restitution_threshold = restitution_threshold;
+    va.max_sq = max_sq;
+    va.radius = d.vertex_radius;
+
     f3 force_acc = vzero();
-    for (int it = int(n_it) - 1; it >= 0; --it) {
+    const bool step_walk = d.step_levels != nullptr && !has_pressure && td.step_slots > 0;
+    if (step_walk) {
+        // the whole step walked as one schedule: last velocity update, the levels reversed (with the
+        // per-vertex passes between substeps), substep 0's integration
+        for (uint32_t i = tid; i < nv; i += T) velocity_adjoint(va, i, n_it - 1);
+        __syncthreads();
+        reverse_step_levels<T>(va, d, td.cons + size_t(q.tape_step) * td.step_slots * 3, td.grad, inv_dt_sq, ring, q.ring_depth,
+                               q.ring_rpt, force_acc);
+        for (uint32_t i = tid; i < nv; i += T) integrate_adjoint(va, i, force_acc);
+        __syncthreads();
+    }
+    for (int it = step_walk ? -1 : int(n_it) - 1; it >= 0; --it) {
         const float4 *ts = td.state + (size_t(q.tape_step) * n_it + it) * 3 * nv;
         // ---- collision and velocity update ----
-        for (uint32_t i = tid; i < nv; i += T) {
-            const float w = sw[i];
-            if (!(w > 0.0f)) {  // kinematic: position and velocity pass through; prev unused
-                lp[i] = make_float4(0, 0, 0, 0);
-                if (it == int(n_it) - 1) {  // velocity clamp of UpdateSoftBodyState
-                    const f3 vk = xyz(ts[nv + i]), lk = xyz(lv[i]);
-                    const float vsq = len_sq(vk);
-                    if (vsq > max_sq) lv[i] = with_w(sqrtf(max_sq / vsq) * (lk - vk * (dot(vk, lk) / vsq)), 0.0f);
-                }
-                continue;
-            }
-            const f3 xs = xyz(ts[i]), pv = xyz(ts[nv + i]), xc = xyz(ts[2 * nv + i]);
-            const f3 lxf = xyz(lx[i]);
-            f3 lv3 = xyz(lv[i]);
-            const f3 v0 = (xc - xs) * inv_dt;
-            const int shape = shapes[i];
-            bool contact = false;
-            f3 n = vzero();
-            float pd = 0.0f;
-            if (shape >= 0) {
-                const float4 pl = planes[i];
-                n = xyz(pl);
-                pd = -(dot(xc, n) + pl.w) + d.vertex_radius;
-                contact = pd > 0.0f;
-            }
-            f3 vn = vzero(), vt = vzero(), v3 = v0;
-            float vtl = 0.0f, f = 0.0f, mu = 0.0f, e = 0.0f;
-            bool unclamped = false, rest = false;
-            if (contact) {
-                mu = cols[shape].x;
-                e = cols[shape].y;
-                vn = n * dot(n, v0);
-                vt = v0 - vn;
-                vtl = len(vt);
-                f3 v1 = v0;
-                if (vtl > 0.0f) {
-                    const float fq = mu * pd / (vtl * dt_sub);
-                    unclamped = !(fq > 1.0f);
-                    f = unclamped ? fq : 1.0f;
-                    v1 = v0 - vt * f;
-                }
-                const f3 v2 = v1 - vn;
-                const float pvn = dot(pv, n);
-                rest = pvn < restitution_threshold;
-                v3 = rest ? v2 - (e * pvn) * n : v2;
-            }
-            if (it == int(n_it) - 1) {  // velocity clamp of UpdateSoftBodyState
-                const float vsq = len_sq(v3);
-                if (vsq > max_sq) {
-                    const float sc = sqrtf(max_sq / vsq);
-                    lv3 = sc * (lv3 - v3 * (dot(v3, lv3) / vsq));
-                }
-            }
-            f3 lxc, lpv = vzero(), lv0;
-            if (!contact) {
-                lv0 = lv3;
-                lxc = lxf;
-            } else {
-                if (rest) lpv = n * (-e * dot(n, lv3));
-                const f3 lv1 = lv3;
-                f3 lvn = vzero() - lv3;
-                lv0 = lv1;
-                f3 lvt = vzero();
-                float lpd = 0.0f;
-                if (vtl > 0.0f) {
-                    lvt = (-f) * lv1;
-                    if (unclamped) {
-                        const float lf = -dot(vt, lv1);
-                        lpd += mu / (vtl * dt_sub) * lf;
-                        const float lvtl = -f / vtl * lf;
-                        lvt = lvt + vt * (lvtl / vtl);
-                    }
-                }
-                lv0 = lv0 + lvt;
-                lvn = lvn - lvt;
-                lv0 = lv0 + n * dot(n, lvn);
-                lpd += dot(n, lxf);
-                lxc = lxf - n * lpd;
-            }
-            lx[i] = with_w(lxc + lv0 * inv_dt, 0.0f);
-            lv[i] = with_w(lpv, 0.0f);
-            lp[i] = with_w(vzero() - lv0 * inv_dt, 0.0f);
-        }
+        for (uint32_t i = tid; i < nv; i += T) velocity_adjoint(va, i, uint32_t(it));
         __syncthreads();
         // ---- constraint levels, reversed ----
         reverse_levels<T>(lx, sw, d, td.cons + (size_t(q.tape_step) * n_it + it) * size_t(td.slots) * 3, td.grad, inv_dt_sq, ring,
                           q.ring_depth, q.ring_rpt);
         // ---- integration: x' = x + v' dt, v' = (v + g dt + F dt w / N) damp ----
-        for (uint32_t i = tid; i < nv; i += T) {
-            const float w = sw[i];
-            const f3 lxp = xyz(lx[i]);
-            const f3 lvp = xyz(lv[i]) + lxp * dt_sub;
-            f3 lvs = lvp;
-            if (w > 0.0f) {
-                lvs = lvp * damp;
-                force_acc = force_acc + lvp * (w * damp);
-            }
-            lx[i] = with_w(lxp + xyz(lp[i]), 0.0f);
-            lv[i] = with_w(lvs, 0.0f);
-        }
+        for (uint32_t i = tid; i < nv; i += T) integrate_adjoint(va, i, force_acc);
         __syncthreads();
         // ---- pressure: v += w coef (x2 - x1) x (x3 - x1) per face, coef = p dt / V6 ----
         if (has_pressure) {

@@ -57,7 +57,7 @@ struct BodyDesc {
     uint32_t num_vertices;
     // whole-step schedule for this body's iteration count (null: walk the per-substep schedule);
     // levels {first slot, bend end | volume end << 16, edge end | LRA end << 16, slots}, vertex slots
-    // {vertex index, 0, 0, 0} from the LRA end on (see build_step_schedule)
+    // {vertex index, substep entered, 0, 0} from the LRA end on (see build_step_schedule)
     const uint4 *step_levels;
     const uint4 *step_records;
     uint32_t num_step_levels;
@@ -99,10 +99,17 @@ struct TapeDesc {
     float4 *plane;   // [segment steps][num_vertices]: collision plane (normal, constant)
     int32_t *shape;  // [segment steps][num_vertices]: colliding shape index, -1 none
     float2 *cols;    // [segment steps][kMaxCollidingShapes]: combined friction, restitution
-    float *grad;     // [slots]: d loss / d compliance of the slot's constraint
-    uint32_t slots;
-    uint32_t pad;
+    float *grad;     // [slots] (or [step_slots]): d loss / d compliance of the slot's constraint
+    uint32_t slots;       // slots of the per-substep schedule
+    uint32_t step_slots;  // > 0: the body walks its whole-step schedule of this many slots; cons is then
+                          // [segment steps][step_slots][3] and grad [step_slots]
 };
+
+// Slot type of a whole-step level {first, bend end | volume end << 16, edge end | LRA end << 16, slots}:
+// 0 bend, 1 volume, 2 edge, 3 LRA, 4 vertex.
+JSB_HD inline int step_slot_type(uint4 lv, uint32_t s) {
+    return s < (lv.y & 0xffffu) ? 0 : (s < (lv.y >> 16) ? 1 : (s < (lv.z & 0xffffu) ? 2 : (s < (lv.z >> 16) ? 3 : 4)));
+}
 
 struct StepParams {
     const BodyDesc *bodies;

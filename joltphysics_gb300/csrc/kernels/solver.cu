@@ -143,15 +143,20 @@ struct VertexPass {
     int ncols;
     f3 sub_g, sub_imp;
     float damp, dt_sub, radius, restitution_threshold;
+    float4 *tape;  // taped forward: this step's substep states [substep][3][nv] (TapeDesc::state)
+    uint32_t nv;
 };
 
 // ApplyCollisionConstraintsAndUpdateVelocities (:700-825, static colliders) of the substep vertex i
-// leaves, then IntegratePositions (:325-365) of the substep it enters, for one vertex: the arithmetic
-// of the two bulk passes of step_body in the same order.
-template <bool kSmemState>
-__device__ __forceinline__ void vertex_between_substeps(float4 *sx, const VertexPass &vp, uint32_t i) {
+// leaves, then IntegratePositions (:325-365) of substep k it enters, for one vertex: the arithmetic of
+// the two bulk passes of step_body in the same order. The taped forward step records the vertex's
+// position after substep k - 1's constraints, and its position and velocity at the start of substep k,
+// where the bulk passes of the per-substep walk record them.
+template <bool kSmemState, bool kTape>
+__device__ __forceinline__ void vertex_between_substeps(float4 *sx, const VertexPass &vp, uint32_t i, uint32_t k) {
     float4 pi = sx[i];
     float4 vel = kSmemState ? vp.sv[i] : vp.gv[i];
+    if (kTape) vp.tape[(size_t(k - 1) * 3 + 2) * vp.nv + i] = pi;
     if (pi.w > 0.0f) {
         const float4 prev = kSmemState ? vp.sprev[i] : vp.gprev[i];
         f3 x = xyz(pi);
@@ -172,12 +177,11 @@ __device__ __forceinline__ void vertex_between_substeps(float4 *sx, const Vertex
         vp.gprev[i] = pi;
         vp.gv[i] = vel;
     }
+    if (kTape) {
+        vp.tape[size_t(k) * 3 * vp.nv + i] = pi;
+        vp.tape[(size_t(k) * 3 + 1) * vp.nv + i] = with_w(xyz(vel), 0.0f);
+    }
     sx[i] = with_w(xyz(pi) + xyz(vel) * vp.dt_sub, pi.w);
-}
-
-// Slot type of a whole-step level: 0 bend, 1 volume, 2 edge, 3 LRA, 4 vertex.
-__device__ __forceinline__ int step_slot_type(uint4 lv, uint32_t s) {
-    return s < (lv.y & 0xffffu) ? 0 : (s < (lv.y >> 16) ? 1 : (s < (lv.z & 0xffffu) ? 2 : (s < (lv.z >> 16) ? 3 : 4)));
 }
 
 // Stages the first ring.slots records of whole-step level `idx` and its descriptor; slots beyond the
@@ -190,9 +194,10 @@ __device__ __forceinline__ void step_ring_stage(const LevelRing &ring, const uin
     if (threadIdx.x == 0) ring.desc[pos] = lv;
 }
 
-template <int T, bool kSmemState, bool kGuard>
+// tape_cons (taped forward): this step's constraint inputs, 3 float4 per whole-step slot.
+template <int T, bool kSmemState, bool kGuard, bool kTape>
 __device__ __forceinline__ void apply_step_levels(float4 *sx, const BodyDesc &d, float inv_dt_sq, const LevelRing &ring,
-                                                  const VertexPass &vp) {
+                                                  const VertexPass &vp, float4 *tape_cons) {
     const uint4 *__restrict__ levels = d.step_levels;
     const uint4 *__restrict__ rec = d.step_records;
     const uint32_t tid = threadIdx.x;
@@ -216,10 +221,12 @@ __device__ __forceinline__ void apply_step_levels(float4 *sx, const BodyDesc &d,
             const uint4 r = s < ring.slots ? ring_rec[s] : __ldg(rec + lv.x + s);
             if (r.x != 0xffffffffu) {
                 const int type = step_slot_type(lv, s);
-                if (type == 4)
-                    vertex_between_substeps<kSmemState>(sx, vp, r.x);
-                else
+                if (type == 4) {
+                    vertex_between_substeps<kSmemState, kTape>(sx, vp, r.x, r.y);
+                } else {
+                    if (kTape) tape_inputs(sx, r, type, tape_cons + size_t(lv.x + s) * 3);
                     project<kGuard>(sx, r, type, inv_dt_sq);
+                }
             }
         }
         if (ahead < L) step_ring_stage<T>(ring, rec, ahead, lv_ahead);
@@ -315,7 +322,7 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     const bool has_pressure = d.pressure > 0.0f && d.num_faces > 0;
     // Whole-step walk: substep 0's integration below, then every substep's constraint levels with the
     // per-vertex passes between substeps inside the walk, then the last substep's velocity update.
-    const bool step_walk = !kTape && d.step_levels != nullptr && !has_pressure;
+    const bool step_walk = d.step_levels != nullptr && !has_pressure && (!kTape || td.step_slots > 0);
     VertexPass vp{};
     if (step_walk) {
         vp.sv = sv;
@@ -332,6 +339,8 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
         vp.dt_sub = dt_sub;
         vp.radius = d.vertex_radius;
         vp.restitution_threshold = restitution_threshold;
+        vp.tape = kTape ? td.state + size_t(p.tape_step) * n_it * 3 * nv : nullptr;
+        vp.nv = nv;
     }
     const uint32_t passes = step_walk ? 1u : n_it;
 
@@ -403,20 +412,23 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
         // Update groups in dependency-level order (NaN-guarded projections for a body holding NaNs)
         float4 *cons = kTape ? td.cons + (size_t(p.tape_step) * n_it + it) * size_t(td.slots) * 3 : nullptr;
         const bool nan_any = __syncthreads_or(nan_seen);
-        if (!kTape && step_walk) {
+        if (step_walk) {
             // (a body that turns non-finite within the step finishes it on the unguarded walk: same
             // result, slower)
+            float4 *step_cons = kTape ? td.cons + size_t(p.tape_step) * td.step_slots * 3 : nullptr;
             if (nan_any)
-                apply_step_levels<T, kSmemState, true>(sx, d, inv_dt_sq, ring, vp);
+                apply_step_levels<T, kSmemState, true, kTape>(sx, d, inv_dt_sq, ring, vp, step_cons);
             else
-                apply_step_levels<T, kSmemState, false>(sx, d, inv_dt_sq, ring, vp);
+                apply_step_levels<T, kSmemState, false, kTape>(sx, d, inv_dt_sq, ring, vp, step_cons);
         } else if (nan_any)
             apply_levels<T, kTape, true>(sx, d, inv_dt_sq, ring, cons);
         else
             apply_levels<T, kTape, false>(sx, d, inv_dt_sq, ring, cons);
         __syncthreads();
-        if (kTape)
-            for (uint32_t i = tid; i < nv; i += T) tape_state[2 * nv + i] = sx[i];
+        if (kTape) {  // position after the constraints of the last substep walked
+            float4 *after = step_walk ? td.state + (size_t(p.tape_step) * n_it + n_it - 1) * 3 * nv : tape_state;
+            for (uint32_t i = tid; i < nv; i += T) after[2 * nv + i] = sx[i];
+        }
         // ApplyCollisionConstraintsAndUpdateVelocities (static colliders)
         for (uint32_t i = tid; i < nv; i += T) {
             float4 pi = sx[i];
@@ -497,10 +509,8 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     __syncthreads();
 }
 
-template <int T, bool kSmemState, bool kTape = false>
-__global__ void __launch_bounds__(T) step_kernel(StepParams p, uint32_t cap) {
-    extern __shared__ float4 smem[];
-    __shared__ Shared sh;
+template <int T, bool kSmemState, bool kTape>
+__device__ __forceinline__ void step_queue(const StepParams &p, uint32_t cap, float4 *smem, Shared &sh) {
     for (;;) {
         if (threadIdx.x == 0) sh.item = atomicAdd(p.queue, 1u);
         __syncthreads();
@@ -509,6 +519,24 @@ __global__ void __launch_bounds__(T) step_kernel(StepParams p, uint32_t cap) {
         if (item >= p.num_work) return;
         step_body<T, kSmemState, kTape>(p, p.work[item], smem, cap, sh);
     }
+}
+
+// Register budget of 128 per thread (65,536 / (T x 512 / T)): enough for the projections without
+// spilling, and small CTAs of small bodies still pack many to an SM.
+template <int T, bool kSmemState>
+__global__ void __launch_bounds__(T, 512 / T) step_kernel(StepParams p, uint32_t cap) {
+    extern __shared__ float4 smem[];
+    __shared__ Shared sh;
+    step_queue<T, kSmemState, false>(p, cap, smem, sh);
+}
+
+// The taped forward step (differentiable runs) holds more live values; one CTA per SM lets it keep
+// them in registers.
+template <bool kSmemState>
+__global__ void __launch_bounds__(128, 1) step_kernel_tape(StepParams p, uint32_t cap) {
+    extern __shared__ float4 smem[];
+    __shared__ Shared sh;
+    step_queue<128, kSmemState, true>(p, cap, smem, sh);
 }
 
 }  // namespace
@@ -542,18 +570,18 @@ cudaError_t launch_step_tape(const StepParams &p, bool smem_state, uint32_t smem
                              cudaStream_t stream) {
     size_t smem = step_smem_bytes(smem_state, smem_vertices, smem_faces, p.ring_slots);
     if (smem_state)
-        step_kernel<128, true, true><<<grid, 128, smem, stream>>>(p, smem_vertices);
+        step_kernel_tape<true><<<grid, 128, smem, stream>>>(p, smem_vertices);
     else
-        step_kernel<128, false, true><<<grid, 128, smem, stream>>>(p, smem_vertices);
+        step_kernel_tape<false><<<grid, 128, smem, stream>>>(p, smem_vertices);
     return cudaGetLastError();
 }
 
 int step_tape_occupancy(bool smem_state, size_t smem) {
     int n = 0;
     if (smem_state)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<128, true, true>, 128, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel_tape<true>, 128, smem);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<128, false, true>, 128, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel_tape<false>, 128, smem);
     return n;
 }
 
@@ -565,8 +593,8 @@ cudaError_t init_step_kernels(int max_dynamic_smem) {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel<TT, SS>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
     JSB_FOR_EACH_SHAPE(JSB_ATTR)
 #undef JSB_ATTR
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel<128, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel<128, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel_tape<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel_tape<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
     return e;
 }
 
