@@ -165,7 +165,7 @@ jsb_status jsb_settings_schedule(const void *blob, size_t len, uint32_t *num_lev
 jsb_status jsb_settings_step_schedule(const void *blob, size_t len, uint32_t num_iterations, uint32_t *num_levels,
                                       uint32_t *num_slots, uint32_t *levels, uint32_t *records, uint32_t *source);
 /* Launch shape of the size bucket of bodies with vertex count <= max_vertices (and above the next
- * smaller bucket): threads per CTA in {32, 64, 128, 256}; state_mode 0 keeps positions, velocities and
+ * smaller bucket): threads per CTA in {32, 64, 128, 256, 512}; state_mode 0 keeps positions, velocities and
  * previous positions in shared memory when they fit, 1 keeps only positions there, 2 sends the
  * bucket's bodies to the thread-block-cluster path. The autotuner writes this table; the calls below
  * set or read it directly. Bodies whose positions do not fit one CTA's shared memory always take the

@@ -35,19 +35,18 @@ cudaError_t launch_step(const StepParams &p, int threads, bool smem_state, uint3
 int step_occupancy(int threads, bool smem_state, size_t smem);
 size_t step_smem_bytes(bool smem_state, uint32_t vertices, uint32_t faces, uint32_t ring_slots);
 cudaError_t init_step_kernels(int max_dynamic_smem);
-cudaError_t launch_step_tape(const StepParams &p, bool smem_state, uint32_t smem_vertices, uint32_t smem_faces, int grid,
+cudaError_t launch_step_tape(const StepParams &p, int threads, bool smem_state, uint32_t smem_vertices, uint32_t smem_faces, int grid,
                              cudaStream_t stream);
-int step_tape_occupancy(bool smem_state, size_t smem);
+int step_tape_occupancy(int threads, bool smem_state, size_t smem);
 size_t cluster_smem_bytes(uint32_t shift, uint32_t desc_cap, uint32_t rpt, int threads);
 cudaError_t launch_cluster_step(const StepParams &p, int cluster, int threads, uint32_t shift, uint32_t desc_cap, uint32_t rpt,
                                 cudaStream_t stream);
 cudaError_t init_cluster_kernels(int max_dynamic_smem);
 int cluster_occupancy(int cluster, int threads, size_t smem);
-size_t adjoint_smem_bytes(uint32_t vertices, uint32_t faces, uint32_t depth, uint32_t rpt);
-int adjoint_threads();
+size_t adjoint_smem_bytes(uint32_t vertices, uint32_t faces, uint32_t depth, uint32_t rpt, int threads);
 cudaError_t init_adjoint_kernels(int max_dynamic_smem);
-int adjoint_occupancy(size_t smem);
-cudaError_t launch_adjoint(const AdjParams &q, uint32_t cap_vertices, uint32_t cap_faces, int grid, cudaStream_t stream);
+int adjoint_occupancy(size_t smem, int threads);
+cudaError_t launch_adjoint(const AdjParams &q, uint32_t cap_vertices, uint32_t cap_faces, int grid, int threads, cudaStream_t stream);
 cudaError_t launch_add(float4 *dst, const float4 *src, uint64_t n, int num_sms, cudaStream_t stream);
 cudaError_t launch_unpack_state(const float *pos3, const float *vel3, float4 *x, float4 *v, uint64_t n, int num_sms,
                                 cudaStream_t stream);
@@ -163,6 +162,7 @@ struct AdjGroup {
     DevBuf<uint32_t> work;
     uint32_t num_work = 0;
     uint32_t cap_vertices = 0, cap_faces = 0, ring_slots = 32, max_level_slots = 0;
+    int threads = 128;  // taped forward and adjoint CTAs: 256 when levels are wider than 192 slots
     bool tape_smem_state = true;
     int tape_grid = 1, adj_grid = 1;
     uint32_t adj_depth = 0, adj_rpt = 1;  // adjoint record / tape ring: levels ahead, slots per thread
@@ -675,7 +675,7 @@ jsb_status enqueue_taped(jsb_context *ctx, const AdjointSession &a, int tape_ste
         p.ring_slots = g.ring_slots;
         p.tape = a.tape_desc.ptr;
         p.tape_step = uint32_t(tape_step);
-        JSB_CUDA(launch_step_tape(p, g.tape_smem_state, g.cap_vertices, g.cap_faces, g.tape_grid, g.stream));
+        JSB_CUDA(launch_step_tape(p, g.threads, g.tape_smem_state, g.cap_vertices, g.cap_faces, g.tape_grid, g.stream));
         ++launches;
         JSB_CUDA(cudaEventRecord(g.done, g.stream));
         JSB_CUDA(cudaStreamWaitEvent(stream, g.done, 0));
@@ -704,7 +704,7 @@ jsb_status enqueue_adjoint(jsb_context *ctx, const AdjointSession &a, int tape_s
         q.dt = a.dt;
         q.ring_depth = g.adj_depth;
         q.ring_rpt = g.adj_rpt;
-        JSB_CUDA(launch_adjoint(q, g.cap_vertices, g.cap_faces, g.adj_grid, g.stream));
+        JSB_CUDA(launch_adjoint(q, g.cap_vertices, g.cap_faces, g.adj_grid, g.threads, g.stream));
         ++launches;
         JSB_CUDA(cudaEventRecord(g.done, g.stream));
         JSB_CUDA(cudaStreamWaitEvent(stream, g.done, 0));
@@ -1180,8 +1180,8 @@ jsb_status jsb_settings_step_schedule(const void *blob, size_t len, uint32_t num
 
 jsb_status jsb_set_bucket_config(jsb_context *ctx, uint32_t max_vertices, uint32_t threads, uint32_t state_mode) {
     if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
-    if (threads != 32 && threads != 64 && threads != 128 && threads != 256)
-        return fail(JSB_ERR_INVALID_ARGUMENT, "threads must be 32, 64, 128 or 256");
+    if (threads != 32 && threads != 64 && threads != 128 && threads != 256 && threads != 512)
+        return fail(JSB_ERR_INVALID_ARGUMENT, "threads must be 32, 64, 128, 256 or 512");
     if (state_mode > 2) return fail(JSB_ERR_INVALID_ARGUMENT, "state_mode must be 0, 1 or 2");
     bool found = false;
     for (Bucket &b : ctx->buckets)
@@ -1263,7 +1263,7 @@ jsb_status jsb_last_kernel_ms(jsb_context *ctx, float *ms) {
 }
 
 // Autotuner: coordinate descent over the bucket table. For every occupied bucket (largest first) each
-// launch shape -- threads per CTA in {32, 64, 128, 256} x vertex state in shared / global memory -- is
+// launch shape -- threads per CTA in {32, 64, 128, 256, 512} x vertex state in shared / global memory -- is
 // tried with the other buckets fixed, and the one giving the fastest whole batched step (all buckets
 // running concurrently, as in jsb_step) is kept. Device state is saved before and restored after.
 jsb_status jsb_autotune(jsb_context *ctx, float dt, int trials) {
@@ -1322,7 +1322,7 @@ jsb_status jsb_autotune(jsb_context *ctx, float dt, int trials) {
     {
         const std::vector<Bucket> current = ctx->buckets;
         std::vector<Bucket> best_table = current;
-        for (int variant = 0; variant < 4 && st == JSB_OK; ++variant) {
+        for (int variant = 0; variant < 5 && st == JSB_OK; ++variant) {
             std::vector<Bucket> t = current;
             for (Bucket &b : t) {
                 if (b.state_mode == 2) continue;
@@ -1331,6 +1331,7 @@ jsb_status jsb_autotune(jsb_context *ctx, float dt, int trials) {
                     case 0: b.state_mode = 1; break;  // positions only in shared memory: more CTAs per SM
                     case 1: b.state_mode = 1, b.threads = large ? 128 : 32; break;
                     case 2: b.state_mode = 1, b.threads = large ? 256 : 64; break;
+                    case 3: b.state_mode = 1, b.threads = large ? 512 : 64; break;
                     default: b.state_mode = 0, b.threads = large ? 128 : 32; break;
                 }
             }
@@ -1346,7 +1347,7 @@ jsb_status jsb_autotune(jsb_context *ctx, float dt, int trials) {
     }
     // Coordinate descent over each occupied bucket's (threads, state placement), largest bucket first,
     // for up to two rounds.
-    const int choices[4] = {32, 64, 128, 256};
+    const int choices[5] = {32, 64, 128, 256, 512};
     for (int round = 0; round < 2 && st == JSB_OK; ++round) {
         bool improved = false;
         for (auto it = occupied.rbegin(); st == JSB_OK && it != occupied.rend(); ++it) {
@@ -1497,7 +1498,6 @@ jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int chec
     JSB_CUDA(a->adj_v.alloc(ctx->total_vertices));
     JSB_CUDA(a->seed_dev.alloc(ctx->total_vertices));
     // One taped-forward / adjoint launch per launch group of the forward step.
-    const uint32_t T = uint32_t(adjoint_threads());
     int least = 0, greatest = 0;
     JSB_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     JSB_CUDA(cudaEventCreateWithFlags(&a->fork, cudaEventDisableTiming));
@@ -1522,21 +1522,24 @@ jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int chec
         while (ag.ring_slots > kMaxRingSlots && step_smem_bytes(ag.tape_smem_state, ag.cap_vertices, ag.cap_faces, ag.ring_slots) > cap)
             ag.ring_slots -= 32;
         const size_t tsmem = step_smem_bytes(ag.tape_smem_state, ag.cap_vertices, ag.cap_faces, ag.ring_slots);
-        if (adjoint_smem_bytes(ag.cap_vertices, ag.cap_faces, 0, 1) > cap || tsmem > cap)
+        ag.threads = ag.max_level_slots > 192 ? 256 : 128;
+        const uint32_t T = uint32_t(ag.threads);
+        if (adjoint_smem_bytes(ag.cap_vertices, ag.cap_faces, 0, 1, ag.threads) > cap || tsmem > cap)
             return fail(JSB_ERR_UNSUPPORTED, "a body is too large for the differentiable (taped) path");
         // Deepest adjoint ring (up to 3 levels ahead, up to 4 slots per thread) that fits beside the state.
         ag.adj_rpt = std::max<uint32_t>(1u, std::min<uint32_t>(4u, (ag.max_level_slots + T - 1) / T));
         ag.adj_depth = 3;
-        while (ag.adj_depth > 0 && adjoint_smem_bytes(ag.cap_vertices, ag.cap_faces, ag.adj_depth, ag.adj_rpt) > cap) {
+        while (ag.adj_depth > 0 && adjoint_smem_bytes(ag.cap_vertices, ag.cap_faces, ag.adj_depth, ag.adj_rpt, ag.threads) > cap) {
             if (ag.adj_rpt > 1)
                 --ag.adj_rpt;
             else
                 --ag.adj_depth;
         }
-        const size_t asmem = adjoint_smem_bytes(ag.cap_vertices, ag.cap_faces, ag.adj_depth, ag.adj_rpt);
+        const size_t asmem = adjoint_smem_bytes(ag.cap_vertices, ag.cap_faces, ag.adj_depth, ag.adj_rpt, ag.threads);
         ag.num_work = uint32_t(g.bodies.size());
-        ag.tape_grid = int(std::min<size_t>(ag.num_work, size_t(std::max(1, step_tape_occupancy(ag.tape_smem_state, tsmem))) * ctx->num_sms));
-        ag.adj_grid = int(std::min<size_t>(ag.num_work, size_t(std::max(1, adjoint_occupancy(asmem))) * ctx->num_sms));
+        ag.tape_grid = int(std::min<size_t>(
+            ag.num_work, size_t(std::max(1, step_tape_occupancy(ag.threads, ag.tape_smem_state, tsmem))) * ctx->num_sms));
+        ag.adj_grid = int(std::min<size_t>(ag.num_work, size_t(std::max(1, adjoint_occupancy(asmem, ag.threads))) * ctx->num_sms));
         JSB_CUDA(ag.work.upload(g.bodies.data(), g.bodies.size()));
         const int prio = (ng > 1 && greatest != least) ? least + (greatest - least) * gi / (ng - 1) : least;
         JSB_CUDA(cudaStreamCreateWithPriority(&ag.stream, cudaStreamNonBlocking, prio));

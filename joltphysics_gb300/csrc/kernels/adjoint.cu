@@ -579,9 +579,8 @@ __device__ void adjoint_body(const AdjParams &q, uint32_t b, float4 *smem, uint3
     __syncthreads();
 }
 
-constexpr int kAdjThreads = 128;
-
-__global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(AdjParams q, uint32_t cap, uint32_t cap_faces) {
+template <int T>
+__global__ void __launch_bounds__(T) adjoint_kernel(AdjParams q, uint32_t cap, uint32_t cap_faces) {
     extern __shared__ float4 smem[];
     __shared__ AdjShared sh;
     for (;;) {
@@ -590,7 +589,7 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(AdjParams q, uint3
         const uint32_t item = sh.item;
         __syncthreads();
         if (item >= q.num_work) return;
-        adjoint_body<kAdjThreads>(q, q.work[item], smem, cap, cap_faces, sh);
+        adjoint_body<T>(q, q.work[item], smem, cap, cap_faces, sh);
     }
 }
 
@@ -603,29 +602,36 @@ __global__ void add_kernel(float4 *__restrict__ dst, const float4 *__restrict__ 
 
 }  // namespace
 
-// Dynamic shared memory of the adjoint CTA: 3 adjoint arrays + inverse masses + pressure scratch +
-// the level ring of `depth` levels ahead with `rpt` slots per thread.
-size_t adjoint_smem_bytes(uint32_t vertices, uint32_t faces, uint32_t depth, uint32_t rpt) {
-    const size_t ring = depth > 0 ? size_t(depth + 1) * rpt * 4 * kAdjThreads * sizeof(uint4) : 0;
+// Dynamic shared memory of the adjoint CTA of `threads` threads: 3 adjoint arrays + inverse masses +
+// pressure scratch + the level ring of `depth` levels ahead with `rpt` slots per thread.
+size_t adjoint_smem_bytes(uint32_t vertices, uint32_t faces, uint32_t depth, uint32_t rpt, int threads) {
+    const size_t ring = depth > 0 ? size_t(depth + 1) * rpt * 4 * size_t(threads) * sizeof(uint4) : 0;
     return size_t(vertices) * sizeof(float4) * 3 + size_t((vertices + 3) / 4) * sizeof(float4) + size_t(faces) * sizeof(float4) +
            ring;
 }
 
-int adjoint_threads() { return kAdjThreads; }
-
 cudaError_t init_adjoint_kernels(int max_dynamic_smem) {
-    return cudaFuncSetAttribute(adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+    cudaError_t e = cudaFuncSetAttribute(adjoint_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(adjoint_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+    return e;
 }
 
-int adjoint_occupancy(size_t smem) {
+// threads: 128 or 256
+int adjoint_occupancy(size_t smem, int threads) {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, adjoint_kernel, kAdjThreads, smem);
+    if (threads == 256)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, adjoint_kernel<256>, 256, smem);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, adjoint_kernel<128>, 128, smem);
     return n;
 }
 
-cudaError_t launch_adjoint(const AdjParams &q, uint32_t cap_vertices, uint32_t cap_faces, int grid, cudaStream_t stream) {
-    adjoint_kernel<<<grid, kAdjThreads, adjoint_smem_bytes(cap_vertices, cap_faces, q.ring_depth, q.ring_rpt), stream>>>(
-        q, cap_vertices, cap_faces);
+cudaError_t launch_adjoint(const AdjParams &q, uint32_t cap_vertices, uint32_t cap_faces, int grid, int threads, cudaStream_t stream) {
+    const size_t smem = adjoint_smem_bytes(cap_vertices, cap_faces, q.ring_depth, q.ring_rpt, threads);
+    if (threads == 256)
+        adjoint_kernel<256><<<grid, 256, smem, stream>>>(q, cap_vertices, cap_faces);
+    else
+        adjoint_kernel<128><<<grid, 128, smem, stream>>>(q, cap_vertices, cap_faces);
     return cudaGetLastError();
 }
 

@@ -532,11 +532,11 @@ __global__ void __launch_bounds__(T, 512 / T) step_kernel(StepParams p, uint32_t
 
 // The taped forward step (differentiable runs) holds more live values; one CTA per SM lets it keep
 // them in registers.
-template <bool kSmemState>
-__global__ void __launch_bounds__(128, 1) step_kernel_tape(StepParams p, uint32_t cap) {
+template <int T, bool kSmemState>
+__global__ void __launch_bounds__(T, 1) step_kernel_tape(StepParams p, uint32_t cap) {
     extern __shared__ float4 smem[];
     __shared__ Shared sh;
-    step_queue<128, kSmemState, true>(p, cap, smem, sh);
+    step_queue<T, kSmemState, true>(p, cap, smem, sh);
 }
 
 }  // namespace
@@ -549,7 +549,8 @@ size_t step_smem_bytes(bool smem_state, uint32_t vertices, uint32_t faces, uint3
     return size_t(vertices) * sizeof(float4) * (smem_state ? 3 : 1) + (faces_bytes > ring_bytes ? faces_bytes : ring_bytes);
 }
 
-#define JSB_FOR_EACH_SHAPE(X) X(32, true) X(64, true) X(128, true) X(256, true) X(32, false) X(64, false) X(128, false) X(256, false)
+#define JSB_FOR_EACH_SHAPE(X) \
+    X(32, true) X(64, true) X(128, true) X(256, true) X(512, true) X(32, false) X(64, false) X(128, false) X(256, false) X(512, false)
 
 // Launches one persistent step over `p.num_work` bodies with `threads` threads per CTA.
 cudaError_t launch_step(const StepParams &p, int threads, bool smem_state, uint32_t smem_vertices, uint32_t smem_faces, int grid,
@@ -565,23 +566,28 @@ cudaError_t launch_step(const StepParams &p, int threads, bool smem_state, uint3
     return cudaErrorInvalidValue;
 }
 
-// Taped forward step (differentiable runs): 128 threads per CTA, every body of the launch.
-cudaError_t launch_step_tape(const StepParams &p, bool smem_state, uint32_t smem_vertices, uint32_t smem_faces, int grid,
+#define JSB_FOR_EACH_TAPE_SHAPE(X) X(128, true) X(256, true) X(128, false) X(256, false)
+
+// Taped forward step (differentiable runs): 128 or 256 threads per CTA, every body of the launch.
+cudaError_t launch_step_tape(const StepParams &p, int threads, bool smem_state, uint32_t smem_vertices, uint32_t smem_faces, int grid,
                              cudaStream_t stream) {
     size_t smem = step_smem_bytes(smem_state, smem_vertices, smem_faces, p.ring_slots);
-    if (smem_state)
-        step_kernel_tape<true><<<grid, 128, smem, stream>>>(p, smem_vertices);
-    else
-        step_kernel_tape<false><<<grid, 128, smem, stream>>>(p, smem_vertices);
-    return cudaGetLastError();
+#define JSB_LAUNCH_TAPE(TT, SS)                                                   \
+    if (threads == TT && smem_state == SS) {                                      \
+        step_kernel_tape<TT, SS><<<grid, TT, smem, stream>>>(p, smem_vertices);   \
+        return cudaGetLastError();                                                \
+    }
+    JSB_FOR_EACH_TAPE_SHAPE(JSB_LAUNCH_TAPE)
+#undef JSB_LAUNCH_TAPE
+    return cudaErrorInvalidValue;
 }
 
-int step_tape_occupancy(bool smem_state, size_t smem) {
+int step_tape_occupancy(int threads, bool smem_state, size_t smem) {
     int n = 0;
-    if (smem_state)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel_tape<true>, 128, smem);
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel_tape<false>, 128, smem);
+#define JSB_OCC_TAPE(TT, SS) \
+    if (threads == TT && smem_state == SS) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel_tape<TT, SS>, TT, smem);
+    JSB_FOR_EACH_TAPE_SHAPE(JSB_OCC_TAPE)
+#undef JSB_OCC_TAPE
     return n;
 }
 
@@ -593,8 +599,10 @@ cudaError_t init_step_kernels(int max_dynamic_smem) {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel<TT, SS>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
     JSB_FOR_EACH_SHAPE(JSB_ATTR)
 #undef JSB_ATTR
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel_tape<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel_tape<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+#define JSB_ATTR_TAPE(TT, SS) \
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(step_kernel_tape<TT, SS>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem);
+    JSB_FOR_EACH_TAPE_SHAPE(JSB_ATTR_TAPE)
+#undef JSB_ATTR_TAPE
     return e;
 }
 

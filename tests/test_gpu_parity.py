@@ -235,12 +235,12 @@ def test_nan_propagation_matches_oracle(jsb, path):
                     assert np.array_equal(snap[b][k], ref[k]), (b, k)
 
 
-@pytest.mark.parametrize("state_mode", [0, 1])
-def test_step_walk_equals_substep_walk_and_oracle(jsb, state_mode):
+@pytest.mark.parametrize("state_mode,threads", [(0, 0), (1, 0), (0, 512), (1, 512)])
+def test_step_walk_equals_substep_walk_and_oracle(jsb, state_mode, threads):
     """Whole-step walk (default) against the per-substep walk and the oracle, through contact: bodies of
     the uneven batch's full size ranges drop onto the floor (cubes land, pinned cloths hang), 90
     steps; state_mode 1 keeps velocities and previous positions in HBM, which the per-vertex passes
-    inside the walk then read and write there."""
+    inside the walk then read and write there; threads 512 (else the default table's) per CTA."""
     scene_bytes = jsb.build_scene("uneven_batch", n_cloth=10, n_cube=6, steps=90, seed=11)
     scene, _ = parse_scene(scene_bytes)
     a = make_ctx(jsb, scene_bytes)
@@ -249,7 +249,7 @@ def test_step_walk_equals_substep_walk_and_oracle(jsb, state_mode):
     b.load_scene(scene_bytes)
     for ctx in (a, b):
         for mv, t, _ in ctx.bucket_table():
-            ctx.set_bucket_config(mv, t, state_mode)
+            ctx.set_bucket_config(mv, threads or t, state_mode)
     o = Oracle(scene)
     cur = 0
     for step in (1, 45, 90):
