@@ -424,6 +424,8 @@ def profile_driver(args) -> None:
         return
     ctx = jsb.Context(0)
     ctx.load_scene(jsb.build_scene(args.profile))
+    for mv, threads, mode in json.loads(args.table or "[]"):
+        ctx.set_bucket_config(mv, threads, mode)
     for _ in range(args.warmup + args.steps):
         ctx.step()
     ctx.synchronize()
@@ -440,6 +442,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and large-body measurements")
     ap.add_argument("--large-steps", type=int, default=10)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch-shape table")
+    ap.add_argument("--table", help="profiling driver: launch-shape table [[max_vertices, threads, state_mode], ...] "
+                                    "(e.g. the bench line's config.buckets_max_vertices_threads_state)")
     ap.add_argument("--profile", choices=["uneven_batch", "large_cloth", "diff_batch_adjoint"],
                     help="profiling driver for ncu: run --warmup then --steps steps of one workload, print nothing")
     args = ap.parse_args()
