@@ -31,13 +31,18 @@ namespace jsb {
 namespace {
 
 
+// Level descriptors are staged this many levels ahead of the record staging into a ring of
+// kDescRing entries, so no level waits on a descriptor load from L2 / HBM.
+constexpr uint32_t kDescAhead = 8;
+constexpr uint32_t kDescRing = 16;
+
 struct Shared {
     SCol cols[kMaxCollidingShapes];
     int ncols;
     uint32_t item;
     float six_volume;
     float delta[3];
-    uint4 ring_desc[4];
+    uint4 ring_desc[kDescRing];
     int last_nan[6];
     float red[32][4];  // per-warp partials for reductions
     int redi[32][4];
@@ -51,22 +56,34 @@ constexpr int kRingLevels = kRingDepth + 1;
 
 struct LevelRing {
     uint4 *rec;      // [kRingLevels][slots]
-    uint4 *desc;     // [kRingLevels] level descriptors
+    uint4 *desc;     // [kDescRing] level descriptors, staged kDescAhead levels ahead of the records
     uint32_t slots;  // capacity per level
 };
 
-// Stages level `idx` (descriptor, and its records when they fit a ring slot) into ring position
-// idx % kRingLevels. idx == num_levels stages the sentinel descriptor only.
+// Descriptor ring. The first kDescAhead descriptors are stored directly (visible after the next
+// barrier); descriptor kDescAhead + j is copied by thread 0 with cp.async in the group of iteration
+// j - kRingDepth of the walk (the prologue's groups first). A thread's wait_group<kRingDepth - 1> at
+// the end of iteration l completes its groups up to iteration l - 2, so descriptors up to
+// l + kDescAhead + 1 have landed before the barrier that ends iteration l, well ahead of their first
+// use (staging level l + 1 + kRingDepth in iteration l + 1). An entry is overwritten kDescRing -
+// kDescAhead - kRingDepth levels after its last read.
+__device__ __forceinline__ void desc_prologue(const LevelRing &ring, const uint4 *__restrict__ levels, uint32_t count) {
+    if (threadIdx.x < kDescAhead && threadIdx.x < count) ring.desc[threadIdx.x] = __ldg(levels + threadIdx.x);
+}
+__device__ __forceinline__ void desc_stage(const LevelRing &ring, const uint4 *__restrict__ levels, uint32_t idx, uint32_t count) {
+    if (threadIdx.x == 0 && idx < count) cp_async16(ring.desc + idx % kDescRing, levels + idx);
+}
+__device__ __forceinline__ uint4 desc_at(const LevelRing &ring, uint32_t idx) { return ring.desc[idx % kDescRing]; }
+
+// Stages the records of per-substep level `idx` (< L) into ring position idx % kRingLevels when they
+// fit a ring slot (wider levels are read in place).
 template <int T>
-__device__ __forceinline__ void ring_stage(const LevelRing &ring, const uint4 *__restrict__ levels, const uint4 *__restrict__ rec,
-                                           uint32_t idx, uint32_t L, uint4 lv, uint32_t next_first) {
+__device__ __forceinline__ void ring_stage(const LevelRing &ring, const uint4 *__restrict__ rec, uint32_t idx, uint4 lv,
+                                           uint32_t next_first) {
     const uint32_t pos = idx % kRingLevels;
-    if (idx < L) {
-        const uint32_t n = next_first - lv.x;
-        if (n <= ring.slots)
-            for (uint32_t s = threadIdx.x; s < n; s += T) cp_async16(ring.rec + pos * ring.slots + s, rec + lv.x + s);
-    }
-    if (threadIdx.x == 0) ring.desc[pos] = lv;
+    const uint32_t n = next_first - lv.x;
+    if (n <= ring.slots)
+        for (uint32_t s = threadIdx.x; s < n; s += T) cp_async16(ring.rec + pos * ring.slots + s, rec + lv.x + s);
 }
 
 // Walks the dependency levels of one substep. Level l + kRingDepth is staged (cp.async) while level
@@ -92,25 +109,23 @@ __device__ __forceinline__ void apply_levels(float4 *sx, const BodyDesc &d, floa
     const uint32_t tid = threadIdx.x;
     const uint32_t L = d.num_levels;
     if (L == 0) return;
-    // prologue: stage levels 0 .. kRingDepth - 1 (levels has L + 2 entries)
+    const uint32_t count = L + 2;  // descriptors, with two sentinels
+    desc_prologue(ring, levels, count);
+    __syncthreads();
+    // prologue: stage the records of levels 0 .. kRingDepth - 1
 #pragma unroll
     for (int k = 0; k < kRingDepth; ++k) {
-        if (uint32_t(k) <= L) ring_stage<T>(ring, levels, rec, k, L, __ldg(levels + k), __ldg(levels + k + 1).x);
+        if (uint32_t(k) < L) ring_stage<T>(ring, rec, k, desc_at(ring, k), desc_at(ring, k + 1).x);
+        desc_stage(ring, levels, kDescAhead + k, count);
         cp_async_commit();
     }
     cp_async_wait<kRingDepth - 1>();
     __syncthreads();
     for (uint32_t l = 0; l < L; ++l) {
         const uint32_t ahead = l + kRingDepth;
-        uint4 lv_ahead = make_uint4(0, 0, 0, 0);
-        uint32_t next_ahead = 0;
-        if (ahead <= L) {
-            lv_ahead = __ldg(levels + ahead);
-            next_ahead = __ldg(levels + ahead + 1).x;
-        }
         const uint32_t pos = l % kRingLevels;
-        const uint4 lv = ring.desc[pos];
-        const uint32_t n = ring.desc[(l + 1) % kRingLevels].x - lv.x;
+        const uint4 lv = desc_at(ring, l);
+        const uint32_t n = desc_at(ring, l + 1).x - lv.x;
         const bool in_ring = n <= ring.slots;
         const uint4 *src = in_ring ? ring.rec + pos * ring.slots : rec + lv.x;
         for (uint32_t s = tid; s < n; s += T) {
@@ -120,12 +135,14 @@ __device__ __forceinline__ void apply_levels(float4 *sx, const BodyDesc &d, floa
                 project<kGuard>(sx, r, slot_type(lv, s), inv_dt_sq);
             }
         }
-        if (ahead <= L) ring_stage<T>(ring, levels, rec, ahead, L, lv_ahead, next_ahead);
+        if (ahead < L) ring_stage<T>(ring, rec, ahead, desc_at(ring, ahead), desc_at(ring, ahead + 1).x);
+        desc_stage(ring, levels, ahead + kDescAhead, count);
         cp_async_commit();
         cp_async_wait<kRingDepth - 1>();
         cta_sync<T>();
     }
     cp_async_wait<0>();
+    __syncthreads();  // the descriptor ring is reused by the next walk
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -184,14 +201,13 @@ __device__ __forceinline__ void vertex_between_substeps(float4 *sx, const Vertex
     sx[i] = with_w(xyz(pi) + xyz(vel) * vp.dt_sub, pi.w);
 }
 
-// Stages the first ring.slots records of whole-step level `idx` and its descriptor; slots beyond the
-// ring's capacity are read in place by the walker.
+// Stages the first ring.slots records of whole-step level `idx`; slots beyond the ring's capacity are
+// read in place by the walker.
 template <int T>
 __device__ __forceinline__ void step_ring_stage(const LevelRing &ring, const uint4 *__restrict__ rec, uint32_t idx, uint4 lv) {
     const uint32_t pos = idx % kRingLevels;
     const uint32_t n = lv.w < ring.slots ? lv.w : ring.slots;
     for (uint32_t s = threadIdx.x; s < n; s += T) cp_async16(ring.rec + pos * ring.slots + s, rec + lv.x + s);
-    if (threadIdx.x == 0) ring.desc[pos] = lv;
 }
 
 // tape_cons (taped forward): this step's constraint inputs, 3 float4 per whole-step slot.
@@ -203,19 +219,20 @@ __device__ __forceinline__ void apply_step_levels(float4 *sx, const BodyDesc &d,
     const uint32_t tid = threadIdx.x;
     const uint32_t L = d.num_step_levels;
     if (L == 0) return;
+    desc_prologue(ring, levels, L);
+    __syncthreads();
 #pragma unroll
     for (int k = 0; k < kRingDepth; ++k) {
-        if (uint32_t(k) < L) step_ring_stage<T>(ring, rec, k, __ldg(levels + k));
+        if (uint32_t(k) < L) step_ring_stage<T>(ring, rec, k, desc_at(ring, k));
+        desc_stage(ring, levels, kDescAhead + k, L);
         cp_async_commit();
     }
     cp_async_wait<kRingDepth - 1>();
     __syncthreads();
     for (uint32_t l = 0; l < L; ++l) {
         const uint32_t ahead = l + kRingDepth;
-        uint4 lv_ahead = make_uint4(0, 0, 0, 0);
-        if (ahead < L) lv_ahead = __ldg(levels + ahead);
         const uint32_t pos = l % kRingLevels;
-        const uint4 lv = ring.desc[pos];
+        const uint4 lv = desc_at(ring, l);
         const uint4 *ring_rec = ring.rec + pos * ring.slots;
         for (uint32_t s = tid; s < lv.w; s += T) {
             const uint4 r = s < ring.slots ? ring_rec[s] : __ldg(rec + lv.x + s);
@@ -229,12 +246,14 @@ __device__ __forceinline__ void apply_step_levels(float4 *sx, const BodyDesc &d,
                 }
             }
         }
-        if (ahead < L) step_ring_stage<T>(ring, rec, ahead, lv_ahead);
+        if (ahead < L) step_ring_stage<T>(ring, rec, ahead, desc_at(ring, ahead));
+        desc_stage(ring, levels, ahead + kDescAhead, L);
         cp_async_commit();
         cp_async_wait<kRingDepth - 1>();
         cta_sync<T>();
     }
     cp_async_wait<0>();
+    __syncthreads();  // the descriptor ring is reused by the next walk
 }
 
 
