@@ -330,7 +330,7 @@ def bench_pinned_cloth(jsb, torch, stream, with_cpu: bool, autotune: bool = True
     ctx.load_scene(scene_bytes)
     if autotune:
         initial = ctx.save_all()
-        ctx.autotune(trials=3)
+        ctx.autotune(trials=5)
         ctx.restore_all(initial)
     sptr = stream.cuda_stream
     steps = ctx.scene_steps
@@ -487,7 +487,7 @@ def main():
     # autotune the launch shape per body-size bucket, then warm up (graph of one step)
     initial = ctx.save_all()
     if not args.no_autotune:
-        ctx.autotune(trials=3)
+        ctx.autotune(trials=5)
     buckets = [b for b in ctx.bucket_table()]
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):

@@ -750,8 +750,11 @@ jsb_status jsb_context_create(int device, jsb_context **out) {
     ctx->device = device;
     ctx->num_sms = prop.multiProcessorCount;
     ctx->max_smem_optin = prop.sharedMemPerBlockOptin;
-    ctx->buckets = {{128, 32, 0},   {256, 32, 0},   {512, 32, 0},   {1024, 64, 0},  {1536, 64, 0},
-                    {2048, 64, 0},  {3072, 128, 0}, {4096, 128, 0}, {8192, 128, 0}, {65536, 128, 0}};
+    // Default launch shapes (the autotuner starts from this table and keeps only measured gains): wide
+    // CTAs with only positions in shared memory for the larger bodies, whose whole-step levels hold up
+    // to a few hundred slots; small CTAs for small bodies, many to an SM.
+    ctx->buckets = {{128, 64, 1},   {256, 64, 1},   {512, 128, 1},  {1024, 256, 1}, {1536, 256, 1},
+                    {2048, 256, 1}, {3072, 256, 1}, {4096, 256, 1}, {8192, 256, 1}, {65536, 256, 1}};
     // static shared memory of the solver kernel is under 4 KB
     JSB_CUDA(init_step_kernels(int(ctx->max_smem_optin - kStaticSmemReserve)));
     JSB_CUDA(init_adjoint_kernels(int(ctx->max_smem_optin - kStaticSmemReserve)));
