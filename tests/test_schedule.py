@@ -176,3 +176,23 @@ def test_step_schedule_shortens_the_chain(jsb):
     levels, _, _ = jsb.settings_step_schedule(b.blob, b.num_iterations)
     assert len(levels) < 0.6 * b.num_iterations * per_substep
     assert jsb.settings_step_schedule(b.blob, 1) is None
+
+
+def test_step_schedule_declines_levels_beyond_16_bits(jsb):
+    """A level of 65,536 slots or more does not fit the packed level descriptor: the builder declines and
+    the body walks every substep instead. Unconstrained vertices put all their per-vertex slots between
+    substeps 0 and 1 into one level, padded to a multiple of 32: 65,505 of them need 65,536 slots,
+    65,504 fit."""
+    import struct
+
+    def blob(nv):
+        b = struct.pack("<I", nv) + struct.pack("<7f", 0, 0, 0, 0, 0, 0, 1.0) * nv
+        b += struct.pack("<I", 0) * 5  # faces, edges, bends, volumes, skinned
+        b += struct.pack("<I", 0) + struct.pack("<I", 0)  # skinned normals, LRA
+        b += struct.pack("<I", 1) + struct.pack("<7I", 0, 0, 0, 0, 0, 0, 0)  # one (empty) update group
+        b += struct.pack("<I", 0) * 3  # rods, inverse bind matrices
+        return b
+
+    assert jsb.settings_step_schedule(blob(65505), 2) is None
+    levels, records, source = jsb.settings_step_schedule(blob(65504), 2)
+    assert len(levels) == 1 and levels[0][3] == 65504 and (source[:, 0] >> 28 == 4).all()
