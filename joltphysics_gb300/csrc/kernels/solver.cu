@@ -43,11 +43,48 @@ struct Shared {
     float six_volume;
     float delta[3];
     uint4 ring_desc[kDescRing];
+    uint64_t stage_bar;  // mbarrier of the bulk copies that stage a body's state (one phase per body)
     int last_nan[6];
     float red[32][4];  // per-warp partials for reductions
     int redi[32][4];
 };
 
+
+// ---- state staging: bulk copies on the TMA unit, completion on an mbarrier ----------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return uint32_t(__cvta_generic_to_shared(p)); }
+
+// Once per CTA, thread 0; the caller's barrier publishes it.
+__device__ __forceinline__ void stage_bar_init(uint64_t *bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Thread 0: announces `bytes` for the barrier's current phase (its single arrival).
+__device__ __forceinline__ void stage_expect(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// Thread 0: one bulk copy of `bytes` (a non-zero multiple of 16; both addresses 16-byte aligned) from
+// global into shared memory, counted on `bar`.
+__device__ __forceinline__ void stage_copy(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Waits (bounded: about 2^20 polls) for phase `parity` of `bar`; false when it gave up.
+__device__ __forceinline__ bool stage_wait(uint64_t *bar, uint32_t parity) {
+    for (uint32_t it = 0; it < (1u << 20); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
 
 // Record ring: kRingDepth levels of up to `slots` records each are streamed into shared memory
 // ahead of the level being projected; the ring holds kRingDepth + 1 levels.
@@ -264,8 +301,9 @@ __device__ __forceinline__ void apply_step_levels(float4 *sx, const BodyDesc &d,
 //   kSmemState:  x[cap] | v[cap] (shape index in v.w) | prev[cap] | faces[...]
 //   otherwise:   x[cap] | faces[...]       (v, prev, shape stay in HBM)
 // faces: per-face triple product, then per-face pressure impulse (pressure bodies only).
+// `phase`: parity of the staging barrier's current phase (flips once per body; the same in every thread).
 template <int T, bool kSmemState, bool kTape = false>
-__device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_t cap, Shared &sh) {
+__device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_t cap, Shared &sh, uint32_t &phase) {
     const uint32_t tid = threadIdx.x;
     const BodyDesc d = p.bodies[b];
     BodyState *st = p.states + b;
@@ -306,11 +344,27 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
             for (int k = 0; k < n; ++k)
                 td.cols[size_t(p.tape_step) * kMaxCollidingShapes + k] = make_float2(sh.cols[k].friction, sh.cols[k].restitution);
     }
-    // Stage the state in shared memory.
-    for (uint32_t i = tid; i < nv; i += T) {
-        sx[i] = gx[i];
-        if (kSmemState) sv[i] = gv[i];
+    // Stage the state in shared memory: one bulk copy per array (TMA unit), completing on the staging
+    // barrier. The fence orders this CTA's earlier accesses of the destination (the previous body)
+    // before the copies.
+    if (tid == 0) {
+        const uint32_t bytes = nv * uint32_t(sizeof(float4));
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        stage_expect(&sh.stage_bar, kSmemState ? 2 * bytes : bytes);
+        if (bytes > 0) {
+            stage_copy(sx, gx, bytes, &sh.stage_bar);
+            if (kSmemState) stage_copy(sv, gv, bytes, &sh.stage_bar);
+        }
     }
+    if (!stage_wait(&sh.stage_bar, phase)) {
+        // never expected; report it, and stage with plain loads (the copies carry the same bytes)
+        if (tid == 0) atomicOr(p.error, kErrTimeout);
+        for (uint32_t i = tid; i < nv; i += T) {
+            sx[i] = gx[i];
+            if (kSmemState) sv[i] = gv[i];
+        }
+    }
+    phase ^= 1u;
     __syncthreads();
 
     // DetermineCollisionPlanes (per vertex, once per step)
@@ -530,13 +584,15 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
 
 template <int T, bool kSmemState, bool kTape>
 __device__ __forceinline__ void step_queue(const StepParams &p, uint32_t cap, float4 *smem, Shared &sh) {
+    if (threadIdx.x == 0) stage_bar_init(&sh.stage_bar);
+    uint32_t phase = 0;
     for (;;) {
         if (threadIdx.x == 0) sh.item = atomicAdd(p.queue, 1u);
         __syncthreads();
         const uint32_t item = sh.item;
         __syncthreads();
         if (item >= p.num_work) return;
-        step_body<T, kSmemState, kTape>(p, p.work[item], smem, cap, sh);
+        step_body<T, kSmemState, kTape>(p, p.work[item], smem, cap, sh, phase);
     }
 }
 
@@ -720,7 +776,10 @@ __global__ void __launch_bounds__(T) step_kernel_noalloc(const __grid_constant__
     p.forces = q.force;
     p.step_forces = q.zero3;
     p.ring_slots = 256;
-    step_body<T, kSmemState>(p, 0, smem, cap, sh);
+    if (threadIdx.x == 0) stage_bar_init(&sh.stage_bar);
+    __syncthreads();
+    uint32_t phase = 0;
+    step_body<T, kSmemState>(p, 0, smem, cap, sh, phase);
 }
 
 constexpr int kThreads = 128;
