@@ -183,7 +183,8 @@ jsb_status jsb_set_cluster_config(jsb_context *ctx, uint32_t cluster_size, uint3
  * velocity update of the substep it leaves and the integration of the next one right after its own last
  * constraint (ApplyCollisionConstraintsAndUpdateVelocities and IntegratePositions are per-vertex passes,
  * SoftBodyMotionProperties.cpp:325-365, 700-825), so substeps overlap. Results are bitwise those of the
- * per-substep walk (enable = 0), which pressurised bodies, differentiable runs and the cluster path keep. */
+ * per-substep walk (enable = 0), which pressurised bodies and the cluster path keep; differentiable runs
+ * tape and reverse the whole-step walk. It cannot change during a differentiable run. */
 jsb_status jsb_set_step_walk(jsb_context *ctx, int enable);
 jsb_status jsb_get_cluster_config(jsb_context *ctx, uint32_t *cluster_size, uint32_t *threads, uint32_t *num_bodies);
 jsb_status jsb_get_bucket_config(jsb_context *ctx, uint32_t index, uint32_t *max_vertices, uint32_t *threads,
@@ -237,6 +238,8 @@ jsb_status jsb_adjoint_seed_all(jsb_context *ctx, int step, const float *dl_dx);
 jsb_status jsb_adjoint_gradients_all(jsb_context *ctx, float *dl_dx0, float *dl_dv0, float *dl_dforce);
 jsb_status jsb_adjoint_gradients(jsb_context *ctx, uint32_t body_id, float *dl_dx0, float *dl_dv0, float *dl_dforce,
                                  float *dl_dedge_compliance, float *dl_dvolume_compliance);
+/* Ends the run. Its device buffers (tape, checkpoints, adjoints) stay with the context and are reused,
+ * grown when needed, by its next differentiable run; jsb_context_destroy frees them. */
 jsb_status jsb_adjoint_end(jsb_context *ctx);
 
 /* ---- allocation-free single-body step -------------------------------------------------------- */

@@ -73,21 +73,23 @@ jsb_status fail(jsb_status code, const std::string &msg) {
 template <class T>
 struct DevBuf {
     T *ptr = nullptr;
-    size_t count = 0;
+    size_t count = 0;     // elements in use
+    size_t capacity = 0;  // elements allocated
     DevBuf() = default;
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
-    DevBuf(DevBuf &&o) noexcept : ptr(o.ptr), count(o.count) {
+    DevBuf(DevBuf &&o) noexcept : ptr(o.ptr), count(o.count), capacity(o.capacity) {
         o.ptr = nullptr;
-        o.count = 0;
+        o.count = o.capacity = 0;
     }
     DevBuf &operator=(DevBuf &&o) noexcept {
         if (this != &o) {
             reset();
             ptr = o.ptr;
             count = o.count;
+            capacity = o.capacity;
             o.ptr = nullptr;
-            o.count = 0;
+            o.count = o.capacity = 0;
         }
         return *this;
     }
@@ -95,14 +97,22 @@ struct DevBuf {
     void reset() {
         if (ptr) cudaFree(ptr);
         ptr = nullptr;
-        count = 0;
+        count = capacity = 0;
     }
     cudaError_t alloc(size_t n) {
         reset();
         if (n == 0) return cudaSuccess;
         cudaError_t e = cudaMalloc(&ptr, n * sizeof(T));
-        if (e == cudaSuccess) count = n;
+        if (e == cudaSuccess) count = capacity = n;
         return e;
+    }
+    // Keeps the allocation when it is large enough (contents undefined), else allocates anew.
+    cudaError_t ensure(size_t n) {
+        if (ptr && n <= capacity) {
+            count = n;
+            return cudaSuccess;
+        }
+        return alloc(n);
     }
     cudaError_t upload(const T *src, size_t n) {
         cudaError_t e = alloc(n);
@@ -173,12 +183,15 @@ struct AdjGroup {
 // State of one differentiable run (jsb_adjoint_*): checkpoints every `every` steps, the tape of one
 // checkpoint segment, adjoint accumulators and loss seeds.
 struct AdjointSession {
-    ~AdjointSession() {
+    ~AdjointSession() { release_launch_groups(); }
+    void release_launch_groups() {
         for (AdjGroup &g : groups) {
             if (g.stream) cudaStreamDestroy(g.stream);
             if (g.done) cudaEventDestroy(g.done);
         }
+        groups.clear();
         if (fork) cudaEventDestroy(fork);
+        fork = nullptr;
     }
     std::vector<AdjGroup> groups;
     cudaEvent_t fork = nullptr;
@@ -243,6 +256,7 @@ struct jsb_context {
     std::vector<uint32_t> single_work_host;
     jsb::DevBuf<uint32_t> single_work;  // identity list for the plain form
     std::unique_ptr<jsb::AdjointSession> adjoint;
+    std::unique_ptr<jsb::AdjointSession> adjoint_spare;  // device buffers of the last run, reused by the next
     cudaEvent_t fork = nullptr;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
@@ -1421,9 +1435,9 @@ namespace {
 
 jsb_status save_state(jsb_context *ctx, DevBuf<float4> &x, DevBuf<float4> &v, DevBuf<BodyState> &st) {
     const uint64_t n = ctx->total_vertices;
-    if (x.count != n) JSB_CUDA(x.alloc(n));
-    if (v.count != n) JSB_CUDA(v.alloc(n));
-    if (st.count != ctx->bodies.size()) JSB_CUDA(st.alloc(ctx->bodies.size()));
+    JSB_CUDA(x.ensure(n));
+    JSB_CUDA(v.ensure(n));
+    JSB_CUDA(st.ensure(ctx->bodies.size()));
     JSB_CUDA(cudaMemcpy(x.ptr, ctx->x.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice));
     JSB_CUDA(cudaMemcpy(v.ptr, ctx->v.ptr, n * sizeof(float4), cudaMemcpyDeviceToDevice));
     JSB_CUDA(cudaMemcpy(st.ptr, ctx->states.ptr, ctx->bodies.size() * sizeof(BodyState), cudaMemcpyDeviceToDevice));
@@ -1453,7 +1467,29 @@ jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int chec
         if (!ctx->settings[ctx->bodies[b].settings_id]->parsed.bends.empty())
             return fail(JSB_ERR_UNSUPPORTED, "body " + std::to_string(b) +
                                                  " has dihedral bend constraints, which differentiable runs do not support");
+    // Reuse the device buffers of the context's previous differentiable run (tape, checkpoints, adjoints):
+    // allocating gigabytes of tape costs time every run otherwise.
     auto a = std::make_unique<AdjointSession>();
+    if (ctx->adjoint_spare) {
+        AdjointSession &o = *ctx->adjoint_spare;
+        a->tape_cons = std::move(o.tape_cons);
+        a->tape_state = std::move(o.tape_state);
+        a->tape_plane = std::move(o.tape_plane);
+        a->tape_shape = std::move(o.tape_shape);
+        a->tape_cols = std::move(o.tape_cols);
+        a->grad_slots = std::move(o.grad_slots);
+        a->grad_force = std::move(o.grad_force);
+        a->adj_x = std::move(o.adj_x);
+        a->adj_v = std::move(o.adj_v);
+        a->seed_dev = std::move(o.seed_dev);
+        a->final_x = std::move(o.final_x);
+        a->final_v = std::move(o.final_v);
+        a->final_state = std::move(o.final_state);
+        a->ckpt_x = std::move(o.ckpt_x);
+        a->ckpt_v = std::move(o.ckpt_v);
+        a->ckpt_state = std::move(o.ckpt_state);
+        ctx->adjoint_spare.reset();
+    }
     a->dt = dt;
     a->steps = num_steps;
     a->every = std::min(checkpoint_every, num_steps);
@@ -1479,13 +1515,13 @@ jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int chec
         planes += K * nv;
         slots += a->step_slots[b] ? a->step_slots[b] : ns;
     }
-    JSB_CUDA(a->tape_cons.alloc(cons));
-    JSB_CUDA(a->tape_state.alloc(state));
-    JSB_CUDA(a->tape_plane.alloc(planes));
-    JSB_CUDA(a->tape_shape.alloc(planes));
-    JSB_CUDA(a->tape_cols.alloc(nb * K * kMaxCollidingShapes));
-    JSB_CUDA(a->grad_slots.alloc(std::max<size_t>(slots, 1)));
-    JSB_CUDA(a->grad_force.alloc(nb * 3));
+    JSB_CUDA(a->tape_cons.ensure(cons));
+    JSB_CUDA(a->tape_state.ensure(state));
+    JSB_CUDA(a->tape_plane.ensure(planes));
+    JSB_CUDA(a->tape_shape.ensure(planes));
+    JSB_CUDA(a->tape_cols.ensure(nb * K * kMaxCollidingShapes));
+    JSB_CUDA(a->grad_slots.ensure(std::max<size_t>(slots, 1)));
+    JSB_CUDA(a->grad_force.ensure(nb * 3));
     for (size_t b = 0; b < nb; ++b) {
         desc[b].cons = a->tape_cons.ptr + cons_off[b];
         desc[b].state = a->tape_state.ptr + state_off[b];
@@ -1497,9 +1533,9 @@ jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int chec
         desc[b].step_slots = a->step_slots[b];
     }
     JSB_CUDA(a->tape_desc.upload(desc.data(), nb));
-    JSB_CUDA(a->adj_x.alloc(ctx->total_vertices));
-    JSB_CUDA(a->adj_v.alloc(ctx->total_vertices));
-    JSB_CUDA(a->seed_dev.alloc(ctx->total_vertices));
+    JSB_CUDA(a->adj_x.ensure(ctx->total_vertices));
+    JSB_CUDA(a->adj_v.ensure(ctx->total_vertices));
+    JSB_CUDA(a->seed_dev.ensure(ctx->total_vertices));
     // One taped-forward / adjoint launch per launch group of the forward step.
     int least = 0, greatest = 0;
     JSB_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
@@ -1755,7 +1791,10 @@ jsb_status jsb_adjoint_end(jsb_context *ctx) {
     if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
-    ctx->adjoint.reset();
+    if (ctx->adjoint) {  // keep the device buffers for the next differentiable run of this context
+        ctx->adjoint->release_launch_groups();
+        ctx->adjoint_spare = std::move(ctx->adjoint);
+    }
     return JSB_OK;
 }
 

@@ -241,3 +241,35 @@ def test_step_walk_adjoint_equals_substep_walk(jsb):
             x, y = np.asarray(ga[key], np.float64), np.asarray(gb[key], np.float64)
             if y.size:
                 assert np.linalg.norm(x - y) <= 1e-5 * max(np.linalg.norm(y), 1e-30), (i, key)
+
+
+def test_runs_in_one_context_reuse_buffers(jsb):
+    """jsb_adjoint_end keeps the run's device buffers for the context's next differentiable run: a run,
+    then one of another length and checkpoint interval (buffers grow and shrink), then the first again
+    from the same state give bit-identical gradients."""
+    scene_bytes = jsb.build_scene("diff_batch", n_cloth=3, n_cube=2, steps=12)
+    scene, _ = parse_scene(scene_bytes)
+    rng = np.random.default_rng(21)
+    n = sum(b.num_vertices for b in scene.bodies)
+    seed = rng.standard_normal((n, 3)).astype(np.float32)
+    ctx = jsb.Context(0)
+    ctx.load_scene(scene_bytes)
+    ctx.set_scene_step_forces()
+    init = ctx.save_all()
+
+    def run(steps, every):
+        ctx.restore_all(init)
+        ctx.adjoint_begin(steps, every)
+        ctx.adjoint_forward()
+        ctx.adjoint_seed_all(steps, seed)
+        ctx.adjoint_backward()
+        g = ctx.adjoint_gradients_all()
+        ctx.adjoint_end()
+        return g
+
+    first = run(10, 4)
+    run(12, 3)
+    again = run(10, 4)
+    for key in ("x0", "v0", "force"):
+        assert np.array_equal(first[key], again[key]), key
+    ctx.close()
