@@ -214,8 +214,8 @@ def bench_adjoint(jsb, stream_ptr, steps: int = 90, every: int = 15) -> dict:
     pressurised tet cubes (U{4..8} cells), per-body step forces N(0, 2 N), v0 N(0, 0.5 m/s), floor + sphere,
     90 steps of 5 iterations. Loss = sum over bodies of |centre of mass - target|^2 after the last step;
     gradients w.r.t. initial positions / velocities, compliance and force, checkpoints every 15 steps.
-    Both sides are timed on the host clock around synchronised work (whole job, one run each after a
-    warm-up run)."""
+    Both sides are timed on the host clock around synchronised work (whole job, the median of three
+    runs each after a warm-up run)."""
     scene_bytes = jsb.build_scene("diff_batch")
     ctx = jsb.Context(0)
     ctx.load_scene(scene_bytes)
@@ -256,14 +256,17 @@ def bench_adjoint(jsb, stream_ptr, steps: int = 90, every: int = 15) -> dict:
         return time.perf_counter() - t0, grads
 
     forward_only()
-    t_fwd = forward_only()
+    t_fwd = statistics.median(forward_only() for _ in range(3))
     forward_adjoint()
-    t_adj, grads = forward_adjoint()
+    runs = [forward_adjoint() for _ in range(3)]
+    t_adj = statistics.median(t for t, _ in runs)
+    grads = runs[-1][1]
     finite = bool(np.isfinite(grads["force"]).all() and np.isfinite(grads["v0"]).all())
     ctx.close()
     return {"workload": "diff_batch", "bodies": nb, "steps": steps, "checkpoint_every": every,
             "forward_s": t_fwd, "forward_adjoint_s": t_adj, "ratio": t_adj / t_fwd, "target_ratio": 4.0,
-            "gradients_finite": bool(finite), "timing": "host clock around synchronised work, forward as a CUDA graph"}
+            "gradients_finite": bool(finite),
+            "timing": "host clock around synchronised work, median of 3 runs each, forward as a CUDA graph"}
 
 
 def bench_large_body(jsb, torch, stream, steps: int, with_cpu: bool) -> dict:
@@ -365,7 +368,8 @@ def bench_pinned_cloth(jsb, torch, stream, with_cpu: bool, autotune: bool = True
 def bench_diff_cloth(jsb, steps: int = 120, every: int = 10) -> dict:
     """The differentiable single cloth (64 x 64, 0.05 m spacing, top row pinned, per-edge compliance
     log-U[1e-6, 1e-4], v0 N(0, 0.1)): forward + adjoint of the 120-step run with checkpoints every 10
-    steps and the loss at steps 60 and 120, against the forward alone (host clock, synchronised)."""
+    steps and the loss at steps 60 and 120, against the forward alone (host clock, synchronised; median
+    of three runs each after a warm-up run)."""
     ctx = jsb.Context(0)
     ctx.load_scene(jsb.build_scene("diff_cloth"))
     init = ctx.save_all()
@@ -396,12 +400,13 @@ def bench_diff_cloth(jsb, steps: int = 120, every: int = 10) -> dict:
         return time.perf_counter() - t0
 
     forward()
-    t_fwd = forward()
+    t_fwd = statistics.median(forward() for _ in range(3))
     forward_adjoint()
-    t_adj = forward_adjoint()
+    t_adj = statistics.median(forward_adjoint() for _ in range(3))
     ctx.close()
     return {"workload": "diff_cloth 64x64", "steps": steps, "checkpoint_every": every, "forward_s": t_fwd,
-            "forward_adjoint_s": t_adj, "ratio": t_adj / t_fwd, "target_ratio": 4.0}
+            "forward_adjoint_s": t_adj, "ratio": t_adj / t_fwd, "target_ratio": 4.0,
+            "timing": "host clock around synchronised work, median of 3 runs each"}
 
 
 def profile_driver(args) -> None:
