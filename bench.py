@@ -37,6 +37,8 @@ import numpy as np
 
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.join(REPO, "tests"))
+from scenes import build_scene  # noqa: E402  (seeded workload generator; not the product library)
 
 METRIC = "soft-body vertex-iterations/s on 1 GB300: batched+adjoint vs plain, % of roofline"
 UNIT = "vertex-iterations/s"
@@ -152,11 +154,9 @@ def run_reference_arm(args, rank, world):
     """CPU oracle on the host cores (the reference arm)."""
     if rank != 0:
         return
-    sys.path.insert(0, os.path.join(REPO, "tests"))
-    import joltphysics_gb300 as jsb
     from jsb_testlib import Oracle, parse_scene
 
-    scene_bytes = jsb.build_scene(WORKLOAD, **scene_params(0))
+    scene_bytes = build_scene(WORKLOAD, **scene_params(0))
     scene, _ = parse_scene(scene_bytes)
     threads = os.cpu_count() or 1
     vi_step = sum(b.num_vertices * b.num_iterations for b in scene.bodies)
@@ -216,7 +216,7 @@ def bench_adjoint(jsb, stream_ptr, steps: int = 90, every: int = 15) -> dict:
     gradients w.r.t. initial positions / velocities, compliance and force, checkpoints every 15 steps.
     Both sides are timed on the host clock around synchronised work (whole job, the median of three
     runs each after a warm-up run)."""
-    scene_bytes = jsb.build_scene("diff_batch")
+    scene_bytes = build_scene("diff_batch")
     ctx = jsb.Context(0)
     ctx.load_scene(scene_bytes)
     ctx.set_scene_step_forces()
@@ -273,7 +273,7 @@ def bench_large_body(jsb, torch, stream, steps: int, with_cpu: bool) -> dict:
     """The 256 x 256 cloth (65,536 vertices, LRA tethers, sphere on a floor, 8 iterations) on the
     thread-block-cluster path: its 600-step run from the initial state, `steps` steps spread evenly over
     it device-timed (CUDA graph of one step, L2 flushed before each)."""
-    scene_bytes = jsb.build_scene("large_cloth")
+    scene_bytes = build_scene("large_cloth")
     ctx = jsb.Context(0)
     ctx.load_scene(scene_bytes)
     sptr = stream.cuda_stream
@@ -328,7 +328,7 @@ def bench_pinned_cloth(jsb, torch, stream, with_cpu: bool, autotune: bool = True
     compliance 1e-5, dihedral bends 1e-4, 5 iterations, no colliders): its 300-step run as one CUDA
     graph, device-timed (after the autotuner picked the launch shape for this one body), and the oracle
     on one thread for the same run."""
-    scene_bytes = jsb.build_scene("pinned_cloth")
+    scene_bytes = build_scene("pinned_cloth")
     ctx = jsb.Context(0)
     ctx.load_scene(scene_bytes)
     if autotune:
@@ -371,7 +371,7 @@ def bench_diff_cloth(jsb, steps: int = 120, every: int = 10) -> dict:
     steps and the loss at steps 60 and 120, against the forward alone (host clock, synchronised; median
     of three runs each after a warm-up run)."""
     ctx = jsb.Context(0)
-    ctx.load_scene(jsb.build_scene("diff_cloth"))
+    ctx.load_scene(build_scene("diff_cloth"))
     init = ctx.save_all()
     n = ctx.total_vertices()
     rng = np.random.default_rng(3)
@@ -417,7 +417,7 @@ def profile_driver(args) -> None:
 
     if args.profile == "diff_batch_adjoint":
         ctx = jsb.Context(0)
-        ctx.load_scene(jsb.build_scene("diff_batch", steps=args.steps))
+        ctx.load_scene(build_scene("diff_batch", steps=args.steps))
         ctx.set_scene_step_forces()
         n = sum(ctx.num_vertices)
         ctx.adjoint_begin(args.steps, 5)
@@ -428,7 +428,7 @@ def profile_driver(args) -> None:
         ctx.synchronize()
         return
     ctx = jsb.Context(0)
-    ctx.load_scene(jsb.build_scene(args.profile))
+    ctx.load_scene(build_scene(args.profile))
     for mv, threads, mode in json.loads(args.table or "[]"):
         ctx.set_bucket_config(mv, threads, mode)
     for _ in range(args.warmup + args.steps):
@@ -477,7 +477,7 @@ def main():
     import joltphysics_gb300 as jsb
     from jsb_testlib import parse_scene
 
-    scene_bytes = jsb.build_scene(WORKLOAD, **scene_params(rank))
+    scene_bytes = build_scene(WORKLOAD, **scene_params(rank))
     scene, _ = parse_scene(scene_bytes)
     ctx = jsb.Context(local)
     ctx.load_scene(scene_bytes)

@@ -201,13 +201,6 @@ jsb_status jsb_last_launch_count(jsb_context *ctx, uint32_t *launches);
  * last jsb_step_graph call, averaged per step. */
 jsb_status jsb_last_kernel_ms(jsb_context *ctx, float *ms_per_step);
 
-/* ---- scenes (seeded synthetic workloads, built with this library's SoftBodySharedSettings mirror) */
-/* Serialises a scene (colliders, bodies with SaveBinaryState bytes, creation settings, forces).
- * name: "pinned_cloth" | "uneven_batch" | "large_cloth" | "diff_cloth" | "diff_batch"; params is a
- * space separated "key=value" list. Call with out == NULL to query *len. */
-jsb_status jsb_scene_build(const char *name, const char *params, void *out, size_t capacity, size_t *len);
-
-
 /* ---- differentiable runs (hand-written adjoint) ----------------------------------------------- */
 /* Per-constraint compliance of one body, in the settings' constraint order (mEdgeConstraints /
  * mVolumeConstraints after SoftBodySharedSettings::Optimize); either array may be NULL. The body's

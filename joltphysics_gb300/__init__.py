@@ -62,7 +62,6 @@ SIGNATURES = {
     "jsb_autotune": [_P, _c.c_float, _c.c_int],
     "jsb_last_launch_count": [_P, _c.POINTER(_c.c_uint32)],
     "jsb_last_kernel_ms": [_P, _c.POINTER(_c.c_float)],
-    "jsb_scene_build": [_c.c_char_p, _c.c_char_p, _P, _c.c_size_t, _c.POINTER(_c.c_size_t)],
     "jsb_body_set_compliance": [_P, _c.c_uint32, _P, _c.c_uint32, _P, _c.c_uint32],
     "jsb_adjoint_begin": [_P, _c.c_float, _c.c_int, _c.c_int],
     "jsb_adjoint_forward": [_P, _c.c_int],
@@ -125,16 +124,6 @@ def blob_counts(blob: bytes) -> dict:
         out[name] = n
         off += 4 + n * size
     return out
-
-
-def build_scene(name: str, **params) -> bytes:
-    """Serialised seeded scene (see csrc/host/scene_io.h) built with this library's settings mirror."""
-    p = " ".join(f"{k}={v}" for k, v in params.items()).encode()
-    n = ctypes.c_size_t(0)
-    check(lib().jsb_scene_build(name.encode(), p, None, 0, ctypes.byref(n)))
-    buf = ctypes.create_string_buffer(n.value)
-    check(lib().jsb_scene_build(name.encode(), p, buf, n.value, ctypes.byref(n)))
-    return buf.raw[: n.value]
 
 
 def settings_schedule(blob: bytes):

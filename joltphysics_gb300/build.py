@@ -9,7 +9,6 @@ for the same reason. Translation units are compiled in parallel.
 from __future__ import annotations
 
 import os
-import shutil
 import subprocess
 import sys
 
@@ -24,7 +23,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["kernels/solver.cu", "kernels/cluster.cu", "kernels/adjoint.cu", "kernels/state_io.cu"]
-CXX_SOURCES = ["host/runtime.cpp", "host/schedule.cpp", "host/shared_settings.cpp"]
+CXX_SOURCES = ["host/runtime.cpp", "host/schedule.cpp"]
 
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-std=c++17",
                      "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(REPO, "include")]
@@ -83,26 +82,5 @@ def build(verbose: bool = False, extra_nvcc: list[str] | None = None) -> str:
     return LIB
 
 
-def build_oracle() -> str:
-    """Compiles the CPU oracle (test infrastructure) with the same float contraction rules."""
-    src = os.path.join(REPO, "oracle", "jsb_oracle.cpp")
-    out = os.path.join(REPO, "oracle", "liboracle.so")
-    if _stale(out, [src]):
-        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", src, "-o", out],
-                       check=True)
-    return out
-
-
-def build_reference(ref: str = "/root/reference", jobs: int | None = None) -> bool:
-    """Builds oracle/_ref from the reference sources when they are present (never on the GPU hosts)."""
-    if not os.path.isdir(os.path.join(ref, "Jolt")) or shutil.which("make") is None:
-        return False
-    j = str(jobs or os.cpu_count() or 4)
-    subprocess.run(["make", "-f", os.path.join("oracle", "Makefile.ref"), f"REF={ref}", f"-j{j}"], cwd=REPO, check=True,
-                   stdout=subprocess.DEVNULL)
-    return True
-
-
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv))
-    print(build_oracle())

@@ -24,9 +24,7 @@
 
 #include "../../../include/jsb.h"
 #include "../kernels/device_types.h"
-#include "scene_io.h"
 #include "schedule.h"
-#include "shared_settings.h"
 
 namespace jsb {
 
@@ -1794,22 +1792,6 @@ jsb_status jsb_adjoint_end(jsb_context *ctx) {
     if (ctx->adjoint) {  // keep the device buffers for the next differentiable run of this context
         ctx->adjoint->release_launch_groups();
         ctx->adjoint_spare = std::move(ctx->adjoint);
-    }
-    return JSB_OK;
-}
-
-jsb_status jsb_scene_build(const char *name, const char *params, void *out, size_t capacity, size_t *len) {
-    if (!name || !len) return fail(JSB_ERR_INVALID_ARGUMENT, "null argument");
-    scene::SceneSpec spec;
-    try {
-        if (!scene::make_named_scene(name, params ? params : "", spec)) return fail(JSB_ERR_INVALID_ARGUMENT, std::string("unknown scene ") + name);
-        std::string bytes = scene::serialize_scene(spec, [](const scene::MeshSpec &m) { return host::build_settings(m).SaveBinaryState(); });
-        *len = bytes.size();
-        if (!out) return JSB_OK;
-        if (capacity < bytes.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "output buffer too small");
-        memcpy(out, bytes.data(), bytes.size());
-    } catch (const std::exception &e) {
-        return fail(JSB_ERR_INVALID_ARGUMENT, std::string("scene build failed: ") + e.what());
     }
     return JSB_OK;
 }

@@ -4,7 +4,7 @@ Soft bodies do not interact within a step (the reference has no soft-soft collis
 SoftBodyMotionProperties.cpp:147), so a batch splits across GPUs with no exchange on the data path.
 Bodies are assigned longest-processing-time first onto the least-loaded rank, by an estimated cost:
 iterations x (dependency levels per substep + vertices / 32), the critical path of one body's step
-on one CTA. `shard_scene` cuts a serialised scene ("JSBS", see csrc/host/scene_io.h) down to one
+on one CTA. `shard_scene` cuts a serialised scene ("JSBS", see tests/scenes/scene_io.h) down to one
 rank's bodies (every rank keeps every collider).
 """
 from __future__ import annotations

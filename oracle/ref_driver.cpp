@@ -1,5 +1,5 @@
 // Reference driver: runs the reference's own soft-body solver (Jolt Physics, built from its sources
-// by oracle/Makefile.ref) on the seeded scenes of joltphysics_gb300/csrc/host/scene_spec.h and
+// by oracle/Makefile.ref) on the seeded scenes of tests/scenes/scene_spec.h and
 // dumps what the tests need. TEST INFRASTRUCTURE ONLY: nothing in the product links or runs this.
 //
 // Bodies are created through the public API only:
@@ -16,7 +16,7 @@
 //
 // Output file (little endian):
 //   'JSBD' u32 version=2 u32 num_dumps u32 scene_len, scene_len bytes of the serialised scene
-//          (joltphysics_gb300/csrc/host/scene_io.h, settings bytes written by Jolt)
+//          (tests/scenes/scene_io.h, settings bytes written by Jolt)
 //   per dump:  i32 step; per body: f32[3] body position, f32[3*N] local positions, f32[3*N] velocities,
 //              u32 state_len, state bytes (SaveState)
 
@@ -44,7 +44,7 @@
 #include <string>
 #include <thread>
 
-#include "../joltphysics_gb300/csrc/host/scene_io.h"
+#include "../tests/scenes/scene_io.h"
 
 using namespace JPH;
 

@@ -144,11 +144,13 @@ def run_reference(variant: str, scene: str, out: str, **kv) -> dict:
 
 
 def build_oracle() -> str:
-    src = os.path.join(ORACLE_DIR, "jsb_oracle.cpp")
-    if (not os.path.exists(ORACLE_LIB)) or os.path.getmtime(ORACLE_LIB) < os.path.getmtime(src):
-        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", src, "-o",
-                        ORACLE_LIB], check=True)
-    return ORACLE_LIB
+    """oracle/build.py's build_oracle (compiles liboracle.so when it is missing or stale)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("oracle_build", os.path.join(ORACLE_DIR, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build_oracle()
 
 
 class Oracle:

@@ -1,5 +1,6 @@
 // Host-side mirror of Jolt's SoftBodySharedSettings (Jolt/Physics/SoftBody/SoftBodySharedSettings.h).
 //
+// TEST AND BENCHMARK INFRASTRUCTURE, not part of the product library (libjsb.so never links it).
 // Jolt users keep building their settings with Jolt and hand the GPU the bytes of
 // SoftBodySharedSettings::SaveBinaryState. This mirror exists so that the same settings can be
 // produced where Jolt is not linked (the GPU test and benchmark hosts): it restates

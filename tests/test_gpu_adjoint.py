@@ -16,6 +16,7 @@ import numpy as np
 import pytest
 
 from jsb_testlib import FD64, parse_scene
+from scenes import build_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -70,7 +71,7 @@ def sample_and_compare(fd, grads, picks, rng):
 
 
 def test_adjoint_cloth_vs_fd(jsb):
-    scene_bytes = jsb.build_scene("diff_cloth", n=10, steps=16)
+    scene_bytes = build_scene("diff_cloth", n=10, steps=16)
     scene, _ = parse_scene(scene_bytes)
     rng = np.random.default_rng(7)
     nv = scene.bodies[0].num_vertices
@@ -87,7 +88,7 @@ def test_adjoint_cloth_vs_fd(jsb):
 
 def contact_scene(jsb):
     """A cloth and a pressurised tet cube dropped 0.15 m onto the floor, with step forces."""
-    return jsb.build_scene("diff_batch", n_cloth=1, n_cube=1, steps=24, drop_mm=150, seed=23)
+    return build_scene("diff_batch", n_cloth=1, n_cube=1, steps=24, drop_mm=150, seed=23)
 
 
 def test_adjoint_contacts_vs_fp64_autodiff(jsb):
@@ -139,7 +140,7 @@ def test_adjoint_contacts_vs_fd_report(jsb):
 
 
 def test_checkpoint_interval_does_not_change_gradients(jsb):
-    scene_bytes = jsb.build_scene("diff_batch", n_cloth=2, n_cube=1, steps=12)
+    scene_bytes = build_scene("diff_batch", n_cloth=2, n_cube=1, steps=12)
     scene, _ = parse_scene(scene_bytes)
     rng = np.random.default_rng(3)
     seeds = {12: {b: rng.standard_normal((body.num_vertices, 3)) for b, body in enumerate(scene.bodies)}}
@@ -156,7 +157,7 @@ def test_torch_autograd_binding(jsb):
 
     from joltphysics_gb300.autograd import Simulation, rollout
 
-    scene_bytes = jsb.build_scene("diff_cloth", n=8, steps=10)
+    scene_bytes = build_scene("diff_cloth", n=8, steps=10)
     scene, _ = parse_scene(scene_bytes)
     ctx = jsb.Context(0)
     ctx.load_scene(scene_bytes)
@@ -190,7 +191,7 @@ def test_bulk_seed_and_gradients_equal_per_body(jsb):
     """jsb_adjoint_seed_all / jsb_adjoint_gradients_all == the per-body calls, and the last checkpoint
     segment taped during the forward pass gives the same gradients as a recomputed one (a second
     backward pass recomputes every segment)."""
-    scene_bytes = jsb.build_scene("diff_batch", n_cloth=3, n_cube=2, steps=10)
+    scene_bytes = build_scene("diff_batch", n_cloth=3, n_cube=2, steps=10)
     scene, _ = parse_scene(scene_bytes)
     rng = np.random.default_rng(8)
     seeds = {10: {b: rng.standard_normal((body.num_vertices, 3)) for b, body in enumerate(scene.bodies)}}
@@ -225,7 +226,7 @@ def test_step_walk_adjoint_equals_substep_walk(jsb):
     every vertex, so position and velocity gradients agree bit for bit; force and compliance gradients
     are sums taken in another order (per thread, per whole-step slot) and agree to 1e-5. A cloth (whole-
     step walk) and a pressurised cube (per-substep walk in both) on a floor, through contact."""
-    scene_bytes = jsb.build_scene("diff_batch", n_cloth=2, n_cube=1, steps=30, seed=3)
+    scene_bytes = build_scene("diff_batch", n_cloth=2, n_cube=1, steps=30, seed=3)
     scene, _ = parse_scene(scene_bytes)
     rng = np.random.default_rng(5)
     seeds = {15: {}, 30: {}}
@@ -247,7 +248,7 @@ def test_runs_in_one_context_reuse_buffers(jsb):
     """jsb_adjoint_end keeps the run's device buffers for the context's next differentiable run: a run,
     then one of another length and checkpoint interval (buffers grow and shrink), then the first again
     from the same state give bit-identical gradients."""
-    scene_bytes = jsb.build_scene("diff_batch", n_cloth=3, n_cube=2, steps=12)
+    scene_bytes = build_scene("diff_batch", n_cloth=3, n_cube=2, steps=12)
     scene, _ = parse_scene(scene_bytes)
     rng = np.random.default_rng(21)
     n = sum(b.num_vertices for b in scene.bodies)

@@ -11,6 +11,7 @@ import pytest
 
 from jsb_testlib import Oracle, parse_scene
 from test_gpu_parity import advance, assert_same, make_ctx, snapshot
+from scenes import build_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -23,7 +24,7 @@ def force_cluster(ctx, cluster_size=0, threads=256):
 
 
 def test_large_cloth_65536_vertices_vs_oracle(jsb):
-    scene_bytes = jsb.build_scene("large_cloth", n=256, steps=3)
+    scene_bytes = build_scene("large_cloth", n=256, steps=3)
     scene, _ = parse_scene(scene_bytes)
     ctx = make_ctx(jsb, scene_bytes)
     cfg = ctx.cluster_config()
@@ -38,7 +39,7 @@ def test_large_cloth_65536_vertices_vs_oracle(jsb):
 @pytest.mark.parametrize("cluster_size,threads", [(2, 128), (4, 512), (8, 256), (16, 256), (16, 512)])
 def test_cluster_shapes_vs_oracle_through_contact(jsb, cluster_size, threads):
     """A 48 x 48 cloth dropped onto the sphere: 40 steps cover the first contacts."""
-    scene_bytes = jsb.build_scene("large_cloth", n=48, steps=40)
+    scene_bytes = build_scene("large_cloth", n=48, steps=40)
     scene, _ = parse_scene(scene_bytes)
     ctx = make_ctx(jsb, scene_bytes)
     force_cluster(ctx, cluster_size, threads)
@@ -52,7 +53,7 @@ def test_cluster_shapes_vs_oracle_through_contact(jsb, cluster_size, threads):
 def test_cluster_equals_one_cta_path_on_a_batch(jsb):
     """Cloths of many sizes (no pressure), floor contact: cluster path == one-CTA path, bitwise, in the
     batched, plain and graph forms."""
-    scene_bytes = jsb.build_scene("uneven_batch", n_cloth=12, n_cube=0, steps=30, seed=9)
+    scene_bytes = build_scene("uneven_batch", n_cloth=12, n_cube=0, steps=30, seed=9)
     a = make_ctx(jsb, scene_bytes)
     advance(a, 30)
     for mode in ("batched", "plain", "graph"):
@@ -65,8 +66,8 @@ def test_cluster_equals_one_cta_path_on_a_batch(jsb):
 
 def test_mixed_launch_cluster_and_one_cta_bodies(jsb):
     """A context holding a 65,536-vertex cloth and small bodies runs both paths in one batched step."""
-    big = jsb.build_scene("large_cloth", n=256, steps=2)
-    small = jsb.build_scene("uneven_batch", n_cloth=6, n_cube=3, steps=2, seed=4)
+    big = build_scene("large_cloth", n=256, steps=2)
+    small = build_scene("uneven_batch", n_cloth=6, n_cube=3, steps=2, seed=4)
     ctx = make_ctx(jsb, big)
     ctx.load_scene(small)
     assert ctx.cluster_config()["bodies"] == 1
@@ -81,7 +82,7 @@ def test_mixed_launch_cluster_and_one_cta_bodies(jsb):
 
 
 def test_pressurised_body_rejected_on_cluster_path(jsb):
-    scene_bytes = jsb.build_scene("uneven_batch", n_cloth=0, n_cube=4, steps=2, seed=3)
+    scene_bytes = build_scene("uneven_batch", n_cloth=0, n_cube=4, steps=2, seed=3)
     scene, _ = parse_scene(scene_bytes)
     ctx = make_ctx(jsb, scene_bytes)
     force_cluster(ctx)

@@ -11,6 +11,7 @@ import pytest
 
 from conftest import golden_path
 from jsb_testlib import Oracle, parse_scene
+from scenes import build_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -95,7 +96,7 @@ def test_plain_and_graph_equal_batched(jsb, mode):
 
 def test_full_size_bodies_vs_oracle(jsb):
     """Full cloth/cube size ranges of the uneven batch (cloth sides 8..64, cubes 4..12 cells)."""
-    scene_bytes = jsb.build_scene("uneven_batch", n_cloth=24, n_cube=8, steps=4)
+    scene_bytes = build_scene("uneven_batch", n_cloth=24, n_cube=8, steps=4)
     scene, _ = parse_scene(scene_bytes)
     o = Oracle(scene)
     ctx = make_ctx(jsb, scene_bytes)
@@ -108,7 +109,7 @@ def test_full_size_bodies_vs_oracle(jsb):
 
 def test_diff_batch_full_vs_oracle(jsb):
     """256-body differentiable batch (forces every step, pressure, floor + sphere) for 2 steps."""
-    scene_bytes = jsb.build_scene("diff_batch", steps=2)
+    scene_bytes = build_scene("diff_batch", steps=2)
     scene, _ = parse_scene(scene_bytes)
     o = Oracle(scene)
     ctx = make_ctx(jsb, scene_bytes, step_forces=True)
@@ -120,7 +121,7 @@ def test_diff_batch_full_vs_oracle(jsb):
 def test_uneven_batch_full_properties(jsb):
     """The full 512-body uneven batch: two runs are bitwise identical, the first step matches the oracle,
     everything stays finite and kinematic vertices stay put in world space."""
-    scene_bytes = jsb.build_scene("uneven_batch")
+    scene_bytes = build_scene("uneven_batch")
     scene, _ = parse_scene(scene_bytes)
     o = Oracle(scene)
     o.step(1)
@@ -195,7 +196,7 @@ def test_nan_propagation_matches_oracle(jsb, path):
     """A body holding NaN positions (as a body that has blown up does) keeps being stepped: the vertices
     that become NaN are those that become NaN in the reference's arithmetic (NaN-guarded projections),
     and the other bodies are untouched, bit for bit."""
-    scene_bytes = jsb.build_scene("uneven_batch", n_cloth=4, n_cube=0, cloth_max=24, steps=3, seed=9)
+    scene_bytes = build_scene("uneven_batch", n_cloth=4, n_cube=0, cloth_max=24, steps=3, seed=9)
     scene, _ = parse_scene(scene_bytes)
     ctx = make_ctx(jsb, scene_bytes)
     if path == "cluster":
@@ -241,7 +242,7 @@ def test_step_walk_equals_substep_walk_and_oracle(jsb, state_mode, threads):
     the uneven batch's full size ranges drop onto the floor (cubes land, pinned cloths hang), 90
     steps; state_mode 1 keeps velocities and previous positions in HBM, which the per-vertex passes
     inside the walk then read and write there; threads 512 (else the default table's) per CTA."""
-    scene_bytes = jsb.build_scene("uneven_batch", n_cloth=10, n_cube=6, steps=90, seed=11)
+    scene_bytes = build_scene("uneven_batch", n_cloth=10, n_cube=6, steps=90, seed=11)
     scene, _ = parse_scene(scene_bytes)
     a = make_ctx(jsb, scene_bytes)
     b = jsb.Context(0)

@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 from conftest import golden_path
+from scenes import build_scene
 
 CASES = {
     "pinned_cloth": ("pinned_cloth", {}),
@@ -17,6 +18,6 @@ CASES = {
 @pytest.mark.parametrize("name", list(CASES))
 def test_mirror_bytes_equal_reference(name, jsb):
     scene, params = CASES[name]
-    mine = jsb.build_scene(scene, **params)
+    mine = build_scene(scene, **params)
     ref = np.load(golden_path(name))["scene"].tobytes()
     assert mine == ref

@@ -12,6 +12,7 @@ import pytest
 torch = pytest.importorskip("torch")
 import torch.distributed as dist  # noqa: E402
 import torch.multiprocessing as mp  # noqa: E402
+from scenes import build_scene  # noqa: E402
 
 
 def _free_port() -> int:
@@ -48,7 +49,7 @@ def test_two_rank_shards_cover_and_balance(jsb, tmp_path):
 
     from jsb_testlib import parse_scene
 
-    scene = jsb.build_scene("uneven_batch", n_cloth=40, n_cube=12, steps=2, seed=6)
+    scene = build_scene("uneven_batch", n_cloth=40, n_cube=12, steps=2, seed=6)
     mp.start_processes(_rank_main, args=(2, _free_port(), scene, str(tmp_path)), nprocs=2, join=True,
                        start_method="spawn")
     res = pickle.load(open(tmp_path / "result.pkl", "rb"))

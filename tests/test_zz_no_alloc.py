@@ -15,6 +15,7 @@ import pytest
 
 from conftest import golden_path
 from jsb_testlib import COLLIDER_FMT, parse_scene
+from scenes import build_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -85,7 +86,7 @@ def test_noalloc_matches_context_step(jsb, name, body):
 
 
 def test_noalloc_rejects_oversize_body(jsb):
-    scene, _ = parse_scene(jsb.build_scene("large_cloth", n=136, steps=1))
+    scene, _ = parse_scene(build_scene("large_cloth", n=136, steps=1))
     b = scene.bodies[0]
     assert b.num_vertices > 16384
     with pytest.raises(jsb.JsbError) as e:
