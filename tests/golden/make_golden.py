@@ -11,6 +11,13 @@ SoftBodySharedSettings::CreateConstraints/Optimize, steps it with PhysicsSystem:
 world positions. A fixture stores the serialised scene (settings bytes written by Jolt) and, per dump
 step, each body's position, local vertex positions and velocities, from the deterministic build
 (JPH_CROSS_PLATFORM_DETERMINISTIC) and, for the final step, from the default FMA build.
+
+The full-size configurations (FULL_CASES) run over their whole stated length; their states are too
+large to commit, so those fixtures ("full_<name>.npz") keep per dump step and body a 16-byte digest of
+the deterministic build's state (jsb_testlib.state_digest: body position, local positions and
+velocities, NaNs canonicalised), the count of NaN position components, and the largest world-position
+difference between the two builds (finite vertices only), plus the SHA-256 of the scene bytes Jolt
+wrote, against which the scene library's mirror output is checked.
 """
 from __future__ import annotations
 
@@ -22,7 +29,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
-from jsb_testlib import parse_dump, run_reference  # noqa: E402
+from jsb_testlib import parse_dump, run_reference, state_digest  # noqa: E402
 
 CASES = {
     # name: (scene, params, dump steps)
@@ -54,7 +61,56 @@ def make(name: str, scene: str, params: dict, steps: list[int]):
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
 
 
+# name: (scene, params, dump steps): every BASELINE configuration at its full size and length
+FULL_CASES = {
+    "pinned_cloth": ("pinned_cloth", {}, [1, 100, 200, 300]),
+    "uneven_batch": ("uneven_batch", {}, [1, 60, 120, 180, 240]),
+    "large_cloth": ("large_cloth", {}, [1, 100, 300, 600]),
+    "diff_cloth": ("diff_cloth", {}, [1, 60, 120]),
+    "diff_batch": ("diff_batch", {}, [1, 45, 90]),
+}
+
+
+def make_full(name: str, scene: str, params: dict, steps: list[int], threads: int):
+    import hashlib
+    import json
+
+    out = {"params": np.frombuffer(json.dumps({"scene": scene, **params}).encode(), np.uint8), "steps": np.array(steps, np.int32)}
+    with tempfile.TemporaryDirectory() as tmp:
+        dumps_by = {}
+        for variant in ("det", "fast"):
+            path = os.path.join(tmp, f"{variant}.bin")
+            run_reference(variant, scene, path, dump=",".join(str(s) for s in steps), threads=threads, **params)
+            sc, dumps = parse_dump(path)
+            if variant == "det":
+                out["scene_sha256"] = np.frombuffer(hashlib.sha256(sc.raw).digest(), np.uint8)
+                out["num_vertices"] = np.array([b.num_vertices for b in sc.bodies], np.int64)
+            dumps_by[variant] = dumps
+            os.remove(path)
+    det, fast = dumps_by["det"], dumps_by["fast"]
+    nb = len(out["num_vertices"])
+    digest = np.zeros((len(steps), nb, 16), np.uint8)
+    nans = np.zeros((len(steps), nb), np.int32)
+    fast_dev = np.zeros((len(steps), nb), np.float64)
+    for k, (d, f) in enumerate(zip(det, fast)):
+        assert d.step == steps[k] and f.step == steps[k]
+        for b in range(nb):
+            digest[k, b] = np.frombuffer(state_digest(d.positions[b], d.local[b], d.velocities[b]), np.uint8)
+            nans[k, b] = int(np.isnan(d.local[b]).sum())
+            wd, wf = d.world(b), f.world(b)
+            ok = np.isfinite(wd).all(axis=1) & np.isfinite(wf).all(axis=1)
+            fast_dev[k, b] = float(np.abs(wd[ok] - wf[ok]).max()) if ok.any() else 0.0
+    out.update(digest=digest, nan_components=nans, fast_max_dev=fast_dev)
+    np.savez_compressed(os.path.join(HERE, f"full_{name}.npz"), **out)
+
+
 if __name__ == "__main__":
+    which = sys.argv[1:]
     for name, (scene, params, steps) in CASES.items():
-        make(name, scene, params, steps)
-        print("wrote", name)
+        if not which or name in which:
+            make(name, scene, params, steps)
+            print("wrote", name)
+    for name, (scene, params, steps) in FULL_CASES.items():
+        if not which or f"full_{name}" in which:
+            make_full(name, scene, params, steps, threads=os.cpu_count() or 1)
+            print("wrote", f"full_{name}")

@@ -135,6 +135,20 @@ def parse_dump(path: str) -> tuple[Scene, list]:
     return scene, dumps
 
 
+def state_digest(position, local, velocity) -> bytes:
+    """16-byte digest of one body's state (float32 body position, local positions and velocities) in which
+    every NaN is replaced by the same quiet NaN, so that states agreeing bit for bit except in the payload
+    and sign of their NaNs (the CPU's default NaN differs from the GPU's) give the same digest."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for a in (position, local, velocity):
+        a = np.array(a, np.float32, copy=True).reshape(-1)
+        a[np.isnan(a)] = np.float32(np.nan)
+        h.update(a.tobytes())
+    return h.digest()[:16]
+
+
 def run_reference(variant: str, scene: str, out: str, **kv) -> dict:
     """Runs the reference driver (only where oracle/_ref was built)."""
     args = [REF_DRIVER[variant], scene, out] + [f"{k}={v}" for k, v in kv.items()]
