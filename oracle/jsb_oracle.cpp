@@ -1,9 +1,15 @@
 // CPU oracle for the soft-body solver step. TEST INFRASTRUCTURE ONLY.
 //
-// This is a plain, single-threaded restatement of Jolt Physics' soft-body update, written to be
-// checked against the reference (oracle/_ref) and then used as the checker of the CUDA path. Only
-// tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference arm load it. The product
-// library (libjsb) never links or calls it.
+// This is a plain restatement of Jolt Physics' soft-body update, written to be checked against the
+// reference (oracle/_ref) and then used as the checker of the CUDA path. Only tests/,
+// __graft_entry__.smoke() and bench.py's cpu_baseline / reference arm load it. The product library
+// (libjsb) never links or calls it.
+//
+// Threads are used the way the reference's job system uses them, without changing a single operation:
+// a world of at least as many bodies as threads steps whole bodies concurrently (bodies do not interact
+// within a step); otherwise each body's parallel update groups (vertex-disjoint) run concurrently and
+// its non-parallel group runs after them, as ParallelApplyConstraints does
+// (SoftBodyMotionProperties.cpp:1057-1115), and the per-vertex passes are split into vertex ranges.
 //
 // Every arithmetic step follows the reference's operation order so that the float instantiation is
 // bit-identical to the reference built with JPH_CROSS_PLATFORM_DETERMINISTIC (-ffp-contract=off):
@@ -28,16 +34,88 @@
 // Build: g++ -O2 -std=c++17 -ffp-contract=off -fPIC -shared oracle/jsb_oracle.cpp -o oracle/liboracle.so
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
+#include <condition_variable>
 #include <cstdint>
 #include <cstring>
+#include <functional>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
 
 namespace oracle {
+
+// Persistent workers: run(count, fn) calls fn(i) for every i < count on the workers and the caller,
+// and returns when all calls have finished.
+class Pool {
+public:
+    explicit Pool(int threads) {
+        for (int t = 1; t < threads; ++t) workers_.emplace_back([this] { loop(); });
+    }
+    ~Pool() {
+        {
+            std::lock_guard<std::mutex> l(m_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto &w : workers_) w.join();
+    }
+    int size() const { return int(workers_.size()) + 1; }
+    void run(size_t count, const std::function<void(size_t)> &fn) {
+        if (workers_.empty() || count < 2) {
+            for (size_t i = 0; i < count; ++i) fn(i);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> l(m_);
+            fn_ = &fn;
+            count_ = count;
+            next_.store(0);
+            pending_ = int(workers_.size());
+            ++generation_;
+        }
+        cv_.notify_all();
+        drain();
+        std::unique_lock<std::mutex> l(m_);
+        done_cv_.wait(l, [this] { return pending_ == 0; });
+        fn_ = nullptr;
+    }
+
+private:
+    void drain() {
+        for (size_t i = next_.fetch_add(1); i < count_; i = next_.fetch_add(1)) (*fn_)(i);
+    }
+    void loop() {
+        size_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> l(m_);
+                cv_.wait(l, [&] { return stop_ || generation_ != seen; });
+                if (stop_) return;
+                seen = generation_;
+            }
+            drain();
+            {
+                std::lock_guard<std::mutex> l(m_);
+                --pending_;
+            }
+            done_cv_.notify_one();
+        }
+    }
+    std::vector<std::thread> workers_;
+    std::mutex m_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void(size_t)> *fn_ = nullptr;
+    size_t count_ = 0;
+    std::atomic<size_t> next_{0};
+    size_t generation_ = 0;
+    int pending_ = 0;
+    bool stop_ = false;
+};
 
 template <class R>
 struct V3 {
@@ -250,24 +328,37 @@ public:
     }
 
     int threads = 1;
+    std::unique_ptr<Pool> pool;
+    Pool *inner = nullptr;  // set while one body is stepped with its groups spread over the pool
 
-    // Bodies are independent within a step, so they may be stepped on several threads (body i on
-    // thread i % threads); each body's arithmetic is unchanged.
+    // Bodies are independent within a step: with at least as many bodies as threads they are stepped
+    // concurrently, one body per task; otherwise one after another, each spreading its parallel update
+    // groups and per-vertex passes over the threads. Each body's arithmetic is unchanged either way.
     void step(R dt, int collision_steps) {
         R step_dt = dt / R(collision_steps);
+        if (threads > 1 && (!pool || pool->size() != threads)) pool.reset(new Pool(threads));
         for (int c = 0; c < collision_steps; ++c) {
-            if (threads <= 1 || bodies.size() < 2) {
+            if (threads <= 1) {
                 for (auto &b : bodies) step_body(b, step_dt);
-                continue;
+            } else if (bodies.size() >= size_t(threads)) {
+                pool->run(bodies.size(), [&](size_t i) { step_body(bodies[i], step_dt); });
+            } else {
+                inner = pool.get();
+                for (auto &b : bodies) step_body(b, step_dt);
+                inner = nullptr;
             }
-            std::vector<std::thread> pool;
-            int n = int(std::min<size_t>(size_t(threads), bodies.size()));
-            for (int t = 0; t < n; ++t)
-                pool.emplace_back([this, t, n, step_dt] {
-                    for (size_t i = size_t(t); i < bodies.size(); i += size_t(n)) step_body(bodies[i], step_dt);
-                });
-            for (auto &th : pool) th.join();
         }
+    }
+
+    // fn(first, last) over vertex ranges of a body (on the pool when one body is spread over it)
+    template <class F>
+    void for_vertex_ranges(size_t n, F &&fn) {
+        const size_t chunk = 4096;
+        if (!inner || n <= chunk) {
+            fn(size_t(0), n);
+            return;
+        }
+        inner->run((n + chunk - 1) / chunk, [&](size_t k) { fn(k * chunk, std::min(n, (k + 1) * chunk)); });
     }
 
     void step_body(Body<R> &b, R dt) {
@@ -324,7 +415,13 @@ public:
             apply_pressure(b, dt_sub);
             integrate(b, g, dt_sub);
             const size_t ng = s.groups.size();
-            for (size_t gi = 0; gi < ng; ++gi) process_group(b, gi, dt_sub);
+            if (inner && ng > 2) {
+                // the parallel groups touch disjoint vertices; the last (non-parallel) group follows them
+                inner->run(ng - 1, [&](size_t gi) { process_group(b, gi, dt_sub); });
+                process_group(b, ng - 1, dt_sub);
+            } else {
+                for (size_t gi = 0; gi < ng; ++gi) process_group(b, gi, dt_sub);
+            }
             collide_and_update_velocities(b, shapes, g, dt_sub);
         }
         update_state(b, dt, disp_g);
@@ -413,15 +510,18 @@ public:
         V3<R> sub_g = mul(g, dt);
         R nv = R(float(b.v.size() > 0 ? b.v.size() : 1));
         V3<R> sub_imp = divs(mul(b.force, dt), nv);
-        for (auto &v : b.v) {
-            if (v.inv_mass > R(0)) {
-                v.vel = add(v.vel, add(sub_g, mul(sub_imp, v.inv_mass)));
-                v.vel = mul(v.vel, damp);
+        for_vertex_ranges(b.v.size(), [&](size_t first, size_t last) {
+            for (size_t i = first; i < last; ++i) {
+                Vertex<R> &v = b.v[i];
+                if (v.inv_mass > R(0)) {
+                    v.vel = add(v.vel, add(sub_g, mul(sub_imp, v.inv_mass)));
+                    v.vel = mul(v.vel, damp);
+                }
+                V3<R> p = v.pos;
+                v.prev = p;
+                v.pos = add(p, mul(v.vel, dt));
             }
-            V3<R> p = v.pos;
-            v.prev = p;
-            v.pos = add(p, mul(v.vel, dt));
-        }
+        });
     }
 
     void process_group(Body<R> &b, size_t gi, R dt) {  // :1030-1055
@@ -516,13 +616,20 @@ public:
     void collide_and_update_velocities(Body<R> &b, const std::vector<CollidingShape<R>> &shapes, V3<R> g, R dt) {  // :700-825
         R restitution_threshold = R(-2.0f) * len(g) * dt;
         R radius = R(b.cs.vertex_radius);
-        for (auto &v : b.v) {
-            if (!(v.inv_mass > R(0))) continue;
+        for_vertex_ranges(b.v.size(), [&](size_t first, size_t last) {
+            for (size_t i = first; i < last; ++i) collide_vertex(b.v[i], shapes, dt, restitution_threshold, radius);
+        });
+    }
+
+    // one vertex of ApplyCollisionConstraintsAndUpdateVelocities
+    void collide_vertex(Vertex<R> &v, const std::vector<CollidingShape<R>> &shapes, R dt, R restitution_threshold, R radius) {
+        {
+            if (!(v.inv_mass > R(0))) return;
             V3<R> prev_v = v.vel;
             v.vel = divs(sub(v.pos, v.prev), dt);
-            if (v.shape_idx < 0) continue;
+            if (v.shape_idx < 0) return;
             R projected = -(dot(v.pos, v.plane_n) + v.plane_c) + radius;
-            if (!(projected > R(0))) continue;
+            if (!(projected > R(0))) return;
             v.contact = true;
             const CollidingShape<R> &cs = shapes[v.shape_idx];
             V3<R> n = v.plane_n;
