@@ -95,6 +95,58 @@ def profile_traffic() -> float | None:
     return None
 
 
+def golden_full(name: str):
+    """Digests of the reference's own states over a configuration's whole run (tests/golden/full_<name>.npz,
+    written by tests/golden/make_golden.py from the reference built with JPH_CROSS_PLATFORM_DETERMINISTIC)."""
+    path = os.path.join(REPO, "tests", "golden", f"full_{name}.npz")
+    return np.load(path) if os.path.exists(path) else None
+
+
+def world_states(ctx, counts, offsets):
+    """(body position, local positions, velocities) of every body, float32, from one bulk download."""
+    loc = np.zeros((int(offsets[-1]), 3), np.float32)
+    vel = np.zeros_like(loc)
+    ctx.download_all(loc, vel)
+    import torch
+
+    torch.cuda.synchronize()  # (not jsb_synchronize: it would clear the device error word the run reports later)
+    pos = ctx.body_positions()
+    return [(pos[b], loc[offsets[b]:offsets[b + 1]], vel[offsets[b]:offsets[b + 1]]) for b in range(len(counts))]
+
+
+def parity_vs_reference(golden, scene_bytes, step_states) -> dict:
+    """Bodies whose state after each dump step is bit for bit the reference's (digest comparison)."""
+    import hashlib
+
+    from jsb_testlib import state_digest
+
+    if golden is None or hashlib.sha256(scene_bytes).digest() != golden["scene_sha256"].tobytes():
+        return {"checked": False, "why": "no reference digests for this scene"}
+    steps = [int(x) for x in golden["steps"]]
+    out = {"checked": True, "steps": [], "bodies": int(len(golden["num_vertices"]))}
+    for k, st in enumerate(steps):
+        if st not in step_states:
+            continue
+        equal = sum(state_digest(*b) == golden["digest"][k, i].tobytes() for i, b in enumerate(step_states[st]))
+        out["steps"].append({"step": st, "bodies_bitwise": int(equal)})
+    out["all_bitwise"] = bool(out["steps"]) and all(x["bodies_bitwise"] == out["bodies"] for x in out["steps"])
+    return out
+
+
+def world_error(states, ref_world) -> dict:
+    """Largest |GPU world position - reference| over vertices finite in both, and the bodies compared."""
+    worst, finite_bodies, nonfinite = 0.0, 0, 0
+    for (pos, loc, _), ref in zip(states, ref_world):
+        w = loc.astype(np.float64) + pos.astype(np.float64)
+        ok = np.isfinite(w).all(axis=1) & np.isfinite(ref).all(axis=1)
+        if not ok.all():
+            nonfinite += 1
+        if ok.any():
+            finite_bodies += 1
+            worst = max(worst, float(np.abs(w[ok] - ref[ok]).max()))
+    return {"max_abs_m": worst, "bodies_with_nonfinite_vertices": nonfinite}
+
+
 class ClockSampler:
     """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
 
@@ -191,22 +243,37 @@ def run_reference_arm(args, rank, world):
     print(json.dumps(line))
 
 
-def cpu_baseline(scene, budget_s: float = 12.0) -> dict:
-    sys.path.insert(0, os.path.join(REPO, "tests"))
-    from jsb_testlib import Oracle
+def cpu_baseline(scene, gpu_states: dict | None = None) -> dict:
+    """The CPU restatement of the reference (the oracle) over the configuration's whole run on all host
+    cores: its time is the CPU baseline; as the checker it also gives the GPU's final state's difference
+    from it (expected: none, bit for bit), and the FP64 re-evaluation of the same constraint order gives
+    the GPU's error against FP64 after the first and the last step (untimed)."""
+    from jsb_testlib import Oracle, state_digest
 
     threads = os.cpu_count() or 1
-    o = Oracle(scene, threads=threads)
+    n = scene.num_steps
+    nb = len(scene.bodies)
     vi_step = sum(b.num_vertices * b.num_iterations for b in scene.bodies)
-    t0 = time.perf_counter()
-    o.step(1)
-    first = time.perf_counter() - t0
-    n = max(1, min(scene.num_steps - 1, int(budget_s / max(first, 1e-6))))
+    o = Oracle(scene, threads=threads)
     t0 = time.perf_counter()
     o.step(n)
     dt = time.perf_counter() - t0
-    return {"value": vi_step * n / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"steps 2..{n + 1} of the run, all {len(scene.bodies)} bodies (after 1 warm-up step)"}
+    out = {"value": vi_step * n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"the whole {n}-step run, all {nb} bodies"}
+    if gpu_states and n in gpu_states:
+        ref = [o.body(b) for b in range(nb)]
+        same = sum(state_digest(*g) == state_digest(*r) for g, r in zip(gpu_states[n], ref))
+        out["oracle_check"] = {"step": n, "bodies_bitwise": int(same), "bodies": nb,
+                               **world_error(gpu_states[n], [r[1].astype(np.float64) + r[0] for r in ref])}
+        fp64 = {}
+        o64 = Oracle(scene, use_double=True, threads=threads)
+        done = 0
+        for st in sorted(x for x in (1, n) if x in gpu_states):
+            o64.step(st - done)
+            done = st
+            fp64[f"step_{st}"] = world_error(gpu_states[st], [o64.world_f64(b) for b in range(nb)])
+        out["fp64_error"] = fp64
+    return out
 
 
 def bench_adjoint(jsb, stream_ptr, steps: int = 90, every: int = 15) -> dict:
@@ -269,6 +336,25 @@ def bench_adjoint(jsb, stream_ptr, steps: int = 90, every: int = 15) -> dict:
             "timing": "host clock around synchronised work, median of 3 runs each, forward as a CUDA graph"}
 
 
+def gradient_checks(jsb) -> dict:
+    """Errors of the adjoint's gradients at the two differentiable configurations (tests/gradcheck.py):
+    the 64 x 64 cloth (120 steps, MSE loss at steps 60 and 120) against FP64 autodiff along the GPU's
+    own trajectory (bar 1e-3) and, for reference only, free-running FP64 central differences on 32
+    parameters (the cloth is chaotic over 120 steps); the same cloth over 6 steps against FP64 central
+    differences (bar 1e-3); the 256-body batch (90 steps, centre-of-mass loss) against FP64 central
+    differences of each perturbed body on 16 (body, axis) parameters (bar 1e-3 on those whose loss is
+    smooth at the 1e-7 scale)."""
+    from gradcheck import diff_batch_check, diff_cloth_check
+
+    t0 = time.perf_counter()
+    out = {"diff_cloth": diff_cloth_check(jsb, build_scene),
+           "diff_cloth_6_steps": diff_cloth_check(jsb, build_scene, steps=6, every=2, loss_steps=(3, 6), pinned=False),
+           "diff_batch": diff_batch_check(jsb, build_scene, n_params=16)}
+    out["diff_batch"].pop("not_smooth", None)
+    out["seconds"] = time.perf_counter() - t0
+    return out
+
+
 def bench_large_body(jsb, torch, stream, steps: int, with_cpu: bool) -> dict:
     """The 256 x 256 cloth (65,536 vertices, LRA tethers, sphere on a floor, 8 iterations) on the
     thread-block-cluster path: its 600-step run from the initial state, `steps` steps spread evenly over
@@ -289,6 +375,11 @@ def bench_large_body(jsb, torch, stream, steps: int, with_cpu: bool) -> dict:
     run_steps = max(ctx.scene_steps, steps)
     timed = sorted({max(1, round((j + 1) * run_steps / steps)) for j in range(steps)})
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in timed]
+    golden = golden_full("large_cloth")
+    check_steps = set(int(x) for x in golden["steps"]) if golden is not None else {1}
+    counts = np.asarray([ctx.total_vertices()], np.int64)
+    offsets = np.concatenate([[0], counts])
+    step_states = {}
     k = 0
     for step in range(1, run_steps + 1):
         with torch.cuda.stream(stream):
@@ -300,6 +391,9 @@ def bench_large_body(jsb, torch, stream, steps: int, with_cpu: bool) -> dict:
                 k += 1
             else:
                 ctx.step_graph(1, 1, stream=sptr)
+        if step in check_steps:  # read back between steps, outside every event pair
+            torch.cuda.synchronize()
+            step_states[step] = world_states(ctx, counts, offsets)
     torch.cuda.synchronize()
     ctx.synchronize()
     step_ms = [a.elapsed_time(b) for a, b in ev]
@@ -309,17 +403,23 @@ def bench_large_body(jsb, torch, stream, steps: int, with_cpu: bool) -> dict:
            "ms_per_step": ms, "step_ms_min_max": [min(step_ms), max(step_ms)], "value": vi_step / (ms / 1000.0),
            "unit": UNIT, "cluster": cfg}
     ctx.close()
+    out["parity"] = {"vs_reference": parity_vs_reference(golden, scene_bytes, step_states)}
     if with_cpu:
         from jsb_testlib import Oracle, parse_scene
 
         scene, _ = parse_scene(scene_bytes)
-        o = Oracle(scene)
+        threads = os.cpu_count() or 1
+        o = Oracle(scene, threads=threads)
         o.step(1)
         t0 = time.perf_counter()
-        o.step(2)
+        o.step(4)
         dt = time.perf_counter() - t0
-        out["cpu_baseline"] = {"value": vi_step * 2 / dt, "unit": UNIT, "cores": 1, "kind": "port",
-                               "sample": "steps 2-3 of the run (one body: the oracle runs it on one thread)"}
+        out["cpu_baseline"] = {"value": vi_step * 4 / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": "steps 2-5 of the run (one body: its parallel update groups and per-vertex "
+                                         "passes spread over the threads, the non-parallel group on one)"}
+        o64 = Oracle(scene, use_double=True, threads=threads)
+        o64.step(1)
+        out["fp64_error"] = {"step_1": world_error(step_states[1], [o64.world_f64(0)])} if 1 in step_states else {}
     return out
 
 
@@ -350,9 +450,28 @@ def bench_pinned_cloth(jsb, torch, stream, with_cpu: bool, autotune: bool = True
         e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
+    # parity: the final state against the reference's deterministic build (bitwise) and its default FMA
+    # build (the stated tolerance: <= 1e-5 m after 1 step, <= 1e-3 m after 300), then step 1 again
+    g = np.load(os.path.join(REPO, "tests", "golden", "pinned_cloth.npz"))
+    counts = np.asarray([ctx.total_vertices()], np.int64)
+    offsets = np.concatenate([[0], counts])
+    states = {steps: world_states(ctx, counts, offsets)}
+    ctx.restore_all(initial)
+    ctx.step()
+    torch.cuda.synchronize()
+    states[1] = world_states(ctx, counts, offsets)
     ctx.close()
+    tol = {}
+    for st in (1, steps):
+        pos, loc, vel = states[st][0]
+        w = loc.astype(np.float64) + pos
+        tol[f"step_{st}"] = {
+            "bitwise_vs_deterministic_build": bool(np.array_equal(loc, g[f"det_local_{st}"]) and np.array_equal(vel, g[f"det_vel_{st}"])
+                                                   and np.array_equal(pos, g[f"det_pos_{st}"][0])),
+            "max_abs_m_vs_default_build": float(np.abs(w - (g[f"fast_local_{st}"].astype(np.float64) + g[f"fast_pos_{st}"][0])).max())}
     out = {"workload": "pinned_cloth 30x30", "steps": steps, "ms_per_step": ms / steps, "value": vi / (ms / 1000.0),
-           "unit": UNIT, "timing": "the whole run as one CUDA graph replay"}
+           "unit": UNIT, "timing": "the whole run as one CUDA graph replay",
+           "parity": {**tol, "bar": "<= 1e-5 m after 1 step and <= 1e-3 m after 300 steps against the default build"}}
     if with_cpu:
         from jsb_testlib import Oracle, parse_scene
 
@@ -362,6 +481,12 @@ def bench_pinned_cloth(jsb, torch, stream, with_cpu: bool, autotune: bool = True
         o.step(steps)
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": vi / dt, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"the {steps}-step run"}
+        o64 = Oracle(scene, use_double=True)
+        o64.step(1)
+        fp64 = {"step_1": world_error(states[1], [o64.world_f64(0)])}
+        o64.step(steps - 1)
+        fp64[f"step_{steps}"] = world_error(states[steps], [o64.world_f64(0)])
+        out["fp64_error"] = fp64
     return out
 
 
@@ -447,6 +572,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and large-body measurements")
     ap.add_argument("--large-steps", type=int, default=10)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch-shape table")
+    ap.add_argument("--no-grad-checks", action="store_true",
+                    help="skip the gradient checks at the two differentiable configurations (about 90 s of CPU)")
     ap.add_argument("--table", help="profiling driver: launch-shape table [[max_vertices, threads, state_mode], ...] "
                                     "(e.g. the bench line's config.buckets_max_vertices_threads_state)")
     ap.add_argument("--profile", choices=["uneven_batch", "large_cloth", "diff_batch_adjoint"],
@@ -507,6 +634,12 @@ def main():
     # own arithmetic, which this solver reproduces), so evenly spread samples stand for the whole run.
     run_steps = max(scene.num_steps, args.steps)
     timed = sorted({max(1, round((j + 1) * run_steps / args.steps)) for j in range(args.steps)})
+    golden = golden_full(WORKLOAD) if rank == 0 and world == 1 else None
+    check_steps = set(int(x) for x in golden["steps"]) if golden is not None else set()
+    check_steps |= {1, run_steps}
+    counts = np.asarray([b.num_vertices for b in scene.bodies], np.int64)
+    offsets = np.concatenate([[0], np.cumsum(counts)])
+    step_states = {}
     ctx.restore_all(initial)
     starts = [torch.cuda.Event(enable_timing=True) for _ in timed]
     ends = [torch.cuda.Event(enable_timing=True) for _ in timed]
@@ -528,6 +661,9 @@ def main():
                     k += 1
                 else:
                     ctx.step_graph(1, 1, stream=sptr)
+            if step in check_steps and rank == 0:  # read back between steps, outside every event pair
+                torch.cuda.synchronize()
+                step_states[step] = world_states(ctx, counts, offsets)
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall
     non_finite = False
@@ -615,6 +751,10 @@ def main():
     mean_step_s = total_ms / 1000.0 / n_timed
     achieved = bytes_step / mean_step_s / 1e9
     traffic = profile_traffic()
+    clock_summary = clocks.summary()
+    num_sms = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_mhz = clock_summary.get("sm_mhz") or clock_summary.get("sm_max_mhz") or 2070.0
+    smem_peak = num_sms * 128.0 * sm_mhz * 1e6 / 1e9  # GB/s: 128 B per clock per SM
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -637,19 +777,26 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                      "peak_source": peaks["source"], "algorithmic_bytes_per_step": bytes_step},
+        "roofline_smem": {"bound": "shared memory (vertex state and staged records live there during the step)",
+                          "achieved": achieved, "peak": smem_peak, "unit": "GB/s", "frac": achieved / smem_peak,
+                          "peak_source": f"{num_sms} SMs x 128 B/clk x {sm_mhz:.0f} MHz (median SM clock in the timed region)"},
+        "parity": {"vs_reference": parity_vs_reference(golden, scene_bytes, step_states),
+                   "note": "state digests of every body after the reference's dump steps of the same run"},
         "plain": {"value": plain_value, "unit": UNIT, "steps": args.plain_steps, "state": "mid-run",
                   "batched_same_state": batched_same,
                   "batched_over_plain": (batched_same / plain_value) if plain_value else None},
-        "clocks": clocks.summary(),
+        "clocks": clock_summary,
         "wall_s": t_wall,
     }
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(scene)
+        line["cpu_baseline"] = cpu_baseline(scene, step_states)
     if not args.no_extras:
         line["adjoint"] = bench_adjoint(jsb, sptr)
         line["large_body"] = bench_large_body(jsb, torch, stream, args.large_steps, not args.no_cpu_baseline)
         line["pinned_cloth"] = bench_pinned_cloth(jsb, torch, stream, not args.no_cpu_baseline, not args.no_autotune)
         line["diff_cloth_adjoint"] = bench_diff_cloth(jsb)
+        if not args.no_cpu_baseline and not args.no_grad_checks:
+            line["gradient_checks"] = gradient_checks(jsb)
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

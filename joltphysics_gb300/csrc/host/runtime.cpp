@@ -123,6 +123,7 @@ struct DevBuf {
 struct StepSchedRec {
     StepSchedule sched;
     DevBuf<uint4> levels, records;
+    std::map<uint32_t, std::pair<DevBuf<uint4>, uint32_t>> chunks;  // staging chunks by ring half: (table, count)
 };
 
 struct SettingsRec {
@@ -132,6 +133,7 @@ struct SettingsRec {
     DevBuf<uint4> levels, records, faces;
     DevBuf<uint32_t> vf_off_dev, vf_dev;
     std::map<uint32_t, std::unique_ptr<StepSchedRec>> steps;  // by iteration count; null: none (a level too wide)
+    std::map<uint32_t, std::pair<DevBuf<uint4>, uint32_t>> chunks;  // staging chunks of `schedule` by ring half
 };
 
 struct BodyRec {
@@ -156,7 +158,7 @@ struct LaunchGroup {  // the bodies of one bucket (or every body on the cluster 
     int threads = 0;
     bool smem_state = true;  // velocities / previous positions staged in shared memory
     uint32_t smem_vertices = 0, smem_faces = 0;
-    uint32_t ring_slots = 32;  // record ring capacity per level
+    uint32_t ring_slots = 32;  // record slots per schedule-ring half (staging chunks are built for it)
     int grid = 0;
     std::vector<uint32_t> bodies;
     DevBuf<uint32_t> work;
@@ -169,7 +171,7 @@ struct LaunchGroup {  // the bodies of one bucket (or every body on the cluster 
 struct AdjGroup {
     DevBuf<uint32_t> work;
     uint32_t num_work = 0;
-    uint32_t cap_vertices = 0, cap_faces = 0, ring_slots = 32, max_level_slots = 0;
+    uint32_t cap_vertices = 0, cap_faces = 0, ring_slots = 32, max_level_slots = 0;  // ring_slots: the forward group's
     int threads = 128;  // taped forward and adjoint CTAs: 256 when levels are wider than 192 slots
     bool tape_smem_state = true;
     int tape_grid = 1, adj_grid = 1;
@@ -239,6 +241,7 @@ struct jsb_context {
     jsb::DevBuf<float4> x, v, prev, plane;
     jsb::DevBuf<int32_t> shape;
     jsb::DevBuf<jsb::BodyDesc> descs;
+    std::vector<jsb::BodyDesc> descs_host;  // staging chunks are set when the launch groups are built
     jsb::DevBuf<jsb::BodyState> states;
     jsb::DevBuf<jsb::ColliderDev> colliders_dev;
     jsb::DevBuf<uint32_t> queues;
@@ -332,6 +335,9 @@ BodyDesc make_desc(const jsb_context *ctx, const BodyRec &b) {
     d.step_levels = ss ? ss->levels.ptr : nullptr;
     d.step_records = ss ? ss->records.ptr : nullptr;
     d.num_step_levels = ss ? ss->sched.num_levels : 0u;
+    d.chunks = d.step_chunks = nullptr;  // set by attach_chunks for the ring of the body's launch group
+    d.num_chunks = d.num_step_chunks = 0;
+    d.stage_half = 0;
     d.num_faces = uint32_t(s.parsed.faces.size());
     d.num_vertices = uint32_t(s.parsed.vertices.size());
     d.vtx_offset = b.vtx_offset;
@@ -363,13 +369,50 @@ uint32_t ring_slots_for(const SettingsRec &s) {
     return std::max<uint32_t>(32u, std::min(r, kMaxRingSlots));
 }
 
-// Record ring capacity for body b: its whole-step schedule's widest level when it walks one.
+// Widest level of the schedule body b walks (rounded up to 32 slots, capped).
 uint32_t ring_slots_for(const jsb_context *ctx, const BodyRec &b) {
     const SettingsRec &s = *ctx->settings[b.settings_id];
     const StepSchedRec *ss = step_sched(ctx, b);
     if (!ss) return ring_slots_for(s);
     uint32_t r = (ss->sched.max_level_slots + 31u) & ~31u;
     return std::max<uint32_t>(32u, std::min(r, kMaxStepRingSlots));
+}
+
+// Record slots per schedule-ring half wanted for body b: two of its widest levels, so that narrow levels
+// stage several to a chunk.
+uint32_t ring_half_for(const jsb_context *ctx, const BodyRec &b) { return 2 * ring_slots_for(ctx, b); }
+
+// Staging chunks of a schedule for ring halves of `half` slots, built and uploaded once per half.
+jsb_status chunk_table(std::map<uint32_t, std::pair<DevBuf<uint4>, uint32_t>> &cache, const std::vector<uint32_t> &levels,
+                       uint32_t num_levels, bool per_substep, uint32_t half, const uint4 *&ptr, uint32_t &count) {
+    auto it = cache.find(half);
+    if (it == cache.end()) {
+        std::vector<uint32_t> c = build_stage_chunks(levels, num_levels, per_substep, half);
+        auto &e = cache[half];
+        JSB_CUDA(e.first.upload(reinterpret_cast<const uint4 *>(c.data()), c.size() / 4));
+        e.second = uint32_t(c.size() / 4);
+        it = cache.find(half);
+    }
+    ptr = it->second.first.ptr;
+    count = it->second.second;
+    return JSB_OK;
+}
+
+// Points body bi's descriptor at the staging chunks of its schedules for ring halves of `half` slots.
+jsb_status attach_chunks(jsb_context *ctx, uint32_t bi, uint32_t half) {
+    BodyRec &b = ctx->bodies[bi];
+    SettingsRec &s = *ctx->settings[b.settings_id];
+    BodyDesc &d = ctx->descs_host[bi];
+    d.stage_half = half;
+    jsb_status st = chunk_table(s.chunks, s.schedule.padded_levels, s.schedule.num_levels, true, half, d.chunks, d.num_chunks);
+    if (st != JSB_OK) return st;
+    d.step_chunks = nullptr;
+    d.num_step_chunks = 0;
+    if (step_sched(ctx, b)) {
+        StepSchedRec &ss = *s.steps[b.creation.num_iterations];
+        st = chunk_table(ss.chunks, ss.sched.levels, ss.sched.num_levels, false, half, d.step_chunks, d.num_step_chunks);
+    }
+    return st;
 }
 
 double body_cost(const jsb_context *ctx, const BodyRec &b, int threads) {
@@ -434,9 +477,9 @@ jsb_status rebuild(jsb_context *ctx) {
     ctx->total_vertices = total;
     jsb_status sst = ensure_step_schedules(ctx);
     if (sst != JSB_OK) return sst;
-    std::vector<BodyDesc> descs;
-    for (const BodyRec &b : ctx->bodies) descs.push_back(make_desc(ctx, b));
-    JSB_CUDA(ctx->descs.upload(descs.data(), descs.size()));
+    ctx->descs_host.clear();
+    for (const BodyRec &b : ctx->bodies) ctx->descs_host.push_back(make_desc(ctx, b));
+    JSB_CUDA(ctx->descs.upload(ctx->descs_host.data(), ctx->descs_host.size()));
     JSB_CUDA(ctx->states.upload(hstate.data(), hstate.size()));
     JSB_CUDA(ctx->colliders_dev.upload(ctx->colliders.data(), ctx->colliders.size()));
     ctx->pending_force.resize(ctx->bodies.size() * 3, 0.0f);
@@ -515,7 +558,7 @@ jsb_status rebuild_groups(jsb_context *ctx) {
         const uint32_t nv = uint32_t(s.parsed.vertices.size());
         size_t k = bucket_for(ctx, nv);
         // Bodies whose positions do not fit one CTA's shared memory take the cluster path.
-        if (ctx->buckets[k].state_mode == 2 || step_smem_bytes(false, nv, pressure_faces(s, b), ring_slots_for(s)) > cap) {
+        if (ctx->buckets[k].state_mode == 2 || step_smem_bytes(false, nv, pressure_faces(s, b), 32) > cap) {
             if (pressure_faces(s, b) > 0)
                 return fail(JSB_ERR_UNSUPPORTED, "a pressurised body with " + std::to_string(nv) +
                                                      " vertices is too large for one CTA, and the cluster path has no pressure");
@@ -529,19 +572,21 @@ jsb_status rebuild_groups(jsb_context *ctx) {
         ctx->groups.emplace_back();
         LaunchGroup &g = ctx->groups.back();
         g.threads = ctx->buckets[k].threads;
+        uint32_t widest = 32;
         for (auto &m : members[k]) {
             const BodyRec &b = ctx->bodies[m.second];
             const SettingsRec &s = *ctx->settings[b.settings_id];
             g.smem_vertices = std::max(g.smem_vertices, uint32_t(s.parsed.vertices.size()));
             g.smem_faces = std::max(g.smem_faces, pressure_faces(s, b));
-            g.ring_slots = std::max(g.ring_slots, ring_slots_for(ctx, b));
+            g.ring_slots = std::max(g.ring_slots, ring_half_for(ctx, b));
+            widest = std::max(widest, ring_slots_for(ctx, b));
         }
-        // A ring wider than the per-substep cap only serves whole-step walks: shrink it (down to that
-        // cap) before giving up shared-memory state.
+        // Ring halves: two of the widest level wanted; shrink towards one widest level before giving up
+        // shared-memory state, then further (wide levels are then staged in part and read in place).
         if (ctx->buckets[k].state_mode == 0)
-            while (g.ring_slots > kMaxRingSlots && step_smem_bytes(true, g.smem_vertices, g.smem_faces, g.ring_slots) > cap)
+            while (g.ring_slots > widest && step_smem_bytes(true, g.smem_vertices, g.smem_faces, g.ring_slots) > cap)
                 g.ring_slots -= 32;
-        while (g.ring_slots > kMaxRingSlots && step_smem_bytes(false, g.smem_vertices, g.smem_faces, g.ring_slots) > cap)
+        while (g.ring_slots > 32 && step_smem_bytes(false, g.smem_vertices, g.smem_faces, g.ring_slots) > cap)
             g.ring_slots -= 32;
         g.smem_state = ctx->buckets[k].state_mode == 0 && step_smem_bytes(true, g.smem_vertices, g.smem_faces, g.ring_slots) <= cap;
         if (step_smem_bytes(g.smem_state, g.smem_vertices, g.smem_faces, g.ring_slots) > cap)
@@ -549,7 +594,11 @@ jsb_status rebuild_groups(jsb_context *ctx) {
                                                  " vertices does not fit the shared-memory solver path");
         // Longest-processing-time-first order for the work queue.
         std::stable_sort(members[k].begin(), members[k].end(), [](const auto &a, const auto &b) { return a.first > b.first; });
-        for (auto &m : members[k]) g.bodies.push_back(m.second);
+        for (auto &m : members[k]) {
+            g.bodies.push_back(m.second);
+            jsb_status st = attach_chunks(ctx, m.second, g.ring_slots);
+            if (st != JSB_OK) return st;
+        }
         JSB_CUDA(g.work.upload(g.bodies.data(), g.bodies.size()));
         size_t smem = step_smem_bytes(g.smem_state, g.smem_vertices, g.smem_faces, g.ring_slots);
         int occ = step_occupancy(g.threads, g.smem_state, smem);
@@ -561,6 +610,7 @@ jsb_status rebuild_groups(jsb_context *ctx) {
         jsb_status st = make_cluster_group(ctx, cluster_bodies, cap);
         if (st != JSB_OK) return st;
     }
+    JSB_CUDA(ctx->descs.upload(ctx->descs_host.data(), ctx->descs_host.size()));
     // Larger buckets get higher stream priority (and are launched first): their bodies carry the
     // longest dependency chains, and a CTA sized for them needs an SM nobody else occupies.
     int least = 0, greatest = 0;
@@ -656,7 +706,7 @@ jsb_status step_impl(jsb_context *ctx, float dt, int collision_steps, cudaStream
                     p.num_work = 1;
                     p.queue = ctx->queues.ptr;
                     const SettingsRec &s = *ctx->settings[ctx->bodies[b].settings_id];
-                    p.ring_slots = g.cluster > 0 ? ring_slots_for(s) : std::min(ring_slots_for(ctx, ctx->bodies[b]), g.ring_slots);
+                    p.ring_slots = g.ring_slots;  // the ring the body's staging chunks were built for
                     if (g.cluster > 0)
                         JSB_CUDA(launch_cluster_step(p, g.cluster, g.threads, g.shift, g.desc_cap, g.rpt, stream));
                     else
@@ -1550,14 +1600,11 @@ jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int chec
             const SettingsRec &s = *ctx->settings[br.settings_id];
             ag.cap_vertices = std::max(ag.cap_vertices, uint32_t(s.parsed.vertices.size()));
             ag.cap_faces = std::max(ag.cap_faces, pressure_faces(s, br));
-            ag.ring_slots = std::max(ag.ring_slots, ring_slots_for(ctx, br));
             const StepSchedRec *ss = step_sched(ctx, br);
             ag.max_level_slots = std::max(ag.max_level_slots, ss ? ss->sched.max_level_slots : s.schedule.max_level_slots);
         }
-        while (ag.ring_slots > kMaxRingSlots && step_smem_bytes(true, ag.cap_vertices, ag.cap_faces, ag.ring_slots) > cap) ag.ring_slots -= 32;
+        ag.ring_slots = g.ring_slots;  // the ring the bodies' staging chunks were built for
         ag.tape_smem_state = step_smem_bytes(true, ag.cap_vertices, ag.cap_faces, ag.ring_slots) <= cap;
-        while (ag.ring_slots > kMaxRingSlots && step_smem_bytes(ag.tape_smem_state, ag.cap_vertices, ag.cap_faces, ag.ring_slots) > cap)
-            ag.ring_slots -= 32;
         const size_t tsmem = step_smem_bytes(ag.tape_smem_state, ag.cap_vertices, ag.cap_faces, ag.ring_slots);
         ag.threads = ag.max_level_slots > 192 ? 256 : 128;
         const uint32_t T = uint32_t(ag.threads);

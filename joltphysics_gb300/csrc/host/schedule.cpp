@@ -144,6 +144,12 @@ Schedule build_schedule(const ParsedSettings &s) {
     std::vector<uint32_t> bucket_start(count.begin(), count.end());
     std::vector<uint32_t> order(n);
     for (uint32_t k = 0; k < n; ++k) order[count[items[k].level * 4 + items[k].type]++] = k;
+    // Inside a level the LRA constraints are ordered by anchor (stably): tethers sharing an anchor sit
+    // next to each other, which the adjoint uses to sum their anchor terms in a fixed order. Order
+    // inside a level does not change the forward result.
+    for (uint32_t l = 0; l < out.num_levels; ++l)
+        std::stable_sort(order.begin() + bucket_start[l * 4 + 3], order.begin() + bucket_start[l * 4 + 4],
+                         [&](uint32_t a, uint32_t b) { return s.lras[items[a].index].v[0] < s.lras[items[b].index].v[0]; });
     out.levels.resize(size_t(out.num_levels + 2) * 4);
     for (uint32_t l = 0; l < out.num_levels; ++l) {
         out.levels[l * 4 + 0] = bucket_start[l * 4 + 0];
@@ -324,7 +330,7 @@ bool build_step_schedule(const ParsedSettings &s, uint32_t num_iterations, StepS
         return u;
     };
     // items are in sequence order, so filling each (level, type) in that order keeps the in-level order
-    // of build_schedule
+    // of build_schedule (LRA constraints are reordered by anchor below, as there)
     for (const Item &it : items) {
         const uint32_t k = slot_of[size_t(it.level) * 5 + it.type]++;
         uint32_t *r = &out.records[size_t(k) * 4];
@@ -368,7 +374,47 @@ bool build_step_schedule(const ParsedSettings &s, uint32_t num_iterations, StepS
                 break;
         }
     }
+    // LRA constraints of a level ordered by anchor (stably; the slots before the padding)
+    for (uint32_t l = 0; l < L; ++l) {
+        const uint32_t first = out.levels[l * 4] + (out.levels[l * 4 + 2] & 0xffffu);
+        const uint32_t n = count[size_t(l) * 5 + kLRA];
+        if (n < 2) continue;
+        std::vector<uint32_t> idx(n);
+        for (uint32_t k = 0; k < n; ++k) idx[k] = k;
+        std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) {
+            return (out.records[size_t(first + a) * 4] & 0xffffu) < (out.records[size_t(first + b) * 4] & 0xffffu);
+        });
+        std::vector<uint32_t> rec(size_t(n) * 4), src;
+        for (uint32_t k = 0; k < n; ++k)
+            for (int w = 0; w < 4; ++w) rec[size_t(k) * 4 + w] = out.records[size_t(first + idx[k]) * 4 + w];
+        std::copy(rec.begin(), rec.end(), out.records.begin() + size_t(first) * 4);
+        if (with_source) {
+            src.resize(size_t(n) * 2);
+            for (uint32_t k = 0; k < n; ++k)
+                for (int w = 0; w < 2; ++w) src[size_t(k) * 2 + w] = out.source[size_t(first + idx[k]) * 2 + w];
+            std::copy(src.begin(), src.end(), out.source.begin() + size_t(first) * 2);
+        }
+    }
     return true;
+}
+
+std::vector<uint32_t> build_stage_chunks(const std::vector<uint32_t> &levels4, uint32_t num_levels, bool per_substep,
+                                         uint32_t half_slots) {
+    std::vector<uint32_t> out;
+    auto slots = [&](uint32_t l) { return per_substep ? levels4[(l + 1) * 4] - levels4[l * 4] : levels4[l * 4 + 3]; };
+    uint32_t l = 0;
+    while (l < num_levels) {
+        const uint32_t first = levels4[l * 4];
+        uint32_t end = l, total = 0;
+        while (end < num_levels && end - l < kStageLevels && total + slots(end) <= half_slots) total += slots(end++);
+        if (end == l) {  // one level wider than a half: stage its first half_slots slots
+            end = l + 1;
+            total = half_slots;
+        }
+        out.insert(out.end(), {l, end, first, total});
+        l = end;
+    }
+    return out;
 }
 
 }  // namespace jsb

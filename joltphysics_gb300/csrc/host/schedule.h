@@ -5,6 +5,8 @@
 #include <string>
 #include <vector>
 
+#include "../kernels/device_types.h"
+
 namespace jsb {
 
 // Parsed SoftBodySharedSettings::SaveBinaryState bytes (SoftBodySharedSettings.cpp:1203-1236).
@@ -114,5 +116,17 @@ enum : uint32_t { kVertexOp = 4 };
 // Returns false (and leaves `out` empty) when a level holds 65,536 slots or more, or num_iterations < 2.
 // `with_source` also fills `source` (for tests of the order).
 bool build_step_schedule(const ParsedSettings &s, uint32_t num_iterations, StepSchedule &out, bool with_source = false);
+
+// Staging chunks of a level schedule. The walkers stage a schedule's records and level descriptors
+// into shared memory chunk by chunk, with one bulk copy of each per chunk, into the two halves of a
+// ring (chunk c into half c % 2, two chunks in flight). A chunk is a run of consecutive levels whose
+// slots fit `half_slots` and whose descriptors fit kStageLevels, or one wider level, of which the
+// first half_slots slots are staged (the walker reads the rest in place).
+//   chunk = {first level, end level, first slot, staged slots}, 4 uint32 each.
+// levels4: per-substep layout (Schedule::padded_levels: a level's slots end where the next level's
+// begin; num_levels + 2 entries) when per_substep, else the whole-step layout (StepSchedule::levels,
+// slot count in the fourth word).
+std::vector<uint32_t> build_stage_chunks(const std::vector<uint32_t> &levels4, uint32_t num_levels, bool per_substep,
+                                         uint32_t half_slots);
 
 }  // namespace jsb

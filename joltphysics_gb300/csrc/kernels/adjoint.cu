@@ -103,21 +103,47 @@ __device__ __forceinline__ void volume_adjoint(float4 *lx, const float *sw, uint
     lx[i4] = with_w(L4 + lcv, 0.0f);
 }
 
-// x1' = x0 + d md / |d| when |d| > md (d = x1 - x0); the anchor x0 is only read.
-__device__ __forceinline__ void lra_adjoint(float4 *lx, uint4 r, const float4 *tin) {
-    const uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16;
+// x1' = x0 + d md / |d| when |d| > md (d = x1 - x0); the anchor x0 is only read. The anchor's term is
+// left in `anchor_term` (the slot's unused second tape entry) and added by lra_anchor_sums after the
+// level: several tethers of one level may share an anchor.
+__device__ __forceinline__ void lra_adjoint(float4 *lx, uint4 r, const float4 *tin, float4 *anchor_term) {
+    const uint32_t i1 = r.x >> 16;
     const float md = __uint_as_float(r.z);
     const f3 dl = xyz(tin[0]);
     const float dls = len_sq(dl);
-    if (!(dls > md * md)) return;
+    if (!(dls > md * md)) {
+        *anchor_term = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return;
+    }
     const float L = sqrtf(dls);
     const f3 l = xyz(lx[i1]);
     const f3 ldl = (md / L) * (l - dl * (dot(dl, l) / dls));
-    const f3 add = l - ldl;
-    atomicAdd(&lx[i0].x, add.x);
-    atomicAdd(&lx[i0].y, add.y);
-    atomicAdd(&lx[i0].z, add.z);
+    *anchor_term = with_w(l - ldl, 0.0f);
     lx[i1] = with_w(ldl, 0.0f);
+}
+
+// After a level's reverse: adds the anchor terms of its LRA slots [first, end) (schedule slot indices)
+// to the anchors' adjoints, each anchor's terms summed in slot order by the thread holding the first of
+// them (the host orders a level's LRA slots by anchor), so the result does not depend on thread timing.
+template <int T>
+__device__ __forceinline__ void lra_anchor_sums(float4 *lx, const uint4 *__restrict__ rec, const float4 *cons, uint32_t first,
+                                                uint32_t end) {
+    for (uint32_t c = first + threadIdx.x; c < end; c += T) {
+        const uint4 r = __ldg(rec + c);
+        if (r.x == 0xffffffffu) continue;
+        const uint32_t a = r.x & 0xffff;
+        if (c > first) {
+            const uint32_t p = __ldg(rec + c - 1).x;
+            if (p != 0xffffffffu && (p & 0xffff) == a) continue;  // not the first tether of its anchor
+        }
+        f3 acc = xyz(lx[a]);
+        for (uint32_t k = c; k < end; ++k) {
+            const uint32_t rk = __ldg(rec + k).x;
+            if (rk == 0xffffffffu || (rk & 0xffff) != a) break;
+            acc = acc + xyz(cons[size_t(k) * 3 + 1]);
+        }
+        lx[a] = with_w(acc, 0.0f);
+    }
 }
 
 
@@ -165,7 +191,7 @@ __device__ __forceinline__ void adj_cp_async_wait(uint32_t pending) {
 // shared-memory ring with cp.async; a thread reads only what it copied itself, so the ring needs no
 // barrier. Ring layout: [(depth + 1) levels][rpt slots][record, 3 taped inputs][T threads] x 16 bytes.
 template <int T>
-__device__ __forceinline__ void reverse_levels(float4 *lx, const float *sw, const BodyDesc &d, const float4 *cons, float *grad,
+__device__ __forceinline__ void reverse_levels(float4 *lx, const float *sw, const BodyDesc &d, float4 *cons, float *grad,
                                                float inv_dt_sq, uint4 *ring, uint32_t depth, uint32_t rpt) {
     const uint4 *__restrict__ levels = d.levels;
     const uint4 *__restrict__ rec = d.records;
@@ -231,9 +257,13 @@ __device__ __forceinline__ void reverse_levels(float4 *lx, const float *sw, cons
             else if (type == 1)
                 volume_adjoint(lx, sw, r, tin, inv_dt_sq, grad + c);
             else if (type == 3)
-                lra_adjoint(lx, r, tin);
+                lra_adjoint(lx, r, tin, cons + size_t(c) * 3 + 1);
         }
         __syncthreads();
+        if (lv.w < n) {  // LRA slots [lv.w, n)
+            lra_anchor_sums<T>(lx, rec, cons, lv.x + lv.w, lv.x + n);
+            __syncthreads();
+        }
     }
     if (depth > 0) adj_cp_async_wait(0);
 }
@@ -362,7 +392,7 @@ __device__ __forceinline__ void integrate_adjoint(const VertexAdj &a, uint32_t i
 // reverse_levels. d loss / d compliance accumulates per whole-step slot (the host sums a constraint's
 // slots over the substeps).
 template <int T>
-__device__ __forceinline__ void reverse_step_levels(const VertexAdj &a, const BodyDesc &d, const float4 *cons, float *grad,
+__device__ __forceinline__ void reverse_step_levels(const VertexAdj &a, const BodyDesc &d, float4 *cons, float *grad,
                                                     float inv_dt_sq, uint4 *ring, uint32_t depth, uint32_t rpt, f3 &force_acc) {
     const uint4 *__restrict__ levels = d.step_levels;
     const uint4 *__restrict__ rec = d.step_records;
@@ -436,10 +466,14 @@ __device__ __forceinline__ void reverse_step_levels(const VertexAdj &a, const Bo
             } else if (type == 1) {
                 volume_adjoint(a.lx, a.sw, r, tin, inv_dt_sq, grad + c);
             } else if (type == 3) {
-                lra_adjoint(a.lx, r, tin);
+                lra_adjoint(a.lx, r, tin, cons + size_t(c) * 3 + 1);
             }
         }
         __syncthreads();
+        if ((lv.z & 0xffffu) < (lv.z >> 16)) {  // LRA slots [edge end, LRA end)
+            lra_anchor_sums<T>(a.lx, rec, cons, lv.x + (lv.z & 0xffffu), lv.x + (lv.z >> 16));
+            __syncthreads();
+        }
     }
     if (depth > 0) adj_cp_async_wait(0);
 }

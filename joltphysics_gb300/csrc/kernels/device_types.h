@@ -37,6 +37,7 @@
 namespace jsb {
 
 constexpr uint32_t kMaxVerticesPerBody = 65536;
+constexpr uint32_t kStageLevels = 64;  // level descriptors per schedule-ring half (the per-substep walk stages one more)
 constexpr uint32_t kMaxCollidingShapes = 16;  // colliding shapes kept per body per step
 
 enum : uint32_t { kFlagUpdatePosition = 1u };
@@ -61,6 +62,13 @@ struct BodyDesc {
     const uint4 *step_levels;
     const uint4 *step_records;
     uint32_t num_step_levels;
+    // staging chunks of the two schedules (host/schedule.h build_stage_chunks) for ring halves of
+    // stage_half record slots: {first level, end level, first slot, staged slots}
+    const uint4 *chunks;
+    const uint4 *step_chunks;
+    uint32_t num_chunks;
+    uint32_t num_step_chunks;
+    uint32_t stage_half;
     // body
     uint32_t vtx_offset;
     uint32_t num_iterations;
@@ -129,7 +137,7 @@ struct StepParams {
     uint32_t *error;
     const float *forces;  // 3 floats per body: AddForce accumulators consumed by this step
     const float *step_forces;  // 3 floats per body: force added before every step (persistent)
-    uint32_t ring_slots;  // record ring capacity per level (multiple of 32); wider levels read HBM/L2 directly
+    uint32_t ring_slots;  // record slots per schedule-ring half (>= every launched body's stage_half)
     const TapeDesc *tape;  // per-body tapes (taped forward only)
     uint32_t tape_step;    // step index within the checkpoint segment (taped forward only)
 };

@@ -43,55 +43,61 @@ __device__ __forceinline__ float4 nan_w(float w) {
 // ---------------------------------------------------------------------------------------------
 // Constraint projections (exact reference arithmetic)
 // ---------------------------------------------------------------------------------------------
-template <bool kGuard = false, class X>
-__device__ __forceinline__ void project_bend(X sx, uint4 r, float inv_dt_sq) {  // :367-456
+// Each projection is written once over a division / square-root policy (common.cuh): it runs with
+// FastOps, and when an operand fell outside FastOps' range it runs again with IeeeOps. The `_impl`
+// functions store nothing on the first run unless FastOps stayed in range, and return true when the
+// projection has to be repeated with IeeeOps; with IeeeOps they always finish (return false).
+template <bool kGuard, class Ops, class X>
+__device__ __forceinline__ bool project_bend_impl(X sx, uint4 r, float inv_dt_sq, Ops &op) {  // :367-456
     uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16, i2 = r.y & 0xffff, i3 = r.y >> 16;
     float compliance = __uint_as_float(r.z), initial_angle = __uint_as_float(r.w);
     float4 p0 = ldx(sx, i0), p1 = ldx(sx, i1), p2 = ldx(sx, i2), p3 = ldx(sx, i3);
     f3 x0 = xyz(p0), x1 = xyz(p1), x2 = xyz(p2), x3 = xyz(p3);
     if (kGuard && (has_nan(x0) || has_nan(x1) || has_nan(x2) || has_nan(x3))) {
         // e_len < 1e-6 is the only exit that can still be taken: with x0 and x1 finite and close
-        if (!has_nan(x0) && !has_nan(x1) && len(x1 - x0) < 1.0e-6f) return;
+        if (!has_nan(x0) && !has_nan(x1) && len(x1 - x0) < 1.0e-6f) return false;
         stx(sx, i0, nan_w(p0.w));
         stx(sx, i1, nan_w(p1.w));
         stx(sx, i2, nan_w(p2.w));
         stx(sx, i3, nan_w(p3.w));
-        return;
+        return false;
     }
     f3 e = x1 - x0;
-    float e_len = len(e);
-    if (e_len < 1.0e-6f) return;
+    float e_len = len_op(op, e);
+    if (e_len < 1.0e-6f) return !op.ok();
     f3 x1x2 = x2 - x1, x1x3 = x3 - x1;
     f3 n1 = cross(x2 - x0, x1x2);
     f3 n2 = cross(x1x3, x3 - x0);
     float n1_len_sq = len_sq(n1), n2_len_sq = len_sq(n2);
     float n1n2 = n1_len_sq * n2_len_sq;
-    if (n1n2 < 1.0e-24f) return;
+    if (n1n2 < 1.0e-24f) return !op.ok();
     float sign = dot(cross(n2, n1), e) < 0.0f ? -1.0f : 1.0f;
-    float d = jdiv(dot(n1, n2), jsqrt(n1n2));
-    float c = sign * acos_approximate(d) - initial_angle;
+    float d = op.div(dot(n1, n2), op.sqrt(n1n2));
+    float c = sign * acos_approximate_op(op, d) - initial_angle;
     if (c > kPi)
         c -= 2.0f * kPi;
     else if (c < -kPi)
         c += 2.0f * kPi;
-    n1 = n1 / n1_len_sq;
-    n2 = n2 / n2_len_sq;
-    f3 d0c = (dot(x1x2, e) * n1 + dot(x1x3, e) * n2) / e_len;
+    n1 = op.div3(n1, n1_len_sq);
+    n2 = op.div3(n2, n2_len_sq);
+    f3 d0c = op.div3(dot(x1x2, e) * n1 + dot(x1x3, e) * n2, e_len);
     f3 d2c = e_len * n1;
     f3 d3c = e_len * n2;
     f3 d1c = (neg(d0c) - d2c) - d3c;
     float w0 = p0.w, w1 = p1.w, w2 = p2.w, w3 = p3.w;
     float denom = w0 * len_sq(d0c) + w1 * len_sq(d1c) + w2 * len_sq(d2c) + w3 * len_sq(d3c) + compliance * inv_dt_sq;
-    if (denom < 1.0e-12f) return;
-    float ml = jdiv(c, denom);
+    if (denom < 1.0e-12f) return !op.ok();
+    float ml = op.div(c, denom);
+    if (!op.ok()) return true;
     stx(sx, i0, with_w(x0 - (ml * w0) * d0c, w0));
     stx(sx, i1, with_w(x1 - (ml * w1) * d1c, w1));
     stx(sx, i2, with_w(x2 - (ml * w2) * d2c, w2));
     stx(sx, i3, with_w(x3 - (ml * w3) * d3c, w3));
+    return false;
 }
 
-template <bool kGuard = false, class X>
-__device__ __forceinline__ void project_volume(X sx, uint4 r, float inv_dt_sq) {  // :458-507
+template <bool kGuard, class Ops, class X>
+__device__ __forceinline__ bool project_volume_impl(X sx, uint4 r, float inv_dt_sq, Ops &op) {  // :458-507
     uint32_t i1 = r.x & 0xffff, i2 = r.x >> 16, i3 = r.y & 0xffff, i4 = r.y >> 16;
     float six_rest = __uint_as_float(r.z), compliance = __uint_as_float(r.w);
     float4 p1 = ldx(sx, i1), p2 = ldx(sx, i2), p3 = ldx(sx, i3), p4 = ldx(sx, i4);
@@ -101,7 +107,7 @@ __device__ __forceinline__ void project_volume(X sx, uint4 r, float inv_dt_sq) {
         stx(sx, i2, nan_w(p2.w));
         stx(sx, i3, nan_w(p3.w));
         stx(sx, i4, nan_w(p4.w));
-        return;
+        return false;
     }
     f3 x1x2 = x2 - x1, x1x3 = x3 - x1, x1x4 = x4 - x1;
     float c = fabsf(dot(cross(x1x2, x1x3), x1x4)) - six_rest;
@@ -111,16 +117,18 @@ __device__ __forceinline__ void project_volume(X sx, uint4 r, float inv_dt_sq) {
     f3 d4c = cross(x1x2, x1x3);
     float w1 = p1.w, w2 = p2.w, w3 = p3.w, w4 = p4.w;
     float denom = w1 * len_sq(d1c) + w2 * len_sq(d2c) + w3 * len_sq(d3c) + w4 * len_sq(d4c) + compliance * inv_dt_sq;
-    if (denom < 1.0e-12f) return;
-    float ml = jdiv(c, denom);
+    if (denom < 1.0e-12f) return false;
+    float ml = op.div(c, denom);
+    if (!op.ok()) return true;
     stx(sx, i1, with_w(x1 - (ml * w1) * d1c, w1));
     stx(sx, i2, with_w(x2 - (ml * w2) * d2c, w2));
     stx(sx, i3, with_w(x3 - (ml * w3) * d3c, w3));
     stx(sx, i4, with_w(x4 - (ml * w4) * d4c, w4));
+    return false;
 }
 
-template <bool kGuard = false, class X>
-__device__ __forceinline__ void project_edge(X sx, uint4 r, float inv_dt_sq) {  // :573-601
+template <bool kGuard, class Ops, class X>
+__device__ __forceinline__ bool project_edge_impl(X sx, uint4 r, float inv_dt_sq, Ops &op) {  // :573-601
     uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16;
     float rest = __uint_as_float(r.z), compliance = __uint_as_float(r.w);
     float4 p0 = ldx(sx, i0), p1 = ldx(sx, i1);
@@ -128,26 +136,66 @@ __device__ __forceinline__ void project_edge(X sx, uint4 r, float inv_dt_sq) {  
     if (kGuard && (has_nan(x0) || has_nan(x1))) {
         stx(sx, i0, nan_w(p0.w));
         stx(sx, i1, nan_w(p1.w));
-        return;
+        return false;
     }
     f3 delta = x1 - x0;
-    float length = len(delta);
+    float length = len_op(op, delta);
     float denom = length * (p0.w + p1.w + compliance * inv_dt_sq);
-    if (denom < 1.0e-12f) return;
-    f3 corr = (delta * (length - rest)) / denom;
+    if (denom < 1.0e-12f) return !op.ok();
+    f3 corr = op.div3(delta * (length - rest), denom);
+    if (!op.ok()) return true;
     stx(sx, i0, with_w(x0 + p0.w * corr, p0.w));
     stx(sx, i1, with_w(x1 - p1.w * corr, p1.w));
+    return false;
 }
 
-template <class X>
-__device__ __forceinline__ void project_lra(X sx, uint4 r) {  // :679-698
+template <class Ops, class X>
+__device__ __forceinline__ bool project_lra_impl(X sx, uint4 r, Ops &op) {  // :679-698
     uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16;
     float md = __uint_as_float(r.z);
     f3 x0 = xyz(ldx(sx, i0));
     float4 p1 = ldx(sx, i1);
     f3 delta = xyz(p1) - x0;
     float dls = len_sq(delta);
-    if (dls > md * md) stx(sx, i1, with_w(x0 + (delta * md) / jsqrt(dls), p1.w));
+    if (dls > md * md) {  // a NaN input fails the distance test: no division, no write
+        f3 np = x0 + op.div3(delta * md, op.sqrt(dls));
+        if (!op.ok()) return true;
+        stx(sx, i1, with_w(np, p1.w));
+    }
+    return false;
+}
+
+template <bool kGuard = false, class X>
+__device__ __forceinline__ void project_bend(X sx, uint4 r, float inv_dt_sq) {
+    FastOps f;
+    if (project_bend_impl<kGuard>(sx, r, inv_dt_sq, f)) {
+        IeeeOps e;
+        project_bend_impl<kGuard>(sx, r, inv_dt_sq, e);
+    }
+}
+template <bool kGuard = false, class X>
+__device__ __forceinline__ void project_volume(X sx, uint4 r, float inv_dt_sq) {
+    FastOps f;
+    if (project_volume_impl<kGuard>(sx, r, inv_dt_sq, f)) {
+        IeeeOps e;
+        project_volume_impl<kGuard>(sx, r, inv_dt_sq, e);
+    }
+}
+template <bool kGuard = false, class X>
+__device__ __forceinline__ void project_edge(X sx, uint4 r, float inv_dt_sq) {
+    FastOps f;
+    if (project_edge_impl<kGuard>(sx, r, inv_dt_sq, f)) {
+        IeeeOps e;
+        project_edge_impl<kGuard>(sx, r, inv_dt_sq, e);
+    }
+}
+template <class X>
+__device__ __forceinline__ void project_lra(X sx, uint4 r) {
+    FastOps f;
+    if (project_lra_impl(sx, r, f)) {
+        IeeeOps e;
+        project_lra_impl(sx, r, e);
+    }
 }
 
 template <bool kGuard = false, class X>
@@ -159,7 +207,7 @@ __device__ __forceinline__ void project(X sx, uint4 r, int type, float inv_dt_sq
     else if (type == 2)
         project_edge<kGuard>(sx, r, inv_dt_sq);
     else
-        project_lra(sx, r);  // a NaN input fails its distance test: no division, no write
+        project_lra(sx, r);
 }
 
 // Type of slot `s` of a level with descriptor {first slot, bend end, volume end, edge end}: the

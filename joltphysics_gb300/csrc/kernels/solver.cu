@@ -31,19 +31,14 @@ namespace jsb {
 namespace {
 
 
-// Level descriptors are staged this many levels ahead of the record staging into a ring of
-// kDescRing entries, so no level waits on a descriptor load from L2 / HBM.
-constexpr uint32_t kDescAhead = 8;
-constexpr uint32_t kDescRing = 16;
-
 struct Shared {
     SCol cols[kMaxCollidingShapes];
     int ncols;
     uint32_t item;
     float six_volume;
     float delta[3];
-    uint4 ring_desc[kDescRing];
-    uint64_t stage_bar;  // mbarrier of the bulk copies that stage a body's state (one phase per body)
+    uint64_t stage_bar;    // mbarrier of the bulk copies that stage a body's state (one phase per body)
+    uint64_t ring_bar[2];  // mbarriers of the two halves of the schedule ring (one phase per chunk)
     int last_nan[6];
     float red[32][4];  // per-warp partials for reductions
     int redi[32][4];
@@ -86,46 +81,44 @@ __device__ __forceinline__ bool stage_wait(uint64_t *bar, uint32_t parity) {
     return false;
 }
 
-// Record ring: kRingDepth levels of up to `slots` records each are streamed into shared memory
-// ahead of the level being projected; the ring holds kRingDepth + 1 levels.
-constexpr int kRingDepth = 3;
-constexpr int kRingLevels = kRingDepth + 1;
-
-struct LevelRing {
-    uint4 *rec;      // [kRingLevels][slots]
-    uint4 *desc;     // [kDescRing] level descriptors, staged kDescAhead levels ahead of the records
-    uint32_t slots;  // capacity per level
+// ---- schedule ring ----------------------------------------------------------------------------------
+// A schedule's records and level descriptors reach shared memory chunk by chunk (host/schedule.h,
+// build_stage_chunks): one thread issues two bulk copies per chunk (records, descriptors) on the TMA
+// unit, completing on the mbarrier of one half of a two-half ring, two chunks ahead of the walk. A
+// chunk is a run of levels that fits a half, so the walk's per-level critical path has no staging in
+// it: descriptor and records from shared memory, positions from shared memory, projection, barrier.
+struct StageRing {
+    uint4 *rec;      // [2][half] record slots
+    uint4 *desc;     // [2][kStageLevels + 1] level descriptors
+    uint32_t half;   // record slots per half (>= the staged slots of every chunk of the bodies launched)
+    uint64_t *bar;   // [2]
 };
 
-// Descriptor ring. The first kDescAhead descriptors are stored directly (visible after the next
-// barrier); descriptor kDescAhead + j is copied by thread 0 with cp.async in the group of iteration
-// j - kRingDepth of the walk (the prologue's groups first). A thread's wait_group<kRingDepth - 1> at
-// the end of iteration l completes its groups up to iteration l - 2, so descriptors up to
-// l + kDescAhead + 1 have landed before the barrier that ends iteration l, well ahead of their first
-// use (staging level l + 1 + kRingDepth in iteration l + 1). An entry is overwritten kDescRing -
-// kDescAhead - kRingDepth levels after its last read.
-__device__ __forceinline__ void desc_prologue(const LevelRing &ring, const uint4 *__restrict__ levels, uint32_t count) {
-    if (threadIdx.x < kDescAhead && threadIdx.x < count) ring.desc[threadIdx.x] = __ldg(levels + threadIdx.x);
-}
-__device__ __forceinline__ void desc_stage(const LevelRing &ring, const uint4 *__restrict__ levels, uint32_t idx, uint32_t count) {
-    if (threadIdx.x == 0 && idx < count) cp_async16(ring.desc + idx % kDescRing, levels + idx);
-}
-__device__ __forceinline__ uint4 desc_at(const LevelRing &ring, uint32_t idx) { return ring.desc[idx % kDescRing]; }
-
-// Stages the records of per-substep level `idx` (< L) into ring position idx % kRingLevels when they
-// fit a ring slot (wider levels are read in place).
-template <int T>
-__device__ __forceinline__ void ring_stage(const LevelRing &ring, const uint4 *__restrict__ rec, uint32_t idx, uint4 lv,
-                                           uint32_t next_first) {
-    const uint32_t pos = idx % kRingLevels;
-    const uint32_t n = next_first - lv.x;
-    if (n <= ring.slots)
-        for (uint32_t s = threadIdx.x; s < n; s += T) cp_async16(ring.rec + pos * ring.slots + s, rec + lv.x + s);
+// Thread 0: stages chunk `ch` of a schedule into half h. The barrier that ended the walk's use of the
+// half precedes this; the proxy fence orders those generic accesses before the copies.
+__device__ __forceinline__ void ring_issue(const StageRing &ring, uint32_t h, uint4 ch, const uint4 *levels, const uint4 *records,
+                                           uint32_t extra_desc) {
+    const uint32_t rec_bytes = ch.w * uint32_t(sizeof(uint4));
+    const uint32_t desc_bytes = (ch.y - ch.x + extra_desc) * uint32_t(sizeof(uint4));
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    stage_expect(&ring.bar[h], rec_bytes + desc_bytes);
+    if (rec_bytes) stage_copy(ring.rec + h * ring.half, records + ch.z, rec_bytes, &ring.bar[h]);
+    stage_copy(ring.desc + h * (kStageLevels + 1), levels + ch.x, desc_bytes, &ring.bar[h]);
 }
 
-// Walks the dependency levels of one substep. Level l + kRingDepth is staged (cp.async) while level
-// l is projected, so the critical path of a level is: descriptor and records from shared memory,
-// positions from shared memory, projection, positions to shared memory, barrier.
+// All threads: waits (bounded) for the chunk in half h. On a timeout the CTA reports it, gives the
+// copies still in flight one more bounded wait, and must stop (returns false in every thread).
+__device__ __forceinline__ bool ring_wait(const StageRing &ring, uint32_t h, uint32_t &phases, uint32_t num_pending, uint32_t *error) {
+    const bool late = !stage_wait(&ring.bar[h], (phases >> h) & 1u);
+    if (__syncthreads_or(late)) {
+        if (threadIdx.x == 0) atomicOr(error, kErrTimeout);
+        for (uint32_t k = 0; k < num_pending; ++k) stage_wait(&ring.bar[(h + k) & 1u], (phases >> ((h + k) & 1u)) & 1u);
+        return false;
+    }
+    phases ^= 1u << h;
+    return true;
+}
+
 // Records a constraint's inputs for the adjoint: vertex differences relative to its first vertex
 // (edge / LRA: x1 - x0; volume / bend: x2 - x1, x3 - x1, x4 - x1 in record order).
 __device__ __forceinline__ void tape_inputs(const float4 *sx, uint4 r, int type, float4 *out) {
@@ -138,48 +131,42 @@ __device__ __forceinline__ void tape_inputs(const float4 *sx, uint4 r, int type,
     }
 }
 
+// Walks the dependency levels of one substep's schedule (tape_cons: the taped forward's constraint
+// inputs of this substep, 3 float4 per slot). Returns false when a staging wait gave up.
 template <int T, bool kTape, bool kGuard>
-__device__ __forceinline__ void apply_levels(float4 *sx, const BodyDesc &d, float inv_dt_sq, const LevelRing &ring,
-                                             float4 *tape_cons) {
+__device__ __forceinline__ bool apply_levels(float4 *sx, const BodyDesc &d, float inv_dt_sq, const StageRing &ring,
+                                             uint32_t &phases, float4 *tape_cons, uint32_t *error) {
     const uint4 *__restrict__ levels = d.levels;
     const uint4 *__restrict__ rec = d.records;
-    const uint32_t tid = threadIdx.x;
-    const uint32_t L = d.num_levels;
-    if (L == 0) return;
-    const uint32_t count = L + 2;  // descriptors, with two sentinels
-    desc_prologue(ring, levels, count);
-    __syncthreads();
-    // prologue: stage the records of levels 0 .. kRingDepth - 1
-#pragma unroll
-    for (int k = 0; k < kRingDepth; ++k) {
-        if (uint32_t(k) < L) ring_stage<T>(ring, rec, k, desc_at(ring, k), desc_at(ring, k + 1).x);
-        desc_stage(ring, levels, kDescAhead + k, count);
-        cp_async_commit();
+    const uint4 *__restrict__ chunks = d.chunks;
+    const uint32_t nc = d.num_chunks;
+    if (nc == 0) return true;
+    if (threadIdx.x == 0) {
+        ring_issue(ring, 0, __ldg(chunks), levels, rec, 1);
+        if (nc > 1) ring_issue(ring, 1, __ldg(chunks + 1), levels, rec, 1);
     }
-    cp_async_wait<kRingDepth - 1>();
-    __syncthreads();
-    for (uint32_t l = 0; l < L; ++l) {
-        const uint32_t ahead = l + kRingDepth;
-        const uint32_t pos = l % kRingLevels;
-        const uint4 lv = desc_at(ring, l);
-        const uint32_t n = desc_at(ring, l + 1).x - lv.x;
-        const bool in_ring = n <= ring.slots;
-        const uint4 *src = in_ring ? ring.rec + pos * ring.slots : rec + lv.x;
-        for (uint32_t s = tid; s < n; s += T) {
-            const uint4 r = src[s];
-            if (r.x != 0xffffffffu) {
-                if (kTape) tape_inputs(sx, r, slot_type(lv, s), tape_cons + size_t(lv.x + s) * 3);
-                project<kGuard>(sx, r, slot_type(lv, s), inv_dt_sq);
+    for (uint32_t c = 0; c < nc; ++c) {
+        const uint32_t h = c & 1u;
+        if (!ring_wait(ring, h, phases, nc - c < 2 ? nc - c : 2, error)) return false;
+        const uint4 ch = __ldg(chunks + c);
+        const uint4 *rr = ring.rec + h * ring.half;
+        const uint4 *dd = ring.desc + h * (kStageLevels + 1);
+        for (uint32_t l = 0; l < ch.y - ch.x; ++l) {
+            const uint4 lv = dd[l];
+            const uint32_t n = dd[l + 1].x - lv.x;
+            const uint32_t rel = lv.x - ch.z;
+            for (uint32_t s = threadIdx.x; s < n; s += T) {
+                const uint4 r = rel + s < ch.w ? rr[rel + s] : __ldg(rec + lv.x + s);
+                if (r.x != 0xffffffffu) {
+                    if (kTape) tape_inputs(sx, r, slot_type(lv, s), tape_cons + size_t(lv.x + s) * 3);
+                    project<kGuard>(sx, r, slot_type(lv, s), inv_dt_sq);
+                }
             }
+            cta_sync<T>();
         }
-        if (ahead < L) ring_stage<T>(ring, rec, ahead, desc_at(ring, ahead), desc_at(ring, ahead + 1).x);
-        desc_stage(ring, levels, ahead + kDescAhead, count);
-        cp_async_commit();
-        cp_async_wait<kRingDepth - 1>();
-        cta_sync<T>();
+        if (threadIdx.x == 0 && c + 2 < nc) ring_issue(ring, h, __ldg(chunks + c + 2), levels, rec, 1);
     }
-    cp_async_wait<0>();
-    __syncthreads();  // the descriptor ring is reused by the next walk
+    return true;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -238,61 +225,47 @@ __device__ __forceinline__ void vertex_between_substeps(float4 *sx, const Vertex
     sx[i] = with_w(xyz(pi) + xyz(vel) * vp.dt_sub, pi.w);
 }
 
-// Stages the first ring.slots records of whole-step level `idx`; slots beyond the ring's capacity are
-// read in place by the walker.
-template <int T>
-__device__ __forceinline__ void step_ring_stage(const LevelRing &ring, const uint4 *__restrict__ rec, uint32_t idx, uint4 lv) {
-    const uint32_t pos = idx % kRingLevels;
-    const uint32_t n = lv.w < ring.slots ? lv.w : ring.slots;
-    for (uint32_t s = threadIdx.x; s < n; s += T) cp_async16(ring.rec + pos * ring.slots + s, rec + lv.x + s);
-}
-
-// tape_cons (taped forward): this step's constraint inputs, 3 float4 per whole-step slot.
+// Walks the whole-step schedule (tape_cons: the taped forward's constraint inputs of this step, 3 float4
+// per whole-step slot). Returns false when a staging wait gave up.
 template <int T, bool kSmemState, bool kGuard, bool kTape>
-__device__ __forceinline__ void apply_step_levels(float4 *sx, const BodyDesc &d, float inv_dt_sq, const LevelRing &ring,
-                                                  const VertexPass &vp, float4 *tape_cons) {
+__device__ __forceinline__ bool apply_step_levels(float4 *sx, const BodyDesc &d, float inv_dt_sq, const StageRing &ring,
+                                                  uint32_t &phases, const VertexPass &vp, float4 *tape_cons, uint32_t *error) {
     const uint4 *__restrict__ levels = d.step_levels;
     const uint4 *__restrict__ rec = d.step_records;
-    const uint32_t tid = threadIdx.x;
-    const uint32_t L = d.num_step_levels;
-    if (L == 0) return;
-    desc_prologue(ring, levels, L);
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < kRingDepth; ++k) {
-        if (uint32_t(k) < L) step_ring_stage<T>(ring, rec, k, desc_at(ring, k));
-        desc_stage(ring, levels, kDescAhead + k, L);
-        cp_async_commit();
+    const uint4 *__restrict__ chunks = d.step_chunks;
+    const uint32_t nc = d.num_step_chunks;
+    if (nc == 0) return true;
+    if (threadIdx.x == 0) {
+        ring_issue(ring, 0, __ldg(chunks), levels, rec, 0);
+        if (nc > 1) ring_issue(ring, 1, __ldg(chunks + 1), levels, rec, 0);
     }
-    cp_async_wait<kRingDepth - 1>();
-    __syncthreads();
-    for (uint32_t l = 0; l < L; ++l) {
-        const uint32_t ahead = l + kRingDepth;
-        const uint32_t pos = l % kRingLevels;
-        const uint4 lv = desc_at(ring, l);
-        const uint4 *ring_rec = ring.rec + pos * ring.slots;
-        for (uint32_t s = tid; s < lv.w; s += T) {
-            const uint4 r = s < ring.slots ? ring_rec[s] : __ldg(rec + lv.x + s);
-            if (r.x != 0xffffffffu) {
-                const int type = step_slot_type(lv, s);
-                if (type == 4) {
-                    vertex_between_substeps<kSmemState, kTape>(sx, vp, r.x, r.y);
-                } else {
-                    if (kTape) tape_inputs(sx, r, type, tape_cons + size_t(lv.x + s) * 3);
-                    project<kGuard>(sx, r, type, inv_dt_sq);
+    for (uint32_t c = 0; c < nc; ++c) {
+        const uint32_t h = c & 1u;
+        if (!ring_wait(ring, h, phases, nc - c < 2 ? nc - c : 2, error)) return false;
+        const uint4 ch = __ldg(chunks + c);
+        const uint4 *rr = ring.rec + h * ring.half;
+        const uint4 *dd = ring.desc + h * (kStageLevels + 1);
+        for (uint32_t l = 0; l < ch.y - ch.x; ++l) {
+            const uint4 lv = dd[l];
+            const uint32_t rel = lv.x - ch.z;
+            for (uint32_t s = threadIdx.x; s < lv.w; s += T) {
+                const uint4 r = rel + s < ch.w ? rr[rel + s] : __ldg(rec + lv.x + s);
+                if (r.x != 0xffffffffu) {
+                    const int type = step_slot_type(lv, s);
+                    if (type == 4) {
+                        vertex_between_substeps<kSmemState, kTape>(sx, vp, r.x, r.y);
+                    } else {
+                        if (kTape) tape_inputs(sx, r, type, tape_cons + size_t(lv.x + s) * 3);
+                        project<kGuard>(sx, r, type, inv_dt_sq);
+                    }
                 }
             }
+            cta_sync<T>();
         }
-        if (ahead < L) step_ring_stage<T>(ring, rec, ahead, desc_at(ring, ahead));
-        desc_stage(ring, levels, ahead + kDescAhead, L);
-        cp_async_commit();
-        cp_async_wait<kRingDepth - 1>();
-        cta_sync<T>();
+        if (threadIdx.x == 0 && c + 2 < nc) ring_issue(ring, h, __ldg(chunks + c + 2), levels, rec, 0);
     }
-    cp_async_wait<0>();
-    __syncthreads();  // the descriptor ring is reused by the next walk
+    return true;
 }
-
 
 // ---------------------------------------------------------------------------------------------
 // One body, one step
@@ -301,9 +274,12 @@ __device__ __forceinline__ void apply_step_levels(float4 *sx, const BodyDesc &d,
 //   kSmemState:  x[cap] | v[cap] (shape index in v.w) | prev[cap] | faces[...]
 //   otherwise:   x[cap] | faces[...]       (v, prev, shape stay in HBM)
 // faces: per-face triple product, then per-face pressure impulse (pressure bodies only).
-// `phase`: parity of the staging barrier's current phase (flips once per body; the same in every thread).
+// `phase`: parity of the staging barrier's current phase (flips once per body; the same in every thread);
+// `ring_phases`: parities of the two schedule-ring halves (bit h; flip once per chunk).
+// Returns false (in every thread) when a bounded wait for staged data gave up; the CTA must then stop.
 template <int T, bool kSmemState, bool kTape = false>
-__device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_t cap, Shared &sh, uint32_t &phase) {
+__device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_t cap, Shared &sh, uint32_t &phase,
+                          uint32_t &ring_phases) {
     const uint32_t tid = threadIdx.x;
     const BodyDesc d = p.bodies[b];
     BodyState *st = p.states + b;
@@ -316,13 +292,14 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     float4 *sx = smem;
     float4 *sv = smem + cap;
     float4 *sprev = smem + 2 * cap;
-    float4 *sface = smem + (kSmemState ? 3 * cap : cap);  // pressure faces; the record ring reuses it
+    float4 *sface = smem + (kSmemState ? 3 * cap : cap);  // pressure faces; the schedule ring reuses it
     TapeDesc td = {};
     if (kTape) td = p.tape[b];
-    LevelRing ring;
+    StageRing ring;
     ring.rec = reinterpret_cast<uint4 *>(sface);
-    ring.desc = sh.ring_desc;
-    ring.slots = p.ring_slots;
+    ring.desc = ring.rec + 2 * p.ring_slots;
+    ring.half = p.ring_slots;
+    ring.bar = sh.ring_bar;
 
     // InitializeUpdateContext (identity body rotation)
     const f3 g = d.gravity_factor * ld3(p.gravity);
@@ -356,16 +333,17 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
             if (kSmemState) stage_copy(sv, gv, bytes, &sh.stage_bar);
         }
     }
-    if (!stage_wait(&sh.stage_bar, phase)) {
-        // never expected; report it, and stage with plain loads (the copies carry the same bytes)
+    const bool timed_out = !stage_wait(&sh.stage_bar, phase);
+    if (__syncthreads_or(timed_out)) {
+        // Never expected. Report it, give the copies still in flight one more bounded wait so that none
+        // lands in shared memory after the CTA has stopped, and stop this CTA's work: the body is left
+        // as it was, and the results of the launch are not valid (jsb_synchronize returns
+        // JSB_ERR_TIMEOUT).
         if (tid == 0) atomicOr(p.error, kErrTimeout);
-        for (uint32_t i = tid; i < nv; i += T) {
-            sx[i] = gx[i];
-            if (kSmemState) sv[i] = gv[i];
-        }
+        stage_wait(&sh.stage_bar, phase);
+        return false;
     }
     phase ^= 1u;
-    __syncthreads();
 
     // DetermineCollisionPlanes (per vertex, once per step)
     const int ncols = sh.ncols;
@@ -485,18 +463,20 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
         // Update groups in dependency-level order (NaN-guarded projections for a body holding NaNs)
         float4 *cons = kTape ? td.cons + (size_t(p.tape_step) * n_it + it) * size_t(td.slots) * 3 : nullptr;
         const bool nan_any = __syncthreads_or(nan_seen);
+        bool walked;
         if (step_walk) {
             // (a body that turns non-finite within the step finishes it on the unguarded walk: same
             // result, slower)
             float4 *step_cons = kTape ? td.cons + size_t(p.tape_step) * td.step_slots * 3 : nullptr;
             if (nan_any)
-                apply_step_levels<T, kSmemState, true, kTape>(sx, d, inv_dt_sq, ring, vp, step_cons);
+                walked = apply_step_levels<T, kSmemState, true, kTape>(sx, d, inv_dt_sq, ring, ring_phases, vp, step_cons, p.error);
             else
-                apply_step_levels<T, kSmemState, false, kTape>(sx, d, inv_dt_sq, ring, vp, step_cons);
+                walked = apply_step_levels<T, kSmemState, false, kTape>(sx, d, inv_dt_sq, ring, ring_phases, vp, step_cons, p.error);
         } else if (nan_any)
-            apply_levels<T, kTape, true>(sx, d, inv_dt_sq, ring, cons);
+            walked = apply_levels<T, kTape, true>(sx, d, inv_dt_sq, ring, ring_phases, cons, p.error);
         else
-            apply_levels<T, kTape, false>(sx, d, inv_dt_sq, ring, cons);
+            walked = apply_levels<T, kTape, false>(sx, d, inv_dt_sq, ring, ring_phases, cons, p.error);
+        if (!walked) return false;  // (uniform: decided at a barrier) the body is left half stepped, flagged
         __syncthreads();
         if (kTape) {  // position after the constraints of the last substep walked
             float4 *after = step_walk ? td.state + (size_t(p.tape_step) * n_it + n_it - 1) * 3 * nv : tape_state;
@@ -580,19 +560,24 @@ __device__ void step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
         gx[i] = shift ? with_w(xyz(pi) - delta, pi.w) : pi;
     }
     __syncthreads();
+    return true;
 }
 
 template <int T, bool kSmemState, bool kTape>
 __device__ __forceinline__ void step_queue(const StepParams &p, uint32_t cap, float4 *smem, Shared &sh) {
-    if (threadIdx.x == 0) stage_bar_init(&sh.stage_bar);
-    uint32_t phase = 0;
+    if (threadIdx.x == 0) {
+        stage_bar_init(&sh.stage_bar);
+        stage_bar_init(&sh.ring_bar[0]);
+        stage_bar_init(&sh.ring_bar[1]);
+    }
+    uint32_t phase = 0, ring_phases = 0;
     for (;;) {
         if (threadIdx.x == 0) sh.item = atomicAdd(p.queue, 1u);
         __syncthreads();
         const uint32_t item = sh.item;
         __syncthreads();
         if (item >= p.num_work) return;
-        step_body<T, kSmemState, kTape>(p, p.work[item], smem, cap, sh, phase);
+        if (!step_body<T, kSmemState, kTape>(p, p.work[item], smem, cap, sh, phase, ring_phases)) return;
     }
 }
 
@@ -620,7 +605,7 @@ __global__ void __launch_bounds__(T, 1) step_kernel_tape(StepParams p, uint32_t 
 // largest pressurised body has `faces` faces.
 size_t step_smem_bytes(bool smem_state, uint32_t vertices, uint32_t faces, uint32_t ring_slots) {
     const size_t faces_bytes = size_t(faces) * sizeof(float4);
-    const size_t ring_bytes = size_t(kRingLevels) * ring_slots * sizeof(uint4);
+    const size_t ring_bytes = (2 * size_t(ring_slots) + 2 * (kStageLevels + 1)) * sizeof(uint4);
     return size_t(vertices) * sizeof(float4) * (smem_state ? 3 : 1) + (faces_bytes > ring_bytes ? faces_bytes : ring_bytes);
 }
 
@@ -731,7 +716,9 @@ constexpr size_t kOffRecords = kOffLevels + kMaxLevels + 2;        // uint4[kMax
 constexpr size_t kOffFaces = kOffRecords + kMaxSlots;              // uint4[kMaxFaces]
 constexpr size_t kOffVfOff = kOffFaces + kMaxFaces;                // uint32[kMaxVertices + 4]
 constexpr size_t kOffVf = kOffVfOff + (kMaxVertices + 4) / 4;      // uint32[3 * kMaxFaces]
-constexpr size_t kScratchFloat4 = kOffVf + (3 * kMaxFaces) / 4;    // about 2.3 MB
+constexpr size_t kOffChunks = kOffVf + (3 * kMaxFaces) / 4;        // uint4[kMaxLevels] staging chunks
+constexpr size_t kScratchFloat4 = kOffChunks + kMaxLevels;         // about 2.4 MB
+constexpr uint32_t kRingHalf = 256;                                // schedule-ring half, record slots
 
 static __device__ __align__(256) float4 g_scratch[kScratchFloat4];
 
@@ -775,11 +762,15 @@ __global__ void __launch_bounds__(T) step_kernel_noalloc(const __grid_constant__
     p.error = q.error;
     p.forces = q.force;
     p.step_forces = q.zero3;
-    p.ring_slots = 256;
-    if (threadIdx.x == 0) stage_bar_init(&sh.stage_bar);
+    p.ring_slots = kRingHalf;
+    if (threadIdx.x == 0) {
+        stage_bar_init(&sh.stage_bar);
+        stage_bar_init(&sh.ring_bar[0]);
+        stage_bar_init(&sh.ring_bar[1]);
+    }
     __syncthreads();
-    uint32_t phase = 0;
-    step_body<T, kSmemState>(p, 0, smem, cap, sh, phase);
+    uint32_t phase = 0, ring_phases = 0;
+    step_body<T, kSmemState>(p, 0, smem, cap, sh, phase, ring_phases);
 }
 
 constexpr int kThreads = 128;
@@ -879,7 +870,9 @@ extern "C" jsb_status jsb_step_body_noalloc(const void *settings_blob, size_t le
     auto copy = [&](size_t off_float4, const void *src, size_t bytes) {
         return bytes ? cudaMemcpyAsync(scratch + off_float4, src, bytes, cudaMemcpyHostToDevice, s) : cudaSuccess;
     };
+    const std::vector<uint32_t> chunks = build_stage_chunks(sched.padded_levels, sched.num_levels, true, kRingHalf);
     e = copy(kOffLevels, sched.padded_levels.data(), sched.padded_levels.size() * sizeof(uint32_t));
+    if (e == cudaSuccess) e = copy(kOffChunks, chunks.data(), chunks.size() * sizeof(uint32_t));
     if (e == cudaSuccess) e = copy(kOffRecords, sched.padded_records.data(), sched.padded_records.size() * sizeof(uint32_t));
     if (e == cudaSuccess && pressure) e = copy(kOffFaces, faces.data(), faces.size() * sizeof(uint4));
     if (e == cudaSuccess && pressure) e = copy(kOffVfOff, vf_off.data(), vf_off.size() * sizeof(uint32_t));
@@ -895,6 +888,9 @@ extern "C" jsb_status jsb_step_body_noalloc(const void *settings_blob, size_t le
     d.vf = reinterpret_cast<const uint32_t *>(scratch + kOffVf);
     d.num_levels = sched.num_levels;
     d.num_records = sched.num_slots;
+    d.chunks = reinterpret_cast<const uint4 *>(scratch + kOffChunks);
+    d.num_chunks = uint32_t(chunks.size() / 4);
+    d.stage_half = kRingHalf;
     d.num_faces = pressure ? nf : 0u;
     d.num_vertices = nv;
     d.vtx_offset = 0;
@@ -935,7 +931,7 @@ extern "C" jsb_status jsb_step_body_noalloc(const void *settings_blob, size_t le
     q.error = error_device;
 
     // Whole vertex state in shared memory when it fits, else positions only (as in the batched path).
-    const uint32_t ring_slots = 256;
+    const uint32_t ring_slots = kRingHalf;
     const bool smem_state = step_smem_bytes(true, nv, nf, ring_slots) <= smem_limit;
     const size_t smem = step_smem_bytes(smem_state, nv, nf, ring_slots);
     if (smem > smem_limit)

@@ -328,3 +328,49 @@ class FD64:
         x0, v0, _ = blob_arrays(b.blob)
         ec, vc = blob_compliance(b.blob)
         return {"x0": x0, "v0": v0, "edge": ec, "volume": vc, "force": np.asarray(b.force, np.float64)}
+
+
+def single_body_scene(scene: Scene, b: int) -> Scene:
+    """The scene reduced to body b (every collider kept): bodies do not interact within a step."""
+    return Scene(gravity=scene.gravity, dt=scene.dt, collision_steps=scene.collision_steps, num_steps=scene.num_steps,
+                 colliders=list(scene.colliders), bodies=[scene.bodies[b]])
+
+
+def run64(scene: Scene, b: int, steps: int, observe, x0=None, v0=None, edge=None, volume=None, force=None) -> dict:
+    """FP64 oracle run of body b alone (optionally with its initial local positions / velocities, edge /
+    volume compliance or step force replaced); world positions (N, 3) after each step in `observe`."""
+    sc = single_body_scene(scene, b)
+    body = sc.bodies[0]
+    L = Oracle.lib()
+    o = Oracle(sc, use_double=True)
+    bx0, bv0, _ = blob_arrays(body.blob)
+    ec, vc = blob_compliance(body.blob)
+    xx = np.ascontiguousarray(bx0 if x0 is None else x0, np.float64)
+    vv = np.ascontiguousarray(bv0 if v0 is None else v0, np.float64)
+    L.oracle_set_state_f64(o.h, 0, xx.ctypes.data, vv.ctypes.data)
+    ee = np.ascontiguousarray(ec if edge is None else edge, np.float64)
+    vo = np.ascontiguousarray(vc if volume is None else volume, np.float64)
+    L.oracle_set_compliance_f64(o.h, 0, ee.ctypes.data, len(ee), vo.ctypes.data, len(vo))
+    f = np.ascontiguousarray(np.asarray(body.force, np.float64) if force is None else force, np.float64)
+    out = {}
+    n = body.num_vertices
+    for s in range(1, steps + 1):
+        if np.any(f != 0.0):
+            L.oracle_set_force_f64(o.h, 0, f.ctypes.data)
+        L.oracle_step(o.h, sc.dt, sc.collision_steps)
+        if s in observe:
+            w = np.zeros((n, 3), np.float64)
+            L.oracle_get_world_f64(o.h, 0, w.ctypes.data)
+            out[s] = w
+    return out
+
+
+def blob_counts_py(blob: bytes) -> dict:
+    """Element counts of a SaveBinaryState blob (vertices, faces, edges, bends, volumes, skinned, ..., lra)."""
+    out, off = {}, 0
+    for name, size in [("vertices", 28), ("faces", 16), ("edges", 16), ("bends", 24), ("volumes", 24), ("skinned", 52),
+                       ("skinned_normals", 4), ("lra", 12)]:
+        (n,) = struct.unpack_from("<I", blob, off)
+        out[name] = n
+        off += 4 + n * size
+    return out

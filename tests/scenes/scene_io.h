@@ -94,7 +94,7 @@ inline bool make_named_scene(const std::string &name, const std::string &params,
                                 int(geti("steps", 240)), uint32_t(geti("cloth_min", 8)), uint32_t(geti("cloth_max", 64)),
                                 uint32_t(geti("cube_min", 4)), uint32_t(geti("cube_max", 12)));
     else if (name == "large_cloth")
-        out = make_large_cloth(uint32_t(geti("n", 256)), int(geti("steps", 600)));
+        out = make_large_cloth(uint32_t(geti("n", 256)), int(geti("steps", 600)), geti("bends", 1) != 0);
     else if (name == "diff_cloth")
         out = make_diff_cloth(uint64_t(geti("seed", 4)), uint32_t(geti("n", 64)), int(geti("steps", 120)));
     else if (name == "diff_batch")

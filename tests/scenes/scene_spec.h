@@ -378,15 +378,16 @@ inline SceneSpec make_uneven_batch(uint64_t seed = 2, uint32_t n_cloth = 384, ui
 // Single large cloth: n x n grid (default 256), 0.02 m spacing, 4 corners pinned, Euclidean LRA
 // tethers, edge compliance 1e-6, bend compliance 1e-3, 8 iterations, dropped from y = 3 (1 m above
 // the top of a static sphere of radius 1 centred at y = 1) onto the sphere resting on a box floor
-// whose top is at y = 0; 600 steps of 1/60 s.
-inline SceneSpec make_large_cloth(uint32_t n = 256, int steps = 600) {
+// whose top is at y = 0; 600 steps of 1/60 s. bends = false leaves out the dihedral bends (a tethered
+// cloth that differentiable runs accept).
+inline SceneSpec make_large_cloth(uint32_t n = 256, int steps = 600, bool bends = true) {
     SceneSpec s;
     BodySpec b;
     b.mesh = make_cloth(n, n, 0.02f, [n](uint32_t x, uint32_t z) {
         return (x == 0 || x == n - 1) && (z == 0 || z == n - 1);
     });
-    b.mesh.attributes = VertexAttributes{1.0e-6f, 1.0e-6f, 1.0e-3f, LRAType::EuclideanDistance, 1.0f};
-    b.mesh.bend_type = BendType::Dihedral;
+    b.mesh.attributes = VertexAttributes{1.0e-6f, 1.0e-6f, bends ? 1.0e-3f : 3.402823466e+38f, LRAType::EuclideanDistance, 1.0f};
+    b.mesh.bend_type = bends ? BendType::Dihedral : BendType::None;
     b.creation.num_iterations = 8;
     b.position[1] = 3.0f;
     s.bodies.push_back(b);

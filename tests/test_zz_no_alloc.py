@@ -93,3 +93,13 @@ def test_noalloc_rejects_oversize_body(jsb):
         run_noalloc(jsb, scene, 0, 1)
     assert e.value.status == 8
     assert "16384" in str(e.value)
+
+
+def test_noalloc_rejects_too_many_colliders(jsb):
+    """More colliders than the fixed collider table holds (16) are refused before any device work."""
+    scene, _ = parse_scene(np.load(golden_path("uneven_small"))["scene"].tobytes())
+    scene.colliders = [scene.colliders[0]] * 17
+    with pytest.raises(jsb.JsbError) as e:
+        run_noalloc(jsb, scene, 0, 1)
+    assert e.value.status == 8
+    assert "16" in str(e.value)
