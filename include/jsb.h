@@ -52,7 +52,7 @@ typedef struct jsb_creation_settings {
     float vertex_radius;          /* mVertexRadius */
     uint8_t update_position;      /* mUpdatePosition */
     uint8_t make_rotation_identity; /* mMakeRotationIdentity (must be 1: bodies keep identity rotation) */
-    uint8_t allow_sleeping;       /* mAllowSleeping (sleeping is not evaluated on the GPU) */
+    uint8_t allow_sleeping;       /* mAllowSleeping: the body may fall asleep (see jsb_set_sleep_settings) */
     uint8_t faces_double_sided;   /* mFacesDoubleSided (queries only) */
 } jsb_creation_settings;
 
@@ -103,6 +103,18 @@ jsb_status jsb_body_add_force(jsb_context *ctx, uint32_t body_id, const float fo
 jsb_status jsb_body_set_step_force(jsb_context *ctx, uint32_t body_id, const float force[3]);
 
 jsb_status jsb_collider_add(jsb_context *ctx, const jsb_collider *collider, uint32_t *collider_id);
+
+/* Sleeping (SoftBodyMotionProperties.cpp:902-915, PhysicsSystem.cpp:2875-2884): after each step a body
+ * created with allow_sleeping whose largest squared vertex velocity (before the velocity clamp) is at or
+ * below point_velocity_sleep_threshold adds the step's dt to its sleep timer, else restarts it; once the
+ * timer reaches time_before_sleep the body goes to sleep: it is no longer stepped and its body velocities
+ * read zero. A force (jsb_body_add_force, or a non-zero jsb_body_set_step_force before every step) wakes
+ * it and restarts its timer, as BodyInterface::AddForce does. PhysicsSettings::mTimeBeforeSleep /
+ * mPointVelocitySleepThreshold (PhysicsSettings.h:95,102); defaults 0.5 s and 0.03 (m/s)^2. */
+jsb_status jsb_set_sleep_settings(jsb_context *ctx, float time_before_sleep, float point_velocity_sleep_threshold);
+/* BodyInterface::IsActive / ActivateBody (restarts the sleep timer) / DeactivateBody. */
+jsb_status jsb_body_is_active(jsb_context *ctx, uint32_t body_id, int *active);
+jsb_status jsb_body_set_active(jsb_context *ctx, uint32_t body_id, int active);
 
 jsb_status jsb_body_num_vertices(jsb_context *ctx, uint32_t body_id, uint32_t *num_vertices);
 

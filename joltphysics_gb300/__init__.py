@@ -39,6 +39,9 @@ SIGNATURES = {
     "jsb_body_add_force": [_P, _c.c_uint32, _c.POINTER(_c.c_float)],
     "jsb_body_set_step_force": [_P, _c.c_uint32, _c.POINTER(_c.c_float)],
     "jsb_collider_add": [_P, _c.c_char_p, _c.POINTER(_c.c_uint32)],
+    "jsb_set_sleep_settings": [_P, _c.c_float, _c.c_float],
+    "jsb_body_is_active": [_P, _c.c_uint32, _c.POINTER(_c.c_int)],
+    "jsb_body_set_active": [_P, _c.c_uint32, _c.c_int],
     "jsb_body_num_vertices": [_P, _c.c_uint32, _c.POINTER(_c.c_uint32)],
     "jsb_step": [_P, _c.c_float, _c.c_int, _P],
     "jsb_step_plain": [_P, _c.c_float, _c.c_int, _P],
@@ -229,6 +232,17 @@ class Context:
                            "num_bends": counts["bends"]})
         self.bodies = self.bodies + bodies
         return bodies
+
+    def set_sleep_settings(self, time_before_sleep: float = 0.5, point_velocity_sleep_threshold: float = 0.03):
+        check(lib().jsb_set_sleep_settings(self.h, time_before_sleep, point_velocity_sleep_threshold))
+
+    def is_active(self, body: int) -> bool:
+        a = ctypes.c_int()
+        check(lib().jsb_body_is_active(self.h, body, ctypes.byref(a)))
+        return bool(a.value)
+
+    def set_active(self, body: int, active: bool):
+        check(lib().jsb_body_set_active(self.h, body, 1 if active else 0))
 
     # -- stepping --------------------------------------------------------------------------------
     def add_force(self, body: int, f):

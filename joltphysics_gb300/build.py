@@ -27,6 +27,10 @@ CXX_SOURCES = ["host/runtime.cpp", "host/schedule.cpp"]
 
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-std=c++17",
                      "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(REPO, "include")]
+# The adjoint reproduces no reference result bit for bit: its own divisions and square roots may round
+# (by at most 2 units in the last place); the forward arithmetic it calls (jdiv / jsqrt, the projections)
+# spells out IEEE rounding explicitly and is unaffected.
+PER_SOURCE_NVCC = {"kernels/adjoint.cu": ["-prec-div=false", "-prec-sqrt=false"]}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I" + os.path.join(CUDA_HOME, "include"),
              "-I" + os.path.join(REPO, "include")]
 
@@ -58,7 +62,9 @@ def build(verbose: bool = False, extra_nvcc: list[str] | None = None) -> str:
         s = os.path.join(CSRC, src)
         o = _obj(src)
         if _stale(o, [s] + headers):
-            jobs.append(([NVCC] + NVCC_FLAGS + (extra_nvcc or []) + ["-c", s, "-o", o], o))
+            own = PER_SOURCE_NVCC.get(src, [])
+            flags = [f for f in NVCC_FLAGS if f.split("=")[0] not in {g.split("=")[0] for g in own}] + own
+            jobs.append(([NVCC] + flags + (extra_nvcc or []) + ["-c", s, "-o", o], o))
     for src in CXX_SOURCES:
         s = os.path.join(CSRC, src)
         o = _obj(src)

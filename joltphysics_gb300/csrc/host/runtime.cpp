@@ -248,6 +248,9 @@ struct jsb_context {
     jsb::DevBuf<uint32_t> error;
     jsb::DevBuf<float> forces;  // per body: 3 floats consumed by the next step
     jsb::DevBuf<float> step_forces;  // per body: 3 floats applied before every step
+    jsb::DevBuf<jsb::BodySleep> sleep;  // per body: sleep timer, active flag
+    float sleep_velocity_threshold = 0.03f;  // PhysicsSettings::mPointVelocitySleepThreshold (PhysicsSettings.h:102)
+    float time_before_sleep = 0.5f;          // PhysicsSettings::mTimeBeforeSleep (PhysicsSettings.h:95)
     std::vector<float> step_force_host;
     jsb::DevBuf<float> staging3;  // host round trip: positions then velocities, 3 floats per vertex
     std::vector<float> pending_force;
@@ -349,7 +352,7 @@ BodyDesc make_desc(const jsb_context *ctx, const BodyRec &b) {
     d.pressure = b.creation.pressure;
     d.gravity_factor = b.creation.gravity_factor;
     d.vertex_radius = b.creation.vertex_radius;
-    d.flags = b.creation.update_position ? kFlagUpdatePosition : 0u;
+    d.flags = (b.creation.update_position ? kFlagUpdatePosition : 0u) | (b.creation.allow_sleeping ? kFlagAllowSleeping : 0u);
     return d;
 }
 
@@ -481,6 +484,12 @@ jsb_status rebuild(jsb_context *ctx) {
     for (const BodyRec &b : ctx->bodies) ctx->descs_host.push_back(make_desc(ctx, b));
     JSB_CUDA(ctx->descs.upload(ctx->descs_host.data(), ctx->descs_host.size()));
     JSB_CUDA(ctx->states.upload(hstate.data(), hstate.size()));
+    {  // sleep records: existing bodies keep theirs, new bodies start awake with a zero timer
+        std::vector<BodySleep> hs(ctx->bodies.size(), BodySleep{0.0f, 1u});
+        const size_t old_sleep = std::min(ctx->sleep.count, hs.size());
+        if (old_sleep) JSB_CUDA(cudaMemcpy(hs.data(), ctx->sleep.ptr, old_sleep * sizeof(BodySleep), cudaMemcpyDeviceToHost));
+        JSB_CUDA(ctx->sleep.upload(hs.data(), hs.size()));
+    }
     JSB_CUDA(ctx->colliders_dev.upload(ctx->colliders.data(), ctx->colliders.size()));
     ctx->pending_force.resize(ctx->bodies.size() * 3, 0.0f);
     if (ctx->pending_force_pinned) cudaFreeHost(ctx->pending_force_pinned);
@@ -647,6 +656,9 @@ StepParams base_params(jsb_context *ctx, float dt) {
     p.ring_slots = kMaxRingSlots;
     p.tape = nullptr;
     p.tape_step = 0;
+    p.sleep = ctx->sleep.ptr;
+    p.sleep_velocity_threshold = ctx->sleep_velocity_threshold;
+    p.time_before_sleep = ctx->time_before_sleep;
     return p;
 }
 
@@ -736,6 +748,7 @@ jsb_status enqueue_taped(jsb_context *ctx, const AdjointSession &a, int tape_ste
         p.queue = ctx->queues.ptr + gi;
         p.ring_slots = g.ring_slots;
         p.tape = a.tape_desc.ptr;
+        p.sleep = nullptr;  // (differentiable runs refuse bodies that may sleep)
         p.tape_step = uint32_t(tape_step);
         JSB_CUDA(launch_step_tape(p, g.threads, g.tape_smem_state, g.cap_vertices, g.cap_faces, g.tape_grid, g.stream));
         ++launches;
@@ -951,6 +964,49 @@ jsb_status jsb_body_set_step_force(jsb_context *ctx, uint32_t body_id, const flo
     return JSB_OK;
 }
 
+jsb_status jsb_set_sleep_settings(jsb_context *ctx, float time_before_sleep, float point_velocity_sleep_threshold) {
+    if (!check_ctx(ctx) || !(time_before_sleep >= 0.0f) || !(point_velocity_sleep_threshold >= 0.0f))
+        return fail(JSB_ERR_INVALID_ARGUMENT, "sleep settings must be >= 0");
+    drop_graph(ctx);  // graphs hold the launch parameters
+    ctx->time_before_sleep = time_before_sleep;
+    ctx->sleep_velocity_threshold = point_velocity_sleep_threshold;
+    return JSB_OK;
+}
+
+jsb_status jsb_body_is_active(jsb_context *ctx, uint32_t body_id, int *active) {
+    if (!check_ctx(ctx) || !active || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    JSB_CUDA(cudaDeviceSynchronize());
+    BodySleep sl;
+    JSB_CUDA(cudaMemcpy(&sl, ctx->sleep.ptr + body_id, sizeof(BodySleep), cudaMemcpyDeviceToHost));
+    *active = sl.active ? 1 : 0;
+    return JSB_OK;
+}
+
+jsb_status jsb_body_set_active(jsb_context *ctx, uint32_t body_id, int active) {
+    if (!check_ctx(ctx) || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    JSB_CUDA(cudaDeviceSynchronize());
+    BodySleep sl;
+    JSB_CUDA(cudaMemcpy(&sl, ctx->sleep.ptr + body_id, sizeof(BodySleep), cudaMemcpyDeviceToHost));
+    if (active) {
+        sl = BodySleep{0.0f, 1u};  // ActivateBody resets the sleep timer (BodyManager.cpp:508-511)
+    } else if (sl.active) {
+        sl.active = 0u;  // DeactivateBody zeroes the body velocities (BodyManager.cpp:559-561)
+        BodyState bs;
+        JSB_CUDA(cudaMemcpy(&bs, ctx->states.ptr + body_id, sizeof(BodyState), cudaMemcpyDeviceToHost));
+        memset(bs.lin_vel, 0, sizeof(bs.lin_vel));
+        memset(bs.ang_vel, 0, sizeof(bs.ang_vel));
+        JSB_CUDA(cudaMemcpy(ctx->states.ptr + body_id, &bs, sizeof(BodyState), cudaMemcpyHostToDevice));
+    }
+    JSB_CUDA(cudaMemcpy(ctx->sleep.ptr + body_id, &sl, sizeof(BodySleep), cudaMemcpyHostToDevice));
+    return JSB_OK;
+}
+
 jsb_status jsb_step(jsb_context *ctx, float dt, int collision_steps, jsb_stream stream) {
     if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
     JSB_CUDA(cudaSetDevice(ctx->device));
@@ -1098,9 +1154,12 @@ jsb_status jsb_body_save_state(jsb_context *ctx, uint32_t body_id, void *state, 
     JSB_CUDA(cudaMemcpy(hx.data(), ctx->x.ptr + b.vtx_offset, nv * sizeof(float4), cudaMemcpyDeviceToHost));
     JSB_CUDA(cudaMemcpy(hv.data(), ctx->v.ptr + b.vtx_offset, nv * sizeof(float4), cudaMemcpyDeviceToHost));
     uint8_t *o = static_cast<uint8_t *>(state);
+    BodySleep sl;
+    JSB_CUDA(cudaMemcpy(&sl, ctx->sleep.ptr + body_id, sizeof(BodySleep), cudaMemcpyDeviceToHost));
     memset(o, 0, kMotionHeader);
     memcpy(o + 0, s.lin_vel, 12);
     memcpy(o + 12, s.ang_vel, 12);
+    memcpy(o + 96, &sl.timer, 4);  // mSleepTestTimer
     o[100] = b.creation.allow_sleeping;
     uint8_t *p = o + kMotionHeader;
     for (size_t i = 0; i < nv; ++i) {
@@ -1131,6 +1190,10 @@ jsb_status jsb_body_restore_state(jsb_context *ctx, uint32_t body_id, const void
     memcpy(s.lin_vel, in + 0, 12);
     memcpy(s.ang_vel, in + 12, 12);
     memcpy(s.position, position, 12);
+    BodySleep sl;  // the timer is restored; whether the body is active is the caller's (jsb_body_activate)
+    JSB_CUDA(cudaMemcpy(&sl, ctx->sleep.ptr + body_id, sizeof(BodySleep), cudaMemcpyDeviceToHost));
+    memcpy(&sl.timer, in + 96, 4);
+    JSB_CUDA(cudaMemcpy(ctx->sleep.ptr + body_id, &sl, sizeof(BodySleep), cudaMemcpyHostToDevice));
     std::vector<float4> hx(nv), hv(nv);
     const uint8_t *p = in + kMotionHeader;
     for (size_t i = 0; i < nv; ++i) {
@@ -1511,6 +1574,9 @@ jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int chec
     if (st != JSB_OK) return st;
     if (ctx->forces_pending)
         return fail(JSB_ERR_INVALID_ARGUMENT, "one-shot AddForce cannot be differentiated; use jsb_body_set_step_force");
+    for (size_t b = 0; b < ctx->bodies.size(); ++b)
+        if (ctx->bodies[b].creation.allow_sleeping)
+            return fail(JSB_ERR_UNSUPPORTED, "body " + std::to_string(b) + " may sleep (allow_sleeping), which differentiable runs do not model");
     for (size_t b = 0; b < ctx->bodies.size(); ++b)
         if (!ctx->settings[ctx->bodies[b].settings_id]->parsed.bends.empty())
             return fail(JSB_ERR_UNSUPPORTED, "body " + std::to_string(b) +

@@ -95,6 +95,7 @@ struct Partials {
     int idx[12];
     float sum[6];  // linear velocity, angular velocity sums
     int last_nan[6];  // last owned vertex with a NaN component (positions x, y, z, predicted x, y, z)
+    float max_v_sq;   // largest squared vertex velocity before the clamp (the sleep test)
 };
 
 struct CShared {
@@ -183,6 +184,8 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
     const uint32_t item = blockIdx.x / C;  // one cluster per body
     if (item >= p.num_work) return;       // uniform over the cluster
     const uint32_t b = p.work[item];
+    bool wake;
+    if (!body_awake(p, b, wake)) return;  // asleep: not stepped (uniform over the cluster)
     const BodyDesc d = p.bodies[b];
     BodyState *st = p.states + b;
     const uint32_t nv = d.num_vertices;
@@ -257,6 +260,7 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
         nan_seen = __syncthreads_or(nan_seen);
         if (tid == 0) sh.nan_flag[it & 1] = nan_seen ? 1 : 0;
         cluster_barrier();  // every position integrated before any constraint reads it
+        if (it == 0 && wake && rank == 0 && tid == 0) p.sleep[b] = BodySleep{0.0f, 1u};  // (every CTA has read the record)
         // NaN-guarded projections when any CTA's vertices hold a NaN (flags double-buffered by substep)
         bool guard = false;
         for (uint32_t q = 0; q < C; ++q) guard = guard || ld_cluster_s32(map_rank(smem_u32(&sh.nan_flag[it & 1]), q)) != 0;
@@ -289,10 +293,12 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
     bounds_init(bd);
     f3 lin = mk(0, 0, 0), ang = mk(0, 0, 0);
     bool finite = true;
+    float max_v_sq = 0.0f;
     for (uint32_t i = first + tid; i < last; i += T) {
         const float4 pi = sx[i - first];
         f3 v = xyz(gv[i]), x = xyz(pi);
         const float vsq = len_sq(v);
+        max_v_sq = fmaxf(max_v_sq, vsq);
         if (vsq > max_sq) v = v * jsqrt(jdiv(max_sq, vsq));
         gv[i] = with_w(v, 0.0f);
         lin = lin + v;
@@ -311,6 +317,7 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
     sums[3] = reduce_sum<T>(sh, ang.x, 3);
     sums[4] = reduce_sum<T>(sh, ang.y, 0);
     sums[5] = reduce_sum<T>(sh, ang.z, 1);
+    max_v_sq = reduce_max<T>(sh, max_v_sq, 2);
     auto write_bounds = [&]() {
         for (int k = 0; k < 3; ++k) {
             sh.part.val[k] = bd.mm[k], sh.part.idx[k] = bd.mi[k];
@@ -322,6 +329,7 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
     if (tid == 0) {
         write_bounds();
         for (int k = 0; k < 6; ++k) sh.part.sum[k] = sums[k], sh.part.last_nan[k] = sh.last_nan[k];
+        sh.part.max_v_sq = max_v_sq;
     }
     cluster_barrier();
     // The body's last NaN index per component (the maximum over the CTAs); a body holding NaNs repeats
@@ -365,6 +373,7 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
                     pick_min(acc.val[k], acc.idx[k], ov, oi);
             }
             for (int k = 0; k < 6; ++k) acc.sum[k] = acc.sum[k] + ld_cluster_f32(base + uint32_t(offsetof(Partials, sum)) + 4u * k);
+            acc.max_v_sq = fmaxf(acc.max_v_sq, ld_cluster_f32(base + uint32_t(offsetof(Partials, max_v_sq))));
         }
         if (redo) {
             const float q = __int_as_float(0x7fffffff);
@@ -377,6 +386,7 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
                                            mk(acc.val[6], acc.val[7], acc.val[8]), mk(acc.val[9], acc.val[10], acc.val[11]), acc.sum,
                                            nvf);
         st3(sh.delta, delta);
+        sleep_test(p, b, d, st, acc.max_v_sq);
     }
     cluster_barrier();
     f3 delta;

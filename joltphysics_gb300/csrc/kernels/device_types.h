@@ -40,7 +40,7 @@ constexpr uint32_t kMaxVerticesPerBody = 65536;
 constexpr uint32_t kStageLevels = 64;  // level descriptors per schedule-ring half (the per-substep walk stages one more)
 constexpr uint32_t kMaxCollidingShapes = 16;  // colliding shapes kept per body per step
 
-enum : uint32_t { kFlagUpdatePosition = 1u };
+enum : uint32_t { kFlagUpdatePosition = 1u, kFlagAllowSleeping = 2u };
 
 // Device error word bits.
 enum : uint32_t { kErrNonFinite = 1u, kErrShapeOverflow = 2u, kErrTimeout = 4u };
@@ -87,6 +87,12 @@ struct BodyState {
     float bmin[3], bmax[3];  // local bounds
     float pmin[3], pmax[3];  // local predicted bounds
     float lin_vel[3], ang_vel[3];
+};
+
+// Sleep state of a body (MotionProperties::mSleepTestTimer and whether the body is in the active set).
+struct BodySleep {
+    float timer;
+    uint32_t active;  // 0: asleep, not stepped until a force or jsb_body_activate wakes it
 };
 
 struct ColliderDev {
@@ -140,6 +146,9 @@ struct StepParams {
     uint32_t ring_slots;  // record slots per schedule-ring half (>= every launched body's stage_half)
     const TapeDesc *tape;  // per-body tapes (taped forward only)
     uint32_t tape_step;    // step index within the checkpoint segment (taped forward only)
+    BodySleep *sleep;      // per body (null: bodies never sleep)
+    float sleep_velocity_threshold;  // PhysicsSettings::mPointVelocitySleepThreshold (compared with |v|^2)
+    float time_before_sleep;         // PhysicsSettings::mTimeBeforeSleep
 };
 
 // Parameters of one adjoint step over a set of bodies (the reverse of one forward step).

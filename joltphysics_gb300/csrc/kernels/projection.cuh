@@ -404,6 +404,39 @@ __device__ inline f3 finish_body_state(BodyState *st, const BodyDesc &d, f3 body
     return delta;
 }
 
+// Sleeping (SoftBodyMotionProperties.cpp:902-915 with the deactivation of PhysicsSystem.cpp:2875-2884 and
+// BodyManager.cpp:559-561), thread 0 after UpdateSoftBodyState: with sleeping allowed, a body whose
+// largest squared vertex velocity of the step (before the clamp; NaN values do not count, as with the
+// reference's std::max) exceeds the point-velocity threshold restarts its sleep timer; otherwise the
+// step's dt is added and, once the timer reaches the time before sleep, the body leaves the active set
+// (its body velocities are zeroed) and is not stepped again until woken.
+__device__ inline void sleep_test(const StepParams &p, uint32_t b, const BodyDesc &d, BodyState *st, float max_v_sq) {
+    if (!p.sleep || !(d.flags & kFlagAllowSleeping)) return;
+    BodySleep &s = p.sleep[b];
+    if (max_v_sq > p.sleep_velocity_threshold) {
+        s.timer = 0.0f;
+        return;
+    }
+    s.timer = s.timer + p.dt;
+    if (s.timer >= p.time_before_sleep) {
+        s.active = 0u;
+        st3(st->lin_vel, mk(0.0f, 0.0f, 0.0f));
+        st3(st->ang_vel, mk(0.0f, 0.0f, 0.0f));
+    }
+}
+
+// Whether body b is stepped (every thread, before anything of the step is written). A body with a force
+// this step is woken first, as BodyInterface::AddForce does (EActivation::Activate resets the sleep timer
+// and activates the body, BodyInterface.cpp:699-713, BodyManager.cpp:508-522); `wake` is then true and
+// thread 0 writes the record after the caller's next barrier.
+__device__ __forceinline__ bool body_awake(const StepParams &p, uint32_t b, bool &wake) {
+    wake = false;
+    if (!p.sleep) return true;
+    const f3 f = ld3(p.forces + 3 * size_t(b)), g = ld3(p.step_forces + 3 * size_t(b));
+    wake = f.x != 0.0f || f.y != 0.0f || f.z != 0.0f || g.x != 0.0f || g.y != 0.0f || g.z != 0.0f;
+    return wake || p.sleep[b].active != 0u;
+}
+
 // Block-wide reductions (results in thread 0); S provides float red[32][4] and int redi[32][4].
 template <int T, class S>
 __device__ __forceinline__ void reduce_minmax4(S &sh, float v[4], int idx[4], const bool is_max[4]) {
@@ -436,6 +469,20 @@ __device__ __forceinline__ void reduce_minmax4(S &sh, float v[4], int idx[4], co
                 }
         __syncthreads();
     }
+}
+
+template <int T, class S>
+__device__ __forceinline__ float reduce_max(S &sh, float v, int slot) {  // fmaxf: NaN operands are ignored
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int off = 16; off > 0; off >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, off));
+    if (T > 32) {
+        if (lane == 0) sh.red[warp][slot] = v;
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int w = 1; w < T / 32; ++w) v = fmaxf(v, sh.red[w][slot]);
+        __syncthreads();
+    }
+    return v;  // valid in thread 0
 }
 
 template <int T, class S>

@@ -281,6 +281,8 @@ template <int T, bool kSmemState, bool kTape = false>
 __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_t cap, Shared &sh, uint32_t &phase,
                           uint32_t &ring_phases) {
     const uint32_t tid = threadIdx.x;
+    bool wake;
+    if (!body_awake(p, b, wake)) return true;  // asleep: not stepped (uniform over the CTA)
     const BodyDesc d = p.bodies[b];
     BodyState *st = p.states + b;
     const uint32_t nv = d.num_vertices;
@@ -344,6 +346,7 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
         return false;
     }
     phase ^= 1u;
+    if (wake && tid == 0) p.sleep[b] = BodySleep{0.0f, 1u};  // (every thread has read the record)
 
     // DetermineCollisionPlanes (per vertex, once per step)
     const int ncols = sh.ncols;
@@ -510,11 +513,13 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     bounds_init(bd);
     f3 lin = mk(0, 0, 0), ang = mk(0, 0, 0);
     bool finite = true;
+    float max_v_sq = 0.0f;
     for (uint32_t i = tid; i < nv; i += T) {
         float4 pi = sx[i];
         float4 vel = kSmemState ? sv[i] : gv[i];
         f3 v = xyz(vel), x = xyz(pi);
         float vsq = len_sq(v);
+        max_v_sq = fmaxf(max_v_sq, vsq);
         if (vsq > max_sq) v = v * jsqrt(jdiv(max_sq, vsq));
         gv[i] = with_w(v, 0.0f);
         lin = lin + v;
@@ -547,10 +552,12 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     sums[3] = reduce_sum<T>(sh, ang.x, 3);
     sums[4] = reduce_sum<T>(sh, ang.y, 0);
     sums[5] = reduce_sum<T>(sh, ang.z, 1);
+    max_v_sq = reduce_max<T>(sh, max_v_sq, 2);
     if (tid == 0) {
         const f3 delta = finish_body_state(st, d, body_pos, mk(bd.mm[0], bd.mm[1], bd.mm[2]), mk(bd.xx[0], bd.xx[1], bd.xx[2]),
                                            mk(bd.pm[0], bd.pm[1], bd.pm[2]), mk(bd.px[0], bd.px[1], bd.px[2]), sums, nvf);
         st3(sh.delta, delta);
+        sleep_test(p, b, d, st, max_v_sq);
     }
     __syncthreads();
     const f3 delta = ld3(sh.delta);
@@ -763,6 +770,7 @@ __global__ void __launch_bounds__(T) step_kernel_noalloc(const __grid_constant__
     p.forces = q.force;
     p.step_forces = q.zero3;
     p.ring_slots = kRingHalf;
+    p.sleep = nullptr;  // (bodies that may sleep are refused by jsb_step_body_noalloc)
     if (threadIdx.x == 0) {
         stage_bar_init(&sh.stage_bar);
         stage_bar_init(&sh.ring_bar[0]);
@@ -822,6 +830,9 @@ extern "C" jsb_status jsb_step_body_noalloc(const void *settings_blob, size_t le
         return report_error(JSB_ERR_INVALID_ARGUMENT, "dt must be > 0 and num_iterations >= 1");
     if (!creation->make_rotation_identity)
         return report_error(JSB_ERR_UNSUPPORTED, "bodies must keep an identity rotation (mMakeRotationIdentity = true)");
+    if (creation->allow_sleeping)
+        return report_error(JSB_ERR_UNSUPPORTED, "jsb_step_body_noalloc keeps no sleep state: create the body with "
+                                                 "allow_sleeping = 0, or step it in a context");
     if (num_colliders > kMaxColliders)
         return report_error(JSB_ERR_CAPACITY, "jsb_step_body_noalloc takes at most " + std::to_string(kMaxColliders) + " colliders");
 

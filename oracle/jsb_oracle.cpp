@@ -253,6 +253,7 @@ struct Creation {
     uint32_t num_iterations;
     float linear_damping, max_linear_velocity, restitution, friction, pressure, gravity_factor, vertex_radius;
     uint32_t update_position;
+    uint32_t allow_sleeping;
 };
 
 template <class R>
@@ -276,6 +277,20 @@ struct Body {
     V3<R> force;
     V3<R> lin_vel, ang_vel;
     std::vector<R> edge_c, vol_c;  // per-constraint compliance (the settings' values unless overridden)
+    R sleep_timer = R(0);  // MotionProperties::mSleepTestTimer
+    bool active = true;    // in the active set (asleep bodies are not stepped)
+    // Collision decisions of every step (frozen-decision runs, see World::freeze_mode)
+    struct Decisions {
+        std::vector<int> shape_collider;  // colliding shapes: collider index, friction, restitution
+        std::vector<R> shape_friction, shape_restitution;
+        std::vector<int> vertex_shape;  // per vertex: shape index, plane normal and constant (world space:
+        std::vector<V3<R>> vertex_n;    // the body position moves with the recentring, the colliders do not)
+        std::vector<R> vertex_c;
+        std::vector<uint8_t> flags;   // [substep][vertex] bit 0 contact, 1 friction clamped, 2 restitution
+        std::vector<uint8_t> vclamp;  // per vertex: velocity clamped after the step
+    };
+    std::vector<Decisions> decisions;
+    size_t decision_step = 0;
 };
 
 template <class R>
@@ -328,6 +343,13 @@ public:
     }
 
     int threads = 1;
+    R time_before_sleep = R(0.5f), sleep_velocity_threshold = R(0.03f);  // PhysicsSettings.h:95,102
+    // Frozen-decision runs (TEST INFRASTRUCTURE for finite differences of what the adjoint differentiates):
+    // 1 = record every collision decision of every step (colliding shapes, each vertex's plane and shape,
+    // per substep contact, friction clamp and restitution, the velocity clamp); 2 = replay them instead
+    // of deciding again, with the planes as constants, so that a perturbed run follows the base run's
+    // collision active set. 0 = the reference's arithmetic.
+    int freeze_mode = 0;
     std::unique_ptr<Pool> pool;
     Pool *inner = nullptr;  // set while one body is stepped with its groups spread over the pool
 
@@ -362,6 +384,7 @@ public:
     }
 
     void step_body(Body<R> &b, R dt) {
+        if (!b.active) return;  // asleep: PhysicsSystem steps only active soft bodies (PhysicsSystem.cpp:2711-2716)
         const Settings &s = *b.settings;
         // InitializeUpdateContext (:937-960), identity body rotation
         V3<R> g = mul(R(b.cs.gravity_factor), gravity);
@@ -374,7 +397,23 @@ public:
 
         // DetermineCollidingShapes (:120-255)
         std::vector<CollidingShape<R>> shapes;
-        {
+        typename Body<R>::Decisions *dec = nullptr;
+        if (freeze_mode == 1) {
+            b.decisions.emplace_back();
+            dec = &b.decisions.back();
+        } else if (freeze_mode == 2) {
+            dec = &b.decisions[b.decision_step++];
+            for (size_t k = 0; k < dec->shape_collider.size(); ++k) {
+                CollidingShape<R> cs;
+                cs.collider = dec->shape_collider[k];
+                const Collider &c = colliders[size_t(cs.collider)];
+                cs.t = sub(V3<R>{R(c.pos[0]), R(c.pos[1]), R(c.pos[2])}, b.position);
+                cs.friction = dec->shape_friction[k];
+                cs.restitution = dec->shape_restitution[k];
+                shapes.push_back(cs);
+            }
+        }
+        if (freeze_mode != 2) {
             V3<R> lmin = vmin(b.bmin, b.pmin), lmax = vmax(b.bmax, b.pmax);
             V3<R> r3 = {R(b.cs.vertex_radius), R(b.cs.vertex_radius), R(b.cs.vertex_radius)};
             lmin = sub(lmin, r3);
@@ -395,11 +434,16 @@ public:
                 cs.friction = std::sqrt(R(b.cs.friction) * R(c.friction));
                 cs.restitution = R(b.cs.restitution) > R(c.restitution) ? R(b.cs.restitution) : R(c.restitution);
                 shapes.push_back(cs);
+                if (dec) {
+                    dec->shape_collider.push_back(cs.collider);
+                    dec->shape_friction.push_back(cs.friction);
+                    dec->shape_restitution.push_back(cs.restitution);
+                }
             }
         }
 
         // DetermineCollisionPlanes (:257-265)
-        for (size_t si = 0; si < shapes.size(); ++si) {
+        for (size_t si = 0; si < shapes.size() && freeze_mode != 2; ++si) {
             const Collider &c = colliders[shapes[si].collider];
             const V3<R> t = shapes[si].t;
             for (auto &v : b.v) {
@@ -411,6 +455,21 @@ public:
             }
         }
 
+        if (freeze_mode == 2) {
+            for (size_t i = 0; i < b.v.size(); ++i) {
+                b.v[i].shape_idx = dec->vertex_shape[i];
+                b.v[i].plane_n = dec->vertex_n[i];
+                b.v[i].plane_c = dec->vertex_c[i] + dot(dec->vertex_n[i], b.position);
+            }
+        } else if (dec) {
+            for (const Vertex<R> &v : b.v) {
+                dec->vertex_shape.push_back(v.shape_idx);
+                dec->vertex_n.push_back(v.plane_n);
+                dec->vertex_c.push_back(v.plane_c - dot(v.plane_n, b.position));
+            }
+            dec->flags.assign(size_t(n_it) * b.v.size(), 0);
+            dec->vclamp.assign(b.v.size(), 0);
+        }
         for (uint32_t it = 0; it < n_it; ++it) {
             apply_pressure(b, dt_sub);
             integrate(b, g, dt_sub);
@@ -422,9 +481,9 @@ public:
             } else {
                 for (size_t gi = 0; gi < ng; ++gi) process_group(b, gi, dt_sub);
             }
-            collide_and_update_velocities(b, shapes, g, dt_sub);
+            collide_and_update_velocities(b, shapes, g, dt_sub, dec ? dec->flags.data() + size_t(it) * b.v.size() : nullptr);
         }
-        update_state(b, dt, disp_g);
+        update_state(b, dt, disp_g, dec);
     }
 
     void collide_box(Vertex<R> &v, const Collider &c, V3<R> t, int idx) {  // BoxShape.cpp:234-283
@@ -613,23 +672,27 @@ public:
         if (dls > md * md) v1.pos = add(x0, divs(mul(delta, md), std::sqrt(dls)));
     }
 
-    void collide_and_update_velocities(Body<R> &b, const std::vector<CollidingShape<R>> &shapes, V3<R> g, R dt) {  // :700-825
+    void collide_and_update_velocities(Body<R> &b, const std::vector<CollidingShape<R>> &shapes, V3<R> g, R dt, uint8_t *flags) {  // :700-825
         R restitution_threshold = R(-2.0f) * len(g) * dt;
         R radius = R(b.cs.vertex_radius);
         for_vertex_ranges(b.v.size(), [&](size_t first, size_t last) {
-            for (size_t i = first; i < last; ++i) collide_vertex(b.v[i], shapes, dt, restitution_threshold, radius);
+            for (size_t i = first; i < last; ++i) collide_vertex(b.v[i], shapes, dt, restitution_threshold, radius, flags ? flags + i : nullptr);
         });
     }
 
     // one vertex of ApplyCollisionConstraintsAndUpdateVelocities
-    void collide_vertex(Vertex<R> &v, const std::vector<CollidingShape<R>> &shapes, R dt, R restitution_threshold, R radius) {
+    void collide_vertex(Vertex<R> &v, const std::vector<CollidingShape<R>> &shapes, R dt, R restitution_threshold, R radius,
+                        uint8_t *flags) {
         {
             if (!(v.inv_mass > R(0))) return;
             V3<R> prev_v = v.vel;
             v.vel = divs(sub(v.pos, v.prev), dt);
             if (v.shape_idx < 0) return;
             R projected = -(dot(v.pos, v.plane_n) + v.plane_c) + radius;
-            if (!(projected > R(0))) return;
+            const bool replay = flags && freeze_mode == 2;
+            const bool contact = replay ? (*flags & 1) != 0 : projected > R(0);
+            if (flags && !replay && contact) *flags |= 1;
+            if (!contact) return;
             v.contact = true;
             const CollidingShape<R> &cs = shapes[v.shape_idx];
             V3<R> n = v.plane_n;
@@ -640,24 +703,38 @@ public:
             R vtl = len(v_tan);
             if (vtl > R(0)) {
                 R f = cs.friction * projected / (vtl * dt);
-                if (f > R(1)) f = R(1);
+                const bool clamped = replay ? (*flags & 2) != 0 : f > R(1);
+                if (flags && !replay && clamped) *flags |= 2;
+                if (clamped) f = R(1);
                 v.vel = sub(v.vel, mul(v_tan, f));
             }
             v.vel = sub(v.vel, v_normal);
             R pvn = dot(prev_v, n);
-            if (pvn < restitution_threshold) v.vel = sub(v.vel, mul(cs.restitution * pvn, n));
+            const bool bounce = replay ? (*flags & 4) != 0 : pvn < restitution_threshold;
+            if (flags && !replay && bounce) *flags |= 4;
+            if (bounce) v.vel = sub(v.vel, mul(cs.restitution * pvn, n));
         }
     }
 
-    void update_state(Body<R> &b, R dt, V3<R> disp_g) {  // :827-921
+    void update_state(Body<R> &b, R dt, V3<R> disp_g, typename Body<R>::Decisions *dec) {  // :827-921
         R max_sq = R(b.cs.max_linear_velocity) * R(b.cs.max_linear_velocity);
+        R max_v_sq = R(0);
         V3<R> lin = {R(0), R(0), R(0)}, ang = {R(0), R(0), R(0)};
         const R big = R(FLT_MAX);
         b.bmin = b.pmin = {big, big, big};
         b.bmax = b.pmax = {-big, -big, -big};
-        for (auto &v : b.v) {
+        for (size_t vi = 0; vi < b.v.size(); ++vi) {
+            Vertex<R> &v = b.v[vi];
             R vsq = len_sq(v.vel);
-            if (vsq > max_sq) v.vel = mul(v.vel, std::sqrt(max_sq / vsq));
+            max_v_sq = std::max(max_v_sq, vsq);
+            bool clamp = vsq > max_sq;
+            if (dec) {
+                if (freeze_mode == 2)
+                    clamp = dec->vclamp[vi] != 0;
+                else
+                    dec->vclamp[vi] = clamp ? 1 : 0;
+            }
+            if (clamp) v.vel = mul(v.vel, std::sqrt(max_sq / vsq));
             lin = add(lin, v.vel);
             ang = add(ang, cross(v.pos, v.vel));
             b.bmin = vmin(b.bmin, v.pos);
@@ -682,6 +759,18 @@ public:
             wd.y = (R(0) * delta.x + R(1) * delta.y) + R(0) * delta.z;
             wd.z = (R(0) * delta.x + R(0) * delta.y) + R(1) * delta.z;
             b.position = add(b.position, wd);
+        }
+        // sleep test (:902-915) and deactivation (PhysicsSystem.cpp:2875-2884, BodyManager.cpp:559-561)
+        if (b.cs.allow_sleeping) {
+            if (max_v_sq > sleep_velocity_threshold) {
+                b.sleep_timer = R(0);
+            } else {
+                b.sleep_timer = b.sleep_timer + dt;
+                if (b.sleep_timer >= time_before_sleep) {
+                    b.active = false;
+                    b.lin_vel = b.ang_vel = {R(0), R(0), R(0)};
+                }
+            }
         }
         b.force = {R(0), R(0), R(0)};  // ResetForce (:920)
     }
@@ -734,8 +823,8 @@ int oracle_add_collider(void *w, int type, const float pos[3], const float half_
 }
 
 // creation: num_iterations, linear_damping, max_linear_velocity, restitution, friction, pressure,
-// gravity_factor, vertex_radius, update_position (as float 0/1)
-int oracle_add_body(void *w, const uint8_t *blob, size_t len, const float pos[3], const float creation[9]) {
+// gravity_factor, vertex_radius, update_position, allow_sleeping (the last two as float 0/1)
+int oracle_add_body(void *w, const uint8_t *blob, size_t len, const float pos[3], const float creation[10]) {
     Handle *h = static_cast<Handle *>(w);
     auto s = std::make_shared<Settings>();
     if (!parse_settings(blob, len, *s, h->err)) return -1;
@@ -753,16 +842,26 @@ int oracle_add_body(void *w, const uint8_t *blob, size_t len, const float pos[3]
     cs.gravity_factor = creation[6];
     cs.vertex_radius = creation[7];
     cs.update_position = creation[8] != 0.0f;
+    cs.allow_sleeping = creation[9] != 0.0f;
     h->wd.add_body(s, pos, cs);
     return h->wf.add_body(s, pos, cs);
 }
 
+// BodyInterface::AddForce (EActivation::Activate): sets the step's force, wakes the body and restarts its
+// sleep timer (BodyInterface.cpp:699-713).
 int oracle_set_force(void *w, int body, const float f[3]) {
     Handle *h = static_cast<Handle *>(w);
     h->wf.bodies[body].force = {f[0], f[1], f[2]};
     h->wd.bodies[body].force = {double(f[0]), double(f[1]), double(f[2])};
+    h->wf.bodies[body].active = h->wd.bodies[body].active = true;
+    h->wf.bodies[body].sleep_timer = 0.0f;
+    h->wd.bodies[body].sleep_timer = 0.0;
     return 0;
 }
+
+int oracle_body_active(void *w, int body) { return static_cast<Handle *>(w)->wf.bodies[body].active ? 1 : 0; }
+
+float oracle_body_sleep_timer(void *w, int body) { return static_cast<Handle *>(w)->wf.bodies[body].sleep_timer; }
 
 int oracle_step(void *w, float dt, int collision_steps) {
     Handle *h = static_cast<Handle *>(w);
@@ -856,6 +955,38 @@ int oracle_set_compliance_f64(void *w, int body, const double *edge, int num_edg
 int oracle_set_force_f64(void *w, int body, const double f[3]) {
     Handle *h = static_cast<Handle *>(w);
     h->wd.bodies[body].force = {f[0], f[1], f[2]};
+    h->wd.bodies[body].active = true;
+    h->wd.bodies[body].sleep_timer = 0.0;
+    return 0;
+}
+
+// Frozen-decision runs (see World::freeze_mode): 0 off, 1 record, 2 replay.
+int oracle_set_freeze(void *w, int mode) {
+    Handle *h = static_cast<Handle *>(w);
+    h->wf.freeze_mode = h->wd.freeze_mode = mode;
+    return 0;
+}
+
+// Copies every body's recorded decisions from world src to world dst (same scene) and rewinds them.
+int oracle_copy_decisions(void *dst, const void *src) {
+    Handle *d = static_cast<Handle *>(dst);
+    const Handle *s = static_cast<const Handle *>(src);
+    if (d->wd.bodies.size() != s->wd.bodies.size()) return -1;
+    for (size_t i = 0; i < d->wd.bodies.size(); ++i) {
+        d->wd.bodies[i].decisions = s->wd.bodies[i].decisions;
+        d->wd.bodies[i].decision_step = 0;
+        d->wf.bodies[i].decisions = s->wf.bodies[i].decisions;
+        d->wf.bodies[i].decision_step = 0;
+    }
+    return 0;
+}
+
+int oracle_set_sleep_settings(void *w, float time_before_sleep, float point_velocity_sleep_threshold) {
+    Handle *h = static_cast<Handle *>(w);
+    h->wf.time_before_sleep = time_before_sleep;
+    h->wf.sleep_velocity_threshold = point_velocity_sleep_threshold;
+    h->wd.time_before_sleep = time_before_sleep;
+    h->wd.sleep_velocity_threshold = point_velocity_sleep_threshold;
     return 0;
 }
 

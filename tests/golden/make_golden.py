@@ -39,6 +39,8 @@ CASES = {
     "large_cloth_32": ("large_cloth", dict(n=32, steps=120), [1, 60, 120]),
     "diff_cloth_16": ("diff_cloth", dict(n=16, steps=40), [1, 40]),
     "diff_batch_small": ("diff_batch", dict(n_cloth=4, n_cube=2, steps=30), [1, 30]),
+    # sleeping allowed: bodies that come to rest on the floor fall asleep and stop being stepped
+    "sleep_small": ("uneven_batch", dict(n_cloth=6, n_cube=3, cloth_max=20, cube_max=5, steps=200, sleep=1), [1, 60, 120, 160, 200]),
 }
 
 
@@ -56,6 +58,8 @@ def make(name: str, scene: str, params: dict, steps: list[int]):
             for d in dumps[1:]:
                 if variant == "fast" and d.step != steps[-1] and name != "pinned_cloth":
                     continue  # (the pinned cloth keeps the default build at every step: its stated tolerance)
+                if variant == "det":  # MotionProperties::mSleepTestTimer from the SaveState bytes (offset 96)
+                    out[f"det_timer_{d.step}"] = np.array([np.frombuffer(st, np.float32, 1, 96)[0] for st in d.states], np.float32)
                 out[f"{variant}_pos_{d.step}"] = np.stack(d.positions).astype(np.float32)
                 out[f"{variant}_local_{d.step}"] = np.concatenate(d.local).astype(np.float32)
                 out[f"{variant}_vel_{d.step}"] = np.concatenate(d.velocities).astype(np.float32)

@@ -182,43 +182,51 @@ def batch_gradients(jsb, scene_bytes, steps=90, every=15, seed=17):
     return grads["force"].astype(np.float64), np.add.reduceat(grads["v0"].astype(np.float64), offsets[:-1], axis=0), targets
 
 
-def batch_fd(scene, b, kind, k, target, steps, eps=1e-6, shift=0.0) -> float:
-    """FP64 central difference of body b's loss term in its force or v0 component k (base point scaled
-    by 1 + shift)."""
+def batch_fd(scene, b, kind, k, target, steps, eps=1e-6, frozen=True) -> float:
+    """FP64 central difference of body b's loss term in its force or initial-velocity component k. frozen:
+    the perturbed runs replay the base run's collision decisions (planes, contacts, friction clamps,
+    restitution, velocity clamp), the derivative the adjoint computes; else they decide again."""
     body = scene.bodies[b]
     f0 = np.asarray(body.force, np.float64)
     _, v0, _ = blob_arrays(body.blob)
+    rec = []
+    if frozen:
+        run64(scene, b, steps, set(), record=rec)
     vals = []
     for sgn in (1.0, -1.0):
+        replay = rec[0] if rec else None
         if kind == "force":
-            f = f0 * (1.0 + shift)
+            f = f0.copy()
             f[k] += sgn * eps
-            out = run64(scene, b, steps, {steps}, force=f)
+            out = run64(scene, b, steps, {steps}, force=f, replay=replay)
         else:
-            v = v0 * (1.0 + shift)
+            v = v0.copy()
             v[:, k] += sgn * eps
-            out = run64(scene, b, steps, {steps}, v0=v)
+            out = run64(scene, b, steps, {steps}, v0=v, replay=replay)
         vals.append(float(((out[steps].mean(axis=0) - target) ** 2).sum()))
     return (vals[0] - vals[1]) / (2 * eps)
 
 
 def diff_batch_check(jsb, build_scene, n_params=32, steps=90, every=15) -> dict:
-    """GPU gradients against FP64 central FD on n_params random (body, axis) parameters, half force, half
-    v0. A parameter whose FD moves by more than 1e-4 relative when the base point moves by 1e-7 relative
-    (a contact makes the loss only piecewise smooth there) is counted apart, not held to the bar."""
+    """GPU gradients against FP64 central FD (with the base run's collision decisions replayed, the
+    derivative the adjoint computes) on n_params random (body, axis) parameters of distinct bodies, half
+    force, half v0. A parameter whose FD with step 1e-6 and with step 4e-6 differ by more than 1e-4
+    relative is not smooth at the FD scale (some hanging cloths are chaotic over the run): it is
+    reported, not held to the bar."""
     scene_bytes = build_scene("diff_batch", steps=steps)
     scene, _ = parse_scene(scene_bytes)
     g_force, g_v0, targets = batch_gradients(jsb, scene_bytes, steps, every)
     rng = np.random.default_rng(23)
     nb = len(scene.bodies)
-    picks = [("force", int(rng.integers(nb)), int(rng.integers(3))) for _ in range(n_params // 2)]
-    picks += [("v0", int(rng.integers(nb)), int(rng.integers(3))) for _ in range(n_params - n_params // 2)]
+    bodies = [int(b) for b in rng.permutation(nb)[:n_params]]
+    picks = [("force" if i < n_params // 2 else "v0", b, int(rng.integers(3))) for i, b in enumerate(bodies)]
     rows = []
     for kind, b, k in picks:
         f = batch_fd(scene, b, kind, k, targets[b], steps)
-        stable = abs(batch_fd(scene, b, kind, k, targets[b], steps, shift=1e-7) - f) <= 1e-4 * max(abs(f), 1e-12)
+        f4 = batch_fd(scene, b, kind, k, targets[b], steps, eps=4e-6)
+        smooth = abs(f4 - f) <= 1e-4 * max(abs(f), 1e-12)
         gpu = float(g_force[b, k] if kind == "force" else g_v0[b, k])
-        rows.append({"kind": kind, "body": b, "axis": k, "gpu": gpu, "fd": f, "smooth": bool(stable)})
+        rows.append({"kind": kind, "body": b, "axis": k, "gpu": gpu, "fd": f, "smooth": bool(smooth)})
     out = {"parameters": len(rows), "finite": bool(np.isfinite(g_force).all() and np.isfinite(g_v0).all())}
     for kind in ("force", "v0"):
         sel = [r for r in rows if r["kind"] == kind and r["smooth"]]

@@ -198,6 +198,12 @@ class Oracle:
                                                     ctypes.c_void_p, ctypes.c_int]
             L.oracle_set_force_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
             L.oracle_get_world_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+            L.oracle_body_active.argtypes = [ctypes.c_void_p, ctypes.c_int]
+            L.oracle_body_sleep_timer.argtypes = [ctypes.c_void_p, ctypes.c_int]
+            L.oracle_body_sleep_timer.restype = ctypes.c_float
+            L.oracle_set_sleep_settings.argtypes = [ctypes.c_void_p, ctypes.c_float, ctypes.c_float]
+            L.oracle_set_freeze.argtypes = [ctypes.c_void_p, ctypes.c_int]
+            L.oracle_copy_decisions.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
             L.oracle_last_error.restype = ctypes.c_char_p
             L.oracle_last_error.argtypes = [ctypes.c_void_p]
             cls._lib = L
@@ -215,7 +221,7 @@ class Oracle:
         self.nv = []
         for b in scene.bodies:
             cr = b.creation
-            creation = (ctypes.c_float * 9)(cr[0], cr[1], cr[2], cr[3], cr[4], cr[5], cr[6], cr[7], cr[8])
+            creation = (ctypes.c_float * 10)(cr[0], cr[1], cr[2], cr[3], cr[4], cr[5], cr[6], cr[7], cr[8], cr[10])
             idx = L.oracle_add_body(self.h, b.blob, len(b.blob), (ctypes.c_float * 3)(*b.position), creation)
             if idx < 0:
                 raise RuntimeError(L.oracle_last_error(self.h).decode())
@@ -233,6 +239,12 @@ class Oracle:
                 if any(f != 0.0 for f in b.force):
                     L.oracle_set_force(self.h, i, (ctypes.c_float * 3)(*b.force))
             L.oracle_step(self.h, self.scene.dt, self.scene.collision_steps)
+
+    def active(self, i: int) -> bool:
+        return bool(self.lib().oracle_body_active(self.h, i))
+
+    def sleep_timer(self, i: int) -> float:
+        return float(self.lib().oracle_body_sleep_timer(self.h, i))
 
     def set_state(self, i: int, local_positions, velocities):
         """Local positions and velocities (N, 3) of body i (float world)."""
@@ -285,10 +297,18 @@ class FD64:
     def __init__(self, scene: Scene, seeds: dict, steps: int):
         self.scene, self.seeds, self.steps = scene, seeds, steps
 
-    def loss(self, overrides: dict | None = None) -> float:
+    def loss(self, overrides: dict | None = None, record: list | None = None, replay=None) -> float:
+        """record: a list receiving the run's oracle with its collision decisions recorded; replay: such an
+        oracle, whose decisions this run replays (the collision active set frozen, as the adjoint has it)."""
         overrides = overrides or {}
         L = Oracle.lib()
         o = Oracle(self.scene, use_double=True)
+        if record is not None:
+            L.oracle_set_freeze(o.h, 1)
+            record.append(o)
+        elif replay is not None:
+            L.oracle_copy_decisions(o.h, replay.h)
+            L.oracle_set_freeze(o.h, 2)
         forces = {}
         for b, body in enumerate(self.scene.bodies):
             ov = overrides.get(b, {})
@@ -313,14 +333,18 @@ class FD64:
                 total += float((np.asarray(r, np.float64) * w).sum())
         return total
 
-    def central(self, body: int, kind: str, index: tuple, eps: float) -> float:
-        """Central difference of the loss in one parameter component."""
+    def central(self, body: int, kind: str, index: tuple, eps: float, frozen: bool = False) -> float:
+        """Central difference of the loss in one parameter component; frozen: the perturbed runs replay the
+        base run's collision decisions (planes, contacts, friction clamps, restitution, velocity clamp)."""
         base = self.base_params(body)[kind]
+        rec = []
+        if frozen:
+            self.loss({}, record=rec)
         vals = []
         for sgn in (1.0, -1.0):
             p = base.copy()
             p[index] += sgn * eps
-            vals.append(self.loss({body: {kind: p}}))
+            vals.append(self.loss({body: {kind: p}}, replay=rec[0] if rec else None))
         return (vals[0] - vals[1]) / (2.0 * eps)
 
     def base_params(self, body: int) -> dict:
@@ -336,13 +360,23 @@ def single_body_scene(scene: Scene, b: int) -> Scene:
                  colliders=list(scene.colliders), bodies=[scene.bodies[b]])
 
 
-def run64(scene: Scene, b: int, steps: int, observe, x0=None, v0=None, edge=None, volume=None, force=None) -> dict:
+def run64(scene: Scene, b: int, steps: int, observe, x0=None, v0=None, edge=None, volume=None, force=None,
+          record=None, replay=None) -> dict:
     """FP64 oracle run of body b alone (optionally with its initial local positions / velocities, edge /
-    volume compliance or step force replaced); world positions (N, 3) after each step in `observe`."""
+    volume compliance or step force replaced); world positions (N, 3) after each step in `observe`.
+    record: a list that receives the run's oracle with every collision decision recorded; replay: such an
+    oracle, whose decisions this run takes instead of deciding again (the collision active set frozen,
+    as the adjoint differentiates it)."""
     sc = single_body_scene(scene, b)
     body = sc.bodies[0]
     L = Oracle.lib()
     o = Oracle(sc, use_double=True)
+    if record is not None:
+        L.oracle_set_freeze(o.h, 1)
+        record.append(o)
+    elif replay is not None:
+        L.oracle_copy_decisions(o.h, replay.h)
+        L.oracle_set_freeze(o.h, 2)
     bx0, bv0, _ = blob_arrays(body.blob)
     ec, vc = blob_compliance(body.blob)
     xx = np.ascontiguousarray(bx0 if x0 is None else x0, np.float64)

@@ -105,6 +105,9 @@ inline bool make_named_scene(const std::string &name, const std::string &params,
     long it;
     if (param_get(params, "iterations", it))
         for (auto &b : out.bodies) b.creation.num_iterations = uint32_t(it);
+    long sleep;
+    if (param_get(params, "sleep", sleep))  // SoftBodyCreationSettings::mAllowSleeping of every body
+        for (auto &b : out.bodies) b.creation.allow_sleeping = sleep != 0;
     return true;
 }
 

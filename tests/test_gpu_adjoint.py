@@ -51,7 +51,7 @@ def gpu_gradients(jsb, scene_bytes, seeds, steps, every, forces=None, trajectory
     return out
 
 
-def sample_and_compare(fd, grads, picks, rng):
+def sample_and_compare(fd, grads, picks, rng, frozen=False):
     errors = []
     for body, kind, count in picks:
         base = fd.base_params(body)[kind]
@@ -62,7 +62,7 @@ def sample_and_compare(fd, grads, picks, rng):
         fds, gps = [], []
         for idx in idxs:
             eps = EPS.get(kind, 1e-6 * abs(base[idx]) + 1e-14)
-            fds.append(fd.central(body, kind, idx, eps))
+            fds.append(fd.central(body, kind, idx, eps, frozen=frozen))
             gps.append(float(gpu[idx]))
         fds, gps = np.array(fds), np.array(gps)
         rel = np.linalg.norm(gps - fds) / max(np.linalg.norm(fds), 1e-30)
@@ -124,8 +124,10 @@ def test_adjoint_contacts_vs_fp64_autodiff(jsb):
     assert worst["free"] <= 1e-2, worst
 
 
-def test_adjoint_contacts_vs_fd_report(jsb):
-    """FD through contact events is only piecewise smooth; reported, with a loose bar."""
+def test_adjoint_contacts_vs_frozen_fd(jsb):
+    """Through contact events: FP64 central FD whose perturbed runs replay the base run's collision
+    decisions (planes in world space, contacts, friction clamps, restitution, velocity clamp), i.e. the
+    derivative the adjoint computes with the collision active set frozen, within 1e-3."""
     scene_bytes = contact_scene(jsb)
     scene, _ = parse_scene(scene_bytes)
     rng = np.random.default_rng(11)
@@ -133,10 +135,10 @@ def test_adjoint_contacts_vs_fd_report(jsb):
     grads = gpu_gradients(jsb, scene_bytes, seeds, 24, 8)
     fd = FD64(scene, seeds, 24)
     errs = sample_and_compare(fd, grads, [(0, "x0", 6), (0, "force", 3), (1, "v0", 6), (1, "volume", 6), (1, "force", 3)],
-                              rng)
+                              rng, frozen=True)
     for kind, body, e, fds, gps in errs:
         print(kind, body, "rel", e, "\n  fd ", fds, "\n  gpu", gps)
-    assert max(e for _, _, e, _, _ in errs) <= 5e-2
+    assert max(e for _, _, e, _, _ in errs) <= 1e-3, [(k, b, e) for k, b, e, _, _ in errs]
 
 
 def test_checkpoint_interval_does_not_change_gradients(jsb):
@@ -296,4 +298,6 @@ def test_tethered_cloth_adjoint_is_deterministic(jsb):
     errs = sample_and_compare(fd, a, [(0, "x0", 8), (0, "v0", 8)], rng)
     for kind, body, e, fds, gps in errs:
         print(kind, body, "rel", e)
-    assert max(e for _, _, e, _, _ in errs) <= 1e-3, [(k, e) for k, _, e, _, _ in errs]
+    # (a tether is a one-sided constraint: its activation |d| > max distance makes the loss only piecewise
+    # smooth, so the bar is looser than for edges alone)
+    assert max(e for _, _, e, _, _ in errs) <= 5e-3, [(k, e) for k, _, e, _, _ in errs]

@@ -15,7 +15,7 @@ from scenes import build_scene
 
 pytestmark = pytest.mark.gpu
 
-GOLDEN = ["pinned_cloth", "uneven_small", "large_cloth_32", "diff_cloth_16", "diff_batch_small"]
+GOLDEN = ["pinned_cloth", "uneven_small", "large_cloth_32", "diff_cloth_16", "diff_batch_small", "sleep_small"]
 
 
 def split(arr, nv):
@@ -71,6 +71,11 @@ def test_bitwise_vs_reference(jsb, name):
         ref = [(g[f"det_pos_{step}"][b], split(g[f"det_local_{step}"], nv)[b], split(g[f"det_vel_{step}"], nv)[b])
                for b in range(len(nv))]
         assert_same(snap, ref, f"{name} step {step}")
+        if f"det_timer_{step}" in g:  # sleep timers in the SaveState bytes, and which bodies sleep
+            for b in range(len(nv)):
+                timer = np.frombuffer(ctx.save_state(b), np.float32, 1, 96)[0]
+                assert timer == g[f"det_timer_{step}"][b], (name, step, b, timer)
+                assert ctx.is_active(b) == bool(timer < 0.5), (name, step, b)
 
 
 def test_pinned_cloth_tolerance_vs_fma_reference(jsb):
@@ -263,3 +268,35 @@ def test_step_walk_equals_substep_walk_and_oracle(jsb, state_mode, threads):
         assert_same(sa, [o.body(i) for i in range(len(scene.bodies))], f"step walk vs oracle, step {step}")
     # the floor was reached: some vertex of a cube sits on it
     assert min((loc[:, 1] + pos[1]).min() for pos, loc, _ in sa[10:]) < 0.05
+
+
+def test_sleeping_body_wakes_on_force(jsb):
+    """A body asleep on the floor is not stepped (its state stays bit for bit); AddForce wakes it and
+    restarts its sleep timer (BodyInterface::AddForce with EActivation::Activate), like the oracle."""
+    g = np.load(golden_path("sleep_small"))
+    scene_bytes = g["scene"].tobytes()
+    scene, _ = parse_scene(scene_bytes)
+    ctx = make_ctx(jsb, scene_bytes)
+    o = Oracle(scene)
+    advance(ctx, 160, "graph")
+    o.step(160)
+    asleep = [b for b in range(len(scene.bodies)) if not ctx.is_active(b)]
+    assert asleep and all(not o.active(b) for b in asleep)
+    before = snapshot(ctx)
+    advance(ctx, 5)
+    after = snapshot(ctx)
+    for b in asleep:
+        for k in range(3):
+            assert np.array_equal(before[b][k], after[b][k])
+    o.step(5)
+    b = asleep[0]
+    ctx.add_force(b, (0.0, 50.0, 0.0))
+    scene.bodies[b].force = (0.0, 50.0, 0.0)  # the oracle applies the force before its next step
+    o.step(1)
+    scene.bodies[b].force = (0.0, 0.0, 0.0)
+    ctx.step()
+    assert ctx.is_active(b) and o.active(b)
+    assert_same(snapshot(ctx), [o.body(i) for i in range(len(scene.bodies))], "after the wake")
+    o.step(3)
+    advance(ctx, 3)
+    assert_same(snapshot(ctx), [o.body(i) for i in range(len(scene.bodies))], "3 steps later")

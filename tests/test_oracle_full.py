@@ -70,9 +70,9 @@ def test_diff_cloth_gradient_conditioning(oracle_lib):
     horizon: FP64 central differences (the oracle in double precision) of its MSE loss, on 8 edge
     compliances and 8 initial velocities, move by more than 1e-2 relative when the initial positions move
     by 1e-7 m and the loss is taken at steps 60 and 120 (the stated configuration), and by less than 1e-3
-    when it is taken at steps 3 and 6. No FP32 trajectory can match a gradient that is not stable under
-    perturbations far below its own rounding, so the full-length gradient is checked along the GPU's own
-    trajectory instead (tests/test_gpu_gradients_full.py)."""
+    (but not much less) when it is taken at steps 3 and 6. No FP32 trajectory can match a gradient that
+    is not stable under perturbations far below its own rounding, so the full-length gradient is checked
+    along the GPU's own trajectory instead (tests/test_gpu_gradients_full.py)."""
     from jsb_testlib import blob_arrays, blob_compliance, run64
 
     scene, _ = parse_scene(build_scene("diff_cloth"))

@@ -10,7 +10,7 @@ import pytest
 from conftest import golden_path
 from jsb_testlib import parse_scene
 
-CASES = ["pinned_cloth", "uneven_small", "large_cloth_32", "diff_cloth_16", "diff_batch_small"]
+CASES = ["pinned_cloth", "uneven_small", "large_cloth_32", "diff_cloth_16", "diff_batch_small", "sleep_small"]
 
 
 def load(name):
@@ -44,6 +44,8 @@ def test_oracle_bitwise_vs_reference(name, oracle_lib):
             assert np.array_equal(pos, ref_pos[b]), (name, step, b)
             assert np.array_equal(loc, ref_loc[b]), (name, step, b)
             assert np.array_equal(vel, ref_vel[b]), (name, step, b)
+            if f"det_timer_{step}" in g:  # sleep timers (MotionProperties::mSleepTestTimer)
+                assert np.float32(o.sleep_timer(b)) == g[f"det_timer_{step}"][b], (name, step, b)
 
 
 @pytest.mark.parametrize("name", ["pinned_cloth"])
