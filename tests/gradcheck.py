@@ -8,13 +8,14 @@ the gradient of a plain FP64 re-implementation (tests/torch_ref.py) by autodiff 
 trajectory, and FP64 central finite differences of the oracle (free running).
 Differentiable batch (256 bodies, 90 steps, checkpoint every 15): loss = sum over bodies of |centre of
 mass at the last step - target|^2; gradients with respect to every body's step force and initial
-velocity; FP64 central finite differences of each perturbed body alone.
+velocity. References: FP64 autodiff of single bodies along the GPU's own trajectory, and FP64 central
+finite differences of each perturbed body alone with the base run's collision decisions replayed.
 """
 from __future__ import annotations
 
 import numpy as np
 
-from jsb_testlib import blob_arrays, blob_compliance, parse_scene, run64
+from jsb_testlib import blob_arrays, blob_compliance, parse_scene, run64, single_body_scene
 
 
 def rel(a, b) -> float:
@@ -153,9 +154,10 @@ def diff_cloth_check(jsb, build_scene, steps=120, every=10, loss_steps=(60, 120)
 
 
 # ---- differentiable batch ----------------------------------------------------------------------------
-def batch_gradients(jsb, scene_bytes, steps=90, every=15, seed=17):
+def batch_gradients(jsb, scene_bytes, steps=90, every=15, seed=17, trajectory_bodies=()):
     """GPU adjoint of the centre-of-mass loss: (force gradients (B, 3), per-body v0 gradients (B, 3),
-    targets (B, 3))."""
+    targets (B, 3), trajectory). trajectory[step] = {b: (world positions, velocities)} for the bodies in
+    trajectory_bodies after every step."""
     scene, _ = parse_scene(scene_bytes)
     nb = len(scene.bodies)
     rng = np.random.default_rng(seed)
@@ -166,6 +168,14 @@ def batch_gradients(jsb, scene_bytes, steps=90, every=15, seed=17):
     counts = np.asarray(ctx.num_vertices, np.int64)
     offsets = np.concatenate([[0], np.cumsum(counts)])
     ctx.adjoint_begin(steps, every)
+    trajectory = {}
+    if trajectory_bodies:
+        for s in range(1, steps + 1):
+            ctx.adjoint_forward(s)
+            trajectory[s] = {}
+            for b in trajectory_bodies:
+                pos, loc, vel = ctx.read_body(b)
+                trajectory[s][b] = (loc.astype(np.float64) + pos.astype(np.float64), vel.astype(np.float64))
     ctx.adjoint_forward()
     loc = np.zeros((int(offsets[-1]), 3), np.float32)
     vel = np.zeros_like(loc)
@@ -179,13 +189,46 @@ def batch_gradients(jsb, scene_bytes, steps=90, every=15, seed=17):
     ctx.adjoint_end()
     ctx.close()
     # every vertex of a body starts with the body's v0: its gradient is the sum over the vertices
-    return grads["force"].astype(np.float64), np.add.reduceat(grads["v0"].astype(np.float64), offsets[:-1], axis=0), targets
+    return (grads["force"].astype(np.float64), np.add.reduceat(grads["v0"].astype(np.float64), offsets[:-1], axis=0), targets,
+            trajectory)
 
 
-def batch_fd(scene, b, kind, k, target, steps, eps=1e-6, frozen=True) -> float:
+def batch_pinned_reference(scene, b, target, steps, trajectory):
+    """FP64 autodiff of body b's loss term, its state moved onto the GPU trajectory after every step:
+    (force gradient (3,), v0 gradient summed over the vertices (3,))."""
+    import torch
+
+    from torch_ref import base_params, simulate
+
+    sc = single_body_scene(scene, b)
+    params = base_params(sc)
+    pin = {s: [trajectory[s][b]] for s in trajectory}
+    out = simulate(sc, params, steps, [steps], pin)
+    loss = ((out[steps][0].mean(0) - torch.tensor(target, dtype=torch.float64)) ** 2).sum()
+    loss.backward()
+    return params[0]["force"].grad.numpy().copy(), params[0]["v0"].grad.numpy().sum(axis=0)
+
+
+def pinned_bodies(scene, count_cloth=2, count_cube=1) -> list[int]:
+    """The smallest cloths (no volume constraints) and tetrahedral cubes of a batch, by vertex count."""
+    from jsb_testlib import blob_counts_py
+
+    rows = [(scene.bodies[b].num_vertices, b, blob_counts_py(scene.bodies[b].blob)["volumes"] > 0) for b in range(len(scene.bodies))]
+    cloths = [b for _, b, cube in sorted(rows) if not cube][:count_cloth]
+    cubes = [b for _, b, cube in sorted(rows) if cube][:count_cube]
+    return cloths + cubes
+
+
+# central-difference steps: the step force enters as force * dt / vertices per substep, so its loss
+# differences at 1e-6 N sit near the FP64 rounding noise of the run
+FD_EPS = {"force": 1e-3, "v0": 1e-6}
+
+
+def batch_fd(scene, b, kind, k, target, steps, eps=None, frozen=True) -> float:
     """FP64 central difference of body b's loss term in its force or initial-velocity component k. frozen:
     the perturbed runs replay the base run's collision decisions (planes, contacts, friction clamps,
     restitution, velocity clamp), the derivative the adjoint computes; else they decide again."""
+    eps = FD_EPS[kind] if eps is None else eps
     body = scene.bodies[b]
     f0 = np.asarray(body.force, np.float64)
     _, v0, _ = blob_arrays(body.blob)
@@ -207,15 +250,26 @@ def batch_fd(scene, b, kind, k, target, steps, eps=1e-6, frozen=True) -> float:
     return (vals[0] - vals[1]) / (2 * eps)
 
 
-def diff_batch_check(jsb, build_scene, n_params=32, steps=90, every=15) -> dict:
-    """GPU gradients against FP64 central FD (with the base run's collision decisions replayed, the
+def diff_batch_check(jsb, build_scene, n_params=32, steps=90, every=15, pinned_counts=(2, 1)) -> dict:
+    """GPU gradients against (pinned) FP64 autodiff of the smallest cloths and cubes (pinned_counts)
+    along the GPU trajectory, and against FP64 central FD (with the base run's collision decisions replayed, the
     derivative the adjoint computes) on n_params random (body, axis) parameters of distinct bodies, half
-    force, half v0. A parameter whose FD with step 1e-6 and with step 4e-6 differ by more than 1e-4
-    relative is not smooth at the FD scale (some hanging cloths are chaotic over the run): it is
-    reported, not held to the bar."""
+    force, half v0. A parameter whose FD with steps eps and 4 eps differ by more than 1e-4 relative is
+    not smooth at the FD scale (some hanging cloths are chaotic over the run): it is reported, not held to
+    the bar."""
     scene_bytes = build_scene("diff_batch", steps=steps)
     scene, _ = parse_scene(scene_bytes)
-    g_force, g_v0, targets = batch_gradients(jsb, scene_bytes, steps, every)
+    pin_bodies = pinned_bodies(scene, *pinned_counts)
+    g_force, g_v0, targets, traj = batch_gradients(jsb, scene_bytes, steps, every, trajectory_bodies=pin_bodies)
+    out = {"finite": bool(np.isfinite(g_force).all() and np.isfinite(g_v0).all())}
+    if pin_bodies:
+        ref = [batch_pinned_reference(scene, b, targets[b], steps, traj) for b in pin_bodies]
+        out["pinned_fp64_autodiff"] = {
+            "bodies": pin_bodies,
+            "force": rel(np.concatenate([g_force[b] for b in pin_bodies]), np.concatenate([r[0] for r in ref])),
+            "v0": rel(np.concatenate([g_v0[b] for b in pin_bodies]), np.concatenate([r[1] for r in ref]))}
+    if not n_params:
+        return out
     rng = np.random.default_rng(23)
     nb = len(scene.bodies)
     bodies = [int(b) for b in rng.permutation(nb)[:n_params]]
@@ -223,14 +277,15 @@ def diff_batch_check(jsb, build_scene, n_params=32, steps=90, every=15) -> dict:
     rows = []
     for kind, b, k in picks:
         f = batch_fd(scene, b, kind, k, targets[b], steps)
-        f4 = batch_fd(scene, b, kind, k, targets[b], steps, eps=4e-6)
+        f4 = batch_fd(scene, b, kind, k, targets[b], steps, eps=4 * FD_EPS[kind])
         smooth = abs(f4 - f) <= 1e-4 * max(abs(f), 1e-12)
         gpu = float(g_force[b, k] if kind == "force" else g_v0[b, k])
         rows.append({"kind": kind, "body": b, "axis": k, "gpu": gpu, "fd": f, "smooth": bool(smooth)})
-    out = {"parameters": len(rows), "finite": bool(np.isfinite(g_force).all() and np.isfinite(g_v0).all())}
+    out["parameters"] = len(rows)
     for kind in ("force", "v0"):
         sel = [r for r in rows if r["kind"] == kind and r["smooth"]]
         out[kind] = {"smooth": len(sel), "of": sum(r["kind"] == kind for r in rows),
                      "rel_error": rel([r["gpu"] for r in sel], [r["fd"] for r in sel]) if sel else None}
     out["not_smooth"] = [r for r in rows if not r["smooth"]]
+    out["rows"] = rows
     return out
