@@ -56,16 +56,18 @@ typedef struct jsb_creation_settings {
     uint8_t faces_double_sided;   /* mFacesDoubleSided (queries only) */
 } jsb_creation_settings;
 
-enum { JSB_COLLIDER_BOX = 0, JSB_COLLIDER_SPHERE = 1 };
+enum { JSB_COLLIDER_BOX = 0, JSB_COLLIDER_SPHERE = 1, JSB_COLLIDER_CAPSULE = 2, JSB_COLLIDER_CYLINDER = 3 };
 
-/* A static rigid body with one convex leaf shape (BoxShape / SphereShape), world space, identity
- * rotation. friction/restitution are the body's; they are combined with the soft body's like
- * ContactConstraintManager's defaults (sqrt(f1 f2), max(r1, r2)). */
+/* A static rigid body with one convex leaf shape (BoxShape / SphereShape / CapsuleShape / CylinderShape),
+ * world space, identity rotation (capsules and cylinders along the Y axis). friction/restitution are the
+ * body's; they are combined with the soft body's like ContactConstraintManager's defaults (sqrt(f1 f2),
+ * max(r1, r2)). */
 typedef struct jsb_collider {
-    int32_t type;
+    int32_t type;         /* JSB_COLLIDER_* */
     float position[3];
-    float half_extent[3]; /* box */
-    float radius;         /* sphere */
+    float half_extent[3]; /* box: half extents; capsule: [1] = half height of the cylinder part
+                             (CapsuleShape's inHalfHeightOfCylinder); cylinder: [1] = half height */
+    float radius;         /* sphere, capsule, cylinder */
     float friction;
     float restitution;
 } jsb_collider;

@@ -923,7 +923,7 @@ jsb_status jsb_body_add(jsb_context *ctx, uint32_t settings_id, const jsb_creati
 
 jsb_status jsb_collider_add(jsb_context *ctx, const jsb_collider *c, uint32_t *collider_id) {
     if (!check_ctx(ctx) || !c || !collider_id) return fail(JSB_ERR_INVALID_ARGUMENT, "null argument");
-    if (c->type != JSB_COLLIDER_BOX && c->type != JSB_COLLIDER_SPHERE) return fail(JSB_ERR_INVALID_ARGUMENT, "unknown collider type");
+    if (c->type < JSB_COLLIDER_BOX || c->type > JSB_COLLIDER_CYLINDER) return fail(JSB_ERR_INVALID_ARGUMENT, "unknown collider type");
     ColliderDev d;
     d.type = c->type;
     for (int k = 0; k < 3; ++k) {

@@ -283,6 +283,73 @@ __device__ __forceinline__ void collide_sphere(f3 p, const SCol &s, int idx, flo
     shape = idx;
 }
 
+// CapsuleShape::CollideSoftBodyVertices (CapsuleShape.cpp:324-374) for one vertex: a capsule along
+// the Y axis (identity rotation), h[1] = half height of its cylinder part, r = radius.
+__device__ __forceinline__ void collide_capsule(f3 p, const SCol &s, int idx, float &largest, float4 &plane, int &shape) {
+    const f3 t = ld3(s.t);
+    const float hh = s.h[1], r = s.r;
+    const f3 local = p + neg(t);
+    if (fabsf(local.y) <= hh) {  // beside the cylinder part: radial normal
+        f3 normal = mk(local.x, 0.0f, local.z);
+        const float nl = len(normal);
+        const float pen = r - nl;
+        if (largest >= pen) return;
+        largest = pen;
+        normal = nl > 0.0f ? normal / nl : mk(1.0f, 0.0f, 0.0f);
+        plane = plane_transformed(normal, r * normal, t);
+    } else {  // beyond an end: the cap's sphere
+        const f3 center = mk(0.0f, (local.y < 0.0f ? -1.0f : 1.0f) * hh, 0.0f);
+        const f3 delta = local - center;
+        const float distance = len(delta);
+        const float pen = r - distance;
+        if (largest >= pen) return;
+        largest = pen;
+        const f3 normal = delta / distance;
+        plane = plane_transformed(normal, center + r * normal, t);
+    }
+    shape = idx;
+}
+
+// Vec3::NormalizedOr (Jolt/Math/Vec3.inl:978-998, SSE4.1 form): v / |v|, or `zero` when
+// |v|^2 = (x x + y y) + z z <= FLT_MIN.
+__device__ __forceinline__ f3 normalized_or(f3 v, f3 zero) {
+    const float px = v.x * v.x, py = v.y * v.y, pz = v.z * v.z;
+    const float len_sq = (px + py) + pz;
+    if (len_sq <= FLT_MIN) return zero;
+    return v / jsqrt(len_sq);
+}
+
+// CylinderShape::CollideSoftBodyVertices (CylinderShape.cpp:317-368) for one vertex: a cylinder along the
+// Y axis (identity rotation), h[1] = half height, r = radius. The plane is that of the closest surface
+// (side, top / bottom, or the rim for a vertex outside both), its penetration measured from the plane.
+__device__ __forceinline__ void collide_cylinder(f3 p, const SCol &s, int idx, float &largest, float4 &plane, int &shape) {
+    const f3 t = ld3(s.t);
+    const float hh = s.h[1], r = s.r;
+    const f3 local = p + neg(t);
+    const f3 side = mk(local.x, 0.0f, local.z);
+    const float side_len = len(side);
+    const float side_pen = r - side_len;
+    const float top_pen = hh - fabsf(local.y);
+    const float sgn = local.y < 0.0f ? -1.0f : 1.0f;
+    f3 point, normal;
+    if (side_pen < 0.0f && top_pen < 0.0f) {
+        point = side * jdiv(r, side_len) + mk(0.0f, hh * sgn, 0.0f);
+        normal = normalized_or(local - point, mk(0.0f, 1.0f, 0.0f));
+    } else if (side_pen < top_pen) {
+        normal = side_len > 0.0f ? side / side_len : mk(1.0f, 0.0f, 0.0f);
+        point = r * normal;
+    } else {
+        normal = mk(0.0f, sgn, 0.0f);
+        point = hh * normal;
+    }
+    const float c = -dot(normal, point);
+    const float pen = -(dot(local, normal) + c);
+    if (largest >= pen) return;
+    largest = pen;
+    plane = plane_transformed(normal, point, t);
+    shape = idx;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Reductions for UpdateSoftBodyState
 // ---------------------------------------------------------------------------------------------
@@ -309,10 +376,12 @@ __device__ __forceinline__ int collision_plane(f3 x, const SCol *cols, int ncols
     int shape = -1;
     float largest = -FLT_MAX;
     for (int s = 0; s < ncols; ++s) {
-        if (cols[s].type == 0)
-            collide_box(x, cols[s], s, largest, plane, shape);
-        else
-            collide_sphere(x, cols[s], s, largest, plane, shape);
+        switch (cols[s].type) {
+            case 0: collide_box(x, cols[s], s, largest, plane, shape); break;
+            case 1: collide_sphere(x, cols[s], s, largest, plane, shape); break;
+            case 2: collide_capsule(x, cols[s], s, largest, plane, shape); break;
+            default: collide_cylinder(x, cols[s], s, largest, plane, shape); break;
+        }
     }
     return shape;
 }
@@ -354,8 +423,18 @@ __device__ inline int colliding_shapes(const StepParams &p, const BodyDesc &d, c
     for (uint32_t ci = 0; ci < p.num_colliders; ++ci) {
         const ColliderDev c = p.colliders[ci];
         f3 cp = ld3(c.position);
-        f3 ext = c.type == 0 ? ld3(c.half_extent) : mk(c.radius, c.radius, c.radius);
-        f3 cmin = cp + neg(ext), cmax = cp + ext;
+        // world bounds of the shape (Shape::GetWorldSpaceBounds; CapsuleShape.cpp:266-276 for a capsule)
+        f3 cmin, cmax;
+        if (c.type == 2) {
+            const f3 rr = mk(c.radius, c.radius, c.radius);
+            cmin = mk(cp.x, cp.y - c.half_extent[1], cp.z) - rr;
+            cmax = mk(cp.x, cp.y + c.half_extent[1], cp.z) + rr;
+        } else {
+            const f3 ext = c.type == 0 ? ld3(c.half_extent)
+                                       : (c.type == 1 ? mk(c.radius, c.radius, c.radius) : mk(c.radius, c.half_extent[1], c.radius));
+            cmin = cp + neg(ext);
+            cmax = cp + ext;
+        }
         bool overlap = !(wmin.x > cmax.x || wmin.y > cmax.y || wmin.z > cmax.z || wmax.x < cmin.x || wmax.y < cmin.y ||
                          wmax.z < cmin.z);
         if (!overlap) continue;

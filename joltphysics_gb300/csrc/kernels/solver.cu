@@ -835,6 +835,9 @@ extern "C" jsb_status jsb_step_body_noalloc(const void *settings_blob, size_t le
                                                  "allow_sleeping = 0, or step it in a context");
     if (num_colliders > kMaxColliders)
         return report_error(JSB_ERR_CAPACITY, "jsb_step_body_noalloc takes at most " + std::to_string(kMaxColliders) + " colliders");
+    for (uint32_t i = 0; i < num_colliders; ++i)
+        if (colliders[i].type < JSB_COLLIDER_BOX || colliders[i].type > JSB_COLLIDER_CYLINDER)
+            return report_error(JSB_ERR_INVALID_ARGUMENT, "unknown collider type");
 
     // Host side: parse the settings and build the padded dependency-level schedule.
     ParsedSettings ps;

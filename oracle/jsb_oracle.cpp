@@ -37,6 +37,7 @@
 #include <atomic>
 #include <cfloat>
 #include <cmath>
+#include <limits>
 #include <condition_variable>
 #include <cstdint>
 #include <cstring>
@@ -422,9 +423,19 @@ public:
             for (size_t ci = 0; ci < colliders.size(); ++ci) {
                 const Collider &c = colliders[ci];
                 V3<R> cp = {R(c.pos[0]), R(c.pos[1]), R(c.pos[2])};
-                V3<R> ext = c.type == 0 ? V3<R>{R(c.half[0]), R(c.half[1]), R(c.half[2])}
-                                        : V3<R>{R(c.radius), R(c.radius), R(c.radius)};
-                V3<R> cmin = add(cp, neg(ext)), cmax = add(cp, ext);
+                // world bounds of the shape (Shape::GetWorldSpaceBounds; CapsuleShape.cpp:266-276)
+                V3<R> cmin, cmax;
+                if (c.type == 2) {
+                    V3<R> rr = {R(c.radius), R(c.radius), R(c.radius)};
+                    cmin = sub(V3<R>{cp.x, cp.y - R(c.half[1]), cp.z}, rr);
+                    cmax = add(V3<R>{cp.x, cp.y + R(c.half[1]), cp.z}, rr);
+                } else {
+                    V3<R> ext = c.type == 0   ? V3<R>{R(c.half[0]), R(c.half[1]), R(c.half[2])}
+                                : c.type == 1 ? V3<R>{R(c.radius), R(c.radius), R(c.radius)}
+                                              : V3<R>{R(c.radius), R(c.half[1]), R(c.radius)};
+                    cmin = add(cp, neg(ext));
+                    cmax = add(cp, ext);
+                }
                 bool overlap = !(wmin.x > cmax.x || wmin.y > cmax.y || wmin.z > cmax.z || wmax.x < cmin.x || wmax.y < cmin.y ||
                                  wmax.z < cmin.z);
                 if (!overlap) continue;
@@ -450,8 +461,12 @@ public:
                 if (!(v.inv_mass > R(0))) continue;
                 if (c.type == 0)
                     collide_box(v, c, t, int(si));
-                else
+                else if (c.type == 1)
                     collide_sphere(v, c, t, int(si));
+                else if (c.type == 2)
+                    collide_capsule(v, c, t, int(si));
+                else
+                    collide_cylinder(v, c, t, int(si));
             }
         }
 
@@ -540,6 +555,61 @@ public:
         v.plane_n = normal;
         v.plane_c = -dot(normal, point);
         v.shape_idx = idx;
+    }
+
+    // CapsuleShape.cpp:324-374: along Y, half[1] = half height of the cylinder part
+    void collide_capsule(Vertex<R> &v, const Collider &c, V3<R> t, int idx) {
+        const V3<R> local = add(v.pos, neg(t));
+        const R hh = R(c.half[1]), r = R(c.radius);
+        if (std::abs(local.y) <= hh) {
+            V3<R> normal = {local.x, R(0), local.z};
+            const R nl = len(normal);
+            const R pen = r - nl;
+            if (v.largest_pen >= pen) return;
+            v.largest_pen = pen;
+            normal = nl > R(0) ? divs(normal, nl) : V3<R>{R(1), R(0), R(0)};
+            set_plane_transformed(v, normal, mul(r, normal), t, idx);
+        } else {
+            const V3<R> center = {R(0), (local.y < R(0) ? R(-1) : R(1)) * hh, R(0)};
+            const V3<R> delta = sub(local, center);
+            const R distance = len(delta);
+            const R pen = r - distance;
+            if (v.largest_pen >= pen) return;
+            v.largest_pen = pen;
+            const V3<R> normal = divs(delta, distance);
+            set_plane_transformed(v, normal, add(center, mul(r, normal)), t, idx);
+        }
+    }
+
+    // CylinderShape.cpp:317-368: along Y, half[1] = half height
+    void collide_cylinder(Vertex<R> &v, const Collider &c, V3<R> t, int idx) {
+        const V3<R> local = add(v.pos, neg(t));
+        const R hh = R(c.half[1]), r = R(c.radius);
+        const V3<R> side = {local.x, R(0), local.z};
+        const R side_len = len(side);
+        const R side_pen = r - side_len;
+        const R top_pen = hh - std::abs(local.y);
+        const R sgn = local.y < R(0) ? R(-1) : R(1);
+        V3<R> point, normal;
+        if (side_pen < R(0) && top_pen < R(0)) {
+            point = add(mul(side, r / side_len), V3<R>{R(0), hh * sgn, R(0)});
+            const V3<R> d = sub(local, point);
+            const R px = d.x * d.x, py = d.y * d.y, pz = d.z * d.z;
+            const R lsq = (px + py) + pz;  // Vec3::NormalizedOr (Vec3.inl:978-998)
+            const R tiny = R(std::numeric_limits<float>::min());
+            normal = lsq <= tiny ? V3<R>{R(0), R(1), R(0)} : divs(d, std::sqrt(lsq));
+        } else if (side_pen < top_pen) {
+            normal = side_len > R(0) ? divs(side, side_len) : V3<R>{R(1), R(0), R(0)};
+            point = mul(r, normal);
+        } else {
+            normal = {R(0), sgn, R(0)};
+            point = mul(hh, normal);
+        }
+        const R cst = -dot(normal, point);
+        const R pen = -(dot(local, normal) + cst);
+        if (v.largest_pen >= pen) return;
+        v.largest_pen = pen;
+        set_plane_transformed(v, normal, point, t, idx);
     }
 
     void apply_pressure(Body<R> &b, R dt) {  // :291-323

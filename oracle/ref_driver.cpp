@@ -30,6 +30,8 @@
 #include <Jolt/Physics/PhysicsSystem.h>
 #include <Jolt/Physics/StateRecorderImpl.h>
 #include <Jolt/Physics/Collision/Shape/BoxShape.h>
+#include <Jolt/Physics/Collision/Shape/CapsuleShape.h>
+#include <Jolt/Physics/Collision/Shape/CylinderShape.h>
 #include <Jolt/Physics/Collision/Shape/SphereShape.h>
 #include <Jolt/Physics/Body/BodyCreationSettings.h>
 #include <Jolt/Physics/SoftBody/SoftBodySharedSettings.h>
@@ -177,8 +179,12 @@ int main(int argc, char **argv) {
             RefConst<Shape> shape;
             if (c.type == jsb::scene::ColliderType::Box)
                 shape = new BoxShape(Vec3(c.half_extent[0], c.half_extent[1], c.half_extent[2]));
-            else
+            else if (c.type == jsb::scene::ColliderType::Sphere)
                 shape = new SphereShape(c.radius);
+            else if (c.type == jsb::scene::ColliderType::Capsule)
+                shape = new CapsuleShape(c.half_extent[1], c.radius);
+            else
+                shape = new CylinderShape(c.half_extent[1], c.radius);
             BodyCreationSettings bcs(shape, RVec3(c.position[0], c.position[1], c.position[2]), Quat::sIdentity(), EMotionType::Static,
                                      Layers::NON_MOVING);
             bcs.mFriction = c.friction;

@@ -40,6 +40,8 @@ CASES = {
     "diff_cloth_16": ("diff_cloth", dict(n=16, steps=40), [1, 40]),
     "diff_batch_small": ("diff_batch", dict(n_cloth=4, n_cube=2, steps=30), [1, 30]),
     # sleeping allowed: bodies that come to rest on the floor fall asleep and stop being stepped
+    # every static shape type: capsule, cylinders, sphere, box floor
+    "shapes_drop": ("shapes_drop", {}, [1, 40, 80, 150]),
     "sleep_small": ("uneven_batch", dict(n_cloth=6, n_cube=3, cloth_max=20, cube_max=5, steps=200, sleep=1), [1, 60, 120, 160, 200]),
 }
 

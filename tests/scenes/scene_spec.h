@@ -112,13 +112,13 @@ struct BodySpec {
     float force[3] = {0, 0, 0};  // added with AddForce before every step
 };
 
-enum class ColliderType : int { Box = 0, Sphere = 1 };
+enum class ColliderType : int { Box = 0, Sphere = 1, Capsule = 2, Cylinder = 3 };
 
-struct ColliderSpec {  // a static rigid body with one convex shape
+struct ColliderSpec {  // a static rigid body with one convex shape (capsules and cylinders along Y)
     ColliderType type = ColliderType::Box;
     float position[3] = {0, 0, 0};
-    float half_extent[3] = {1, 1, 1};  // box
-    float radius = 1.0f;               // sphere
+    float half_extent[3] = {1, 1, 1};  // box; [1]: half height of a capsule's cylinder part / a cylinder
+    float radius = 1.0f;               // sphere, capsule, cylinder
     float friction = 0.2f;
     float restitution = 0.0f;
 };
@@ -465,6 +465,61 @@ inline SceneSpec make_diff_batch(uint64_t seed = 5, uint32_t n_cloth = 192, uint
     sphere.radius = 0.5f;
     sphere.position[1] = 0.5f;
     s.colliders.push_back(sphere);
+    s.num_steps = steps;
+    return s;
+}
+
+// Bodies dropped onto every static shape type: a box floor (top at y = 0) and, standing on it, a
+// capsule (radius 0.4, cylinder half height 0.5), a cylinder (radius 0.5, half height 0.4), a flat
+// cylinder (radius 0.8, half height 0.1) and a sphere (radius 0.5), 3 m apart along X. Over each shape a
+// 16 x 16 cloth (0.08 m spacing, dihedral bends, unpinned) and a 4-cell 5-tet cube of 0.12 m cells
+// (pressure 0 or 300 in turn), both offset by a seeded U[-0.3, 0.3] m in X and Z, so that they land on
+// the cap, rim, side and top faces; 5 iterations, `steps` steps of 1/60 s.
+inline SceneSpec make_shapes_drop(uint64_t seed = 7, int steps = 150) {
+    SceneSpec s;
+    Rng rng(seed);
+    struct Stand {
+        ColliderType type;
+        float radius, half_height, top;
+    };
+    const Stand stands[4] = {{ColliderType::Capsule, 0.4f, 0.5f, 1.8f},
+                             {ColliderType::Cylinder, 0.5f, 0.4f, 0.8f},
+                             {ColliderType::Cylinder, 0.8f, 0.1f, 0.2f},
+                             {ColliderType::Sphere, 0.5f, 0.0f, 1.0f}};
+    for (int k = 0; k < 4; ++k) {
+        const float x = -4.5f + 3.0f * float(k);
+        ColliderSpec c;
+        c.type = stands[k].type;
+        c.radius = stands[k].radius;
+        c.half_extent[1] = stands[k].half_height;
+        c.position[0] = x;
+        c.position[1] = 0.5f * stands[k].top;
+        c.friction = 0.4f;
+        c.restitution = 0.1f;
+        s.colliders.push_back(c);
+        BodySpec cloth;
+        cloth.mesh = make_cloth(16, 16, 0.08f, [](uint32_t, uint32_t) { return false; });
+        cloth.mesh.attributes = VertexAttributes{1.0e-5f, 1.0e-5f, 1.0e-4f};
+        cloth.mesh.bend_type = BendType::Dihedral;
+        cloth.position[0] = x + float(rng.uniform() * 0.6 - 0.3);
+        cloth.position[1] = stands[k].top + 0.6f;
+        cloth.position[2] = float(rng.uniform() * 0.6 - 0.3);
+        s.bodies.push_back(cloth);
+        BodySpec cube;
+        cube.mesh = make_tet_cube(4, 0.12f, 0.0f, 1.0e-6f);
+        cube.creation.pressure = (k & 1) ? 300.0f : 0.0f;
+        cube.position[0] = x + float(rng.uniform() * 0.6 - 0.3);
+        cube.position[1] = stands[k].top + 1.6f;
+        cube.position[2] = float(rng.uniform() * 0.6 - 0.3);
+        s.bodies.push_back(cube);
+    }
+    ColliderSpec floor;
+    floor.type = ColliderType::Box;
+    floor.half_extent[0] = 10.0f;
+    floor.half_extent[1] = 1.0f;
+    floor.half_extent[2] = 10.0f;
+    floor.position[1] = -1.0f;
+    s.colliders.push_back(floor);
     s.num_steps = steps;
     return s;
 }

@@ -15,7 +15,7 @@ from scenes import build_scene
 
 pytestmark = pytest.mark.gpu
 
-GOLDEN = ["pinned_cloth", "uneven_small", "large_cloth_32", "diff_cloth_16", "diff_batch_small", "sleep_small"]
+GOLDEN = ["pinned_cloth", "uneven_small", "large_cloth_32", "diff_cloth_16", "diff_batch_small", "sleep_small", "shapes_drop"]
 
 
 def split(arr, nv):

@@ -10,7 +10,7 @@ import pytest
 from conftest import golden_path
 from jsb_testlib import parse_scene
 
-CASES = ["pinned_cloth", "uneven_small", "large_cloth_32", "diff_cloth_16", "diff_batch_small", "sleep_small"]
+CASES = ["pinned_cloth", "uneven_small", "large_cloth_32", "diff_cloth_16", "diff_batch_small", "sleep_small", "shapes_drop"]
 
 
 def load(name):

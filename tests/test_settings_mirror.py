@@ -13,6 +13,7 @@ CASES = {
     "diff_cloth_16": ("diff_cloth", dict(n=16, steps=40)),
     "diff_batch_small": ("diff_batch", dict(n_cloth=4, n_cube=2, steps=30)),
     "sleep_small": ("uneven_batch", dict(n_cloth=6, n_cube=3, cloth_max=20, cube_max=5, steps=200, sleep=1)),
+    "shapes_drop": ("shapes_drop", {}),
 }
 
 

@@ -83,6 +83,8 @@ def _planes(scene: Scene, m: BodyModel, x, v, P, bounds, dt):
         wmin, wmax = P + lmin - m.radius, P + lmax + m.radius
         s = 0
         for c in scene.colliders:
+            if c.type not in (0, 1):
+                raise NotImplementedError("the FP64 reference models box and sphere colliders only")
             cp = np.asarray(c.position, np.float64)
             ext = np.asarray(c.half_extent if c.type == 0 else (c.radius,) * 3, np.float64)
             if np.any(wmin > cp + ext) or np.any(wmax < cp - ext):
