@@ -342,15 +342,15 @@ def gradient_checks(jsb) -> dict:
     own trajectory (bar 1e-3) and, for reference only, free-running FP64 central differences on 32
     parameters (the cloth is chaotic over 120 steps); the same cloth over 6 steps against FP64 central
     differences (bar 5e-2); the 256-body batch (90 steps, centre-of-mass loss) against FP64 autodiff of
-    its smallest cloth along the GPU's own trajectory (bar 1e-3) and FP64 central differences of each
-    perturbed body, its collision decisions replayed, on 16 (body, axis) parameters (bar 1e-3 on those
-    whose finite difference is the same with steps eps and 4 eps)."""
+    its two smallest cloths and smallest cube along the GPU's own trajectory (bar 1e-3) and FP64 central
+    differences of each perturbed body, the GPU run's collision decisions replayed, on 16 (body, axis)
+    parameters (bar 1e-3 on the conditioned ones, see tests/gradcheck.py)."""
     from gradcheck import diff_batch_check, diff_cloth_check
 
     t0 = time.perf_counter()
     out = {"diff_cloth": diff_cloth_check(jsb, build_scene),
            "diff_cloth_6_steps": diff_cloth_check(jsb, build_scene, steps=6, every=2, loss_steps=(3, 6), pinned=False),
-           "diff_batch": diff_batch_check(jsb, build_scene, n_params=16, pinned_counts=(1, 0))}
+           "diff_batch": diff_batch_check(jsb, build_scene, n_params=16)}
     out["diff_batch"].pop("not_smooth", None)
     out["diff_batch"].pop("rows", None)
     out["seconds"] = time.perf_counter() - t0

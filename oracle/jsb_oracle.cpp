@@ -848,6 +848,8 @@ public:
 
 struct Handle {
     int use_double;
+    double noise = 0.0;
+    uint64_t noise_seed = 0, noise_step = 0;
     World<float> wf;
     World<double> wd;
     std::string err;
@@ -935,10 +937,38 @@ float oracle_body_sleep_timer(void *w, int body) { return static_cast<Handle *>(
 
 int oracle_step(void *w, float dt, int collision_steps) {
     Handle *h = static_cast<Handle *>(w);
-    if (h->use_double)
+    if (h->use_double) {
         h->wd.step(double(dt), collision_steps);
-    else
+        if (h->noise > 0.0) {  // a conditioning probe: a fixed relative perturbation of the state after every step
+            ++h->noise_step;
+            for (size_t bi = 0; bi < h->wd.bodies.size(); ++bi)
+                for (size_t i = 0; i < h->wd.bodies[bi].v.size(); ++i) {
+                    Vertex<double> &v = h->wd.bodies[bi].v[i];
+                    double *c[6] = {&v.pos.x, &v.pos.y, &v.pos.z, &v.vel.x, &v.vel.y, &v.vel.z};
+                    for (int k = 0; k < 6; ++k) {
+                        // splitmix64 of (seed, step, body, vertex, component) -> U(-1, 1)
+                        uint64_t z = h->noise_seed + 0x9e3779b97f4a7c15ull * (((h->noise_step * 1024 + bi) * 65536 + i) * 8 + k + 1);
+                        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+                        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+                        z ^= z >> 31;
+                        const double u = double(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+                        *c[k] += h->noise * std::abs(*c[k]) * u;
+                    }
+                }
+        }
+    } else {
         h->wf.step(dt, collision_steps);
+    }
+    return 0;
+}
+
+// Conditioning probe of double runs: after every step each position and velocity component x becomes
+// x (1 + relative u) with u ~ U(-1, 1) fixed by (seed, step, body, vertex, component).
+int oracle_set_noise(void *w, double relative, uint64_t seed) {
+    Handle *h = static_cast<Handle *>(w);
+    h->noise = relative;
+    h->noise_seed = seed;
+    h->noise_step = 0;
     return 0;
 }
 
@@ -1038,12 +1068,34 @@ int oracle_set_freeze(void *w, int mode) {
 }
 
 // Copies every body's recorded decisions from world src to world dst (same scene) and rewinds them.
+// The decisions of a float run, widened to double (a double run that replays a float run's collision
+// decisions and planes).
+static Body<double>::Decisions widen(const Body<float>::Decisions &f) {
+    Body<double>::Decisions d;
+    d.shape_collider = f.shape_collider;
+    d.shape_friction.assign(f.shape_friction.begin(), f.shape_friction.end());
+    d.shape_restitution.assign(f.shape_restitution.begin(), f.shape_restitution.end());
+    d.vertex_shape = f.vertex_shape;
+    for (const V3<float> &n : f.vertex_n) d.vertex_n.push_back({double(n.x), double(n.y), double(n.z)});
+    d.vertex_c.assign(f.vertex_c.begin(), f.vertex_c.end());
+    d.flags = f.flags;
+    d.vclamp = f.vclamp;
+    return d;
+}
+
+// Copies the recorded decisions of `src` into `dst` for replay. A float oracle's (use_double = 0)
+// decisions also become the double world's, widened.
 int oracle_copy_decisions(void *dst, const void *src) {
     Handle *d = static_cast<Handle *>(dst);
     const Handle *s = static_cast<const Handle *>(src);
     if (d->wd.bodies.size() != s->wd.bodies.size()) return -1;
     for (size_t i = 0; i < d->wd.bodies.size(); ++i) {
-        d->wd.bodies[i].decisions = s->wd.bodies[i].decisions;
+        if (s->use_double) {
+            d->wd.bodies[i].decisions = s->wd.bodies[i].decisions;
+        } else {
+            d->wd.bodies[i].decisions.clear();
+            for (const auto &f : s->wf.bodies[i].decisions) d->wd.bodies[i].decisions.push_back(widen(f));
+        }
         d->wd.bodies[i].decision_step = 0;
         d->wf.bodies[i].decisions = s->wf.bodies[i].decisions;
         d->wf.bodies[i].decision_step = 0;

@@ -204,6 +204,7 @@ class Oracle:
             L.oracle_set_sleep_settings.argtypes = [ctypes.c_void_p, ctypes.c_float, ctypes.c_float]
             L.oracle_set_freeze.argtypes = [ctypes.c_void_p, ctypes.c_int]
             L.oracle_copy_decisions.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+            L.oracle_set_noise.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64]
             L.oracle_last_error.restype = ctypes.c_char_p
             L.oracle_last_error.argtypes = [ctypes.c_void_p]
             cls._lib = L
@@ -333,18 +334,25 @@ class FD64:
                 total += float((np.asarray(r, np.float64) * w).sum())
         return total
 
+    def record_f32(self):
+        """Float run of the base parameters with every collision decision recorded: the GPU's own decisions
+        (the float oracle is bitwise equal to the GPU)."""
+        o = Oracle(self.scene)
+        Oracle.lib().oracle_set_freeze(o.h, 1)
+        o.step(self.steps)
+        return o
+
     def central(self, body: int, kind: str, index: tuple, eps: float, frozen: bool = False) -> float:
         """Central difference of the loss in one parameter component; frozen: the perturbed runs replay the
-        base run's collision decisions (planes, contacts, friction clamps, restitution, velocity clamp)."""
+        collision decisions (planes, contacts, friction clamps, restitution, velocity clamp) of the base
+        parameters' float run, i.e. of the GPU's run."""
         base = self.base_params(body)[kind]
-        rec = []
-        if frozen:
-            self.loss({}, record=rec)
+        rec = self.record_f32() if frozen else None
         vals = []
         for sgn in (1.0, -1.0):
             p = base.copy()
             p[index] += sgn * eps
-            vals.append(self.loss({body: {kind: p}}, replay=rec[0] if rec else None))
+            vals.append(self.loss({body: {kind: p}}, replay=rec))
         return (vals[0] - vals[1]) / (2.0 * eps)
 
     def base_params(self, body: int) -> dict:
@@ -361,16 +369,19 @@ def single_body_scene(scene: Scene, b: int) -> Scene:
 
 
 def run64(scene: Scene, b: int, steps: int, observe, x0=None, v0=None, edge=None, volume=None, force=None,
-          record=None, replay=None) -> dict:
+          record=None, replay=None, noise=0.0) -> dict:
     """FP64 oracle run of body b alone (optionally with its initial local positions / velocities, edge /
     volume compliance or step force replaced); world positions (N, 3) after each step in `observe`.
     record: a list that receives the run's oracle with every collision decision recorded; replay: such an
     oracle, whose decisions this run takes instead of deciding again (the collision active set frozen,
-    as the adjoint differentiates it)."""
+    as the adjoint differentiates it). noise: relative size of a fixed perturbation of the state after every
+    step (the same in every run), a probe of how much the gradient depends on the trajectory."""
     sc = single_body_scene(scene, b)
     body = sc.bodies[0]
     L = Oracle.lib()
     o = Oracle(sc, use_double=True)
+    if noise:
+        L.oracle_set_noise(o.h, float(noise), 12345)
     if record is not None:
         L.oracle_set_freeze(o.h, 1)
         record.append(o)
@@ -397,6 +408,17 @@ def run64(scene: Scene, b: int, steps: int, observe, x0=None, v0=None, edge=None
             L.oracle_get_world_f64(o.h, 0, w.ctypes.data)
             out[s] = w
     return out
+
+
+def record32(scene: Scene, b: int, steps: int):
+    """Float oracle run of body b alone over `steps` steps with its scene force, recording every collision
+    decision: the decisions of the GPU's own (bitwise equal) run, for FP64 runs to replay."""
+    sc = single_body_scene(scene, b)
+    L = Oracle.lib()
+    o = Oracle(sc)
+    L.oracle_set_freeze(o.h, 1)
+    o.step(steps)
+    return o
 
 
 def blob_counts_py(blob: bytes) -> dict:
