@@ -82,6 +82,32 @@ struct BodyDesc {
     uint32_t flags;
 };
 
+enum : int32_t { kMotionStatic = 0, kMotionKinematic = 1, kMotionDynamic = 2 };  // EMotionType
+
+// A colliding shape of one body determined on the host (jsb_colliding_shape as uploaded): the fields of
+// SoftBodyMotionProperties::CollidingShape and its LeafShape that the step reads.
+struct ShapeEntry {
+    int32_t type, motion;
+    float xf[12];  // leaf transform relative to the soft body: rotation columns 0-2, then translation
+    float half_extent[3], radius, friction, restitution;
+    float inv_mass_scale;   // mSoftBodyInvMassScale
+    float inv_mass;         // dynamic: mInvMass
+    float inv_inertia[12];  // dynamic: mInvInertia, columns 0-3
+    float com[3];           // mCenterOfMassTransform translation
+    float lin[3], ang[3];   // dynamic: velocities at the start of the step (soft-body space)
+};
+
+// Per body with host-determined colliding shapes: the shapes, and after a step the dynamic shapes'
+// velocities (mLinearVelocity / mAngularVelocity) and which of them a contact changed (mUpdateVelocities).
+struct ShapeTable {
+    uint32_t count;
+    uint32_t updated;  // bit s: shape s
+    uint32_t pad[2];
+    ShapeEntry e[kMaxCollidingShapes];
+    float lin[kMaxCollidingShapes][4];
+    float ang[kMaxCollidingShapes][4];
+};
+
 struct BodyState {
     float position[3];  // body position in world space
     float bmin[3], bmax[3];  // local bounds
@@ -146,6 +172,9 @@ struct StepParams {
     uint32_t ring_slots;  // record slots per schedule-ring half (>= every launched body's stage_half)
     const TapeDesc *tape;  // per-body tapes (taped forward only)
     uint32_t tape_step;    // step index within the checkpoint segment (taped forward only)
+    ShapeTable *tables;        // host-determined colliding shapes (null: none)
+    const int32_t *table_slot; // per body: index into tables, -1 = the context's colliders
+    int32_t *dyn_list;         // per vertex (context indexing): scratch for the vertices touching dynamic shapes
     BodySleep *sleep;      // per body (null: bodies never sleep)
     float sleep_velocity_threshold;  // PhysicsSettings::mPointVelocitySleepThreshold (compared with |v|^2)
     float time_before_sleep;         // PhysicsSettings::mTimeBeforeSleep

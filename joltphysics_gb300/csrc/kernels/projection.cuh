@@ -20,12 +20,17 @@ __device__ __forceinline__ void stx(float4 *sx, uint32_t i, float4 v) { sx[i] = 
 
 struct SCol {  // one colliding shape, relative to the soft body
     int32_t type;
+    int32_t flags;  // kColRotated: transform in c / ic / it (host-determined shapes); kColDynamic
     float t[3];
     float h[3];
     float r;
     float friction;
     float restitution;
+    float isc;           // mSoftBodyInvMassScale
+    float c[9];          // rotation columns
+    float ic[9], it[3];  // inverse transform (Mat44::InversedRotationTranslation): rotation columns, translation
 };
+enum : int32_t { kColRotated = 1, kColDynamic = 2 };
 
 // NaN positions (a body that has blown up in the reference's own arithmetic) would send every division
 // and square root of a projection down the IEEE routines' slow path. For a body holding NaN positions
@@ -240,10 +245,40 @@ __device__ __forceinline__ float4 plane_transformed(f3 normal, f3 point, f3 t) {
     return make_float4(n2.x, n2.y, n2.z, c - dot(t, n2));
 }
 
+// Mat44 * Vec3 with columns c0..c2 and translation t (Jolt/Math/Mat44.inl:295-302): ((c0 x + c1 y) + c2 z) + t.
+__device__ __forceinline__ f3 mat_mul(const float *c, f3 v, f3 t) {
+    return mk(((c[0] * v.x + c[3] * v.y) + c[6] * v.z) + t.x, ((c[1] * v.x + c[4] * v.y) + c[7] * v.z) + t.y,
+              ((c[2] * v.x + c[5] * v.y) + c[8] * v.z) + t.z);
+}
+// Mat44::Multiply3x3 (Mat44.inl:384-390): (c0 x + c1 y) + c2 z.
+__device__ __forceinline__ f3 mat_mul3(const float *c, f3 v) {
+    return mk((c[0] * v.x + c[3] * v.y) + c[6] * v.z, (c[1] * v.x + c[4] * v.y) + c[7] * v.z, (c[2] * v.x + c[5] * v.y) + c[8] * v.z);
+}
+
+// Transform of a colliding shape relative to the soft body. XformT: a translation only (shapes the GPU
+// finds among the context's colliders); XformR: a full rotation + translation (host-determined shapes),
+// the shape's CollideSoftBodyVertices mapping the vertex with InversedRotationTranslation() and its
+// plane back with Plane::GetTransformed (Jolt/Geometry/Plane.h:42-46).
+struct XformT {
+    f3 t;
+    __device__ __forceinline__ f3 local(f3 p) const { return p + neg(t); }
+    __device__ __forceinline__ float4 plane(f3 normal, f3 point) const { return plane_transformed(normal, point, t); }
+};
+struct XformR {
+    const SCol &s;
+    __device__ __forceinline__ f3 local(f3 p) const { return mat_mul(s.ic, p, ld3(s.it)); }
+    __device__ __forceinline__ float4 plane(f3 normal, f3 point) const {
+        const float c = -dot(normal, point);
+        const f3 n2 = mat_mul3(s.c, normal);
+        return make_float4(n2.x, n2.y, n2.z, c - dot(ld3(s.t), n2));
+    }
+};
+
 // BoxShape::CollideSoftBodyVertices (BoxShape.cpp:234-283) for one vertex.
-__device__ __forceinline__ void collide_box(f3 p, const SCol &s, int idx, float &largest, float4 &plane, int &shape) {
-    f3 t = ld3(s.t), h = ld3(s.h);
-    f3 local = p + neg(t);
+template <class X>
+__device__ __forceinline__ void collide_box(f3 p, const SCol &s, const X &xf, int idx, float &largest, float4 &plane, int &shape) {
+    f3 h = ld3(s.h);
+    f3 local = xf.local(p);
     f3 clamped = vmax(vmin(local, h), neg(h));
     if (clamped.x == local.x && clamped.y == local.y && clamped.z == local.z) {
         f3 delta = h - mk(fabsf(local.x), fabsf(local.y), fabsf(local.z));
@@ -255,7 +290,7 @@ __device__ __forceinline__ void collide_box(f3 p, const SCol &s, int idx, float 
         f3 axis = mk(index == 0 ? 1.0f : 0.0f, index == 1 ? 1.0f : 0.0f, index == 2 ? 1.0f : 0.0f);
         f3 normal = mk(sgn.x * axis.x, sgn.y * axis.y, sgn.z * axis.z);
         f3 point = mk(normal.x * h.x, normal.y * h.y, normal.z * h.z);
-        plane = plane_transformed(normal, point, t);
+        plane = xf.plane(normal, point);
         shape = idx;
     } else {
         f3 normal = local - clamped;
@@ -264,12 +299,13 @@ __device__ __forceinline__ void collide_box(f3 p, const SCol &s, int idx, float 
         if (largest >= pen) return;
         largest = pen;
         normal = normal / nl;
-        plane = plane_transformed(normal, clamped, t);
+        plane = xf.plane(normal, clamped);
         shape = idx;
     }
 }
 
-// SphereShape::CollideSoftBodyVertices (SphereShape.cpp:279-300) for one vertex.
+// SphereShape::CollideSoftBodyVertices (SphereShape.cpp:279-300) for one vertex (the centre is the
+// transform's translation; the plane is already relative to the soft body).
 __device__ __forceinline__ void collide_sphere(f3 p, const SCol &s, int idx, float &largest, float4 &plane, int &shape) {
     f3 center = ld3(s.t);
     f3 delta = p - center;
@@ -284,11 +320,11 @@ __device__ __forceinline__ void collide_sphere(f3 p, const SCol &s, int idx, flo
 }
 
 // CapsuleShape::CollideSoftBodyVertices (CapsuleShape.cpp:324-374) for one vertex: a capsule along
-// the Y axis (identity rotation), h[1] = half height of its cylinder part, r = radius.
-__device__ __forceinline__ void collide_capsule(f3 p, const SCol &s, int idx, float &largest, float4 &plane, int &shape) {
-    const f3 t = ld3(s.t);
+// its Y axis, h[1] = half height of its cylinder part, r = radius.
+template <class X>
+__device__ __forceinline__ void collide_capsule(f3 p, const SCol &s, const X &xf, int idx, float &largest, float4 &plane, int &shape) {
     const float hh = s.h[1], r = s.r;
-    const f3 local = p + neg(t);
+    const f3 local = xf.local(p);
     if (fabsf(local.y) <= hh) {  // beside the cylinder part: radial normal
         f3 normal = mk(local.x, 0.0f, local.z);
         const float nl = len(normal);
@@ -296,7 +332,7 @@ __device__ __forceinline__ void collide_capsule(f3 p, const SCol &s, int idx, fl
         if (largest >= pen) return;
         largest = pen;
         normal = nl > 0.0f ? normal / nl : mk(1.0f, 0.0f, 0.0f);
-        plane = plane_transformed(normal, r * normal, t);
+        plane = xf.plane(normal, r * normal);
     } else {  // beyond an end: the cap's sphere
         const f3 center = mk(0.0f, (local.y < 0.0f ? -1.0f : 1.0f) * hh, 0.0f);
         const f3 delta = local - center;
@@ -305,7 +341,7 @@ __device__ __forceinline__ void collide_capsule(f3 p, const SCol &s, int idx, fl
         if (largest >= pen) return;
         largest = pen;
         const f3 normal = delta / distance;
-        plane = plane_transformed(normal, center + r * normal, t);
+        plane = xf.plane(normal, center + r * normal);
     }
     shape = idx;
 }
@@ -319,13 +355,13 @@ __device__ __forceinline__ f3 normalized_or(f3 v, f3 zero) {
     return v / jsqrt(len_sq);
 }
 
-// CylinderShape::CollideSoftBodyVertices (CylinderShape.cpp:317-368) for one vertex: a cylinder along the
-// Y axis (identity rotation), h[1] = half height, r = radius. The plane is that of the closest surface
-// (side, top / bottom, or the rim for a vertex outside both), its penetration measured from the plane.
-__device__ __forceinline__ void collide_cylinder(f3 p, const SCol &s, int idx, float &largest, float4 &plane, int &shape) {
-    const f3 t = ld3(s.t);
+// CylinderShape::CollideSoftBodyVertices (CylinderShape.cpp:317-368) for one vertex: a cylinder along its
+// Y axis, h[1] = half height, r = radius. The plane is that of the closest surface (side, top / bottom,
+// or the rim for a vertex outside both), its penetration measured from the plane.
+template <class X>
+__device__ __forceinline__ void collide_cylinder(f3 p, const SCol &s, const X &xf, int idx, float &largest, float4 &plane, int &shape) {
     const float hh = s.h[1], r = s.r;
-    const f3 local = p + neg(t);
+    const f3 local = xf.local(p);
     const f3 side = mk(local.x, 0.0f, local.z);
     const float side_len = len(side);
     const float side_pen = r - side_len;
@@ -346,8 +382,18 @@ __device__ __forceinline__ void collide_cylinder(f3 p, const SCol &s, int idx, f
     const float pen = -(dot(local, normal) + c);
     if (largest >= pen) return;
     largest = pen;
-    plane = plane_transformed(normal, point, t);
+    plane = xf.plane(normal, point);
     shape = idx;
+}
+
+template <class X>
+__device__ __forceinline__ void collide_shape(f3 x, const SCol &s, const X &xf, int idx, float &largest, float4 &plane, int &shape) {
+    switch (s.type) {
+        case 0: collide_box(x, s, xf, idx, largest, plane, shape); break;
+        case 1: collide_sphere(x, s, idx, largest, plane, shape); break;
+        case 2: collide_capsule(x, s, xf, idx, largest, plane, shape); break;
+        default: collide_cylinder(x, s, xf, idx, largest, plane, shape); break;
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -376,12 +422,10 @@ __device__ __forceinline__ int collision_plane(f3 x, const SCol *cols, int ncols
     int shape = -1;
     float largest = -FLT_MAX;
     for (int s = 0; s < ncols; ++s) {
-        switch (cols[s].type) {
-            case 0: collide_box(x, cols[s], s, largest, plane, shape); break;
-            case 1: collide_sphere(x, cols[s], s, largest, plane, shape); break;
-            case 2: collide_capsule(x, cols[s], s, largest, plane, shape); break;
-            default: collide_cylinder(x, cols[s], s, largest, plane, shape); break;
-        }
+        if (cols[s].flags & kColRotated)
+            collide_shape(x, cols[s], XformR{cols[s]}, s, largest, plane, shape);
+        else
+            collide_shape(x, cols[s], XformT{ld3(cols[s].t)}, s, largest, plane, shape);
     }
     return shape;
 }
@@ -396,17 +440,56 @@ __device__ __forceinline__ bool collide_vertex(f3 &x, f3 &v, f3 prev_v, float4 p
     float projected = -(dot(x, n) + pl.w) + radius;
     if (!(projected > 0.0f)) return false;
     x = x + n * projected;
+    if (!(cs.isc > 0.0f)) return true;  // the soft body is not moved by this shape (mSoftBodyInvMassScale = 0)
     f3 v_normal = n * dot(n, v);
     f3 v_tan = v - v_normal;
     float vtl = len(v_tan);
     if (vtl > 0.0f) {
         float fr = jdiv(cs.friction * projected, vtl * dt_sub);
-        fr = fr > 1.0f ? 1.0f : fr;
+        fr = fr < 1.0f ? fr : 1.0f;  // min(fr, 1)
         v = v - v_tan * fr;
     }
     v = v - v_normal;
     float pvn = dot(prev_v, n);
     if (pvn < restitution_threshold) v = v - (cs.restitution * pvn) * n;
+    return true;
+}
+
+// The dynamic-body branch of ApplyCollisionConstraintsAndUpdateVelocities (:752-797) for one vertex
+// whose collision plane belongs to a dynamic shape: pushes x out of the plane, then exchanges an impulse
+// between the vertex and the body (friction and restitution against the body's point velocity), updating
+// the body's velocities lin / ang in place, which the next vertex in index order sees. Returns whether an
+// impulse was applied (CollidingShape::mUpdateVelocities).
+__device__ __forceinline__ bool collide_vertex_dynamic(f3 &x, f3 &v, f3 prev_v, float w, float4 pl, const ShapeEntry &e, f3 &lin,
+                                                       f3 &ang, float radius, float dt_sub, float restitution_threshold) {
+    const f3 n = xyz(pl);
+    const float projected = -(dot(x, n) + pl.w) + radius;
+    if (!(projected > 0.0f)) return false;
+    x = x + n * projected;
+    const f3 r2 = x - ld3(e.com);
+    const f3 v2 = lin + cross(ang, r2);  // CollidingShape::GetPointVelocity
+    const f3 relative = v - v2;
+    const f3 v_normal = n * dot(n, relative);
+    const f3 v_tan = relative - v_normal;
+    const float vtl = len(v_tan);
+    const float vertex_inv_mass = e.inv_mass_scale * w;
+    const f3 r2xn = cross(r2, n);
+    const float w2 = e.inv_mass + dot(r2xn, mat_mul(e.inv_inertia, r2xn, ld3(e.inv_inertia + 9)));
+    const float w12 = vertex_inv_mass + w2;
+    if (!(w12 > 0.0f)) return false;
+    f3 dv = mk(0.0f, 0.0f, 0.0f);
+    if (vtl > 0.0f) {
+        float fr = jdiv(e.friction * projected, vtl * dt_sub);
+        fr = fr < 1.0f ? fr : 1.0f;
+        dv = v_tan * fr;
+    }
+    dv = dv + v_normal;
+    const float pvn = dot(prev_v - v2, n);
+    if (pvn < restitution_threshold) dv = dv + (e.restitution * pvn) * n;
+    const f3 imp = dv / w12;
+    v = v - imp * vertex_inv_mass;
+    lin = lin + imp * e.inv_mass;
+    ang = ang + mat_mul(e.inv_inertia, cross(r2, imp), ld3(e.inv_inertia + 9));
     return true;
 }
 
@@ -444,12 +527,47 @@ __device__ inline int colliding_shapes(const StepParams &p, const BodyDesc &d, c
         }
         SCol &s = cols[n++];
         s.type = c.type;
+        s.flags = 0;
+        s.isc = 1.0f;
         st3(s.t, cp - body_pos);
         st3(s.h, ld3(c.half_extent));
         s.r = c.radius;
         s.friction = sqrtf(d.friction * c.friction);
         s.restitution = d.restitution > c.restitution ? d.restitution : c.restitution;
     }
+    return n;
+}
+
+// Host-determined colliding shapes of a body (jsb_body_set_colliding_shapes) into `cols`, with the inverse
+// of each transform as Mat44::InversedRotationTranslation computes it (Mat44.inl): the transposed
+// rotation and -(R^T t) = 0 - ((c0' t.x + c1' t.y) + c2' t.z). Resets the table's output velocities to the
+// input ones. Returns the count; `dynamic` tells whether a dynamic shape is among them.
+__device__ inline int load_shape_table(ShapeTable *tb, SCol *cols, bool &dynamic) {
+    const int n = int(tb->count < kMaxCollidingShapes ? tb->count : kMaxCollidingShapes);
+    dynamic = false;
+    for (int k = 0; k < n; ++k) {
+        const ShapeEntry &e = tb->e[k];
+        SCol &s = cols[k];
+        s.type = e.type;
+        s.flags = kColRotated | (e.motion == kMotionDynamic ? kColDynamic : 0);
+        dynamic = dynamic || e.motion == kMotionDynamic;
+        for (int j = 0; j < 9; ++j) s.c[j] = e.xf[j];
+        for (int col = 0; col < 3; ++col)
+            for (int row = 0; row < 3; ++row) s.ic[3 * col + row] = e.xf[3 * row + col];
+        const f3 t = mk(e.xf[9], e.xf[10], e.xf[11]);
+        st3(s.t, t);
+        st3(s.it, neg(mat_mul3(s.ic, t)));
+        st3(s.h, ld3(e.half_extent));
+        s.r = e.radius;
+        s.friction = e.friction;
+        s.restitution = e.restitution;
+        s.isc = e.inv_mass_scale;
+        for (int j = 0; j < 3; ++j) {
+            tb->lin[k][j] = e.lin[j];
+            tb->ang[k][j] = e.ang[j];
+        }
+    }
+    tb->updated = 0;
     return n;
 }
 

@@ -34,6 +34,7 @@
 // Build: g++ -O2 -std=c++17 -ffp-contract=off -fPIC -shared oracle/jsb_oracle.cpp -o oracle/liboracle.so
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cfloat>
 #include <cmath>
@@ -250,6 +251,17 @@ struct Collider {
     float friction, restitution;
 };
 
+// A colliding shape determined on the host for one body and step (the layout of jsb_colliding_shape):
+// the fields of SoftBodyMotionProperties::CollidingShape and its LeafShape the step reads.
+struct TableShapeIn {  // 172 bytes
+    int32_t type, motion;  // motion: EMotionType (2 = dynamic)
+    float xf[12];          // leaf transform: rotation columns 0-2, translation
+    float half_extent[3], radius, friction, restitution;
+    float inv_mass_scale, inv_mass;
+    float inv_inertia[12];  // columns 0-3
+    float com[3], lin[3], ang[3];
+};
+
 struct Creation {
     uint32_t num_iterations;
     float linear_damping, max_linear_velocity, restitution, friction, pressure, gravity_factor, vertex_radius;
@@ -292,14 +304,41 @@ struct Body {
     };
     std::vector<Decisions> decisions;
     size_t decision_step = 0;
+    // host-determined colliding shapes (used instead of the world's colliders when has_table), and
+    // after a step each shape's {updated, linear velocity, angular velocity}
+    bool has_table = false;
+    std::vector<TableShapeIn> table;
+    std::vector<std::array<float, 7>> table_out;
 };
 
 template <class R>
 struct CollidingShape {
-    int collider;
-    V3<R> t;  // translation relative to the soft body (identity rotation)
+    int collider = -1;  // world collider index (-1: host-determined)
+    int type = 0;
+    V3<R> t;  // translation relative to the soft body
+    V3<R> h;  // half extent (capsule / cylinder: h.y = half height)
+    R r = R(0);
     R friction, restitution;
+    R isc = R(1);  // mSoftBodyInvMassScale
+    bool rotated = false, dynamic = false;
+    V3<R> c[3], ic[3], it;  // rotation columns; Mat44::InversedRotationTranslation columns and translation
+    R inv_mass = R(0);
+    V3<R> inertia[4];  // mInvInertia columns 0-3
+    V3<R> com, lin, ang;
+    bool updated = false;
 };
+
+// Mat44 * Vec3 (Mat44.inl:295-302) and Mat44::Multiply3x3 (:384-390) over columns
+template <class R>
+inline V3<R> mat3(const V3<R> c[3], V3<R> v) {
+    return {(c[0].x * v.x + c[1].x * v.y) + c[2].x * v.z, (c[0].y * v.x + c[1].y * v.y) + c[2].y * v.z,
+            (c[0].z * v.x + c[1].z * v.y) + c[2].z * v.z};
+}
+template <class R>
+inline V3<R> mat4(const V3<R> c[3], V3<R> t, V3<R> v) {
+    V3<R> m = mat3(c, v);
+    return {m.x + t.x, m.y + t.y, m.z + t.z};
+}
 
 template <class R>
 class World {
@@ -408,13 +447,16 @@ public:
                 CollidingShape<R> cs;
                 cs.collider = dec->shape_collider[k];
                 const Collider &c = colliders[size_t(cs.collider)];
+                set_shape_geometry(cs, c);
                 cs.t = sub(V3<R>{R(c.pos[0]), R(c.pos[1]), R(c.pos[2])}, b.position);
                 cs.friction = dec->shape_friction[k];
                 cs.restitution = dec->shape_restitution[k];
                 shapes.push_back(cs);
             }
         }
-        if (freeze_mode != 2) {
+        if (b.has_table) {
+            shapes_from_table(b, shapes);
+        } else if (freeze_mode != 2) {
             V3<R> lmin = vmin(b.bmin, b.pmin), lmax = vmax(b.bmax, b.pmax);
             V3<R> r3 = {R(b.cs.vertex_radius), R(b.cs.vertex_radius), R(b.cs.vertex_radius)};
             lmin = sub(lmin, r3);
@@ -441,6 +483,7 @@ public:
                 if (!overlap) continue;
                 CollidingShape<R> cs;
                 cs.collider = int(ci);
+                set_shape_geometry(cs, c);
                 cs.t = sub(cp, b.position);
                 cs.friction = std::sqrt(R(b.cs.friction) * R(c.friction));
                 cs.restitution = R(b.cs.restitution) > R(c.restitution) ? R(b.cs.restitution) : R(c.restitution);
@@ -455,18 +498,17 @@ public:
 
         // DetermineCollisionPlanes (:257-265)
         for (size_t si = 0; si < shapes.size() && freeze_mode != 2; ++si) {
-            const Collider &c = colliders[shapes[si].collider];
-            const V3<R> t = shapes[si].t;
+            const CollidingShape<R> &cs = shapes[si];
             for (auto &v : b.v) {
                 if (!(v.inv_mass > R(0))) continue;
-                if (c.type == 0)
-                    collide_box(v, c, t, int(si));
-                else if (c.type == 1)
-                    collide_sphere(v, c, t, int(si));
-                else if (c.type == 2)
-                    collide_capsule(v, c, t, int(si));
+                if (cs.type == 0)
+                    collide_box(v, cs, int(si));
+                else if (cs.type == 1)
+                    collide_sphere(v, cs, int(si));
+                else if (cs.type == 2)
+                    collide_capsule(v, cs, int(si));
                 else
-                    collide_cylinder(v, c, t, int(si));
+                    collide_cylinder(v, cs, int(si));
             }
         }
 
@@ -499,11 +541,64 @@ public:
             collide_and_update_velocities(b, shapes, g, dt_sub, dec ? dec->flags.data() + size_t(it) * b.v.size() : nullptr);
         }
         update_state(b, dt, disp_g, dec);
+        if (b.has_table) {
+            b.table_out.assign(shapes.size(), {});
+            for (size_t k = 0; k < shapes.size(); ++k)
+                b.table_out[k] = {shapes[k].updated ? 1.0f : 0.0f, float(shapes[k].lin.x), float(shapes[k].lin.y), float(shapes[k].lin.z),
+                                  float(shapes[k].ang.x), float(shapes[k].ang.y), float(shapes[k].ang.z)};
+        }
     }
 
-    void collide_box(Vertex<R> &v, const Collider &c, V3<R> t, int idx) {  // BoxShape.cpp:234-283
-        V3<R> local = add(v.pos, neg(t));  // inverse transform: R^T p + (-(R^T t)), R = identity
-        V3<R> h = {R(c.half[0]), R(c.half[1]), R(c.half[2])};
+    static void set_shape_geometry(CollidingShape<R> &cs, const Collider &c) {
+        cs.type = c.type;
+        cs.h = {R(c.half[0]), R(c.half[1]), R(c.half[2])};
+        cs.r = R(c.radius);
+    }
+
+    // Host-determined shapes (oracle_set_colliding_shapes), with the inverse transform as
+    // Mat44::InversedRotationTranslation computes it: transposed rotation, 0 - (R^T t).
+    static void shapes_from_table(const Body<R> &b, std::vector<CollidingShape<R>> &shapes) {
+        for (const TableShapeIn &e : b.table) {
+            CollidingShape<R> cs;
+            cs.type = e.type;
+            cs.rotated = true;
+            cs.dynamic = e.motion == 2;
+            for (int k = 0; k < 3; ++k) cs.c[k] = {R(e.xf[3 * k]), R(e.xf[3 * k + 1]), R(e.xf[3 * k + 2])};
+            for (int k = 0; k < 3; ++k) cs.ic[k] = {comp(cs.c[0], k), comp(cs.c[1], k), comp(cs.c[2], k)};
+            cs.t = {R(e.xf[9]), R(e.xf[10]), R(e.xf[11])};
+            cs.it = neg(mat3(cs.ic, cs.t));
+            cs.h = {R(e.half_extent[0]), R(e.half_extent[1]), R(e.half_extent[2])};
+            cs.r = R(e.radius);
+            cs.friction = R(e.friction);
+            cs.restitution = R(e.restitution);
+            cs.isc = R(e.inv_mass_scale);
+            cs.inv_mass = R(e.inv_mass);
+            for (int k = 0; k < 4; ++k) cs.inertia[k] = {R(e.inv_inertia[3 * k]), R(e.inv_inertia[3 * k + 1]), R(e.inv_inertia[3 * k + 2])};
+            cs.com = {R(e.com[0]), R(e.com[1]), R(e.com[2])};
+            cs.lin = {R(e.lin[0]), R(e.lin[1]), R(e.lin[2])};
+            cs.ang = {R(e.ang[0]), R(e.ang[1]), R(e.ang[2])};
+            shapes.push_back(cs);
+        }
+    }
+
+    // The shape's CollideSoftBodyVertices maps the vertex with its InversedRotationTranslation ...
+    static V3<R> local_of(const CollidingShape<R> &cs, V3<R> p) { return cs.rotated ? mat4(cs.ic, cs.it, p) : add(p, neg(cs.t)); }
+    // ... and stores Plane::sFromPointAndNormal(point, normal).GetTransformed(transform) (Plane.h:42-46)
+    static void set_plane(Vertex<R> &v, const CollidingShape<R> &cs, V3<R> normal, V3<R> point, int idx) {
+        if (!cs.rotated) {
+            set_plane_transformed(v, normal, point, cs.t, idx);
+            return;
+        }
+        R c = -dot(normal, point);
+        V3<R> n2 = mat3(cs.c, normal);
+        v.plane_n = n2;
+        v.plane_c = c - dot(cs.t, n2);
+        v.shape_idx = idx;
+    }
+
+    static void collide_box(Vertex<R> &v, const CollidingShape<R> &cs, int idx) {  // BoxShape.cpp:234-283
+        V3<R> local = local_of(cs, v.pos);
+        V3<R> h = cs.h;
         V3<R> nh = neg(h);
         V3<R> clamped = vmax(vmin(local, h), nh);
         if (clamped.x == local.x && clamped.y == local.y && clamped.z == local.z) {
@@ -517,7 +612,7 @@ public:
             V3<R> axis = {index == 0 ? R(1) : R(0), index == 1 ? R(1) : R(0), index == 2 ? R(1) : R(0)};
             V3<R> normal = {sign.x * axis.x, sign.y * axis.y, sign.z * axis.z};
             V3<R> point = {normal.x * h.x, normal.y * h.y, normal.z * h.z};
-            set_plane_transformed(v, normal, point, t, idx);
+            set_plane(v, cs, normal, point, idx);
         } else {
             V3<R> normal = sub(local, clamped);
             R nl = len(normal);
@@ -525,12 +620,12 @@ public:
             if (v.largest_pen >= pen) return;
             v.largest_pen = pen;
             normal = divs(normal, nl);
-            set_plane_transformed(v, normal, clamped, t, idx);
+            set_plane(v, cs, normal, clamped, idx);
         }
     }
 
     // Plane::sFromPointAndNormal(point, normal).GetTransformed(translation t, identity rotation)
-    void set_plane_transformed(Vertex<R> &v, V3<R> normal, V3<R> point, V3<R> t, int idx) {
+    static void set_plane_transformed(Vertex<R> &v, V3<R> normal, V3<R> point, V3<R> t, int idx) {
         R c = -dot(normal, point);
         // Multiply3x3 with identity columns: ((c0*x + c1*y) + c2*z)
         V3<R> n2;
@@ -542,9 +637,9 @@ public:
         v.shape_idx = idx;
     }
 
-    void collide_sphere(Vertex<R> &v, const Collider &c, V3<R> t, int idx) {  // SphereShape.cpp:279-300
-        V3<R> center = t;
-        R radius = R(c.radius);
+    static void collide_sphere(Vertex<R> &v, const CollidingShape<R> &cs, int idx) {  // SphereShape.cpp:279-300
+        V3<R> center = cs.t;
+        R radius = cs.r;
         V3<R> delta = sub(v.pos, center);
         R distance = len(delta);
         R pen = radius - distance;
@@ -558,9 +653,9 @@ public:
     }
 
     // CapsuleShape.cpp:324-374: along Y, half[1] = half height of the cylinder part
-    void collide_capsule(Vertex<R> &v, const Collider &c, V3<R> t, int idx) {
-        const V3<R> local = add(v.pos, neg(t));
-        const R hh = R(c.half[1]), r = R(c.radius);
+    static void collide_capsule(Vertex<R> &v, const CollidingShape<R> &cs, int idx) {
+        const V3<R> local = local_of(cs, v.pos);
+        const R hh = cs.h.y, r = cs.r;
         if (std::abs(local.y) <= hh) {
             V3<R> normal = {local.x, R(0), local.z};
             const R nl = len(normal);
@@ -568,7 +663,7 @@ public:
             if (v.largest_pen >= pen) return;
             v.largest_pen = pen;
             normal = nl > R(0) ? divs(normal, nl) : V3<R>{R(1), R(0), R(0)};
-            set_plane_transformed(v, normal, mul(r, normal), t, idx);
+            set_plane(v, cs, normal, mul(r, normal), idx);
         } else {
             const V3<R> center = {R(0), (local.y < R(0) ? R(-1) : R(1)) * hh, R(0)};
             const V3<R> delta = sub(local, center);
@@ -577,14 +672,14 @@ public:
             if (v.largest_pen >= pen) return;
             v.largest_pen = pen;
             const V3<R> normal = divs(delta, distance);
-            set_plane_transformed(v, normal, add(center, mul(r, normal)), t, idx);
+            set_plane(v, cs, normal, add(center, mul(r, normal)), idx);
         }
     }
 
     // CylinderShape.cpp:317-368: along Y, half[1] = half height
-    void collide_cylinder(Vertex<R> &v, const Collider &c, V3<R> t, int idx) {
-        const V3<R> local = add(v.pos, neg(t));
-        const R hh = R(c.half[1]), r = R(c.radius);
+    static void collide_cylinder(Vertex<R> &v, const CollidingShape<R> &cs, int idx) {
+        const V3<R> local = local_of(cs, v.pos);
+        const R hh = cs.h.y, r = cs.r;
         const V3<R> side = {local.x, R(0), local.z};
         const R side_len = len(side);
         const R side_pen = r - side_len;
@@ -609,7 +704,7 @@ public:
         const R pen = -(dot(local, normal) + cst);
         if (v.largest_pen >= pen) return;
         v.largest_pen = pen;
-        set_plane_transformed(v, normal, point, t, idx);
+        set_plane(v, cs, normal, point, idx);
     }
 
     void apply_pressure(Body<R> &b, R dt) {  // :291-323
@@ -742,17 +837,22 @@ public:
         if (dls > md * md) v1.pos = add(x0, divs(mul(delta, md), std::sqrt(dls)));
     }
 
-    void collide_and_update_velocities(Body<R> &b, const std::vector<CollidingShape<R>> &shapes, V3<R> g, R dt, uint8_t *flags) {  // :700-825
+    void collide_and_update_velocities(Body<R> &b, std::vector<CollidingShape<R>> &shapes, V3<R> g, R dt, uint8_t *flags) {  // :700-825
         R restitution_threshold = R(-2.0f) * len(g) * dt;
         R radius = R(b.cs.vertex_radius);
+        bool dynamic = false;
+        for (const auto &cs : shapes) dynamic = dynamic || cs.dynamic;
+        if (dynamic) {  // dynamic shapes carry velocities from one vertex to the next: in index order
+            for (size_t i = 0; i < b.v.size(); ++i) collide_vertex(b.v[i], shapes, dt, restitution_threshold, radius, flags ? flags + i : nullptr);
+            return;
+        }
         for_vertex_ranges(b.v.size(), [&](size_t first, size_t last) {
             for (size_t i = first; i < last; ++i) collide_vertex(b.v[i], shapes, dt, restitution_threshold, radius, flags ? flags + i : nullptr);
         });
     }
 
     // one vertex of ApplyCollisionConstraintsAndUpdateVelocities
-    void collide_vertex(Vertex<R> &v, const std::vector<CollidingShape<R>> &shapes, R dt, R restitution_threshold, R radius,
-                        uint8_t *flags) {
+    void collide_vertex(Vertex<R> &v, std::vector<CollidingShape<R>> &shapes, R dt, R restitution_threshold, R radius, uint8_t *flags) {
         {
             if (!(v.inv_mass > R(0))) return;
             V3<R> prev_v = v.vel;
@@ -764,16 +864,21 @@ public:
             if (flags && !replay && contact) *flags |= 1;
             if (!contact) return;
             v.contact = true;
-            const CollidingShape<R> &cs = shapes[v.shape_idx];
+            CollidingShape<R> &cs = shapes[v.shape_idx];
             V3<R> n = v.plane_n;
             v.pos = add(v.pos, mul(n, projected));
-            // static body, soft body inverse mass scale 1 (:798-816)
+            if (cs.dynamic) {
+                collide_dynamic(v, cs, n, projected, prev_v, dt, restitution_threshold);
+                return;
+            }
+            if (!(cs.isc > R(0))) return;
+            // static or kinematic body (:798-816)
             V3<R> v_normal = mul(n, dot(n, v.vel));
             V3<R> v_tan = sub(v.vel, v_normal);
             R vtl = len(v_tan);
             if (vtl > R(0)) {
                 R f = cs.friction * projected / (vtl * dt);
-                const bool clamped = replay ? (*flags & 2) != 0 : f > R(1);
+                const bool clamped = replay ? (*flags & 2) != 0 : !(f < R(1));  // min(f, 1)
                 if (flags && !replay && clamped) *flags |= 2;
                 if (clamped) f = R(1);
                 v.vel = sub(v.vel, mul(v_tan, f));
@@ -784,6 +889,35 @@ public:
             if (flags && !replay && bounce) *flags |= 4;
             if (bounce) v.vel = sub(v.vel, mul(cs.restitution * pvn, n));
         }
+    }
+
+    // the dynamic-body branch (:752-797) after the push out of the plane
+    static void collide_dynamic(Vertex<R> &v, CollidingShape<R> &cs, V3<R> n, R projected, V3<R> prev_v, R dt, R restitution_threshold) {
+        const V3<R> r2 = sub(v.pos, cs.com);
+        const V3<R> v2 = add(cs.lin, cross(cs.ang, r2));
+        const V3<R> relative = sub(v.vel, v2);
+        const V3<R> v_normal = mul(n, dot(n, relative));
+        const V3<R> v_tan = sub(relative, v_normal);
+        const R vtl = len(v_tan);
+        const R vertex_inv_mass = cs.isc * v.inv_mass;
+        const V3<R> r2xn = cross(r2, n);
+        const R w2 = cs.inv_mass + dot(r2xn, mat4(cs.inertia, cs.inertia[3], r2xn));
+        const R w12 = vertex_inv_mass + w2;
+        if (!(w12 > R(0))) return;
+        V3<R> dv = {R(0), R(0), R(0)};
+        if (vtl > R(0)) {
+            R f = cs.friction * projected / (vtl * dt);
+            if (!(f < R(1))) f = R(1);
+            dv = mul(v_tan, f);
+        }
+        dv = add(dv, v_normal);
+        const R pvn = dot(sub(prev_v, v2), n);
+        if (pvn < restitution_threshold) dv = add(dv, mul(cs.restitution * pvn, n));
+        const V3<R> imp = divs(dv, w12);
+        v.vel = sub(v.vel, mul(imp, vertex_inv_mass));
+        cs.lin = add(cs.lin, mul(imp, cs.inv_mass));
+        cs.ang = add(cs.ang, mat4(cs.inertia, cs.inertia[3], cross(r2, imp)));
+        cs.updated = true;
     }
 
     void update_state(Body<R> &b, R dt, V3<R> disp_g, typename Body<R>::Decisions *dec) {  // :827-921
@@ -960,6 +1094,26 @@ int oracle_step(void *w, float dt, int collision_steps) {
         h->wf.step(dt, collision_steps);
     }
     return 0;
+}
+
+// Host-determined colliding shapes of one body (jsb_colliding_shape layout), used by the following steps
+// instead of the world's colliders; n < 0 returns the body to the world's colliders.
+int oracle_set_colliding_shapes(void *w, int body, const void *entries, int n) {
+    Handle *h = static_cast<Handle *>(w);
+    const TableShapeIn *e = static_cast<const TableShapeIn *>(entries);
+    for (auto *bs : {&h->wf.bodies[body].table, &h->wd.bodies[body].table}) bs->assign(e, e + (n > 0 ? n : 0));
+    h->wf.bodies[body].has_table = h->wd.bodies[body].has_table = n >= 0;
+    return 0;
+}
+
+// After a step with host-determined shapes: per shape {updated, linear velocity[3], angular velocity[3]}.
+// Returns the number of shapes.
+int oracle_get_shape_velocities(void *w, int body, float *out) {
+    Handle *h = static_cast<Handle *>(w);
+    const auto &o = h->use_double ? h->wd.bodies[body].table_out : h->wf.bodies[body].table_out;
+    for (size_t k = 0; k < o.size(); ++k)
+        for (int j = 0; j < 7; ++j) out[7 * k + j] = o[k][j];
+    return int(o.size());
 }
 
 // Conditioning probe of double runs: after every step each position and velocity component x becomes

@@ -14,6 +14,15 @@
 //   keys : steps, dump (comma list of step numbers, 0 = initial), threads, seed, n, n_cloth, n_cube,
 //          cloth_min, cloth_max, cube_min, cube_max, time_only (1 = no dumps, print timing JSON)
 //
+// Scenes with rigid bodies (SceneSpec::rigid) take tables=<path>: for every step, every soft body's
+// colliding shapes as the reference determined them (SoftBodyMotionProperties::DetermineCollidingShapes,
+// SoftBodyMotionProperties.cpp:120-255), recorded by a SoftBodyContactListener that accepts every contact
+// and recomputes the collector's values with the same calls, then each rigid body's velocities after the
+// step (which hold the soft bodies' velocity deltas, :923-935):
+//   'JSBT' u32 version=1 u32 steps u32 num_rigid
+//   per step: i32 step, u32 num_entries, num_entries x TableEntry, num_rigid x f32[6] (linear, angular
+//             velocity after the step, world space)
+//
 // Output file (little endian):
 //   'JSBD' u32 version=2 u32 num_dumps u32 scene_len, scene_len bytes of the serialised scene
 //          (tests/scenes/scene_io.h, settings bytes written by Jolt)
@@ -37,11 +46,15 @@
 #include <Jolt/Physics/SoftBody/SoftBodySharedSettings.h>
 #include <Jolt/Physics/SoftBody/SoftBodyCreationSettings.h>
 #include <Jolt/Physics/SoftBody/SoftBodyMotionProperties.h>
+#include <Jolt/Physics/SoftBody/SoftBodyContactListener.h>
+#include <Jolt/Physics/Body/BodyLockMulti.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <sstream>
 #include <string>
 #include <thread>
@@ -126,6 +139,77 @@ std::string save_settings(const SoftBodySharedSettings &s) {
 
 void put_u32(FILE *f, uint32_t v) { fwrite(&v, 4, 1, f); }
 
+RefConst<Shape> make_shape(jsb::scene::ColliderType type, const float half_extent[3], float radius) {
+    if (type == jsb::scene::ColliderType::Box) return new BoxShape(Vec3(half_extent[0], half_extent[1], half_extent[2]));
+    if (type == jsb::scene::ColliderType::Sphere) return new SphereShape(radius);
+    if (type == jsb::scene::ColliderType::Capsule) return new CapsuleShape(half_extent[1], radius);
+    return new CylinderShape(half_extent[1], radius);
+}
+
+// One colliding shape of one soft body in one step (the fields of SoftBodyMotionProperties::CollidingShape
+// and its LeafShape), as the tables file stores it.
+struct TableEntry {
+    uint32_t soft_body, rigid;
+    int32_t type, motion;
+    float leaf[16];       // LeafShape::mTransform (columns)
+    float half_extent[3], radius, friction, restitution;
+    float inv_mass_scale1, inv_mass;
+    float inv_inertia[16];  // CollidingShape::mInvInertia (columns)
+    float com[16];          // CollidingShape::mCenterOfMassTransform (columns)
+    float lin[3], ang[3];   // CollidingShape::mLinearVelocity / mAngularVelocity (soft-body space)
+    float lin_world[3], ang_world[3];  // the rigid body's velocities when the shape was collected
+};
+
+void put_mat(float out[16], Mat44Arg m) {
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) out[4 * c + r] = m(r, c);
+}
+
+// Accepts every contact and records, per soft body, what SoftBodyMotionProperties::DetermineCollidingShapes'
+// collector stores for the shape (SoftBodyMotionProperties.cpp:139-225), computed with the same calls.
+class TableRecorder final : public SoftBodyContactListener {
+public:
+    std::map<uint32_t, uint32_t> soft_index, rigid_index;  // BodyID index -> spec index
+    const jsb::scene::SceneSpec *spec = nullptr;
+    const PhysicsSystem *system = nullptr;
+    std::mutex mutex;
+    std::vector<TableEntry> entries;  // of the current step
+
+    SoftBodyValidateResult OnSoftBodyContactValidate(const Body &inSoftBody, const Body &inOtherBody, SoftBodyContactSettings &ioSettings) override {
+        TableEntry e{};
+        e.soft_body = soft_index.at(inSoftBody.GetID().GetIndex());
+        e.rigid = rigid_index.at(inOtherBody.GetID().GetIndex());
+        const jsb::scene::RigidSpec &rs = spec->rigid[e.rigid];
+        e.type = int32_t(rs.type);
+        e.motion = int32_t(inOtherBody.GetMotionType());
+        RMat44 inverse = inSoftBody.GetCenterOfMassTransform().InversedRotationTranslation();
+        Mat44 com = (inverse * inOtherBody.GetCenterOfMassTransform()).ToMat44();
+        put_mat(e.com, com);
+        put_mat(e.leaf, Mat44::sRotationTranslation(com.GetQuaternion(), com.GetTranslation()));
+        for (int k = 0; k < 3; ++k) e.half_extent[k] = rs.half_extent[k];
+        e.radius = rs.radius;
+        e.friction = system->GetCombineFriction()(inSoftBody, SubShapeID(), inOtherBody, SubShapeID());
+        e.restitution = system->GetCombineRestitution()(inSoftBody, SubShapeID(), inOtherBody, SubShapeID());
+        e.inv_mass_scale1 = ioSettings.mInvMassScale1;
+        if (inOtherBody.GetMotionType() == EMotionType::Dynamic) {
+            const MotionProperties *mp = inOtherBody.GetMotionProperties();
+            e.inv_mass = ioSettings.mInvMassScale2 * mp->GetInverseMass();
+            put_mat(e.inv_inertia, ioSettings.mInvInertiaScale2 * mp->GetInverseInertiaForRotation(com.GetRotation()));
+            Vec3 lin = inverse.Multiply3x3(mp->GetLinearVelocity()), ang = inverse.Multiply3x3(mp->GetAngularVelocity());
+            Vec3 lw = mp->GetLinearVelocity(), aw = mp->GetAngularVelocity();
+            for (int k = 0; k < 3; ++k) {
+                e.lin[k] = lin[k];
+                e.ang[k] = ang[k];
+                e.lin_world[k] = lw[k];
+                e.ang_world[k] = aw[k];
+            }
+        }
+        std::lock_guard<std::mutex> lock(mutex);
+        entries.push_back(e);
+        return SoftBodyValidateResult::AcceptContact;
+    }
+};
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -171,25 +255,39 @@ int main(int argc, char **argv) {
         ObjVsBP obj_vs_bp;
         LayerPairFilter pair_filter;
         PhysicsSystem system;
-        system.Init(uint(spec.bodies.size() + spec.colliders.size() + 16), 0, 65536, 65536, bp_layers, obj_vs_bp, pair_filter);
+        system.Init(uint(spec.bodies.size() + spec.colliders.size() + spec.rigid.size() + 16), 0, 65536, 65536, bp_layers, obj_vs_bp,
+                    pair_filter);
         system.SetGravity(Vec3(spec.gravity[0], spec.gravity[1], spec.gravity[2]));
         BodyInterface &bi = system.GetBodyInterface();
 
         for (auto &c : spec.colliders) {
-            RefConst<Shape> shape;
-            if (c.type == jsb::scene::ColliderType::Box)
-                shape = new BoxShape(Vec3(c.half_extent[0], c.half_extent[1], c.half_extent[2]));
-            else if (c.type == jsb::scene::ColliderType::Sphere)
-                shape = new SphereShape(c.radius);
-            else if (c.type == jsb::scene::ColliderType::Capsule)
-                shape = new CapsuleShape(c.half_extent[1], c.radius);
-            else
-                shape = new CylinderShape(c.half_extent[1], c.radius);
-            BodyCreationSettings bcs(shape, RVec3(c.position[0], c.position[1], c.position[2]), Quat::sIdentity(), EMotionType::Static,
-                                     Layers::NON_MOVING);
+            BodyCreationSettings bcs(make_shape(c.type, c.half_extent, c.radius), RVec3(c.position[0], c.position[1], c.position[2]),
+                                     Quat::sIdentity(), EMotionType::Static, Layers::NON_MOVING);
             bcs.mFriction = c.friction;
             bcs.mRestitution = c.restitution;
             bi.CreateAndAddBody(bcs, EActivation::DontActivate);
+        }
+        TableRecorder recorder;
+        recorder.spec = &spec;
+        recorder.system = &system;
+        std::vector<BodyID> rigid_ids;
+        for (size_t r = 0; r < spec.rigid.size(); ++r) {
+            const jsb::scene::RigidSpec &c = spec.rigid[r];
+            const bool moving = c.motion != 0;
+            BodyCreationSettings bcs(make_shape(c.type, c.half_extent, c.radius), RVec3(c.position[0], c.position[1], c.position[2]),
+                                     Quat(c.rotation[0], c.rotation[1], c.rotation[2], c.rotation[3]), EMotionType(c.motion),
+                                     moving ? Layers::MOVING : Layers::NON_MOVING);
+            bcs.mFriction = c.friction;
+            bcs.mRestitution = c.restitution;
+            if (c.motion == 2) {
+                bcs.mOverrideMassProperties = EOverrideMassProperties::CalculateInertia;
+                bcs.mMassPropertiesOverride.mMass = c.mass;
+            }
+            bcs.mLinearVelocity = Vec3(c.velocity[0], c.velocity[1], c.velocity[2]);
+            bcs.mAngularVelocity = Vec3(c.angular_velocity[0], c.angular_velocity[1], c.angular_velocity[2]);
+            BodyID id = bi.CreateAndAddBody(bcs, moving ? EActivation::Activate : EActivation::DontActivate);
+            rigid_ids.push_back(id);
+            recorder.rigid_index[id.GetIndex()] = uint32_t(r);
         }
 
         std::vector<Ref<SoftBodySharedSettings>> settings;
@@ -211,8 +309,22 @@ int main(int argc, char **argv) {
             sbcs.mAllowSleeping = b.creation.allow_sleeping;
             sbcs.mFacesDoubleSided = b.creation.faces_double_sided;
             ids.push_back(bi.CreateAndAddSoftBody(sbcs, EActivation::Activate));
+            recorder.soft_index[ids.back().GetIndex()] = uint32_t(ids.size() - 1);
         }
         system.OptimizeBroadPhase();
+        FILE *tables = nullptr;
+        if (!spec.rigid.empty() && kv.count("tables")) {
+            system.SetSoftBodyContactListener(&recorder);
+            tables = fopen(kv["tables"].c_str(), "wb");
+            if (!tables) {
+                fprintf(stderr, "cannot open %s\n", kv["tables"].c_str());
+                return 1;
+            }
+            fwrite("JSBT", 4, 1, tables);
+            put_u32(tables, 1);
+            put_u32(tables, uint32_t(steps));
+            put_u32(tables, uint32_t(spec.rigid.size()));
+        }
 
         FILE *f = nullptr;
         if (!time_only) {
@@ -292,8 +404,24 @@ int main(int argc, char **argv) {
                 dump(step);
                 ++next_dump;
             }
+            if (tables) {
+                // entries of one soft body keep their collection order; soft bodies in index order
+                std::stable_sort(recorder.entries.begin(), recorder.entries.end(),
+                                 [](const TableEntry &a, const TableEntry &b) { return a.soft_body < b.soft_body; });
+                int32_t st = step;
+                fwrite(&st, 4, 1, tables);
+                put_u32(tables, uint32_t(recorder.entries.size()));
+                fwrite(recorder.entries.data(), sizeof(TableEntry), recorder.entries.size(), tables);
+                recorder.entries.clear();
+                for (BodyID id : rigid_ids) {
+                    Vec3 lv = bi.GetLinearVelocity(id), av = bi.GetAngularVelocity(id);
+                    float v6[6] = {lv.GetX(), lv.GetY(), lv.GetZ(), av.GetX(), av.GetY(), av.GetZ()};
+                    fwrite(v6, 4, 6, tables);
+                }
+            }
         }
         if (f) fclose(f);
+        if (tables) fclose(tables);
         printf("{\"scene\": \"%s\", \"bodies\": %zu, \"vertices\": %llu, \"steps\": %d, \"threads\": %d, \"seconds\": %.6f, "
                "\"vertex_iterations_per_s\": %.6e}\n",
                scene_name.c_str(), spec.bodies.size(), (unsigned long long)total_vertices, steps, threads, seconds,

@@ -68,6 +68,36 @@ def make(name: str, scene: str, params: dict, steps: list[int]):
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
 
 
+def make_coupling(name: str = "coupling", steps: int = 90, dump: tuple = (1, 10, 17, 18, 19, 20, 30, 45, 60, 75, 90)):
+    """Two-way coupling (rigid bodies simulated by the reference's own solver): per dump step the
+    deterministic build's soft-body states, and for every step each soft body's colliding shapes as the
+    reference determined them (tables_*: jsb_colliding_shape bytes, soft body, rigid body, the rigid body's
+    world velocities when collected) and the rigid bodies' velocities after the step."""
+    from jsb_testlib import SHAPE_BYTES, parse_tables
+
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        path, tab = os.path.join(tmp, "det.bin"), os.path.join(tmp, "det.tab")
+        run_reference("det", "coupling", path, dump=",".join(str(s) for s in [0, *dump]), steps=steps, tables=tab)
+        sc, dumps = parse_dump(path)
+        t = parse_tables(tab)
+    out["scene"] = np.frombuffer(sc.raw, np.uint8)
+    out["steps"] = np.array(dump, np.int32)
+    out["num_vertices"] = np.array([b.num_vertices for b in sc.bodies], np.int64)
+    for d in dumps[1:]:
+        out[f"det_pos_{d.step}"] = np.stack(d.positions).astype(np.float32)
+        out[f"det_local_{d.step}"] = np.concatenate(d.local).astype(np.float32)
+        out[f"det_vel_{d.step}"] = np.concatenate(d.velocities).astype(np.float32)
+    rows = [(st, *r) for st in sorted(t["steps"]) for r in t["steps"][st]]
+    out["tables_step"] = np.array([r[0] for r in rows], np.int32)
+    out["tables_body"] = np.array([r[1] for r in rows], np.int32)
+    out["tables_rigid"] = np.array([r[2] for r in rows], np.int32)
+    out["tables_shape"] = np.frombuffer(b"".join(r[3] for r in rows), np.uint8).reshape(len(rows), SHAPE_BYTES)
+    out["tables_rigid_velocity"] = np.stack([r[4] for r in rows]).astype(np.float32)
+    out["rigid_after"] = t["rigid_after"]
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+
+
 # name: (scene, params, dump steps): every BASELINE configuration at its full size and length
 FULL_CASES = {
     "pinned_cloth": ("pinned_cloth", {}, [1, 100, 200, 300]),
@@ -117,6 +147,9 @@ if __name__ == "__main__":
         if not which or name in which:
             make(name, scene, params, steps)
             print("wrote", name)
+    if not which or "coupling" in which:
+        make_coupling()
+        print("wrote coupling")
     for name, (scene, params, steps) in FULL_CASES.items():
         if not which or f"full_{name}" in which:
             make_full(name, scene, params, steps, threads=os.cpu_count() or 1)

@@ -157,6 +157,46 @@ def run_reference(variant: str, scene: str, out: str, **kv) -> dict:
     return json.loads(res.stdout.strip().splitlines()[-1])
 
 
+# jsb_colliding_shape (include/jsb.h): type, motion type, transform[12], half_extent[3], radius, friction,
+# restitution, soft-body inverse-mass scale, inverse mass, inverse inertia[12], centre of mass[3], linear
+# velocity[3], angular velocity[3]
+SHAPE_FMT = "<2i41f"
+SHAPE_BYTES = struct.calcsize(SHAPE_FMT)
+_TABLE_ENTRY = "<2I2i16f3f3f2f16f16f3f3f3f3f"  # oracle/ref_driver.cpp TableEntry
+
+
+def parse_tables(path: str) -> dict:
+    """The reference driver's tables file: {"steps": {step: [(soft body, rigid index, shape bytes
+    (SHAPE_FMT), rigid linear and angular velocity (world) when collected)]}, "rigid_after": (steps,
+    num_rigid, 6) velocities after each step}."""
+    buf = open(path, "rb").read()
+    assert buf[:4] == b"JSBT"
+    _, steps, nr = struct.unpack_from("<III", buf, 4)
+    off, esz = 16, struct.calcsize(_TABLE_ENTRY)
+    out, after = {}, np.zeros((steps, nr, 6), np.float32)
+    for k in range(steps):
+        st, n = struct.unpack_from("<iI", buf, off)
+        off += 8
+        rows = []
+        for _ in range(n):
+            v = struct.unpack_from(_TABLE_ENTRY, buf, off)
+            off += esz
+            sb, rg, ty, mo = v[0:4]
+            leaf = np.array(v[4:20], np.float32).reshape(4, 4)  # columns
+            he, rad, fr, rs = v[20:23], v[23], v[24], v[25]
+            isc, im = v[26], v[27]
+            inert = np.array(v[28:44], np.float32).reshape(4, 4)
+            com = np.array(v[44:60], np.float32).reshape(4, 4)
+            lin, ang, lw, aw = v[60:63], v[63:66], v[66:69], v[69:72]
+            shape = struct.pack(SHAPE_FMT, ty, mo, *leaf[:, :3].ravel(), *he, rad, fr, rs, isc, im, *inert[:, :3].ravel(),
+                                *com[3, :3], *lin, *ang)
+            rows.append((sb, rg, shape, np.array(lw + aw, np.float32)))
+        out[st] = rows
+        after[k] = np.frombuffer(buf, np.float32, 6 * nr, off).reshape(nr, 6)
+        off += 24 * nr
+    return {"steps": out, "rigid_after": after}
+
+
 def build_oracle() -> str:
     """oracle/build.py's build_oracle (compiles liboracle.so when it is missing or stale)."""
     import importlib.util
@@ -205,6 +245,8 @@ class Oracle:
             L.oracle_set_freeze.argtypes = [ctypes.c_void_p, ctypes.c_int]
             L.oracle_copy_decisions.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
             L.oracle_set_noise.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64]
+            L.oracle_set_colliding_shapes.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
+            L.oracle_get_shape_velocities.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
             L.oracle_last_error.restype = ctypes.c_char_p
             L.oracle_last_error.argtypes = [ctypes.c_void_p]
             cls._lib = L
@@ -240,6 +282,18 @@ class Oracle:
                 if any(f != 0.0 for f in b.force):
                     L.oracle_set_force(self.h, i, (ctypes.c_float * 3)(*b.force))
             L.oracle_step(self.h, self.scene.dt, self.scene.collision_steps)
+
+    def set_colliding_shapes(self, i: int, shapes: list[bytes] | None):
+        """Host-determined colliding shapes of body i for the following steps (SHAPE_FMT records); None
+        returns the body to the scene's colliders."""
+        data = b"".join(shapes or [])
+        self.lib().oracle_set_colliding_shapes(self.h, i, data, -1 if shapes is None else len(shapes))
+
+    def shape_velocities(self, i: int) -> np.ndarray:
+        """After a step with host-determined shapes: per shape (updated, linear velocity, angular velocity)."""
+        out = np.zeros((16, 7), np.float32)
+        n = self.lib().oracle_get_shape_velocities(self.h, i, out.ctypes.data)
+        return out[:n]
 
     def active(self, i: int) -> bool:
         return bool(self.lib().oracle_body_active(self.h, i))

@@ -100,6 +100,8 @@ inline bool make_named_scene(const std::string &name, const std::string &params,
     else if (name == "diff_batch")
         out = make_diff_batch(uint64_t(geti("seed", 5)), uint32_t(geti("n_cloth", 192)), uint32_t(geti("n_cube", 64)),
                               int(geti("steps", 90)), float(geti("drop_mm", 1000)) * 0.001f);
+    else if (name == "coupling")
+        out = make_coupling(int(geti("steps", 90)));
     else if (name == "shapes_drop")
         out = make_shapes_drop(uint64_t(geti("seed", 7)), int(geti("steps", 150)));
     else

@@ -123,9 +123,28 @@ struct ColliderSpec {  // a static rigid body with one convex shape (capsules an
     float restitution = 0.0f;
 };
 
+// A rigid body that only the reference driver creates and simulates with Jolt's own rigid-body solver
+// (scenes of two-way coupling); it is not part of the serialised scene: the soft bodies' colliding
+// shapes, as the reference determined them each step, reach the GPU and the oracle through the
+// host-determined colliding-shape tables.
+struct RigidSpec {
+    ColliderType type = ColliderType::Box;
+    int motion = 2;                        // EMotionType: 0 static, 1 kinematic, 2 dynamic
+    float position[3] = {0, 0, 0};
+    float rotation[4] = {0, 0, 0, 1};      // quaternion x, y, z, w
+    float half_extent[3] = {1, 1, 1};      // box; [1]: half height of a capsule's cylinder part / a cylinder
+    float radius = 1.0f;
+    float mass = 1.0f;                     // dynamic bodies (inertia from the shape)
+    float friction = 0.2f;
+    float restitution = 0.0f;
+    float velocity[3] = {0, 0, 0};
+    float angular_velocity[3] = {0, 0, 0};
+};
+
 struct SceneSpec {
     std::vector<BodySpec> bodies;
     std::vector<ColliderSpec> colliders;
+    std::vector<RigidSpec> rigid;  // reference driver only
     float gravity[3] = {0.0f, -9.81f, 0.0f};
     float dt = 1.0f / 60.0f;
     int collision_steps = 1;
@@ -520,6 +539,80 @@ inline SceneSpec make_shapes_drop(uint64_t seed = 7, int steps = 150) {
     floor.half_extent[2] = 10.0f;
     floor.position[1] = -1.0f;
     s.colliders.push_back(floor);
+    s.num_steps = steps;
+    return s;
+}
+
+// Two-way coupling: three 20 x 20 cloths (0.06 m spacing, 40 g per vertex, dihedral bends) over a static
+// floor (top at y = 0). Trampolines A and B have every border vertex pinned at y = 1: a dynamic sphere
+// (radius 0.15, 2 kg) falls onto A from 0.5 m above, a dynamic box (half extent 0.12, 2 kg, turned 0.5 rad
+// about a tilted axis and spinning) onto B. Cloth C is free and falls onto a static box turned 0.4 rad about Z.
+// The rigid bodies move under Jolt's own solver in the reference run; the soft bodies see them through
+// each step's colliding shapes. `steps` steps of 1/60 s.
+inline SceneSpec make_coupling(int steps = 90) {
+    SceneSpec s;
+    const float xs[3] = {-1.6f, 0.0f, 1.6f};
+    for (int k = 0; k < 3; ++k) {
+        BodySpec b;
+        const uint32_t n = 20;
+        if (k < 2)
+            b.mesh = make_cloth(n, n, 0.06f, [n](uint32_t x, uint32_t z) { return x == 0 || z == 0 || x == n - 1 || z == n - 1; });
+        else
+            b.mesh = make_cloth(n, n, 0.06f, [](uint32_t, uint32_t) { return false; });
+        for (float &w : b.mesh.inv_mass)
+            if (w > 0.0f) w = 25.0f;  // 40 g per vertex
+        b.mesh.attributes = VertexAttributes{1.0e-6f, 1.0e-6f, 1.0e-4f};
+        b.mesh.bend_type = BendType::Dihedral;
+        b.creation.friction = 0.5f;
+        b.position[0] = xs[k];
+        b.position[1] = k < 2 ? 1.0f : 1.4f;
+        s.bodies.push_back(b);
+    }
+    RigidSpec floor;
+    floor.type = ColliderType::Box;
+    floor.motion = 0;
+    floor.half_extent[0] = 5.0f;
+    floor.half_extent[1] = 0.5f;
+    floor.half_extent[2] = 5.0f;
+    floor.position[1] = -0.5f;
+    s.rigid.push_back(floor);
+    RigidSpec ball;
+    ball.type = ColliderType::Sphere;
+    ball.radius = 0.15f;
+    ball.mass = 2.0f;
+    ball.friction = 0.4f;
+    ball.restitution = 0.2f;
+    ball.position[0] = xs[0];
+    ball.position[1] = 1.5f;
+    s.rigid.push_back(ball);
+    RigidSpec box;
+    box.type = ColliderType::Box;
+    box.half_extent[0] = box.half_extent[1] = box.half_extent[2] = 0.12f;
+    box.mass = 2.0f;
+    box.friction = 0.6f;
+    box.position[0] = xs[1] + 0.05f;
+    box.position[1] = 1.5f;
+    box.position[2] = -0.04f;
+    // 0.5 rad about the unit axis (0.36, 0.48, 0.8)
+    const float sh = std::sin(0.25f), ch = std::cos(0.25f);
+    box.rotation[0] = 0.36f * sh;
+    box.rotation[1] = 0.48f * sh;
+    box.rotation[2] = 0.8f * sh;
+    box.rotation[3] = ch;
+    box.angular_velocity[1] = 2.0f;
+    s.rigid.push_back(box);
+    RigidSpec ramp;
+    ramp.type = ColliderType::Box;
+    ramp.motion = 0;
+    ramp.half_extent[0] = 0.5f;
+    ramp.half_extent[1] = 0.1f;
+    ramp.half_extent[2] = 0.5f;
+    ramp.position[0] = xs[2];
+    ramp.position[1] = 0.5f;
+    ramp.rotation[2] = std::sin(0.2f);
+    ramp.rotation[3] = std::cos(0.2f);
+    ramp.friction = 0.3f;
+    s.rigid.push_back(ramp);
     s.num_steps = steps;
     return s;
 }

@@ -1,0 +1,85 @@
+"""The CPU oracle's host-determined colliding shapes against the reference's two-way coupling run
+(tests/golden/coupling.npz, written by tests/golden/make_golden.py from the reference driver).
+
+Three cloths under a static floor: a dynamic sphere and a turned, spinning dynamic box fall onto two
+trampolines, a third cloth onto a static turned box. Jolt's own rigid-body solver moves the rigid bodies;
+each step every soft body's colliding shapes are fed to the oracle as the reference determined them
+(transforms, combined friction / restitution, the dynamic bodies' mass, inertia and velocities). Bar:
+- every soft body's state bitwise equal to the reference (deterministic build) at every dumped step;
+- the dynamic bodies' velocity changes (UpdateRigidBodyVelocities, SoftBodyMotionProperties.cpp:923-935):
+  the rigid body's velocity when collected plus the oracle's change equals the reference's velocity after
+  the step, bitwise.
+"""
+import struct
+
+import numpy as np
+
+from conftest import golden_path
+from jsb_testlib import SHAPE_FMT, parse_scene
+
+
+def tables_by_step(g):
+    out = {}
+    for k in range(len(g["tables_step"])):
+        out.setdefault(int(g["tables_step"][k]), []).append((int(g["tables_body"][k]), int(g["tables_rigid"][k]),
+                                                            g["tables_shape"][k].tobytes(), g["tables_rigid_velocity"][k]))
+    return out
+
+
+def world_delta(local_new, local_old):
+    """inContext.mCenterOfMassTransform.Multiply3x3(new - old) with the soft body's identity rotation, in
+    float32 with Mat44::Multiply3x3's order: (c0 x + c1 y) + c2 z."""
+    d = (np.asarray(local_new, np.float32) - np.asarray(local_old, np.float32)).astype(np.float32)
+    one, zero = np.float32(1), np.float32(0)
+    cols = [(one, zero, zero), (zero, one, zero), (zero, zero, one)]
+    return np.array([(cols[0][i] * d[0] + cols[1][i] * d[1]) + cols[2][i] * d[2] for i in range(3)], np.float32)
+
+
+def check_velocity_changes(rows, shape_out_by_body, after):
+    """rows: the step's (body, rigid, shape bytes, world velocities when collected); shape_out_by_body:
+    per body the solver's (updated, lin[3], ang[3]) per shape; after: the reference's (num_rigid, 6)."""
+    per_body_index = {}
+    checked = 0
+    for body, rigid, shape, vel0 in rows:
+        k = per_body_index.get(body, 0)
+        per_body_index[body] = k + 1
+        v = struct.unpack(SHAPE_FMT, shape)
+        if v[1] != 2:
+            continue
+        out = shape_out_by_body[body][k]
+        lin_in, ang_in = np.array(v[37:40], np.float32), np.array(v[40:43], np.float32)
+        if out[0] == 0:
+            assert np.array_equal(out[1:4], lin_in) and np.array_equal(out[4:7], ang_in)
+            assert np.array_equal(after[rigid], vel0), (body, rigid)
+            continue
+        lin = (vel0[:3] + world_delta(out[1:4], lin_in)).astype(np.float32)
+        ang = (vel0[3:] + world_delta(out[4:7], ang_in)).astype(np.float32)
+        assert np.array_equal(lin, after[rigid][:3]), (body, rigid, lin, after[rigid][:3])
+        assert np.array_equal(ang, after[rigid][3:]), (body, rigid, ang, after[rigid][3:])
+        checked += 1
+    return checked
+
+
+def test_oracle_coupling_bitwise_vs_reference(oracle_lib):
+    g = np.load(golden_path("coupling"))
+    scene, _ = parse_scene(g["scene"].tobytes())
+    nv = list(g["num_vertices"])
+    tables = tables_by_step(g)
+    o = oracle_lib(scene)
+    dumps = set(int(s) for s in g["steps"])
+    changes = 0
+    for step in range(1, int(g["steps"][-1]) + 1):
+        rows = tables.get(step, [])
+        for b in range(len(nv)):
+            o.set_colliding_shapes(b, [r[2] for r in rows if r[0] == b])
+        o.step(1)
+        changes += check_velocity_changes(rows, {b: o.shape_velocities(b) for b in range(len(nv))}, g["rigid_after"][step - 1])
+        if step in dumps:
+            off = 0
+            for b in range(len(nv)):
+                pos, loc, vel = o.body(b)
+                assert np.array_equal(pos, g[f"det_pos_{step}"][b]), (step, b)
+                assert np.array_equal(loc, g[f"det_local_{step}"][off:off + nv[b]]), (step, b)
+                assert np.array_equal(vel, g[f"det_vel_{step}"][off:off + nv[b]]), (step, b)
+                off += nv[b]
+    assert changes > 50, changes  # the sphere and the box are pushed by their trampolines most of the run
