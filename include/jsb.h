@@ -120,6 +120,43 @@ jsb_status jsb_body_set_active(jsb_context *ctx, uint32_t body_id, int active);
 
 jsb_status jsb_body_num_vertices(jsb_context *ctx, uint32_t body_id, uint32_t *num_vertices);
 
+/* ---- host-determined colliding shapes (rigid bodies that move; two-way coupling) ------------- */
+enum { JSB_MOTION_STATIC = 0, JSB_MOTION_KINEMATIC = 1, JSB_MOTION_DYNAMIC = 2 }; /* EMotionType */
+
+/* One colliding shape of a soft body, as SoftBodyMotionProperties::DetermineCollidingShapes collects it
+ * (SoftBodyMotionProperties.cpp:120-255; fields of CollidingShape and its LeafShape, SoftBodyMotionProperties.h):
+ * the adapter fills it from the same values inside PhysicsSystem's soft-body prepare job. Matrices are
+ * Jolt's Mat44 columns, xyz of each. */
+typedef struct jsb_colliding_shape {
+    int32_t type;             /* JSB_COLLIDER_*: the leaf shape (Box / Sphere / Capsule / Cylinder) */
+    int32_t motion_type;      /* JSB_MOTION_*: CollidingShape::mMotionType */
+    float transform[12];      /* LeafShape::mTransform (relative to the soft body): rotation columns 0-2, translation */
+    float half_extent[3];     /* box; [1] = half height of a capsule's cylinder part / a cylinder */
+    float radius;             /* sphere, capsule, cylinder */
+    float friction;           /* CollidingShape::mFriction (combined) */
+    float restitution;        /* CollidingShape::mRestitution (combined) */
+    float soft_body_inv_mass_scale; /* mSoftBodyInvMassScale (1 unless a contact listener changed it) */
+    float inv_mass;           /* dynamic: mInvMass */
+    float inv_inertia[12];    /* dynamic: mInvInertia, columns 0-3 */
+    float center_of_mass[3];  /* mCenterOfMassTransform's translation */
+    float linear_velocity[3]; /* dynamic: mLinearVelocity at the start of the step (soft-body space) */
+    float angular_velocity[3];/* dynamic: mAngularVelocity */
+} jsb_colliding_shape;
+
+/* Replaces the context's static colliders for one body with `count` (<= 16) host-determined shapes, in
+ * the order the reference collects them; they apply to every following step (each of its collision
+ * steps) until set again or cleared. Vertices on a dynamic shape take the dynamic-body branch of
+ * ApplyCollisionConstraintsAndUpdateVelocities (:752-797) in vertex order, such bodies walk their schedule
+ * substep by substep, and the shape's velocities change with each impulse. Not for bodies on the
+ * thread-block-cluster path, graphs (jsb_step_graph) or differentiable runs (JSB_ERR_UNSUPPORTED). */
+jsb_status jsb_body_set_colliding_shapes(jsb_context *ctx, uint32_t body_id, const jsb_colliding_shape *shapes, uint32_t count);
+jsb_status jsb_body_clear_colliding_shapes(jsb_context *ctx, uint32_t body_id);
+/* After a step (synchronises the device): per host-determined shape of the body, 7 floats {updated (1 when a
+ * contact changed the shape's velocities: CollidingShape::mUpdateVelocities), linear velocity[3], angular
+ * velocity[3]} in soft-body space; *count = the number of shapes. UpdateRigidBodyVelocities (:923-935) then
+ * adds the soft body's rotation times (velocity - the shape's input velocity) to the rigid body. */
+jsb_status jsb_body_shape_velocities(jsb_context *ctx, uint32_t body_id, float *out, uint32_t *count);
+
 /* ---- stepping ----------------------------------------------------------------------------- */
 /* PhysicsSystem::Update's soft-body part for every body in the context: InitializeUpdateContext,
  * DetermineCollidingShapes, DetermineCollisionPlanes, num_iterations x (pressure, integrate,

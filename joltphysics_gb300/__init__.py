@@ -43,6 +43,9 @@ SIGNATURES = {
     "jsb_body_is_active": [_P, _c.c_uint32, _c.POINTER(_c.c_int)],
     "jsb_body_set_active": [_P, _c.c_uint32, _c.c_int],
     "jsb_body_num_vertices": [_P, _c.c_uint32, _c.POINTER(_c.c_uint32)],
+    "jsb_body_set_colliding_shapes": [_P, _c.c_uint32, _c.c_char_p, _c.c_uint32],
+    "jsb_body_clear_colliding_shapes": [_P, _c.c_uint32],
+    "jsb_body_shape_velocities": [_P, _c.c_uint32, _P, _c.POINTER(_c.c_uint32)],
     "jsb_step": [_P, _c.c_float, _c.c_int, _P],
     "jsb_step_plain": [_P, _c.c_float, _c.c_int, _P],
     "jsb_step_graph": [_P, _c.c_float, _c.c_int, _c.c_int, _c.c_int, _P],
@@ -243,6 +246,21 @@ class Context:
 
     def set_active(self, body: int, active: bool):
         check(lib().jsb_body_set_active(self.h, body, 1 if active else 0))
+
+    def set_colliding_shapes(self, body: int, shapes: list[bytes] | None):
+        """Host-determined colliding shapes of a body (jsb_colliding_shape records, 172 bytes each), or None
+        to return it to the context's colliders."""
+        if shapes is None:
+            check(lib().jsb_body_clear_colliding_shapes(self.h, body))
+        else:
+            check(lib().jsb_body_set_colliding_shapes(self.h, body, b"".join(shapes), len(shapes)))
+
+    def shape_velocities(self, body: int) -> np.ndarray:
+        """Per host-determined shape after the last step: (updated, linear velocity[3], angular velocity[3])."""
+        out = np.zeros((16, 7), np.float32)
+        n = ctypes.c_uint32()
+        check(lib().jsb_body_shape_velocities(self.h, body, out.ctypes.data, ctypes.byref(n)))
+        return out[:n.value]
 
     # -- stepping --------------------------------------------------------------------------------
     def add_force(self, body: int, f):

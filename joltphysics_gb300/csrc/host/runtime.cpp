@@ -249,6 +249,13 @@ struct jsb_context {
     jsb::DevBuf<float> forces;  // per body: 3 floats consumed by the next step
     jsb::DevBuf<float> step_forces;  // per body: 3 floats applied before every step
     jsb::DevBuf<jsb::BodySleep> sleep;  // per body: sleep timer, active flag
+    std::map<uint32_t, std::vector<jsb::ShapeEntry>> table_host;  // host-determined colliding shapes by body
+    bool tables_dirty = false;
+    std::vector<int32_t> table_slot_host;
+    std::vector<jsb::ShapeTable> tables_staging;
+    jsb::DevBuf<jsb::ShapeTable> tables_dev;
+    jsb::DevBuf<int32_t> table_slot_dev;
+    jsb::DevBuf<int32_t> dyn_list;
     float sleep_velocity_threshold = 0.03f;  // PhysicsSettings::mPointVelocitySleepThreshold (PhysicsSettings.h:102)
     float time_before_sleep = 0.5f;          // PhysicsSettings::mTimeBeforeSleep (PhysicsSettings.h:95)
     std::vector<float> step_force_host;
@@ -659,7 +666,38 @@ StepParams base_params(jsb_context *ctx, float dt) {
     p.sleep = ctx->sleep.ptr;
     p.sleep_velocity_threshold = ctx->sleep_velocity_threshold;
     p.time_before_sleep = ctx->time_before_sleep;
+    const bool tables = !ctx->table_host.empty();
+    p.tables = tables ? ctx->tables_dev.ptr : nullptr;
+    p.table_slot = tables ? ctx->table_slot_dev.ptr : nullptr;
+    p.dyn_list = tables ? ctx->dyn_list.ptr : nullptr;
     return p;
+}
+
+// Host-determined colliding shapes set since the last step: one ShapeTable per body that has them
+// (slot order), uploaded on the step's stream ahead of its launches.
+jsb_status upload_tables(jsb_context *ctx, cudaStream_t stream) {
+    if (!ctx->tables_dirty) return JSB_OK;
+    ctx->table_slot_host.assign(ctx->bodies.size(), -1);
+    ctx->tables_staging.assign(ctx->table_host.size(), ShapeTable{});
+    int32_t slot = 0;
+    for (const auto &kv : ctx->table_host) {
+        ShapeTable &t = ctx->tables_staging[size_t(slot)];
+        t.count = uint32_t(kv.second.size());
+        for (size_t k = 0; k < kv.second.size(); ++k) t.e[k] = kv.second[k];
+        ctx->table_slot_host[kv.first] = slot++;
+    }
+    if (!ctx->tables_staging.empty()) {
+        JSB_CUDA(ctx->tables_dev.ensure(ctx->tables_staging.size()));
+        JSB_CUDA(cudaMemcpyAsync(ctx->tables_dev.ptr, ctx->tables_staging.data(), ctx->tables_staging.size() * sizeof(ShapeTable),
+                                 cudaMemcpyHostToDevice, stream));
+    }
+    JSB_CUDA(ctx->table_slot_dev.ensure(std::max<size_t>(ctx->table_slot_host.size(), 1)));
+    if (!ctx->table_slot_host.empty())
+        JSB_CUDA(cudaMemcpyAsync(ctx->table_slot_dev.ptr, ctx->table_slot_host.data(), ctx->table_slot_host.size() * sizeof(int32_t),
+                                 cudaMemcpyHostToDevice, stream));
+    JSB_CUDA(ctx->dyn_list.ensure(std::max<uint64_t>(ctx->total_vertices, 1)));
+    ctx->tables_dirty = false;
+    return JSB_OK;
 }
 
 // Enqueues one batched step (all launch groups) on `stream`.
@@ -703,6 +741,14 @@ jsb_status step_impl(jsb_context *ctx, float dt, int collision_steps, cudaStream
     if (!(dt > 0.0f) || collision_steps < 1) return fail(JSB_ERR_INVALID_ARGUMENT, "dt must be > 0 and collision_steps >= 1");
     jsb_status st = rebuild(ctx);
     if (st != JSB_OK) return st;
+    if (!ctx->table_host.empty()) {
+        for (const LaunchGroup &g : ctx->groups)
+            if (g.cluster > 0)
+                for (uint32_t b : g.bodies)
+                    if (ctx->table_host.count(b))
+                        return fail(JSB_ERR_UNSUPPORTED, "host-determined colliding shapes on a body of the thread-block-cluster path");
+    }
+    if ((st = upload_tables(ctx, stream)) != JSB_OK) return st;
     const float step_dt = dt / float(collision_steps);
     for (int c = 0; c < collision_steps; ++c) {
         bool uploaded = false;
@@ -973,6 +1019,52 @@ jsb_status jsb_set_sleep_settings(jsb_context *ctx, float time_before_sleep, flo
     return JSB_OK;
 }
 
+jsb_status jsb_body_set_colliding_shapes(jsb_context *ctx, uint32_t body_id, const jsb_colliding_shape *shapes, uint32_t count) {
+    static_assert(sizeof(jsb_colliding_shape) == sizeof(ShapeEntry), "jsb_colliding_shape and ShapeEntry share a layout");
+    if (!check_ctx(ctx) || body_id >= ctx->bodies.size() || (count && !shapes)) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    if (count > kMaxCollidingShapes) return fail(JSB_ERR_CAPACITY, "at most 16 colliding shapes per body");
+    std::vector<ShapeEntry> t(count);
+    for (uint32_t k = 0; k < count; ++k) {
+        if (shapes[k].type < JSB_COLLIDER_BOX || shapes[k].type > JSB_COLLIDER_CYLINDER)
+            return fail(JSB_ERR_INVALID_ARGUMENT, "unknown collider type");
+        if (shapes[k].motion_type < JSB_MOTION_STATIC || shapes[k].motion_type > JSB_MOTION_DYNAMIC)
+            return fail(JSB_ERR_INVALID_ARGUMENT, "unknown motion type");
+        std::memcpy(&t[k], &shapes[k], sizeof(ShapeEntry));
+    }
+    ctx->table_host[body_id] = std::move(t);
+    ctx->tables_dirty = true;
+    drop_graph(ctx);
+    return JSB_OK;
+}
+
+jsb_status jsb_body_clear_colliding_shapes(jsb_context *ctx, uint32_t body_id) {
+    if (!check_ctx(ctx) || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    if (ctx->table_host.erase(body_id)) ctx->tables_dirty = true;
+    return JSB_OK;
+}
+
+jsb_status jsb_body_shape_velocities(jsb_context *ctx, uint32_t body_id, float *out, uint32_t *count) {
+    if (!check_ctx(ctx) || body_id >= ctx->bodies.size() || !out || !count) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    auto it = ctx->table_host.find(body_id);
+    if (it == ctx->table_host.end() || ctx->tables_dirty || body_id >= ctx->table_slot_host.size() || ctx->table_slot_host[body_id] < 0)
+        return fail(JSB_ERR_INVALID_ARGUMENT, "the body has not been stepped with host-determined colliding shapes");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    JSB_CUDA(cudaDeviceSynchronize());
+    ShapeTable t;
+    JSB_CUDA(cudaMemcpy(&t, ctx->tables_dev.ptr + ctx->table_slot_host[body_id], sizeof(ShapeTable), cudaMemcpyDeviceToHost));
+    const bool dynamic = std::any_of(it->second.begin(), it->second.end(), [](const ShapeEntry &e) { return e.motion == kMotionDynamic; });
+    *count = t.count;
+    for (uint32_t k = 0; k < t.count; ++k) {
+        const ShapeEntry &e = it->second[k];
+        out[7 * k] = (t.updated >> k) & 1u ? 1.0f : 0.0f;
+        for (int j = 0; j < 3; ++j) {  // (bodies without a dynamic shape leave the outputs untouched)
+            out[7 * k + 1 + j] = dynamic ? t.lin[k][j] : e.lin[j];
+            out[7 * k + 4 + j] = dynamic ? t.ang[k][j] : e.ang[j];
+        }
+    }
+    return JSB_OK;
+}
+
 jsb_status jsb_body_is_active(jsb_context *ctx, uint32_t body_id, int *active) {
     if (!check_ctx(ctx) || !active || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
     JSB_CUDA(cudaSetDevice(ctx->device));
@@ -1033,6 +1125,8 @@ jsb_status jsb_step_graph(jsb_context *ctx, float dt, int collision_steps, int n
     if (st != JSB_OK) return st;
     if (ctx->forces_pending)
         return fail(JSB_ERR_INVALID_ARGUMENT, "pending AddForce: forces are consumed per step; use jsb_step for forced steps");
+    if (!ctx->table_host.empty())
+        return fail(JSB_ERR_UNSUPPORTED, "host-determined colliding shapes change every step; use jsb_step");
     cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
     uint32_t launches = 0;
     if (!ctx->graph_exec || ctx->graph_steps != num_steps || ctx->graph_dt != dt || ctx->graph_collision_steps != collision_steps) {
@@ -1574,6 +1668,8 @@ jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int chec
     if (st != JSB_OK) return st;
     if (ctx->forces_pending)
         return fail(JSB_ERR_INVALID_ARGUMENT, "one-shot AddForce cannot be differentiated; use jsb_body_set_step_force");
+    if (!ctx->table_host.empty())
+        return fail(JSB_ERR_UNSUPPORTED, "differentiable runs use the context's static colliders (no host-determined shapes)");
     for (size_t b = 0; b < ctx->bodies.size(); ++b)
         if (ctx->bodies[b].creation.allow_sleeping)
             return fail(JSB_ERR_UNSUPPORTED, "body " + std::to_string(b) + " may sleep (allow_sleeping), which differentiable runs do not model");

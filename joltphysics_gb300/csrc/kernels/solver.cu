@@ -42,7 +42,13 @@ struct Shared {
     int last_nan[6];
     float red[32][4];  // per-warp partials for reductions
     int redi[32][4];
+    int32_t table_slot;  // host-determined colliding shapes of the body (-1: the context's colliders)
+    int dynamic;         // a dynamic shape is among them
+    uint32_t ndyn;       // vertices whose shape is dynamic (their list is in StepParams::dyn_list)
+    uint32_t dyn_updated;
+    float dvel[kMaxCollidingShapes][6];  // the dynamic shapes' velocities during the step
 };
+static_assert(sizeof(Shared) + 256 <= 4096, "static shared memory of the solver kernels (the runtime reserves 4 KB)");
 
 
 // ---- state staging: bulk copies on the TMA unit, completion on an mbarrier ----------------------------
@@ -315,10 +321,22 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     const f3 body_pos = ld3(st->position);
     const f3 force = ld3(p.forces + 3 * size_t(b)) + ld3(p.step_forces + 3 * size_t(b));
 
-    // DetermineCollidingShapes: world AABB of (bounds U predicted bounds) grown by the vertex radius
+    // DetermineCollidingShapes: world AABB of (bounds U predicted bounds) grown by the vertex radius,
+    // or the shapes the host determined for the body
     if (tid == 0) {
-        const int n = colliding_shapes(p, d, st, body_pos, sh.cols);
+        const int32_t slot = p.table_slot ? p.table_slot[b] : -1;
+        bool dynamic = false;
+        const int n = slot >= 0 ? load_shape_table(p.tables + slot, sh.cols, dynamic) : colliding_shapes(p, d, st, body_pos, sh.cols);
         sh.ncols = n;
+        sh.table_slot = slot;
+        sh.dynamic = dynamic ? 1 : 0;
+        sh.dyn_updated = 0;
+        if (dynamic)
+            for (int k = 0; k < n; ++k)
+                for (int j = 0; j < 3; ++j) {
+                    sh.dvel[k][j] = p.tables[slot].e[k].lin[j];
+                    sh.dvel[k][3 + j] = p.tables[slot].e[k].ang[j];
+                }
         if (kTape)
             for (int k = 0; k < n; ++k)
                 td.cols[size_t(p.tape_step) * kMaxCollidingShapes + k] = make_float2(sh.cols[k].friction, sh.cols[k].restitution);
@@ -350,6 +368,7 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
 
     // DetermineCollisionPlanes (per vertex, once per step)
     const int ncols = sh.ncols;
+    const bool has_dynamic = sh.dynamic != 0;
     for (uint32_t i = tid; i < nv; i += T) {
         float4 pi = sx[i];
         int shape = -1;
@@ -366,6 +385,21 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
         }
     }
 
+    if (has_dynamic) {
+        // The dynamic-body branch carries the body's velocities from one vertex to the next in index
+        // order: list the vertices whose shape is dynamic (the shapes are fixed for the step).
+        __syncthreads();
+        if (tid == 0) {
+            int32_t *list = p.dyn_list + d.vtx_offset;
+            uint32_t n = 0;
+            for (uint32_t i = 0; i < nv; ++i) {
+                const int s = kSmemState ? __float_as_int(sv[i].w) : gshape[i];
+                if (s >= 0 && (sh.cols[s].flags & kColDynamic)) list[n++] = int32_t(i);
+            }
+            sh.ndyn = n;
+        }
+    }
+
     const float inv_dt_sq = 1.0f / (dt_sub * dt_sub);
     float damp = 1.0f - d.linear_damping * dt_sub;
     damp = damp < 0.0f ? 0.0f : damp;
@@ -376,7 +410,7 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     const bool has_pressure = d.pressure > 0.0f && d.num_faces > 0;
     // Whole-step walk: substep 0's integration below, then every substep's constraint levels with the
     // per-vertex passes between substeps inside the walk, then the last substep's velocity update.
-    const bool step_walk = d.step_levels != nullptr && !has_pressure && (!kTape || td.step_slots > 0);
+    const bool step_walk = d.step_levels != nullptr && !has_pressure && !has_dynamic && (!kTape || td.step_slots > 0);
     VertexPass vp{};
     if (step_walk) {
         vp.sv = sv;
@@ -496,6 +530,7 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
             f3 v = (x - xyz(prev)) / dt_sub;
             int shape = -1;
             if (ncols > 0) shape = kSmemState ? __float_as_int(vel.w) : gshape[i];
+            if (has_dynamic && shape >= 0 && (sh.cols[shape].flags & kColDynamic)) continue;  // below, in vertex order
             if (shape >= 0 && collide_vertex(x, v, prev_v, gplane[i], sh.cols[shape], d.vertex_radius, dt_sub, restitution_threshold))
                 sx[i] = with_w(x, pi.w);
             if (kSmemState)
@@ -504,6 +539,33 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
                 gv[i] = with_w(v, vel.w);
         }
         __syncthreads();
+        if (has_dynamic) {  // the vertices on dynamic shapes, one thread, in index order
+            if (tid == 0) {
+                const ShapeTable &tb = p.tables[sh.table_slot];
+                const int32_t *list = p.dyn_list + d.vtx_offset;
+                for (uint32_t k = 0; k < sh.ndyn; ++k) {
+                    const uint32_t i = uint32_t(list[k]);
+                    const float4 pi = sx[i];
+                    const float4 vel = kSmemState ? sv[i] : gv[i];
+                    const float4 prev = kSmemState ? sprev[i] : gprev[i];
+                    const int s = kSmemState ? __float_as_int(vel.w) : gshape[i];
+                    f3 x = xyz(pi), v = (x - xyz(prev)) / dt_sub;
+                    f3 lin = mk(sh.dvel[s][0], sh.dvel[s][1], sh.dvel[s][2]), ang = mk(sh.dvel[s][3], sh.dvel[s][4], sh.dvel[s][5]);
+                    if (collide_vertex_dynamic(x, v, xyz(vel), pi.w, gplane[i], tb.e[s], lin, ang, d.vertex_radius, dt_sub,
+                                               restitution_threshold)) {
+                        sh.dvel[s][0] = lin.x, sh.dvel[s][1] = lin.y, sh.dvel[s][2] = lin.z;
+                        sh.dvel[s][3] = ang.x, sh.dvel[s][4] = ang.y, sh.dvel[s][5] = ang.z;
+                        sh.dyn_updated |= 1u << s;
+                    }
+                    sx[i] = with_w(x, pi.w);
+                    if (kSmemState)
+                        sv[i] = with_w(v, vel.w);
+                    else
+                        gv[i] = with_w(v, vel.w);
+                }
+            }
+            __syncthreads();
+        }
     }
 
     // UpdateSoftBodyState
@@ -558,6 +620,15 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
                                            mk(bd.pm[0], bd.pm[1], bd.pm[2]), mk(bd.px[0], bd.px[1], bd.px[2]), sums, nvf);
         st3(sh.delta, delta);
         sleep_test(p, b, d, st, max_v_sq);
+        if (has_dynamic) {  // UpdateRigidBodyVelocities' inputs (:923-935) for the host
+            ShapeTable &tb = p.tables[sh.table_slot];
+            for (int k = 0; k < ncols; ++k)
+                for (int j = 0; j < 3; ++j) {
+                    tb.lin[k][j] = sh.dvel[k][j];
+                    tb.ang[k][j] = sh.dvel[k][3 + j];
+                }
+            tb.updated = sh.dyn_updated;
+        }
     }
     __syncthreads();
     const f3 delta = ld3(sh.delta);
@@ -771,6 +842,9 @@ __global__ void __launch_bounds__(T) step_kernel_noalloc(const __grid_constant__
     p.step_forces = q.zero3;
     p.ring_slots = kRingHalf;
     p.sleep = nullptr;  // (bodies that may sleep are refused by jsb_step_body_noalloc)
+    p.tables = nullptr;
+    p.table_slot = nullptr;
+    p.dyn_list = nullptr;
     if (threadIdx.x == 0) {
         stage_bar_init(&sh.stage_bar);
         stage_bar_init(&sh.ring_bar[0]);
