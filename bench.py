@@ -538,7 +538,8 @@ def bench_diff_cloth(jsb, steps: int = 120, every: int = 10) -> dict:
 
 def profile_driver(args) -> None:
     """A bare step loop of one workload for ncu captures (warm-up steps, then the captured steps):
-    uneven_batch and large_cloth run batched steps on the default stream; diff_batch_adjoint runs a
+    uneven_batch (uneven_batch_quarter: a quarter of its bodies), large_cloth and pinned_cloth run
+    batched steps on the default stream; diff_batch_adjoint runs a
     forward+adjoint pass of `--steps` steps of the differentiable batch (checkpoint every 5)."""
     import joltphysics_gb300 as jsb
 
@@ -555,7 +556,10 @@ def profile_driver(args) -> None:
         ctx.synchronize()
         return
     ctx = jsb.Context(0)
-    ctx.load_scene(build_scene(args.profile))
+    if args.profile == "uneven_batch_quarter":  # 96 cloths and 32 cubes of the same distributions
+        ctx.load_scene(build_scene("uneven_batch", n_cloth=96, n_cube=32))
+    else:
+        ctx.load_scene(build_scene(args.profile))
     for mv, threads, mode in json.loads(args.table or "[]"):
         ctx.set_bucket_config(mv, threads, mode)
     for _ in range(args.warmup + args.steps):
@@ -578,7 +582,7 @@ def main():
                     help="skip the gradient checks at the two differentiable configurations (about 90 s of CPU)")
     ap.add_argument("--table", help="profiling driver: launch-shape table [[max_vertices, threads, state_mode], ...] "
                                     "(e.g. the bench line's config.buckets_max_vertices_threads_state)")
-    ap.add_argument("--profile", choices=["uneven_batch", "large_cloth", "diff_batch_adjoint"],
+    ap.add_argument("--profile", choices=["uneven_batch", "uneven_batch_quarter", "large_cloth", "pinned_cloth", "diff_batch_adjoint"],
                     help="profiling driver for ncu: run --warmup then --steps steps of one workload, print nothing")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
