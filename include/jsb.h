@@ -267,9 +267,11 @@ jsb_status jsb_body_set_compliance(jsb_context *ctx, uint32_t body_id, const flo
  * segment with a tape and reverses it (collision active set frozen) and leaves the context at the
  * forward run's final state; jsb_adjoint_gradients returns d loss / d initial positions and
  * velocities (3 floats per vertex), d loss / d the body's step force (3 floats, jsb_body_set_step_force)
- * and d loss / d each edge and volume compliance (settings order); any output may be NULL.
- * Bodies with dihedral bends are rejected (JSB_ERR_UNSUPPORTED): the reference's ACosApproximate is not
- * differentiable at flat triangle pairs. Positions and the body position are related by the body's
+ * and d loss / d each edge and volume compliance (settings order); any output may be NULL
+ * (jsb_adjoint_bend_gradients: d loss / d each dihedral bend's compliance). Dihedral bends are
+ * differentiated through their signed angle: C = ACosApproximate-based angle - initial angle is smooth
+ * in the angle, so the derivative stays bounded at flat triangle pairs, where ACosApproximate's own
+ * derivative is not (it is the limit of the derivative there). Positions and the body position are related by the body's
  * recentering, which leaves world positions unchanged; the adjoint is taken in world coordinates. */
 jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int checkpoint_every);
 jsb_status jsb_adjoint_forward(jsb_context *ctx, int until_step); /* -1 = all num_steps; may be called in pieces */
@@ -282,6 +284,7 @@ jsb_status jsb_adjoint_seed_all(jsb_context *ctx, int step, const float *dl_dx);
 jsb_status jsb_adjoint_gradients_all(jsb_context *ctx, float *dl_dx0, float *dl_dv0, float *dl_dforce);
 jsb_status jsb_adjoint_gradients(jsb_context *ctx, uint32_t body_id, float *dl_dx0, float *dl_dv0, float *dl_dforce,
                                  float *dl_dedge_compliance, float *dl_dvolume_compliance);
+jsb_status jsb_adjoint_bend_gradients(jsb_context *ctx, uint32_t body_id, float *dl_dbend_compliance);
 /* Ends the run. Its device buffers (tape, checkpoints, adjoints) stay with the context and are reused,
  * grown when needed, by its next differentiable run; jsb_context_destroy frees them. */
 jsb_status jsb_adjoint_end(jsb_context *ctx);

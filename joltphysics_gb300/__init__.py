@@ -44,6 +44,7 @@ SIGNATURES = {
     "jsb_body_set_active": [_P, _c.c_uint32, _c.c_int],
     "jsb_body_num_vertices": [_P, _c.c_uint32, _c.POINTER(_c.c_uint32)],
     "jsb_body_set_colliding_shapes": [_P, _c.c_uint32, _c.c_char_p, _c.c_uint32],
+    "jsb_adjoint_bend_gradients": [_P, _c.c_uint32, _P],
     "jsb_body_clear_colliding_shapes": [_P, _c.c_uint32],
     "jsb_body_shape_velocities": [_P, _c.c_uint32, _P, _c.POINTER(_c.c_uint32)],
     "jsb_step": [_P, _c.c_float, _c.c_int, _P],
@@ -423,6 +424,13 @@ class Context:
         check(lib().jsb_adjoint_gradients(self.h, body, dx.ctypes.data, dv.ctypes.data, df.ctypes.data,
                                           de.ctypes.data if num_edges else None, dvol.ctypes.data if num_volumes else None))
         return {"x0": dx, "v0": dv, "force": df, "edge_compliance": de, "volume_compliance": dvol}
+
+    def adjoint_bend_gradients(self, body: int, num_bends: int) -> np.ndarray:
+        """d loss / d each dihedral bend's compliance (settings order) after adjoint_backward."""
+        out = np.zeros(num_bends, np.float32)
+        if num_bends:
+            check(lib().jsb_adjoint_bend_gradients(self.h, body, out.ctypes.data))
+        return out
 
     def adjoint_end(self):
         check(lib().jsb_adjoint_end(self.h))

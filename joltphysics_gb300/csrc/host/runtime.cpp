@@ -1673,10 +1673,6 @@ jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int chec
     for (size_t b = 0; b < ctx->bodies.size(); ++b)
         if (ctx->bodies[b].creation.allow_sleeping)
             return fail(JSB_ERR_UNSUPPORTED, "body " + std::to_string(b) + " may sleep (allow_sleeping), which differentiable runs do not model");
-    for (size_t b = 0; b < ctx->bodies.size(); ++b)
-        if (!ctx->settings[ctx->bodies[b].settings_id]->parsed.bends.empty())
-            return fail(JSB_ERR_UNSUPPORTED, "body " + std::to_string(b) +
-                                                 " has dihedral bend constraints, which differentiable runs do not support");
     // Reuse the device buffers of the context's previous differentiable run (tape, checkpoints, adjoints):
     // allocating gigabytes of tape costs time every run otherwise.
     auto a = std::make_unique<AdjointSession>();
@@ -1990,6 +1986,32 @@ jsb_status jsb_adjoint_gradients(jsb_context *ctx, uint32_t body_id, float *dl_d
             if (type == kEdge && dl_dedge_compliance) dl_dedge_compliance[idx] += g[c];
             if (type == kVolume && dl_dvolume_compliance) dl_dvolume_compliance[idx] += g[c];
         }
+    }
+    return JSB_OK;
+}
+
+jsb_status jsb_adjoint_bend_gradients(jsb_context *ctx, uint32_t body_id, float *dl_dbend_compliance) {
+    if (!check_ctx(ctx) || !ctx->adjoint || body_id >= ctx->bodies.size() || !dl_dbend_compliance)
+        return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument or no differentiable run");
+    AdjointSession &a = *ctx->adjoint;
+    if (!a.backward_done) return fail(JSB_ERR_INVALID_ARGUMENT, "jsb_adjoint_backward has not run");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    JSB_CUDA(cudaDeviceSynchronize());
+    const BodyRec &b = ctx->bodies[body_id];
+    const SettingsRec &s = *ctx->settings[b.settings_id];
+    const uint32_t step_slots = a.step_slots[body_id];
+    StepSchedule steps;
+    if (step_slots && (!build_step_schedule(s.parsed, b.creation.num_iterations, steps, true) || steps.num_slots != step_slots))
+        return fail(JSB_ERR_CAPACITY, "whole-step schedule rebuild failed");
+    const std::vector<uint32_t> &source = step_slots ? steps.source : s.schedule.padded_source;
+    const size_t stride = step_slots ? 2 : 1;
+    std::vector<float> g(step_slots ? step_slots : s.schedule.num_slots);
+    if (!g.empty())
+        JSB_CUDA(cudaMemcpy(g.data(), a.grad_slots.ptr + a.slot_offset[body_id], g.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    std::fill(dl_dbend_compliance, dl_dbend_compliance + s.parsed.bends.size(), 0.0f);
+    for (size_t c = 0; c < g.size(); ++c) {
+        const uint32_t src = source[c * stride];
+        if (src != 0xffffffffu && (src >> 28) == kBend) dl_dbend_compliance[src & 0x0fffffffu] += g[c];
     }
     return JSB_OK;
 }

@@ -5,7 +5,8 @@
 //   ApplyCollisionConstraintsAndUpdateVelocities (SoftBodyMotionProperties.cpp:700-825), with the
 //     collision active set frozen: the plane, shape index and the contact / friction-clamp /
 //     restitution branch decisions are those of the forward pass
-//   the constraint levels in reverse order (edge :573-601, tetra volume :458-507, LRA :679-698)
+//   the constraint levels in reverse order (dihedral bend :367-456, edge :573-601, tetra volume
+//     :458-507, LRA :679-698)
 //   IntegratePositions (:325-365), accumulating d loss / d force
 //   ApplyPressure (:291-323)
 // Recentering of the body (UpdateSoftBodyState :882-898) moves local positions and the body
@@ -14,7 +15,8 @@
 // The forward values each reverse stage needs come from the tape written by the taped forward step
 // (constraint inputs, substep states, collision planes). Constraints of one level write disjoint
 // vertices, so their reverse projections also run concurrently between barriers; an LRA anchor is only
-// read, and the adjoint contributions of several LRA constraints to one anchor are added atomically.
+// read, and the adjoint contributions of several LRA constraints to one anchor are summed after the
+// level in a fixed order (lra_anchor_sums).
 // d loss / d compliance accumulates per schedule slot; a slot is reversed by the same thread in every
 // substep, so the accumulation is race free and deterministic.
 //
@@ -23,8 +25,8 @@
 // of the substep the vertex entered and the velocity update of the one it left, then substep 0's
 // integration. The taped forward step records the same substep states either way.
 //
-// Dihedral bends are not differentiated (the runtime rejects differentiable runs of bodies with
-// bends): the reference's ACosApproximate has an unbounded derivative at flat triangle pairs.
+// Dihedral bends are differentiated through their signed angle (bend_adjoint), which keeps the
+// derivative bounded at flat triangle pairs.
 
 #include <cuda_runtime.h>
 #include <float.h>
@@ -101,6 +103,104 @@ __device__ __forceinline__ void volume_adjoint(float4 *lx, const float *sw, uint
     lx[i2] = with_w(L2 + la, 0.0f);
     lx[i3] = with_w(L3 + lb, 0.0f);
     lx[i4] = with_w(L4 + lcv, 0.0f);
+}
+
+// Dihedral bend (:367-456). The reference's constraint gradients d_i are exactly the gradients of the
+// signed dihedral angle theta = atan2(((n2 x n1) . e) / |e|, n1 . n2) (|theta| = acos(n1 . n2 / |n1||n2|),
+// its sign the reference's `sign`), and C = F(theta) - initial angle with F(theta) = sign(theta)
+// ACosApproximate(cos |theta|). F is smooth in theta, flat triangle pairs included (there
+// ACosApproximate's own derivative is unbounded but cos' vanishes), with
+//   F'(theta) = h p / sqrt(2) + 0.175394 s sin|theta|,
+//   cos|theta| >= 0: s = sqrt(1 - cos), p = pi/2 - 0.175394 cos, h = cos(|theta| / 2) = sqrt((1 + cos) / 2)
+//   cos|theta| <  0: s = sqrt(1 + cos), p = pi/2 + 0.175394 cos, h = sin(|theta| / 2) = sqrt((1 - cos) / 2).
+// So dC/dx_i = F'(theta) d_i. The map x_i' = x_i - ml w_i d_i, ml = C / (sum w_j |d_j|^2 + alpha k), is
+// reversed through ml, C, the denominator and the d_i themselves (d0 = (((x2 - x1) . e) n1 / |n1|^2 +
+// ((x3 - x1) . e) n2 / |n2|^2) / |e|, d2 = |e| n1 / |n1|^2, d3 = |e| n2 / |n2|^2, d1 = -d0 - d2 - d3,
+// n1 = (x2 - x0) x (x2 - x1), n2 = (x3 - x1) x (x3 - x0), e = x1 - x0). Where the forward skipped the
+// projection (|e| < 1e-6, |n1|^2 |n2|^2 < 1e-24, denominator < 1e-12) the adjoint passes through.
+// Taped inputs: x1 - x0, x2 - x0, x3 - x0.
+__device__ __forceinline__ void bend_adjoint(float4 *lx, const float *sw, uint4 r, const float4 *tin, float inv_dt_sq, float *grad) {
+    const uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16, i2 = r.y & 0xffff, i3 = r.y >> 16;
+    const float w[4] = {sw[i0], sw[i1], sw[i2], sw[i3]};
+    const float alpha = __uint_as_float(r.z), angle = __uint_as_float(r.w);
+    const f3 x1 = xyz(tin[0]), x2 = xyz(tin[1]), x3 = xyz(tin[2]);  // x0 = 0
+    const f3 e = x1;
+    const float el = len(e);
+    if (el < 1.0e-6f) return;
+    const f3 x1x2 = x2 - x1, x1x3 = x3 - x1;
+    const f3 n1 = cross(x2, x1x2), n2 = cross(x1x3, x3);
+    const float n1s = len_sq(n1), n2s = len_sq(n2), n1n2 = n1s * n2s;
+    if (n1n2 < 1.0e-24f) return;
+    const float sgn = dot(cross(n2, n1), e) < 0.0f ? -1.0f : 1.0f;
+    float d = dot(n1, n2) / sqrtf(n1n2);
+    float c = sgn * acos_approximate(d) - angle;
+    if (c > kPi)
+        c -= 2.0f * kPi;
+    else if (c < -kPi)
+        c += 2.0f * kPi;
+    const f3 n1h = n1 / n1s, n2h = n2 / n2s;
+    const float A = dot(x1x2, e), B = dot(x1x3, e);
+    const f3 u = A * n1h + B * n2h;
+    f3 D[4];
+    D[0] = u / el;
+    D[2] = el * n1h;
+    D[3] = el * n2h;
+    D[1] = (neg(D[0]) - D[2]) - D[3];
+    const float den = w[0] * len_sq(D[0]) + w[1] * len_sq(D[1]) + w[2] * len_sq(D[2]) + w[3] * len_sq(D[3]) + alpha * inv_dt_sq;
+    if (den < 1.0e-12f) return;
+    const float ml = c / den;
+    const uint32_t idx[4] = {i0, i1, i2, i3};
+    f3 L[4], xb[4], Db[4];
+    float mlb = 0.0f;
+    for (int i = 0; i < 4; ++i) {
+        L[i] = xyz(lx[idx[i]]);
+        xb[i] = L[i];
+        mlb -= w[i] * dot(L[i], D[i]);
+    }
+    const float cb = mlb / den, denb = -mlb * ml / den;
+    *grad += denb * inv_dt_sq;
+    // dC/dtheta
+    d = fminf(1.0f, fmaxf(-1.0f, d));
+    const float sinphi = sqrtf(fmaxf(0.0f, 1.0f - d * d));
+    float s, pp, h;
+    if (d >= 0.0f) {
+        s = sqrtf(1.0f - d);
+        pp = kPi / 2 - 0.175394f * d;
+        h = sqrtf(0.5f * (1.0f + d));
+    } else {
+        s = sqrtf(1.0f + d);
+        pp = kPi / 2 + 0.175394f * d;
+        h = sqrtf(0.5f * (1.0f - d));
+    }
+    const float thb = cb * (h * pp * 0.70710678f + 0.175394f * s * sinphi);
+    for (int i = 0; i < 4; ++i) {
+        Db[i] = (-ml * w[i]) * L[i] + (2.0f * w[i] * denb) * D[i];
+        xb[i] = xb[i] + thb * D[i];
+    }
+    // through d1 = -d0 - d2 - d3, d2 = el n1h, d3 = el n2h, d0 = u / el
+    Db[0] = Db[0] - Db[1];
+    Db[2] = Db[2] - Db[1];
+    Db[3] = Db[3] - Db[1];
+    float elb = dot(Db[2], n1h) + dot(Db[3], n2h) - dot(Db[0], D[0]) / el;
+    const f3 ub = Db[0] / el;
+    const float Ab = dot(ub, n1h), Bb = dot(ub, n2h);
+    const f3 n1hb = el * Db[2] + A * ub, n2hb = el * Db[3] + B * ub;
+    f3 x1x2b = Ab * e, x1x3b = Bb * e;
+    f3 eb = Ab * x1x2 + Bb * x1x3;
+    // n_h = n / |n|^2
+    const f3 n1b = n1hb / n1s + (2.0f * (-dot(n1hb, n1h) / n1s)) * n1;
+    const f3 n2b = n2hb / n2s + (2.0f * (-dot(n2hb, n2h) / n2s)) * n2;
+    eb = eb + (elb / el) * e;
+    // n1 = (x2 - x0) x x1x2, n2 = x1x3 x (x3 - x0)
+    const f3 Pb = cross(x1x2, n1b);
+    x1x2b = x1x2b + cross(n1b, x2);
+    x1x3b = x1x3b + cross(x3, n2b);
+    const f3 Vb = cross(n2b, x1x3);
+    xb[2] = xb[2] + Pb + x1x2b;
+    xb[3] = xb[3] + Vb + x1x3b;
+    xb[1] = xb[1] - x1x2b - x1x3b + eb;
+    xb[0] = xb[0] - Pb - Vb - eb;
+    for (int i = 0; i < 4; ++i) lx[idx[i]] = with_w(xb[i], 0.0f);
 }
 
 // x1' = x0 + d md / |d| when |d| > md (d = x1 - x0); the anchor x0 is only read. The anchor's term is
@@ -209,7 +309,7 @@ __device__ __forceinline__ void reverse_levels(float4 *lx, const float *sw, cons
             const float4 *src = cons + size_t(c) * 3;
             adj_cp_async16(dst, rec + c);
             adj_cp_async16(dst + T, src);
-            if (adj_slot_type(lv, s) == 1) {
+            if (adj_slot_type(lv, s) <= 1) {
                 adj_cp_async16(dst + 2 * T, src + 1);
                 adj_cp_async16(dst + 3 * T, src + 2);
             }
@@ -238,7 +338,7 @@ __device__ __forceinline__ void reverse_levels(float4 *lx, const float *sw, cons
                 const uint4 *src = slot(uint32_t(l), k);
                 r = src[0];
                 tin[0] = *reinterpret_cast<const float4 *>(src + T);
-                if (type == 1) {
+                if (type <= 1) {
                     tin[1] = *reinterpret_cast<const float4 *>(src + 2 * T);
                     tin[2] = *reinterpret_cast<const float4 *>(src + 3 * T);
                 }
@@ -246,7 +346,7 @@ __device__ __forceinline__ void reverse_levels(float4 *lx, const float *sw, cons
                 r = __ldg(rec + c);
                 const float4 *src = cons + size_t(c) * 3;
                 tin[0] = src[0];
-                if (type == 1) {
+                if (type <= 1) {
                     tin[1] = src[1];
                     tin[2] = src[2];
                 }
@@ -254,6 +354,8 @@ __device__ __forceinline__ void reverse_levels(float4 *lx, const float *sw, cons
             if (r.x == 0xffffffffu) continue;
             if (type == 2)
                 edge_adjoint(lx, sw, r, tin, inv_dt_sq, grad + c);
+            else if (type == 0)
+                bend_adjoint(lx, sw, r, tin, inv_dt_sq, grad + c);
             else if (type == 1)
                 volume_adjoint(lx, sw, r, tin, inv_dt_sq, grad + c);
             else if (type == 3)
@@ -411,7 +513,7 @@ __device__ __forceinline__ void reverse_step_levels(const VertexAdj &a, const Bo
             if (type == 4) continue;
             const float4 *src = cons + size_t(c) * 3;
             adj_cp_async16(dst + T, src);
-            if (type == 1) {
+            if (type <= 1) {
                 adj_cp_async16(dst + 2 * T, src + 1);
                 adj_cp_async16(dst + 3 * T, src + 2);
             }
@@ -441,7 +543,7 @@ __device__ __forceinline__ void reverse_step_levels(const VertexAdj &a, const Bo
                 r = src[0];
                 if (type != 4) {
                     tin[0] = *reinterpret_cast<const float4 *>(src + T);
-                    if (type == 1) {
+                    if (type <= 1) {
                         tin[1] = *reinterpret_cast<const float4 *>(src + 2 * T);
                         tin[2] = *reinterpret_cast<const float4 *>(src + 3 * T);
                     }
@@ -451,7 +553,7 @@ __device__ __forceinline__ void reverse_step_levels(const VertexAdj &a, const Bo
                 if (type != 4) {
                     const float4 *src = cons + size_t(c) * 3;
                     tin[0] = src[0];
-                    if (type == 1) {
+                    if (type <= 1) {
                         tin[1] = src[1];
                         tin[2] = src[2];
                     }
@@ -463,6 +565,8 @@ __device__ __forceinline__ void reverse_step_levels(const VertexAdj &a, const Bo
                 velocity_adjoint(a, r.x, r.y - 1);
             } else if (type == 2) {
                 edge_adjoint(a.lx, a.sw, r, tin, inv_dt_sq, grad + c);
+            } else if (type == 0) {
+                bend_adjoint(a.lx, a.sw, r, tin, inv_dt_sq, grad + c);
             } else if (type == 1) {
                 volume_adjoint(a.lx, a.sw, r, tin, inv_dt_sq, grad + c);
             } else if (type == 3) {

@@ -15,7 +15,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from jsb_testlib import blob_arrays, blob_compliance, parse_scene, record32, run64, single_body_scene
+from jsb_testlib import blob_arrays, blob_bend_compliance, blob_compliance, parse_scene, record32, run64, single_body_scene
 
 
 def rel(a, b) -> float:
@@ -67,6 +67,7 @@ def cloth_adjoint(jsb, scene_bytes, steps, every, targets, trajectory=None):
         ctx.adjoint_seed(s, 0, (2.0 * (world[s] - t) / m).astype(np.float32))
     ctx.adjoint_backward()
     g = ctx.adjoint_gradients(0, num_edges=len(blob_compliance(scene.bodies[0].blob)[0]))
+    g["bend_compliance"] = ctx.adjoint_bend_gradients(0, len(blob_bend_compliance(scene.bodies[0].blob)))
     ctx.adjoint_end()
     ctx.close()
     return g, loss
@@ -84,7 +85,9 @@ def cloth_pinned_reference(scene, targets, trajectory):
     m = 3.0 * scene.bodies[0].num_vertices * len(targets)
     loss = sum(((out[s][0] - torch.tensor(t)) ** 2).sum() for s, t in targets.items()) / m
     loss.backward()
-    return {"edge": params[0]["edge"].grad.numpy(), "v0": params[0]["v0"].grad.numpy()}, float(loss)
+    bend = params[0]["bend"].grad
+    return ({"edge": params[0]["edge"].grad.numpy(), "v0": params[0]["v0"].grad.numpy(),
+             "bend": bend.numpy() if bend is not None else np.zeros(0)}, float(loss.detach()))
 
 
 def cloth_params(scene, rng, count=32):
@@ -130,10 +133,11 @@ def pick(g, params) -> tuple[np.ndarray, np.ndarray]:
     return e, v
 
 
-def diff_cloth_check(jsb, build_scene, steps=120, every=10, loss_steps=(60, 120), fd_params=32, pinned=True) -> dict:
+def diff_cloth_check(jsb, build_scene, steps=120, every=10, loss_steps=(60, 120), fd_params=32, pinned=True, bends=False) -> dict:
     """Relative errors of the GPU gradients: against FP64 autodiff along the GPU trajectory (pinned) and
-    against free-running FP64 central differences on `fd_params` random parameters."""
-    scene_bytes = build_scene("diff_cloth", steps=steps)
+    against free-running FP64 central differences on `fd_params` random parameters. bends: the same
+    cloth with dihedral bends (then also d loss / d bend compliance against the pinned autodiff)."""
+    scene_bytes = build_scene("diff_cloth", steps=steps, bends=int(bends))
     scene, _ = parse_scene(scene_bytes)
     targets = cloth_target(jsb, scene_bytes, loss_steps)
     traj = {} if pinned else None
@@ -143,6 +147,8 @@ def diff_cloth_check(jsb, build_scene, steps=120, every=10, loss_steps=(60, 120)
         ref, ref_loss = cloth_pinned_reference(scene, targets, traj)
         out["pinned_fp64_autodiff"] = {"edge_compliance": rel(g["edge_compliance"], ref["edge"]), "v0": rel(g["v0"], ref["v0"]),
                                        "loss_rel": abs(ref_loss - loss) / abs(loss)}
+        if bends:
+            out["pinned_fp64_autodiff"]["bend_compliance"] = rel(g["bend_compliance"], ref["bend"])
     if fd_params:
         params = cloth_params(scene, np.random.default_rng(4))
         fd = cloth_fd(scene, targets, params)

@@ -342,6 +342,16 @@ def blob_compliance(blob: bytes):
     return edges, vols
 
 
+def blob_bend_compliance(blob: bytes) -> np.ndarray:
+    """Dihedral bend compliance array (settings order) of a settings blob."""
+    off = 0
+    for size in (28, 16, 16):  # vertices, faces, edges
+        (n,) = struct.unpack_from("<I", blob, off)
+        off += 4 + n * size
+    (nb,) = struct.unpack_from("<I", blob, off)
+    return np.frombuffer(blob, np.float32, 6 * nb, off + 4).reshape(nb, 6)[:, 4].astype(np.float64) if nb else np.zeros(0)
+
+
 class FD64:
     """Linear functionals of the FP64 oracle trajectory, for central finite differences.
 

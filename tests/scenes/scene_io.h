@@ -96,7 +96,7 @@ inline bool make_named_scene(const std::string &name, const std::string &params,
     else if (name == "large_cloth")
         out = make_large_cloth(uint32_t(geti("n", 256)), int(geti("steps", 600)), geti("bends", 1) != 0);
     else if (name == "diff_cloth")
-        out = make_diff_cloth(uint64_t(geti("seed", 4)), uint32_t(geti("n", 64)), int(geti("steps", 120)));
+        out = make_diff_cloth(uint64_t(geti("seed", 4)), uint32_t(geti("n", 64)), int(geti("steps", 120)), geti("bends", 0) != 0);
     else if (name == "diff_batch")
         out = make_diff_batch(uint64_t(geti("seed", 5)), uint32_t(geti("n_cloth", 192)), uint32_t(geti("n_cube", 64)),
                               int(geti("steps", 90)), float(geti("drop_mm", 1000)) * 0.001f);

@@ -427,16 +427,15 @@ inline SceneSpec make_large_cloth(uint32_t n = 256, int steps = 600, bool bends 
 }
 
 // Differentiable single cloth: n x n (default 64), 0.05 m spacing, top row (z = n-1) pinned, edges
-// only (no bend constraints: the dihedral angle function has an unbounded derivative at flat
-// configurations), per-edge compliance log-U[1e-6, 1e-4] assigned in optimized edge order, initial
+// only (bends = true adds dihedral bends of compliance 1e-4), per-edge compliance log-U[1e-6, 1e-4] assigned in optimized edge order, initial
 // velocities N(0, 0.1) m/s per component; 120 steps.
-inline SceneSpec make_diff_cloth(uint64_t seed = 4, uint32_t n = 64, int steps = 120) {
+inline SceneSpec make_diff_cloth(uint64_t seed = 4, uint32_t n = 64, int steps = 120, bool bends = false) {
     SceneSpec s;
     Rng rng(seed);
     BodySpec b;
     b.mesh = make_cloth(n, n, 0.05f, [n](uint32_t, uint32_t z) { return z == n - 1; });
-    b.mesh.attributes = VertexAttributes{1.0e-5f, 1.0e-5f, 3.402823466e+38f};
-    b.mesh.bend_type = BendType::None;
+    b.mesh.attributes = VertexAttributes{1.0e-5f, 1.0e-5f, bends ? 1.0e-4f : 3.402823466e+38f};
+    b.mesh.bend_type = bends ? BendType::Dihedral : BendType::None;
     for (size_t v = 0; v < b.mesh.velocities.size(); ++v)
         for (int k = 0; k < 3; ++k) b.mesh.velocities[v][k] = float(0.1 * rng.normal());
     b.position[1] = 2.0f;

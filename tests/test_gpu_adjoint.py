@@ -86,6 +86,46 @@ def test_adjoint_cloth_vs_fd(jsb):
     assert max(e for _, _, e, _, _ in errs) <= 1e-3, [(k, e) for k, _, e, _, _ in errs]
 
 
+def test_adjoint_cloth_with_bends_vs_fd(jsb):
+    """A 10 x 10 cloth with dihedral bends (flat at the start: the bend adjoint goes through the signed
+    angle, bounded at flat pairs), 16 steps: positions, velocities, edge compliances and force against
+    FP64 central differences, and bend compliances against FP64 autodiff (pinned to the GPU trajectory),
+    1e-3."""
+    from torch_ref import reference_gradients
+
+    scene_bytes = build_scene("diff_cloth", n=10, steps=16, bends=1)
+    scene, _ = parse_scene(scene_bytes)
+    rng = np.random.default_rng(9)
+    nv = scene.bodies[0].num_vertices
+    seeds = {8: {0: rng.standard_normal((nv, 3))}, 16: {0: rng.standard_normal((nv, 3))}}
+    force = {0: np.array([0.3, -0.2, 0.1], np.float32)}
+    traj = {}
+    grads = gpu_gradients(jsb, scene_bytes, seeds, 16, 5, force, trajectory=traj)
+    scene.bodies[0].force = tuple(float(v) for v in force[0])
+    fd = FD64(scene, seeds, 16)
+    errs = sample_and_compare(fd, grads, [(0, "x0", 10), (0, "v0", 10), (0, "edge", 9), (0, "force", 3)], rng)
+    for kind, body, e, fds, gps in errs:
+        print(kind, body, "rel", e, "\n  fd ", fds, "\n  gpu", gps)
+    assert max(e for _, _, e, _, _ in errs) <= 1e-3, [(k, e) for k, _, e, _, _ in errs]
+    ctx = jsb.Context(0)  # bend compliance gradients of the same run
+    ctx.load_scene(scene_bytes)
+    ctx.set_step_force(0, force[0])
+    ctx.adjoint_begin(16, 5)
+    ctx.adjoint_forward()
+    for step, per_body in seeds.items():
+        ctx.adjoint_seed(step, 0, per_body[0].astype(np.float32))
+    ctx.adjoint_backward()
+    from jsb_testlib import blob_bend_compliance
+
+    gb = ctx.adjoint_bend_gradients(0, len(blob_bend_compliance(scene.bodies[0].blob))).astype(np.float64)
+    ctx.adjoint_end()
+    ctx.close()
+    ref, _ = reference_gradients(scene, seeds, 16, traj)
+    e = np.linalg.norm(gb - ref[0]["bend"]) / np.linalg.norm(ref[0]["bend"])
+    print("bend compliance rel", e)
+    assert e <= 1e-3, e
+
+
 def contact_scene(jsb):
     """A cloth and a pressurised tet cube dropped 0.15 m onto the floor, with step forces."""
     return build_scene("diff_batch", n_cloth=1, n_cube=1, steps=24, drop_mm=150, seed=23)

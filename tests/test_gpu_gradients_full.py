@@ -45,6 +45,16 @@ def test_diff_cloth_gradients_along_trajectory(jsb):
     assert p["edge_compliance"] <= 1e-3 and p["v0"] <= 1e-3, p
 
 
+def test_diff_cloth_with_bends_gradients_along_trajectory(jsb):
+    """The differentiable cloth with dihedral bends (compliance 1e-4), full size and length: edge and bend
+    compliance and initial-velocity gradients against FP64 autodiff along the GPU trajectory, 1e-3."""
+    r = diff_cloth_check(jsb, build_scene, fd_params=0, bends=True)
+    print("diff_cloth with bends, 120 steps:", r)
+    p = r["pinned_fp64_autodiff"]
+    assert p["loss_rel"] <= 1e-6
+    assert p["edge_compliance"] <= 1e-3 and p["v0"] <= 1e-3 and p["bend_compliance"] <= 1e-3, p
+
+
 def test_diff_cloth_gradients_vs_fd_short_horizon(jsb):
     r = diff_cloth_check(jsb, build_scene, steps=6, every=2, loss_steps=(3, 6), pinned=False)
     print("diff_cloth, 6 steps:", r)

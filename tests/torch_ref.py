@@ -1,7 +1,8 @@
 """Plain FP64 re-implementation of the soft-body step in torch, for reference gradients by autodiff.
 
 TEST INFRASTRUCTURE. It restates the same step as the CPU oracle (SoftBodyMotionProperties.cpp:
-pressure :291-323, integration :325-365, edge :573-601 / volume :458-507 / LRA :679-698 projections in
+pressure :291-323, integration :325-365, dihedral bend :367-456 (through the signed angle, smooth at
+flat triangle pairs), edge :573-601 / volume :458-507 / LRA :679-698 projections in
 update-group order, collision + velocity update :700-825 against static boxes and spheres, velocity clamp
 :827-921) in float64 with autograd. Collision planes are computed at the start of every step without
 gradient (the collision active set is frozen, as in the GPU adjoint). Constraints are applied level by
@@ -15,9 +16,11 @@ import numpy as np
 import torch
 
 import joltphysics_gb300 as jsb
-from jsb_testlib import Scene, blob_arrays, blob_compliance
+from jsb_testlib import Scene, blob_arrays, blob_bend_compliance, blob_compliance
 
 F64 = torch.float64
+PI32 = float(np.float32(np.pi))  # the reference's float constants (JPH_PI, Trigonometry.h)
+ACOS_C = float(np.float32(0.175394))
 FLT_MAX = 3.402823466e38
 
 
@@ -56,9 +59,8 @@ class BodyModel:
                 r = records[a:z]
                 idx = np.stack([r[:, 0] & 0xFFFF, r[:, 0] >> 16, r[:, 1] & 0xFFFF, r[:, 1] >> 16], 1).astype(np.int64)
                 groups[name] = (torch.tensor(idx), torch.tensor((source[a:z] & 0x0FFFFFFF).astype(np.int64)),
-                                torch.tensor(r[:, 2].view(np.float32).astype(np.float64), dtype=F64))
-            if "bend" in groups:
-                raise ValueError("dihedral bends are not part of the differentiable reference")
+                                torch.tensor(r[:, 2].view(np.float32).astype(np.float64), dtype=F64),
+                                torch.tensor(r[:, 3].view(np.float32).astype(np.float64), dtype=F64))
             self.levels.append(groups)
 
 
@@ -126,11 +128,47 @@ def _planes(scene: Scene, m: BodyModel, x, v, P, bounds, dt):
         return normal, const, shape, torch.tensor(mu + [0.0], dtype=F64), torch.tensor(rest + [0.0], dtype=F64)
 
 
-def _project_levels(m: BodyModel, x, edge_c, vol_c, k):
+def _bend_angle_term(theta):
+    """sign(theta) ACosApproximate(cos |theta|) (Jolt/Math/Trigonometry.h:48-65), written so that it is
+    smooth in theta at flat triangle pairs: sqrt(1 - cos t) = sqrt(2) sin(t / 2) for |t| <= pi / 2,
+    sqrt(1 + cos t) = sqrt(2) cos(t / 2) beyond."""
+    cos_t = torch.cos(theta)
+    r2 = np.sqrt(2.0)
+    near = r2 * torch.sin(0.5 * theta) * (PI32 / 2 - ACOS_C * cos_t)
+    far = torch.where(theta < 0, -1.0, 1.0).to(F64) * (PI32 - r2 * torch.cos(0.5 * theta) * (PI32 / 2 + ACOS_C * cos_t))
+    return torch.where(cos_t >= 0, near, far)
+
+
+def _project_levels(m: BodyModel, x, edge_c, vol_c, k, bend_c=None):
     w = m.w
     for groups in m.levels:
+        if "bend" in groups:  # SoftBodyMotionProperties.cpp:367-456
+            idx, src, _, angle = groups["bend"]
+            c_ = bend_c[src]
+            i0, i1, i2, i3 = idx.T
+            x0, x1, x2, x3 = x[i0], x[i1], x[i2], x[i3]
+            e = x1 - x0
+            el = e.norm(dim=-1)
+            x1x2, x1x3 = x2 - x1, x3 - x1
+            n1, n2 = _cross(x2 - x0, x1x2), _cross(x1x3, x3 - x0)
+            n1s, n2s = _dot(n1, n1), _dot(n2, n2)
+            ok = (el >= 1e-6) & (n1s * n2s >= 1e-24)
+            n1s_, n2s_, el_ = (torch.where(ok, v, torch.ones_like(v)) for v in (n1s, n2s, el))
+            theta = torch.atan2(_dot(_cross(n2, n1), e) / el_, _dot(n1, n2))
+            c = _bend_angle_term(theta) - angle
+            c = torch.where(c > PI32, c - 2 * PI32, torch.where(c < -PI32, c + 2 * PI32, c))
+            n1h, n2h = n1 / n1s_[:, None], n2 / n2s_[:, None]
+            d0 = (_dot(x1x2, e)[:, None] * n1h + _dot(x1x3, e)[:, None] * n2h) / el_[:, None]
+            d2, d3 = el_[:, None] * n1h, el_[:, None] * n2h
+            d1 = -d0 - d2 - d3
+            w0, w1, w2, w3 = w[i0], w[i1], w[i2], w[i3]
+            denom = w0 * _dot(d0, d0) + w1 * _dot(d1, d1) + w2 * _dot(d2, d2) + w3 * _dot(d3, d3) + c_ * k
+            ok = (ok & (denom >= 1e-12))[:, None]
+            ml = c / torch.where(denom >= 1e-12, denom, torch.ones_like(denom))
+            for ii, xi, wi, di in ((i0, x0, w0, d0), (i1, x1, w1, d1), (i2, x2, w2, d2), (i3, x3, w3, d3)):
+                x = x.index_put((ii,), torch.where(ok, xi - (ml * wi)[:, None] * di, xi))
         if "volume" in groups:
-            idx, src, v0 = groups["volume"]
+            idx, src, v0, _ = groups["volume"]
             c_ = vol_c[src]
             i1, i2, i3, i4 = idx.T
             x1, x2, x3, x4 = x[i1], x[i2], x[i3], x[i4]
@@ -144,7 +182,7 @@ def _project_levels(m: BodyModel, x, edge_c, vol_c, k):
             for ii, xi, wi, di in ((i1, x1, w1, d1), (i2, x2, w2, d2), (i3, x3, w3, d3), (i4, x4, w4, d4)):
                 x = x.index_put((ii,), torch.where(ok, xi - (ml * wi)[:, None] * di, xi))
         if "edge" in groups:
-            idx, src, rest = groups["edge"]
+            idx, src, rest, _ = groups["edge"]
             c_ = edge_c[src]
             i0, i1 = idx[:, 0], idx[:, 1]
             x0, x1 = x[i0], x[i1]
@@ -156,7 +194,7 @@ def _project_levels(m: BodyModel, x, edge_c, vol_c, k):
             x = x.index_put((i0,), torch.where(ok, x0 + w[i0][:, None] * corr, x0))
             x = x.index_put((i1,), torch.where(ok, x1 - w[i1][:, None] * corr, x1))
         if "lra" in groups:
-            idx, src, md = groups["lra"]
+            idx, src, md, _ = groups["lra"]
             i0, i1 = idx[:, 0], idx[:, 1]
             d = x[i1] - x[i0]
             dls = _dot(d, d)
@@ -207,7 +245,7 @@ def simulate(scene: Scene, params: list[dict], steps: int, observe: list[int], p
                 v = torch.where(w > 0, (v + (gb * dts + sub_imp * w)) * damp, v)
                 prev = x
                 x = x + v * dts
-                x = _project_levels(m, x, p["edge"], p["volume"], k)
+                x = _project_levels(m, x, p["edge"], p["volume"], k, p.get("bend"))
                 # collision and velocity update (w > 0)
                 pv = v
                 vn0 = (x - prev) / dts
@@ -247,8 +285,10 @@ def base_params(scene: Scene, requires_grad=True) -> list[dict]:
     for body in scene.bodies:
         x0, v0, _ = blob_arrays(body.blob)
         ec, vc = blob_compliance(body.blob)
+        bc = blob_bend_compliance(body.blob)
         p = {"x0": torch.tensor(x0, dtype=F64), "v0": torch.tensor(v0, dtype=F64), "edge": torch.tensor(ec, dtype=F64),
-             "volume": torch.tensor(vc, dtype=F64), "force": torch.tensor(np.asarray(body.force, np.float64), dtype=F64)}
+             "volume": torch.tensor(vc, dtype=F64), "force": torch.tensor(np.asarray(body.force, np.float64), dtype=F64),
+             "bend": torch.tensor(bc, dtype=F64)}
         for t in p.values():
             t.requires_grad_(requires_grad)
         ps.append(p)
