@@ -101,6 +101,53 @@ __device__ __forceinline__ bool project_bend_impl(X sx, uint4 r, float inv_dt_sq
     return false;
 }
 
+// The bend of project_bend_impl with FastOps, computed without branches up to the store: every value is
+// computed speculatively (FastOps have no slow path and cannot fault), so the independent chains (edge
+// length, the two normals, the angle, the gradients) overlap instead of waiting at each exit test; the
+// exits are then taken in the reference's order with the values they would have seen. Same operations
+// on the same operands as project_bend_impl, so the same bits. Returns true when FastOps went out of
+// range before the projection's outcome was decided (the caller repeats it with IeeeOps).
+template <class X>
+__device__ __forceinline__ bool project_bend_fast(X sx, uint4 r, float inv_dt_sq) {
+    const uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16, i2 = r.y & 0xffff, i3 = r.y >> 16;
+    const float compliance = __uint_as_float(r.z), initial_angle = __uint_as_float(r.w);
+    const float4 p0 = ldx(sx, i0), p1 = ldx(sx, i1), p2 = ldx(sx, i2), p3 = ldx(sx, i3);
+    const f3 x0 = xyz(p0), x1 = xyz(p1), x2 = xyz(p2), x3 = xyz(p3);
+    FastOps op;
+    const f3 e = x1 - x0;
+    const float e_len = len_op(op, e);
+    const bool ok_len = op.ok();
+    const f3 x1x2 = x2 - x1, x1x3 = x3 - x1;
+    f3 n1 = cross(x2 - x0, x1x2);
+    f3 n2 = cross(x1x3, x3 - x0);
+    const float n1_len_sq = len_sq(n1), n2_len_sq = len_sq(n2);
+    const float n1n2 = n1_len_sq * n2_len_sq;
+    const float sign = dot(cross(n2, n1), e) < 0.0f ? -1.0f : 1.0f;
+    const float d = op.div(dot(n1, n2), op.sqrt(n1n2));
+    float c = sign * acos_approximate_op(op, d) - initial_angle;
+    c = c > kPi ? c - 2.0f * kPi : (c < -kPi ? c + 2.0f * kPi : c);
+    n1 = op.div3(n1, n1_len_sq);
+    n2 = op.div3(n2, n2_len_sq);
+    const f3 d0c = op.div3(dot(x1x2, e) * n1 + dot(x1x3, e) * n2, e_len);
+    const f3 d2c = e_len * n1;
+    const f3 d3c = e_len * n2;
+    const f3 d1c = (neg(d0c) - d2c) - d3c;
+    const float w0 = p0.w, w1 = p1.w, w2 = p2.w, w3 = p3.w;
+    const float denom = w0 * len_sq(d0c) + w1 * len_sq(d1c) + w2 * len_sq(d2c) + w3 * len_sq(d3c) + compliance * inv_dt_sq;
+    const bool ok_denom = op.ok();
+    const float ml = op.div(c, denom);
+    if (!ok_len) return true;
+    if (e_len < 1.0e-6f || n1n2 < 1.0e-24f) return false;
+    if (!ok_denom) return true;
+    if (denom < 1.0e-12f) return false;
+    if (!op.ok()) return true;
+    stx(sx, i0, with_w(x0 - (ml * w0) * d0c, w0));
+    stx(sx, i1, with_w(x1 - (ml * w1) * d1c, w1));
+    stx(sx, i2, with_w(x2 - (ml * w2) * d2c, w2));
+    stx(sx, i3, with_w(x3 - (ml * w3) * d3c, w3));
+    return false;
+}
+
 template <bool kGuard, class Ops, class X>
 __device__ __forceinline__ bool project_volume_impl(X sx, uint4 r, float inv_dt_sq, Ops &op) {  // :458-507
     uint32_t i1 = r.x & 0xffff, i2 = r.x >> 16, i3 = r.y & 0xffff, i4 = r.y >> 16;
@@ -154,6 +201,51 @@ __device__ __forceinline__ bool project_edge_impl(X sx, uint4 r, float inv_dt_sq
     return false;
 }
 
+// Edge and volume with FastOps, branch-free up to the store like project_bend_fast.
+template <class X>
+__device__ __forceinline__ bool project_edge_fast(X sx, uint4 r, float inv_dt_sq) {
+    const uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16;
+    const float rest = __uint_as_float(r.z), compliance = __uint_as_float(r.w);
+    const float4 p0 = ldx(sx, i0), p1 = ldx(sx, i1);
+    const f3 x0 = xyz(p0), x1 = xyz(p1);
+    FastOps op;
+    const f3 delta = x1 - x0;
+    const float length = len_op(op, delta);
+    const bool ok_len = op.ok();
+    const float denom = length * (p0.w + p1.w + compliance * inv_dt_sq);
+    const f3 corr = op.div3(delta * (length - rest), denom);
+    if (!ok_len) return true;
+    if (denom < 1.0e-12f) return false;
+    if (!op.ok()) return true;
+    stx(sx, i0, with_w(x0 + p0.w * corr, p0.w));
+    stx(sx, i1, with_w(x1 - p1.w * corr, p1.w));
+    return false;
+}
+template <class X>
+__device__ __forceinline__ bool project_volume_fast(X sx, uint4 r, float inv_dt_sq) {
+    const uint32_t i1 = r.x & 0xffff, i2 = r.x >> 16, i3 = r.y & 0xffff, i4 = r.y >> 16;
+    const float six_rest = __uint_as_float(r.z), compliance = __uint_as_float(r.w);
+    const float4 p1 = ldx(sx, i1), p2 = ldx(sx, i2), p3 = ldx(sx, i3), p4 = ldx(sx, i4);
+    const f3 x1 = xyz(p1), x2 = xyz(p2), x3 = xyz(p3), x4 = xyz(p4);
+    FastOps op;
+    const f3 x1x2 = x2 - x1, x1x3 = x3 - x1, x1x4 = x4 - x1;
+    const float c = fabsf(dot(cross(x1x2, x1x3), x1x4)) - six_rest;
+    const f3 d1c = cross(x4 - x2, x3 - x2);
+    const f3 d2c = cross(x1x3, x1x4);
+    const f3 d3c = cross(x1x4, x1x2);
+    const f3 d4c = cross(x1x2, x1x3);
+    const float w1 = p1.w, w2 = p2.w, w3 = p3.w, w4 = p4.w;
+    const float denom = w1 * len_sq(d1c) + w2 * len_sq(d2c) + w3 * len_sq(d3c) + w4 * len_sq(d4c) + compliance * inv_dt_sq;
+    const float ml = op.div(c, denom);
+    if (denom < 1.0e-12f) return false;
+    if (!op.ok()) return true;
+    stx(sx, i1, with_w(x1 - (ml * w1) * d1c, w1));
+    stx(sx, i2, with_w(x2 - (ml * w2) * d2c, w2));
+    stx(sx, i3, with_w(x3 - (ml * w3) * d3c, w3));
+    stx(sx, i4, with_w(x4 - (ml * w4) * d4c, w4));
+    return false;
+}
+
 template <class Ops, class X>
 __device__ __forceinline__ bool project_lra_impl(X sx, uint4 r, Ops &op) {  // :679-698
     uint32_t i0 = r.x & 0xffff, i1 = r.x >> 16;
@@ -172,24 +264,42 @@ __device__ __forceinline__ bool project_lra_impl(X sx, uint4 r, Ops &op) {  // :
 
 template <bool kGuard = false, class X>
 __device__ __forceinline__ void project_bend(X sx, uint4 r, float inv_dt_sq) {
-    FastOps f;
-    if (project_bend_impl<kGuard>(sx, r, inv_dt_sq, f)) {
+    bool again;
+    if (kGuard) {
+        FastOps f;
+        again = project_bend_impl<kGuard>(sx, r, inv_dt_sq, f);
+    } else {
+        again = project_bend_fast(sx, r, inv_dt_sq);
+    }
+    if (again) {
         IeeeOps e;
         project_bend_impl<kGuard>(sx, r, inv_dt_sq, e);
     }
 }
 template <bool kGuard = false, class X>
 __device__ __forceinline__ void project_volume(X sx, uint4 r, float inv_dt_sq) {
-    FastOps f;
-    if (project_volume_impl<kGuard>(sx, r, inv_dt_sq, f)) {
+    bool again;
+    if (kGuard) {
+        FastOps f;
+        again = project_volume_impl<kGuard>(sx, r, inv_dt_sq, f);
+    } else {
+        again = project_volume_fast(sx, r, inv_dt_sq);
+    }
+    if (again) {
         IeeeOps e;
         project_volume_impl<kGuard>(sx, r, inv_dt_sq, e);
     }
 }
 template <bool kGuard = false, class X>
 __device__ __forceinline__ void project_edge(X sx, uint4 r, float inv_dt_sq) {
-    FastOps f;
-    if (project_edge_impl<kGuard>(sx, r, inv_dt_sq, f)) {
+    bool again;
+    if (kGuard) {
+        FastOps f;
+        again = project_edge_impl<kGuard>(sx, r, inv_dt_sq, f);
+    } else {
+        again = project_edge_fast(sx, r, inv_dt_sq);
+    }
+    if (again) {
         IeeeOps e;
         project_edge_impl<kGuard>(sx, r, inv_dt_sq, e);
     }
