@@ -182,6 +182,10 @@ jsb_status jsb_body_read(jsb_context *ctx, uint32_t body_id, float position[3], 
 /* SoftBodyMotionProperties::SaveState bytes for RestoreState; *len receives the size (call with
  * state == NULL to query). */
 jsb_status jsb_body_save_state(jsb_context *ctx, uint32_t body_id, void *state, size_t capacity, size_t *len);
+/* The body's local bounds and local predicted bounds after the last step ({min xyz, max xyz} each;
+ * SoftBodyMotionProperties::mLocalBounds / mLocalPredictedBounds), which DetermineCollidingShapes grows by
+ * the vertex radius for its broad-phase query (SoftBodyMotionProperties.cpp:229-236). */
+jsb_status jsb_body_bounds(jsb_context *ctx, uint32_t body_id, float local_bounds[6], float predicted_bounds[6]);
 
 /* Bulk transfer of all bodies' local positions and velocities in body order (used for the
  * host-buffer round trip): 3 floats per vertex each. */

@@ -45,6 +45,7 @@ SIGNATURES = {
     "jsb_body_num_vertices": [_P, _c.c_uint32, _c.POINTER(_c.c_uint32)],
     "jsb_body_set_colliding_shapes": [_P, _c.c_uint32, _c.c_char_p, _c.c_uint32],
     "jsb_adjoint_bend_gradients": [_P, _c.c_uint32, _P],
+    "jsb_body_bounds": [_P, _c.c_uint32, _P, _P],
     "jsb_body_clear_colliding_shapes": [_P, _c.c_uint32],
     "jsb_body_shape_velocities": [_P, _c.c_uint32, _P, _c.POINTER(_c.c_uint32)],
     "jsb_step": [_P, _c.c_float, _c.c_int, _P],

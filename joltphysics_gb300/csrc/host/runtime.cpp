@@ -1190,6 +1190,24 @@ jsb_status jsb_synchronize(jsb_context *ctx) {
     return JSB_OK;
 }
 
+jsb_status jsb_body_bounds(jsb_context *ctx, uint32_t body_id, float local_bounds[6], float predicted_bounds[6]) {
+    if (!check_ctx(ctx) || body_id >= ctx->bodies.size() || !local_bounds || !predicted_bounds)
+        return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    JSB_CUDA(cudaDeviceSynchronize());
+    BodyState s;
+    JSB_CUDA(cudaMemcpy(&s, ctx->states.ptr + body_id, sizeof(BodyState), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 3; ++k) {
+        local_bounds[k] = s.bmin[k];
+        local_bounds[3 + k] = s.bmax[k];
+        predicted_bounds[k] = s.pmin[k];
+        predicted_bounds[3 + k] = s.pmax[k];
+    }
+    return JSB_OK;
+}
+
 jsb_status jsb_body_read(jsb_context *ctx, uint32_t body_id, float position[3], float *local_positions, float *velocities) {
     if (!check_ctx(ctx) || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
     JSB_CUDA(cudaSetDevice(ctx->device));
