@@ -56,7 +56,7 @@ typedef struct jsb_creation_settings {
     uint8_t faces_double_sided;   /* mFacesDoubleSided (queries only) */
 } jsb_creation_settings;
 
-enum { JSB_COLLIDER_BOX = 0, JSB_COLLIDER_SPHERE = 1, JSB_COLLIDER_CAPSULE = 2, JSB_COLLIDER_CYLINDER = 3 };
+enum { JSB_COLLIDER_BOX = 0, JSB_COLLIDER_SPHERE = 1, JSB_COLLIDER_CAPSULE = 2, JSB_COLLIDER_CYLINDER = 3, JSB_COLLIDER_HULL = 4 };
 
 /* A static rigid body with one convex leaf shape (BoxShape / SphereShape / CapsuleShape / CylinderShape),
  * world space, identity rotation (capsules and cylinders along the Y axis). friction/restitution are the
@@ -128,7 +128,7 @@ enum { JSB_MOTION_STATIC = 0, JSB_MOTION_KINEMATIC = 1, JSB_MOTION_DYNAMIC = 2 }
  * the adapter fills it from the same values inside PhysicsSystem's soft-body prepare job. Matrices are
  * Jolt's Mat44 columns, xyz of each. */
 typedef struct jsb_colliding_shape {
-    int32_t type;             /* JSB_COLLIDER_*: the leaf shape (Box / Sphere / Capsule / Cylinder) */
+    int32_t type;             /* JSB_COLLIDER_*: the leaf shape (Box / Sphere / Capsule / Cylinder / ConvexHull) */
     int32_t motion_type;      /* JSB_MOTION_*: CollidingShape::mMotionType */
     float transform[12];      /* LeafShape::mTransform (relative to the soft body): rotation columns 0-2, translation */
     float half_extent[3];     /* box; [1] = half height of a capsule's cylinder part / a cylinder */
@@ -141,7 +141,22 @@ typedef struct jsb_colliding_shape {
     float center_of_mass[3];  /* mCenterOfMassTransform's translation */
     float linear_velocity[3]; /* dynamic: mLinearVelocity at the start of the step (soft-body space) */
     float angular_velocity[3];/* dynamic: mAngularVelocity */
+    uint32_t hull_id;         /* JSB_COLLIDER_HULL: the id jsb_hull_add returned */
 } jsb_colliding_shape;
+
+/* A ConvexHullShape as Jolt built it (host-determined shapes only): its points relative to the shape's
+ * centre of mass (GetPoint), one plane per face (GetPlanes: normal xyz, constant) and each face's vertex
+ * indices (GetFaceVertices), at most 256 points and 255 faces. CollideSoftBodyVertices of an unscaled hull
+ * (ConvexHullShape.cpp:1060-1163) then runs on the GPU. Hulls are registered once and used by id. */
+typedef struct jsb_convex_hull {
+    uint32_t num_points;
+    const float *points;                /* 3 per point */
+    uint32_t num_faces;
+    const float *planes;                /* 4 per face */
+    const uint32_t *face_vertex_counts; /* per face */
+    const uint32_t *face_vertices;      /* the faces' vertex indices, concatenated */
+} jsb_convex_hull;
+jsb_status jsb_hull_add(jsb_context *ctx, const jsb_convex_hull *hull, uint32_t *hull_id);
 
 /* Replaces the context's static colliders for one body with `count` (<= 16) host-determined shapes, in
  * the order the reference collects them; they apply to every following step (each of its collision

@@ -46,6 +46,7 @@ SIGNATURES = {
     "jsb_body_set_colliding_shapes": [_P, _c.c_uint32, _c.c_char_p, _c.c_uint32],
     "jsb_adjoint_bend_gradients": [_P, _c.c_uint32, _P],
     "jsb_body_bounds": [_P, _c.c_uint32, _P, _P],
+    "jsb_hull_add": [_P, _P, _c.POINTER(_c.c_uint32)],
     "jsb_body_clear_colliding_shapes": [_P, _c.c_uint32],
     "jsb_body_shape_velocities": [_P, _c.c_uint32, _P, _c.POINTER(_c.c_uint32)],
     "jsb_step": [_P, _c.c_float, _c.c_int, _P],
@@ -256,6 +257,22 @@ class Context:
             check(lib().jsb_body_clear_colliding_shapes(self.h, body))
         else:
             check(lib().jsb_body_set_colliding_shapes(self.h, body, b"".join(shapes), len(shapes)))
+
+    def add_hull(self, points, planes, faces) -> int:
+        """Registers a convex hull (ConvexHullShape's points, per-face planes and vertex lists); returns its id."""
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        pls = np.ascontiguousarray(planes, np.float32).reshape(-1, 4)
+        counts = np.array([len(f) for f in faces], np.uint32)
+        idx = np.ascontiguousarray(np.concatenate([np.asarray(f, np.uint32) for f in faces]), np.uint32)
+
+        class Hull(ctypes.Structure):
+            _fields_ = [("num_points", ctypes.c_uint32), ("points", ctypes.c_void_p), ("num_faces", ctypes.c_uint32),
+                        ("planes", ctypes.c_void_p), ("face_vertex_counts", ctypes.c_void_p), ("face_vertices", ctypes.c_void_p)]
+
+        h = Hull(len(pts), pts.ctypes.data, len(pls), pls.ctypes.data, counts.ctypes.data, idx.ctypes.data)
+        out = ctypes.c_uint32()
+        check(lib().jsb_hull_add(self.h, ctypes.byref(h), ctypes.byref(out)))
+        return out.value
 
     def shape_velocities(self, body: int) -> np.ndarray:
         """Per host-determined shape after the last step: (updated, linear velocity[3], angular velocity[3])."""

@@ -250,6 +250,13 @@ struct jsb_context {
     jsb::DevBuf<float> step_forces;  // per body: 3 floats applied before every step
     jsb::DevBuf<jsb::BodySleep> sleep;  // per body: sleep timer, active flag
     std::map<uint32_t, std::vector<jsb::ShapeEntry>> table_host;  // host-determined colliding shapes by body
+    std::vector<jsb::HullDev> hulls_host;  // registered convex hulls (jsb_hull_add) and their data
+    std::vector<float4> hull_f4_host;
+    std::vector<uint32_t> hull_u32_host;
+    bool hulls_dirty = false;
+    jsb::DevBuf<jsb::HullDev> hulls_dev;
+    jsb::DevBuf<float4> hull_f4_dev;
+    jsb::DevBuf<uint32_t> hull_u32_dev;
     bool tables_dirty = false;
     std::vector<int32_t> table_slot_host;
     std::vector<jsb::ShapeTable> tables_staging;
@@ -670,12 +677,21 @@ StepParams base_params(jsb_context *ctx, float dt) {
     p.tables = tables ? ctx->tables_dev.ptr : nullptr;
     p.table_slot = tables ? ctx->table_slot_dev.ptr : nullptr;
     p.dyn_list = tables ? ctx->dyn_list.ptr : nullptr;
+    p.hulls = ctx->hulls_dev.ptr;
+    p.hull_f4 = ctx->hull_f4_dev.ptr;
+    p.hull_u32 = ctx->hull_u32_dev.ptr;
     return p;
 }
 
 // Host-determined colliding shapes set since the last step: one ShapeTable per body that has them
 // (slot order), uploaded on the step's stream ahead of its launches.
 jsb_status upload_tables(jsb_context *ctx, cudaStream_t stream) {
+    if (ctx->hulls_dirty) {  // registered hulls (synchronous: they are few and set up front)
+        JSB_CUDA(ctx->hulls_dev.upload(ctx->hulls_host.data(), ctx->hulls_host.size()));
+        JSB_CUDA(ctx->hull_f4_dev.upload(ctx->hull_f4_host.data(), ctx->hull_f4_host.size()));
+        JSB_CUDA(ctx->hull_u32_dev.upload(ctx->hull_u32_host.data(), ctx->hull_u32_host.size()));
+        ctx->hulls_dirty = false;
+    }
     if (!ctx->tables_dirty) return JSB_OK;
     ctx->table_slot_host.assign(ctx->bodies.size(), -1);
     ctx->tables_staging.assign(ctx->table_host.size(), ShapeTable{});
@@ -1025,8 +1041,10 @@ jsb_status jsb_body_set_colliding_shapes(jsb_context *ctx, uint32_t body_id, con
     if (count > kMaxCollidingShapes) return fail(JSB_ERR_CAPACITY, "at most 16 colliding shapes per body");
     std::vector<ShapeEntry> t(count);
     for (uint32_t k = 0; k < count; ++k) {
-        if (shapes[k].type < JSB_COLLIDER_BOX || shapes[k].type > JSB_COLLIDER_CYLINDER)
+        if (shapes[k].type < JSB_COLLIDER_BOX || shapes[k].type > JSB_COLLIDER_HULL)
             return fail(JSB_ERR_INVALID_ARGUMENT, "unknown collider type");
+        if (shapes[k].type == JSB_COLLIDER_HULL && shapes[k].hull_id >= ctx->hulls_host.size())
+            return fail(JSB_ERR_INVALID_ARGUMENT, "unknown hull id");
         if (shapes[k].motion_type < JSB_MOTION_STATIC || shapes[k].motion_type > JSB_MOTION_DYNAMIC)
             return fail(JSB_ERR_INVALID_ARGUMENT, "unknown motion type");
         std::memcpy(&t[k], &shapes[k], sizeof(ShapeEntry));
@@ -1034,6 +1052,41 @@ jsb_status jsb_body_set_colliding_shapes(jsb_context *ctx, uint32_t body_id, con
     ctx->table_host[body_id] = std::move(t);
     ctx->tables_dirty = true;
     drop_graph(ctx);
+    return JSB_OK;
+}
+
+jsb_status jsb_hull_add(jsb_context *ctx, const jsb_convex_hull *h, uint32_t *hull_id) {
+    if (!check_ctx(ctx) || !h || !hull_id || !h->points || !h->planes || !h->face_vertex_counts || !h->face_vertices)
+        return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    if (h->num_points < 4 || h->num_points > 256 || h->num_faces < 4 || h->num_faces > 255)
+        return fail(JSB_ERR_INVALID_ARGUMENT, "a hull has 4 to 256 points and 4 to 255 faces");
+    HullDev d;
+    d.num_faces = h->num_faces;
+    d.num_points = h->num_points;
+    d.f4 = uint32_t(ctx->hull_f4_host.size());
+    d.faces = uint32_t(ctx->hull_u32_host.size());
+    std::vector<uint32_t> u32(2 * size_t(h->num_faces));
+    uint32_t next = 0;
+    for (uint32_t f = 0; f < h->num_faces; ++f) {
+        const uint32_t n = h->face_vertex_counts[f];
+        if (n < 3 || n > h->num_points) return fail(JSB_ERR_INVALID_ARGUMENT, "a hull face has 3 to num_points vertices");
+        u32[2 * f] = d.faces + 2 * h->num_faces + next;
+        u32[2 * f + 1] = n;
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint32_t v = h->face_vertices[next + k];
+            if (v >= h->num_points) return fail(JSB_ERR_INVALID_ARGUMENT, "hull face vertex out of range");
+            u32.push_back(v);
+        }
+        next += n;
+    }
+    for (uint32_t f = 0; f < h->num_faces; ++f)
+        ctx->hull_f4_host.push_back(make_float4(h->planes[4 * f], h->planes[4 * f + 1], h->planes[4 * f + 2], h->planes[4 * f + 3]));
+    for (uint32_t i = 0; i < h->num_points; ++i)
+        ctx->hull_f4_host.push_back(make_float4(h->points[3 * i], h->points[3 * i + 1], h->points[3 * i + 2], 0.0f));
+    ctx->hull_u32_host.insert(ctx->hull_u32_host.end(), u32.begin(), u32.end());
+    ctx->hulls_host.push_back(d);
+    ctx->hulls_dirty = true;
+    *hull_id = uint32_t(ctx->hulls_host.size() - 1);
     return JSB_OK;
 }
 

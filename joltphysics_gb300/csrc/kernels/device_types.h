@@ -95,6 +95,16 @@ struct ShapeEntry {
     float inv_inertia[12];  // dynamic: mInvInertia, columns 0-3
     float com[3];           // mCenterOfMassTransform translation
     float lin[3], ang[3];   // dynamic: velocities at the start of the step (soft-body space)
+    uint32_t hull;          // convex hulls: index into StepParams::hulls
+};
+
+// A registered convex hull (jsb_hull_add): planes then points as float4 from `f4` (StepParams::hull_f4),
+// each face's first vertex and vertex count {first, count} from `faces`, vertex indices from `indices`
+// (StepParams::hull_u32).
+struct HullDev {
+    uint32_t num_faces, num_points;
+    uint32_t f4;       // planes at [f4, f4 + num_faces), points at [f4 + num_faces, ... + num_points)
+    uint32_t faces;    // {first, count} pairs at [faces, faces + 2 num_faces) in hull_u32
 };
 
 // Per body with host-determined colliding shapes: the shapes, and after a step the dynamic shapes'
@@ -175,6 +185,9 @@ struct StepParams {
     ShapeTable *tables;        // host-determined colliding shapes (null: none)
     const int32_t *table_slot; // per body: index into tables, -1 = the context's colliders
     int32_t *dyn_list;         // per vertex (context indexing): scratch for the vertices touching dynamic shapes
+    const HullDev *hulls;      // registered convex hulls
+    const float4 *hull_f4;
+    const uint32_t *hull_u32;
     BodySleep *sleep;      // per body (null: bodies never sleep)
     float sleep_velocity_threshold;  // PhysicsSettings::mPointVelocitySleepThreshold (compared with |v|^2)
     float time_before_sleep;         // PhysicsSettings::mTimeBeforeSleep

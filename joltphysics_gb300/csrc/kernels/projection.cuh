@@ -27,6 +27,7 @@ struct SCol {  // one colliding shape, relative to the soft body
     float friction;
     float restitution;
     float isc;           // mSoftBodyInvMassScale
+    int32_t hull;        // convex hulls: index into StepParams::hulls
     float c[9];          // rotation columns
     float ic[9], it[3];  // inverse transform (Mat44::InversedRotationTranslation): rotation columns, translation
 };
@@ -496,6 +497,84 @@ __device__ __forceinline__ void collide_cylinder(f3 p, const SCol &s, const X &x
     shape = idx;
 }
 
+// ClosestPoint::GetClosestPointOnLine (Jolt/Geometry/ClosestPoint.h:15-43, 129-150): the point of segment
+// (a, b) closest to the origin.
+__device__ __forceinline__ f3 closest_point_on_line(f3 a, f3 b) {
+    const f3 ab = b - a;
+    const float den = len_sq(ab);
+    float u, v;
+    if (den < FLT_EPSILON * FLT_EPSILON) {
+        const bool a_closer = len_sq(a) < len_sq(b);
+        u = a_closer ? 1.0f : 0.0f;
+        v = a_closer ? 0.0f : 1.0f;
+    } else {
+        v = jdiv(-dot(a, ab), den);
+        u = 1.0f - v;
+    }
+    if (v <= 0.0f) return a;
+    if (u <= 0.0f) return b;
+    return u * a + v * b;
+}
+
+// Registered convex hulls (jsb_hull_add).
+struct HullRefs {
+    const HullDev *hulls;
+    const float4 *f4;
+    const uint32_t *u32;
+};
+
+// ConvexHullShape::CollideSoftBodyVertices (ConvexHullShape.cpp:1060-1163), unscaled, for one vertex: the
+// most facing plane; outside the hull the closest point on that face's edges where the vertex lies
+// beyond them; the plane through the closest point.
+__device__ __forceinline__ void collide_hull(f3 p, const SCol &s, const XformR &xf, const HullRefs &hr, int idx, float &largest,
+                                             float4 &plane, int &shape) {
+    const HullDev h = hr.hulls[s.hull];
+    const f3 local = xf.local(p);
+    float max_distance = -FLT_MAX;
+    f3 max_n = mk(0.0f, 0.0f, 0.0f);
+    uint32_t max_i = 0;
+    for (uint32_t i = 0; i < h.num_faces; ++i) {
+        const float4 pl = hr.f4[h.f4 + i];
+        const float distance = dot(local, xyz(pl)) + pl.w;
+        if (distance > max_distance) {
+            max_distance = distance;
+            max_n = xyz(pl);
+            max_i = i;
+        }
+    }
+    f3 closest = (-max_distance) * max_n;
+    const bool outside = max_distance > 0.0f;
+    if (outside) {
+        float best = FLT_MAX;
+        const uint32_t first = hr.u32[h.faces + 2 * max_i], count = hr.u32[h.faces + 2 * max_i + 1];
+        const float4 *points = hr.f4 + h.f4 + h.num_faces;
+        for (uint32_t k = 0; k < count; ++k) {
+            const f3 p1 = xyz(points[hr.u32[first + k]]);
+            const f3 p2 = xyz(points[hr.u32[first + (k + 1 == count ? 0 : k + 1)]]);
+            if (dot(cross(p2 - p1, max_n), local - p1) > 0.0f) {  // beyond this edge
+                const f3 c = closest_point_on_line(p1 - local, p2 - local);
+                const float dsq = len_sq(c);
+                if (dsq < best) {
+                    best = dsq;
+                    closest = c;
+                }
+            }
+        }
+    }
+    f3 normal = neg(closest);
+    const float nl = len(normal);
+    float pen = nl;
+    if (outside)
+        pen = -pen;
+    else
+        normal = neg(normal);
+    if (largest >= pen) return;
+    largest = pen;
+    normal = nl > 1.0e-12f ? normal / nl : max_n;
+    plane = xf.plane(normal, local + closest);
+    shape = idx;
+}
+
 template <class X>
 __device__ __forceinline__ void collide_shape(f3 x, const SCol &s, const X &xf, int idx, float &largest, float4 &plane, int &shape) {
     switch (s.type) {
@@ -528,11 +607,13 @@ __device__ __forceinline__ void pick_max(float &v, int &i, float ov, int oi) {
 // DetermineCollisionPlanes (SoftBodyMotionProperties.cpp:257-265) for one vertex: the plane of the
 // colliding shape with the largest penetration (strictly larger replaces, CollideSoftBodyVertexIterator.h:86).
 // Returns the shape index, -1 for none.
-__device__ __forceinline__ int collision_plane(f3 x, const SCol *cols, int ncols, float4 &plane) {
+__device__ __forceinline__ int collision_plane(f3 x, const SCol *cols, int ncols, float4 &plane, const HullRefs &hr = HullRefs{}) {
     int shape = -1;
     float largest = -FLT_MAX;
     for (int s = 0; s < ncols; ++s) {
-        if (cols[s].flags & kColRotated)
+        if (cols[s].type == 4)  // (host-determined shapes only)
+            collide_hull(x, cols[s], XformR{cols[s]}, hr, s, largest, plane, shape);
+        else if (cols[s].flags & kColRotated)
             collide_shape(x, cols[s], XformR{cols[s]}, s, largest, plane, shape);
         else
             collide_shape(x, cols[s], XformT{ld3(cols[s].t)}, s, largest, plane, shape);
@@ -672,6 +753,7 @@ __device__ inline int load_shape_table(ShapeTable *tb, SCol *cols, bool &dynamic
         s.friction = e.friction;
         s.restitution = e.restitution;
         s.isc = e.inv_mass_scale;
+        s.hull = int32_t(e.hull);
         for (int j = 0; j < 3; ++j) {
             tb->lin[k][j] = e.lin[j];
             tb->ang[k][j] = e.ang[j];

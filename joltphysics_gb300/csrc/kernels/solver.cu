@@ -373,7 +373,7 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
         float4 pi = sx[i];
         int shape = -1;
         float4 plane = make_float4(0, 0, 0, 0);
-        if (pi.w > 0.0f && ncols > 0) shape = collision_plane(xyz(pi), sh.cols, ncols, plane);
+        if (pi.w > 0.0f && ncols > 0) shape = collision_plane(xyz(pi), sh.cols, ncols, plane, HullRefs{p.hulls, p.hull_f4, p.hull_u32});
         if (kSmemState)
             sv[i].w = __int_as_float(shape);
         else
@@ -845,6 +845,9 @@ __global__ void __launch_bounds__(T) step_kernel_noalloc(const __grid_constant__
     p.tables = nullptr;
     p.table_slot = nullptr;
     p.dyn_list = nullptr;
+    p.hulls = nullptr;
+    p.hull_f4 = nullptr;
+    p.hull_u32 = nullptr;
     if (threadIdx.x == 0) {
         stage_bar_init(&sh.stage_bar);
         stage_bar_init(&sh.ring_bar[0]);

@@ -253,13 +253,22 @@ struct Collider {
 
 // A colliding shape determined on the host for one body and step (the layout of jsb_colliding_shape):
 // the fields of SoftBodyMotionProperties::CollidingShape and its LeafShape the step reads.
-struct TableShapeIn {  // 172 bytes
+struct TableShapeIn {  // 176 bytes
     int32_t type, motion;  // motion: EMotionType (2 = dynamic)
     float xf[12];          // leaf transform: rotation columns 0-2, translation
     float half_extent[3], radius, friction, restitution;
     float inv_mass_scale, inv_mass;
     float inv_inertia[12];  // columns 0-3
     float com[3], lin[3], ang[3];
+    uint32_t hull;  // type 4: index of a hull added with oracle_add_hull
+};
+
+// A convex hull as ConvexHullShape holds it: points relative to its centre of mass, one plane per face
+// (normal, constant), each face's vertex indices.
+struct HullData {
+    std::vector<float> points;  // 3 per point
+    std::vector<float> planes;  // 4 per face
+    std::vector<std::vector<uint32_t>> faces;
 };
 
 struct Creation {
@@ -321,6 +330,7 @@ struct CollidingShape {
     R friction, restitution;
     R isc = R(1);  // mSoftBodyInvMassScale
     bool rotated = false, dynamic = false;
+    const HullData *hull = nullptr;  // type 4
     V3<R> c[3], ic[3], it;  // rotation columns; Mat44::InversedRotationTranslation columns and translation
     R inv_mass = R(0);
     V3<R> inertia[4];  // mInvInertia columns 0-3
@@ -343,6 +353,7 @@ inline V3<R> mat4(const V3<R> c[3], V3<R> t, V3<R> v) {
 template <class R>
 class World {
 public:
+    const std::vector<HullData> *hulls = nullptr;  // the handle's registered hulls
     V3<R> gravity{R(0), R(-9.81f), R(0)};
     std::vector<Collider> colliders;
     std::vector<Body<R>> bodies;
@@ -501,7 +512,9 @@ public:
             const CollidingShape<R> &cs = shapes[si];
             for (auto &v : b.v) {
                 if (!(v.inv_mass > R(0))) continue;
-                if (cs.type == 0)
+                if (cs.type == 4)
+                    collide_hull(v, cs, int(si));
+                else if (cs.type == 0)
                     collide_box(v, cs, int(si));
                 else if (cs.type == 1)
                     collide_sphere(v, cs, int(si));
@@ -557,10 +570,11 @@ public:
 
     // Host-determined shapes (oracle_set_colliding_shapes), with the inverse transform as
     // Mat44::InversedRotationTranslation computes it: transposed rotation, 0 - (R^T t).
-    static void shapes_from_table(const Body<R> &b, std::vector<CollidingShape<R>> &shapes) {
+    void shapes_from_table(const Body<R> &b, std::vector<CollidingShape<R>> &shapes) const {
         for (const TableShapeIn &e : b.table) {
             CollidingShape<R> cs;
             cs.type = e.type;
+            if (e.type == 4) cs.hull = &(*hulls)[e.hull];
             cs.rotated = true;
             cs.dynamic = e.motion == 2;
             for (int k = 0; k < 3; ++k) cs.c[k] = {R(e.xf[3 * k]), R(e.xf[3 * k + 1]), R(e.xf[3 * k + 2])};
@@ -674,6 +688,74 @@ public:
             const V3<R> normal = divs(delta, distance);
             set_plane(v, cs, normal, add(center, mul(r, normal)), idx);
         }
+    }
+
+    // ClosestPoint::GetClosestPointOnLine (Jolt/Geometry/ClosestPoint.h:15-43, 129-150)
+    static V3<R> closest_point_on_line(V3<R> a, V3<R> b) {
+        const V3<R> ab = sub(b, a);
+        const R den = len_sq(ab);
+        R u, v;
+        const R eps = R(FLT_EPSILON * FLT_EPSILON);
+        if (den < eps) {
+            const bool a_closer = len_sq(a) < len_sq(b);
+            u = a_closer ? R(1) : R(0);
+            v = a_closer ? R(0) : R(1);
+        } else {
+            v = -dot(a, ab) / den;
+            u = R(1) - v;
+        }
+        if (v <= R(0)) return a;
+        if (u <= R(0)) return b;
+        return add(mul(u, a), mul(v, b));
+    }
+
+    // ConvexHullShape.cpp:1060-1163, unscaled
+    static void collide_hull(Vertex<R> &v, const CollidingShape<R> &cs, int idx) {
+        const HullData &h = *cs.hull;
+        const V3<R> local = local_of(cs, v.pos);
+        R max_distance = -R(FLT_MAX);
+        V3<R> max_n = {R(0), R(0), R(0)};
+        size_t max_i = 0;
+        const size_t nf = h.planes.size() / 4;
+        for (size_t i = 0; i < nf; ++i) {
+            const V3<R> n = {R(h.planes[4 * i]), R(h.planes[4 * i + 1]), R(h.planes[4 * i + 2])};
+            const R distance = dot(local, n) + R(h.planes[4 * i + 3]);
+            if (distance > max_distance) {
+                max_distance = distance;
+                max_n = n;
+                max_i = i;
+            }
+        }
+        V3<R> closest = mul(-max_distance, max_n);
+        const bool outside = max_distance > R(0);
+        if (outside) {
+            R best = R(FLT_MAX);
+            const std::vector<uint32_t> &face = h.faces[max_i];
+            for (size_t k = 0; k < face.size(); ++k) {
+                const uint32_t a = face[k], b = face[k + 1 == face.size() ? 0 : k + 1];
+                const V3<R> p1 = {R(h.points[3 * a]), R(h.points[3 * a + 1]), R(h.points[3 * a + 2])};
+                const V3<R> p2 = {R(h.points[3 * b]), R(h.points[3 * b + 1]), R(h.points[3 * b + 2])};
+                if (dot(cross(sub(p2, p1), max_n), sub(local, p1)) > R(0)) {
+                    const V3<R> c = closest_point_on_line(sub(p1, local), sub(p2, local));
+                    const R dsq = len_sq(c);
+                    if (dsq < best) {
+                        best = dsq;
+                        closest = c;
+                    }
+                }
+            }
+        }
+        V3<R> normal = neg(closest);
+        const R nl = len(normal);
+        R pen = nl;
+        if (outside)
+            pen = -pen;
+        else
+            normal = neg(normal);
+        if (v.largest_pen >= pen) return;
+        v.largest_pen = pen;
+        normal = nl > R(1.0e-12f) ? divs(normal, nl) : max_n;
+        set_plane(v, cs, normal, add(local, closest), idx);
     }
 
     // CylinderShape.cpp:317-368: along Y, half[1] = half height
@@ -982,6 +1064,7 @@ public:
 
 struct Handle {
     int use_double;
+    std::vector<HullData> hulls;
     double noise = 0.0;
     uint64_t noise_seed = 0, noise_step = 0;
     World<float> wf;
@@ -998,6 +1081,7 @@ extern "C" {
 void *oracle_world_create(const float gravity[3], int use_double) {
     Handle *h = new Handle();
     h->use_double = use_double;
+    h->wf.hulls = h->wd.hulls = &h->hulls;
     h->wf.gravity = {gravity[0], gravity[1], gravity[2]};
     h->wd.gravity = {double(gravity[0]), double(gravity[1]), double(gravity[2])};
     return h;
@@ -1094,6 +1178,23 @@ int oracle_step(void *w, float dt, int collision_steps) {
         h->wf.step(dt, collision_steps);
     }
     return 0;
+}
+
+// Registers a convex hull (points 3 per point, planes 4 per face, face vertex counts and indices);
+// returns its index for TableShapeIn::hull.
+int oracle_add_hull(void *w, const float *points, int num_points, const float *planes, int num_faces, const uint32_t *counts,
+                    const uint32_t *indices) {
+    Handle *h = static_cast<Handle *>(w);
+    HullData d;
+    d.points.assign(points, points + 3 * num_points);
+    d.planes.assign(planes, planes + 4 * num_faces);
+    size_t next = 0;
+    for (int f = 0; f < num_faces; ++f) {
+        d.faces.emplace_back(indices + next, indices + next + counts[f]);
+        next += counts[f];
+    }
+    h->hulls.push_back(std::move(d));
+    return int(h->hulls.size() - 1);
 }
 
 // Host-determined colliding shapes of one body (jsb_colliding_shape layout), used by the following steps

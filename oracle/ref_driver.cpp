@@ -19,7 +19,9 @@
 // SoftBodyMotionProperties.cpp:120-255), recorded by a SoftBodyContactListener that accepts every contact
 // and recomputes the collector's values with the same calls, then each rigid body's velocities after the
 // step (which hold the soft bodies' velocity deltas, :923-935):
-//   'JSBT' u32 version=1 u32 steps u32 num_rigid
+//   'JSBT' u32 version=2 u32 steps u32 num_rigid
+//   per rigid body: u32 num_points, f32[3] per point, u32 num_faces, per face f32[4] plane, u32 count,
+//                   count x u32 vertex index (convex hulls; 0, 0 for other shapes)
 //   per step: i32 step, u32 num_entries, num_entries x TableEntry, num_rigid x f32[6] (linear, angular
 //             velocity after the step, world space)
 //
@@ -40,6 +42,7 @@
 #include <Jolt/Physics/StateRecorderImpl.h>
 #include <Jolt/Physics/Collision/Shape/BoxShape.h>
 #include <Jolt/Physics/Collision/Shape/CapsuleShape.h>
+#include <Jolt/Physics/Collision/Shape/ConvexHullShape.h>
 #include <Jolt/Physics/Collision/Shape/CylinderShape.h>
 #include <Jolt/Physics/Collision/Shape/SphereShape.h>
 #include <Jolt/Physics/Body/BodyCreationSettings.h>
@@ -274,7 +277,15 @@ int main(int argc, char **argv) {
         for (size_t r = 0; r < spec.rigid.size(); ++r) {
             const jsb::scene::RigidSpec &c = spec.rigid[r];
             const bool moving = c.motion != 0;
-            BodyCreationSettings bcs(make_shape(c.type, c.half_extent, c.radius), RVec3(c.position[0], c.position[1], c.position[2]),
+            RefConst<Shape> shape;
+            if (c.type == jsb::scene::ColliderType::Hull) {
+                Array<Vec3> pts;
+                for (auto &q : c.hull_points) pts.push_back(Vec3(q[0], q[1], q[2]));
+                shape = ConvexHullShapeSettings(pts).Create().Get();
+            } else {
+                shape = make_shape(c.type, c.half_extent, c.radius);
+            }
+            BodyCreationSettings bcs(shape, RVec3(c.position[0], c.position[1], c.position[2]),
                                      Quat(c.rotation[0], c.rotation[1], c.rotation[2], c.rotation[3]), EMotionType(c.motion),
                                      moving ? Layers::MOVING : Layers::NON_MOVING);
             bcs.mFriction = c.friction;
@@ -321,9 +332,38 @@ int main(int argc, char **argv) {
                 return 1;
             }
             fwrite("JSBT", 4, 1, tables);
-            put_u32(tables, 1);
+            put_u32(tables, 2);
             put_u32(tables, uint32_t(steps));
             put_u32(tables, uint32_t(spec.rigid.size()));
+            // per rigid body, its convex hull as ConvexHullShape holds it (points relative to the centre of
+            // mass, one plane per face, each face's vertex indices); nothing for other shapes
+            BodyLockInterfaceNoLock const &lk = system.GetBodyLockInterfaceNoLock();
+            for (BodyID id : rigid_ids) {
+                BodyLockRead lock(lk, id);
+                const Shape *sh = lock.GetBody().GetShape();
+                if (sh->GetSubType() != EShapeSubType::ConvexHull) {
+                    put_u32(tables, 0);
+                    put_u32(tables, 0);
+                    continue;
+                }
+                const ConvexHullShape *hull = static_cast<const ConvexHullShape *>(sh);
+                put_u32(tables, hull->GetNumPoints());
+                for (uint i = 0; i < hull->GetNumPoints(); ++i) {
+                    Vec3 q = hull->GetPoint(i);
+                    float f3[3] = {q.GetX(), q.GetY(), q.GetZ()};
+                    fwrite(f3, 4, 3, tables);
+                }
+                put_u32(tables, hull->GetNumFaces());
+                for (uint i = 0; i < hull->GetNumFaces(); ++i) {
+                    const Plane &pl = hull->GetPlanes()[i];
+                    float f4[4] = {pl.GetNormal().GetX(), pl.GetNormal().GetY(), pl.GetNormal().GetZ(), pl.GetConstant()};
+                    fwrite(f4, 4, 4, tables);
+                    uint idx[256];
+                    const uint nfv = hull->GetFaceVertices(i, 256, idx);
+                    put_u32(tables, nfv);
+                    for (uint k = 0; k < nfv; ++k) put_u32(tables, idx[k]);
+                }
+            }
         }
 
         FILE *f = nullptr;

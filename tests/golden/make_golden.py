@@ -68,8 +68,9 @@ def make(name: str, scene: str, params: dict, steps: list[int]):
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
 
 
-def make_coupling(name: str = "coupling", steps: int = 90, dump: tuple = (1, 10, 17, 18, 19, 20, 30, 45, 60, 75, 90)):
-    """Two-way coupling (rigid bodies simulated by the reference's own solver): per dump step the
+def make_coupling(name: str = "coupling", steps: int = 90, dump: tuple = (1, 10, 17, 18, 19, 20, 30, 45, 60, 75, 90), **params):
+    """Two-way coupling (rigid bodies simulated by the reference's own solver; params: scene parameters,
+    hulls=1 adds convex hulls): per dump step the
     deterministic build's soft-body states, and for every step each soft body's colliding shapes as the
     reference determined them (tables_*: jsb_colliding_shape bytes, soft body, rigid body, the rigid body's
     world velocities when collected) and the rigid bodies' velocities after the step."""
@@ -78,7 +79,7 @@ def make_coupling(name: str = "coupling", steps: int = 90, dump: tuple = (1, 10,
     out = {}
     with tempfile.TemporaryDirectory() as tmp:
         path, tab = os.path.join(tmp, "det.bin"), os.path.join(tmp, "det.tab")
-        run_reference("det", "coupling", path, dump=",".join(str(s) for s in [0, *dump]), steps=steps, tables=tab)
+        run_reference("det", "coupling", path, dump=",".join(str(s) for s in [0, *dump]), steps=steps, tables=tab, **params)
         sc, dumps = parse_dump(path)
         t = parse_tables(tab)
     out["scene"] = np.frombuffer(sc.raw, np.uint8)
@@ -95,6 +96,11 @@ def make_coupling(name: str = "coupling", steps: int = 90, dump: tuple = (1, 10,
     out["tables_shape"] = np.frombuffer(b"".join(r[3] for r in rows), np.uint8).reshape(len(rows), SHAPE_BYTES)
     out["tables_rigid_velocity"] = np.stack([r[4] for r in rows]).astype(np.float32)
     out["rigid_after"] = t["rigid_after"]
+    for r, (pts, planes, faces) in t["hulls"].items():  # convex hulls as ConvexHullShape holds them
+        out[f"hull{r}_points"] = pts
+        out[f"hull{r}_planes"] = planes
+        out[f"hull{r}_counts"] = np.array([len(f) for f in faces], np.uint32)
+        out[f"hull{r}_indices"] = np.concatenate([np.asarray(f, np.uint32) for f in faces])
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
 
 
@@ -150,6 +156,9 @@ if __name__ == "__main__":
     if not which or "coupling" in which:
         make_coupling()
         print("wrote coupling")
+    if not which or "coupling_hulls" in which:  # + a static and a dynamic convex hull under a fourth cloth
+        make_coupling("coupling_hulls", hulls=1)
+        print("wrote coupling_hulls")
     for name, (scene, params, steps) in FULL_CASES.items():
         if not which or f"full_{name}" in which:
             make_full(name, scene, params, steps, threads=os.cpu_count() or 1)

@@ -159,20 +159,38 @@ def run_reference(variant: str, scene: str, out: str, **kv) -> dict:
 
 # jsb_colliding_shape (include/jsb.h): type, motion type, transform[12], half_extent[3], radius, friction,
 # restitution, soft-body inverse-mass scale, inverse mass, inverse inertia[12], centre of mass[3], linear
-# velocity[3], angular velocity[3]
-SHAPE_FMT = "<2i41f"
+# velocity[3], angular velocity[3], hull id
+SHAPE_FMT = "<2i41fI"  # (+ hull id)
 SHAPE_BYTES = struct.calcsize(SHAPE_FMT)
 _TABLE_ENTRY = "<2I2i16f3f3f2f16f16f3f3f3f3f"  # oracle/ref_driver.cpp TableEntry
 
 
 def parse_tables(path: str) -> dict:
     """The reference driver's tables file: {"steps": {step: [(soft body, rigid index, shape bytes
-    (SHAPE_FMT), rigid linear and angular velocity (world) when collected)]}, "rigid_after": (steps,
-    num_rigid, 6) velocities after each step}."""
+    (SHAPE_FMT; a hull's id field holds its rigid index), rigid linear and angular velocity (world) when
+    collected)]}, "rigid_after": (steps, num_rigid, 6) velocities after each step, "hulls": {rigid index:
+    (points (N, 3), planes (F, 4), [face vertex lists])}}."""
     buf = open(path, "rb").read()
     assert buf[:4] == b"JSBT"
-    _, steps, nr = struct.unpack_from("<III", buf, 4)
+    version, steps, nr = struct.unpack_from("<III", buf, 4)
     off, esz = 16, struct.calcsize(_TABLE_ENTRY)
+    hulls = {}
+    if version >= 2:
+        for r in range(nr):
+            (npts,) = struct.unpack_from("<I", buf, off)
+            off += 4
+            pts = np.frombuffer(buf, np.float32, 3 * npts, off).reshape(npts, 3).copy()
+            off += 12 * npts
+            (nf,) = struct.unpack_from("<I", buf, off)
+            off += 4
+            planes, faces = [], []
+            for _ in range(nf):
+                planes.append(np.frombuffer(buf, np.float32, 4, off).copy())
+                (cnt,) = struct.unpack_from("<I", buf, off + 16)
+                faces.append(list(struct.unpack_from(f"<{cnt}I", buf, off + 20)))
+                off += 20 + 4 * cnt
+            if npts:
+                hulls[r] = (pts, np.array(planes, np.float32).reshape(nf, 4), faces)
     out, after = {}, np.zeros((steps, nr, 6), np.float32)
     for k in range(steps):
         st, n = struct.unpack_from("<iI", buf, off)
@@ -189,12 +207,12 @@ def parse_tables(path: str) -> dict:
             com = np.array(v[44:60], np.float32).reshape(4, 4)
             lin, ang, lw, aw = v[60:63], v[63:66], v[66:69], v[69:72]
             shape = struct.pack(SHAPE_FMT, ty, mo, *leaf[:, :3].ravel(), *he, rad, fr, rs, isc, im, *inert[:, :3].ravel(),
-                                *com[3, :3], *lin, *ang)
+                                *com[3, :3], *lin, *ang, rg if ty == 4 else 0)
             rows.append((sb, rg, shape, np.array(lw + aw, np.float32)))
         out[st] = rows
         after[k] = np.frombuffer(buf, np.float32, 6 * nr, off).reshape(nr, 6)
         off += 24 * nr
-    return {"steps": out, "rigid_after": after}
+    return {"steps": out, "rigid_after": after, "hulls": hulls}
 
 
 def build_oracle() -> str:
@@ -247,6 +265,8 @@ class Oracle:
             L.oracle_set_noise.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64]
             L.oracle_set_colliding_shapes.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
             L.oracle_get_shape_velocities.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+            L.oracle_add_hull.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                          ctypes.c_void_p, ctypes.c_void_p]
             L.oracle_last_error.restype = ctypes.c_char_p
             L.oracle_last_error.argtypes = [ctypes.c_void_p]
             cls._lib = L
@@ -288,6 +308,15 @@ class Oracle:
         returns the body to the scene's colliders."""
         data = b"".join(shapes or [])
         self.lib().oracle_set_colliding_shapes(self.h, i, data, -1 if shapes is None else len(shapes))
+
+    def add_hull(self, points, planes, faces) -> int:
+        """Registers a convex hull (points (N, 3), planes (F, 4), face vertex lists); returns its index."""
+        pts = np.ascontiguousarray(points, np.float32)
+        pls = np.ascontiguousarray(planes, np.float32)
+        counts = np.array([len(f) for f in faces], np.uint32)
+        idx = np.ascontiguousarray(np.concatenate([np.asarray(f, np.uint32) for f in faces]), np.uint32)
+        return self.lib().oracle_add_hull(self.h, pts.ctypes.data, len(pts), pls.ctypes.data, len(pls), counts.ctypes.data,
+                                          idx.ctypes.data)
 
     def shape_velocities(self, i: int) -> np.ndarray:
         """After a step with host-determined shapes: per shape (updated, linear velocity, angular velocity)."""

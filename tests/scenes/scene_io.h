@@ -101,7 +101,7 @@ inline bool make_named_scene(const std::string &name, const std::string &params,
         out = make_diff_batch(uint64_t(geti("seed", 5)), uint32_t(geti("n_cloth", 192)), uint32_t(geti("n_cube", 64)),
                               int(geti("steps", 90)), float(geti("drop_mm", 1000)) * 0.001f);
     else if (name == "coupling")
-        out = make_coupling(int(geti("steps", 90)));
+        out = make_coupling(int(geti("steps", 90)), geti("hulls", 0) != 0);
     else if (name == "shapes_drop")
         out = make_shapes_drop(uint64_t(geti("seed", 7)), int(geti("steps", 150)));
     else

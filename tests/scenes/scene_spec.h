@@ -112,7 +112,7 @@ struct BodySpec {
     float force[3] = {0, 0, 0};  // added with AddForce before every step
 };
 
-enum class ColliderType : int { Box = 0, Sphere = 1, Capsule = 2, Cylinder = 3 };
+enum class ColliderType : int { Box = 0, Sphere = 1, Capsule = 2, Cylinder = 3, Hull = 4 };
 
 struct ColliderSpec {  // a static rigid body with one convex shape (capsules and cylinders along Y)
     ColliderType type = ColliderType::Box;
@@ -139,6 +139,7 @@ struct RigidSpec {
     float restitution = 0.0f;
     float velocity[3] = {0, 0, 0};
     float angular_velocity[3] = {0, 0, 0};
+    std::vector<std::array<float, 3>> hull_points;  // ColliderType::Hull: the points the hull is built from
 };
 
 struct SceneSpec {
@@ -547,8 +548,9 @@ inline SceneSpec make_shapes_drop(uint64_t seed = 7, int steps = 150) {
 // (radius 0.15, 2 kg) falls onto A from 0.5 m above, a dynamic box (half extent 0.12, 2 kg, turned 0.5 rad
 // about a tilted axis and spinning) onto B. Cloth C is free and falls onto a static box turned 0.4 rad about Z.
 // The rigid bodies move under Jolt's own solver in the reference run; the soft bodies see them through
-// each step's colliding shapes. `steps` steps of 1/60 s.
-inline SceneSpec make_coupling(int steps = 90) {
+// each step's colliding shapes. hulls: a fourth cloth falls onto a static irregular convex hull (24
+// points on a jittered ellipsoid), and a small dynamic hull drops onto it. `steps` steps of 1/60 s.
+inline SceneSpec make_coupling(int steps = 90, bool hulls = false) {
     SceneSpec s;
     const float xs[3] = {-1.6f, 0.0f, 1.6f};
     for (int k = 0; k < 3; ++k) {
@@ -612,6 +614,41 @@ inline SceneSpec make_coupling(int steps = 90) {
     ramp.rotation[3] = std::cos(0.2f);
     ramp.friction = 0.3f;
     s.rigid.push_back(ramp);
+    if (hulls) {
+        // a fourth cloth (free) falls onto a static irregular convex hull, and a dynamic one drops on top
+        BodySpec b;
+        const uint32_t n = 20;
+        b.mesh = make_cloth(n, n, 0.06f, [](uint32_t, uint32_t) { return false; });
+        for (float &w : b.mesh.inv_mass) w = 25.0f;
+        b.mesh.attributes = VertexAttributes{1.0e-6f, 1.0e-6f, 1.0e-4f};
+        b.mesh.bend_type = BendType::Dihedral;
+        b.creation.friction = 0.5f;
+        b.position[0] = 3.2f;
+        b.position[1] = 1.3f;
+        s.bodies.push_back(b);
+        Rng rng(11);
+        for (int k = 0; k < 2; ++k) {
+            RigidSpec h;
+            h.type = ColliderType::Hull;
+            h.motion = k == 0 ? 0 : 2;
+            h.mass = 1.5f;
+            h.friction = 0.5f;
+            const float scale = k == 0 ? 0.45f : 0.18f;
+            for (int i = 0; i < 24; ++i) {  // points on an ellipsoid, jittered
+                const double u = rng.uniform() * 2.0 - 1.0, a = rng.uniform() * 6.283185307179586;
+                const double r = std::sqrt(1.0 - u * u);
+                h.hull_points.push_back({float(scale * 1.3 * r * std::cos(a)), float(scale * 0.8 * u), float(scale * r * std::sin(a))});
+            }
+            h.position[0] = 3.2f + (k == 0 ? 0.0f : 0.07f);
+            h.position[1] = k == 0 ? 0.36f : 2.0f;
+            h.position[2] = k == 0 ? 0.0f : -0.05f;
+            if (k == 1) {
+                h.rotation[0] = std::sin(0.3f);
+                h.rotation[3] = std::cos(0.3f);
+            }
+            s.rigid.push_back(h);
+        }
+    }
     s.num_steps = steps;
     return s;
 }

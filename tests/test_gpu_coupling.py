@@ -13,21 +13,23 @@ import pytest
 
 from conftest import golden_path
 from jsb_testlib import parse_scene
-from test_oracle_coupling import check_velocity_changes, tables_by_step
+from test_oracle_coupling import check_velocity_changes, register_hulls, tables_by_step
 
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("mode", ["batched", "plain"])
-def test_coupling_bitwise_vs_reference_and_oracle(jsb, oracle_lib, mode):
-    g = np.load(golden_path("coupling"))
+@pytest.mark.parametrize("name,mode", [("coupling", "batched"), ("coupling", "plain"), ("coupling_hulls", "batched")])
+def test_coupling_bitwise_vs_reference_and_oracle(jsb, oracle_lib, name, mode):
+    g = np.load(golden_path(name))
     scene_bytes = g["scene"].tobytes()
     scene, _ = parse_scene(scene_bytes)
     nv = list(g["num_vertices"])
-    tables = tables_by_step(g)
     ctx = jsb.Context(0)
     ctx.load_scene(scene_bytes)
     o = oracle_lib(scene)
+    gpu_hulls = register_hulls(g, ctx.add_hull)
+    assert gpu_hulls == register_hulls(g, o.add_hull)  # (same ids: both count from 0)
+    tables = tables_by_step(g, gpu_hulls)
     dumps = set(int(s) for s in g["steps"])
     changes = 0
     for step in range(1, int(g["steps"][-1]) + 1):

@@ -2,7 +2,8 @@
 (tests/golden/coupling.npz, written by tests/golden/make_golden.py from the reference driver).
 
 Three cloths under a static floor: a dynamic sphere and a turned, spinning dynamic box fall onto two
-trampolines, a third cloth onto a static turned box. Jolt's own rigid-body solver moves the rigid bodies;
+trampolines, a third cloth onto a static turned box (coupling_hulls adds a fourth cloth falling onto a
+static convex hull, with a small dynamic hull dropped onto it). Jolt's own rigid-body solver moves the rigid bodies;
 each step every soft body's colliding shapes are fed to the oracle as the reference determined them
 (transforms, combined friction / restitution, the dynamic bodies' mass, inertia and velocities). Bar:
 - every soft body's state bitwise equal to the reference (deterministic build) at every dumped step;
@@ -13,17 +14,37 @@ each step every soft body's colliding shapes are fed to the oracle as the refere
 import struct
 
 import numpy as np
+import pytest
 
 from conftest import golden_path
 from jsb_testlib import SHAPE_FMT, parse_scene
 
 
-def tables_by_step(g):
+def tables_by_step(g, hull_ids=None):
+    """Per step: (soft body, rigid body, jsb_colliding_shape bytes, the rigid body's velocities when collected).
+    hull_ids: rigid index -> id of its registered hull, written into the hulls' records."""
     out = {}
     for k in range(len(g["tables_step"])):
-        out.setdefault(int(g["tables_step"][k]), []).append((int(g["tables_body"][k]), int(g["tables_rigid"][k]),
-                                                            g["tables_shape"][k].tobytes(), g["tables_rigid_velocity"][k]))
+        shape = g["tables_shape"][k].tobytes()
+        rigid = int(g["tables_rigid"][k])
+        if hull_ids is not None and struct.unpack_from("<i", shape, 0)[0] == 4:
+            shape = shape[:-4] + struct.pack("<I", hull_ids[rigid])
+        out.setdefault(int(g["tables_step"][k]), []).append((int(g["tables_body"][k]), rigid, shape, g["tables_rigid_velocity"][k]))
     return out
+
+
+def register_hulls(g, add) -> dict:
+    """Registers the golden's convex hulls with add(points, planes, faces); returns rigid index -> id."""
+    ids = {}
+    for key in sorted(k for k in g.files if k.endswith("_points") and k.startswith("hull")):
+        r = int(key[4:-7])
+        counts, idx = g[f"hull{r}_counts"], g[f"hull{r}_indices"]
+        faces, off = [], 0
+        for c in counts:
+            faces.append(idx[off:off + c])
+            off += c
+        ids[r] = add(g[key], g[f"hull{r}_planes"], faces)
+    return ids
 
 
 def world_delta(local_new, local_old):
@@ -60,12 +81,13 @@ def check_velocity_changes(rows, shape_out_by_body, after):
     return checked
 
 
-def test_oracle_coupling_bitwise_vs_reference(oracle_lib):
-    g = np.load(golden_path("coupling"))
+@pytest.mark.parametrize("name", ["coupling", "coupling_hulls"])
+def test_oracle_coupling_bitwise_vs_reference(oracle_lib, name):
+    g = np.load(golden_path(name))
     scene, _ = parse_scene(g["scene"].tobytes())
     nv = list(g["num_vertices"])
-    tables = tables_by_step(g)
     o = oracle_lib(scene)
+    tables = tables_by_step(g, register_hulls(g, o.add_hull))
     dumps = set(int(s) for s in g["steps"])
     changes = 0
     for step in range(1, int(g["steps"][-1]) + 1):
