@@ -296,12 +296,15 @@ def bench_adjoint(jsb, stream_ptr, steps: int = 90, every: int = 15) -> dict:
     loc = np.zeros((int(offsets[-1]), 3), np.float32)
     vel = np.zeros_like(loc)
 
+    device = {}
+
     def forward_only():
         ctx.restore_all(init)
         ctx.synchronize()
         t0 = time.perf_counter()
         ctx.step_graph(steps, 1, stream=stream_ptr)
         ctx.synchronize()
+        device["graph_forward_ms"] = ctx.last_kernel_ms() * steps
         return time.perf_counter() - t0
 
     def forward_adjoint():
@@ -318,6 +321,7 @@ def bench_adjoint(jsb, stream_ptr, steps: int = 90, every: int = 15) -> dict:
         ctx.adjoint_seed_all(steps, seed.astype(np.float32))
         ctx.adjoint_backward()
         grads = ctx.adjoint_gradients_all()
+        device.update(ctx.adjoint_timings())
         ctx.adjoint_end()
         ctx.synchronize()
         return time.perf_counter() - t0, grads
@@ -333,7 +337,11 @@ def bench_adjoint(jsb, stream_ptr, steps: int = 90, every: int = 15) -> dict:
     return {"workload": "diff_batch", "bodies": nb, "steps": steps, "checkpoint_every": every,
             "forward_s": t_fwd, "forward_adjoint_s": t_adj, "ratio": t_adj / t_fwd, "target_ratio": 4.0,
             "gradients_finite": bool(finite),
-            "timing": "host clock around synchronised work, median of 3 runs each, forward as a CUDA graph"}
+            "timing": "host clock around synchronised work, median of 3 runs each, forward as a CUDA graph",
+            "device_ms": {k: round(v, 3) for k, v in device.items()},
+            "device_split": "CUDA events of the last run: the forward steps of the differentiable run (last segment "
+                            "taped), the taped recomputation of the other segments, the reverse steps; and the "
+                            "forward-only graph"}
 
 
 def gradient_checks(jsb) -> dict:

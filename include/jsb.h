@@ -304,6 +304,10 @@ jsb_status jsb_adjoint_gradients_all(jsb_context *ctx, float *dl_dx0, float *dl_
 jsb_status jsb_adjoint_gradients(jsb_context *ctx, uint32_t body_id, float *dl_dx0, float *dl_dv0, float *dl_dforce,
                                  float *dl_dedge_compliance, float *dl_dvolume_compliance);
 jsb_status jsb_adjoint_bend_gradients(jsb_context *ctx, uint32_t body_id, float *dl_dbend_compliance);
+/* Device time (CUDA events) of the last differentiable run's phases, ms: the forward steps
+ * (jsb_adjoint_forward, the last segment taped), the taped recomputation of the other segments and the
+ * reverse steps (jsb_adjoint_backward). */
+jsb_status jsb_adjoint_timings(jsb_context *ctx, float out_ms[3]);
 /* Ends the run. Its device buffers (tape, checkpoints, adjoints) stay with the context and are reused,
  * grown when needed, by its next differentiable run; jsb_context_destroy frees them. */
 jsb_status jsb_adjoint_end(jsb_context *ctx);

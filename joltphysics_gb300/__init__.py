@@ -47,6 +47,7 @@ SIGNATURES = {
     "jsb_adjoint_bend_gradients": [_P, _c.c_uint32, _P],
     "jsb_body_bounds": [_P, _c.c_uint32, _P, _P],
     "jsb_hull_add": [_P, _P, _c.POINTER(_c.c_uint32)],
+    "jsb_adjoint_timings": [_P, _P],
     "jsb_body_clear_colliding_shapes": [_P, _c.c_uint32],
     "jsb_body_shape_velocities": [_P, _c.c_uint32, _P, _c.POINTER(_c.c_uint32)],
     "jsb_step": [_P, _c.c_float, _c.c_int, _P],
@@ -442,6 +443,12 @@ class Context:
         check(lib().jsb_adjoint_gradients(self.h, body, dx.ctypes.data, dv.ctypes.data, df.ctypes.data,
                                           de.ctypes.data if num_edges else None, dvol.ctypes.data if num_volumes else None))
         return {"x0": dx, "v0": dv, "force": df, "edge_compliance": de, "volume_compliance": dvol}
+
+    def adjoint_timings(self) -> dict:
+        """Device milliseconds of the last differentiable run's forward, taped recomputation and reverse."""
+        out = np.zeros(3, np.float32)
+        check(lib().jsb_adjoint_timings(self.h, out.ctypes.data))
+        return {"forward_ms": float(out[0]), "recompute_ms": float(out[1]), "reverse_ms": float(out[2])}
 
     def adjoint_bend_gradients(self, body: int, num_bends: int) -> np.ndarray:
         """d loss / d each dihedral bend's compliance (settings order) after adjoint_backward."""

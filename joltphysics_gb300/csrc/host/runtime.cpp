@@ -213,6 +213,26 @@ struct AdjointSession {
     DevBuf<float4> adj_x, adj_v, seed_dev;
     std::vector<std::pair<int, std::vector<float4>>> seeds;  // (step, dL/dx of every vertex)
     int tape_segment = -1;  // checkpoint segment whose tape is in the tape buffers
+    float forward_ms = 0.0f, recompute_ms = 0.0f, reverse_ms = 0.0f;  // device time of the last run's phases
+};
+
+// Device time between events recorded on the legacy default stream (the phases' fork / join stream).
+struct PhaseTimer {
+    std::vector<cudaEvent_t> ev;
+    cudaError_t mark() {
+        cudaEvent_t e;
+        cudaError_t r = cudaEventCreate(&e);
+        if (r != cudaSuccess) return r;
+        ev.push_back(e);
+        return cudaEventRecord(e, 0);
+    }
+    float between(size_t a, size_t b) const {
+        float ms = 0.0f;
+        return cudaEventElapsedTime(&ms, ev[a], ev[b]) == cudaSuccess ? ms : 0.0f;
+    }
+    ~PhaseTimer() {
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    }
 };
 
 }  // namespace
@@ -1882,18 +1902,23 @@ jsb_status jsb_adjoint_forward(jsb_context *ctx, int until_step) {
     }
     uint32_t launches = 0;
     const int last_seg_start = ((a.steps - 1) / a.every) * a.every;
+    if (a.cur_step == 0) a.forward_ms = 0.0f;
+    PhaseTimer timer;  // per step: start, end (the checkpoint copies between steps are not counted)
     for (int s = a.cur_step; s < until_step; ++s) {
         if (s % a.every == 0) {
             JSB_CUDA(cudaDeviceSynchronize());
             if ((st = save_state(ctx, a.ckpt_x[s / a.every], a.ckpt_v[s / a.every], a.ckpt_state[s / a.every])) != JSB_OK) return st;
         }
+        JSB_CUDA(timer.mark());
         if (s >= last_seg_start) {
             // The last segment runs taped, so the backward pass starts without recomputing it.
             if ((st = enqueue_taped(ctx, a, s - last_seg_start, 0, launches)) != JSB_OK) return st;
         } else if ((st = enqueue_batched(ctx, a.dt, 0, launches)) != JSB_OK)
             return st;
+        JSB_CUDA(timer.mark());
     }
     JSB_CUDA(cudaDeviceSynchronize());
+    for (size_t k = 0; k + 1 < timer.ev.size(); k += 2) a.forward_ms += timer.between(k, k + 1);
     a.cur_step = until_step;
     if (a.cur_step == a.steps) {
         if ((st = save_state(ctx, a.final_x, a.final_v, a.final_state)) != JSB_OK) return st;
@@ -1984,14 +2009,17 @@ jsb_status jsb_adjoint_backward(jsb_context *ctx) {
     JSB_CUDA(cudaMemset(a.grad_force.ptr, 0, a.grad_force.count * sizeof(float)));
     uint32_t launches = 0;
     const int n_ckpt = int(a.ckpt_x.size());
+    PhaseTimer timer;  // per segment: recompute start / end, reverse end
     for (int seg = n_ckpt - 1; seg >= 0; --seg) {
         const int s0 = seg * a.every, s1 = std::min(s0 + a.every, a.steps);
+        JSB_CUDA(timer.mark());
         if (a.tape_segment != seg) {  // the forward pass leaves the last segment's tape in place
             if ((st = load_state(ctx, a.ckpt_x[seg], a.ckpt_v[seg], a.ckpt_state[seg])) != JSB_OK) return st;
             for (int s = s0; s < s1; ++s)  // recompute the segment, recording the tape
                 if ((st = enqueue_taped(ctx, a, s - s0, 0, launches)) != JSB_OK) return st;
             a.tape_segment = seg;
         }
+        JSB_CUDA(timer.mark());
         for (int s = s1 - 1; s >= s0; --s) {  // reverse the segment
             for (auto &sd : a.seeds)
                 if (sd.first == s + 1) {
@@ -2001,8 +2029,14 @@ jsb_status jsb_adjoint_backward(jsb_context *ctx) {
                 }
             if ((st = enqueue_adjoint(ctx, a, s - s0, 0, launches)) != JSB_OK) return st;
         }
+        JSB_CUDA(timer.mark());
     }
     JSB_CUDA(cudaDeviceSynchronize());
+    a.recompute_ms = a.reverse_ms = 0.0f;
+    for (size_t k = 0; k + 2 < timer.ev.size() + 1; k += 3) {
+        a.recompute_ms += timer.between(k, k + 1);
+        a.reverse_ms += timer.between(k + 1, k + 2);
+    }
     if ((st = load_state(ctx, a.final_x, a.final_v, a.final_state)) != JSB_OK) return st;
     a.backward_done = true;
     ctx->last_launches = launches;
@@ -2058,6 +2092,14 @@ jsb_status jsb_adjoint_gradients(jsb_context *ctx, uint32_t body_id, float *dl_d
             if (type == kVolume && dl_dvolume_compliance) dl_dvolume_compliance[idx] += g[c];
         }
     }
+    return JSB_OK;
+}
+
+jsb_status jsb_adjoint_timings(jsb_context *ctx, float out_ms[3]) {
+    if (!check_ctx(ctx) || !ctx->adjoint || !out_ms) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument or no differentiable run");
+    out_ms[0] = ctx->adjoint->forward_ms;
+    out_ms[1] = ctx->adjoint->recompute_ms;
+    out_ms[2] = ctx->adjoint->reverse_ms;
     return JSB_OK;
 }
 
