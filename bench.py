@@ -358,7 +358,7 @@ def gradient_checks(jsb) -> dict:
     t0 = time.perf_counter()
     out = {"diff_cloth": diff_cloth_check(jsb, build_scene),
            "diff_cloth_6_steps": diff_cloth_check(jsb, build_scene, steps=6, every=2, loss_steps=(3, 6), pinned=False),
-           "diff_batch": diff_batch_check(jsb, build_scene, n_params=16)}
+           "diff_batch": diff_batch_check(jsb, build_scene, n_params=8)}
     out["diff_batch"].pop("not_smooth", None)
     out["diff_batch"].pop("rows", None)
     out["seconds"] = time.perf_counter() - t0
