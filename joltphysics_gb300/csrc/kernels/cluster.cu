@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
             const float4 vel = gv[i];
             const float4 prev = gprev[i];
             const f3 prev_v = xyz(vel);
-            f3 v = (x - xyz(prev)) / dt_sub;
+            f3 v = div3_rn(x - xyz(prev), dt_sub);
             const int shape = ncols > 0 ? gshape[i] : -1;
             if (shape >= 0 && collide_vertex(x, v, prev_v, gplane[i], sh.cols[shape], d.vertex_radius, dt_sub, restitution_threshold))
                 sx[i - first] = with_w(x, pi.w);

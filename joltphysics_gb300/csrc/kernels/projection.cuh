@@ -634,9 +634,9 @@ __device__ __forceinline__ bool collide_vertex(f3 &x, f3 &v, f3 prev_v, float4 p
     if (!(cs.isc > 0.0f)) return true;  // the soft body is not moved by this shape (mSoftBodyInvMassScale = 0)
     f3 v_normal = n * dot(n, v);
     f3 v_tan = v - v_normal;
-    float vtl = len(v_tan);
+    float vtl = sqrt_rn(len_sq(v_tan));
     if (vtl > 0.0f) {
-        float fr = jdiv(cs.friction * projected, vtl * dt_sub);
+        float fr = div_rn(cs.friction * projected, vtl * dt_sub);
         fr = fr < 1.0f ? fr : 1.0f;  // min(fr, 1)
         v = v - v_tan * fr;
     }
@@ -662,7 +662,7 @@ __device__ __forceinline__ bool collide_vertex_dynamic(f3 &x, f3 &v, f3 prev_v, 
     const f3 relative = v - v2;
     const f3 v_normal = n * dot(n, relative);
     const f3 v_tan = relative - v_normal;
-    const float vtl = len(v_tan);
+    const float vtl = sqrt_rn(len_sq(v_tan));
     const float vertex_inv_mass = e.inv_mass_scale * w;
     const f3 r2xn = cross(r2, n);
     const float w2 = e.inv_mass + dot(r2xn, mat_mul(e.inv_inertia, r2xn, ld3(e.inv_inertia + 9)));
@@ -670,14 +670,14 @@ __device__ __forceinline__ bool collide_vertex_dynamic(f3 &x, f3 &v, f3 prev_v, 
     if (!(w12 > 0.0f)) return false;
     f3 dv = mk(0.0f, 0.0f, 0.0f);
     if (vtl > 0.0f) {
-        float fr = jdiv(e.friction * projected, vtl * dt_sub);
+        float fr = div_rn(e.friction * projected, vtl * dt_sub);
         fr = fr < 1.0f ? fr : 1.0f;
         dv = v_tan * fr;
     }
     dv = dv + v_normal;
     const float pvn = dot(prev_v - v2, n);
     if (pvn < restitution_threshold) dv = dv + (e.restitution * pvn) * n;
-    const f3 imp = dv / w12;
+    const f3 imp = div3_rn(dv, w12);
     v = v - imp * vertex_inv_mass;
     lin = lin + imp * e.inv_mass;
     ang = ang + mat_mul(e.inv_inertia, cross(r2, imp), ld3(e.inv_inertia + 9));

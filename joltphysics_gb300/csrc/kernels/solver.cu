@@ -208,7 +208,7 @@ __device__ __forceinline__ void vertex_between_substeps(float4 *sx, const Vertex
         const float4 prev = kSmemState ? vp.sprev[i] : vp.gprev[i];
         f3 x = xyz(pi);
         const f3 prev_v = xyz(vel);
-        f3 v = (x - xyz(prev)) / vp.dt_sub;
+        f3 v = div3_rn(x - xyz(prev), vp.dt_sub);
         int shape = -1;
         if (vp.ncols > 0) shape = kSmemState ? __float_as_int(vel.w) : vp.gshape[i];
         if (shape >= 0 && collide_vertex(x, v, prev_v, vp.gplane[i], vp.cols[shape], vp.radius, vp.dt_sub, vp.restitution_threshold))
@@ -527,7 +527,7 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
             float4 vel = kSmemState ? sv[i] : gv[i];
             float4 prev = kSmemState ? sprev[i] : gprev[i];
             f3 prev_v = xyz(vel);
-            f3 v = (x - xyz(prev)) / dt_sub;
+            f3 v = div3_rn(x - xyz(prev), dt_sub);
             int shape = -1;
             if (ncols > 0) shape = kSmemState ? __float_as_int(vel.w) : gshape[i];
             if (has_dynamic && shape >= 0 && (sh.cols[shape].flags & kColDynamic)) continue;  // below, in vertex order
@@ -549,7 +549,7 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
                     const float4 vel = kSmemState ? sv[i] : gv[i];
                     const float4 prev = kSmemState ? sprev[i] : gprev[i];
                     const int s = kSmemState ? __float_as_int(vel.w) : gshape[i];
-                    f3 x = xyz(pi), v = (x - xyz(prev)) / dt_sub;
+                    f3 x = xyz(pi), v = div3_rn(x - xyz(prev), dt_sub);
                     f3 lin = mk(sh.dvel[s][0], sh.dvel[s][1], sh.dvel[s][2]), ang = mk(sh.dvel[s][3], sh.dvel[s][4], sh.dvel[s][5]);
                     if (collide_vertex_dynamic(x, v, xyz(vel), pi.w, gplane[i], tb.e[s], lin, ang, d.vertex_radius, dt_sub,
                                                restitution_threshold)) {
