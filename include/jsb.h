@@ -172,6 +172,21 @@ jsb_status jsb_body_clear_colliding_shapes(jsb_context *ctx, uint32_t body_id);
  * adds the soft body's rotation times (velocity - the shape's input velocity) to the rigid body. */
 jsb_status jsb_body_shape_velocities(jsb_context *ctx, uint32_t body_id, float *out, uint32_t *count);
 
+/* ---- contacts (SoftBodyManifold) ---------------------------------------------------------------- */
+/* Records, every step, what SoftBodyManifold exposes to ContactListener::OnSoftBodyContactAdded
+ * (SoftBodyManifold.h; SoftBodyMotionProperties.cpp:832-845): per vertex whether it touched its collision
+ * plane in any substep (mHasContact), the contact point GetLocalContactPoint (in the body's local frame
+ * before the step's recentring) and the contact normal GetContactNormal; plus the recentring offset of the
+ * step. Off by default (it costs a byte per vertex per substep of stores). */
+jsb_status jsb_set_contact_readback(jsb_context *ctx, int enable);
+/* After a step with the readback on (synchronises the device): per vertex has_contact (0 / 1), contact point
+ * and normal (3 floats each, zero without contact) and the colliding shape's index (the host-determined
+ * table's order, or the order of the context colliders the body's bounds overlapped; -1 without contact),
+ * and the recentring offset delta (local positions after the step = before - delta). Any output may be
+ * NULL. Not recorded on the thread-block-cluster path (JSB_ERR_UNSUPPORTED). */
+jsb_status jsb_body_contacts(jsb_context *ctx, uint32_t body_id, uint8_t *has_contact, float *contact_points, float *normals,
+                             int32_t *shape_index, float delta[3]);
+
 /* ---- stepping ----------------------------------------------------------------------------- */
 /* PhysicsSystem::Update's soft-body part for every body in the context: InitializeUpdateContext,
  * DetermineCollidingShapes, DetermineCollisionPlanes, num_iterations x (pressure, integrate,

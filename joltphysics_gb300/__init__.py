@@ -48,6 +48,8 @@ SIGNATURES = {
     "jsb_body_bounds": [_P, _c.c_uint32, _P, _P],
     "jsb_hull_add": [_P, _P, _c.POINTER(_c.c_uint32)],
     "jsb_adjoint_timings": [_P, _P],
+    "jsb_set_contact_readback": [_P, _c.c_int],
+    "jsb_body_contacts": [_P, _c.c_uint32, _P, _P, _P, _P, _P],
     "jsb_body_clear_colliding_shapes": [_P, _c.c_uint32],
     "jsb_body_shape_velocities": [_P, _c.c_uint32, _P, _c.POINTER(_c.c_uint32)],
     "jsb_step": [_P, _c.c_float, _c.c_int, _P],
@@ -274,6 +276,22 @@ class Context:
         out = ctypes.c_uint32()
         check(lib().jsb_hull_add(self.h, ctypes.byref(h), ctypes.byref(out)))
         return out.value
+
+    def set_contact_readback(self, enable: bool = True):
+        check(lib().jsb_set_contact_readback(self.h, 1 if enable else 0))
+
+    def contacts(self, body: int) -> dict:
+        """The body's SoftBodyManifold after the last step: has_contact (N,), contact points (N, 3, local,
+        before the recentring), normals (N, 3), shape index (N,), recentring offset (3,)."""
+        n = self.num_vertices[body]
+        has = np.zeros(n, np.uint8)
+        cp = np.zeros((n, 3), np.float32)
+        nrm = np.zeros((n, 3), np.float32)
+        shape = np.zeros(n, np.int32)
+        delta = np.zeros(3, np.float32)
+        check(lib().jsb_body_contacts(self.h, body, has.ctypes.data, cp.ctypes.data, nrm.ctypes.data, shape.ctypes.data,
+                                      delta.ctypes.data))
+        return {"has_contact": has, "points": cp, "normals": nrm, "shape": shape, "delta": delta}
 
     def shape_velocities(self, body: int) -> np.ndarray:
         """Per host-determined shape after the last step: (updated, linear velocity[3], angular velocity[3])."""

@@ -274,6 +274,10 @@ struct jsb_context {
     std::vector<float4> hull_f4_host;
     std::vector<uint32_t> hull_u32_host;
     bool hulls_dirty = false;
+    bool contact_readback = false;  // record SoftBodyManifold data every step (jsb_set_contact_readback)
+    jsb::DevBuf<uint8_t> contact;
+    jsb::DevBuf<float4> contact_point;
+    jsb::DevBuf<float> contact_delta;
     jsb::DevBuf<jsb::HullDev> hulls_dev;
     jsb::DevBuf<float4> hull_f4_dev;
     jsb::DevBuf<uint32_t> hull_u32_dev;
@@ -700,7 +704,27 @@ StepParams base_params(jsb_context *ctx, float dt) {
     p.hulls = ctx->hulls_dev.ptr;
     p.hull_f4 = ctx->hull_f4_dev.ptr;
     p.hull_u32 = ctx->hull_u32_dev.ptr;
+    const bool contacts = ctx->contact_readback && ctx->contact.count >= ctx->total_vertices;
+    p.contact = contacts ? ctx->contact.ptr : nullptr;
+    p.contact_point = contacts ? ctx->contact_point.ptr : nullptr;
+    p.contact_delta = contacts ? ctx->contact_delta.ptr : nullptr;
     return p;
+}
+
+// Buffers of the contact readback, sized for the current bodies (zeroed: no contact yet).
+jsb_status ensure_contact_buffers(jsb_context *ctx) {
+    if (!ctx->contact_readback) return JSB_OK;
+    const size_t n = std::max<uint64_t>(ctx->total_vertices, 1), nb = std::max<size_t>(ctx->bodies.size(), 1);
+    if (ctx->contact.count < n) {
+        JSB_CUDA(ctx->contact.alloc(n));
+        JSB_CUDA(cudaMemset(ctx->contact.ptr, 0, n));
+        JSB_CUDA(ctx->contact_point.alloc(n));
+    }
+    if (ctx->contact_delta.count < 3 * nb) {
+        JSB_CUDA(ctx->contact_delta.alloc(3 * nb));
+        JSB_CUDA(cudaMemset(ctx->contact_delta.ptr, 0, 3 * nb * sizeof(float)));
+    }
+    return JSB_OK;
 }
 
 // Host-determined colliding shapes set since the last step: one ShapeTable per body that has them
@@ -785,6 +809,7 @@ jsb_status step_impl(jsb_context *ctx, float dt, int collision_steps, cudaStream
                         return fail(JSB_ERR_UNSUPPORTED, "host-determined colliding shapes on a body of the thread-block-cluster path");
     }
     if ((st = upload_tables(ctx, stream)) != JSB_OK) return st;
+    if ((st = ensure_contact_buffers(ctx)) != JSB_OK) return st;
     const float step_dt = dt / float(collision_steps);
     for (int c = 0; c < collision_steps; ++c) {
         bool uploaded = false;
@@ -1107,6 +1132,47 @@ jsb_status jsb_hull_add(jsb_context *ctx, const jsb_convex_hull *h, uint32_t *hu
     ctx->hulls_host.push_back(d);
     ctx->hulls_dirty = true;
     *hull_id = uint32_t(ctx->hulls_host.size() - 1);
+    return JSB_OK;
+}
+
+jsb_status jsb_set_contact_readback(jsb_context *ctx, int enable) {
+    if (!check_ctx(ctx)) return JSB_ERR_INVALID_ARGUMENT;
+    ctx->contact_readback = enable != 0;
+    drop_graph(ctx);
+    return JSB_OK;
+}
+
+jsb_status jsb_body_contacts(jsb_context *ctx, uint32_t body_id, uint8_t *has_contact, float *contact_points, float *normals,
+                             int32_t *shape_index, float delta[3]) {
+    if (!check_ctx(ctx) || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    if (!ctx->contact_readback || ctx->contact.count < ctx->total_vertices || ctx->dirty)
+        return fail(JSB_ERR_INVALID_ARGUMENT, "contact readback is off (jsb_set_contact_readback) or no step has run since");
+    for (const LaunchGroup &g : ctx->groups)
+        if (g.cluster > 0 && std::find(g.bodies.begin(), g.bodies.end(), body_id) != g.bodies.end())
+            return fail(JSB_ERR_UNSUPPORTED, "contact readback is not recorded on the thread-block-cluster path");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    JSB_CUDA(cudaDeviceSynchronize());
+    const BodyRec &b = ctx->bodies[body_id];
+    const size_t nv = ctx->settings[b.settings_id]->parsed.vertices.size();
+    std::vector<uint8_t> flag(nv);
+    std::vector<float4> cp(nv), plane(nv);
+    std::vector<int32_t> shape(nv);
+    JSB_CUDA(cudaMemcpy(flag.data(), ctx->contact.ptr + b.vtx_offset, nv, cudaMemcpyDeviceToHost));
+    JSB_CUDA(cudaMemcpy(cp.data(), ctx->contact_point.ptr + b.vtx_offset, nv * sizeof(float4), cudaMemcpyDeviceToHost));
+    JSB_CUDA(cudaMemcpy(plane.data(), ctx->plane.ptr + b.vtx_offset, nv * sizeof(float4), cudaMemcpyDeviceToHost));
+    JSB_CUDA(cudaMemcpy(shape.data(), ctx->shape.ptr + b.vtx_offset, nv * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (delta) JSB_CUDA(cudaMemcpy(delta, ctx->contact_delta.ptr + 3 * size_t(body_id), 3 * sizeof(float), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < nv; ++i) {
+        const bool c = flag[i] != 0;
+        if (has_contact) has_contact[i] = c ? 1 : 0;
+        for (int k = 0; k < 3; ++k) {
+            const float pk = k == 0 ? cp[i].x : (k == 1 ? cp[i].y : cp[i].z);
+            const float nk = k == 0 ? plane[i].x : (k == 1 ? plane[i].y : plane[i].z);
+            if (contact_points) contact_points[3 * i + k] = c ? pk : 0.0f;
+            if (normals) normals[3 * i + k] = c ? 0.0f - nk : 0.0f;  // GetContactNormal: -plane normal
+        }
+        if (shape_index) shape_index[i] = c ? shape[i] : -1;
+    }
     return JSB_OK;
 }
 

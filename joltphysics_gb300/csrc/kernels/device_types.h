@@ -185,6 +185,9 @@ struct StepParams {
     ShapeTable *tables;        // host-determined colliding shapes (null: none)
     const int32_t *table_slot; // per body: index into tables, -1 = the context's colliders
     int32_t *dyn_list;         // per vertex (context indexing): scratch for the vertices touching dynamic shapes
+    uint8_t *contact;          // per vertex (null: not recorded): touched its collision plane this step (mHasContact)
+    float4 *contact_point;     // per vertex: SoftBodyManifold::GetLocalContactPoint (before the recentring)
+    float *contact_delta;      // 3 per body: the recentring offset of the step
     const HullDev *hulls;      // registered convex hulls
     const float4 *hull_f4;
     const uint32_t *hull_u32;

@@ -652,10 +652,11 @@ __device__ __forceinline__ bool collide_vertex(f3 &x, f3 &v, f3 prev_v, float4 p
 // the body's velocities lin / ang in place, which the next vertex in index order sees. Returns whether an
 // impulse was applied (CollidingShape::mUpdateVelocities).
 __device__ __forceinline__ bool collide_vertex_dynamic(f3 &x, f3 &v, f3 prev_v, float w, float4 pl, const ShapeEntry &e, f3 &lin,
-                                                       f3 &ang, float radius, float dt_sub, float restitution_threshold) {
+                                                       f3 &ang, float radius, float dt_sub, float restitution_threshold, bool &contact) {
     const f3 n = xyz(pl);
     const float projected = -(dot(x, n) + pl.w) + radius;
-    if (!(projected > 0.0f)) return false;
+    contact = projected > 0.0f;
+    if (!contact) return false;
     x = x + n * projected;
     const f3 r2 = x - ld3(e.com);
     const f3 v2 = lin + cross(ang, r2);  // CollidingShape::GetPointVelocity

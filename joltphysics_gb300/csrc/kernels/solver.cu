@@ -192,6 +192,7 @@ struct VertexPass {
     float damp, dt_sub, radius, restitution_threshold;
     float4 *tape;  // taped forward: this step's substep states [substep][3][nv] (TapeDesc::state)
     uint32_t nv;
+    uint8_t *contact;  // the body's contact flags (null: not recorded)
 };
 
 // ApplyCollisionConstraintsAndUpdateVelocities (:700-825, static colliders) of the substep vertex i
@@ -211,8 +212,10 @@ __device__ __forceinline__ void vertex_between_substeps(float4 *sx, const Vertex
         f3 v = div3_rn(x - xyz(prev), vp.dt_sub);
         int shape = -1;
         if (vp.ncols > 0) shape = kSmemState ? __float_as_int(vel.w) : vp.gshape[i];
-        if (shape >= 0 && collide_vertex(x, v, prev_v, vp.gplane[i], vp.cols[shape], vp.radius, vp.dt_sub, vp.restitution_threshold))
+        if (shape >= 0 && collide_vertex(x, v, prev_v, vp.gplane[i], vp.cols[shape], vp.radius, vp.dt_sub, vp.restitution_threshold)) {
             pi = with_w(x, pi.w);
+            if (vp.contact) vp.contact[i] = 1;
+        }
         v = v + (vp.sub_g + vp.sub_imp * pi.w);
         v = v * vp.damp;
         vel = with_w(v, vel.w);
@@ -376,9 +379,9 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
         if (pi.w > 0.0f && ncols > 0) shape = collision_plane(xyz(pi), sh.cols, ncols, plane, HullRefs{p.hulls, p.hull_f4, p.hull_u32});
         if (kSmemState)
             sv[i].w = __int_as_float(shape);
-        else
-            gshape[i] = shape;
+        if (!kSmemState || p.contact) gshape[i] = shape;
         if (shape >= 0) gplane[i] = plane;
+        if (p.contact) p.contact[d.vtx_offset + i] = 0;
         if (kTape) {
             td.plane[size_t(p.tape_step) * nv + i] = plane;
             td.shape[size_t(p.tape_step) * nv + i] = shape;
@@ -429,6 +432,7 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
         vp.restitution_threshold = restitution_threshold;
         vp.tape = kTape ? td.state + size_t(p.tape_step) * n_it * 3 * nv : nullptr;
         vp.nv = nv;
+        vp.contact = p.contact ? p.contact + d.vtx_offset : nullptr;
     }
     const uint32_t passes = step_walk ? 1u : n_it;
 
@@ -531,8 +535,10 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
             int shape = -1;
             if (ncols > 0) shape = kSmemState ? __float_as_int(vel.w) : gshape[i];
             if (has_dynamic && shape >= 0 && (sh.cols[shape].flags & kColDynamic)) continue;  // below, in vertex order
-            if (shape >= 0 && collide_vertex(x, v, prev_v, gplane[i], sh.cols[shape], d.vertex_radius, dt_sub, restitution_threshold))
+            if (shape >= 0 && collide_vertex(x, v, prev_v, gplane[i], sh.cols[shape], d.vertex_radius, dt_sub, restitution_threshold)) {
                 sx[i] = with_w(x, pi.w);
+                if (p.contact) p.contact[d.vtx_offset + i] = 1;
+            }
             if (kSmemState)
                 sv[i] = with_w(v, vel.w);
             else
@@ -551,8 +557,11 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
                     const int s = kSmemState ? __float_as_int(vel.w) : gshape[i];
                     f3 x = xyz(pi), v = div3_rn(x - xyz(prev), dt_sub);
                     f3 lin = mk(sh.dvel[s][0], sh.dvel[s][1], sh.dvel[s][2]), ang = mk(sh.dvel[s][3], sh.dvel[s][4], sh.dvel[s][5]);
-                    if (collide_vertex_dynamic(x, v, xyz(vel), pi.w, gplane[i], tb.e[s], lin, ang, d.vertex_radius, dt_sub,
-                                               restitution_threshold)) {
+                    bool touched;
+                    const bool impulse = collide_vertex_dynamic(x, v, xyz(vel), pi.w, gplane[i], tb.e[s], lin, ang, d.vertex_radius,
+                                                                dt_sub, restitution_threshold, touched);
+                    if (touched && p.contact) p.contact[d.vtx_offset + i] = 1;
+                    if (impulse) {
                         sh.dvel[s][0] = lin.x, sh.dvel[s][1] = lin.y, sh.dvel[s][2] = lin.z;
                         sh.dvel[s][3] = ang.x, sh.dvel[s][4] = ang.y, sh.dvel[s][5] = ang.z;
                         sh.dyn_updated |= 1u << s;
@@ -633,6 +642,16 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     __syncthreads();
     const f3 delta = ld3(sh.delta);
     const bool shift = (d.flags & kFlagUpdatePosition) != 0;
+    if (p.contact) {  // SoftBodyManifold (read by OnSoftBodyContactAdded before the recentring): contact points
+        for (uint32_t i = tid; i < nv; i += T)
+            if (p.contact[d.vtx_offset + i]) {
+                const f3 x = xyz(sx[i]);
+                const float4 pl = gplane[i];
+                const f3 n = xyz(pl);
+                p.contact_point[d.vtx_offset + i] = with_w(x - n * (dot(x, n) + pl.w), 0.0f);
+            }
+        if (tid == 0) st3(p.contact_delta + 3 * size_t(b), shift ? delta : mk(0.0f, 0.0f, 0.0f));
+    }
     for (uint32_t i = tid; i < nv; i += T) {
         float4 pi = sx[i];
         gx[i] = shift ? with_w(xyz(pi) - delta, pi.w) : pi;
@@ -848,6 +867,9 @@ __global__ void __launch_bounds__(T) step_kernel_noalloc(const __grid_constant__
     p.hulls = nullptr;
     p.hull_f4 = nullptr;
     p.hull_u32 = nullptr;
+    p.contact = nullptr;
+    p.contact_point = nullptr;
+    p.contact_delta = nullptr;
     if (threadIdx.x == 0) {
         stage_bar_init(&sh.stage_bar);
         stage_bar_init(&sh.ring_bar[0]);

@@ -19,11 +19,13 @@
 // SoftBodyMotionProperties.cpp:120-255), recorded by a SoftBodyContactListener that accepts every contact
 // and recomputes the collector's values with the same calls, then each rigid body's velocities after the
 // step (which hold the soft bodies' velocity deltas, :923-935):
-//   'JSBT' u32 version=2 u32 steps u32 num_rigid
+//   'JSBT' u32 version=3 u32 steps u32 num_rigid
 //   per rigid body: u32 num_points, f32[3] per point, u32 num_faces, per face f32[4] plane, u32 count,
 //                   count x u32 vertex index (convex hulls; 0, 0 for other shapes)
 //   per step: i32 step, u32 num_entries, num_entries x TableEntry, num_rigid x f32[6] (linear, angular
-//             velocity after the step, world space)
+//             velocity after the step, world space), then per soft body u32 n (0 = no contact callback) and
+//             n x {u32 has contact, f32[3] local contact point, f32[3] contact normal, i32 rigid index}: the
+//             SoftBodyManifold passed to OnSoftBodyContactAdded
 //
 // Output file (little endian):
 //   'JSBD' u32 version=2 u32 num_dumps u32 scene_len, scene_len bytes of the serialised scene
@@ -50,6 +52,7 @@
 #include <Jolt/Physics/SoftBody/SoftBodyCreationSettings.h>
 #include <Jolt/Physics/SoftBody/SoftBodyMotionProperties.h>
 #include <Jolt/Physics/SoftBody/SoftBodyContactListener.h>
+#include <Jolt/Physics/SoftBody/SoftBodyManifold.h>
 #include <Jolt/Physics/Body/BodyLockMulti.h>
 
 #include <algorithm>
@@ -211,6 +214,35 @@ public:
         entries.push_back(e);
         return SoftBodyValidateResult::AcceptContact;
     }
+
+    // SoftBodyManifold of each soft body that had a contact this step (SoftBodyMotionProperties.cpp:832-845)
+    struct ManifoldVertex {
+        uint32_t has;
+        float point[3], normal[3];
+        int32_t rigid;
+    };
+    std::map<uint32_t, std::vector<ManifoldVertex>> manifolds;
+
+    void OnSoftBodyContactAdded(const Body &inSoftBody, const SoftBodyManifold &inManifold) override {
+        std::vector<ManifoldVertex> out;
+        for (const SoftBodyVertex &v : inManifold.GetVertices()) {
+            ManifoldVertex m{};
+            m.rigid = -1;
+            if (inManifold.HasContact(v)) {
+                m.has = 1;
+                Vec3 p = inManifold.GetLocalContactPoint(v), n = inManifold.GetContactNormal(v);
+                for (int k = 0; k < 3; ++k) {
+                    m.point[k] = p[k];
+                    m.normal[k] = n[k];
+                }
+                BodyID id = inManifold.GetContactBodyID(v);
+                m.rigid = rigid_index.count(id.GetIndex()) ? int32_t(rigid_index.at(id.GetIndex())) : -2;
+            }
+            out.push_back(m);
+        }
+        std::lock_guard<std::mutex> lock(mutex);
+        manifolds[soft_index.at(inSoftBody.GetID().GetIndex())] = std::move(out);
+    }
 };
 
 }  // namespace
@@ -332,7 +364,7 @@ int main(int argc, char **argv) {
                 return 1;
             }
             fwrite("JSBT", 4, 1, tables);
-            put_u32(tables, 2);
+            put_u32(tables, 3);
             put_u32(tables, uint32_t(steps));
             put_u32(tables, uint32_t(spec.rigid.size()));
             // per rigid body, its convex hull as ConvexHullShape holds it (points relative to the centre of
@@ -458,6 +490,13 @@ int main(int argc, char **argv) {
                     float v6[6] = {lv.GetX(), lv.GetY(), lv.GetZ(), av.GetX(), av.GetY(), av.GetZ()};
                     fwrite(v6, 4, 6, tables);
                 }
+                for (uint32_t b = 0; b < uint32_t(ids.size()); ++b) {  // manifolds (none: 0)
+                    auto it = recorder.manifolds.find(b);
+                    put_u32(tables, it == recorder.manifolds.end() ? 0u : uint32_t(it->second.size()));
+                    if (it != recorder.manifolds.end())
+                        fwrite(it->second.data(), sizeof(TableRecorder::ManifoldVertex), it->second.size(), tables);
+                }
+                recorder.manifolds.clear();
             }
         }
         if (f) fclose(f);
