@@ -318,6 +318,9 @@ struct Body {
     bool has_table = false;
     std::vector<TableShapeIn> table;
     std::vector<std::array<float, 7>> table_out;
+    // the last step's SoftBodyManifold (World::record_manifold): per vertex {has contact, local contact
+    // point, contact normal, shape index}
+    std::vector<std::array<float, 8>> manifold;
 };
 
 template <class R>
@@ -354,6 +357,7 @@ template <class R>
 class World {
 public:
     const std::vector<HullData> *hulls = nullptr;  // the handle's registered hulls
+    bool record_manifold = false;
     V3<R> gravity{R(0), R(-9.81f), R(0)};
     std::vector<Collider> colliders;
     std::vector<Body<R>> bodies;
@@ -1003,6 +1007,18 @@ public:
     }
 
     void update_state(Body<R> &b, R dt, V3<R> disp_g, typename Body<R>::Decisions *dec) {  // :827-921
+        if (record_manifold) {  // SoftBodyManifold as OnSoftBodyContactAdded sees it (:832-845, SoftBodyManifold.h)
+            b.manifold.assign(b.v.size(), {});
+            for (size_t vi = 0; vi < b.v.size(); ++vi) {
+                const Vertex<R> &v = b.v[vi];
+                std::array<float, 8> &m = b.manifold[vi];
+                m[7] = -1.0f;
+                if (!v.contact) continue;
+                const V3<R> pt = sub(v.pos, mul(v.plane_n, dot(v.pos, v.plane_n) + v.plane_c));
+                const V3<R> nrm = neg(v.plane_n);
+                m = {1.0f, float(pt.x), float(pt.y), float(pt.z), float(nrm.x), float(nrm.y), float(nrm.z), float(v.shape_idx)};
+            }
+        }
         R max_sq = R(b.cs.max_linear_velocity) * R(b.cs.max_linear_velocity);
         R max_v_sq = R(0);
         V3<R> lin = {R(0), R(0), R(0)}, ang = {R(0), R(0), R(0)};
@@ -1178,6 +1194,23 @@ int oracle_step(void *w, float dt, int collision_steps) {
         h->wf.step(dt, collision_steps);
     }
     return 0;
+}
+
+// Records every step's SoftBodyManifold (oracle_get_contacts).
+int oracle_set_contact_readback(void *w, int on) {
+    Handle *h = static_cast<Handle *>(w);
+    h->wf.record_manifold = h->wd.record_manifold = on != 0;
+    return 0;
+}
+
+// The last step's manifold of one body: 8 floats per vertex {has contact, contact point xyz, normal xyz,
+// shape index}. Returns the vertex count (0 when nothing was recorded).
+int oracle_get_contacts(void *w, int body, float *out) {
+    Handle *h = static_cast<Handle *>(w);
+    const auto &m = h->use_double ? h->wd.bodies[body].manifold : h->wf.bodies[body].manifold;
+    for (size_t i = 0; i < m.size(); ++i)
+        for (int k = 0; k < 8; ++k) out[8 * i + k] = m[i][k];
+    return int(m.size());
 }
 
 // Registers a convex hull (points 3 per point, planes 4 per face, face vertex counts and indices);

@@ -81,7 +81,7 @@ def make_coupling(name: str = "coupling", steps: int = 90, dump: tuple = (1, 10,
         path, tab = os.path.join(tmp, "det.bin"), os.path.join(tmp, "det.tab")
         run_reference("det", "coupling", path, dump=",".join(str(s) for s in [0, *dump]), steps=steps, tables=tab, **params)
         sc, dumps = parse_dump(path)
-        t = parse_tables(tab)
+        t = parse_tables(tab, len(sc.bodies))
     out["scene"] = np.frombuffer(sc.raw, np.uint8)
     out["steps"] = np.array(dump, np.int32)
     out["num_vertices"] = np.array([b.num_vertices for b in sc.bodies], np.int64)
@@ -96,6 +96,14 @@ def make_coupling(name: str = "coupling", steps: int = 90, dump: tuple = (1, 10,
     out["tables_shape"] = np.frombuffer(b"".join(r[3] for r in rows), np.uint8).reshape(len(rows), SHAPE_BYTES)
     out["tables_rigid_velocity"] = np.stack([r[4] for r in rows]).astype(np.float32)
     out["rigid_after"] = t["rigid_after"]
+    keys = sorted(t["manifolds"])  # the manifolds OnSoftBodyContactAdded saw: (step, body) -> per vertex
+    out["manifold_step"] = np.array([k[0] for k in keys], np.int32)
+    out["manifold_body"] = np.array([k[1] for k in keys], np.int32)
+    if keys:
+        out["manifold_has"] = np.concatenate([t["manifolds"][k]["has"] for k in keys]).astype(np.uint8)
+        out["manifold_point"] = np.concatenate([t["manifolds"][k]["point"] for k in keys]).astype(np.float32)
+        out["manifold_normal"] = np.concatenate([t["manifolds"][k]["normal"] for k in keys]).astype(np.float32)
+        out["manifold_rigid"] = np.concatenate([t["manifolds"][k]["rigid"] for k in keys]).astype(np.int32)
     for r, (pts, planes, faces) in t["hulls"].items():  # convex hulls as ConvexHullShape holds them
         out[f"hull{r}_points"] = pts
         out[f"hull{r}_planes"] = planes

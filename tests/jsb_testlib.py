@@ -165,11 +165,12 @@ SHAPE_BYTES = struct.calcsize(SHAPE_FMT)
 _TABLE_ENTRY = "<2I2i16f3f3f2f16f16f3f3f3f3f"  # oracle/ref_driver.cpp TableEntry
 
 
-def parse_tables(path: str) -> dict:
+def parse_tables(path: str, num_soft: int = 0) -> dict:
     """The reference driver's tables file: {"steps": {step: [(soft body, rigid index, shape bytes
     (SHAPE_FMT; a hull's id field holds its rigid index), rigid linear and angular velocity (world) when
     collected)]}, "rigid_after": (steps, num_rigid, 6) velocities after each step, "hulls": {rigid index:
-    (points (N, 3), planes (F, 4), [face vertex lists])}}."""
+    (points (N, 3), planes (F, 4), [face vertex lists])}, "manifolds": {(step, soft body): per vertex
+    (has, point, normal, rigid)} (version 3; num_soft: the scene's soft bodies)}."""
     buf = open(path, "rb").read()
     assert buf[:4] == b"JSBT"
     version, steps, nr = struct.unpack_from("<III", buf, 4)
@@ -191,7 +192,7 @@ def parse_tables(path: str) -> dict:
                 off += 20 + 4 * cnt
             if npts:
                 hulls[r] = (pts, np.array(planes, np.float32).reshape(nf, 4), faces)
-    out, after = {}, np.zeros((steps, nr, 6), np.float32)
+    out, after, manifolds = {}, np.zeros((steps, nr, 6), np.float32), {}
     for k in range(steps):
         st, n = struct.unpack_from("<iI", buf, off)
         off += 8
@@ -212,7 +213,16 @@ def parse_tables(path: str) -> dict:
         out[st] = rows
         after[k] = np.frombuffer(buf, np.float32, 6 * nr, off).reshape(nr, 6)
         off += 24 * nr
-    return {"steps": out, "rigid_after": after, "hulls": hulls}
+        if version >= 3:  # per soft body: the SoftBodyManifold of OnSoftBodyContactAdded, if it was called
+            for b in range(num_soft):
+                (n,) = struct.unpack_from("<I", buf, off)
+                off += 4
+                if n:
+                    rec = np.frombuffer(buf, np.dtype([("has", "<u4"), ("point", "<f4", 3), ("normal", "<f4", 3), ("rigid", "<i4")]),
+                                        n, off)
+                    manifolds[(st, b)] = rec.copy()
+                    off += 32 * n
+    return {"steps": out, "rigid_after": after, "hulls": hulls, "manifolds": manifolds}
 
 
 def build_oracle() -> str:
@@ -267,6 +277,8 @@ class Oracle:
             L.oracle_get_shape_velocities.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
             L.oracle_add_hull.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                           ctypes.c_void_p, ctypes.c_void_p]
+            L.oracle_set_contact_readback.argtypes = [ctypes.c_void_p, ctypes.c_int]
+            L.oracle_get_contacts.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
             L.oracle_last_error.restype = ctypes.c_char_p
             L.oracle_last_error.argtypes = [ctypes.c_void_p]
             cls._lib = L
@@ -317,6 +329,15 @@ class Oracle:
         idx = np.ascontiguousarray(np.concatenate([np.asarray(f, np.uint32) for f in faces]), np.uint32)
         return self.lib().oracle_add_hull(self.h, pts.ctypes.data, len(pts), pls.ctypes.data, len(pls), counts.ctypes.data,
                                           idx.ctypes.data)
+
+    def set_contact_readback(self, on: bool = True):
+        self.lib().oracle_set_contact_readback(self.h, 1 if on else 0)
+
+    def contacts(self, i: int) -> np.ndarray:
+        """The last step's manifold of body i: (N, 8) {has contact, point xyz, normal xyz, shape index}."""
+        out = np.zeros((self.nv[i], 8), np.float32)
+        n = self.lib().oracle_get_contacts(self.h, i, out.ctypes.data)
+        return out[:n]
 
     def shape_velocities(self, i: int) -> np.ndarray:
         """After a step with host-determined shapes: per shape (updated, linear velocity, angular velocity)."""

@@ -6,14 +6,15 @@ and a turned, spinning dynamic box on two trampolines, a turned static box and t
 cloth), then the batched step runs. Bar: every body's state bitwise equal to the reference
 (deterministic build) at every dumped step and to the oracle at every step; the dynamic bodies' velocity
 changes read back through jsb_body_shape_velocities give the reference's velocities after each step
-bitwise (as in tests/test_oracle_coupling.py).
+bitwise, and the SoftBodyManifold read back through jsb_body_contacts (contact flags, points, normals,
+contacted body) is the reference's, bitwise (as in tests/test_oracle_coupling.py).
 """
 import numpy as np
 import pytest
 
 from conftest import golden_path
 from jsb_testlib import parse_scene
-from test_oracle_coupling import check_velocity_changes, register_hulls, tables_by_step
+from test_oracle_coupling import check_manifold, check_velocity_changes, manifolds_by_key, register_hulls, tables_by_step
 
 pytestmark = pytest.mark.gpu
 
@@ -30,6 +31,9 @@ def test_coupling_bitwise_vs_reference_and_oracle(jsb, oracle_lib, name, mode):
     gpu_hulls = register_hulls(g, ctx.add_hull)
     assert gpu_hulls == register_hulls(g, o.add_hull)  # (same ids: both count from 0)
     tables = tables_by_step(g, gpu_hulls)
+    manifolds = manifolds_by_key(g)
+    ctx.set_contact_readback(True)
+    contacts = 0
     dumps = set(int(s) for s in g["steps"])
     changes = 0
     for step in range(1, int(g["steps"][-1]) + 1):
@@ -48,6 +52,10 @@ def test_coupling_bitwise_vs_reference_and_oracle(jsb, oracle_lib, name, mode):
         for b in range(len(nv)):
             assert np.array_equal(out[b], o.shape_velocities(b)), (step, b)
         changes += check_velocity_changes(rows, out, g["rigid_after"][step - 1])
+        if mode == "batched":
+            for b in range(len(nv)):
+                c = ctx.contacts(b)
+                contacts += check_manifold(manifolds.get((step, b)), b, rows, c["has_contact"], c["points"], c["normals"], c["shape"])
         off = 0
         for b in range(len(nv)):
             pos, loc, vel = ctx.read_body(b)
@@ -60,6 +68,7 @@ def test_coupling_bitwise_vs_reference_and_oracle(jsb, oracle_lib, name, mode):
             off += nv[b]
     ctx.close()
     assert changes > 50, changes
+    assert mode != "batched" or contacts > 1000, contacts
 
 
 def test_coupling_refused_where_unsupported(jsb):

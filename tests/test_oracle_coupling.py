@@ -9,7 +9,9 @@ each step every soft body's colliding shapes are fed to the oracle as the refere
 - every soft body's state bitwise equal to the reference (deterministic build) at every dumped step;
 - the dynamic bodies' velocity changes (UpdateRigidBodyVelocities, SoftBodyMotionProperties.cpp:923-935):
   the rigid body's velocity when collected plus the oracle's change equals the reference's velocity after
-  the step, bitwise.
+  the step, bitwise;
+- every step's SoftBodyManifold (what OnSoftBodyContactAdded sees): contact flags, local contact points and
+  normals bitwise, and the contacted rigid body.
 """
 import struct
 
@@ -81,21 +83,54 @@ def check_velocity_changes(rows, shape_out_by_body, after):
     return checked
 
 
+def manifolds_by_key(g):
+    """(step, soft body) -> the reference's SoftBodyManifold: (has (N,), points (N, 3), normals (N, 3), rigid (N,))."""
+    out, off = {}, 0
+    nv = list(g["num_vertices"])
+    for st, b in zip(g["manifold_step"], g["manifold_body"]):
+        n = nv[int(b)]
+        out[(int(st), int(b))] = (g["manifold_has"][off:off + n], g["manifold_point"][off:off + n], g["manifold_normal"][off:off + n],
+                                  g["manifold_rigid"][off:off + n])
+        off += n
+    return out
+
+
+def check_manifold(ref, body, rows, has, points, normals, shapes):
+    """A solver's manifold of one body and step (has, points, normals, shape index per vertex) against the
+    reference's (None: OnSoftBodyContactAdded was not called, so no vertex may touch)."""
+    has = np.asarray(has).astype(bool)
+    if ref is None:
+        assert not has.any()
+        return 0
+    rhas, rpts, rnrm, rrig = ref
+    assert np.array_equal(has, rhas.astype(bool))
+    assert np.array_equal(np.asarray(points)[has], rpts[has])
+    assert np.array_equal(np.asarray(normals)[has], rnrm[has])
+    rigid_of_shape = [r[1] for r in rows if r[0] == body]
+    assert [rigid_of_shape[s] for s in np.asarray(shapes)[has]] == list(rrig[has])
+    return int(has.sum())
+
+
 @pytest.mark.parametrize("name", ["coupling", "coupling_hulls"])
 def test_oracle_coupling_bitwise_vs_reference(oracle_lib, name):
     g = np.load(golden_path(name))
     scene, _ = parse_scene(g["scene"].tobytes())
     nv = list(g["num_vertices"])
     o = oracle_lib(scene)
+    o.set_contact_readback(True)
     tables = tables_by_step(g, register_hulls(g, o.add_hull))
+    manifolds = manifolds_by_key(g)
     dumps = set(int(s) for s in g["steps"])
-    changes = 0
+    changes = contacts = 0
     for step in range(1, int(g["steps"][-1]) + 1):
         rows = tables.get(step, [])
         for b in range(len(nv)):
             o.set_colliding_shapes(b, [r[2] for r in rows if r[0] == b])
         o.step(1)
         changes += check_velocity_changes(rows, {b: o.shape_velocities(b) for b in range(len(nv))}, g["rigid_after"][step - 1])
+        for b in range(len(nv)):
+            m = o.contacts(b)
+            contacts += check_manifold(manifolds.get((step, b)), b, rows, m[:, 0], m[:, 1:4], m[:, 4:7], m[:, 7].astype(np.int64))
         if step in dumps:
             off = 0
             for b in range(len(nv)):
@@ -105,3 +140,4 @@ def test_oracle_coupling_bitwise_vs_reference(oracle_lib, name):
                 assert np.array_equal(vel, g[f"det_vel_{step}"][off:off + nv[b]]), (step, b)
                 off += nv[b]
     assert changes > 50, changes  # the sphere and the box are pushed by their trampolines most of the run
+    assert contacts > 1000, contacts
