@@ -15,8 +15,8 @@
 //      body's state back (SoftBodyMotionProperties::RestoreState, body position).
 // Bodies the GPU path does not run (skinned constraints, rods, more than 65,536 vertices, a non-identity
 // rotation) are refused at AddBody; contact listeners and sensors are not consulted (the colliding
-// shapes use the default contact settings). Leaf shapes other than box, sphere, capsule and cylinder
-// (convex hulls, meshes, height fields) are not collided with: keep bodies that touch them on Jolt's CPU
+// shapes use the default contact settings). Leaf shapes other than box, sphere, capsule, cylinder and
+// convex hull (meshes, height fields) are not collided with: keep bodies that touch them on Jolt's CPU
 // path.
 #pragma once
 
@@ -30,6 +30,7 @@
 #include <Jolt/Physics/Collision/TransformedShape.h>
 #include <Jolt/Physics/Collision/Shape/BoxShape.h>
 #include <Jolt/Physics/Collision/Shape/CapsuleShape.h>
+#include <Jolt/Physics/Collision/Shape/ConvexHullShape.h>
 #include <Jolt/Physics/Collision/Shape/CylinderShape.h>
 #include <Jolt/Physics/Collision/Shape/SphereShape.h>
 #include <Jolt/Physics/SoftBody/SoftBodyCreationSettings.h>
@@ -189,6 +190,10 @@ private:
                     s.radius = static_cast<const CylinderShape *>(shape)->GetRadius();
                     s.half_extent[1] = static_cast<const CylinderShape *>(shape)->GetHalfHeight();
                     break;
+                case EShapeSubType::ConvexHull:
+                    s.type = JSB_COLLIDER_HULL;
+                    if (!HullID(static_cast<const ConvexHullShape *>(shape), s.hull_id)) continue;
+                    break;
                 default:
                     continue;  // not on the GPU path (see the header comment)
             }
@@ -240,6 +245,34 @@ private:
         }
     }
 
+    // Registers a ConvexHullShape once (its points, planes and faces as Jolt built them).
+    bool HullID(const JPH::ConvexHullShape *inHull, uint32_t &outID) {
+        auto it = mHulls.find(inHull);
+        if (it != mHulls.end()) {
+            outID = it->second;
+            return true;
+        }
+        std::vector<float> points, planes;
+        std::vector<uint32_t> counts, indices;
+        for (JPH::uint i = 0; i < inHull->GetNumPoints(); ++i) {
+            const JPH::Vec3 p = inHull->GetPoint(i);
+            points.insert(points.end(), {p.GetX(), p.GetY(), p.GetZ()});
+        }
+        JPH::uint face[256];
+        for (JPH::uint f = 0; f < inHull->GetNumFaces(); ++f) {
+            const JPH::Plane &pl = inHull->GetPlanes()[f];
+            planes.insert(planes.end(), {pl.GetNormal().GetX(), pl.GetNormal().GetY(), pl.GetNormal().GetZ(), pl.GetConstant()});
+            const JPH::uint n = inHull->GetFaceVertices(f, 256, face);
+            counts.push_back(n);
+            indices.insert(indices.end(), face, face + n);
+        }
+        jsb_convex_hull h = {uint32_t(inHull->GetNumPoints()), points.data(), uint32_t(inHull->GetNumFaces()), planes.data(),
+                             counts.data(), indices.data()};
+        if (jsb_hull_add(mCtx, &h, &outID) != JSB_OK) return false;
+        mHulls[inHull] = outID;
+        return true;
+    }
+
     bool UploadSettings(const JPH::SoftBodySharedSettings *inSettings, uint32_t &outID) {  // once per settings object
         auto it = mSettings.find(inSettings);
         if (it != mSettings.end()) {
@@ -262,6 +295,7 @@ private:
 
     jsb_context *mCtx = nullptr;
     std::unordered_map<const JPH::SoftBodySharedSettings *, uint32_t> mSettings;
+    std::unordered_map<const JPH::ConvexHullShape *, uint32_t> mHulls;
     std::vector<Entry> mBodies;
     std::vector<Shapes> mShapes;
 };
