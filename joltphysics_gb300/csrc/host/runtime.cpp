@@ -36,8 +36,8 @@ cudaError_t init_step_kernels(int max_dynamic_smem);
 cudaError_t launch_step_tape(const StepParams &p, int threads, bool smem_state, uint32_t smem_vertices, uint32_t smem_faces, int grid,
                              cudaStream_t stream);
 int step_tape_occupancy(int threads, bool smem_state, size_t smem);
-size_t cluster_smem_bytes(uint32_t shift, uint32_t desc_cap, uint32_t rpt, int threads);
-cudaError_t launch_cluster_step(const StepParams &p, int cluster, int threads, uint32_t shift, uint32_t desc_cap, uint32_t rpt,
+size_t cluster_smem_bytes(uint32_t shift, uint32_t desc_cap);
+cudaError_t launch_cluster_step(const StepParams &p, int cluster, int threads, uint32_t shift, uint32_t desc_cap,
                                 cudaStream_t stream);
 cudaError_t init_cluster_kernels(int max_dynamic_smem);
 int cluster_occupancy(int cluster, int threads, size_t smem);
@@ -154,7 +154,7 @@ struct Bucket {
 
 struct LaunchGroup {  // the bodies of one bucket (or every body on the cluster path)
     int cluster = 0;  // > 0: CTAs per cluster, one cluster per body (cluster.cu)
-    uint32_t shift = 0, desc_cap = 0, rpt = 1;  // cluster path: vertices per CTA (log2), cached level descriptors, ring depth
+    uint32_t shift = 0, desc_cap = 0;  // cluster path: vertices per CTA (log2), cached level descriptors
     int threads = 0;
     bool smem_state = true;  // velocities / previous positions staged in shared memory
     uint32_t smem_vertices = 0, smem_faces = 0;
@@ -423,6 +423,19 @@ uint32_t ring_slots_for(const jsb_context *ctx, const BodyRec &b) {
 // stage several to a chunk.
 uint32_t ring_half_for(const jsb_context *ctx, const BodyRec &b) { return 2 * ring_slots_for(ctx, b); }
 
+constexpr uint32_t kMaxGrownRingSlots = 4096;  // 64 KB per half
+
+// Record slots per half at which body b's chunks would average kStageLevels levels (its schedule's slots
+// per level x kStageLevels, rounded up to 32, capped).
+uint32_t ring_half_full(const jsb_context *ctx, const BodyRec &b) {
+    const SettingsRec &s = *ctx->settings[b.settings_id];
+    const StepSchedRec *ss = step_sched(ctx, b);
+    const uint64_t slots = ss ? ss->sched.num_slots : s.schedule.num_slots;
+    const uint64_t levels = std::max<uint64_t>(1, ss ? ss->sched.num_levels : s.schedule.num_levels);
+    const uint64_t r = ((slots * kStageLevels / levels) + 31u) & ~uint64_t(31);
+    return uint32_t(std::min<uint64_t>(r, kMaxGrownRingSlots));
+}
+
 // Staging chunks of a schedule for ring halves of `half` slots, built and uploaded once per half.
 jsb_status chunk_table(std::map<uint32_t, std::pair<DevBuf<uint4>, uint32_t>> &cache, const std::vector<uint32_t> &levels,
                        uint32_t num_levels, bool per_substep, uint32_t half, const uint4 *&ptr, uint32_t &count) {
@@ -553,12 +566,11 @@ jsb_status rebuild(jsb_context *ctx) {
 // The launch group of the cluster path: one cluster per body; the cluster size is the configured one,
 // or the largest (16, 8, 4, 2) that the device can co-schedule with the shared memory it needs.
 jsb_status make_cluster_group(jsb_context *ctx, const std::vector<uint32_t> &bodies, size_t cap) {
-    uint32_t max_nv = 0, max_levels = 0, max_slots = 0;
+    uint32_t max_nv = 0, max_levels = 0;
     for (uint32_t bi : bodies) {
         const SettingsRec &s = *ctx->settings[ctx->bodies[bi].settings_id];
         max_nv = std::max(max_nv, uint32_t(s.parsed.vertices.size()));
         max_levels = std::max(max_levels, s.schedule.num_levels);
-        max_slots = std::max(max_slots, s.schedule.max_level_slots);
     }
     const int T = ctx->cluster_threads;
     const int sizes[4] = {16, 8, 4, 2};
@@ -567,12 +579,10 @@ jsb_status make_cluster_group(jsb_context *ctx, const std::vector<uint32_t> &bod
         const uint32_t per_cta = std::max<uint32_t>(32u, (max_nv + uint32_t(c) - 1) / uint32_t(c));
         uint32_t shift = 5;
         while ((1u << shift) < per_cta) ++shift;
-        uint32_t rpt = std::max<uint32_t>(1u, std::min<uint32_t>(4u, (max_slots + uint32_t(c * T) - 1) / uint32_t(c * T)));
         uint32_t desc_cap = std::min<uint32_t>(max_levels + 2, kMaxCachedLevels);
-        // Shrink the descriptor cache, then the ring, until the CTA fits.
-        while (cluster_smem_bytes(shift, desc_cap, rpt, T) > cap && desc_cap > 0) desc_cap = desc_cap > 256 ? desc_cap - 256 : 0;
-        while (cluster_smem_bytes(shift, desc_cap, rpt, T) > cap && rpt > 1) --rpt;
-        const size_t smem = cluster_smem_bytes(shift, desc_cap, rpt, T);
+        // Shrink the descriptor cache until the CTA fits.
+        while (cluster_smem_bytes(shift, desc_cap) > cap && desc_cap > 0) desc_cap = desc_cap > 256 ? desc_cap - 256 : 0;
+        const size_t smem = cluster_smem_bytes(shift, desc_cap);
         if (smem > cap || cluster_occupancy(c, T, smem) < 1) continue;
         ctx->groups.emplace_back();
         LaunchGroup &g = ctx->groups.back();
@@ -580,7 +590,6 @@ jsb_status make_cluster_group(jsb_context *ctx, const std::vector<uint32_t> &bod
         g.threads = T;
         g.shift = shift;
         g.desc_cap = desc_cap;
-        g.rpt = rpt;
         g.smem_vertices = max_nv;
         g.bodies = bodies;
         g.grid = c * int(bodies.size());
@@ -614,6 +623,8 @@ jsb_status rebuild_groups(jsb_context *ctx) {
         }
         members[k].push_back({body_cost(ctx, b, ctx->buckets[k].threads), uint32_t(bi)});
     }
+    size_t one_cta_bodies = 0;
+    for (auto &m : members) one_cta_bodies += m.size();
     for (size_t k = 0; k < ctx->buckets.size(); ++k) {
         if (members[k].empty()) continue;
         ctx->groups.emplace_back();
@@ -639,6 +650,25 @@ jsb_status rebuild_groups(jsb_context *ctx) {
         if (step_smem_bytes(g.smem_state, g.smem_vertices, g.smem_faces, g.ring_slots) > cap)
             return fail(JSB_ERR_UNSUPPORTED, "a body with " + std::to_string(g.smem_vertices) +
                                                  " vertices does not fit the shared-memory solver path");
+        // Every chunk costs a wait and two bulk copies: when every body can have an SM to itself, grow
+        // the halves towards chunks of kStageLevels levels while neither the CTAs per SM nor the
+        // placement of the state (in shared memory or not; also for the taped forward step, which
+        // stages with the same ring) change. (In a batch of more bodies than SMs, larger rings cost
+        // co-resident CTAs of the other buckets more than the fewer chunk turns save.)
+        if (one_cta_bodies <= size_t(ctx->num_sms)) {
+            uint32_t want = 0;
+            for (auto &m : members[k]) want = std::max(want, ring_half_full(ctx, ctx->bodies[m.second]));
+            const int occ0 = step_occupancy(g.threads, g.smem_state, step_smem_bytes(g.smem_state, g.smem_vertices, g.smem_faces, g.ring_slots));
+            const bool state_fits = step_smem_bytes(true, g.smem_vertices, g.smem_faces, g.ring_slots) <= cap;
+            while (g.ring_slots < want) {
+                const uint32_t r = std::min(want, g.ring_slots + std::max<uint32_t>(32, g.ring_slots / 2)) & ~31u;
+                const size_t bytes = step_smem_bytes(g.smem_state, g.smem_vertices, g.smem_faces, r);
+                if (r <= g.ring_slots || bytes > cap || step_occupancy(g.threads, g.smem_state, bytes) < occ0 ||
+                    (state_fits && step_smem_bytes(true, g.smem_vertices, g.smem_faces, r) > cap))
+                    break;
+                g.ring_slots = r;
+            }
+        }
         // Longest-processing-time-first order for the work queue.
         std::stable_sort(members[k].begin(), members[k].end(), [](const auto &a, const auto &b) { return a.first > b.first; });
         for (auto &m : members[k]) {
@@ -775,7 +805,7 @@ jsb_status enqueue_batched(jsb_context *ctx, float dt, cudaStream_t stream, uint
         p.queue = ctx->queues.ptr + gi;
         p.ring_slots = g.ring_slots;
         if (g.cluster > 0)
-            JSB_CUDA(launch_cluster_step(p, g.cluster, g.threads, g.shift, g.desc_cap, g.rpt, g.stream));
+            JSB_CUDA(launch_cluster_step(p, g.cluster, g.threads, g.shift, g.desc_cap, g.stream));
         else
             JSB_CUDA(launch_step(p, g.threads, g.smem_state, g.smem_vertices, g.smem_faces, g.grid, g.stream));
         ++launches;
@@ -827,7 +857,7 @@ jsb_status step_impl(jsb_context *ctx, float dt, int collision_steps, cudaStream
                     const SettingsRec &s = *ctx->settings[ctx->bodies[b].settings_id];
                     p.ring_slots = g.ring_slots;  // the ring the body's staging chunks were built for
                     if (g.cluster > 0)
-                        JSB_CUDA(launch_cluster_step(p, g.cluster, g.threads, g.shift, g.desc_cap, g.rpt, stream));
+                        JSB_CUDA(launch_cluster_step(p, g.cluster, g.threads, g.shift, g.desc_cap, stream));
                     else
                         JSB_CUDA(launch_step(p, g.threads, g.smem_state, uint32_t(s.parsed.vertices.size()),
                                              pressure_faces(s, ctx->bodies[b]), 1, stream));

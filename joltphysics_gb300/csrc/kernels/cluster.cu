@@ -86,8 +86,6 @@ __device__ __forceinline__ void stx(ClusterX c, uint32_t i, float4 v) {
                  : "memory");
 }
 
-constexpr int kCRingDepth = 3;  // levels staged ahead
-constexpr int kCRingLevels = kCRingDepth + 1;
 
 // Per-CTA partial results of UpdateSoftBodyState, read by rank 0 through distributed shared memory.
 struct Partials {
@@ -113,17 +111,19 @@ struct CShared {
 // CTA is dealt round-robin over the cluster: thread g (= rank * T + tid) projects slots g, g + G, ...
 // (G = cluster threads) and the level ends at a cluster barrier. A level of at most T slots goes to
 // CTA 0 alone (slot s to thread s); a run of such levels is separated by CTA 0's own barriers and ends
-// with one cluster barrier, which the other CTAs reach directly. The first `rpt` slots of each thread
-// are staged kCRingDepth levels ahead into the thread's ring slice.
+// with one cluster barrier, which the other CTAs reach directly. Each thread loads its first record of
+// the next level (and that level's descriptor) into registers before projecting the current one, so
+// the load is in flight during the projection and the barrier; a thread's further slots of a level
+// wider than the cluster are read where they are projected. No staging ring and no async-copy wait sit
+// in the level's critical path.
 template <int T, bool kGuard>
-__device__ __forceinline__ void cluster_levels(ClusterX cx, const BodyDesc &d, const uint4 *sdesc, uint32_t desc_cap, uint4 *ring,
-                                               uint32_t rpt, uint32_t rank, uint32_t G, float inv_dt_sq) {
+__device__ __forceinline__ void cluster_levels(ClusterX cx, const BodyDesc &d, const uint4 *sdesc, uint32_t desc_cap, uint32_t rank,
+                                               uint32_t G, float inv_dt_sq) {
     const uint32_t L = d.num_levels;
     if (L == 0) return;
     const uint4 *__restrict__ rec = d.records;
     const uint4 *__restrict__ levels = d.levels;
     const uint32_t tid = threadIdx.x, g = rank * T + tid;
-    uint4 *mine = ring + tid;
     auto desc = [&](uint32_t l) { return l < desc_cap ? sdesc[l] : __ldg(levels + l); };
     // First slot of this thread in a level of n slots (>= n: none) and the stride to its next slot.
     auto first_slot = [&](uint32_t n, uint32_t &stride) -> uint32_t {
@@ -134,49 +134,48 @@ __device__ __forceinline__ void cluster_levels(ClusterX cx, const BodyDesc &d, c
         stride = G;
         return g;
     };
-    auto stage = [&](uint32_t l) {
-        const uint4 lv = desc(l);
-        const uint32_t n = desc(l + 1).x - lv.x;
-        uint4 *dst = mine + (l % kCRingLevels) * rpt * T;
+    // This thread's first record of a level (a padding record when it has no slot there).
+    auto first_record = [&](uint4 lv, uint32_t n) -> uint4 {
+        uint32_t stride;
+        const uint32_t s = first_slot(n, stride);
+        return s < n ? __ldg(rec + lv.x + s) : make_uint4(0xffffffffu, 0u, 0u, 0u);
+    };
+    uint4 lv = desc(0);
+    uint32_t end = desc(1).x;
+    uint4 r0 = first_record(lv, end - lv.x);
+    for (uint32_t l = 0; l < L; ++l) {
+        const uint32_t n = end - lv.x;
+        uint4 lv1 = lv, r1 = r0;
+        uint32_t end1 = end;
+        if (l + 1 < L) {  // the next level (sentinel descriptors follow the last level)
+            lv1 = desc(l + 1);
+            end1 = desc(l + 2).x;
+            r1 = first_record(lv1, end1 - lv1.x);
+        }
         uint32_t stride;
         uint32_t s = first_slot(n, stride);
-        for (uint32_t k = 0; k < rpt && s < n; ++k, s += stride) cp_async16(dst + k * T, rec + lv.x + s);
-    };
-#pragma unroll
-    for (int k = 0; k < kCRingDepth; ++k) {
-        if (uint32_t(k) < L) stage(k);
-        cp_async_commit();
-    }
-    uint32_t next_first = desc(0).x;
-    for (uint32_t l = 0; l < L; ++l) {
-        if (l + kCRingDepth < L) stage(l + kCRingDepth);
-        cp_async_commit();
-        cp_async_wait<kCRingDepth>();  // this thread's copies of level l have landed
-        const uint4 lv = desc(l);
-        const uint32_t end = desc(l + 1).x;
-        const uint32_t n = end - lv.x;
-        next_first = end;
-        const uint4 *src = mine + (l % kCRingLevels) * rpt * T;
-        uint32_t stride;
-        uint32_t k = 0;
-        for (uint32_t s = first_slot(n, stride); s < n; s += stride, ++k) {
-            const uint4 r = k < rpt ? src[k * T] : __ldg(rec + lv.x + s);
-            if (r.x != 0xffffffffu) project<kGuard>(cx, r, slot_type(lv, s), inv_dt_sq);
+        if (s < n) {
+            if (r0.x != 0xffffffffu) project<kGuard>(cx, r0, slot_type(lv, s), inv_dt_sq);
+            for (s += stride; s < n; s += stride) {
+                const uint4 r = __ldg(rec + lv.x + s);
+                if (r.x != 0xffffffffu) project<kGuard>(cx, r, slot_type(lv, s), inv_dt_sq);
+            }
         }
-        const bool narrow_pair = n <= uint32_t(T) && l + 1 < L && desc(l + 2).x - next_first <= uint32_t(T);
+        const bool narrow_pair = n <= uint32_t(T) && l + 1 < L && end1 - end <= uint32_t(T);
         if (narrow_pair) {
             if (rank == 0) __syncthreads();  // only CTA 0 works on both levels
         } else {
             cluster_barrier();
         }
+        lv = lv1;
+        end = end1;
+        r0 = r1;
     }
-    cp_async_wait<0>();
 }
 
-// Dynamic shared memory of one CTA: positions [1 << shift] | level descriptors [desc_cap] |
-// record ring [kCRingLevels][rpt][T].
+// Dynamic shared memory of one CTA: positions [1 << shift] | level descriptors [desc_cap].
 template <int T>
-__global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t shift, uint32_t desc_cap, uint32_t rpt) {
+__global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t shift, uint32_t desc_cap) {
     extern __shared__ float4 smem[];
     __shared__ CShared sh;
     const uint32_t tid = threadIdx.x;
@@ -192,7 +191,6 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
     const uint32_t first = min(nv, rank << shift), last = min(nv, (rank + 1) << shift);
     float4 *sx = smem;
     uint4 *sdesc = reinterpret_cast<uint4 *>(smem + (size_t(1) << shift));
-    uint4 *ring = sdesc + desc_cap;
     const ClusterX cx{smem_u32(sx), shift};
     float4 *__restrict__ gx = p.x + d.vtx_offset;
     float4 *__restrict__ gv = p.v + d.vtx_offset;
@@ -265,9 +263,9 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
         bool guard = false;
         for (uint32_t q = 0; q < C; ++q) guard = guard || ld_cluster_s32(map_rank(smem_u32(&sh.nan_flag[it & 1]), q)) != 0;
         if (guard)
-            cluster_levels<T, true>(cx, d, sdesc, desc_cap, ring, rpt, rank, G, inv_dt_sq);
+            cluster_levels<T, true>(cx, d, sdesc, desc_cap, rank, G, inv_dt_sq);
         else
-            cluster_levels<T, false>(cx, d, sdesc, desc_cap, ring, rpt, rank, G, inv_dt_sq);
+            cluster_levels<T, false>(cx, d, sdesc, desc_cap, rank, G, inv_dt_sq);
         // ApplyCollisionConstraintsAndUpdateVelocities (owned vertices; the last level's barrier made
         // every remote write visible). The next integration touches owned vertices only.
         for (uint32_t i = first + tid; i < last; i += T) {
@@ -405,9 +403,8 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
 }  // namespace
 
 // Bytes of dynamic shared memory of one cluster CTA.
-size_t cluster_smem_bytes(uint32_t shift, uint32_t desc_cap, uint32_t rpt, int threads) {
-    return (size_t(1) << shift) * sizeof(float4) + size_t(desc_cap) * sizeof(uint4) +
-           size_t(kCRingLevels) * rpt * size_t(threads) * sizeof(uint4);
+size_t cluster_smem_bytes(uint32_t shift, uint32_t desc_cap) {
+    return (size_t(1) << shift) * sizeof(float4) + size_t(desc_cap) * sizeof(uint4);
 }
 
 #define JSB_FOR_EACH_CLUSTER_SHAPE(X) X(128) X(256) X(512)
@@ -429,13 +426,13 @@ static cudaLaunchConfig_t cluster_config(int cluster, int threads, size_t smem, 
 }
 
 // Launches one step of `p.num_work` bodies, one cluster of `cluster` CTAs each.
-cudaError_t launch_cluster_step(const StepParams &p, int cluster, int threads, uint32_t shift, uint32_t desc_cap, uint32_t rpt,
+cudaError_t launch_cluster_step(const StepParams &p, int cluster, int threads, uint32_t shift, uint32_t desc_cap,
                                 cudaStream_t stream) {
     cudaLaunchAttribute attr;
-    const cudaLaunchConfig_t cfg = cluster_config(cluster, threads, cluster_smem_bytes(shift, desc_cap, rpt, threads),
+    const cudaLaunchConfig_t cfg = cluster_config(cluster, threads, cluster_smem_bytes(shift, desc_cap),
                                                   unsigned(cluster) * p.num_work, stream, &attr);
 #define JSB_CLAUNCH(TT) \
-    if (threads == TT) return cudaLaunchKernelEx(&cfg, cluster_step_kernel<TT>, p, shift, desc_cap, rpt);
+    if (threads == TT) return cudaLaunchKernelEx(&cfg, cluster_step_kernel<TT>, p, shift, desc_cap);
     JSB_FOR_EACH_CLUSTER_SHAPE(JSB_CLAUNCH)
 #undef JSB_CLAUNCH
     return cudaErrorInvalidValue;

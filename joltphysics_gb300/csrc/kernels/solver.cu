@@ -73,6 +73,45 @@ __device__ __forceinline__ void stage_copy(void *dst, const void *src, uint32_t 
                  : "memory");
 }
 
+// L2 eviction policies. The whole-step records of a batch stream through L2 once per step (hundreds of
+// MB, more than L2 holds); copied with evict_first they do not push out the per-vertex collision planes,
+// which are written at the start of the step and read again in every substep's collision pass, stored
+// and loaded with evict_last.
+__device__ __forceinline__ uint64_t l2_evict_first() {
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ uint64_t l2_evict_last() {
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+// Thread 0: as stage_copy, for data read once (records and level descriptors of a schedule).
+__device__ __forceinline__ void stage_copy_stream(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(l2_evict_first())
+                 : "memory");
+}
+
+// A collision plane, kept in L2 (evict_last) between the writes at the start of a step and the reads of
+// the substeps.
+__device__ __forceinline__ void store_plane(float4 *dst, float4 v) {
+    asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(dst), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w),
+                 "l"(l2_evict_last())
+                 : "memory");
+}
+__device__ __forceinline__ float4 load_plane(const float4 *src) {
+    float4 v;
+    asm volatile("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "l"(src), "l"(l2_evict_last())
+                 : "memory");
+    return v;
+}
+
 // Waits (bounded: about 2^20 polls) for phase `parity` of `bar`; false when it gave up.
 __device__ __forceinline__ bool stage_wait(uint64_t *bar, uint32_t parity) {
     for (uint32_t it = 0; it < (1u << 20); ++it) {
@@ -108,8 +147,8 @@ __device__ __forceinline__ void ring_issue(const StageRing &ring, uint32_t h, ui
     const uint32_t desc_bytes = (ch.y - ch.x + extra_desc) * uint32_t(sizeof(uint4));
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     stage_expect(&ring.bar[h], rec_bytes + desc_bytes);
-    if (rec_bytes) stage_copy(ring.rec + h * ring.half, records + ch.z, rec_bytes, &ring.bar[h]);
-    stage_copy(ring.desc + h * (kStageLevels + 1), levels + ch.x, desc_bytes, &ring.bar[h]);
+    if (rec_bytes) stage_copy_stream(ring.rec + h * ring.half, records + ch.z, rec_bytes, &ring.bar[h]);
+    stage_copy_stream(ring.desc + h * (kStageLevels + 1), levels + ch.x, desc_bytes, &ring.bar[h]);
 }
 
 // All threads: waits (bounded) for the chunk in half h. On a timeout the CTA reports it, gives the
@@ -206,13 +245,17 @@ __device__ __forceinline__ void vertex_between_substeps(float4 *sx, const Vertex
     float4 vel = kSmemState ? vp.sv[i] : vp.gv[i];
     if (kTape) vp.tape[(size_t(k - 1) * 3 + 2) * vp.nv + i] = pi;
     if (pi.w > 0.0f) {
+        int shape = -1;
+        float4 plane;
+        if (vp.ncols > 0) {
+            shape = kSmemState ? __float_as_int(vel.w) : vp.gshape[i];
+            if (shape >= 0) plane = load_plane(vp.gplane + i);  // issued first: the longest latency of the pass
+        }
         const float4 prev = kSmemState ? vp.sprev[i] : vp.gprev[i];
         f3 x = xyz(pi);
         const f3 prev_v = xyz(vel);
         f3 v = div3_rn(x - xyz(prev), vp.dt_sub);
-        int shape = -1;
-        if (vp.ncols > 0) shape = kSmemState ? __float_as_int(vel.w) : vp.gshape[i];
-        if (shape >= 0 && collide_vertex(x, v, prev_v, vp.gplane[i], vp.cols[shape], vp.radius, vp.dt_sub, vp.restitution_threshold)) {
+        if (shape >= 0 && collide_vertex(x, v, prev_v, plane, vp.cols[shape], vp.radius, vp.dt_sub, vp.restitution_threshold)) {
             pi = with_w(x, pi.w);
             if (vp.contact) vp.contact[i] = 1;
         }
@@ -380,7 +423,7 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
         if (kSmemState)
             sv[i].w = __int_as_float(shape);
         if (!kSmemState || p.contact) gshape[i] = shape;
-        if (shape >= 0) gplane[i] = plane;
+        if (shape >= 0) store_plane(gplane + i, plane);
         if (p.contact) p.contact[d.vtx_offset + i] = 0;
         if (kTape) {
             td.plane[size_t(p.tape_step) * nv + i] = plane;
@@ -535,7 +578,7 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
             int shape = -1;
             if (ncols > 0) shape = kSmemState ? __float_as_int(vel.w) : gshape[i];
             if (has_dynamic && shape >= 0 && (sh.cols[shape].flags & kColDynamic)) continue;  // below, in vertex order
-            if (shape >= 0 && collide_vertex(x, v, prev_v, gplane[i], sh.cols[shape], d.vertex_radius, dt_sub, restitution_threshold)) {
+            if (shape >= 0 && collide_vertex(x, v, prev_v, load_plane(gplane + i), sh.cols[shape], d.vertex_radius, dt_sub, restitution_threshold)) {
                 sx[i] = with_w(x, pi.w);
                 if (p.contact) p.contact[d.vtx_offset + i] = 1;
             }
