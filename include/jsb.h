@@ -122,6 +122,10 @@ jsb_status jsb_body_num_vertices(jsb_context *ctx, uint32_t body_id, uint32_t *n
 
 /* ---- host-determined colliding shapes (rigid bodies that move; two-way coupling) ------------- */
 enum { JSB_MOTION_STATIC = 0, JSB_MOTION_KINEMATIC = 1, JSB_MOTION_DYNAMIC = 2 }; /* EMotionType */
+/* A leaf shape of a sensor (SoftBodyMotionProperties::CollidingSensor, collected when the contact listener
+ * accepts a body with SoftBodyContactSettings::mIsSensor: SoftBodyMotionProperties.cpp:191-198): it moves
+ * no vertex; the step reports whether a vertex with inverse mass > 0 penetrates it (jsb_body_sensor_contacts). */
+enum { JSB_MOTION_SENSOR = 3 };
 
 /* One colliding shape of a soft body, as SoftBodyMotionProperties::DetermineCollidingShapes collects it
  * (SoftBodyMotionProperties.cpp:120-255; fields of CollidingShape and its LeafShape, SoftBodyMotionProperties.h):
@@ -186,6 +190,12 @@ jsb_status jsb_set_contact_readback(jsb_context *ctx, int enable);
  * NULL. Not recorded on the thread-block-cluster path (JSB_ERR_UNSUPPORTED). */
 jsb_status jsb_body_contacts(jsb_context *ctx, uint32_t body_id, uint8_t *has_contact, float *contact_points, float *normals,
                              int32_t *shape_index, float delta[3]);
+/* After a step (synchronises the device): bit k of *mask is set when shape k of the body's host-determined
+ * shapes is a sensor shape (JSB_MOTION_SENSOR) that a vertex with inverse mass > 0 penetrated at the start
+ * of the step (DetermineSensorCollisions, SoftBodyMotionProperties.cpp:267-289: CollidingSensor::mHasContact;
+ * the sensors of SoftBodyManifold::GetSensorContactBodyID are those with a set bit in any of their shapes).
+ * 0 for a body without host-determined shapes. */
+jsb_status jsb_body_sensor_contacts(jsb_context *ctx, uint32_t body_id, uint32_t *mask);
 
 /* ---- stepping ----------------------------------------------------------------------------- */
 /* PhysicsSystem::Update's soft-body part for every body in the context: InitializeUpdateContext,

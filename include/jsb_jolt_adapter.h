@@ -14,10 +14,14 @@
 //   4. writes the rigid bodies' velocity changes back (UpdateRigidBodyVelocities, :923-935) and each soft
 //      body's state back (SoftBodyMotionProperties::RestoreState, body position).
 // Bodies the GPU path does not run (skinned constraints, rods, more than 65,536 vertices, a non-identity
-// rotation) are refused at AddBody; contact listeners and sensors are not consulted (the colliding
-// shapes use the default contact settings). Leaf shapes other than box, sphere, capsule, cylinder and
-// convex hull (meshes, height fields) are not collided with: keep bodies that touch them on Jolt's CPU
-// path.
+// rotation) are refused at AddBody. With a SoftBodyContactListener set (SetContactListener), every
+// candidate body goes through its OnSoftBodyContactValidate like in the reference (rejections, inverse
+// mass scales, sensors); without one, sensors are ignored and the default contact settings apply, as in
+// the reference. SoftBodyManifold cannot be built outside Jolt (its constructor is private), so the
+// contacts OnSoftBodyContactAdded would report reach an adapter callback instead (SetContactCallback):
+// per vertex contact flag, local contact point, normal and rigid body, plus the sensors a vertex entered.
+// Leaf shapes other than box, sphere, capsule, cylinder and convex hull (meshes, height fields) are not
+// collided with: keep bodies that touch them on Jolt's CPU path.
 #pragma once
 
 #include <Jolt/Jolt.h>
@@ -33,10 +37,12 @@
 #include <Jolt/Physics/Collision/Shape/ConvexHullShape.h>
 #include <Jolt/Physics/Collision/Shape/CylinderShape.h>
 #include <Jolt/Physics/Collision/Shape/SphereShape.h>
+#include <Jolt/Physics/SoftBody/SoftBodyContactListener.h>
 #include <Jolt/Physics/SoftBody/SoftBodyCreationSettings.h>
 #include <Jolt/Physics/SoftBody/SoftBodyMotionProperties.h>
 
 #include <cstring>
+#include <functional>
 #include <sstream>
 #include <string>
 #include <unordered_map>
@@ -45,6 +51,16 @@
 #include "jsb.h"
 
 namespace jsb_jolt {
+
+// What OnSoftBodyContactAdded's SoftBodyManifold reports for one soft body after a step.
+struct SoftBodyContacts {
+    JPH::BodyID mSoftBody;
+    std::vector<uint8_t> mHasContact;       // per vertex (SoftBodyManifold::HasContact)
+    std::vector<float> mLocalContactPoint;  // 3 per vertex (GetLocalContactPoint)
+    std::vector<float> mContactNormal;      // 3 per vertex (GetContactNormal)
+    std::vector<JPH::BodyID> mContactBody;  // per vertex (GetContactBodyID; invalid without contact)
+    std::vector<JPH::BodyID> mSensors;      // GetSensorContactBodyID
+};
 
 class GpuSoftBodyStepper {
 public:
@@ -78,6 +94,16 @@ public:
         return true;
     }
 
+    // The reference's SoftBodyContactListener, consulted for every candidate rigid body (null: none).
+    void SetContactListener(JPH::SoftBodyContactListener *inListener) { mListener = inListener; }
+
+    // Called after a step for every soft body that touched a shape or entered a sensor (where the reference
+    // calls OnSoftBodyContactAdded); switches the contact readback on.
+    void SetContactCallback(std::function<void(const SoftBodyContacts &)> inCallback) {
+        mContactCallback = std::move(inCallback);
+        Check(jsb_set_contact_readback(mCtx, mContactCallback ? 1 : 0));
+    }
+
     // Replaces the soft-body part of PhysicsSystem::Update for the registered bodies; call it where the
     // soft-body jobs would run (after the rigid bodies' position solve). inStream: the CUDA stream.
     void Step(JPH::PhysicsSystem &ioSystem, float inDeltaTime, int inCollisionSteps, jsb_stream inStream) {
@@ -106,6 +132,7 @@ public:
         for (size_t b = 0; b < mBodies.size(); ++b) {
             const Entry &e = mBodies[b];
             WriteBackVelocities(ioSystem, bi, e, mShapes[b]);
+            if (mContactCallback) ReportContacts(e, mShapes[b]);
             size_t len = 0;
             Check(jsb_body_save_state(mCtx, e.mGpu, nullptr, 0, &len));
             std::string bytes(len, '\0');
@@ -139,7 +166,8 @@ private:
             for (int r = 0; r < 3; ++r) outColumns[3 * c + r] = inM(r, c);
     }
 
-    // SoftBodyMotionProperties::DetermineCollidingShapes for one body (:120-255), default contact settings.
+    // SoftBodyMotionProperties::DetermineCollidingShapes for one body (:120-255), with the listener's
+    // contact settings (or the defaults).
     void CollectShapes(JPH::PhysicsSystem &ioSystem, const Entry &inEntry, Shapes &outShapes) {
         using namespace JPH;
         float lb[6], pb[6];
@@ -161,9 +189,19 @@ private:
             BodyLockRead lock(ioSystem.GetBodyLockInterfaceNoLock(), id);
             if (!lock.Succeeded()) continue;
             const Body &body = lock.GetBody();
-            if (!body.IsRigidBody() || body.IsSensor() || !soft_body.GetCollisionGroup().CanCollide(body.GetCollisionGroup()) ||
+            if (!body.IsRigidBody() || !soft_body.GetCollisionGroup().CanCollide(body.GetCollisionGroup()) ||
                 !world_bounds.Overlaps(body.GetWorldSpaceBounds()))
                 continue;
+            SoftBodyContactSettings settings;
+            settings.mIsSensor = body.IsSensor();
+            if (mListener == nullptr) {
+                if (settings.mIsSensor) continue;  // no listener: sensors are ignored
+            } else {
+                if (mListener->OnSoftBodyContactValidate(soft_body, body, settings) != SoftBodyValidateResult::AcceptContact) continue;
+                if (!settings.mIsSensor && settings.mInvMassScale1 == 0.0f &&
+                    (body.GetMotionType() != EMotionType::Dynamic || settings.mInvMassScale2 == 0.0f))
+                    continue;  // no interaction
+            }
             const Mat44 com = (inverse * body.GetCenterOfMassTransform()).ToMat44();
             jsb_colliding_shape s = {};
             const Shape *shape = body.GetShape();
@@ -199,18 +237,18 @@ private:
             }
             // LeafShape::mTransform as CollectTransformedShapes + the collector rebuild it
             PutMatrix(Mat44::sRotationTranslation(com.GetQuaternion(), com.GetTranslation()), s.transform, 4);
-            s.motion_type = int32_t(body.GetMotionType());
+            s.motion_type = settings.mIsSensor ? int32_t(JSB_MOTION_SENSOR) : int32_t(body.GetMotionType());
             s.friction = ioSystem.GetCombineFriction()(soft_body, SubShapeID(), body, SubShapeID());
             s.restitution = ioSystem.GetCombineRestitution()(soft_body, SubShapeID(), body, SubShapeID());
-            s.soft_body_inv_mass_scale = 1.0f;
+            s.soft_body_inv_mass_scale = settings.mInvMassScale1;
             const Vec3 t = com.GetTranslation();
             s.center_of_mass[0] = t.GetX();
             s.center_of_mass[1] = t.GetY();
             s.center_of_mass[2] = t.GetZ();
-            if (body.GetMotionType() == EMotionType::Dynamic) {
+            if (!settings.mIsSensor && body.GetMotionType() == EMotionType::Dynamic) {
                 const MotionProperties *mp = body.GetMotionProperties();
-                s.inv_mass = mp->GetInverseMass();
-                PutMatrix(mp->GetInverseInertiaForRotation(com.GetRotation()), s.inv_inertia, 4);
+                s.inv_mass = settings.mInvMassScale2 * mp->GetInverseMass();
+                PutMatrix(settings.mInvInertiaScale2 * mp->GetInverseInertiaForRotation(com.GetRotation()), s.inv_inertia, 4);
                 const Vec3 lin = inverse.Multiply3x3(mp->GetLinearVelocity()), ang = inverse.Multiply3x3(mp->GetAngularVelocity());
                 for (int k = 0; k < 3; ++k) {
                     s.linear_velocity[k] = lin[k];
@@ -243,6 +281,36 @@ private:
             const Vec3 ang0(s.angular_velocity[0], s.angular_velocity[1], s.angular_velocity[2]);
             ioBI.AddLinearAndAngularVelocity(inShapes.bodies[k], com_transform.Multiply3x3(lin - lin0), com_transform.Multiply3x3(ang - ang0));
         }
+    }
+
+    // The step's contacts of one soft body to the contact callback, if it touched a shape or entered a sensor.
+    void ReportContacts(const Entry &inEntry, const Shapes &inShapes) {
+        uint32_t nv = 0;
+        Check(jsb_body_num_vertices(mCtx, inEntry.mGpu, &nv));
+        SoftBodyContacts c;
+        c.mSoftBody = inEntry.mJolt;
+        c.mHasContact.resize(nv);
+        c.mLocalContactPoint.resize(3 * size_t(nv));
+        c.mContactNormal.resize(3 * size_t(nv));
+        std::vector<int32_t> shape(nv);
+        Check(jsb_body_contacts(mCtx, inEntry.mGpu, c.mHasContact.data(), c.mLocalContactPoint.data(), c.mContactNormal.data(),
+                                shape.data(), nullptr));
+        uint32_t sensors = 0;
+        Check(jsb_body_sensor_contacts(mCtx, inEntry.mGpu, &sensors));
+        bool any = false;
+        c.mContactBody.resize(nv);
+        for (uint32_t i = 0; i < nv; ++i)
+            if (c.mHasContact[i] && shape[i] >= 0 && size_t(shape[i]) < inShapes.bodies.size()) {
+                c.mContactBody[i] = inShapes.bodies[size_t(shape[i])];
+                any = true;
+            }
+        for (size_t k = 0; k < inShapes.bodies.size(); ++k)
+            if ((sensors >> k) & 1u) {
+                bool seen = false;  // a sensor body with several leaf shapes is reported once
+                for (const JPH::BodyID &id : c.mSensors) seen = seen || id == inShapes.bodies[k];
+                if (!seen) c.mSensors.push_back(inShapes.bodies[k]);
+            }
+        if (any || !c.mSensors.empty()) mContactCallback(c);
     }
 
     // Registers a ConvexHullShape once (its points, planes and faces as Jolt built them).
@@ -298,6 +366,8 @@ private:
     std::unordered_map<const JPH::ConvexHullShape *, uint32_t> mHulls;
     std::vector<Entry> mBodies;
     std::vector<Shapes> mShapes;
+    JPH::SoftBodyContactListener *mListener = nullptr;
+    std::function<void(const SoftBodyContacts &)> mContactCallback;
 };
 
 }  // namespace jsb_jolt

@@ -52,6 +52,7 @@ SIGNATURES = {
     "jsb_body_contacts": [_P, _c.c_uint32, _P, _P, _P, _P, _P],
     "jsb_body_clear_colliding_shapes": [_P, _c.c_uint32],
     "jsb_body_shape_velocities": [_P, _c.c_uint32, _P, _c.POINTER(_c.c_uint32)],
+    "jsb_body_sensor_contacts": [_P, _c.c_uint32, _c.POINTER(_c.c_uint32)],
     "jsb_step": [_P, _c.c_float, _c.c_int, _P],
     "jsb_step_plain": [_P, _c.c_float, _c.c_int, _P],
     "jsb_step_graph": [_P, _c.c_float, _c.c_int, _c.c_int, _c.c_int, _P],
@@ -292,6 +293,12 @@ class Context:
         check(lib().jsb_body_contacts(self.h, body, has.ctypes.data, cp.ctypes.data, nrm.ctypes.data, shape.ctypes.data,
                                       delta.ctypes.data))
         return {"has_contact": has, "points": cp, "normals": nrm, "shape": shape, "delta": delta}
+
+    def sensor_contacts(self, body: int) -> int:
+        """Bit k: host-determined shape k is a sensor shape a vertex penetrated in the last step."""
+        m = ctypes.c_uint32()
+        check(lib().jsb_body_sensor_contacts(self.h, body, ctypes.byref(m)))
+        return int(m.value)
 
     def shape_velocities(self, body: int) -> np.ndarray:
         """Per host-determined shape after the last step: (updated, linear velocity[3], angular velocity[3])."""

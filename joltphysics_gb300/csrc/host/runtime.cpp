@@ -278,6 +278,7 @@ struct jsb_context {
     jsb::DevBuf<uint8_t> contact;
     jsb::DevBuf<float4> contact_point;
     jsb::DevBuf<float> contact_delta;
+    jsb::DevBuf<uint32_t> sensor_contact;  // per body: sensor shapes of its table with a vertex inside
     jsb::DevBuf<jsb::HullDev> hulls_dev;
     jsb::DevBuf<float4> hull_f4_dev;
     jsb::DevBuf<uint32_t> hull_u32_dev;
@@ -541,6 +542,10 @@ jsb_status rebuild(jsb_context *ctx) {
         if (old_sleep) JSB_CUDA(cudaMemcpy(hs.data(), ctx->sleep.ptr, old_sleep * sizeof(BodySleep), cudaMemcpyDeviceToHost));
         JSB_CUDA(ctx->sleep.upload(hs.data(), hs.size()));
     }
+    if (ctx->sensor_contact.count < std::max<size_t>(ctx->bodies.size(), 1)) {
+        JSB_CUDA(ctx->sensor_contact.alloc(std::max<size_t>(ctx->bodies.size(), 1)));
+        JSB_CUDA(cudaMemset(ctx->sensor_contact.ptr, 0, ctx->sensor_contact.count * sizeof(uint32_t)));
+    }
     JSB_CUDA(ctx->colliders_dev.upload(ctx->colliders.data(), ctx->colliders.size()));
     ctx->pending_force.resize(ctx->bodies.size() * 3, 0.0f);
     if (ctx->pending_force_pinned) cudaFreeHost(ctx->pending_force_pinned);
@@ -738,6 +743,7 @@ StepParams base_params(jsb_context *ctx, float dt) {
     p.contact = contacts ? ctx->contact.ptr : nullptr;
     p.contact_point = contacts ? ctx->contact_point.ptr : nullptr;
     p.contact_delta = contacts ? ctx->contact_delta.ptr : nullptr;
+    p.sensor_contact = tables ? ctx->sensor_contact.ptr : nullptr;
     return p;
 }
 
@@ -1120,7 +1126,7 @@ jsb_status jsb_body_set_colliding_shapes(jsb_context *ctx, uint32_t body_id, con
             return fail(JSB_ERR_INVALID_ARGUMENT, "unknown collider type");
         if (shapes[k].type == JSB_COLLIDER_HULL && shapes[k].hull_id >= ctx->hulls_host.size())
             return fail(JSB_ERR_INVALID_ARGUMENT, "unknown hull id");
-        if (shapes[k].motion_type < JSB_MOTION_STATIC || shapes[k].motion_type > JSB_MOTION_DYNAMIC)
+        if (shapes[k].motion_type < JSB_MOTION_STATIC || shapes[k].motion_type > JSB_MOTION_SENSOR)
             return fail(JSB_ERR_INVALID_ARGUMENT, "unknown motion type");
         std::memcpy(&t[k], &shapes[k], sizeof(ShapeEntry));
     }
@@ -1162,6 +1168,17 @@ jsb_status jsb_hull_add(jsb_context *ctx, const jsb_convex_hull *h, uint32_t *hu
     ctx->hulls_host.push_back(d);
     ctx->hulls_dirty = true;
     *hull_id = uint32_t(ctx->hulls_host.size() - 1);
+    return JSB_OK;
+}
+
+jsb_status jsb_body_sensor_contacts(jsb_context *ctx, uint32_t body_id, uint32_t *mask) {
+    if (!check_ctx(ctx) || body_id >= ctx->bodies.size() || !mask) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    *mask = 0;
+    auto it = ctx->table_host.find(body_id);
+    if (it == ctx->table_host.end() || ctx->dirty || ctx->sensor_contact.count <= body_id) return JSB_OK;
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    JSB_CUDA(cudaDeviceSynchronize());
+    JSB_CUDA(cudaMemcpy(mask, ctx->sensor_contact.ptr + body_id, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     return JSB_OK;
 }
 

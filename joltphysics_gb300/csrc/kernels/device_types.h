@@ -83,6 +83,7 @@ struct BodyDesc {
 };
 
 enum : int32_t { kMotionStatic = 0, kMotionKinematic = 1, kMotionDynamic = 2 };  // EMotionType
+constexpr int32_t kMotionSensor = 3;  // a leaf shape of a sensor (SoftBodyMotionProperties::CollidingSensor)
 
 // A colliding shape of one body determined on the host (jsb_colliding_shape as uploaded): the fields of
 // SoftBodyMotionProperties::CollidingShape and its LeafShape that the step reads.
@@ -191,6 +192,7 @@ struct StepParams {
     const HullDev *hulls;      // registered convex hulls
     const float4 *hull_f4;
     const uint32_t *hull_u32;
+    uint32_t *sensor_contact;  // per body: bit k = sensor shape k of its table has a vertex inside it (mHasContact)
     BodySleep *sleep;      // per body (null: bodies never sleep)
     float sleep_velocity_threshold;  // PhysicsSettings::mPointVelocitySleepThreshold (compared with |v|^2)
     float time_before_sleep;         // PhysicsSettings::mTimeBeforeSleep

@@ -31,7 +31,7 @@ struct SCol {  // one colliding shape, relative to the soft body
     float c[9];          // rotation columns
     float ic[9], it[3];  // inverse transform (Mat44::InversedRotationTranslation): rotation columns, translation
 };
-enum : int32_t { kColRotated = 1, kColDynamic = 2 };
+enum : int32_t { kColRotated = 1, kColDynamic = 2, kColSensor = 4 };
 
 // NaN positions (a body that has blown up in the reference's own arithmetic) would send every division
 // and square root of a projection down the IEEE routines' slow path. For a body holding NaN positions
@@ -611,6 +611,7 @@ __device__ __forceinline__ int collision_plane(f3 x, const SCol *cols, int ncols
     int shape = -1;
     float largest = -FLT_MAX;
     for (int s = 0; s < ncols; ++s) {
+        if (cols[s].flags & kColSensor) continue;  // (host-determined shapes only; sensor_hits)
         if (cols[s].type == 4)  // (host-determined shapes only)
             collide_hull(x, cols[s], XformR{cols[s]}, hr, s, largest, plane, shape);
         else if (cols[s].flags & kColRotated)
@@ -619,6 +620,25 @@ __device__ __forceinline__ int collision_plane(f3 x, const SCol *cols, int ncols
             collide_shape(x, cols[s], XformT{ld3(cols[s].t)}, s, largest, plane, shape);
     }
     return shape;
+}
+
+// DetermineSensorCollisions (:267-289) for one vertex (inverse mass > 0): bit s set for each sensor shape s
+// the vertex penetrates. The reference shares one penetration over all vertices of a sensor and reports a
+// contact when the largest is positive, that is when some vertex penetrates.
+__device__ __forceinline__ uint32_t sensor_hits(f3 x, const SCol *cols, int ncols, uint32_t sensors, const HullRefs &hr) {
+    uint32_t hits = 0;
+    for (int s = 0; s < ncols; ++s) {
+        if (!((sensors >> s) & 1u)) continue;
+        float largest = -FLT_MAX;
+        float4 plane;
+        int shape = -1;
+        if (cols[s].type == 4)
+            collide_hull(x, cols[s], XformR{cols[s]}, hr, s, largest, plane, shape);
+        else
+            collide_shape(x, cols[s], XformR{cols[s]}, s, largest, plane, shape);
+        if (largest > 0.0f) hits |= 1u << s;
+    }
+    return hits;
 }
 
 // ApplyCollisionConstraintsAndUpdateVelocities (:700-825), static-collider branch (:798-816), for one
@@ -741,7 +761,7 @@ __device__ inline int load_shape_table(ShapeTable *tb, SCol *cols, bool &dynamic
         const ShapeEntry &e = tb->e[k];
         SCol &s = cols[k];
         s.type = e.type;
-        s.flags = kColRotated | (e.motion == kMotionDynamic ? kColDynamic : 0);
+        s.flags = kColRotated | (e.motion == kMotionDynamic ? kColDynamic : 0) | (e.motion == kMotionSensor ? kColSensor : 0);
         dynamic = dynamic || e.motion == kMotionDynamic;
         for (int j = 0; j < 9; ++j) s.c[j] = e.xf[j];
         for (int col = 0; col < 3; ++col)

@@ -47,6 +47,8 @@ struct Shared {
     uint32_t ndyn;       // vertices whose shape is dynamic (their list is in StepParams::dyn_list)
     uint32_t dyn_updated;
     float dvel[kMaxCollidingShapes][6];  // the dynamic shapes' velocities during the step
+    uint32_t sensors;     // bit k: host-determined shape k belongs to a sensor
+    uint32_t sensor_hit;  // bit k: a vertex penetrates sensor shape k (DetermineSensorCollisions)
 };
 static_assert(sizeof(Shared) + 256 <= 4096, "static shared memory of the solver kernels (the runtime reserves 4 KB)");
 
@@ -377,6 +379,12 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
         sh.table_slot = slot;
         sh.dynamic = dynamic ? 1 : 0;
         sh.dyn_updated = 0;
+        uint32_t sensors = 0;
+        if (slot >= 0)
+            for (int k = 0; k < n; ++k)
+                if (sh.cols[k].flags & kColSensor) sensors |= 1u << k;
+        sh.sensors = sensors;
+        sh.sensor_hit = 0;
         if (dynamic)
             for (int k = 0; k < n; ++k)
                 for (int j = 0; j < 3; ++j) {
@@ -412,14 +420,17 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     phase ^= 1u;
     if (wake && tid == 0) p.sleep[b] = BodySleep{0.0f, 1u};  // (every thread has read the record)
 
-    // DetermineCollisionPlanes (per vertex, once per step)
+    // DetermineCollisionPlanes (per vertex, once per step), and DetermineSensorCollisions
     const int ncols = sh.ncols;
     const bool has_dynamic = sh.dynamic != 0;
+    const uint32_t sensors = sh.sensors;
+    uint32_t hits = 0;
     for (uint32_t i = tid; i < nv; i += T) {
         float4 pi = sx[i];
         int shape = -1;
         float4 plane = make_float4(0, 0, 0, 0);
         if (pi.w > 0.0f && ncols > 0) shape = collision_plane(xyz(pi), sh.cols, ncols, plane, HullRefs{p.hulls, p.hull_f4, p.hull_u32});
+        if (sensors && pi.w > 0.0f) hits |= sensor_hits(xyz(pi), sh.cols, ncols, sensors, HullRefs{p.hulls, p.hull_f4, p.hull_u32});
         if (kSmemState)
             sv[i].w = __int_as_float(shape);
         if (!kSmemState || p.contact) gshape[i] = shape;
@@ -430,6 +441,7 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
             td.shape[size_t(p.tape_step) * nv + i] = shape;
         }
     }
+    if (hits) atomicOr(&sh.sensor_hit, hits);
 
     if (has_dynamic) {
         // The dynamic-body branch carries the body's velocities from one vertex to the next in index
@@ -695,6 +707,7 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
             }
         if (tid == 0) st3(p.contact_delta + 3 * size_t(b), shift ? delta : mk(0.0f, 0.0f, 0.0f));
     }
+    if (tid == 0 && p.sensor_contact) p.sensor_contact[b] = sh.sensor_hit;  // (barriers since the atomics)
     for (uint32_t i = tid; i < nv; i += T) {
         float4 pi = sx[i];
         gx[i] = shift ? with_w(xyz(pi) - delta, pi.w) : pi;
@@ -913,6 +926,7 @@ __global__ void __launch_bounds__(T) step_kernel_noalloc(const __grid_constant__
     p.contact = nullptr;
     p.contact_point = nullptr;
     p.contact_delta = nullptr;
+    p.sensor_contact = nullptr;
     if (threadIdx.x == 0) {
         stage_bar_init(&sh.stage_bar);
         stage_bar_init(&sh.ring_bar[0]);

@@ -321,6 +321,7 @@ struct Body {
     // the last step's SoftBodyManifold (World::record_manifold): per vertex {has contact, local contact
     // point, contact normal, shape index}
     std::vector<std::array<float, 8>> manifold;
+    uint32_t sensor_hits = 0;  // bit k: table shape k is a sensor shape a vertex penetrated (last step)
 };
 
 template <class R>
@@ -333,6 +334,7 @@ struct CollidingShape {
     R friction, restitution;
     R isc = R(1);  // mSoftBodyInvMassScale
     bool rotated = false, dynamic = false;
+    bool sensor = false;  // a sensor's leaf shape (CollidingSensor): no collision plane, only a contact test
     const HullData *hull = nullptr;  // type 4
     V3<R> c[3], ic[3], it;  // rotation columns; Mat44::InversedRotationTranslation columns and translation
     R inv_mass = R(0);
@@ -511,9 +513,28 @@ public:
             }
         }
 
+        // DetermineSensorCollisions (:267-289): one penetration shared by all vertices of a sensor shape,
+        // a contact when the largest is positive
+        b.sensor_hits = 0;
+        for (size_t si = 0; si < shapes.size(); ++si) {
+            const CollidingShape<R> &cs = shapes[si];
+            if (!cs.sensor) continue;
+            for (const auto &v : b.v) {
+                if (!(v.inv_mass > R(0))) continue;
+                Vertex<R> t = v;
+                t.largest_pen = R(-FLT_MAX);
+                collide_one(t, cs, int(si));
+                if (t.largest_pen > R(0)) {
+                    b.sensor_hits |= 1u << si;
+                    break;
+                }
+            }
+        }
+
         // DetermineCollisionPlanes (:257-265)
         for (size_t si = 0; si < shapes.size() && freeze_mode != 2; ++si) {
             const CollidingShape<R> &cs = shapes[si];
+            if (cs.sensor) continue;
             for (auto &v : b.v) {
                 if (!(v.inv_mass > R(0))) continue;
                 if (cs.type == 4)
@@ -581,6 +602,7 @@ public:
             if (e.type == 4) cs.hull = &(*hulls)[e.hull];
             cs.rotated = true;
             cs.dynamic = e.motion == 2;
+            cs.sensor = e.motion == 3;
             for (int k = 0; k < 3; ++k) cs.c[k] = {R(e.xf[3 * k]), R(e.xf[3 * k + 1]), R(e.xf[3 * k + 2])};
             for (int k = 0; k < 3; ++k) cs.ic[k] = {comp(cs.c[0], k), comp(cs.c[1], k), comp(cs.c[2], k)};
             cs.t = {R(e.xf[9]), R(e.xf[10]), R(e.xf[11])};
@@ -597,6 +619,19 @@ public:
             cs.ang = {R(e.ang[0]), R(e.ang[1]), R(e.ang[2])};
             shapes.push_back(cs);
         }
+    }
+
+    static void collide_one(Vertex<R> &v, const CollidingShape<R> &cs, int idx) {
+        if (cs.type == 4)
+            collide_hull(v, cs, idx);
+        else if (cs.type == 0)
+            collide_box(v, cs, idx);
+        else if (cs.type == 1)
+            collide_sphere(v, cs, idx);
+        else if (cs.type == 2)
+            collide_capsule(v, cs, idx);
+        else
+            collide_cylinder(v, cs, idx);
     }
 
     // The shape's CollideSoftBodyVertices maps the vertex with its InversedRotationTranslation ...
@@ -1211,6 +1246,13 @@ int oracle_get_contacts(void *w, int body, float *out) {
     for (size_t i = 0; i < m.size(); ++i)
         for (int k = 0; k < 8; ++k) out[8 * i + k] = m[i][k];
     return int(m.size());
+}
+
+// After a step with host-determined shapes: bit k = shape k is a sensor shape a vertex penetrated.
+int oracle_get_sensor_contacts(void *w, int body, uint32_t *mask) {
+    Handle *h = static_cast<Handle *>(w);
+    *mask = h->use_double ? h->wd.bodies[body].sensor_hits : h->wf.bodies[body].sensor_hits;
+    return 0;
 }
 
 // Registers a convex hull (points 3 per point, planes 4 per face, face vertex counts and indices);

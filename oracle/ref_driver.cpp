@@ -19,13 +19,15 @@
 // SoftBodyMotionProperties.cpp:120-255), recorded by a SoftBodyContactListener that accepts every contact
 // and recomputes the collector's values with the same calls, then each rigid body's velocities after the
 // step (which hold the soft bodies' velocity deltas, :923-935):
-//   'JSBT' u32 version=3 u32 steps u32 num_rigid
+//   'JSBT' u32 version=4 u32 steps u32 num_rigid
 //   per rigid body: u32 num_points, f32[3] per point, u32 num_faces, per face f32[4] plane, u32 count,
 //                   count x u32 vertex index (convex hulls; 0, 0 for other shapes)
 //   per step: i32 step, u32 num_entries, num_entries x TableEntry, num_rigid x f32[6] (linear, angular
 //             velocity after the step, world space), then per soft body u32 n (0 = no contact callback) and
 //             n x {u32 has contact, f32[3] local contact point, f32[3] contact normal, i32 rigid index}: the
-//             SoftBodyManifold passed to OnSoftBodyContactAdded
+//             SoftBodyManifold passed to OnSoftBodyContactAdded, then u32 m and m x i32: the rigid indices of
+//             its sensor contacts (GetSensorContactBodyID)
+// A table entry of a sensor (SoftBodyContactSettings::mIsSensor) has motion 3.
 //
 // Output file (little endian):
 //   'JSBD' u32 version=2 u32 num_dumps u32 scene_len, scene_len bytes of the serialised scene
@@ -187,7 +189,7 @@ public:
         e.rigid = rigid_index.at(inOtherBody.GetID().GetIndex());
         const jsb::scene::RigidSpec &rs = spec->rigid[e.rigid];
         e.type = int32_t(rs.type);
-        e.motion = int32_t(inOtherBody.GetMotionType());
+        e.motion = ioSettings.mIsSensor ? 3 : int32_t(inOtherBody.GetMotionType());
         RMat44 inverse = inSoftBody.GetCenterOfMassTransform().InversedRotationTranslation();
         Mat44 com = (inverse * inOtherBody.GetCenterOfMassTransform()).ToMat44();
         put_mat(e.com, com);
@@ -222,6 +224,7 @@ public:
         int32_t rigid;
     };
     std::map<uint32_t, std::vector<ManifoldVertex>> manifolds;
+    std::map<uint32_t, std::vector<int32_t>> sensor_contacts;
 
     void OnSoftBodyContactAdded(const Body &inSoftBody, const SoftBodyManifold &inManifold) override {
         std::vector<ManifoldVertex> out;
@@ -240,8 +243,14 @@ public:
             }
             out.push_back(m);
         }
+        std::vector<int32_t> sensors;
+        for (uint i = 0; i < inManifold.GetNumSensorContacts(); ++i) {
+            BodyID id = inManifold.GetSensorContactBodyID(i);
+            sensors.push_back(rigid_index.count(id.GetIndex()) ? int32_t(rigid_index.at(id.GetIndex())) : -2);
+        }
         std::lock_guard<std::mutex> lock(mutex);
         manifolds[soft_index.at(inSoftBody.GetID().GetIndex())] = std::move(out);
+        sensor_contacts[soft_index.at(inSoftBody.GetID().GetIndex())] = std::move(sensors);
     }
 };
 
@@ -322,6 +331,7 @@ int main(int argc, char **argv) {
                                      moving ? Layers::MOVING : Layers::NON_MOVING);
             bcs.mFriction = c.friction;
             bcs.mRestitution = c.restitution;
+            bcs.mIsSensor = c.sensor;
             if (c.motion == 2) {
                 bcs.mOverrideMassProperties = EOverrideMassProperties::CalculateInertia;
                 bcs.mMassPropertiesOverride.mMass = c.mass;
@@ -364,7 +374,7 @@ int main(int argc, char **argv) {
                 return 1;
             }
             fwrite("JSBT", 4, 1, tables);
-            put_u32(tables, 3);
+            put_u32(tables, 4);
             put_u32(tables, uint32_t(steps));
             put_u32(tables, uint32_t(spec.rigid.size()));
             // per rigid body, its convex hull as ConvexHullShape holds it (points relative to the centre of
@@ -495,8 +505,13 @@ int main(int argc, char **argv) {
                     put_u32(tables, it == recorder.manifolds.end() ? 0u : uint32_t(it->second.size()));
                     if (it != recorder.manifolds.end())
                         fwrite(it->second.data(), sizeof(TableRecorder::ManifoldVertex), it->second.size(), tables);
+                    auto sit = recorder.sensor_contacts.find(b);
+                    const uint32_t ns = sit == recorder.sensor_contacts.end() ? 0u : uint32_t(sit->second.size());
+                    put_u32(tables, ns);
+                    if (ns) fwrite(sit->second.data(), 4, ns, tables);
                 }
                 recorder.manifolds.clear();
+                recorder.sensor_contacts.clear();
             }
         }
         if (f) fclose(f);

@@ -70,7 +70,7 @@ def make(name: str, scene: str, params: dict, steps: list[int]):
 
 def make_coupling(name: str = "coupling", steps: int = 90, dump: tuple = (1, 10, 17, 18, 19, 20, 30, 45, 60, 75, 90), **params):
     """Two-way coupling (rigid bodies simulated by the reference's own solver; params: scene parameters,
-    hulls=1 adds convex hulls): per dump step the
+    hulls=1 adds convex hulls, sensors=1 sensors): per dump step the
     deterministic build's soft-body states, and for every step each soft body's colliding shapes as the
     reference determined them (tables_*: jsb_colliding_shape bytes, soft body, rigid body, the rigid body's
     world velocities when collected) and the rigid bodies' velocities after the step."""
@@ -104,6 +104,10 @@ def make_coupling(name: str = "coupling", steps: int = 90, dump: tuple = (1, 10,
         out["manifold_point"] = np.concatenate([t["manifolds"][k]["point"] for k in keys]).astype(np.float32)
         out["manifold_normal"] = np.concatenate([t["manifolds"][k]["normal"] for k in keys]).astype(np.float32)
         out["manifold_rigid"] = np.concatenate([t["manifolds"][k]["rigid"] for k in keys]).astype(np.int32)
+    sens = [(k[0], k[1], r) for k in sorted(t["sensors"]) for r in t["sensors"][k]]  # manifold sensor contacts
+    out["sensor_step"] = np.array([x[0] for x in sens], np.int32)
+    out["sensor_body"] = np.array([x[1] for x in sens], np.int32)
+    out["sensor_rigid"] = np.array([x[2] for x in sens], np.int32)
     for r, (pts, planes, faces) in t["hulls"].items():  # convex hulls as ConvexHullShape holds them
         out[f"hull{r}_points"] = pts
         out[f"hull{r}_planes"] = planes
@@ -167,6 +171,9 @@ if __name__ == "__main__":
     if not which or "coupling_hulls" in which:  # + a static and a dynamic convex hull under a fourth cloth
         make_coupling("coupling_hulls", hulls=1)
         print("wrote coupling_hulls")
+    if not which or "coupling_sensors" in which:  # + a static box sensor and a rising kinematic sphere sensor
+        make_coupling("coupling_sensors", sensors=1)
+        print("wrote coupling_sensors")
     for name, (scene, params, steps) in FULL_CASES.items():
         if not which or f"full_{name}" in which:
             make_full(name, scene, params, steps, threads=os.cpu_count() or 1)

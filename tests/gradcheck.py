@@ -133,11 +133,13 @@ def pick(g, params) -> tuple[np.ndarray, np.ndarray]:
     return e, v
 
 
-def diff_cloth_check(jsb, build_scene, steps=120, every=10, loss_steps=(60, 120), fd_params=32, pinned=True, bends=False) -> dict:
+def diff_cloth_check(jsb, build_scene, steps=120, every=10, loss_steps=(60, 120), fd_params=32, pinned=True, bends=False,
+                     wave_mm=0) -> dict:
     """Relative errors of the GPU gradients: against FP64 autodiff along the GPU trajectory (pinned) and
     against free-running FP64 central differences on `fd_params` random parameters. bends: the same
-    cloth with dihedral bends (then also d loss / d bend compliance against the pinned autodiff)."""
-    scene_bytes = build_scene("diff_cloth", steps=steps, bends=int(bends))
+    cloth with dihedral bends (then also d loss / d bend compliance against the pinned autodiff);
+    wave_mm: the cloth starts as a height field of that amplitude instead of flat."""
+    scene_bytes = build_scene("diff_cloth", steps=steps, bends=int(bends), wave_mm=int(wave_mm))
     scene, _ = parse_scene(scene_bytes)
     targets = cloth_target(jsb, scene_bytes, loss_steps)
     traj = {} if pinned else None

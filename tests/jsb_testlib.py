@@ -170,7 +170,8 @@ def parse_tables(path: str, num_soft: int = 0) -> dict:
     (SHAPE_FMT; a hull's id field holds its rigid index), rigid linear and angular velocity (world) when
     collected)]}, "rigid_after": (steps, num_rigid, 6) velocities after each step, "hulls": {rigid index:
     (points (N, 3), planes (F, 4), [face vertex lists])}, "manifolds": {(step, soft body): per vertex
-    (has, point, normal, rigid)} (version 3; num_soft: the scene's soft bodies)}."""
+    (has, point, normal, rigid)} (version 3; num_soft: the scene's soft bodies), "sensors": {(step, soft
+    body): rigid indices of the manifold's sensor contacts} (version 4)}."""
     buf = open(path, "rb").read()
     assert buf[:4] == b"JSBT"
     version, steps, nr = struct.unpack_from("<III", buf, 4)
@@ -192,7 +193,7 @@ def parse_tables(path: str, num_soft: int = 0) -> dict:
                 off += 20 + 4 * cnt
             if npts:
                 hulls[r] = (pts, np.array(planes, np.float32).reshape(nf, 4), faces)
-    out, after, manifolds = {}, np.zeros((steps, nr, 6), np.float32), {}
+    out, after, manifolds, sensors = {}, np.zeros((steps, nr, 6), np.float32), {}, {}
     for k in range(steps):
         st, n = struct.unpack_from("<iI", buf, off)
         off += 8
@@ -222,7 +223,13 @@ def parse_tables(path: str, num_soft: int = 0) -> dict:
                                         n, off)
                     manifolds[(st, b)] = rec.copy()
                     off += 32 * n
-    return {"steps": out, "rigid_after": after, "hulls": hulls, "manifolds": manifolds}
+                if version >= 4:  # the manifold's sensor contacts (rigid indices)
+                    (ns,) = struct.unpack_from("<I", buf, off)
+                    off += 4
+                    if ns:
+                        sensors[(st, b)] = list(struct.unpack_from(f"<{ns}i", buf, off))
+                        off += 4 * ns
+    return {"steps": out, "rigid_after": after, "hulls": hulls, "manifolds": manifolds, "sensors": sensors}
 
 
 def build_oracle() -> str:
@@ -279,6 +286,7 @@ class Oracle:
                                           ctypes.c_void_p, ctypes.c_void_p]
             L.oracle_set_contact_readback.argtypes = [ctypes.c_void_p, ctypes.c_int]
             L.oracle_get_contacts.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+            L.oracle_get_sensor_contacts.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_uint32)]
             L.oracle_last_error.restype = ctypes.c_char_p
             L.oracle_last_error.argtypes = [ctypes.c_void_p]
             cls._lib = L
@@ -338,6 +346,12 @@ class Oracle:
         out = np.zeros((self.nv[i], 8), np.float32)
         n = self.lib().oracle_get_contacts(self.h, i, out.ctypes.data)
         return out[:n]
+
+    def sensor_contacts(self, i: int) -> int:
+        """After a step with host-determined shapes: bit k = shape k is a sensor shape a vertex penetrated."""
+        m = ctypes.c_uint32()
+        self.lib().oracle_get_sensor_contacts(self.h, i, ctypes.byref(m))
+        return int(m.value)
 
     def shape_velocities(self, i: int) -> np.ndarray:
         """After a step with host-determined shapes: per shape (updated, linear velocity, angular velocity)."""

@@ -96,12 +96,13 @@ inline bool make_named_scene(const std::string &name, const std::string &params,
     else if (name == "large_cloth")
         out = make_large_cloth(uint32_t(geti("n", 256)), int(geti("steps", 600)), geti("bends", 1) != 0);
     else if (name == "diff_cloth")
-        out = make_diff_cloth(uint64_t(geti("seed", 4)), uint32_t(geti("n", 64)), int(geti("steps", 120)), geti("bends", 0) != 0);
+        out = make_diff_cloth(uint64_t(geti("seed", 4)), uint32_t(geti("n", 64)), int(geti("steps", 120)), geti("bends", 0) != 0,
+                              float(geti("wave_mm", 0)) * 1.0e-3f);
     else if (name == "diff_batch")
         out = make_diff_batch(uint64_t(geti("seed", 5)), uint32_t(geti("n_cloth", 192)), uint32_t(geti("n_cube", 64)),
                               int(geti("steps", 90)), float(geti("drop_mm", 1000)) * 0.001f);
     else if (name == "coupling")
-        out = make_coupling(int(geti("steps", 90)), geti("hulls", 0) != 0);
+        out = make_coupling(int(geti("steps", 90)), geti("hulls", 0) != 0, geti("sensors", 0) != 0);
     else if (name == "shapes_drop")
         out = make_shapes_drop(uint64_t(geti("seed", 7)), int(geti("steps", 150)));
     else

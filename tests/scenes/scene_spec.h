@@ -140,6 +140,7 @@ struct RigidSpec {
     float velocity[3] = {0, 0, 0};
     float angular_velocity[3] = {0, 0, 0};
     std::vector<std::array<float, 3>> hull_points;  // ColliderType::Hull: the points the hull is built from
+    bool sensor = false;                   // BodyCreationSettings::mIsSensor
 };
 
 struct SceneSpec {
@@ -430,11 +431,17 @@ inline SceneSpec make_large_cloth(uint32_t n = 256, int steps = 600, bool bends 
 // Differentiable single cloth: n x n (default 64), 0.05 m spacing, top row (z = n-1) pinned, edges
 // only (bends = true adds dihedral bends of compliance 1e-4), per-edge compliance log-U[1e-6, 1e-4] assigned in optimized edge order, initial
 // velocities N(0, 0.1) m/s per component; 120 steps.
-inline SceneSpec make_diff_cloth(uint64_t seed = 4, uint32_t n = 64, int steps = 120, bool bends = false) {
+// wave: amplitude (m) of a height field y = wave sin(2 pi x / 0.8 m) sin(2 pi z / 0.8 m) laid over the
+// grid, so that neighbouring triangles start folded by up to about 0.3 rad instead of flat.
+inline SceneSpec make_diff_cloth(uint64_t seed = 4, uint32_t n = 64, int steps = 120, bool bends = false, float wave = 0.0f) {
     SceneSpec s;
     Rng rng(seed);
     BodySpec b;
     b.mesh = make_cloth(n, n, 0.05f, [n](uint32_t, uint32_t z) { return z == n - 1; });
+    if (wave != 0.0f) {
+        const double k = 2.0 * 3.14159265358979323846 / 0.8;
+        for (auto &p : b.mesh.positions) p[1] = float(double(wave) * std::sin(k * double(p[0])) * std::sin(k * double(p[2])));
+    }
     b.mesh.attributes = VertexAttributes{1.0e-5f, 1.0e-5f, bends ? 1.0e-4f : 3.402823466e+38f};
     b.mesh.bend_type = bends ? BendType::Dihedral : BendType::None;
     for (size_t v = 0; v < b.mesh.velocities.size(); ++v)
@@ -550,7 +557,9 @@ inline SceneSpec make_shapes_drop(uint64_t seed = 7, int steps = 150) {
 // The rigid bodies move under Jolt's own solver in the reference run; the soft bodies see them through
 // each step's colliding shapes. hulls: a fourth cloth falls onto a static irregular convex hull (24
 // points on a jittered ellipsoid), and a small dynamic hull drops onto it. `steps` steps of 1/60 s.
-inline SceneSpec make_coupling(int steps = 90, bool hulls = false) {
+// sensors: adds a static box sensor under the first trampoline (it sags into it) and a kinematic sphere
+// sensor rising through the second cloth.
+inline SceneSpec make_coupling(int steps = 90, bool hulls = false, bool sensors = false) {
     SceneSpec s;
     const float xs[3] = {-1.6f, 0.0f, 1.6f};
     for (int k = 0; k < 3; ++k) {
@@ -648,6 +657,26 @@ inline SceneSpec make_coupling(int steps = 90, bool hulls = false) {
             }
             s.rigid.push_back(h);
         }
+    }
+    if (sensors) {
+        RigidSpec zone;
+        zone.type = ColliderType::Box;
+        zone.motion = 0;
+        zone.sensor = true;
+        zone.half_extent[0] = zone.half_extent[2] = 0.25f;
+        zone.half_extent[1] = 0.2f;
+        zone.position[0] = xs[0];
+        zone.position[1] = 0.75f;
+        s.rigid.push_back(zone);
+        RigidSpec probe;
+        probe.type = ColliderType::Sphere;
+        probe.motion = 1;
+        probe.sensor = true;
+        probe.radius = 0.25f;
+        probe.position[0] = xs[1] + 0.1f;
+        probe.position[1] = 0.2f;
+        probe.velocity[1] = 0.6f;
+        s.rigid.push_back(probe);
     }
     s.num_steps = steps;
     return s;

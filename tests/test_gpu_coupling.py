@@ -7,19 +7,22 @@ cloth), then the batched step runs. Bar: every body's state bitwise equal to the
 (deterministic build) at every dumped step and to the oracle at every step; the dynamic bodies' velocity
 changes read back through jsb_body_shape_velocities give the reference's velocities after each step
 bitwise, and the SoftBodyManifold read back through jsb_body_contacts (contact flags, points, normals,
-contacted body) is the reference's, bitwise (as in tests/test_oracle_coupling.py).
+contacted body) is the reference's, bitwise (as in tests/test_oracle_coupling.py); coupling_sensors adds
+two sensors, whose contacts read back through jsb_body_sensor_contacts are the manifold's sensor contacts.
 """
 import numpy as np
 import pytest
 
 from conftest import golden_path
 from jsb_testlib import parse_scene
-from test_oracle_coupling import check_manifold, check_velocity_changes, manifolds_by_key, register_hulls, tables_by_step
+from test_oracle_coupling import (check_manifold, check_sensors, check_velocity_changes, manifolds_by_key, register_hulls,
+                                  sensors_by_key, tables_by_step)
 
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("name,mode", [("coupling", "batched"), ("coupling", "plain"), ("coupling_hulls", "batched")])
+@pytest.mark.parametrize("name,mode", [("coupling", "batched"), ("coupling", "plain"), ("coupling_hulls", "batched"),
+                                       ("coupling_sensors", "batched")])
 def test_coupling_bitwise_vs_reference_and_oracle(jsb, oracle_lib, name, mode):
     g = np.load(golden_path(name))
     scene_bytes = g["scene"].tobytes()
@@ -32,8 +35,9 @@ def test_coupling_bitwise_vs_reference_and_oracle(jsb, oracle_lib, name, mode):
     assert gpu_hulls == register_hulls(g, o.add_hull)  # (same ids: both count from 0)
     tables = tables_by_step(g, gpu_hulls)
     manifolds = manifolds_by_key(g)
+    sensors = sensors_by_key(g)
     ctx.set_contact_readback(True)
-    contacts = 0
+    contacts = sensor_shapes = 0
     dumps = set(int(s) for s in g["steps"])
     changes = 0
     for step in range(1, int(g["steps"][-1]) + 1):
@@ -56,6 +60,10 @@ def test_coupling_bitwise_vs_reference_and_oracle(jsb, oracle_lib, name, mode):
             for b in range(len(nv)):
                 c = ctx.contacts(b)
                 contacts += check_manifold(manifolds.get((step, b)), b, rows, c["has_contact"], c["points"], c["normals"], c["shape"])
+        for b in range(len(nv)):
+            mask = ctx.sensor_contacts(b)
+            assert mask == o.sensor_contacts(b), (step, b)
+            sensor_shapes += check_sensors(sensors.get((step, b)), b, rows, mask)
         off = 0
         for b in range(len(nv)):
             pos, loc, vel = ctx.read_body(b)
@@ -69,6 +77,7 @@ def test_coupling_bitwise_vs_reference_and_oracle(jsb, oracle_lib, name, mode):
     ctx.close()
     assert changes > 50, changes
     assert mode != "batched" or contacts > 1000, contacts
+    assert name != "coupling_sensors" or (len(sensors) > 100 and sensor_shapes > len(sensors)), (len(sensors), sensor_shapes)
 
 
 def test_coupling_refused_where_unsupported(jsb):

@@ -3,7 +3,8 @@
 
 Three cloths under a static floor: a dynamic sphere and a turned, spinning dynamic box fall onto two
 trampolines, a third cloth onto a static turned box (coupling_hulls adds a fourth cloth falling onto a
-static convex hull, with a small dynamic hull dropped onto it). Jolt's own rigid-body solver moves the rigid bodies;
+static convex hull, with a small dynamic hull dropped onto it; coupling_sensors adds a static box sensor under the
+first trampoline and a kinematic sphere sensor rising through the second cloth). Jolt's own rigid-body solver moves the rigid bodies;
 each step every soft body's colliding shapes are fed to the oracle as the reference determined them
 (transforms, combined friction / restitution, the dynamic bodies' mass, inertia and velocities). Bar:
 - every soft body's state bitwise equal to the reference (deterministic build) at every dumped step;
@@ -11,7 +12,9 @@ each step every soft body's colliding shapes are fed to the oracle as the refere
   the rigid body's velocity when collected plus the oracle's change equals the reference's velocity after
   the step, bitwise;
 - every step's SoftBodyManifold (what OnSoftBodyContactAdded sees): contact flags, local contact points and
-  normals bitwise, and the contacted rigid body.
+  normals bitwise, and the contacted rigid body;
+- its sensor contacts (GetSensorContactBodyID): the sensors a vertex penetrated (DetermineSensorCollisions,
+  SoftBodyMotionProperties.cpp:267-289).
 """
 import struct
 
@@ -95,6 +98,24 @@ def manifolds_by_key(g):
     return out
 
 
+def sensors_by_key(g):
+    """(step, soft body) -> the rigid indices of the reference manifold's sensor contacts."""
+    out = {}
+    if "sensor_step" in g.files:
+        for st, b, r in zip(g["sensor_step"], g["sensor_body"], g["sensor_rigid"]):
+            out.setdefault((int(st), int(b)), set()).add(int(r))
+    return out
+
+
+def check_sensors(ref, body, rows, mask):
+    """A solver's sensor mask of one body and step (bit k: table shape k) against the reference's sensor
+    contacts (a set of rigid indices). Returns the number of sensor shapes of the body in the step."""
+    rigid_of_shape = [r[1] for r in rows if r[0] == body]
+    got = {rigid_of_shape[k] for k in range(len(rigid_of_shape)) if (mask >> k) & 1}
+    assert got == (ref or set()), (body, got, ref)
+    return sum(1 for r in rows if r[0] == body and struct.unpack_from("<i", r[2], 4)[0] == 3)
+
+
 def check_manifold(ref, body, rows, has, points, normals, shapes):
     """A solver's manifold of one body and step (has, points, normals, shape index per vertex) against the
     reference's (None: OnSoftBodyContactAdded was not called, so no vertex may touch)."""
@@ -111,7 +132,7 @@ def check_manifold(ref, body, rows, has, points, normals, shapes):
     return int(has.sum())
 
 
-@pytest.mark.parametrize("name", ["coupling", "coupling_hulls"])
+@pytest.mark.parametrize("name", ["coupling", "coupling_hulls", "coupling_sensors"])
 def test_oracle_coupling_bitwise_vs_reference(oracle_lib, name):
     g = np.load(golden_path(name))
     scene, _ = parse_scene(g["scene"].tobytes())
@@ -120,8 +141,9 @@ def test_oracle_coupling_bitwise_vs_reference(oracle_lib, name):
     o.set_contact_readback(True)
     tables = tables_by_step(g, register_hulls(g, o.add_hull))
     manifolds = manifolds_by_key(g)
+    sensors = sensors_by_key(g)
     dumps = set(int(s) for s in g["steps"])
-    changes = contacts = 0
+    changes = contacts = sensor_shapes = 0
     for step in range(1, int(g["steps"][-1]) + 1):
         rows = tables.get(step, [])
         for b in range(len(nv)):
@@ -131,6 +153,7 @@ def test_oracle_coupling_bitwise_vs_reference(oracle_lib, name):
         for b in range(len(nv)):
             m = o.contacts(b)
             contacts += check_manifold(manifolds.get((step, b)), b, rows, m[:, 0], m[:, 1:4], m[:, 4:7], m[:, 7].astype(np.int64))
+            sensor_shapes += check_sensors(sensors.get((step, b)), b, rows, o.sensor_contacts(b))
         if step in dumps:
             off = 0
             for b in range(len(nv)):
@@ -141,3 +164,5 @@ def test_oracle_coupling_bitwise_vs_reference(oracle_lib, name):
                 off += nv[b]
     assert changes > 50, changes  # the sphere and the box are pushed by their trampolines most of the run
     assert contacts > 1000, contacts
+    if name == "coupling_sensors":
+        assert len(sensors) > 100 and sensor_shapes > len(sensors), (len(sensors), sensor_shapes)
