@@ -249,6 +249,21 @@ jsb_status jsb_body_schedule_info(jsb_context *ctx, uint32_t body_id, uint32_t *
 jsb_status jsb_settings_schedule(const void *blob, size_t len, uint32_t *num_levels, uint32_t *num_records,
                                  uint32_t *levels, uint32_t *records, uint32_t *source);
 
+/* Host only, opt-in and NOT the reference's order: regrouped settings bytes. Each constraint type is
+ * reordered by a greedy colouring in the reference's sequence order (first fit over constraints of the
+ * type sharing a written vertex; tethers also over their anchors) and every constraint goes into one
+ * update group, which SoftBodyMotionProperties processes sequentially (volumes, bends, edges, LRA,
+ * ProcessGroup :1030-1055), each type by colour. The bytes are a valid SaveBinaryState of
+ * SoftBodySharedSettings (Jolt itself runs them the same way); their dependency schedule has about the
+ * colour counts of the types added up as levels per substep (tens for a cloth, instead of the hundreds
+ * to thousands of the reference's order), at the price of a different Gauss-Seidel order: results differ
+ * from the reference's by what reordering the constraint sweep does. This replaces the reference's
+ * SoftBodySharedSettings::Optimize grouping (SoftBodySharedSettings.cpp:613-1182) for callers who accept that.
+ * Pass out = NULL to query *out_len. remap (may be NULL; num_edges + num_bends + num_volumes + num_lra
+ * entries): for the edges, bends, volumes and LRA constraints in their new order, each one's index in the
+ * input. Skinned constraints and rods are refused (JSB_ERR_UNSUPPORTED). */
+jsb_status jsb_settings_regroup(const void *blob, size_t len, void *out, size_t capacity, size_t *out_len, uint32_t *remap);
+
 /* Host only: the whole-step schedule (see jsb_set_step_walk) of these settings for `num_iterations`
  * substeps, in the padded device layout. levels receives 4 x num_levels uint32 {first slot, bend end |
  * volume end << 16, edge end | LRA end << 16, slots of the level} (ends relative to the first slot;

@@ -53,6 +53,7 @@ SIGNATURES = {
     "jsb_body_clear_colliding_shapes": [_P, _c.c_uint32],
     "jsb_body_shape_velocities": [_P, _c.c_uint32, _P, _c.POINTER(_c.c_uint32)],
     "jsb_body_sensor_contacts": [_P, _c.c_uint32, _c.POINTER(_c.c_uint32)],
+    "jsb_settings_regroup": [_c.c_char_p, _c.c_size_t, _P, _c.c_size_t, _c.POINTER(_c.c_size_t), _P],
     "jsb_step": [_P, _c.c_float, _c.c_int, _P],
     "jsb_step_plain": [_P, _c.c_float, _c.c_int, _P],
     "jsb_step_graph": [_P, _c.c_float, _c.c_int, _c.c_int, _c.c_int, _P],
@@ -149,6 +150,31 @@ def settings_schedule(blob: bytes):
     check(lib().jsb_settings_schedule(blob, len(blob), ctypes.byref(nl), ctypes.byref(nr), levels.ctypes.data,
                                       records.ctypes.data, source.ctypes.data))
     return levels, records, source
+
+
+def settings_regroup(blob: bytes):
+    """Opt-in regrouped settings bytes (not the reference's constraint order; jsb_settings_regroup) and
+    the remap: for the edges, bends, volumes and LRA constraints in their new order, the original index."""
+    n = ctypes.c_size_t(0)
+    check(lib().jsb_settings_regroup(blob, len(blob), None, 0, ctypes.byref(n), None))
+    out = ctypes.create_string_buffer(n.value)
+    remap = np.zeros(len(blob) // 12 + 1, np.uint32)  # more than the constraints of any blob of this size
+    check(lib().jsb_settings_regroup(blob, len(blob), out, n.value, ctypes.byref(n), remap.ctypes.data))
+    counts = blob_constraint_counts(out.raw[: n.value])
+    return out.raw[: n.value], remap[:counts]
+
+
+def blob_constraint_counts(blob: bytes) -> int:
+    """Edges + bends + volumes + LRA constraints of settings bytes."""
+    import struct
+
+    off, total = 0, 0
+    for name, size in (("v", 28), ("f", 16), ("e", 16), ("b", 24), ("vol", 24), ("sk", 52), ("skn", 4), ("lra", 12)):
+        (n,) = struct.unpack_from("<I", blob, off)
+        if name in ("e", "b", "vol", "lra"):
+            total += n
+        off += 4 + n * size
+    return total
 
 
 def settings_step_schedule(blob: bytes, num_iterations: int):

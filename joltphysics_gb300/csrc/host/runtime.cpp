@@ -1583,6 +1583,22 @@ jsb_status jsb_settings_schedule(const void *blob, size_t len, uint32_t *num_lev
     return JSB_OK;
 }
 
+jsb_status jsb_settings_regroup(const void *blob, size_t len, void *out, size_t capacity, size_t *out_len, uint32_t *remap) {
+    if (!out_len) return fail(JSB_ERR_INVALID_ARGUMENT, "null argument");
+    ParsedSettings ps;
+    bool unsupported = false;
+    std::string err = parse_settings(blob, len, ps, unsupported);
+    if (!err.empty()) return fail(unsupported ? JSB_ERR_UNSUPPORTED : JSB_ERR_BLOB, err);
+    std::vector<uint32_t> map;
+    const std::vector<uint8_t> bytes = regroup_settings(ps, map);
+    *out_len = bytes.size();
+    if (!out) return JSB_OK;
+    if (capacity < bytes.size()) return fail(JSB_ERR_CAPACITY, "output buffer too small");
+    memcpy(out, bytes.data(), bytes.size());
+    if (remap) memcpy(remap, map.data(), map.size() * sizeof(uint32_t));
+    return JSB_OK;
+}
+
 jsb_status jsb_settings_step_schedule(const void *blob, size_t len, uint32_t num_iterations, uint32_t *num_levels,
                                       uint32_t *num_slots, uint32_t *levels, uint32_t *records, uint32_t *source) {
     if (!num_levels || !num_slots) return fail(JSB_ERR_INVALID_ARGUMENT, "null argument");

@@ -398,6 +398,116 @@ bool build_step_schedule(const ParsedSettings &s, uint32_t num_iterations, StepS
     return true;
 }
 
+namespace {
+
+// First-fit colours of a sequence of constraints over vertex sets: per vertex the colours in which it
+// is written (w) and read (r), as bit masks grown on demand.
+class Colouring {
+public:
+    explicit Colouring(uint32_t nv) : nv_(nv), words_(1), w_(nv, 0), r_(nv, 0) {}
+    // Smallest colour in which none of `writes` is written or read and none of `reads` is written.
+    uint32_t place(const uint32_t *writes, int nw, const uint32_t *reads, int nr) {
+        for (uint32_t word = 0;; ++word) {
+            if (word == words_) grow();
+            uint64_t used = 0;
+            for (int i = 0; i < nw; ++i) used |= w_[size_t(writes[i]) * words_ + word] | r_[size_t(writes[i]) * words_ + word];
+            for (int i = 0; i < nr; ++i) used |= w_[size_t(reads[i]) * words_ + word];
+            if (used != ~uint64_t(0)) {
+                const uint32_t bit = uint32_t(__builtin_ctzll(~used));
+                for (int i = 0; i < nw; ++i) w_[size_t(writes[i]) * words_ + word] |= uint64_t(1) << bit;
+                for (int i = 0; i < nr; ++i) r_[size_t(reads[i]) * words_ + word] |= uint64_t(1) << bit;
+                return word * 64 + bit;
+            }
+        }
+    }
+
+private:
+    void grow() {
+        const uint32_t nw = words_ * 2;
+        std::vector<uint64_t> w(size_t(nv_) * nw, 0), r(size_t(nv_) * nw, 0);
+        for (uint32_t v = 0; v < nv_; ++v)
+            for (uint32_t k = 0; k < words_; ++k) {
+                w[size_t(v) * nw + k] = w_[size_t(v) * words_ + k];
+                r[size_t(v) * nw + k] = r_[size_t(v) * words_ + k];
+            }
+        w_.swap(w);
+        r_.swap(r);
+        words_ = nw;
+    }
+    uint32_t nv_, words_;
+    std::vector<uint64_t> w_, r_;
+};
+
+// Indices 0..n-1 ordered by colour, stably.
+std::vector<uint32_t> by_colour(const std::vector<uint32_t> &colour) {
+    std::vector<uint32_t> order(colour.size());
+    for (uint32_t i = 0; i < order.size(); ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return colour[a] < colour[b]; });
+    return order;
+}
+
+template <class T>
+void put_array(std::vector<uint8_t> &out, const std::vector<T> &items, const std::vector<uint32_t> *order) {
+    const uint32_t n = uint32_t(items.size());
+    const uint8_t *pn = reinterpret_cast<const uint8_t *>(&n);
+    out.insert(out.end(), pn, pn + 4);
+    for (uint32_t k = 0; k < n; ++k) {
+        const uint8_t *p = reinterpret_cast<const uint8_t *>(&items[order ? (*order)[k] : k]);
+        out.insert(out.end(), p, p + sizeof(T));
+    }
+}
+
+}  // namespace
+
+std::vector<uint8_t> regroup_settings(const ParsedSettings &s, std::vector<uint32_t> &remap) {
+    const uint32_t nv = uint32_t(s.vertices.size());
+    std::vector<uint32_t> cv(s.volumes.size()), cb(s.bends.size()), ce(s.edges.size()), cl(s.lras.size());
+    {
+        Colouring c(nv);
+        for (size_t i = 0; i < s.volumes.size(); ++i) cv[i] = c.place(s.volumes[i].v, 4, nullptr, 0);
+    }
+    {
+        Colouring c(nv);
+        for (size_t i = 0; i < s.bends.size(); ++i) cb[i] = c.place(s.bends[i].v, 4, nullptr, 0);
+    }
+    {
+        Colouring c(nv);
+        for (size_t i = 0; i < s.edges.size(); ++i) ce[i] = c.place(s.edges[i].v, 2, nullptr, 0);
+    }
+    {
+        Colouring c(nv);
+        for (size_t i = 0; i < s.lras.size(); ++i) {
+            const uint32_t a = s.lras[i].v[0], b = s.lras[i].v[1];
+            cl[i] = a == b ? c.place(&b, 1, nullptr, 0) : c.place(&b, 1, &a, 1);
+        }
+    }
+    // The reference's sequence of one group is its volumes, bends, edges, LRA; colour the constraints of
+    // each type in the order they came (parallel groups first, the non-parallel group last).
+    const std::vector<uint32_t> ov = by_colour(cv), ob = by_colour(cb), oe = by_colour(ce), ol = by_colour(cl);
+    remap.clear();
+    remap.insert(remap.end(), oe.begin(), oe.end());
+    remap.insert(remap.end(), ob.begin(), ob.end());
+    remap.insert(remap.end(), ov.begin(), ov.end());
+    remap.insert(remap.end(), ol.begin(), ol.end());
+    std::vector<uint8_t> out;
+    put_array(out, s.vertices, nullptr);
+    put_array(out, s.faces, nullptr);
+    put_array(out, s.edges, &oe);
+    put_array(out, s.bends, &ob);
+    put_array(out, s.volumes, &ov);
+    const std::vector<uint32_t> none;
+    put_array(out, none, nullptr);  // skinned constraints
+    put_array(out, none, nullptr);  // skinned constraint normals
+    put_array(out, s.lras, &ol);
+    ParsedSettings::Group g{uint32_t(s.edges.size()), uint32_t(s.lras.size()), 0, 0, uint32_t(s.bends.size()),
+                            uint32_t(s.volumes.size()), 0};
+    put_array(out, std::vector<ParsedSettings::Group>{g}, nullptr);
+    put_array(out, none, nullptr);  // rod stretch-shear
+    put_array(out, none, nullptr);  // rod bend-twist
+    put_array(out, none, nullptr);  // inverse bind matrices
+    return out;
+}
+
 std::vector<uint32_t> build_stage_chunks(const std::vector<uint32_t> &levels4, uint32_t num_levels, bool per_substep,
                                          uint32_t half_slots) {
     std::vector<uint32_t> out;

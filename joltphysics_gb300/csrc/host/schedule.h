@@ -117,6 +117,19 @@ enum : uint32_t { kVertexOp = 4 };
 // `with_source` also fills `source` (for tests of the order).
 bool build_step_schedule(const ParsedSettings &s, uint32_t num_iterations, StepSchedule &out, bool with_source = false);
 
+// Opt-in regrouping (not the reference's constraint order). Reorders each constraint type by a greedy
+// graph colouring in the reference's sequence order (first fit: a constraint takes the smallest colour
+// no constraint of its type sharing a written vertex has; an LRA tether also avoids colours in which its
+// anchor is written or its vertex is read), stably by colour, and puts every constraint into one update
+// group, which the reference processes sequentially: volumes, bends, edges, LRA, each by colour. The
+// bytes are valid SoftBodySharedSettings (SaveBinaryState layout, one group, no skinned constraints or
+// rods), so the reference, the oracle and the GPU all run the new order the same way; the dependency
+// levels of that order are about the colours of each type added up (tens per substep for a cloth, where
+// the reference's order has hundreds or thousands). The result differs from the reference's order the
+// way any other Gauss-Seidel order does. remap (edges, bends, volumes, LRA in their new order): the
+// original index of each constraint within its type.
+std::vector<uint8_t> regroup_settings(const ParsedSettings &s, std::vector<uint32_t> &remap);
+
 // Staging chunks of a level schedule. The walkers stage a schedule's records and level descriptors
 // into shared memory chunk by chunk, with one bulk copy of each per chunk, into the two halves of a
 // ring (chunk c into half c % 2, two chunks in flight). A chunk is a run of consecutive levels whose

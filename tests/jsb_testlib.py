@@ -96,6 +96,20 @@ def parse_scene(buf: bytes, off: int = 0) -> tuple[Scene, int]:
     return sc, off
 
 
+def rewrite_scene_blobs(buf: bytes, rewrite) -> bytes:
+    """The scene bytes with every body's settings blob replaced by rewrite(blob)."""
+    assert buf[:4] == b"JSBS", "not a scene"
+    _, nb, nc = struct.unpack_from("<III", buf, 4)
+    off = 40 + 40 * nc
+    out = bytearray(buf[:off])
+    for _ in range(nb):
+        (bl,) = struct.unpack_from("<I", buf, off + 60)
+        blob = rewrite(bytes(buf[off + 64:off + 64 + bl]))
+        out += buf[off:off + 60] + struct.pack("<I", len(blob)) + blob
+        off += 64 + bl
+    return bytes(out)
+
+
 @dataclass
 class Dump:
     step: int
