@@ -437,9 +437,8 @@ def bench_regrouped(jsb, torch, stream) -> dict:
     """The opt-in regrouped settings (jsb_settings_regroup: each constraint type greedily coloured, one
     update group; NOT the reference's order) on the three workloads: device time per step (CUDA graph of
     one step, L2 flushed before each timed step, steps spread evenly over the run), the levels per step,
-    and the deviation of the regrouped run from the reference's order after the whole run (the
-    reference-order run on the GPU is bitwise the reference's): the largest position difference over
-    the bodies finite in both, against the largest motion of the reference-order run."""
+    and the deviation of the regrouped run from the reference's order (the reference-order run on the GPU
+    is bitwise the reference's) after 1, 10 and 60 steps and the whole run (regroup_deviation)."""
     from jsb_testlib import rewrite_scene_blobs
 
     sptr = stream.cuda_stream
@@ -472,6 +471,8 @@ def bench_regrouped(jsb, torch, stream) -> dict:
         timed = sorted({max(1, round((j + 1) * run_steps / timed_n)) for j in range(timed_n)})
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in timed]
         start = world_states(ref, counts, offsets)
+        probe = sorted({1, 10, 60, run_steps})
+        deviation = {}
         k = 0
         for step in range(1, run_steps + 1):
             with torch.cuda.stream(stream):
@@ -484,28 +485,65 @@ def bench_regrouped(jsb, torch, stream) -> dict:
                     k += 1
                 else:
                     reg.step_graph(1, 1, stream=sptr)
+            if step in probe:  # read back between steps, outside every event pair
+                torch.cuda.synchronize()
+                deviation[str(step)] = regroup_deviation(world_states(ref, counts, offsets), world_states(reg, counts, offsets), start)
         torch.cuda.synchronize()
-        a, b = world_states(ref, counts, offsets), world_states(reg, counts, offsets)
-        dev, moved, nonfinite = 0.0, 0.0, [0, 0]
-        for (pa, la, _), (pb, lb, _), (p0, l0, _) in zip(a, b, start):
-            xa, xb, x0 = pa + la, pb + lb, p0 + l0
-            fa, fb = bool(np.isfinite(xa).all()), bool(np.isfinite(xb).all())
-            nonfinite[0] += not fa
-            nonfinite[1] += not fb
-            if fa and fb:
-                dev = max(dev, float(np.abs(xa - xb).max()))
-                moved = max(moved, float(np.abs(xa - x0).max()))
         step_ms = [e0.elapsed_time(e1) for e0, e1 in ev]
         ms = sum(step_ms) / len(step_ms)
         levels = [ctx_levels(c) for c in ctxs]
         out[name] = {"workload": label, "ms_per_step": ms, "value": vi_step / (ms / 1000.0), "unit": UNIT,
                      "timed_steps": f"{len(timed)} steps spread evenly over the {run_steps}-step run",
                      "levels_per_substep_max": {"reference_order": levels[0], "regrouped": levels[1]},
-                     "deviation_after_run_m": dev, "max_motion_m": moved,
-                     "nonfinite_bodies": {"reference_order": nonfinite[0], "regrouped": nonfinite[1]}}
+                     "deviation": deviation}
         for c in ctxs:
             c.close()
     return out
+
+
+def regroup_deviation(a, b, start) -> dict:
+    """Regrouped run b against the reference-order run a: bodies blown up (non-finite, or beyond 1 km) in
+    each, and over the bodies sane in both the largest position difference and the largest motion of a."""
+    dev, moved, blown = 0.0, 0.0, [0, 0]
+    for (pa, la, _), (pb, lb, _), (p0, l0, _) in zip(a, b, start):
+        xa, xb, x0 = pa + la, pb + lb, p0 + l0
+        sane = [bool(np.isfinite(x).all() and np.abs(x).max() < 1.0e3) for x in (xa, xb)]
+        blown[0] += not sane[0]
+        blown[1] += not sane[1]
+        if all(sane):
+            dev = max(dev, float(np.abs(xa - xb).max()))
+            moved = max(moved, float(np.abs(xa - x0).max()))
+    return {"max_deviation_m": dev, "max_motion_m": moved, "blown_up_bodies": {"reference_order": blown[0], "regrouped": blown[1]}}
+
+
+def set_table(ctx, table):
+    for mv, t, m in table:
+        ctx.set_bucket_config(mv, t, m)
+
+
+def run_sample_ms(ctx, torch, stream, flush, run_steps: int, n: int) -> float:
+    """Mean device time of n steps spread evenly over a run of run_steps from the context's current state
+    (CUDA graph of one step, L2 flushed before each timed step)."""
+    sptr = stream.cuda_stream
+    timed = sorted({max(1, round((j + 1) * run_steps / n)) for j in range(n)})
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in timed]
+    k = 0
+    with torch.cuda.stream(stream):
+        ctx.step_graph(1, 1, stream=sptr)  # capture outside the sample
+    torch.cuda.synchronize()
+    for step in range(2, run_steps + 1):
+        with torch.cuda.stream(stream):
+            if k < len(timed) and step == timed[k]:
+                flush.fill_(step & 0xFF)
+                ev[k][0].record(stream)
+                ctx.step_graph(1, 1, stream=sptr)
+                ev[k][1].record(stream)
+                k += 1
+            else:
+                ctx.step_graph(1, 1, stream=sptr)
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in ev[:k]]
+    return sum(ms) / max(1, len(ms))
 
 
 def ctx_levels(ctx) -> int:
@@ -710,16 +748,35 @@ def main():
     sptr = stream.cuda_stream
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
-    # autotune the launch shape per body-size bucket on the state half way through the run (most of the
-    # run has the bodies on the floor, which the free-falling first steps do not show), then warm up
-    # (graph of one step)
+    # Launch shape per body-size bucket: the autotuner times a few consecutive steps from the state it is
+    # given, and the cost of a step changes along the run (bodies land; nine large stiff cloths blow up),
+    # so its tables from the first state and from the state half way through, the default table and an
+    # alternative one are each timed over the whole run (12 steps spread over it, L2 flushed before each)
+    # and the fastest kept.
     initial = ctx.save_all()
+    table_choice = None
     if not args.no_autotune:
+        candidates = {"default": ctx.bucket_table(),
+                      # a table that measured well on this batch in earlier A/B runs of whole runs
+                      "alternative": [[128, 64, 1], [256, 256, 0], [512, 128, 1], [1024, 128, 1], [1536, 256, 1],
+                                      [2048, 256, 1], [3072, 256, 1], [4096, 256, 1], [8192, 256, 1], [65536, 256, 1]]}
+        ctx.autotune(trials=5)
+        candidates["autotuned_at_start"] = ctx.bucket_table()
+        ctx.restore_all(initial)
         ctx.step_graph(max(1, scene.num_steps // 2), 1, stream=sptr)
         torch.cuda.synchronize()
         ctx.autotune(trials=5)
+        candidates["autotuned_mid_run"] = ctx.bucket_table()
+        table_choice = {}
+        for name, table in candidates.items():
+            set_table(ctx, table)
+            ctx.restore_all(initial)
+            table_choice[name] = run_sample_ms(ctx, torch, stream, flush, scene.num_steps, 12)
+        best = min(table_choice, key=table_choice.get)
+        set_table(ctx, candidates[best])
+        table_choice = {"chosen": best, "sample_ms": table_choice}
         ctx.restore_all(initial)
-        try:  # clears the device error word: by then nine bodies have gone non-finite, as in the reference
+        try:  # clears the device error word: nine bodies have gone non-finite, as in the reference
             ctx.synchronize()
         except jsb.JsbError as e:
             if e.status != jsb.JSB_ERR_NONFINITE:
@@ -874,7 +931,7 @@ def main():
                    "step_ms_min_max": [min(step_ms), max(step_ms)],
                    "step_ms": {str(st): round(ms, 3) for st, ms in zip(timed, step_ms)},
                    "reference_non_finite_bodies_in_run": non_finite,
-                   "buckets_max_vertices_threads_state": buckets},
+                   "buckets_max_vertices_threads_state": buckets, "launch_table_choice": table_choice},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
                 "steps": e2e_steps, "note": "the whole run through the C ABI, host copies every step"},
         "gpu_launches": launches,
