@@ -503,17 +503,22 @@ def bench_regrouped(jsb, torch, stream) -> dict:
 
 def regroup_deviation(a, b, start) -> dict:
     """Regrouped run b against the reference-order run a: bodies blown up (non-finite, or beyond 1 km) in
-    each, and over the bodies sane in both the largest position difference and the largest motion of a."""
-    dev, moved, blown = 0.0, 0.0, [0, 0]
+    each, and over the bodies sane in both the largest position difference, the largest motion of a, and
+    the median and 90th percentile over bodies of (largest difference / largest motion) per body."""
+    dev, moved, blown, ratios = 0.0, 0.0, [0, 0], []
     for (pa, la, _), (pb, lb, _), (p0, l0, _) in zip(a, b, start):
         xa, xb, x0 = pa + la, pb + lb, p0 + l0
         sane = [bool(np.isfinite(x).all() and np.abs(x).max() < 1.0e3) for x in (xa, xb)]
         blown[0] += not sane[0]
         blown[1] += not sane[1]
         if all(sane):
-            dev = max(dev, float(np.abs(xa - xb).max()))
-            moved = max(moved, float(np.abs(xa - x0).max()))
-    return {"max_deviation_m": dev, "max_motion_m": moved, "blown_up_bodies": {"reference_order": blown[0], "regrouped": blown[1]}}
+            d, m = float(np.abs(xa - xb).max()), float(np.abs(xa - x0).max())
+            dev, moved = max(dev, d), max(moved, m)
+            if m > 0.0:
+                ratios.append(d / m)
+    q = (lambda f: float(np.quantile(ratios, f))) if ratios else (lambda f: None)
+    return {"max_deviation_m": dev, "max_motion_m": moved, "per_body_deviation_over_motion": {"median": q(0.5), "p90": q(0.9)},
+            "blown_up_bodies": {"reference_order": blown[0], "regrouped": blown[1]}}
 
 
 def set_table(ctx, table):
