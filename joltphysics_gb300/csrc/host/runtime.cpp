@@ -656,19 +656,19 @@ jsb_status rebuild_groups(jsb_context *ctx) {
             return fail(JSB_ERR_UNSUPPORTED, "a body with " + std::to_string(g.smem_vertices) +
                                                  " vertices does not fit the shared-memory solver path");
         // Every chunk costs a wait and two bulk copies: when every body can have an SM to itself, grow
-        // the halves towards chunks of kStageLevels levels while neither the CTAs per SM nor the
+        // the halves towards chunks of kStageLevels levels while the CTA still fits an SM and the
         // placement of the state (in shared memory or not; also for the taped forward step, which
-        // stages with the same ring) change. (In a batch of more bodies than SMs, larger rings cost
-        // co-resident CTAs of the other buckets more than the fewer chunk turns save.)
+        // stages with the same ring) does not change; with at most one CTA per SM needed, CTAs per SM
+        // do not matter. (In a batch of more bodies than SMs, larger rings cost co-resident CTAs of the
+        // other buckets more than the fewer chunk turns save.)
         if (one_cta_bodies <= size_t(ctx->num_sms)) {
             uint32_t want = 0;
             for (auto &m : members[k]) want = std::max(want, ring_half_full(ctx, ctx->bodies[m.second]));
-            const int occ0 = step_occupancy(g.threads, g.smem_state, step_smem_bytes(g.smem_state, g.smem_vertices, g.smem_faces, g.ring_slots));
             const bool state_fits = step_smem_bytes(true, g.smem_vertices, g.smem_faces, g.ring_slots) <= cap;
             while (g.ring_slots < want) {
                 const uint32_t r = std::min(want, g.ring_slots + std::max<uint32_t>(32, g.ring_slots / 2)) & ~31u;
                 const size_t bytes = step_smem_bytes(g.smem_state, g.smem_vertices, g.smem_faces, r);
-                if (r <= g.ring_slots || bytes > cap || step_occupancy(g.threads, g.smem_state, bytes) < occ0 ||
+                if (r <= g.ring_slots || bytes > cap || step_occupancy(g.threads, g.smem_state, bytes) < 1 ||
                     (state_fits && step_smem_bytes(true, g.smem_vertices, g.smem_faces, r) > cap))
                     break;
                 g.ring_slots = r;
