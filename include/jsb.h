@@ -190,6 +190,21 @@ jsb_status jsb_set_contact_readback(jsb_context *ctx, int enable);
  * NULL. Not recorded on the thread-block-cluster path (JSB_ERR_UNSUPPORTED). */
 jsb_status jsb_body_contacts(jsb_context *ctx, uint32_t body_id, uint8_t *has_contact, float *contact_points, float *normals,
                              int32_t *shape_index, float delta[3]);
+/* ---- skinning (skinned constraints) --------------------------------------------------------- */
+/* SoftBodyMotionProperties::SkinVertices (SoftBodyMotionProperties.cpp:1139-1230) for a body whose settings
+ * have skinned constraints: the skinned positions from `num_joints` joint matrices (16 floats each, Mat44
+ * columns, in the soft body's space) times the settings' inverse bind matrices and skin weights, their
+ * normals from the skinned faces, the previous skinned positions kept for the interpolation over the next
+ * step's iterations; hard_skin_all moves every skinned vertex to its skinned position and zeroes its
+ * velocity. Call it between steps; the next step's ApplySkinConstraints (:509-571: back stop sphere and
+ * maximum distance) use it. Synchronous (host arithmetic in the reference's operation order). Skinned bodies
+ * run on the one-CTA path only (not the cluster path, not differentiable runs, not jsb_step_body_noalloc). */
+jsb_status jsb_body_skin_vertices(jsb_context *ctx, uint32_t body_id, const float *joint_matrices, uint32_t num_joints,
+                                  int hard_skin_all);
+/* SetEnableSkinConstraints / SetSkinnedMaxDistanceMultiplier (SoftBodyMotionProperties.h:93-98). */
+jsb_status jsb_body_set_skin_settings(jsb_context *ctx, uint32_t body_id, int enable_skin_constraints,
+                                      float max_distance_multiplier);
+
 /* After a step (synchronises the device): bit k of *mask is set when shape k of the body's host-determined
  * shapes is a sensor shape (JSB_MOTION_SENSOR) that a vertex with inverse mass > 0 penetrated at the start
  * of the step (DetermineSensorCollisions, SoftBodyMotionProperties.cpp:267-289: CollidingSensor::mHasContact;

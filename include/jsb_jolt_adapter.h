@@ -13,8 +13,9 @@
 //   3. steps every GPU soft body in one call,
 //   4. writes the rigid bodies' velocity changes back (UpdateRigidBodyVelocities, :923-935) and each soft
 //      body's state back (SoftBodyMotionProperties::RestoreState, body position).
-// Bodies the GPU path does not run (skinned constraints, rods, more than 65,536 vertices, a non-identity
-// rotation) are refused at AddBody. With a SoftBodyContactListener set (SetContactListener), every
+// Bodies the GPU path does not run (rods, more than 65,536 vertices, a non-identity rotation) are refused
+// at AddBody; skinned bodies take their joint matrices through SkinVertices (instead of
+// SoftBodyMotionProperties::SkinVertices) and must fit one CTA. With a SoftBodyContactListener set (SetContactListener), every
 // candidate body goes through its OnSoftBodyContactValidate like in the reference (rejections, inverse
 // mass scales, sensors); without one, sensors are ignored and the default contact settings apply, as in
 // the reference. SoftBodyManifold cannot be built outside Jolt (its constructor is private), so the
@@ -94,6 +95,27 @@ public:
         return true;
     }
 
+    // SoftBodyMotionProperties::SkinVertices for a registered body (joint matrices relative to its centre of
+    // mass), and its SetEnableSkinConstraints / SetSkinnedMaxDistanceMultiplier; call between steps.
+    bool SkinVertices(const JPH::BodyID &inID, const JPH::Mat44 *inJointMatrices, uint32_t inNumJoints, bool inHardSkinAll) {
+        const Entry *e = Find(inID);
+        if (e == nullptr) return false;
+        std::vector<float> m(16 * size_t(inNumJoints));
+        for (uint32_t j = 0; j < inNumJoints; ++j)
+            for (int c = 0; c < 4; ++c) {
+                const JPH::Vec4 col = inJointMatrices[j].GetColumn4(c);
+                m[16 * j + 4 * c + 0] = col.GetX();
+                m[16 * j + 4 * c + 1] = col.GetY();
+                m[16 * j + 4 * c + 2] = col.GetZ();
+                m[16 * j + 4 * c + 3] = col.GetW();
+            }
+        return jsb_body_skin_vertices(mCtx, e->mGpu, m.data(), inNumJoints, inHardSkinAll ? 1 : 0) == JSB_OK;
+    }
+    bool SetSkinSettings(const JPH::BodyID &inID, bool inEnableSkinConstraints, float inMaxDistanceMultiplier) {
+        const Entry *e = Find(inID);
+        return e != nullptr && jsb_body_set_skin_settings(mCtx, e->mGpu, inEnableSkinConstraints ? 1 : 0, inMaxDistanceMultiplier) == JSB_OK;
+    }
+
     // The reference's SoftBodyContactListener, consulted for every candidate rigid body (null: none).
     void SetContactListener(JPH::SoftBodyContactListener *inListener) { mListener = inListener; }
 
@@ -160,6 +182,12 @@ private:
         std::vector<jsb_colliding_shape> shapes;
         std::vector<JPH::BodyID> bodies;  // the rigid body of each shape
     };
+
+    const Entry *Find(const JPH::BodyID &inID) const {
+        for (const Entry &e : mBodies)
+            if (e.mJolt == inID) return &e;
+        return nullptr;
+    }
 
     static void PutMatrix(JPH::Mat44Arg inM, float *outColumns, int inColumns) {
         for (int c = 0; c < inColumns; ++c)

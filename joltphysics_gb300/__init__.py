@@ -54,6 +54,8 @@ SIGNATURES = {
     "jsb_body_shape_velocities": [_P, _c.c_uint32, _P, _c.POINTER(_c.c_uint32)],
     "jsb_body_sensor_contacts": [_P, _c.c_uint32, _c.POINTER(_c.c_uint32)],
     "jsb_settings_regroup": [_c.c_char_p, _c.c_size_t, _P, _c.c_size_t, _c.POINTER(_c.c_size_t), _P],
+    "jsb_body_skin_vertices": [_P, _c.c_uint32, _P, _c.c_uint32, _c.c_int],
+    "jsb_body_set_skin_settings": [_P, _c.c_uint32, _c.c_int, _c.c_float],
     "jsb_step": [_P, _c.c_float, _c.c_int, _P],
     "jsb_step_plain": [_P, _c.c_float, _c.c_int, _P],
     "jsb_step_graph": [_P, _c.c_float, _c.c_int, _c.c_int, _c.c_int, _P],
@@ -319,6 +321,14 @@ class Context:
         check(lib().jsb_body_contacts(self.h, body, has.ctypes.data, cp.ctypes.data, nrm.ctypes.data, shape.ctypes.data,
                                       delta.ctypes.data))
         return {"has_contact": has, "points": cp, "normals": nrm, "shape": shape, "delta": delta}
+
+    def skin_vertices(self, body: int, joint_matrices, hard_skin_all: bool = False):
+        """SkinVertices: joint_matrices (J, 4, 4) column-major (Mat44 columns) as float32."""
+        m = np.ascontiguousarray(joint_matrices, np.float32)
+        check(lib().jsb_body_skin_vertices(self.h, body, m.ctypes.data, m.shape[0], 1 if hard_skin_all else 0))
+
+    def set_skin_settings(self, body: int, enable: bool = True, max_distance_multiplier: float = 1.0):
+        check(lib().jsb_body_set_skin_settings(self.h, body, 1 if enable else 0, max_distance_multiplier))
 
     def sensor_contacts(self, body: int) -> int:
         """Bit k: host-determined shape k is a sensor shape a vertex penetrated in the last step."""

@@ -132,6 +132,7 @@ struct SettingsRec {
     std::vector<uint32_t> vf_off, vf;
     DevBuf<uint4> levels, records, faces;
     DevBuf<uint32_t> vf_off_dev, vf_dev;
+    DevBuf<float4> skin_params;  // per skinned constraint {max distance, back stop distance, back stop radius, vertex}
     std::map<uint32_t, std::unique_ptr<StepSchedRec>> steps;  // by iteration count; null: none (a level too wide)
     std::map<uint32_t, std::pair<DevBuf<uint4>, uint32_t>> chunks;  // staging chunks of `schedule` by ring half
 };
@@ -279,6 +280,8 @@ struct jsb_context {
     jsb::DevBuf<float4> contact_point;
     jsb::DevBuf<float> contact_delta;
     jsb::DevBuf<uint32_t> sensor_contact;  // per body: sensor shapes of its table with a vertex inside
+    jsb::DevBuf<float4> skin_state;        // 3 per vertex (SkinState) when any body has skinned constraints
+    jsb::DevBuf<jsb::SkinCtl> skin_ctl;    // per body
     jsb::DevBuf<jsb::HullDev> hulls_dev;
     jsb::DevBuf<float4> hull_f4_dev;
     jsb::DevBuf<uint32_t> hull_u32_dev;
@@ -363,6 +366,12 @@ jsb_status ensure_step_schedules(jsb_context *ctx) {
     return JSB_OK;
 }
 
+inline float __uint_as_float_host(uint32_t u) {
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
 BodyDesc make_desc(const jsb_context *ctx, const BodyRec &b) {
     const SettingsRec &s = *ctx->settings[b.settings_id];
     BodyDesc d;
@@ -392,6 +401,9 @@ BodyDesc make_desc(const jsb_context *ctx, const BodyRec &b) {
     d.gravity_factor = b.creation.gravity_factor;
     d.vertex_radius = b.creation.vertex_radius;
     d.flags = (b.creation.update_position ? kFlagUpdatePosition : 0u) | (b.creation.allow_sleeping ? kFlagAllowSleeping : 0u);
+    const bool skinned = !s.parsed.skinned.empty() && ctx->skin_state.ptr;
+    d.skin_params = skinned ? s.skin_params.ptr : nullptr;
+    d.skin_state = skinned ? ctx->skin_state.ptr + size_t(b.vtx_offset) * 3 : nullptr;
     return d;
 }
 
@@ -530,6 +542,20 @@ jsb_status rebuild(jsb_context *ctx) {
     JSB_CUDA(ctx->plane.alloc(total));
     JSB_CUDA(ctx->shape.alloc(total));
     ctx->total_vertices = total;
+    {  // skin states (SoftBodyMotionProperties::mSkinState, zero at creation) and switches; existing bodies keep theirs
+        bool any = false;
+        for (const BodyRec &b : ctx->bodies) any = any || !ctx->settings[b.settings_id]->parsed.skinned.empty();
+        if (any) {
+            std::vector<float4> hs(size_t(total) * 3, make_float4(0, 0, 0, 0));
+            const size_t old = std::min(ctx->skin_state.count, hs.size());
+            if (old) JSB_CUDA(cudaMemcpy(hs.data(), ctx->skin_state.ptr, old * sizeof(float4), cudaMemcpyDeviceToHost));
+            JSB_CUDA(ctx->skin_state.upload(hs.data(), hs.size()));
+        }
+        std::vector<SkinCtl> hc(std::max<size_t>(ctx->bodies.size(), 1), SkinCtl{1.0f, kSkinEnabled});
+        const size_t oldc = std::min(ctx->skin_ctl.count, hc.size());
+        if (oldc) JSB_CUDA(cudaMemcpy(hc.data(), ctx->skin_ctl.ptr, oldc * sizeof(SkinCtl), cudaMemcpyDeviceToHost));
+        JSB_CUDA(ctx->skin_ctl.upload(hc.data(), hc.size()));
+    }
     jsb_status sst = ensure_step_schedules(ctx);
     if (sst != JSB_OK) return sst;
     ctx->descs_host.clear();
@@ -623,6 +649,9 @@ jsb_status rebuild_groups(jsb_context *ctx) {
             if (pressure_faces(s, b) > 0)
                 return fail(JSB_ERR_UNSUPPORTED, "a pressurised body with " + std::to_string(nv) +
                                                      " vertices is too large for one CTA, and the cluster path has no pressure");
+            if (!s.parsed.skinned.empty())
+                return fail(JSB_ERR_UNSUPPORTED, "a body with skinned constraints and " + std::to_string(nv) +
+                                                     " vertices is too large for one CTA, and the cluster path has no skinning");
             cluster_bodies.push_back(uint32_t(bi));
             continue;
         }
@@ -744,6 +773,7 @@ StepParams base_params(jsb_context *ctx, float dt) {
     p.contact_point = contacts ? ctx->contact_point.ptr : nullptr;
     p.contact_delta = contacts ? ctx->contact_delta.ptr : nullptr;
     p.sensor_contact = tables ? ctx->sensor_contact.ptr : nullptr;
+    p.skin_ctl = ctx->skin_ctl.ptr;
     return p;
 }
 
@@ -1026,6 +1056,14 @@ jsb_status jsb_settings_upload(jsb_context *ctx, const void *blob, size_t len, u
     JSB_CUDA(rec->faces.upload(faces.data(), faces.size()));
     JSB_CUDA(rec->vf_off_dev.upload(rec->vf_off.data(), rec->vf_off.size()));
     JSB_CUDA(rec->vf_dev.upload(rec->vf.data(), rec->vf.size()));
+    if (!ps.skinned.empty()) {
+        std::vector<float4> sp(ps.skinned.size());
+        for (size_t k = 0; k < sp.size(); ++k) {
+            const auto &sk = ps.skinned[k];
+            sp[k] = make_float4(sk.max_distance, sk.backstop_distance, sk.backstop_radius, __uint_as_float_host(sk.vertex));
+        }
+        JSB_CUDA(rec->skin_params.upload(sp.data(), sp.size()));
+    }
     ctx->settings.push_back(std::move(rec));
     *settings_id = uint32_t(ctx->settings.size() - 1);
     return JSB_OK;
@@ -1168,6 +1206,132 @@ jsb_status jsb_hull_add(jsb_context *ctx, const jsb_convex_hull *h, uint32_t *hu
     ctx->hulls_host.push_back(d);
     ctx->hulls_dirty = true;
     *hull_id = uint32_t(ctx->hulls_host.size() - 1);
+    return JSB_OK;
+}
+
+// ---- skinning (SoftBodyMotionProperties::SkinVertices, :1139-1230) -------------------------------------
+// Host arithmetic in the operation order of the reference's deterministic SSE build: Mat44 * Mat44 and
+// Mat44 * Vec3 as ((c0 x + c1 y) + c2 z) + c3 (Mat44.inl:241-302), Vec3::Cross with separately rounded
+// products, NormalizedOr with the length (x x + y y) + z z, a zero vector at or below FLT_MIN.
+namespace {
+struct V3h {
+    float x, y, z;
+};
+inline V3h operator+(V3h a, V3h b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3h operator-(V3h a, V3h b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3h operator*(float s, V3h a) { return {s * a.x, s * a.y, s * a.z}; }
+inline V3h cross_h(V3h a, V3h b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline V3h normalized_or_zero(V3h v) {
+    const float xx = v.x * v.x, yy = v.y * v.y, zz = v.z * v.z;
+    const float len_sq = (xx + yy) + zz;
+    if (len_sq <= FLT_MIN) return {0.0f, 0.0f, 0.0f};
+    const float len = std::sqrt(len_sq);
+    return {v.x / len, v.y / len, v.z / len};
+}
+struct M44h {
+    float c[4][4];  // columns
+};
+inline M44h mat_mul_h(const M44h &a, const M44h &b) {
+    M44h r;
+    for (int i = 0; i < 4; ++i)
+        for (int k = 0; k < 4; ++k)
+            r.c[i][k] = ((a.c[0][k] * b.c[i][0] + a.c[1][k] * b.c[i][1]) + a.c[2][k] * b.c[i][2]) + a.c[3][k] * b.c[i][3];
+    return r;
+}
+inline V3h mat_vec_h(const M44h &a, V3h v) {
+    float o[3];
+    for (int k = 0; k < 3; ++k) o[k] = ((a.c[0][k] * v.x + a.c[1][k] * v.y) + a.c[2][k] * v.z) + a.c[3][k];
+    return {o[0], o[1], o[2]};
+}
+}  // namespace
+
+jsb_status jsb_body_skin_vertices(jsb_context *ctx, uint32_t body_id, const float *joint_matrices, uint32_t num_joints, int hard_skin_all) {
+    if (!check_ctx(ctx) || body_id >= ctx->bodies.size() || (num_joints && !joint_matrices))
+        return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    const BodyRec &b = ctx->bodies[body_id];
+    const ParsedSettings &ps = ctx->settings[b.settings_id]->parsed;
+    if (ps.skinned.empty()) return fail(JSB_ERR_INVALID_ARGUMENT, "the body has no skinned constraints");
+    std::vector<M44h> skin(ps.inv_binds.size());
+    for (size_t k = 0; k < skin.size(); ++k) {
+        const auto &ib = ps.inv_binds[k];
+        if (ib.joint >= num_joints) return fail(JSB_ERR_INVALID_ARGUMENT, "inverse bind matrix refers to a joint out of range");
+        M44h j, m;
+        memcpy(j.c, joint_matrices + 16 * size_t(ib.joint), 64);
+        memcpy(m.c, ib.m, 64);
+        skin[k] = mat_mul_h(j, m);
+    }
+    const size_t nv = ps.vertices.size();
+    JSB_CUDA(cudaDeviceSynchronize());
+    std::vector<float4> hs(nv * 3);
+    float4 *dev = ctx->skin_state.ptr + size_t(b.vtx_offset) * 3;
+    JSB_CUDA(cudaMemcpy(hs.data(), dev, hs.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+    auto get = [&](size_t i, int k) { return V3h{hs[i * 3 + k].x, hs[i * 3 + k].y, hs[i * 3 + k].z}; };
+    auto put = [&](size_t i, int k, V3h v) { hs[i * 3 + k] = make_float4(v.x, v.y, v.z, 0.0f); };
+    for (const auto &sk : ps.skinned) {
+        const auto &bv = ps.vertices[sk.vertex];
+        const V3h bind{bv.pos[0], bv.pos[1], bv.pos[2]};
+        V3h pos{0.0f, 0.0f, 0.0f};
+        for (const auto &w : sk.w) {
+            if (w.weight == 0.0f) break;  // the first zero weight ends the list
+            pos = pos + w.weight * mat_vec_h(skin[w.inv_bind], bind);
+        }
+        put(sk.vertex, 0, get(sk.vertex, 1));
+        put(sk.vertex, 1, pos);
+    }
+    for (const auto &sk : ps.skinned) {
+        V3h n{0.0f, 0.0f, 0.0f};
+        const uint32_t nf = sk.normal_info >> 24;
+        if (nf > 0) {
+            for (uint32_t k = 0; k < nf; ++k) {
+                const auto &f = ps.faces[ps.skinned_normals[(sk.normal_info & 0xffffffu) + k]];
+                const V3h v0 = get(f.v[0], 1), v1 = get(f.v[1], 1), v2 = get(f.v[2], 1);
+                n = n + normalized_or_zero(cross_h(v1 - v0, v2 - v0));
+            }
+            n = normalized_or_zero(n);
+        }
+        put(sk.vertex, 2, n);
+    }
+    SkinCtl ctl;
+    JSB_CUDA(cudaMemcpy(&ctl, ctx->skin_ctl.ptr + body_id, sizeof(SkinCtl), cudaMemcpyDeviceToHost));
+    const bool enabled = (ctl.flags & kSkinEnabled) != 0;
+    if (hard_skin_all || !enabled) {  // hard skin every vertex (velocities reset), or only the kinematic ones
+        std::vector<float4> hx(nv), hv(nv);
+        JSB_CUDA(cudaMemcpy(hx.data(), ctx->x.ptr + b.vtx_offset, nv * sizeof(float4), cudaMemcpyDeviceToHost));
+        JSB_CUDA(cudaMemcpy(hv.data(), ctx->v.ptr + b.vtx_offset, nv * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (const auto &sk : ps.skinned) {
+            if (!hard_skin_all && sk.max_distance != 0.0f) continue;
+            const V3h p = get(sk.vertex, 1);
+            if (hard_skin_all) {
+                put(sk.vertex, 0, p);
+                hv[sk.vertex] = make_float4(0.0f, 0.0f, 0.0f, hv[sk.vertex].w);
+            }
+            hx[sk.vertex] = make_float4(p.x, p.y, p.z, hx[sk.vertex].w);
+        }
+        JSB_CUDA(cudaMemcpy(ctx->x.ptr + b.vtx_offset, hx.data(), nv * sizeof(float4), cudaMemcpyHostToDevice));
+        JSB_CUDA(cudaMemcpy(ctx->v.ptr + b.vtx_offset, hv.data(), nv * sizeof(float4), cudaMemcpyHostToDevice));
+    }
+    JSB_CUDA(cudaMemcpy(dev, hs.data(), hs.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    ctl.flags |= kSkinPreviousValid;
+    JSB_CUDA(cudaMemcpy(ctx->skin_ctl.ptr + body_id, &ctl, sizeof(SkinCtl), cudaMemcpyHostToDevice));
+    drop_graph(ctx);
+    return JSB_OK;
+}
+
+jsb_status jsb_body_set_skin_settings(jsb_context *ctx, uint32_t body_id, int enable_skin_constraints, float max_distance_multiplier) {
+    if (!check_ctx(ctx) || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
+    JSB_CUDA(cudaSetDevice(ctx->device));
+    jsb_status st = rebuild(ctx);
+    if (st != JSB_OK) return st;
+    JSB_CUDA(cudaDeviceSynchronize());
+    SkinCtl ctl;
+    JSB_CUDA(cudaMemcpy(&ctl, ctx->skin_ctl.ptr + body_id, sizeof(SkinCtl), cudaMemcpyDeviceToHost));
+    ctl.flags = (ctl.flags & ~kSkinEnabled) | (enable_skin_constraints ? kSkinEnabled : 0u);
+    ctl.max_distance_multiplier = max_distance_multiplier;
+    JSB_CUDA(cudaMemcpy(ctx->skin_ctl.ptr + body_id, &ctl, sizeof(SkinCtl), cudaMemcpyHostToDevice));
+    drop_graph(ctx);
     return JSB_OK;
 }
 
@@ -1438,7 +1602,8 @@ jsb_status jsb_body_save_state(jsb_context *ctx, uint32_t body_id, void *state, 
     if (!check_ctx(ctx) || !len || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
     const BodyRec &b = ctx->bodies[body_id];
     const size_t nv = ctx->settings[b.settings_id]->parsed.vertices.size();
-    const size_t need = kMotionHeader + nv * 24 + 48;
+    const bool skinned = !ctx->settings[b.settings_id]->parsed.skinned.empty();
+    const size_t need = kMotionHeader + nv * 24 + (skinned ? nv * 36 : 0) + 48;
     *len = need;
     if (!state) return JSB_OK;
     if (capacity < need) return fail(JSB_ERR_INVALID_ARGUMENT, "state buffer too small");
@@ -1465,6 +1630,14 @@ jsb_status jsb_body_save_state(jsb_context *ctx, uint32_t body_id, void *state, 
         memcpy(p, pv, 24);
         p += 24;
     }
+    if (skinned) {  // SkinState: previous position, position, normal (SoftBodyMotionProperties.cpp:1462-1467)
+        std::vector<float4> hs(nv * 3);
+        JSB_CUDA(cudaMemcpy(hs.data(), ctx->skin_state.ptr + size_t(b.vtx_offset) * 3, nv * 3 * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < nv * 3; ++i) {
+            memcpy(p, &hs[i], 12);
+            p += 12;
+        }
+    }
     memcpy(p, s.bmin, 12);
     memcpy(p + 12, s.bmax, 12);
     memcpy(p + 24, s.pmin, 12);
@@ -1477,7 +1650,9 @@ jsb_status jsb_body_restore_state(jsb_context *ctx, uint32_t body_id, const void
     const BodyRec &b = ctx->bodies[body_id];
     const ParsedSettings &ps = ctx->settings[b.settings_id]->parsed;
     const size_t nv = ps.vertices.size();
-    if (len != kMotionHeader + nv * 24 + 48) return fail(JSB_ERR_BLOB, "state size does not match the body's vertex count");
+    const bool skinned = !ps.skinned.empty();
+    if (len != kMotionHeader + nv * 24 + (skinned ? nv * 36 : 0) + 48)
+        return fail(JSB_ERR_BLOB, "state size does not match the body's vertex count");
     JSB_CUDA(cudaSetDevice(ctx->device));
     jsb_status st = rebuild(ctx);
     if (st != JSB_OK) return st;
@@ -1500,6 +1675,14 @@ jsb_status jsb_body_restore_state(jsb_context *ctx, uint32_t body_id, const void
         p += 24;
         hx[i] = make_float4(pv[0], pv[1], pv[2], ps.vertices[i].inv_mass);
         hv[i] = make_float4(pv[3], pv[4], pv[5], 0.0f);
+    }
+    if (skinned) {
+        std::vector<float4> hs(nv * 3, make_float4(0, 0, 0, 0));
+        for (size_t i = 0; i < nv * 3; ++i) {
+            memcpy(&hs[i], p, 12);
+            p += 12;
+        }
+        JSB_CUDA(cudaMemcpy(ctx->skin_state.ptr + size_t(b.vtx_offset) * 3, hs.data(), nv * 3 * sizeof(float4), cudaMemcpyHostToDevice));
     }
     memcpy(s.bmin, p, 12);
     memcpy(s.bmax, p + 12, 12);
@@ -1589,6 +1772,7 @@ jsb_status jsb_settings_regroup(const void *blob, size_t len, void *out, size_t 
     bool unsupported = false;
     std::string err = parse_settings(blob, len, ps, unsupported);
     if (!err.empty()) return fail(unsupported ? JSB_ERR_UNSUPPORTED : JSB_ERR_BLOB, err);
+    if (!ps.skinned.empty()) return fail(JSB_ERR_UNSUPPORTED, "settings with skinned constraints are not regrouped");
     std::vector<uint32_t> map;
     const std::vector<uint8_t> bytes = regroup_settings(ps, map);
     *out_len = bytes.size();
@@ -1893,6 +2077,9 @@ jsb_status jsb_adjoint_begin(jsb_context *ctx, float dt, int num_steps, int chec
     for (size_t b = 0; b < ctx->bodies.size(); ++b)
         if (ctx->bodies[b].creation.allow_sleeping)
             return fail(JSB_ERR_UNSUPPORTED, "body " + std::to_string(b) + " may sleep (allow_sleeping), which differentiable runs do not model");
+    for (size_t b = 0; b < ctx->bodies.size(); ++b)
+        if (!ctx->settings[ctx->bodies[b].settings_id]->parsed.skinned.empty())
+            return fail(JSB_ERR_UNSUPPORTED, "body " + std::to_string(b) + " has skinned constraints, which differentiable runs do not model");
     // Reuse the device buffers of the context's previous differentiable run (tape, checkpoints, adjoints):
     // allocating gigabytes of tape costs time every run otherwise.
     auto a = std::make_unique<AdjointSession>();

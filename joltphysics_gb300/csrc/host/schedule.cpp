@@ -48,17 +48,19 @@ std::string parse_settings(const void *blob, size_t len, ParsedSettings &s, bool
     static_assert(sizeof(ParsedSettings::Vertex) == 28 && sizeof(ParsedSettings::Face) == 16 &&
                       sizeof(ParsedSettings::Edge) == 16 && sizeof(ParsedSettings::Bend) == 24 &&
                       sizeof(ParsedSettings::Volume) == 24 && sizeof(ParsedSettings::LRA) == 12 &&
-                      sizeof(ParsedSettings::Group) == 28,
+                      sizeof(ParsedSettings::Group) == 28 && sizeof(ParsedSettings::Skinned) == 52 &&
+                      sizeof(ParsedSettings::InvBind) == 68,
                   "SaveBinaryState element sizes");
     unsupported = false;
     if (!blob) return "null settings blob";
     ByteReader r(static_cast<const uint8_t *>(blob), len);
-    uint32_t skinned_normals = 0;
     if (!(r.array(s.vertices, 28) && r.array(s.faces, 16) && r.array(s.edges, 16) && r.array(s.bends, 24) &&
-          r.array(s.volumes, 24) && r.skip_array(52, s.num_skinned) && r.skip_array(4, skinned_normals) && r.array(s.lras, 12) &&
+          r.array(s.volumes, 24) && r.array(s.skinned, 52) && r.array(s.skinned_normals, 4) && r.array(s.lras, 12) &&
           r.array(s.groups, 28) && r.skip_array(36, s.num_rod_stretch_shear) && r.skip_array(28, s.num_rod_bend_twist) &&
-          r.skip_array(68, s.num_inv_bind)))
+          r.array(s.inv_binds, 68)))
         return "truncated settings blob";
+    s.num_skinned = uint32_t(s.skinned.size());
+    s.num_inv_bind = uint32_t(s.inv_binds.size());
     if (r.remaining() != 0) return "trailing bytes after settings blob";
     const uint32_t nv = uint32_t(s.vertices.size());
     if (s.groups.empty()) return "settings have no update groups (SoftBodySharedSettings::Optimize was not called)";
@@ -77,6 +79,15 @@ std::string parse_settings(const void *blob, size_t len, ParsedSettings &s, bool
         if (bad(v.v, 4)) return "volume vertex index out of range";
     for (auto &l : s.lras)
         if (bad(l.v, 2)) return "LRA vertex index out of range";
+    for (auto &k : s.skinned) {
+        if (bad(&k.vertex, 1)) return "skinned constraint vertex index out of range";
+        for (auto &w : k.w)
+            if (w.weight != 0.0f && w.inv_bind >= s.inv_binds.size()) return "skin weight inverse bind index out of range";
+        const uint32_t start = k.normal_info & 0xffffffu, count = k.normal_info >> 24;
+        if (uint64_t(start) + count > s.skinned_normals.size()) return "skinned constraint normal range out of range";
+    }
+    for (uint32_t f : s.skinned_normals)
+        if (f >= s.faces.size()) return "skinned constraint normal face index out of range";
     ParsedSettings::Group prev{0, 0, 0, 0, 0, 0, 0};
     for (auto &g : s.groups) {
         if (g.edge < prev.edge || g.lra < prev.lra || g.bend < prev.bend || g.volume < prev.volume || g.rod_ss < prev.rod_ss ||
@@ -88,9 +99,13 @@ std::string parse_settings(const void *blob, size_t len, ParsedSettings &s, bool
         prev.volume != s.volumes.size() || prev.rod_ss != s.num_rod_stretch_shear || prev.rod_bt != s.num_rod_bend_twist ||
         prev.skinned != s.num_skinned)
         return "update groups do not cover all constraints";
-    if (s.num_skinned || s.num_rod_stretch_shear || s.num_rod_bend_twist) {
+    if (s.num_rod_stretch_shear || s.num_rod_bend_twist) {
         unsupported = true;
-        return "skinned constraints and Cosserat rods are not supported by the GPU solver";
+        return "Cosserat rods are not supported by the GPU solver";
+    }
+    if (s.skinned.size() >= (1u << 24)) {
+        unsupported = true;
+        return "more than 2^24 skinned constraints";
     }
     if (nv > 65536) {
         unsupported = true;
@@ -106,7 +121,7 @@ Schedule build_schedule(const ParsedSettings &s) {
         uint32_t level, type, index;
     };
     std::vector<Item> items;
-    items.reserve(s.edges.size() + s.bends.size() + s.volumes.size() + s.lras.size());
+    items.reserve(s.edges.size() + s.bends.size() + s.volumes.size() + s.lras.size() + s.skinned.size());
     uint32_t max_level = 0;
     auto place_rw = [&](const uint32_t *v, int k, uint32_t type, uint32_t index) {
         int32_t lvl = 0;
@@ -121,6 +136,7 @@ Schedule build_schedule(const ParsedSettings &s) {
         const ParsedSettings::Group &c = s.groups[g];
         for (uint32_t i = p.volume; i < c.volume; ++i) place_rw(s.volumes[i].v, 4, kVolume, i);
         for (uint32_t i = p.bend; i < c.bend; ++i) place_rw(s.bends[i].v, 4, kBend, i);
+        for (uint32_t i = p.skinned; i < c.skinned; ++i) place_rw(&s.skinned[i].vertex, 1, kEdge, kSkinRecord | i);
         for (uint32_t i = p.edge; i < c.edge; ++i) place_rw(s.edges[i].v, 2, kEdge, i);
         for (uint32_t i = p.lra; i < c.lra; ++i) {
             uint32_t a = s.lras[i].v[0], b = s.lras[i].v[1];
@@ -188,6 +204,13 @@ Schedule build_schedule(const ParsedSettings &s) {
                 break;
             }
             case kEdge: {
+                if (it.index & kSkinRecord) {
+                    r[0] = s.skinned[it.index & ~kSkinRecord].vertex;
+                    r[1] = it.index;
+                    r[2] = 0;
+                    r[3] = 0;
+                    break;
+                }
                 const auto &e = s.edges[it.index];
                 r[0] = e.v[0] | (e.v[1] << 16);
                 r[1] = 0;
@@ -204,7 +227,7 @@ Schedule build_schedule(const ParsedSettings &s) {
                 break;
             }
         }
-        out.source[k] = (it.type << 28) | it.index;
+        out.source[k] = (it.index & kSkinRecord) ? ((kSkinSource << 28) | (it.index & ~kSkinRecord)) : ((it.type << 28) | it.index);
     }
     // padded device layout
     auto pad = [](uint32_t v) { return (v + 31u) & ~31u; };
@@ -257,7 +280,7 @@ bool build_step_schedule(const ParsedSettings &s, uint32_t num_iterations, StepS
     };
     std::vector<Item> items;
     uint32_t cur_substep = 0;
-    const size_t per_substep = s.edges.size() + s.bends.size() + s.volumes.size() + s.lras.size() + nv;
+    const size_t per_substep = s.edges.size() + s.bends.size() + s.volumes.size() + s.lras.size() + s.skinned.size() + nv;
     items.reserve(per_substep * num_iterations);
     uint32_t max_level = 0;
     auto place_rw = [&](const uint32_t *v, int k, uint32_t type, uint32_t index) {
@@ -277,6 +300,7 @@ bool build_step_schedule(const ParsedSettings &s, uint32_t num_iterations, StepS
             const ParsedSettings::Group &c = s.groups[g];
             for (uint32_t i = p.volume; i < c.volume; ++i) place_rw(s.volumes[i].v, 4, kVolume, i);
             for (uint32_t i = p.bend; i < c.bend; ++i) place_rw(s.bends[i].v, 4, kBend, i);
+            for (uint32_t i = p.skinned; i < c.skinned; ++i) place_rw(&s.skinned[i].vertex, 1, kEdge, kSkinRecord | i);
             for (uint32_t i = p.edge; i < c.edge; ++i) place_rw(s.edges[i].v, 2, kEdge, i);
             for (uint32_t i = p.lra; i < c.lra; ++i) {
                 uint32_t a = s.lras[i].v[0], b = s.lras[i].v[1];
@@ -335,7 +359,8 @@ bool build_step_schedule(const ParsedSettings &s, uint32_t num_iterations, StepS
         const uint32_t k = slot_of[size_t(it.level) * 5 + it.type]++;
         uint32_t *r = &out.records[size_t(k) * 4];
         if (with_source) {
-            out.source[size_t(k) * 2] = (it.type << 28) | it.index;
+            out.source[size_t(k) * 2] =
+                (it.index & kSkinRecord) ? ((kSkinSource << 28) | (it.index & ~kSkinRecord)) : ((it.type << 28) | it.index);
             out.source[size_t(k) * 2 + 1] = it.substep;
         }
         switch (it.type) {
@@ -356,6 +381,11 @@ bool build_step_schedule(const ParsedSettings &s, uint32_t num_iterations, StepS
                 break;
             }
             case kEdge: {
+                if (it.index & kSkinRecord) {
+                    r[0] = s.skinned[it.index & ~kSkinRecord].vertex | (it.substep << 16);
+                    r[1] = it.index;
+                    break;
+                }
                 const auto &e = s.edges[it.index];
                 r[0] = e.v[0] | (e.v[1] << 16);
                 r[2] = fbits(e.rest);
@@ -460,6 +490,8 @@ void put_array(std::vector<uint8_t> &out, const std::vector<T> &items, const std
 }  // namespace
 
 std::vector<uint8_t> regroup_settings(const ParsedSettings &s, std::vector<uint32_t> &remap) {
+    remap.clear();
+    if (!s.skinned.empty()) return {};  // (not regrouped: the caller reports it)
     const uint32_t nv = uint32_t(s.vertices.size());
     std::vector<uint32_t> cv(s.volumes.size()), cb(s.bends.size()), ce(s.edges.size()), cl(s.lras.size());
     {

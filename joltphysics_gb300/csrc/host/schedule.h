@@ -36,6 +36,19 @@ struct ParsedSettings {
     struct Group {
         uint32_t edge, lra, rod_ss, rod_bt, bend, volume, skinned;
     };
+    struct Skinned {  // SoftBodySharedSettings::Skinned
+        uint32_t vertex;
+        struct {
+            uint32_t inv_bind;
+            float weight;
+        } w[4];
+        float max_distance, backstop_distance, backstop_radius;
+        uint32_t normal_info;  // start in skinned_normals (low 24 bits), face count (high 8 bits)
+    };
+    struct InvBind {  // SoftBodySharedSettings::InvBind
+        uint32_t joint;
+        float m[16];  // Mat44 columns
+    };
     std::vector<Vertex> vertices;
     std::vector<Face> faces;
     std::vector<Edge> edges;
@@ -43,6 +56,9 @@ struct ParsedSettings {
     std::vector<Volume> volumes;
     std::vector<LRA> lras;
     std::vector<Group> groups;
+    std::vector<Skinned> skinned;
+    std::vector<uint32_t> skinned_normals;  // face indices
+    std::vector<InvBind> inv_binds;
     uint32_t num_skinned = 0, num_rod_stretch_shear = 0, num_rod_bend_twist = 0, num_inv_bind = 0;
 };
 
@@ -52,6 +68,11 @@ std::string parse_settings(const void *blob, size_t len, ParsedSettings &out, bo
 
 // Constraint type order inside one dependency level (matches the level descriptor fields).
 enum RecordType : uint32_t { kBend = 0, kVolume = 1, kEdge = 2, kLRA = 3 };
+// Skinned constraints (ApplySkinConstraints, one vertex each) share the edge slots of a level: their
+// record is {vertex | substep << 16, kSkinRecord | skinned index, 0, 0} (an edge's second word is 0), the
+// substep being set in whole-step schedules only. In `source` they have type 5.
+constexpr uint32_t kSkinRecord = 0x80000000u;
+constexpr uint32_t kSkinSource = 5;
 
 struct Schedule {
     // levels[l] = {first record, end of bends, end of volumes, end of edges}; levels has
@@ -80,7 +101,8 @@ constexpr uint32_t kPadRecord = 0xffffffffu;  // first word of a padding slot
 // Builds the dependency-level schedule of one substep's constraint projection.
 //
 // Sequence: the update groups in order (parallel groups first, the non-parallel group last), and in
-// each group volumes, dihedral bends, edges, LRA (ProcessGroup, SoftBodyMotionProperties.cpp:1030-1055).
+// each group volumes, dihedral bends, skinned constraints, edges, LRA (ProcessGroup,
+// SoftBodyMotionProperties.cpp:1030-1055).
 // Level of a constraint = 1 + the latest level that wrote one of its vertices, and for vertices it
 // writes also 1 + the latest level that read them (LRA constraints only read their anchor vertex).
 // Constraints of one level therefore touch disjoint written vertices, so any execution order inside a

@@ -80,7 +80,20 @@ struct BodyDesc {
     float gravity_factor;
     float vertex_radius;
     uint32_t flags;
+    // skinned constraints (null: none): per constraint {max distance, back stop distance, back stop radius,
+    // vertex}; per vertex of the body three float4 {previous position, position, normal}
+    // (SoftBodyMotionProperties::SkinState)
+    const float4 *skin_params;
+    float4 *skin_state;
 };
+
+// Run-time skinning switches of one body (SoftBodyMotionProperties::mEnableSkinConstraints,
+// mSkinnedMaxDistanceMultiplier, mSkinStatePreviousPositionValid).
+struct SkinCtl {
+    float max_distance_multiplier;
+    uint32_t flags;  // kSkinEnabled | kSkinPreviousValid
+};
+enum : uint32_t { kSkinEnabled = 1, kSkinPreviousValid = 2 };
 
 enum : int32_t { kMotionStatic = 0, kMotionKinematic = 1, kMotionDynamic = 2 };  // EMotionType
 constexpr int32_t kMotionSensor = 3;  // a leaf shape of a sensor (SoftBodyMotionProperties::CollidingSensor)
@@ -193,6 +206,7 @@ struct StepParams {
     const float4 *hull_f4;
     const uint32_t *hull_u32;
     uint32_t *sensor_contact;  // per body: bit k = sensor shape k of its table has a vertex inside it (mHasContact)
+    SkinCtl *skin_ctl;         // per body
     BodySleep *sleep;      // per body (null: bodies never sleep)
     float sleep_velocity_threshold;  // PhysicsSettings::mPointVelocitySleepThreshold (compared with |v|^2)
     float time_before_sleep;         // PhysicsSettings::mTimeBeforeSleep

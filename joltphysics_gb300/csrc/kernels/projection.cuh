@@ -314,15 +314,71 @@ __device__ __forceinline__ void project_lra(X sx, uint4 r) {
     }
 }
 
+// What a skinned constraint's projection reads besides the vertex: the body's constraint parameters and
+// skin states, its switches and the substep (1-based iteration count mNextIteration / mNumIterations).
+struct SkinRefs {
+    const float4 *params;
+    const float4 *state;
+    float multiplier;
+    uint32_t flags;
+    uint32_t num_iterations;
+    uint32_t substep;  // of a per-substep walk (whole-step records carry their own)
+};
+
+// ApplySkinConstraints (SoftBodyMotionProperties.cpp:509-571) for one constraint: the skinned position
+// interpolated from the previous to the current skin state by the iteration, then the back stop sphere
+// and the maximum distance, or the skinned position itself for a kinematic (max distance 0) vertex.
+template <class X>
+__device__ __forceinline__ void project_skin(X sx, uint4 r, const SkinRefs &sk, bool whole_step) {
+    if (!(sk.flags & kSkinEnabled)) return;
+    const uint32_t v = r.x & 0xffffu;
+    const uint32_t substep = whole_step ? (r.x >> 16) : sk.substep;
+    const float4 prm = sk.params[r.y & 0xffffffu];
+    const float4 *st = sk.state + size_t(v) * 3;
+    const float factor = (sk.flags & kSkinPreviousValid) ? div_rn(float(substep + 1), float(sk.num_iterations)) : 1.0f;
+    const float prev_factor = 1.0f - factor;
+    const float max_distance = prm.x * sk.multiplier;
+    const f3 skin_pos = prev_factor * xyz(st[0]) + factor * xyz(st[1]);
+    const float4 p = ldx(sx, v);
+    f3 x = xyz(p);
+    if (max_distance > 0.0f) {
+        const float bsd = prm.y, bsr = prm.z;
+        if (bsd < max_distance) {
+            const f3 n = xyz(st[2]);
+            const f3 center = skin_pos - n * (bsd + bsr);
+            const f3 delta = x - center;
+            const float dls = len_sq(delta);
+            if (dls < bsr * bsr) {
+                const float dl = sqrt_rn(dls);
+                x = dl > 0.0f ? center + delta * div_rn(bsr, dl) : center + n * bsr;
+            }
+        }
+        if (max_distance < FLT_MAX) {
+            const f3 delta = x - skin_pos;
+            const float dls = len_sq(delta);
+            const float mds = max_distance * max_distance;
+            if (dls > mds) x = skin_pos + delta * sqrt_rn(div_rn(mds, dls));
+        }
+    } else {
+        x = skin_pos;
+    }
+    stx(sx, v, with_w(x, p.w));
+}
+
 template <bool kGuard = false, class X>
-__device__ __forceinline__ void project(X sx, uint4 r, int type, float inv_dt_sq) {
+__device__ __forceinline__ void project(X sx, uint4 r, int type, float inv_dt_sq, const SkinRefs *sk = nullptr,
+                                        bool whole_step = false) {
     if (type == 0)
         project_bend<kGuard>(sx, r, inv_dt_sq);
     else if (type == 1)
         project_volume<kGuard>(sx, r, inv_dt_sq);
-    else if (type == 2)
-        project_edge<kGuard>(sx, r, inv_dt_sq);
-    else
+    else if (type == 2) {
+        if (r.y & 0x80000000u) {
+            if (sk) project_skin(sx, r, *sk, whole_step);
+        } else {
+            project_edge<kGuard>(sx, r, inv_dt_sq);
+        }
+    } else
         project_lra(sx, r);
 }
 

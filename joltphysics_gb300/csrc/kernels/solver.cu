@@ -182,7 +182,7 @@ __device__ __forceinline__ void tape_inputs(const float4 *sx, uint4 r, int type,
 // inputs of this substep, 3 float4 per slot). Returns false when a staging wait gave up.
 template <int T, bool kTape, bool kGuard>
 __device__ __forceinline__ bool apply_levels(float4 *sx, const BodyDesc &d, float inv_dt_sq, const StageRing &ring,
-                                             uint32_t &phases, float4 *tape_cons, uint32_t *error) {
+                                             uint32_t &phases, float4 *tape_cons, uint32_t *error, const SkinRefs *sk) {
     const uint4 *__restrict__ levels = d.levels;
     const uint4 *__restrict__ rec = d.records;
     const uint4 *__restrict__ chunks = d.chunks;
@@ -206,7 +206,7 @@ __device__ __forceinline__ bool apply_levels(float4 *sx, const BodyDesc &d, floa
                 const uint4 r = rel + s < ch.w ? rr[rel + s] : __ldg(rec + lv.x + s);
                 if (r.x != 0xffffffffu) {
                     if (kTape) tape_inputs(sx, r, slot_type(lv, s), tape_cons + size_t(lv.x + s) * 3);
-                    project<kGuard>(sx, r, slot_type(lv, s), inv_dt_sq);
+                    project<kGuard>(sx, r, slot_type(lv, s), inv_dt_sq, sk, false);
                 }
             }
             cta_sync<T>();
@@ -283,7 +283,8 @@ __device__ __forceinline__ void vertex_between_substeps(float4 *sx, const Vertex
 // per whole-step slot). Returns false when a staging wait gave up.
 template <int T, bool kSmemState, bool kGuard, bool kTape>
 __device__ __forceinline__ bool apply_step_levels(float4 *sx, const BodyDesc &d, float inv_dt_sq, const StageRing &ring,
-                                                  uint32_t &phases, const VertexPass &vp, float4 *tape_cons, uint32_t *error) {
+                                                  uint32_t &phases, const VertexPass &vp, float4 *tape_cons, uint32_t *error,
+                                                  const SkinRefs *sk) {
     const uint4 *__restrict__ levels = d.step_levels;
     const uint4 *__restrict__ rec = d.step_records;
     const uint4 *__restrict__ chunks = d.step_chunks;
@@ -310,7 +311,7 @@ __device__ __forceinline__ bool apply_step_levels(float4 *sx, const BodyDesc &d,
                         vertex_between_substeps<kSmemState, kTape>(sx, vp, r.x, r.y);
                     } else {
                         if (kTape) tape_inputs(sx, r, type, tape_cons + size_t(lv.x + s) * 3);
-                        project<kGuard>(sx, r, type, inv_dt_sq);
+                        project<kGuard>(sx, r, type, inv_dt_sq, sk, true);
                     }
                 }
             }
@@ -491,7 +492,15 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     }
     const uint32_t passes = step_walk ? 1u : n_it;
 
+    SkinRefs skin_refs{};
+    const SkinRefs *skin = nullptr;
+    if (d.skin_params && p.skin_ctl) {
+        const SkinCtl ctl = p.skin_ctl[b];
+        skin_refs = SkinRefs{d.skin_params, d.skin_state, ctl.max_distance_multiplier, ctl.flags, n_it, 0};
+        skin = &skin_refs;
+    }
     for (uint32_t it = 0; it < passes; ++it) {
+        skin_refs.substep = it;
         float4 *tape_state = nullptr;
         if (kTape) {
             tape_state = td.state + (size_t(p.tape_step) * n_it + it) * 3 * nv;
@@ -565,13 +574,13 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
             // result, slower)
             float4 *step_cons = kTape ? td.cons + size_t(p.tape_step) * td.step_slots * 3 : nullptr;
             if (nan_any)
-                walked = apply_step_levels<T, kSmemState, true, kTape>(sx, d, inv_dt_sq, ring, ring_phases, vp, step_cons, p.error);
+                walked = apply_step_levels<T, kSmemState, true, kTape>(sx, d, inv_dt_sq, ring, ring_phases, vp, step_cons, p.error, skin);
             else
-                walked = apply_step_levels<T, kSmemState, false, kTape>(sx, d, inv_dt_sq, ring, ring_phases, vp, step_cons, p.error);
+                walked = apply_step_levels<T, kSmemState, false, kTape>(sx, d, inv_dt_sq, ring, ring_phases, vp, step_cons, p.error, skin);
         } else if (nan_any)
-            walked = apply_levels<T, kTape, true>(sx, d, inv_dt_sq, ring, ring_phases, cons, p.error);
+            walked = apply_levels<T, kTape, true>(sx, d, inv_dt_sq, ring, ring_phases, cons, p.error, skin);
         else
-            walked = apply_levels<T, kTape, false>(sx, d, inv_dt_sq, ring, ring_phases, cons, p.error);
+            walked = apply_levels<T, kTape, false>(sx, d, inv_dt_sq, ring, ring_phases, cons, p.error, skin);
         if (!walked) return false;  // (uniform: decided at a barrier) the body is left half stepped, flagged
         __syncthreads();
         if (kTape) {  // position after the constraints of the last substep walked
@@ -711,6 +720,14 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     for (uint32_t i = tid; i < nv; i += T) {
         float4 pi = sx[i];
         gx[i] = shift ? with_w(xyz(pi) - delta, pi.w) : pi;
+    }
+    if (d.skin_state) {  // UpdateSoftBodyState (:889-892, :916-917): the skin positions move with the body
+        if (shift)
+            for (uint32_t i = tid; i < nv; i += T) {
+                float4 &sp = d.skin_state[size_t(i) * 3 + 1];
+                sp = with_w(xyz(sp) - delta, sp.w);
+            }
+        if (tid == 0 && p.skin_ctl) p.skin_ctl[b].flags &= ~kSkinPreviousValid;
     }
     __syncthreads();
     return true;
@@ -927,6 +944,7 @@ __global__ void __launch_bounds__(T) step_kernel_noalloc(const __grid_constant__
     p.contact_point = nullptr;
     p.contact_delta = nullptr;
     p.sensor_contact = nullptr;
+    p.skin_ctl = nullptr;
     if (threadIdx.x == 0) {
         stage_bar_init(&sh.stage_bar);
         stage_bar_init(&sh.ring_bar[0]);
@@ -1000,6 +1018,7 @@ extern "C" jsb_status jsb_step_body_noalloc(const void *settings_blob, size_t le
     bool unsupported = false;
     std::string err = parse_settings(settings_blob, len, ps, unsupported);
     if (!err.empty()) return report_error(unsupported ? JSB_ERR_UNSUPPORTED : JSB_ERR_BLOB, err);
+    if (!ps.skinned.empty()) return report_error(JSB_ERR_UNSUPPORTED, "jsb_step_body_noalloc does not take skinned constraints");
     const uint32_t nv = uint32_t(ps.vertices.size());
     const bool pressure = creation->pressure > 0.0f;
     const uint32_t nf = pressure ? uint32_t(ps.faces.size()) : 0u;

@@ -175,6 +175,13 @@ struct LRA { uint32_t v[2]; float max_distance; };
 struct Face { uint32_t v[3]; uint32_t material; };
 struct Group { uint32_t edge, lra, rod_ss, rod_bt, bend, volume, skinned; };
 struct SVertex { float pos[3], vel[3], inv_mass; };
+struct Skinned {  // SoftBodySharedSettings::Skinned
+    uint32_t vertex;
+    struct { uint32_t inv_bind; float weight; } w[4];
+    float max_distance, backstop_distance, backstop_radius;
+    uint32_t normal_info;  // start in skinned_normals (low 24 bits), face count (high 8 bits)
+};
+struct InvBind { uint32_t joint; float m[16]; };  // SoftBodySharedSettings::InvBind, Mat44 columns
 
 struct Settings {
     std::vector<SVertex> vertices;
@@ -184,6 +191,9 @@ struct Settings {
     std::vector<Volume> volumes;
     std::vector<LRA> lras;
     std::vector<Group> groups;
+    std::vector<Skinned> skinned;
+    std::vector<uint32_t> skinned_normals;
+    std::vector<InvBind> inv_binds;
     uint32_t n_skinned = 0, n_rod_ss = 0, n_rod_bt = 0;
 };
 
@@ -227,8 +237,9 @@ private:
 inline bool parse_settings(const uint8_t *blob, size_t len, Settings &s, std::string &err) {
     Reader r(blob, len);
     bool ok = r.array(s.vertices, 28) && r.array(s.faces, 16) && r.array(s.edges, 16) && r.array(s.bends, 24) &&
-              r.array(s.volumes, 24) && r.skip_array(52, &s.n_skinned) && r.skip_array(4, nullptr) && r.array(s.lras, 12) &&
-              r.array(s.groups, 28) && r.skip_array(36, &s.n_rod_ss) && r.skip_array(28, &s.n_rod_bt) && r.skip_array(68, nullptr);
+              r.array(s.volumes, 24) && r.array(s.skinned, 52) && r.array(s.skinned_normals, 4) && r.array(s.lras, 12) &&
+              r.array(s.groups, 28) && r.skip_array(36, &s.n_rod_ss) && r.skip_array(28, &s.n_rod_bt) && r.array(s.inv_binds, 68);
+    s.n_skinned = uint32_t(s.skinned.size());
     if (!ok) {
         err = "truncated settings blob";
         return false;
@@ -322,6 +333,11 @@ struct Body {
     // point, contact normal, shape index}
     std::vector<std::array<float, 8>> manifold;
     uint32_t sensor_hits = 0;  // bit k: table shape k is a sensor shape a vertex penetrated (last step)
+    // SkinState per vertex (sized when the settings have skinned constraints) and the skinning switches
+    std::vector<V3<R>> skin_prev, skin_pos, skin_normal;
+    bool skin_enabled = true, skin_prev_valid = false;
+    R skin_mult = R(1);
+    uint32_t cur_iteration = 0;  // of the step being run (ApplySkinConstraints' mNextIteration - 1)
 };
 
 template <class R>
@@ -375,6 +391,12 @@ public:
         b.bmin = {big, big, big};
         b.bmax = {-big, -big, -big};
         b.v.resize(s->vertices.size());
+        if (!s->skinned.empty()) {
+            const V3<R> z = {R(0), R(0), R(0)};
+            b.skin_prev.assign(s->vertices.size(), z);
+            b.skin_pos.assign(s->vertices.size(), z);
+            b.skin_normal.assign(s->vertices.size(), z);
+        }
         for (const Edge &e : s->edges) b.edge_c.push_back(R(e.compliance));
         for (const Volume &vol : s->volumes) b.vol_c.push_back(R(vol.compliance));
         for (size_t i = 0; i < s->vertices.size(); ++i) {  // SoftBodyMotionProperties::Initialize :59-105
@@ -566,6 +588,7 @@ public:
             dec->vclamp.assign(b.v.size(), 0);
         }
         for (uint32_t it = 0; it < n_it; ++it) {
+            b.cur_iteration = it;
             apply_pressure(b, dt_sub);
             integrate(b, g, dt_sub);
             const size_t ng = s.groups.size();
@@ -877,8 +900,101 @@ public:
         R inv_dt_sq = R(1) / (dt * dt);
         for (uint32_t i = prev.volume; i < cur.volume; ++i) apply_volume(b, s.volumes[i], b.vol_c[i], inv_dt_sq);
         for (uint32_t i = prev.bend; i < cur.bend; ++i) apply_bend(b, s.bends[i], inv_dt_sq);
+        for (uint32_t i = prev.skinned; i < cur.skinned; ++i) apply_skin(b, s.skinned[i]);
         for (uint32_t i = prev.edge; i < cur.edge; ++i) apply_edge(b, s.edges[i], b.edge_c[i], inv_dt_sq);
         for (uint32_t i = prev.lra; i < cur.lra; ++i) apply_lra(b, s.lras[i]);
+    }
+
+    void apply_skin(Body<R> &b, const Skinned &sk) {  // ApplySkinConstraints :509-571
+        if (!b.skin_enabled) return;
+        const R factor = b.skin_prev_valid ? R(float(b.cur_iteration + 1)) / R(float(b.cs.num_iterations)) : R(1);
+        const R prev_factor = R(1) - factor;
+        Vertex<R> &v = b.v[sk.vertex];
+        const R max_distance = R(sk.max_distance) * b.skin_mult;
+        const V3<R> skin_pos = add(mul(prev_factor, b.skin_prev[sk.vertex]), mul(factor, b.skin_pos[sk.vertex]));
+        if (max_distance > R(0)) {
+            const R bsd = R(sk.backstop_distance), bsr = R(sk.backstop_radius);
+            if (bsd < max_distance) {
+                const V3<R> n = b.skin_normal[sk.vertex];
+                const V3<R> center = sub(skin_pos, mul(bsd + bsr, n));
+                const V3<R> delta = sub(v.pos, center);
+                const R dls = len_sq(delta);
+                if (dls < bsr * bsr) {
+                    const R dl = std::sqrt(dls);
+                    v.pos = dl > R(0) ? add(center, mul(bsr / dl, delta)) : add(center, mul(bsr, n));
+                }
+            }
+            if (max_distance < R(FLT_MAX)) {
+                const V3<R> delta = sub(v.pos, skin_pos);
+                const R dls = len_sq(delta);
+                const R mds = max_distance * max_distance;
+                if (dls > mds) v.pos = add(skin_pos, mul(std::sqrt(mds / dls), delta));
+            }
+        } else {
+            v.pos = skin_pos;
+        }
+    }
+
+    // SkinVertices (:1139-1230) with joint matrices (16 floats each, Mat44 columns): Mat44 * Mat44 and
+    // Mat44 * Vec3 as ((c0 x + c1 y) + c2 z) + c3 (Mat44.inl:241-302).
+    void skin_vertices(Body<R> &b, const float *joints, uint32_t nj, bool hard) {
+        const Settings &s = *b.settings;
+        std::vector<std::array<R, 16>> mats(s.inv_binds.size());
+        for (size_t k = 0; k < mats.size(); ++k) {
+            const float *J = joints + 16 * size_t(s.inv_binds[k].joint);
+            const float *M = s.inv_binds[k].m;
+            for (int i = 0; i < 4; ++i)
+                for (int r = 0; r < 4; ++r)
+                    mats[k][4 * i + r] = ((R(J[r]) * R(M[4 * i]) + R(J[4 + r]) * R(M[4 * i + 1])) + R(J[8 + r]) * R(M[4 * i + 2])) +
+                                         R(J[12 + r]) * R(M[4 * i + 3]);
+        }
+        (void)nj;
+        for (const Skinned &sk : s.skinned) {
+            const SVertex &bv = s.vertices[sk.vertex];
+            const R bx = R(bv.pos[0]), by = R(bv.pos[1]), bz = R(bv.pos[2]);
+            V3<R> pos = {R(0), R(0), R(0)};
+            for (const auto &w : sk.w) {
+                if (w.weight == 0.0f) break;
+                const auto &m = mats[w.inv_bind];
+                V3<R> mv;
+                mv.x = ((m[0] * bx + m[4] * by) + m[8] * bz) + m[12];
+                mv.y = ((m[1] * bx + m[5] * by) + m[9] * bz) + m[13];
+                mv.z = ((m[2] * bx + m[6] * by) + m[10] * bz) + m[14];
+                pos = add(pos, mul(R(w.weight), mv));
+            }
+            b.skin_prev[sk.vertex] = b.skin_pos[sk.vertex];
+            b.skin_pos[sk.vertex] = pos;
+        }
+        auto normalized_or_zero = [](V3<R> v) {
+            const R l2 = (v.x * v.x + v.y * v.y) + v.z * v.z;
+            if (l2 <= R(FLT_MIN)) return V3<R>{R(0), R(0), R(0)};
+            const R l = std::sqrt(l2);
+            return V3<R>{v.x / l, v.y / l, v.z / l};
+        };
+        for (const Skinned &sk : s.skinned) {
+            V3<R> n = {R(0), R(0), R(0)};
+            const uint32_t nf = sk.normal_info >> 24;
+            if (nf > 0) {
+                for (uint32_t k = 0; k < nf; ++k) {
+                    const Face &f = s.faces[s.skinned_normals[(sk.normal_info & 0xffffffu) + k]];
+                    const V3<R> v0 = b.skin_pos[f.v[0]], v1 = b.skin_pos[f.v[1]], v2 = b.skin_pos[f.v[2]];
+                    n = add(n, normalized_or_zero(cross(sub(v1, v0), sub(v2, v0))));
+                }
+                n = normalized_or_zero(n);
+            }
+            b.skin_normal[sk.vertex] = n;
+        }
+        if (hard) {
+            for (const Skinned &sk : s.skinned) {
+                b.skin_prev[sk.vertex] = b.skin_pos[sk.vertex];
+                b.v[sk.vertex].pos = b.skin_pos[sk.vertex];
+                b.v[sk.vertex].vel = {R(0), R(0), R(0)};
+            }
+        } else if (!b.skin_enabled) {
+            for (const Skinned &sk : s.skinned)
+                if (sk.max_distance == 0.0f) b.v[sk.vertex].pos = b.skin_pos[sk.vertex];
+        }
+        b.skin_prev_valid = true;
     }
 
     void apply_bend(Body<R> &b, const Bend &c, R inv_dt_sq) {  // :367-456
@@ -1087,6 +1203,7 @@ public:
         if (b.cs.update_position) {
             V3<R> delta = mul(R(0.5f), add(b.bmin, b.bmax));
             for (auto &v : b.v) v.pos = sub(v.pos, delta);
+            for (auto &p : b.skin_pos) p = sub(p, delta);  // (:889-892)
             b.bmin = sub(b.bmin, delta);
             b.bmax = sub(b.bmax, delta);
             b.pmin = sub(b.pmin, delta);
@@ -1097,6 +1214,7 @@ public:
             wd.z = (R(0) * delta.x + R(0) * delta.y) + R(1) * delta.z;
             b.position = add(b.position, wd);
         }
+        b.skin_prev_valid = false;  // (:916-917)
         // sleep test (:902-915) and deactivation (PhysicsSystem.cpp:2875-2884, BodyManager.cpp:559-561)
         if (b.cs.allow_sleeping) {
             if (max_v_sq > sleep_velocity_threshold) {
@@ -1169,8 +1287,8 @@ int oracle_add_body(void *w, const uint8_t *blob, size_t len, const float pos[3]
     Handle *h = static_cast<Handle *>(w);
     auto s = std::make_shared<Settings>();
     if (!parse_settings(blob, len, *s, h->err)) return -1;
-    if (s->n_skinned || s->n_rod_ss || s->n_rod_bt) {
-        h->err = "skinned constraints and rods are not supported";
+    if (s->n_rod_ss || s->n_rod_bt) {
+        h->err = "rods are not supported";
         return -1;
     }
     Creation cs;
@@ -1431,6 +1549,52 @@ int oracle_copy_decisions(void *dst, const void *src) {
         d->wf.bodies[i].decision_step = 0;
     }
     return 0;
+}
+
+// SkinVertices of one body (joint matrices: 16 floats each, Mat44 columns).
+int oracle_skin_vertices(void *w, int body, const float *joints, int num_joints, int hard_skin_all) {
+    Handle *h = static_cast<Handle *>(w);
+    if (h->wf.bodies[body].skin_pos.empty()) return -1;
+    h->wf.skin_vertices(h->wf.bodies[body], joints, uint32_t(num_joints), hard_skin_all != 0);
+    h->wd.skin_vertices(h->wd.bodies[body], joints, uint32_t(num_joints), hard_skin_all != 0);
+    return 0;
+}
+
+// SetEnableSkinConstraints / SetSkinnedMaxDistanceMultiplier.
+int oracle_set_skin_settings(void *w, int body, int enable, float multiplier) {
+    Handle *h = static_cast<Handle *>(w);
+    h->wf.bodies[body].skin_enabled = h->wd.bodies[body].skin_enabled = enable != 0;
+    h->wf.bodies[body].skin_mult = multiplier;
+    h->wd.bodies[body].skin_mult = double(multiplier);
+    return 0;
+}
+
+// The body's skin states: 9 floats per vertex {previous position, position, normal}; returns the vertex
+// count (0 without skinned constraints).
+int oracle_get_skin_state(void *w, int body, float *out) {
+    Handle *h = static_cast<Handle *>(w);
+    if (h->use_double) {
+        const auto &b = h->wd.bodies[body];
+        for (size_t i = 0; i < b.skin_pos.size(); ++i) {
+            const V3<double> *a[3] = {&b.skin_prev[i], &b.skin_pos[i], &b.skin_normal[i]};
+            for (int k = 0; k < 3; ++k) {
+                out[9 * i + 3 * k] = float(a[k]->x);
+                out[9 * i + 3 * k + 1] = float(a[k]->y);
+                out[9 * i + 3 * k + 2] = float(a[k]->z);
+            }
+        }
+        return int(b.skin_pos.size());
+    }
+    const auto &b = h->wf.bodies[body];
+    for (size_t i = 0; i < b.skin_pos.size(); ++i) {
+        const V3<float> *a[3] = {&b.skin_prev[i], &b.skin_pos[i], &b.skin_normal[i]};
+        for (int k = 0; k < 3; ++k) {
+            out[9 * i + 3 * k] = a[k]->x;
+            out[9 * i + 3 * k + 1] = a[k]->y;
+            out[9 * i + 3 * k + 2] = a[k]->z;
+        }
+    }
+    return int(b.skin_pos.size());
 }
 
 int oracle_set_sleep_settings(void *w, float time_before_sleep, float point_velocity_sleep_threshold) {

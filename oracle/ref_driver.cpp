@@ -131,6 +131,20 @@ Ref<SoftBodySharedSettings> build_settings(const jsb::scene::MeshSpec &m) {
                                                                           m.volumes[i][3], m.volume_compliance[i]));
         s->CalculateVolumeConstraintVolumes();
     }
+    if (!m.skinned.empty()) {  // skinned constraints and inverse bind matrices, then their normals
+        for (auto &ib : m.inv_binds) {
+            Mat44 mm;
+            for (int c = 0; c < 4; ++c)
+                mm.SetColumn4(c, Vec4(ib.second[4 * c], ib.second[4 * c + 1], ib.second[4 * c + 2], ib.second[4 * c + 3]));
+            s->mInvBindMatrices.push_back(SoftBodySharedSettings::InvBind(ib.first, mm));
+        }
+        for (auto &k : m.skinned) {
+            SoftBodySharedSettings::Skinned sk(k.vertex, k.max_distance, k.backstop_distance, k.backstop_radius);
+            for (int w = 0; w < 4; ++w) sk.mWeights[w] = SoftBodySharedSettings::SkinWeight(k.weights[w].first, k.weights[w].second);
+            s->mSkinnedConstraints.push_back(sk);
+        }
+        s->CalculateSkinnedConstraintNormals();
+    }
     s->Optimize();
     if (!m.post_optimize_edge_compliance.empty())
         for (size_t i = 0; i < s->mEdgeConstraints.size(); ++i)
@@ -365,6 +379,19 @@ int main(int argc, char **argv) {
             recorder.soft_index[ids.back().GetIndex()] = uint32_t(ids.size() - 1);
         }
         system.OptimizeBroadPhase();
+        // Skinned bodies (skin=<path>): before every step the joints' matrices relative to the body's centre
+        // of mass go to SoftBodyMotionProperties::SkinVertices (hard skinning on the first step); the
+        // maximum distance multiplier becomes 1.5 from step 40 and skin constraints are off for steps 61-65.
+        // Per step and skinned body: i32 step, u32 body, f32 multiplier, u32 enabled, u32 hard, 2 x 16 f32.
+        FILE *skin = nullptr;
+        if (kv.count("skin")) {
+            skin = fopen(kv["skin"].c_str(), "wb");
+            if (!skin) {
+                fprintf(stderr, "cannot open %s\n", kv["skin"].c_str());
+                return 1;
+            }
+            fwrite("JSBK", 4, 1, skin);
+        }
         FILE *tables = nullptr;
         if (!spec.rigid.empty() && kv.count("tables")) {
             system.SetSoftBodyContactListener(&recorder);
@@ -474,6 +501,36 @@ int main(int argc, char **argv) {
                 const float *fv = spec.bodies[b].force;
                 if (fv[0] != 0.0f || fv[1] != 0.0f || fv[2] != 0.0f) bi.AddForce(ids[b], Vec3(fv[0], fv[1], fv[2]));
             }
+            for (size_t b = 0; b < spec.bodies.size() && skin; ++b) {
+                if (spec.bodies[b].mesh.skinned.empty()) continue;
+                const float phi = 6.2831853f * float(step) / 60.0f;
+                const Mat44 j0 = Mat44::sTranslation(Vec3(0.3f * std::sin(phi), 1.5f, 0.0f)) * Mat44::sRotationX(0.2f * std::sin(phi));
+                const Mat44 j1 = j0 * Mat44::sTranslation(Vec3(0.0f, 0.0f, 0.6f)) * Mat44::sRotationX(0.3f * std::sin(phi));
+                BodyLockWrite lock(system.GetBodyLockInterface(), ids[b]);
+                Body &body = lock.GetBody();
+                SoftBodyMotionProperties *mp = static_cast<SoftBodyMotionProperties *>(body.GetMotionProperties());
+                const RMat44 com = body.GetCenterOfMassTransform();
+                const Mat44 inv = com.InversedRotationTranslation().ToMat44();
+                const Mat44 joints[2] = {inv * j0, inv * j1};
+                const float mult = step >= 40 ? 1.5f : 1.0f;
+                const bool enabled = !(step >= 61 && step <= 65);
+                const bool hard = step == 1;
+                mp->SetSkinnedMaxDistanceMultiplier(mult);
+                mp->SetEnableSkinConstraints(enabled);
+                mp->SkinVertices(com, joints, 2, hard, temp_allocator);
+                int32_t st = step;
+                fwrite(&st, 4, 1, skin);
+                put_u32(skin, uint32_t(b));
+                fwrite(&mult, 4, 1, skin);
+                put_u32(skin, enabled ? 1u : 0u);
+                put_u32(skin, hard ? 1u : 0u);
+                for (const Mat44 &m : joints)
+                    for (int c = 0; c < 4; ++c) {
+                        const Vec4 col = m.GetColumn4(c);
+                        float f4[4] = {col.GetX(), col.GetY(), col.GetZ(), col.GetW()};
+                        fwrite(f4, 4, 4, skin);
+                    }
+            }
             auto t0 = std::chrono::steady_clock::now();
             EPhysicsUpdateError err = system.Update(spec.dt, spec.collision_steps, &temp_allocator, &job_system);
             auto t1 = std::chrono::steady_clock::now();
@@ -516,6 +573,7 @@ int main(int argc, char **argv) {
         }
         if (f) fclose(f);
         if (tables) fclose(tables);
+        if (skin) fclose(skin);
         printf("{\"scene\": \"%s\", \"bodies\": %zu, \"vertices\": %llu, \"steps\": %d, \"threads\": %d, \"seconds\": %.6f, "
                "\"vertex_iterations_per_s\": %.6e}\n",
                scene_name.c_str(), spec.bodies.size(), (unsigned long long)total_vertices, steps, threads, seconds,

@@ -126,6 +126,33 @@ FULL_CASES = {
 }
 
 
+def make_skinned(name: str = "skinned_cloth", steps: int = 90, dump: tuple = (1, 2, 10, 39, 40, 60, 62, 66, 90)):
+    """A skinned cloth (skinned constraints, SkinVertices before every step): per dump step the
+    deterministic build's states (with the SaveState bytes, skin states included), and per step the
+    joint matrices relative to the body's centre of mass, the max-distance multiplier, the skin switch and
+    the hard-skinning flag the driver passed."""
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        path, sk = os.path.join(tmp, "det.bin"), os.path.join(tmp, "det.skin")
+        run_reference("det", "skinned_cloth", path, dump=",".join(str(s) for s in [0, *dump]), steps=steps, skin=sk)
+        sc, dumps = parse_dump(path)
+        buf = open(sk, "rb").read()
+    assert buf[:4] == b"JSBK"
+    rec = np.dtype([("step", "<i4"), ("body", "<u4"), ("mult", "<f4"), ("enabled", "<u4"), ("hard", "<u4"), ("joints", "<f4", (2, 16))])
+    ev = np.frombuffer(buf, rec, (len(buf) - 4) // rec.itemsize, 4)
+    out["scene"] = np.frombuffer(sc.raw, np.uint8)
+    out["steps"] = np.array(dump, np.int32)
+    out["num_vertices"] = np.array([b.num_vertices for b in sc.bodies], np.int64)
+    for d in dumps[1:]:
+        out[f"det_pos_{d.step}"] = np.stack(d.positions).astype(np.float32)
+        out[f"det_local_{d.step}"] = np.concatenate(d.local).astype(np.float32)
+        out[f"det_vel_{d.step}"] = np.concatenate(d.velocities).astype(np.float32)
+        out[f"det_state_{d.step}"] = np.frombuffer(d.states[0], np.uint8)
+    for k in ("step", "body", "mult", "enabled", "hard", "joints"):
+        out[f"skin_{k}"] = ev[k].copy()
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+
+
 def make_full(name: str, scene: str, params: dict, steps: list[int], threads: int):
     import hashlib
     import json
@@ -171,6 +198,9 @@ if __name__ == "__main__":
     if not which or "coupling_hulls" in which:  # + a static and a dynamic convex hull under a fourth cloth
         make_coupling("coupling_hulls", hulls=1)
         print("wrote coupling_hulls")
+    if not which or "skinned_cloth" in which:  # skinned constraints driven by two animated joints
+        make_skinned()
+        print("wrote skinned_cloth")
     if not which or "coupling_sensors" in which:  # + a static box sensor and a rising kinematic sphere sensor
         make_coupling("coupling_sensors", sensors=1)
         print("wrote coupling_sensors")

@@ -301,6 +301,9 @@ class Oracle:
             L.oracle_set_contact_readback.argtypes = [ctypes.c_void_p, ctypes.c_int]
             L.oracle_get_contacts.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
             L.oracle_get_sensor_contacts.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_uint32)]
+            L.oracle_skin_vertices.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+            L.oracle_set_skin_settings.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_float]
+            L.oracle_get_skin_state.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
             L.oracle_last_error.restype = ctypes.c_char_p
             L.oracle_last_error.argtypes = [ctypes.c_void_p]
             cls._lib = L
@@ -360,6 +363,20 @@ class Oracle:
         out = np.zeros((self.nv[i], 8), np.float32)
         n = self.lib().oracle_get_contacts(self.h, i, out.ctypes.data)
         return out[:n]
+
+    def skin_vertices(self, i: int, joints, hard: bool = False):
+        """SkinVertices of body i; joints (J, 16) float32, Mat44 columns."""
+        j = np.ascontiguousarray(joints, np.float32)
+        assert self.lib().oracle_skin_vertices(self.h, i, j.ctypes.data, j.shape[0], 1 if hard else 0) == 0
+
+    def set_skin_settings(self, i: int, enable: bool, multiplier: float):
+        self.lib().oracle_set_skin_settings(self.h, i, 1 if enable else 0, multiplier)
+
+    def skin_state(self, i: int) -> np.ndarray:
+        """(N, 3, 3): per vertex previous skinned position, skinned position, normal."""
+        out = np.zeros((self.nv[i], 9), np.float32)
+        n = self.lib().oracle_get_skin_state(self.h, i, out.ctypes.data)
+        return out[:n].reshape(n, 3, 3)
 
     def sensor_contacts(self, i: int) -> int:
         """After a step with host-determined shapes: bit k = shape k is a sensor shape a vertex penetrated."""

@@ -103,6 +103,8 @@ inline bool make_named_scene(const std::string &name, const std::string &params,
                               int(geti("steps", 90)), float(geti("drop_mm", 1000)) * 0.001f);
     else if (name == "coupling")
         out = make_coupling(int(geti("steps", 90)), geti("hulls", 0) != 0, geti("sensors", 0) != 0);
+    else if (name == "skinned_cloth")
+        out = make_skinned_cloth(int(geti("steps", 90)));
     else if (name == "shapes_drop")
         out = make_shapes_drop(uint64_t(geti("seed", 7)), int(geti("steps", 150)));
     else

@@ -88,6 +88,16 @@ struct MeshSpec {
     std::vector<float> volume_compliance;  // per tetrahedron
     // Optional per-edge compliance written after Optimize, indexed in the optimized edge order.
     std::vector<float> post_optimize_edge_compliance;
+    // Skinned constraints (reference driver only): per constraint the vertex, up to 4 (inverse bind index,
+    // weight) pairs, max distance, back stop distance and radius; inverse bind matrices (joint, Mat44
+    // columns). Added before Optimize, with CalculateSkinnedConstraintNormals.
+    struct Skin {
+        uint32_t vertex;
+        std::array<std::pair<uint32_t, float>, 4> weights;
+        float max_distance, backstop_distance, backstop_radius;
+    };
+    std::vector<Skin> skinned;
+    std::vector<std::pair<uint32_t, std::array<float, 16>>> inv_binds;
 };
 
 struct CreationScalars {  // mirrors SoftBodyCreationSettings (SoftBodyCreationSettings.h:61-72)
@@ -431,6 +441,39 @@ inline SceneSpec make_large_cloth(uint32_t n = 256, int steps = 600, bool bends 
 // Differentiable single cloth: n x n (default 64), 0.05 m spacing, top row (z = n-1) pinned, edges
 // only (bends = true adds dihedral bends of compliance 1e-4), per-edge compliance log-U[1e-6, 1e-4] assigned in optimized edge order, initial
 // velocities N(0, 0.1) m/s per component; 120 steps.
+// A 16 x 16 cloth (0.1 m spacing) hanging from two joints (reference driver only: the reference's
+// SkinVertices is called before every step with the joints' matrices, which the driver records): the top
+// row kinematic on joint 0 (max distance 0), the other rows skinned to joints 0 and 1 blended by row, with
+// max distances growing down the cloth and a back stop sphere on every other row.
+inline SceneSpec make_skinned_cloth(int steps = 90) {
+    SceneSpec s;
+    BodySpec b;
+    const uint32_t n = 16;
+    b.mesh = make_cloth(n, n, 0.1f, [](uint32_t, uint32_t) { return false; });
+    b.mesh.attributes = VertexAttributes{1.0e-5f, 1.0e-5f, 1.0e-3f};
+    b.mesh.bend_type = BendType::Dihedral;
+    for (uint32_t z = 0; z < n; ++z)
+        for (uint32_t x = 0; x < n; ++x) {
+            MeshSpec::Skin k;
+            k.vertex = x + z * n;
+            const float t = float(z) / float(n - 1);
+            k.weights = {{{0u, 1.0f - t}, {1u, t}, {0u, 0.0f}, {0u, 0.0f}}};
+            if (z == 0) k.weights = {{{0u, 1.0f}, {0u, 0.0f}, {0u, 0.0f}, {0u, 0.0f}}};
+            k.max_distance = z == 0 ? 0.0f : 0.02f + 0.01f * float(z);
+            k.backstop_distance = (z & 1) ? 0.01f : k.max_distance;  // a back stop on odd rows only
+            k.backstop_radius = 0.3f;
+            b.mesh.skinned.push_back(k);
+        }
+    std::array<float, 16> ident{1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    std::array<float, 16> down = ident;
+    down[14] = -0.6f;  // joint 1 binds 0.6 m along the cloth (+z): its inverse bind matrix moves back by that
+    b.mesh.inv_binds = {{0u, ident}, {1u, down}};
+    b.position[1] = 1.5f;
+    s.bodies.push_back(b);
+    s.num_steps = steps;
+    return s;
+}
+
 // wave: amplitude (m) of a height field y = wave sin(2 pi x / 0.8 m) sin(2 pi z / 0.8 m) laid over the
 // grid, so that neighbouring triangles start folded by up to about 0.3 rad instead of flat.
 inline SceneSpec make_diff_cloth(uint64_t seed = 4, uint32_t n = 64, int steps = 120, bool bends = false, float wave = 0.0f) {

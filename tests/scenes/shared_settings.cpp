@@ -12,6 +12,7 @@
 //     tether attaches to.
 // Compile with -ffp-contract=off.
 
+#include <stdexcept>
 #include "shared_settings.h"
 
 #include <algorithm>
@@ -598,6 +599,7 @@ std::string SoftBodySharedSettings::SaveBinaryState() const {
 }
 
 SoftBodySharedSettings build_settings(const scene::MeshSpec &m) {
+    if (!m.skinned.empty()) throw std::runtime_error("skinned settings are built by the reference driver only");
     SoftBodySharedSettings s;
     s.mVertices.resize(m.positions.size());
     for (size_t i = 0; i < m.positions.size(); ++i) {
