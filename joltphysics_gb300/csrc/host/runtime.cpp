@@ -282,6 +282,8 @@ struct jsb_context {
     jsb::DevBuf<uint32_t> sensor_contact;  // per body: sensor shapes of its table with a vertex inside
     jsb::DevBuf<float4> skin_state;        // 3 per vertex (SkinState) when any body has skinned constraints
     jsb::DevBuf<jsb::SkinCtl> skin_ctl;    // per body
+    jsb::DevBuf<float4> face_scratch;      // pressure bodies: one float4 per face (cluster path)
+    std::vector<size_t> face_off;          // per body, into face_scratch
     jsb::DevBuf<jsb::HullDev> hulls_dev;
     jsb::DevBuf<float4> hull_f4_dev;
     jsb::DevBuf<uint32_t> hull_u32_dev;
@@ -404,6 +406,10 @@ BodyDesc make_desc(const jsb_context *ctx, const BodyRec &b) {
     const bool skinned = !s.parsed.skinned.empty() && ctx->skin_state.ptr;
     d.skin_params = skinned ? s.skin_params.ptr : nullptr;
     d.skin_state = skinned ? ctx->skin_state.ptr + size_t(b.vtx_offset) * 3 : nullptr;
+    const size_t bi = size_t(&b - ctx->bodies.data());
+    d.face_scratch = (b.creation.pressure > 0.0f && bi < ctx->face_off.size() && ctx->face_scratch.ptr)
+                         ? ctx->face_scratch.ptr + ctx->face_off[bi]
+                         : nullptr;
     return d;
 }
 
@@ -556,6 +562,15 @@ jsb_status rebuild(jsb_context *ctx) {
         if (oldc) JSB_CUDA(cudaMemcpy(hc.data(), ctx->skin_ctl.ptr, oldc * sizeof(SkinCtl), cudaMemcpyDeviceToHost));
         JSB_CUDA(ctx->skin_ctl.upload(hc.data(), hc.size()));
     }
+    {  // face scratch of the pressure bodies (used where a pressure body runs on the cluster path)
+        size_t nf = 0;
+        ctx->face_off.assign(ctx->bodies.size(), 0);
+        for (size_t bi = 0; bi < ctx->bodies.size(); ++bi) {
+            ctx->face_off[bi] = nf;
+            if (ctx->bodies[bi].creation.pressure > 0.0f) nf += ctx->settings[ctx->bodies[bi].settings_id]->parsed.faces.size();
+        }
+        if (nf && ctx->face_scratch.count < nf) JSB_CUDA(ctx->face_scratch.alloc(nf));
+    }
     jsb_status sst = ensure_step_schedules(ctx);
     if (sst != JSB_OK) return sst;
     ctx->descs_host.clear();
@@ -646,9 +661,6 @@ jsb_status rebuild_groups(jsb_context *ctx) {
         size_t k = bucket_for(ctx, nv);
         // Bodies whose positions do not fit one CTA's shared memory take the cluster path.
         if (ctx->buckets[k].state_mode == 2 || step_smem_bytes(false, nv, pressure_faces(s, b), 32) > cap) {
-            if (pressure_faces(s, b) > 0)
-                return fail(JSB_ERR_UNSUPPORTED, "a pressurised body with " + std::to_string(nv) +
-                                                     " vertices is too large for one CTA, and the cluster path has no pressure");
             if (!s.parsed.skinned.empty())
                 return fail(JSB_ERR_UNSUPPORTED, "a body with skinned constraints and " + std::to_string(nv) +
                                                      " vertices is too large for one CTA, and the cluster path has no skinning");

@@ -18,8 +18,8 @@
 // barrier is needed for the ring: a thread only waits for its own copies. The level descriptors are
 // copied into shared memory once per step.
 //
-// Pressure (ApplyPressure) needs a sequential sum over all faces and is not supported on this path;
-// the host rejects such bodies. The taped (differentiable) step does not run here either.
+// Pressure (ApplyPressure): the per-face terms are dealt over the cluster and summed in face order by
+// one thread, through a per-body face scratch in HBM. The taped (differentiable) step does not run here.
 
 #include <cuda_runtime.h>
 #include <float.h>
@@ -99,6 +99,7 @@ struct Partials {
 struct CShared {
     SCol cols[kMaxCollidingShapes];
     int ncols;
+    float six_volume;  // (rank 0) GetVolumeTimesSix of the substep
     int nan_flag[2];  // this CTA's vertices hold a NaN after the substep's integration (by substep parity)
     float delta[3];
     Partials part;
@@ -237,8 +238,48 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
     const f3 sub_imp = (force * dt_sub) / nvf;
     const float restitution_threshold = -2.0f * len(g) * dt_sub;
     const uint32_t G = C * T;
+    const uint32_t g0 = rank * T + tid;
 
+    const bool has_pressure = d.pressure > 0.0f && d.num_faces > 0 && d.face_scratch;
     for (uint32_t it = 0; it < n_it; ++it) {
+        // ApplyPressure (:291-323): per-face triple products dealt over the cluster into the body's face
+        // scratch, their sum in face order by one thread (the reference sums sequentially), then per face
+        // the impulse and per owned vertex its faces' impulses in face order.
+        if (has_pressure) {
+            float4 *fs = d.face_scratch;
+            // every CTA's positions final (the staging, or the last substep's collision pass on the owned
+            // vertices) before any face reads them
+            cluster_barrier();
+            for (uint32_t f = g0; f < d.num_faces; f += G) {
+                const uint4 fc = __ldg(d.faces + f);
+                fs[f] = make_float4(dot(cross(xyz(ldx(cx, fc.x)), xyz(ldx(cx, fc.y))), xyz(ldx(cx, fc.z))), 0.0f, 0.0f, 0.0f);
+            }
+            cluster_barrier();
+            if (rank == 0 && tid == 0) {
+                float six = 0.0f;
+                for (uint32_t f = 0; f < d.num_faces; ++f) six = six + fs[f].x;
+                sh.six_volume = six;
+            }
+            cluster_barrier();
+            const float six = ld_cluster_f32(map_rank(smem_u32(&sh.six_volume), 0));
+            if (six > 0.0f) {  // (the same value in every CTA)
+                const float coefficient = jdiv(d.pressure * dt_sub, six);
+                for (uint32_t f = g0; f < d.num_faces; f += G) {
+                    const uint4 fc = __ldg(d.faces + f);
+                    const f3 x1 = xyz(ldx(cx, fc.x)), x2 = xyz(ldx(cx, fc.y)), x3 = xyz(ldx(cx, fc.z));
+                    fs[f] = with_w(coefficient * cross(x2 - x1, x3 - x1), 0.0f);
+                }
+                cluster_barrier();
+                for (uint32_t i = first + tid; i < last; i += T) {
+                    const float w = sx[i - first].w;
+                    const float4 vel = gv[i];
+                    f3 v = xyz(vel);
+                    for (uint32_t k = __ldg(d.vf_off + i), ke = __ldg(d.vf_off + i + 1); k < ke; ++k) v = v + w * xyz(fs[__ldg(d.vf + k)]);
+                    gv[i] = with_w(v, vel.w);
+                }
+            }
+            cluster_barrier();  // every CTA has read the faces before they are written again
+        }
         // IntegratePositions (owned vertices)
         bool nan_seen = false;
         for (uint32_t i = first + tid; i < last; i += T) {

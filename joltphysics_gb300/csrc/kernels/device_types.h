@@ -85,6 +85,7 @@ struct BodyDesc {
     // (SoftBodyMotionProperties::SkinState)
     const float4 *skin_params;
     float4 *skin_state;
+    float4 *face_scratch;  // pressure on the cluster path: one float4 per face (null: none)
 };
 
 // Run-time skinning switches of one body (SoftBodyMotionProperties::mEnableSkinConstraints,

@@ -81,16 +81,21 @@ def test_mixed_launch_cluster_and_one_cta_bodies(jsb):
     assert_same(snapshot(ctx), [o.body(i) for i in range(len(scene.bodies))], "cluster and one-CTA bodies")
 
 
-def test_pressurised_body_rejected_on_cluster_path(jsb):
-    scene_bytes = build_scene("uneven_batch", n_cloth=0, n_cube=4, steps=2, seed=3)
+@pytest.mark.parametrize("cluster_size,threads", [(2, 128), (4, 256), (16, 256)])
+def test_pressurised_bodies_on_cluster_path_vs_oracle(jsb, cluster_size, threads):
+    """Pressurised tet cubes (with unpressurised ones) forced onto the cluster path: ApplyPressure's face
+    terms dealt over the cluster and summed in face order; bitwise equal to the oracle through the floor
+    contact."""
+    scene_bytes = build_scene("uneven_batch", n_cloth=0, n_cube=8, cube_max=7, steps=40, seed=3)
     scene, _ = parse_scene(scene_bytes)
+    assert any(float(b.creation[5]) > 0.0 for b in scene.bodies), "no pressurised cube drawn"
     ctx = make_ctx(jsb, scene_bytes)
-    force_cluster(ctx)
-    if all(float(b.creation[5]) == 0.0 for b in scene.bodies):
-        pytest.skip("no pressurised cube drawn")
-    with pytest.raises(jsb.JsbError) as e:
-        ctx.step()
-    assert e.value.status == jsb.JSB_ERR_UNSUPPORTED
+    force_cluster(ctx, cluster_size, threads)
+    o = Oracle(scene, threads=os.cpu_count() or 1)
+    for k in range(2):
+        o.step(20)
+        advance(ctx, 20)
+        assert_same(snapshot(ctx), [o.body(b) for b in range(len(scene.bodies))], f"step {20 * (k + 1)}")
 
 
 def test_cluster_config_validation(jsb):
