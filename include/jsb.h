@@ -187,7 +187,7 @@ jsb_status jsb_set_contact_readback(jsb_context *ctx, int enable);
  * and normal (3 floats each, zero without contact) and the colliding shape's index (the host-determined
  * table's order, or the order of the context colliders the body's bounds overlapped; -1 without contact),
  * and the recentring offset delta (local positions after the step = before - delta). Any output may be
- * NULL. Not recorded on the thread-block-cluster path (JSB_ERR_UNSUPPORTED). */
+ * NULL. */
 jsb_status jsb_body_contacts(jsb_context *ctx, uint32_t body_id, uint8_t *has_contact, float *contact_points, float *normals,
                              int32_t *shape_index, float delta[3]);
 /* ---- skinning (skinned constraints) --------------------------------------------------------- */

@@ -1370,9 +1370,6 @@ jsb_status jsb_body_contacts(jsb_context *ctx, uint32_t body_id, uint8_t *has_co
     if (!check_ctx(ctx) || body_id >= ctx->bodies.size()) return fail(JSB_ERR_INVALID_ARGUMENT, "bad argument");
     if (!ctx->contact_readback || ctx->contact.count < ctx->total_vertices || ctx->dirty)
         return fail(JSB_ERR_INVALID_ARGUMENT, "contact readback is off (jsb_set_contact_readback) or no step has run since");
-    for (const LaunchGroup &g : ctx->groups)
-        if (g.cluster > 0 && std::find(g.bodies.begin(), g.bodies.end(), body_id) != g.bodies.end())
-            return fail(JSB_ERR_UNSUPPORTED, "contact readback is not recorded on the thread-block-cluster path");
     JSB_CUDA(cudaSetDevice(ctx->device));
     JSB_CUDA(cudaDeviceSynchronize());
     const BodyRec &b = ctx->bodies[body_id];

@@ -228,6 +228,7 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
         if (pi.w > 0.0f && ncols > 0) shape = collision_plane(xyz(pi), sh.cols, ncols, plane);
         gshape[i] = shape;
         if (shape >= 0) gplane[i] = plane;
+        if (p.contact) p.contact[d.vtx_offset + i] = 0;
     }
 
     const float inv_dt_sq = 1.0f / (dt_sub * dt_sub);
@@ -318,8 +319,10 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
             const f3 prev_v = xyz(vel);
             f3 v = div3_rn(x - xyz(prev), dt_sub);
             const int shape = ncols > 0 ? gshape[i] : -1;
-            if (shape >= 0 && collide_vertex(x, v, prev_v, gplane[i], sh.cols[shape], d.vertex_radius, dt_sub, restitution_threshold))
+            if (shape >= 0 && collide_vertex(x, v, prev_v, gplane[i], sh.cols[shape], d.vertex_radius, dt_sub, restitution_threshold)) {
                 sx[i - first] = with_w(x, pi.w);
+                if (p.contact) p.contact[d.vtx_offset + i] = 1;
+            }
             gv[i] = with_w(v, vel.w);
         }
     }
@@ -434,6 +437,16 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
         delta = mk(ld_cluster_f32(base), ld_cluster_f32(base + 4), ld_cluster_f32(base + 8));
     }
     const bool recentre = (d.flags & kFlagUpdatePosition) != 0;
+    if (p.contact) {  // SoftBodyManifold: contact points before the recentring, and the offset
+        for (uint32_t i = first + tid; i < last; i += T)
+            if (p.contact[d.vtx_offset + i]) {
+                const f3 x = xyz(sx[i - first]);
+                const float4 pl = gplane[i];
+                const f3 n = xyz(pl);
+                p.contact_point[d.vtx_offset + i] = with_w(x - n * (dot(x, n) + pl.w), 0.0f);
+            }
+        if (rank == 0 && tid == 0) st3(p.contact_delta + 3 * size_t(b), recentre ? delta : mk(0.0f, 0.0f, 0.0f));
+    }
     for (uint32_t i = first + tid; i < last; i += T) {
         const float4 pi = sx[i - first];
         gx[i] = recentre ? with_w(xyz(pi) - delta, pi.w) : pi;

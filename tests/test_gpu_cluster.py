@@ -107,3 +107,24 @@ def test_cluster_config_validation(jsb):
     ctx.set_cluster_config(0, 512)
     assert ctx.cluster_config() == {"cluster_size": 0, "threads": 512, "bodies": 0}
     ctx.close()
+
+
+def test_contact_readback_cluster_equals_one_cta_path(jsb):
+    """SoftBodyManifold readback (jsb_body_contacts) on the cluster path equals the one-CTA path's (itself
+    checked against the reference's manifolds), bitwise: cloths and cubes (some pressurised) dropped onto a
+    capsule, two cylinders, a sphere and the floor."""
+    scene_bytes = build_scene("shapes_drop", steps=60)
+    a, b = make_ctx(jsb, scene_bytes), make_ctx(jsb, scene_bytes)
+    force_cluster(b, 2, 128)
+    for c in (a, b):
+        c.set_contact_readback(True)
+    touched = 0
+    for step in range(60):
+        advance(a, 1)
+        advance(b, 1)
+        for body in range(len(a.bodies)):
+            ca, cb = a.contacts(body), b.contacts(body)
+            for k in ("has_contact", "points", "normals", "shape", "delta"):
+                assert np.array_equal(ca[k], cb[k]), (step, body, k)
+            touched += int(ca["has_contact"].sum())
+    assert touched > 100, touched
