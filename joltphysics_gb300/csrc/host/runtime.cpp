@@ -661,9 +661,6 @@ jsb_status rebuild_groups(jsb_context *ctx) {
         size_t k = bucket_for(ctx, nv);
         // Bodies whose positions do not fit one CTA's shared memory take the cluster path.
         if (ctx->buckets[k].state_mode == 2 || step_smem_bytes(false, nv, pressure_faces(s, b), 32) > cap) {
-            if (!s.parsed.skinned.empty())
-                return fail(JSB_ERR_UNSUPPORTED, "a body with skinned constraints and " + std::to_string(nv) +
-                                                     " vertices is too large for one CTA, and the cluster path has no skinning");
             cluster_bodies.push_back(uint32_t(bi));
             continue;
         }

@@ -4,8 +4,8 @@ against the reference's own run (tests/golden/skinned_cloth.npz) and the CPU ora
 The 16 x 16 cloth skinned to two animated joints (see tests/test_oracle_skinned.py). Bar: body position,
 local positions and velocities bitwise equal to the reference at every dumped step and to the oracle at
 every step, and the skin block of jsb_body_save_state bitwise equal to the reference's SaveState bytes; on
-the whole-step walk (the default) and the per-substep walk. Bodies the skinned path does not take are
-refused.
+the whole-step walk (the default), the per-substep walk and the thread-block-cluster path (two cluster
+shapes). Differentiable runs do not take skinned bodies and are refused.
 """
 import numpy as np
 import pytest
@@ -17,8 +17,13 @@ from test_oracle_skinned import MOTION_HEADER, skin_events, skin_from_state
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("step_walk", [True, False])
-def test_skinned_cloth_bitwise_vs_reference_and_oracle(jsb, oracle_lib, step_walk):
+PATHS = {"whole_step": (True, None), "per_substep": (False, None), "cluster_2x128": (True, (2, 128)),
+         "cluster_4x256": (True, (4, 256))}
+
+
+@pytest.mark.parametrize("path", list(PATHS))
+def test_skinned_cloth_bitwise_vs_reference_and_oracle(jsb, oracle_lib, path):
+    step_walk, cluster = PATHS[path]
     g = np.load(golden_path("skinned_cloth"))
     scene_bytes = g["scene"].tobytes()
     scene, _ = parse_scene(scene_bytes)
@@ -26,6 +31,10 @@ def test_skinned_cloth_bitwise_vs_reference_and_oracle(jsb, oracle_lib, step_wal
     ctx = jsb.Context(0)
     ctx.load_scene(scene_bytes)
     ctx.set_step_walk(step_walk)
+    if cluster is not None:
+        for mv, t, _ in ctx.bucket_table():
+            ctx.set_bucket_config(mv, t, 2)
+        ctx.set_cluster_config(*cluster)
     o = oracle_lib(scene)
     ev = skin_events(g)
     dumps = set(int(s) for s in g["steps"])
@@ -53,14 +62,10 @@ def test_skinned_cloth_bitwise_vs_reference_and_oracle(jsb, oracle_lib, step_wal
 
 
 def test_skinned_refused_where_unsupported(jsb):
-    """Differentiable runs and the thread-block-cluster path do not take skinned bodies."""
+    """Differentiable runs do not take skinned bodies."""
     g = np.load(golden_path("skinned_cloth"))
     ctx = jsb.Context(0)
     ctx.load_scene(g["scene"].tobytes())
     with pytest.raises(jsb.JsbError):
         ctx.adjoint_begin(2, 1)
-    for mv, t, _ in ctx.bucket_table():
-        ctx.set_bucket_config(mv, t, 2)
-    with pytest.raises(jsb.JsbError):
-        ctx.step()
     ctx.close()
