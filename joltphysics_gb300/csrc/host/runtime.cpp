@@ -876,13 +876,6 @@ jsb_status step_impl(jsb_context *ctx, float dt, int collision_steps, cudaStream
     if (!(dt > 0.0f) || collision_steps < 1) return fail(JSB_ERR_INVALID_ARGUMENT, "dt must be > 0 and collision_steps >= 1");
     jsb_status st = rebuild(ctx);
     if (st != JSB_OK) return st;
-    if (!ctx->table_host.empty()) {
-        for (const LaunchGroup &g : ctx->groups)
-            if (g.cluster > 0)
-                for (uint32_t b : g.bodies)
-                    if (ctx->table_host.count(b))
-                        return fail(JSB_ERR_UNSUPPORTED, "host-determined colliding shapes on a body of the thread-block-cluster path");
-    }
     if ((st = upload_tables(ctx, stream)) != JSB_OK) return st;
     if ((st = ensure_contact_buffers(ctx)) != JSB_OK) return st;
     const float step_dt = dt / float(collision_steps);

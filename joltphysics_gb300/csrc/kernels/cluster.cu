@@ -99,6 +99,13 @@ struct Partials {
 struct CShared {
     SCol cols[kMaxCollidingShapes];
     int ncols;
+    int32_t table_slot;  // host-determined colliding shapes (-1: the context's colliders)
+    int dynamic;         // some shape is a dynamic body
+    uint32_t sensors;    // bit k: shape k is a sensor
+    uint32_t sensor_hit;  // sensors touched by this CTA's vertices
+    uint32_t ndyn;        // this CTA's owned vertices on dynamic shapes
+    uint32_t dyn_updated;  // (rank 0) bit k: dynamic shape k took an impulse
+    float dvel[kMaxCollidingShapes][6];  // (rank 0) the dynamic shapes' linear | angular velocities
     float six_volume;  // (rank 0) GetVolumeTimesSix of the substep
     int nan_flag[2];  // this CTA's vertices hold a NaN after the substep's integration (by substep parity)
     float delta[3];
@@ -211,24 +218,65 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
     const f3 body_pos = ld3(st->position);
     const f3 force = ld3(p.forces + 3 * size_t(b)) + ld3(p.step_forces + 3 * size_t(b));
 
-    // DetermineCollidingShapes (every CTA evaluates it; the result is the same), level descriptors and
-    // the positions this CTA owns.
-    if (tid == 0) sh.ncols = colliding_shapes(p, d, st, body_pos, sh.cols);
+    // DetermineCollidingShapes, or the shapes the host determined for the body (every CTA evaluates it;
+    // the result is the same), level descriptors and the positions this CTA owns.
+    if (tid == 0) {
+        const int32_t slot = p.table_slot ? p.table_slot[b] : -1;
+        bool dynamic = false;
+        const int n = slot >= 0 ? load_shape_table(p.tables + slot, sh.cols, dynamic) : colliding_shapes(p, d, st, body_pos, sh.cols);
+        sh.ncols = n;
+        sh.table_slot = slot;
+        sh.dynamic = dynamic ? 1 : 0;
+        sh.dyn_updated = 0;
+        uint32_t sensors = 0;
+        if (slot >= 0)
+            for (int k = 0; k < n; ++k)
+                if (sh.cols[k].flags & kColSensor) sensors |= 1u << k;
+        sh.sensors = sensors;
+        sh.sensor_hit = 0;
+        if (dynamic)
+            for (int k = 0; k < n; ++k)
+                for (int j = 0; j < 3; ++j) {
+                    sh.dvel[k][j] = p.tables[slot].e[k].lin[j];
+                    sh.dvel[k][3 + j] = p.tables[slot].e[k].ang[j];
+                }
+    }
     const uint32_t nd = min(d.num_levels + 2, desc_cap);
     for (uint32_t l = tid; l < nd; l += T) sdesc[l] = __ldg(d.levels + l);
     for (uint32_t i = first + tid; i < last; i += T) sx[i - first] = gx[i];
     __syncthreads();
 
-    // DetermineCollisionPlanes (owned vertices)
+    // DetermineCollisionPlanes and DetermineSensorCollisions (owned vertices)
     const int ncols = sh.ncols;
+    const bool has_dynamic = sh.dynamic != 0;  // (uniform over the cluster)
+    const uint32_t sensors = sh.sensors;
+    const HullRefs hr{p.hulls, p.hull_f4, p.hull_u32};
+    uint32_t hits = 0;
     for (uint32_t i = first + tid; i < last; i += T) {
         const float4 pi = sx[i - first];
         int shape = -1;
         float4 plane = make_float4(0, 0, 0, 0);
-        if (pi.w > 0.0f && ncols > 0) shape = collision_plane(xyz(pi), sh.cols, ncols, plane);
+        if (pi.w > 0.0f && ncols > 0) shape = collision_plane(xyz(pi), sh.cols, ncols, plane, hr);
+        if (sensors && pi.w > 0.0f) hits |= sensor_hits(xyz(pi), sh.cols, ncols, sensors, hr);
         gshape[i] = shape;
         if (shape >= 0) gplane[i] = plane;
         if (p.contact) p.contact[d.vtx_offset + i] = 0;
+    }
+    if (hits) atomicOr(&sh.sensor_hit, hits);
+    if (has_dynamic) {
+        // The dynamic-body branch carries the body's velocities from one vertex to the next in index
+        // order: each CTA lists its owned vertices on dynamic shapes (the shapes are fixed for the step);
+        // rank 0 walks the lists in rank order, which is index order.
+        __syncthreads();
+        if (tid == 0) {
+            int32_t *list = p.dyn_list + d.vtx_offset + first;
+            uint32_t n = 0;
+            for (uint32_t i = first; i < last; ++i) {
+                const int s = gshape[i];
+                if (s >= 0 && (sh.cols[s].flags & kColDynamic)) list[n++] = int32_t(i);
+            }
+            sh.ndyn = n;
+        }
     }
 
     const float inv_dt_sq = 1.0f / (dt_sub * dt_sub);
@@ -327,11 +375,45 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
             const f3 prev_v = xyz(vel);
             f3 v = div3_rn(x - xyz(prev), dt_sub);
             const int shape = ncols > 0 ? gshape[i] : -1;
+            if (has_dynamic && shape >= 0 && (sh.cols[shape].flags & kColDynamic)) continue;  // below, in vertex order
             if (shape >= 0 && collide_vertex(x, v, prev_v, gplane[i], sh.cols[shape], d.vertex_radius, dt_sub, restitution_threshold)) {
                 sx[i - first] = with_w(x, pi.w);
                 if (p.contact) p.contact[d.vtx_offset + i] = 1;
             }
             gv[i] = with_w(v, vel.w);
+        }
+        if (has_dynamic) {
+            // The vertices on dynamic shapes, one thread of rank 0, in index order over the cluster (the
+            // lists were complete at the integration's cluster barrier); the barrier after it makes the
+            // remote position writes visible before the owners' next pass.
+            if (rank == 0 && tid == 0) {
+                const ShapeTable &tb = p.tables[sh.table_slot];
+                for (uint32_t q = 0; q < C; ++q) {
+                    const uint32_t nq = uint32_t(ld_cluster_s32(map_rank(smem_u32(&sh.ndyn), q)));
+                    const int32_t *list = p.dyn_list + d.vtx_offset + min(nv, q << shift);
+                    for (uint32_t k = 0; k < nq; ++k) {
+                        const uint32_t i = uint32_t(list[k]);
+                        const float4 pi = ldx(cx, i);
+                        const float4 vel = gv[i];
+                        const float4 prev = gprev[i];
+                        const int s = gshape[i];
+                        f3 x = xyz(pi), v = div3_rn(x - xyz(prev), dt_sub);
+                        f3 lin = mk(sh.dvel[s][0], sh.dvel[s][1], sh.dvel[s][2]), ang = mk(sh.dvel[s][3], sh.dvel[s][4], sh.dvel[s][5]);
+                        bool touched;
+                        const bool impulse = collide_vertex_dynamic(x, v, xyz(vel), pi.w, gplane[i], tb.e[s], lin, ang, d.vertex_radius,
+                                                                    dt_sub, restitution_threshold, touched);
+                        if (touched && p.contact) p.contact[d.vtx_offset + i] = 1;
+                        if (impulse) {
+                            sh.dvel[s][0] = lin.x, sh.dvel[s][1] = lin.y, sh.dvel[s][2] = lin.z;
+                            sh.dvel[s][3] = ang.x, sh.dvel[s][4] = ang.y, sh.dvel[s][5] = ang.z;
+                            sh.dyn_updated |= 1u << s;
+                        }
+                        stx(cx, i, with_w(x, pi.w));
+                        gv[i] = with_w(v, vel.w);
+                    }
+                }
+            }
+            cluster_barrier();
         }
     }
 
@@ -437,6 +519,20 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
                                            nvf);
         st3(sh.delta, delta);
         sleep_test(p, b, d, st, acc.max_v_sq);
+        if (has_dynamic) {  // UpdateRigidBodyVelocities' inputs (:923-935) for the host
+            ShapeTable &tb = p.tables[sh.table_slot];
+            for (int k = 0; k < ncols; ++k)
+                for (int j = 0; j < 3; ++j) {
+                    tb.lin[k][j] = sh.dvel[k][j];
+                    tb.ang[k][j] = sh.dvel[k][3 + j];
+                }
+            tb.updated = sh.dyn_updated;
+        }
+        if (p.sensor_contact) {  // the sensors touched by any CTA (the atomics precede the barriers since)
+            uint32_t touched = sh.sensor_hit;
+            for (uint32_t r = 1; r < C; ++r) touched |= uint32_t(ld_cluster_s32(map_rank(smem_u32(&sh.sensor_hit), r)));
+            p.sensor_contact[b] = touched;
+        }
     }
     cluster_barrier();
     f3 delta;

@@ -9,6 +9,7 @@ changes read back through jsb_body_shape_velocities give the reference's velocit
 bitwise, and the SoftBodyManifold read back through jsb_body_contacts (contact flags, points, normals,
 contacted body) is the reference's, bitwise (as in tests/test_oracle_coupling.py); coupling_sensors adds
 two sensors, whose contacts read back through jsb_body_sensor_contacts are the manifold's sensor contacts.
+The same bar holds with every body forced onto the thread-block-cluster path (mode "cluster").
 """
 import numpy as np
 import pytest
@@ -22,7 +23,8 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("name,mode", [("coupling", "batched"), ("coupling", "plain"), ("coupling_hulls", "batched"),
-                                       ("coupling_sensors", "batched")])
+                                       ("coupling_sensors", "batched"), ("coupling", "cluster"), ("coupling_hulls", "cluster"),
+                                       ("coupling_sensors", "cluster")])
 def test_coupling_bitwise_vs_reference_and_oracle(jsb, oracle_lib, name, mode):
     g = np.load(golden_path(name))
     scene_bytes = g["scene"].tobytes()
@@ -37,6 +39,10 @@ def test_coupling_bitwise_vs_reference_and_oracle(jsb, oracle_lib, name, mode):
     manifolds = manifolds_by_key(g)
     sensors = sensors_by_key(g)
     ctx.set_contact_readback(True)
+    if mode == "cluster":  # every body on the thread-block-cluster path
+        for mv, t, _ in ctx.bucket_table():
+            ctx.set_bucket_config(mv, t, 2)
+        ctx.set_cluster_config(2, 128)
     contacts = sensor_shapes = 0
     dumps = set(int(s) for s in g["steps"])
     changes = 0
@@ -56,7 +62,7 @@ def test_coupling_bitwise_vs_reference_and_oracle(jsb, oracle_lib, name, mode):
         for b in range(len(nv)):
             assert np.array_equal(out[b], o.shape_velocities(b)), (step, b)
         changes += check_velocity_changes(rows, out, g["rigid_after"][step - 1])
-        if mode == "batched":
+        if mode != "plain":
             for b in range(len(nv)):
                 c = ctx.contacts(b)
                 contacts += check_manifold(manifolds.get((step, b)), b, rows, c["has_contact"], c["points"], c["normals"], c["shape"])
@@ -76,7 +82,7 @@ def test_coupling_bitwise_vs_reference_and_oracle(jsb, oracle_lib, name, mode):
             off += nv[b]
     ctx.close()
     assert changes > 50, changes
-    assert mode != "batched" or contacts > 1000, contacts
+    assert mode == "plain" or contacts > 1000, contacts
     assert name != "coupling_sensors" or (len(sensors) > 100 and sensor_shapes > len(sensors)), (len(sensors), sensor_shapes)
 
 
