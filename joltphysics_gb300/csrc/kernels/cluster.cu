@@ -124,9 +124,9 @@ struct CShared {
 // the load is in flight during the projection and the barrier; a thread's further slots of a level
 // wider than the cluster are read where they are projected. No staging ring and no async-copy wait sit
 // in the level's critical path.
-template <int T, bool kGuard>
+template <int T, bool kGuard, bool kSkin>
 __device__ __forceinline__ void cluster_levels(ClusterX cx, const BodyDesc &d, const uint4 *sdesc, uint32_t desc_cap, uint32_t rank,
-                                               uint32_t G, float inv_dt_sq, const SkinRefs *sk) {
+                                               uint32_t G, float inv_dt_sq, SkinRefs sk) {
     const uint32_t L = d.num_levels;
     if (L == 0) return;
     const uint4 *__restrict__ rec = d.records;
@@ -163,10 +163,10 @@ __device__ __forceinline__ void cluster_levels(ClusterX cx, const BodyDesc &d, c
         uint32_t stride;
         uint32_t s = first_slot(n, stride);
         if (s < n) {
-            if (r0.x != 0xffffffffu) project<kGuard>(cx, r0, slot_type(lv, s), inv_dt_sq, sk, false);
+            if (r0.x != 0xffffffffu) project<kGuard>(cx, r0, slot_type(lv, s), inv_dt_sq, kSkin ? &sk : nullptr, false);
             for (s += stride; s < n; s += stride) {
                 const uint4 r = __ldg(rec + lv.x + s);
-                if (r.x != 0xffffffffu) project<kGuard>(cx, r, slot_type(lv, s), inv_dt_sq, sk, false);
+                if (r.x != 0xffffffffu) project<kGuard>(cx, r, slot_type(lv, s), inv_dt_sq, kSkin ? &sk : nullptr, false);
             }
         }
         const bool narrow_pair = n <= uint32_t(T) && l + 1 < L && end1 - end <= uint32_t(T);
@@ -290,15 +290,9 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
     const uint32_t g0 = rank * T + tid;
 
     const bool has_pressure = d.pressure > 0.0f && d.num_faces > 0 && d.face_scratch;
-    SkinRefs skin_refs{};
-    const SkinRefs *skin = nullptr;
-    if (d.skin_params && p.skin_ctl) {
-        const SkinCtl ctl = p.skin_ctl[b];
-        skin_refs = SkinRefs{d.skin_params, d.skin_state, ctl.max_distance_multiplier, ctl.flags, n_it, 0};
-        skin = &skin_refs;
-    }
+    const bool skinned = d.skin_params && p.skin_ctl;
+    const SkinCtl skin_ctl = skinned ? p.skin_ctl[b] : SkinCtl{};
     for (uint32_t it = 0; it < n_it; ++it) {
-        skin_refs.substep = it;
         // ApplyPressure (:291-323): per-face triple products dealt over the cluster into the body's face
         // scratch, their sum in face order by one thread (the reference sums sequentially), then per face
         // the impulse and per owned vertex its faces' impulses in face order.
@@ -360,10 +354,15 @@ __global__ void __launch_bounds__(T) cluster_step_kernel(StepParams p, uint32_t 
         // NaN-guarded projections when any CTA's vertices hold a NaN (flags double-buffered by substep)
         bool guard = false;
         for (uint32_t q = 0; q < C; ++q) guard = guard || ld_cluster_s32(map_rank(smem_u32(&sh.nan_flag[it & 1]), q)) != 0;
-        if (guard)
-            cluster_levels<T, true>(cx, d, sdesc, desc_cap, rank, G, inv_dt_sq, skin);
+        // (skinned bodies get their own instantiation: the skin projection's registers stay out of the
+        // common walk)
+        if (skinned)
+            cluster_levels<T, true, true>(cx, d, sdesc, desc_cap, rank, G, inv_dt_sq,
+                                          SkinRefs{d.skin_params, d.skin_state, skin_ctl.max_distance_multiplier, skin_ctl.flags, n_it, it});
+        else if (guard)
+            cluster_levels<T, true, false>(cx, d, sdesc, desc_cap, rank, G, inv_dt_sq, SkinRefs{});
         else
-            cluster_levels<T, false>(cx, d, sdesc, desc_cap, rank, G, inv_dt_sq, skin);
+            cluster_levels<T, false, false>(cx, d, sdesc, desc_cap, rank, G, inv_dt_sq, SkinRefs{});
         // ApplyCollisionConstraintsAndUpdateVelocities (owned vertices; the last level's barrier made
         // every remote write visible). The next integration touches owned vertices only.
         for (uint32_t i = first + tid; i < last; i += T) {
