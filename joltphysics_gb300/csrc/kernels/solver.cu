@@ -33,6 +33,7 @@ namespace {
 
 struct Shared {
     SCol cols[kMaxCollidingShapes];
+    SkinRefs skin;  // skinned bodies: written by thread 0 before each walk (no per-thread copy)
     int ncols;
     uint32_t item;
     float six_volume;
@@ -492,15 +493,12 @@ __device__ bool step_body(const StepParams &p, uint32_t b, float4 *smem, uint32_
     }
     const uint32_t passes = step_walk ? 1u : n_it;
 
-    SkinRefs skin_refs{};
-    const SkinRefs *skin = nullptr;
-    if (d.skin_params && p.skin_ctl) {
-        const SkinCtl ctl = p.skin_ctl[b];
-        skin_refs = SkinRefs{d.skin_params, d.skin_state, ctl.max_distance_multiplier, ctl.flags, n_it, 0};
-        skin = &skin_refs;
-    }
+    const SkinRefs *skin = d.skin_params && p.skin_ctl ? &sh.skin : nullptr;
     for (uint32_t it = 0; it < passes; ++it) {
-        skin_refs.substep = it;
+        if (skin && tid == 0) {  // (read after the integration's barrier; the last walk ended at one)
+            const SkinCtl ctl = p.skin_ctl[b];
+            sh.skin = SkinRefs{d.skin_params, d.skin_state, ctl.max_distance_multiplier, ctl.flags, n_it, it};
+        }
         float4 *tape_state = nullptr;
         if (kTape) {
             tape_state = td.state + (size_t(p.tape_step) * n_it + it) * 3 * nv;
