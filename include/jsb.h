@@ -166,8 +166,8 @@ jsb_status jsb_hull_add(jsb_context *ctx, const jsb_convex_hull *hull, uint32_t 
  * the order the reference collects them; they apply to every following step (each of its collision
  * steps) until set again or cleared. Vertices on a dynamic shape take the dynamic-body branch of
  * ApplyCollisionConstraintsAndUpdateVelocities (:752-797) in vertex order, such bodies walk their schedule
- * substep by substep, and the shape's velocities change with each impulse. Not for bodies on the
- * thread-block-cluster path, graphs (jsb_step_graph) or differentiable runs (JSB_ERR_UNSUPPORTED). */
+ * substep by substep, and the shape's velocities change with each impulse. Taken on the one-CTA and the
+ * thread-block-cluster paths; not for graphs (jsb_step_graph) or differentiable runs (JSB_ERR_UNSUPPORTED). */
 jsb_status jsb_body_set_colliding_shapes(jsb_context *ctx, uint32_t body_id, const jsb_colliding_shape *shapes, uint32_t count);
 jsb_status jsb_body_clear_colliding_shapes(jsb_context *ctx, uint32_t body_id);
 /* After a step (synchronises the device): per host-determined shape of the body, 7 floats {updated (1 when a
@@ -198,7 +198,8 @@ jsb_status jsb_body_contacts(jsb_context *ctx, uint32_t body_id, uint8_t *has_co
  * step's iterations; hard_skin_all moves every skinned vertex to its skinned position and zeroes its
  * velocity. Call it between steps; the next step's ApplySkinConstraints (:509-571: back stop sphere and
  * maximum distance) use it. Synchronous (host arithmetic in the reference's operation order). Skinned bodies
- * run on the one-CTA path only (not the cluster path, not differentiable runs, not jsb_step_body_noalloc). */
+ * run on the one-CTA and the thread-block-cluster paths (not in differentiable runs, not through
+ * jsb_step_body_noalloc). */
 jsb_status jsb_body_skin_vertices(jsb_context *ctx, uint32_t body_id, const float *joint_matrices, uint32_t num_joints,
                                   int hard_skin_all);
 /* SetEnableSkinConstraints / SetSkinnedMaxDistanceMultiplier (SoftBodyMotionProperties.h:93-98). */
